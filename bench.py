@@ -1,0 +1,331 @@
+"""Benchmark of the GB300 draw path.
+
+Default workload (one JSON line): the instanced scene at 1920x1080 - the
+64x32 UV sphere drawn as 1024 instances with per-instance model matrices,
+Blinn-Phong with 4 point lights and a 1024^2 RGBA8 noise texture, RGBA8
+colour + float32 depth. One step = one frame: clear + draw_instanced.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2|c1|c3|c4]
+  python bench.py --impl reference ...   # the CPU restatement of the reference path
+
+Metric: frames/s (whole job, all ranks). value = device-timed frames with
+inputs resident in HBM; L2 is flushed (a 256 MiB write) between timed frames.
+e2e = the same frames through the C ABI from pinned host buffers: per frame
+the uniform block and instance matrices are uploaded, the frame is drawn and
+the colour attachment is read back to pinned host memory.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "frames/s at 1080p, batched vs per-draw GPU (exact coverage); adjoint ms/frame"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload_config(name):
+    from softlight_gb300 import scenes as S
+    if name == "c1":
+        return S.build_c1, {}, {"workload": "single UV sphere 64x32 (4096 tris), Lambert, 256^2 checker", "resolution": "640x480"}
+    if name == "c2":
+        return S.build_c2, {}, {"workload": "instanced UV sphere 64x32 x 1024 instances (4.19M tris), Blinn-Phong 4 point lights, 1024^2 RGBA8 noise texture",
+                                 "resolution": "1920x1080", "instances": 1024}
+    if name == "c3":
+        return S.build_c3, {}, {"workload": "2M-triangle soup, 30% back-facing, 10% near-plane clipped, alpha blend, 2048^2 texture",
+                                 "resolution": "1920x1080"}
+    return S.build_c4, {}, {"workload": "256 uneven meshes (12..65k tris), per-draw 512^2 textures, Lambert+ambient, one batched launch",
+                             "resolution": "3840x2160", "draws": 256}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(workload, kernel):
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        d = json.load(fh)
+    return d.get(workload, {}).get(kernel)
+
+
+def cpu_port_time(builder, kwargs, sample_frac_instances, threads, seconds):
+    """Times the CPU restatement (oracle port) on a bounded sample of the
+    workload; returns (frames/s scaled to the full workload, description)."""
+    import oracle
+    ctx = oracle.Context(num_threads=threads)
+    scene = builder(ctx, **kwargs)
+    full_draws = list(scene.draws)
+    scale = 1.0
+    if sample_frac_instances is not None:
+        m, n, s = full_draws[0]
+        k = max(1, int(n * sample_frac_instances))
+        scene.draws = [(m, k, s)]
+        scale = n / k
+    scene.render()
+    times = []
+    t_end = time.perf_counter() + seconds
+    while time.perf_counter() < t_end or len(times) < 2:
+        t0 = time.perf_counter()
+        scene.render()
+        times.append(time.perf_counter() - t0)
+        if len(times) >= 50:
+            break
+    t = statistics.median(times) * scale
+    ctx.close()
+    return 1.0 / t, len(times), scale
+
+
+def run_reference(args):
+    """--impl reference: the reference path's CPU restatement on all host cores."""
+    rank, world, _ = dist_env()
+    if world > 1 and rank != 0:
+        return
+    builder, kwargs, cfg = workload_config(args.workload)
+    import oracle
+    threads = os.cpu_count() or 1
+    ctx = oracle.Context(num_threads=threads)
+    scene = builder(ctx, **kwargs)
+    scale = 1.0
+    if args.workload == "c2":
+        m, n, s = scene.draws[0]
+        k = 128
+        scene.draws = [(m, k, s)]
+        scale = n / k
+    for _ in range(args.warmup):
+        scene.render()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        scene.render()
+    dt = (time.perf_counter() - t0) * scale
+    fps = args.steps / dt
+    sample = (f"each step renders {scene.draws[0][1]} of {int(scene.draws[0][1] * scale)} instances; time scaled to the full frame"
+              if scale != 1.0 else "full frames")
+    line = {"impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / fps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
+                             "sample": sample + "; reference sources cannot be shipped to this host, so the oracle port "
+                                                "(CPU restatement of the reference's portable path) is timed"},
+            "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    import softlight_gb300 as sg
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    sg.build()
+    builder, kwargs, cfg = workload_config(args.workload)
+    ctx = sg.Context()
+    scene = builder(ctx, **kwargs)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    for _ in range(max(3, args.warmup)):
+        scene.render()
+    ctx.finish()
+
+    ctx.profile_stages(True)
+    step_ms, stage_ms = [], []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(i & 0xFF)
+                ev0 = torch.cuda.Event(enable_timing=True)
+                ev1 = torch.cuda.Event(enable_timing=True)
+                ev0.record(stream)
+            scene.render()
+            with torch.cuda.stream(stream):
+                ev1.record(stream)
+            ev1.synchronize()
+            step_ms.append(ev0.elapsed_time(ev1))
+            stage_ms.append(ctx.stage_times())
+    ctx.finish()
+    torch.cuda.synchronize()
+    ctx.profile_stages(False)
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    fps = world * args.steps / (total_ms / 1000.0)
+
+    # end to end through the C ABI with pinned host buffers
+    ubo_id, ubo_bytes = scene.frame_ubos[0]
+    ubo_host = torch.empty(len(ubo_bytes), dtype=torch.uint8, pin_memory=True).numpy()
+    ubo_host[:] = np.frombuffer(ubo_bytes, dtype=np.uint8)
+    h2d = len(ubo_bytes)
+    inst = getattr(scene, "instance_matrices", None)
+    if inst is not None:
+        inst_host = torch.empty(inst[1].nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+        inst_host[:] = inst[1].view(np.uint8).reshape(-1)
+        h2d += inst_host.nbytes
+    color_host = torch.empty(scene.height * scene.width * 4, dtype=torch.uint8, pin_memory=True).numpy()
+    for _ in range(2):
+        scene.render()
+        ctx.texture_read(scene.color_tex, (scene.height, scene.width, 4), np.uint8, out=color_host.reshape(scene.height, scene.width, 4))
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.ubo_assign(ubo_id, ubo_host)
+        if inst is not None:
+            ctx.vbo_assign(inst[0], inst_host)
+        scene.render()
+        ctx.texture_read(scene.color_tex, (scene.height, scene.width, 4), np.uint8, out=color_host.reshape(scene.height, scene.width, 4))
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_fps = world * args.steps / e2e_s
+
+    # roofline of the dominant kernel
+    stages = np.asarray(stage_ms)
+    mean_stage = stages.mean(0)
+    names = ["vs_setup", "tile_scan", "bin_fill", "raster"]
+    dom = int(np.argmax(mean_stage))
+    geo = scene.geometry_bytes
+    algo = {"vs_setup": geo, "tile_scan": 0, "bin_fill": 0, "raster": scene.texture_bytes + scene.framebuffer_bytes()}
+    frame_bytes = geo + scene.texture_bytes + scene.framebuffer_bytes()
+    peak, peak_kind = measured_peaks()
+    achieved = algo[names[dom]] / (mean_stage[dom] / 1000.0) / 1e9
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": profiled_traffic(args.workload, names[dom]),
+                "algorithmic_bytes": algo[names[dom]], "kernel_ms": float(mean_stage[dom]),
+                "stage_ms": {n: float(v) for n, v in zip(names, mean_stage)},
+                "frame_algorithmic_bytes": frame_bytes,
+                "frame_frac": frame_bytes / (total_ms / args.steps / 1000.0) / 1e9 / peak}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        frac = (64 / 1024) if args.workload == "c2" else None
+        v, frames, sc = cpu_port_time(builder, kwargs, frac, threads, args.cpu_sample_seconds)
+        cpu = {"value": v, "unit": "frames/s", "cores": threads, "kind": "port",
+               "sample": (f"{frames} frames of 64 of 1024 instances, time scaled x{sc:g}" if frac else f"{frames} full frames")}
+
+    if rank == 0:
+        cfg = dict(cfg)
+        cfg.update({"l2": "flushed between timed frames (256 MiB write)", "tile": "32x32",
+                    "triangles_per_frame": scene.num_triangles})
+        line = {"metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": cfg,
+                "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": scene.height * scene.width * 4},
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks.summary(),
+                "gpu_launches": args.steps * 6}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

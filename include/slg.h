@@ -1,0 +1,250 @@
+/*
+ * slg.h - C ABI of the GB300 draw path (SoftLight-compatible).
+ *
+ * Every entry point mirrors a member of SoftLight's SL_Context or of one of
+ * the resource objects it owns; the reference interface each one replaces is
+ * cited beside it (paths relative to the SoftLight source tree). Resource ids
+ * are size_t handles exactly as in SL_Context; set-up calls return
+ * SLG_INVALID_ID or a negative status on error, draws return a status where
+ * SL_Context::draw returns void (the facade in slg_context.hpp keeps the
+ * void signature). The text of the last error is available through
+ * slg_last_error().
+ *
+ * Only plain C types cross this boundary: no CUDA, torch or C++ types.
+ */
+#ifndef SLG_H
+#define SLG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SLG_INVALID_ID ((size_t)-1)
+
+/* status codes */
+enum slg_status
+{
+    SLG_OK              = 0,
+    SLG_ERR_INVALID_ID  = -1, /* unknown resource id */
+    SLG_ERR_INVALID_ARG = -2, /* bad size, type or state */
+    SLG_ERR_CUDA        = -3, /* a CUDA runtime call failed */
+    SLG_ERR_OVERFLOW    = -4, /* an internal buffer was too small (retried internally) */
+    SLG_ERR_TIMEOUT     = -5, /* a bounded device-side wait ran out */
+    SLG_ERR_NO_MEMORY   = -6
+};
+
+/* SL_DataType (softlight/include/softlight/SL_Geometry.hpp:30) */
+enum slg_data_type
+{
+    SLG_VERTEX_DATA_BYTE = 0,
+    SLG_VERTEX_DATA_SHORT,
+    SLG_VERTEX_DATA_INT,
+    SLG_VERTEX_DATA_LONG,
+    SLG_VERTEX_DATA_FLOAT,
+    SLG_VERTEX_DATA_DOUBLE,
+    SLG_VERTEX_DATA_INVALID
+};
+
+/* SL_RenderMode (softlight/include/softlight/SL_Mesh.hpp:16) */
+enum slg_render_mode
+{
+    SLG_RENDER_MODE_POINTS            = 0x01,
+    SLG_RENDER_MODE_INDEXED_POINTS    = 0x03,
+    SLG_RENDER_MODE_LINES             = 0x04,
+    SLG_RENDER_MODE_INDEXED_LINES     = 0x0C,
+    SLG_RENDER_MODE_TRIANGLES         = 0x10,
+    SLG_RENDER_MODE_INDEXED_TRIANGLES = 0x30,
+    SLG_RENDER_MODE_TRI_WIRE          = 0x50,
+    SLG_RENDER_MODE_INDEXED_TRI_WIRE  = 0x70
+};
+
+/* SL_CullMode, SL_DepthTest, SL_DepthMask, SL_BlendMode
+ * (softlight/include/softlight/SL_PipelineState.hpp:15-66) */
+enum slg_cull_mode  { SLG_CULL_BACK_FACE = 0, SLG_CULL_FRONT_FACE, SLG_CULL_OFF };
+enum slg_depth_test
+{
+    SLG_DEPTH_TEST_OFF = 0,
+    SLG_DEPTH_TEST_LESS_THAN,
+    SLG_DEPTH_TEST_LESS_EQUAL,
+    SLG_DEPTH_TEST_GREATER_THAN,
+    SLG_DEPTH_TEST_GREATER_EQUAL,
+    SLG_DEPTH_TEST_EQUAL,
+    SLG_DEPTH_TEST_NOT_EQUAL
+};
+enum slg_depth_mask { SLG_DEPTH_MASK_OFF = 0, SLG_DEPTH_MASK_ON };
+enum slg_blend_mode
+{
+    SLG_BLEND_OFF = 0,
+    SLG_BLEND_ALPHA,
+    SLG_BLEND_PREMULTIPLED_ALPHA,
+    SLG_BLEND_ADDITIVE,
+    SLG_BLEND_SCREEN
+};
+
+/* SL_ColorDataType subset used by framebuffers and textures
+ * (softlight/include/softlight/SL_Color.hpp:31). Values are the reference's. */
+enum slg_color_type
+{
+    SLG_COLOR_R_FLOAT    = 5,
+    SLG_COLOR_RGBA_8U    = 21,
+    SLG_COLOR_RGBA_FLOAT = 26
+};
+
+/* Built-in device shader programs. In SoftLight a shader is a host function
+ * pointer (SL_VertexShader::shader, SL_FragmentShader::shader,
+ * softlight/include/softlight/SL_Shader.hpp:58-92); on the GPU it is a
+ * __device__ function compiled into a pipeline instance, named by this id. */
+enum slg_shader_program
+{
+    SLG_PROGRAM_LAMBERT_TEX        = 1, /* textured Lambert + ambient, per-draw model matrix */
+    SLG_PROGRAM_BLINN_PHONG_INST   = 2, /* textured Blinn-Phong, 4 point lights, per-instance matrices */
+    SLG_PROGRAM_VCOLOR_TEX_ALPHA   = 3, /* vertex colour x RGBA8 texture, vertex alpha */
+    SLG_PROGRAM_VCOLOR_TEXF        = 4, /* vertex colour x RGBA float texture */
+    SLG_PROGRAM_FLAT_COLOR         = 5  /* uniform colour, no varyings */
+};
+
+/* SL_Mesh (softlight/include/softlight/SL_Mesh.hpp:30-39), same layout */
+typedef struct slg_mesh
+{
+    size_t   vaoId;
+    size_t   elementBegin;
+    size_t   elementEnd;
+    uint32_t mode;
+    uint32_t materialId;
+} slg_mesh;
+
+/* SL_VertexShader (softlight/include/softlight/SL_Shader.hpp:58) */
+typedef struct slg_vertex_shader
+{
+    uint8_t  numVaryings;
+    uint8_t  cullMode;
+    uint32_t program;     /* slg_shader_program */
+} slg_vertex_shader;
+
+/* SL_FragmentShader (softlight/include/softlight/SL_Shader.hpp:89) */
+typedef struct slg_fragment_shader
+{
+    uint8_t  numVaryings;
+    uint8_t  numOutputs;
+    uint8_t  blend;
+    uint8_t  depthTest;
+    uint8_t  depthMask;
+    uint32_t program;     /* slg_shader_program */
+} slg_fragment_shader;
+
+/* One draw of a batch: the arguments of one SL_Context::draw or
+ * draw_instanced call (softlight/src/SL_Context.cpp:714-740). */
+typedef struct slg_draw_cmd
+{
+    slg_mesh mesh;
+    size_t   numInstances;
+    size_t   shaderId;
+} slg_draw_cmd;
+
+typedef struct slg_context slg_context;
+
+/* SL_Context::SL_Context / ~SL_Context (softlight/src/SL_Context.cpp:21-50) */
+int         slg_context_create(slg_context** outCtx);
+void        slg_context_destroy(slg_context* ctx);
+const char* slg_last_error(const slg_context* ctx);
+
+/* SL_Context::num_threads (softlight/src/SL_Context.cpp:1135,1145): accepted,
+ * returns the value stored; the GPU path does not use host threads. */
+unsigned slg_num_threads(slg_context* ctx, unsigned n);
+
+/* SL_Context::create_vbo + SL_VertexBuffer::init/assign
+ * (softlight/src/SL_Context.cpp:335; softlight/src/SL_VertexBuffer.cpp:96) */
+size_t slg_create_vbo(slg_context* ctx);
+int    slg_vbo_init(slg_context* ctx, size_t vboId, size_t numBytes, const void* data);
+int    slg_vbo_assign(slg_context* ctx, size_t vboId, const void* data, size_t offset, size_t numBytes);
+
+/* SL_Context::create_ibo + SL_IndexBuffer::init
+ * (softlight/src/SL_Context.cpp:386; softlight/src/SL_IndexBuffer.cpp:138) */
+size_t slg_create_ibo(slg_context* ctx);
+int    slg_ibo_init(slg_context* ctx, size_t iboId, size_t numElements, int indexType, const void* data);
+
+/* SL_Context::create_vao + SL_VertexArray::set_vertex_buffer / set_index_buffer /
+ * set_binding (softlight/src/SL_Context.cpp:181;
+ * softlight/include/softlight/SL_VertexArray.hpp:56-85,176,216) */
+size_t slg_create_vao(slg_context* ctx);
+int    slg_vao_set_vertex_buffer(slg_context* ctx, size_t vaoId, size_t vboId);
+int    slg_vao_set_index_buffer(slg_context* ctx, size_t vaoId, size_t iboId);
+int    slg_vao_set_binding(slg_context* ctx, size_t vaoId, unsigned bindId, ptrdiff_t offset,
+                           ptrdiff_t stride, unsigned numComponents, int dataType);
+
+/* SL_Context::create_texture + SL_Texture::init / set_texels / data
+ * (softlight/src/SL_Context.cpp:232; softlight/src/SL_Texture.cpp:276;
+ * softlight/include/softlight/SL_Texture.hpp:77-181) */
+size_t slg_create_texture(slg_context* ctx);
+int    slg_texture_init(slg_context* ctx, size_t texId, int colorType, uint16_t w, uint16_t h, uint16_t d);
+int    slg_texture_set_texels(slg_context* ctx, size_t texId, const void* data, size_t numBytes);
+/* Device-to-host read of a texture (replaces SL_Context::blit to a swapchain,
+ * softlight/src/SL_Context.cpp:747-880): copies w*h*d texels. */
+int    slg_texture_read(slg_context* ctx, size_t texId, void* dst, size_t numBytes);
+
+/* SL_Context::create_framebuffer + SL_Framebuffer::reserve_color_buffers /
+ * attach_color_buffer / attach_depth_buffer (softlight/src/SL_Context.cpp:284;
+ * softlight/src/SL_Framebuffer.cpp:823,855,908) */
+size_t slg_create_framebuffer(slg_context* ctx);
+int    slg_fbo_reserve_color_buffers(slg_context* ctx, size_t fboId, unsigned numColorBuffers);
+int    slg_fbo_attach_color_buffer(slg_context* ctx, size_t fboId, unsigned index, size_t texId);
+int    slg_fbo_attach_depth_buffer(slg_context* ctx, size_t fboId, size_t texId);
+
+/* SL_Context::create_ubo (softlight/src/SL_Context.cpp:437) + SL_UniformBuffer (1024 bytes,
+ * softlight/include/softlight/SL_UniformBuffer.hpp:12-20). Texture and buffer
+ * references inside a uniform block are ids, not host pointers. */
+size_t slg_create_ubo(slg_context* ctx);
+int    slg_ubo_assign(slg_context* ctx, size_t uboId, const void* data, size_t numBytes);
+
+/* SL_Context::create_shader (softlight/src/SL_Context.cpp:488-606): same
+ * validation, SLG_INVALID_ID where the reference returns (size_t)-1. */
+size_t slg_create_shader(slg_context* ctx, const slg_vertex_shader* vs,
+                         const slg_fragment_shader* fs, size_t uboId);
+
+/* SL_Context::clear_framebuffer / clear_color_buffer / clear_depth_buffer
+ * (softlight/src/SL_Context.cpp:881-969) */
+int slg_clear_framebuffer(slg_context* ctx, size_t fboId, unsigned attachment, const double rgba[4], double depth);
+int slg_clear_color_buffer(slg_context* ctx, size_t fboId, unsigned attachment, const double rgba[4]);
+int slg_clear_depth_buffer(slg_context* ctx, size_t fboId, double depth);
+
+/* SL_Context::draw / draw_instanced / draw_multiple
+ * (softlight/include/softlight/SL_Context.hpp:215-225; softlight/src/SL_Context.cpp:714-740) */
+int slg_draw(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId);
+int slg_draw_instanced(slg_context* ctx, const slg_mesh* m, size_t numInstances, size_t shaderId, size_t fboId);
+int slg_draw_multiple(slg_context* ctx, const slg_mesh* meshes, size_t numMeshes, size_t shaderId, size_t fboId);
+
+/* Many draws (each possibly instanced, each with its own shader/uniforms) in
+ * one launch sequence with the same result as issuing them one by one with
+ * slg_draw / slg_draw_instanced. No single reference counterpart: it replaces
+ * a caller loop over SL_Context::draw (softlight/tests/sl_instancing_test.cpp:236-279). */
+int slg_draw_batch(slg_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, size_t fboId);
+
+/* Wait for all queued work (SL_Context::draw is synchronous in the reference;
+ * here results are synchronous at slg_finish / slg_texture_read). */
+int slg_finish(slg_context* ctx);
+
+/*-----------------------------------------------------------------------------
+ * GPU-only controls (no reference counterpart: SoftLight's only runtime knob
+ * is num_threads).
+-----------------------------------------------------------------------------*/
+/* The cudaStream_t the context enqueues its work on, as an opaque pointer. */
+void* slg_context_stream(slg_context* ctx);
+
+/* Screen-tile size of the binning and raster stages. Supported sizes:
+ * 8x8, 16x16, 32x16, 32x32 (default), 64x32, 64x64. */
+int slg_set_tile_size(slg_context* ctx, int tileW, int tileH);
+
+/* When enabled, every draw records CUDA events around its four stages;
+ * slg_stage_times returns the last draw's stage durations in milliseconds:
+ * [0] vertex/set-up, [1] tile scan, [2] bin fill, [3] raster+shade. */
+int slg_profile_stages(slg_context* ctx, int enable);
+int slg_stage_times(slg_context* ctx, float ms[4]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SLG_H */

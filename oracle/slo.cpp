@@ -1,0 +1,1352 @@
+/*
+ * slo.cpp - CPU oracle for the GB300 draw path (test infrastructure only).
+ *
+ * This file restates, in plain C++, the arithmetic and ordering of
+ * SoftLight's triangle draw path as compiled WITHOUT any LS_X86_* / LS_ARM_*
+ * macro, i.e. the portable branches of every #if ladder, with FP contraction
+ * off and one thread. Nothing in the product links or calls it: the tests,
+ * the smoke check and the benchmark's CPU-baseline leg use it as the checker
+ * and as the timed CPU restatement.
+ *
+ * Each function names the reference code it follows (paths relative to the
+ * SoftLight source tree). The reference's vector library (LightMath, an
+ * absent git submodule) is restated with these definitions, shared with the
+ * GPU path and with the compatibility shim used to build the reference
+ * sources themselves:
+ *   fmadd(a,b,c) = a*b + c (two roundings); rcp(x) = 1/x;
+ *   dot / sum fold left: ((a0+a1)+a2)+a3;  mix(a,b,t) = (b-a)*t + a;
+ *   cross(vec4 a, vec4 b) = (a1*b2-a2*b1, a2*b0-a0*b2, a0*b1-a1*b0, 0);
+ *   cross(vec2 a, vec2 b) = a0*b1 - a1*b0;  max(a,b) = a<b ? b : a;
+ *   min(a,b) = b<a ? b : a;  vec4 <= / >= compare all four components;
+ *   mat4 * vec4 = m[0]*v0 + m[1]*v1 + m[2]*v2 + m[3]*v3 (columns, left fold);
+ *   float -> int32 conversions behave like x86 cvttss2si (NaN / out of
+ *   range -> INT32_MIN) so the result does not depend on the host ISA.
+ */
+#include "slo.h"
+#include "../include/slg_programs.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace
+{
+
+/*-----------------------------------------------------------------------------
+ * Restated LightMath helpers
+-----------------------------------------------------------------------------*/
+struct V4
+{
+    float v[4];
+    float& operator[](int i) { return v[i]; }
+    float operator[](int i) const { return v[i]; }
+};
+
+static inline V4 mk(float a, float b, float c, float d) { V4 r; r.v[0] = a; r.v[1] = b; r.v[2] = c; r.v[3] = d; return r; }
+static inline V4 add(const V4& a, const V4& b) { return mk(a[0] + b[0], a[1] + b[1], a[2] + b[2], a[3] + b[3]); }
+static inline V4 sub(const V4& a, const V4& b) { return mk(a[0] - b[0], a[1] - b[1], a[2] - b[2], a[3] - b[3]); }
+static inline V4 mul(const V4& a, const V4& b) { return mk(a[0] * b[0], a[1] * b[1], a[2] * b[2], a[3] * b[3]); }
+static inline V4 mulf(const V4& a, float s) { return mk(a[0] * s, a[1] * s, a[2] * s, a[3] * s); }
+static inline float dot(const V4& a, const V4& b) { return ((a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]) + a[3] * b[3]; }
+static inline float lm_max(float a, float b) { return (a < b) ? b : a; }
+static inline float lm_min(float a, float b) { return (b < a) ? b : a; }
+static inline V4 mix(const V4& a, const V4& b, float t)
+{
+    return mk((b[0] - a[0]) * t + a[0], (b[1] - a[1]) * t + a[1], (b[2] - a[2]) * t + a[2], (b[3] - a[3]) * t + a[3]);
+}
+static inline int sign_mask(float f) { uint32_t u; std::memcpy(&u, &f, 4); return (int)(u >> 31); }
+
+static inline int32_t f2i(float f)
+{
+    if (!(f >= -2147483648.f && f < 2147483648.f))
+    {
+        return INT32_MIN;
+    }
+    return (int32_t)f;
+}
+
+static inline uint8_t f2u8(float f) { return (uint8_t)(uint32_t)f2i(f); }
+
+/* mat4 (column-major, 16 floats) * vec4 as ls::math does it */
+static inline V4 mat_mul(const float* m, const V4& v)
+{
+    V4 r;
+    for (int row = 0; row < 4; ++row)
+    {
+        r[row] = ((m[0 + row] * v[0] + m[4 + row] * v[1]) + m[8 + row] * v[2]) + m[12 + row] * v[3];
+    }
+    return r;
+}
+
+/*-----------------------------------------------------------------------------
+ * Resources
+-----------------------------------------------------------------------------*/
+struct Texture
+{
+    int type = -1;
+    uint16_t w = 0, h = 0, d = 0;
+    unsigned bpt = 0;
+    std::vector<uint8_t> bytes;
+};
+
+struct Vbo { std::vector<uint8_t> bytes; };
+
+struct Ibo
+{
+    int type = SLG_VERTEX_DATA_INVALID;
+    size_t count = 0;
+    std::vector<uint8_t> bytes;
+};
+
+struct Binding { ptrdiff_t offset = 0, stride = 0; unsigned comps = 0; int type = 0; };
+
+struct Vao
+{
+    size_t vbo = SLG_INVALID_ID, ibo = SLG_INVALID_ID;
+    Binding bindings[8];
+};
+
+struct Fbo
+{
+    unsigned numColors = 0;
+    size_t colors[4] = {SLG_INVALID_ID, SLG_INVALID_ID, SLG_INVALID_ID, SLG_INVALID_ID};
+    size_t depth = SLG_INVALID_ID;
+};
+
+struct Ubo { alignas(16) uint8_t bytes[1024]; };
+
+struct Shader
+{
+    uint8_t cull, depthTest, depthMask, blend, numVaryings, numOutputs;
+    uint32_t vsProgram, fsProgram;
+    size_t ubo;
+};
+
+/* SL_TransformedVert (softlight/include/softlight/SL_ShaderUtil.hpp:612) */
+struct TVert
+{
+    V4 vert;
+    V4 varyings[4];
+};
+
+/* SL_FragmentBin (softlight/include/softlight/SL_ShaderUtil.hpp:627) */
+struct Bin
+{
+    V4 screen[3];
+    V4 bc[3];
+    V4 varyings[12];
+    size_t primIndex;
+    uint32_t drawIndex;
+};
+
+static size_t bytes_per_color(int type)
+{
+    switch (type)
+    {
+        case SLG_COLOR_R_FLOAT: return 4;
+        case SLG_COLOR_RGBA_8U: return 4;
+        case SLG_COLOR_RGBA_FLOAT: return 16;
+        default: return 0;
+    }
+}
+
+static size_t index_bytes(int type)
+{
+    switch (type)
+    {
+        case SLG_VERTEX_DATA_BYTE: return 1;
+        case SLG_VERTEX_DATA_SHORT: return 2;
+        case SLG_VERTEX_DATA_INT: return 4;
+        default: return 0;
+    }
+}
+
+} // namespace
+
+struct slo_context
+{
+    std::string err;
+    unsigned numThreads = 1;
+    std::vector<Vbo> vbos;
+    std::vector<Ibo> ibos;
+    std::vector<Vao> vaos;
+    std::vector<Texture*> textures;
+    std::vector<Fbo> fbos;
+    std::vector<Ubo*> ubos;
+    std::vector<Shader> shaders;
+    uint64_t lastBins = 0, lastFrags = 0;
+
+    ~slo_context()
+    {
+        for (Texture* t : textures) delete t;
+        for (Ubo* u : ubos) delete u;
+    }
+
+    int fail(int code, const char* msg) { err = msg; return code; }
+};
+
+namespace
+{
+
+/*-----------------------------------------------------------------------------
+ * Shader environment for the built-in programs
+-----------------------------------------------------------------------------*/
+/* sl_sample_bilinear<color, SL_WrapMode::REPEAT, ORDERED>
+ * (softlight/include/softlight/SL_Sampler.hpp:97-115,187-218) */
+static inline float wrap_repeat(float uvw)
+{
+    return (uvw < 0.f ? 1.f : 0.f) + std::fmod(uvw, 1.f);
+}
+
+struct BilinearCoords
+{
+    uint32_t i00, i01, i10, i11;
+    float omdx, omdy, dx, dy;
+};
+
+static inline BilinearCoords bilinear_coords(const Texture& t, float x, float y)
+{
+    const float xf = wrap_repeat(x) * (float)t.w;
+    const float yf = wrap_repeat(y) * (float)t.h;
+    const uint16_t xi0 = (uint16_t)(uint32_t)f2i(xf);
+    const uint16_t yi0 = (uint16_t)(uint32_t)f2i(yf);
+    const uint16_t xn = (uint16_t)(xi0 + 1u);
+    const uint16_t yn = (uint16_t)(yi0 + 1u);
+    const uint16_t xi1 = (t.w < xn) ? t.w : xn;
+    const uint16_t yi1 = (t.h < yn) ? t.h : yn;
+    BilinearCoords c;
+    c.dx = xf - (float)xi0;
+    c.dy = yf - (float)yi0;
+    c.omdx = 1.f - c.dx;
+    c.omdy = 1.f - c.dy;
+    c.i00 = (uint32_t)xi0 + (uint32_t)t.w * yi0;
+    c.i01 = (uint32_t)xi0 + (uint32_t)t.w * yi1;
+    c.i10 = (uint32_t)xi1 + (uint32_t)t.w * yi0;
+    c.i11 = (uint32_t)xi1 + (uint32_t)t.w * yi1;
+    return c;
+}
+
+static inline V4 sample_rgba8(const Texture& t, float x, float y)
+{
+    const BilinearCoords c = bilinear_coords(t, x, y);
+    const uint8_t* p = t.bytes.data();
+    V4 px[4];
+    const uint32_t idx[4] = {c.i00, c.i01, c.i10, c.i11};
+    for (int k = 0; k < 4; ++k)
+    {
+        const uint8_t* q = p + 4u * (size_t)idx[k];
+        /* color_cast<float, uint8_t> (softlight/include/softlight/SL_Color.hpp:674) */
+        px[k] = mk((float)q[0] * 0.00392156862745f, (float)q[1] * 0.00392156862745f,
+                   (float)q[2] * 0.00392156862745f, (float)q[3] * 0.00392156862745f);
+    }
+    const V4 w0 = mulf(mulf(px[0], c.omdx), c.omdy);
+    const V4 w1 = mulf(mulf(px[1], c.omdx), c.dy);
+    const V4 w2 = mulf(mulf(px[2], c.dx), c.omdy);
+    const V4 w3 = mulf(mulf(px[3], c.dx), c.dy);
+    const V4 s = add(add(add(w0, w1), w2), w3);
+    /* color_cast<uint8_t, float> then back to float in the shader */
+    V4 r;
+    for (int k = 0; k < 4; ++k)
+    {
+        r[k] = (float)f2u8(s[k] * 255.f) * 0.00392156862745f;
+    }
+    return r;
+}
+
+static inline V4 sample_rgbaf(const Texture& t, float x, float y)
+{
+    const BilinearCoords c = bilinear_coords(t, x, y);
+    const float* p = reinterpret_cast<const float*>(t.bytes.data());
+    V4 px[4];
+    const uint32_t idx[4] = {c.i00, c.i01, c.i10, c.i11};
+    for (int k = 0; k < 4; ++k)
+    {
+        const float* q = p + 4u * (size_t)idx[k];
+        px[k] = mk(q[0], q[1], q[2], q[3]);
+    }
+    const V4 w0 = mulf(mulf(px[0], c.omdx), c.omdy);
+    const V4 w1 = mulf(mulf(px[1], c.omdx), c.dy);
+    const V4 w2 = mulf(mulf(px[2], c.dx), c.omdy);
+    const V4 w3 = mulf(mulf(px[3], c.dx), c.dy);
+    return add(add(add(w0, w1), w2), w3);
+}
+
+struct Env
+{
+    const slo_context* ctx;
+    const uint8_t* vboBytes;
+    Binding b0;
+    const uint8_t* ubo;
+
+    const float* vertex(uint64_t vertId) const
+    {
+        return reinterpret_cast<const float*>(vboBytes + b0.offset + b0.stride * (ptrdiff_t)vertId);
+    }
+    const void* uniforms() const { return ubo; }
+    const float* buffer(uint32_t vboId) const
+    {
+        return reinterpret_cast<const float*>(ctx->vbos[vboId].bytes.data());
+    }
+    slg_v4 sample_rgba8(uint32_t texId, float u, float v) const
+    {
+        const V4 r = ::sample_rgba8(*ctx->textures[texId], u, v);
+        return slg_make_v4(r[0], r[1], r[2], r[3]);
+    }
+    slg_v4 sample_rgbaf(uint32_t texId, float u, float v) const
+    {
+        const V4 r = ::sample_rgbaf(*ctx->textures[texId], u, v);
+        return slg_make_v4(r[0], r[1], r[2], r[3]);
+    }
+};
+
+static inline V4 from_slg(const slg_v4& a) { return mk(a.x, a.y, a.z, a.w); }
+static inline slg_v4 to_slg(const V4& a) { return slg_make_v4(a[0], a[1], a[2], a[3]); }
+
+static V4 run_vs(uint32_t program, const Env& env, uint64_t vertId, uint64_t instId, V4* varyings)
+{
+    slg_v4 vary[4];
+    slg_v4 r;
+    switch (program)
+    {
+        case SLG_PROGRAM_LAMBERT_TEX:      r = slg_vs_lambert(env, vertId, instId, vary); break;
+        case SLG_PROGRAM_BLINN_PHONG_INST: r = slg_vs_blinn(env, vertId, instId, vary); break;
+        case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
+        case SLG_PROGRAM_VCOLOR_TEXF:      r = slg_vs_vcolor(env, vertId, instId, vary); break;
+        default:                           r = slg_vs_flat(env, vertId, instId, vary); break;
+    }
+    for (int i = 0; i < 4; ++i) varyings[i] = from_slg(vary[i]);
+    return from_slg(r);
+}
+
+static bool run_fs(uint32_t program, const Env& env, const V4* varyings, V4* outputs)
+{
+    slg_v4 vary[4], outs[4];
+    for (int i = 0; i < 4; ++i) { vary[i] = to_slg(varyings[i]); outs[i] = slg_make_v4(0.f, 0.f, 0.f, 0.f); }
+    bool r;
+    switch (program)
+    {
+        case SLG_PROGRAM_LAMBERT_TEX:      r = slg_fs_lambert(env, vary, outs); break;
+        case SLG_PROGRAM_BLINN_PHONG_INST: r = slg_fs_blinn(env, vary, outs); break;
+        case SLG_PROGRAM_VCOLOR_TEX_ALPHA: r = slg_fs_vcolor_tex_alpha(env, vary, outs); break;
+        case SLG_PROGRAM_VCOLOR_TEXF:      r = slg_fs_vcolor_texf(env, vary, outs); break;
+        default:                           r = slg_fs_flat(env, vary, outs); break;
+    }
+    for (int i = 0; i < 4; ++i) outputs[i] = from_slg(outs[i]);
+    return r;
+}
+
+/*-----------------------------------------------------------------------------
+ * Vertex stage (softlight/src/SL_TriProcessor.cpp)
+-----------------------------------------------------------------------------*/
+/* face_determinant, portable branch (SL_TriProcessor.cpp:98-115) */
+static inline float face_determinant(const V4& p0, const V4& p1, const V4& p2)
+{
+    const float w0 = 1.f / p0[3];
+    const float w1 = 1.f / p1[3];
+    const float w2 = 1.f / p2[3];
+    const V4 v0 = mulf(p0, w0);
+    const V4 v1 = mulf(p1, w1);
+    const V4 v2 = mulf(p2, w2);
+    const V4 yCAB = mk(v2[1], v0[1], v1[1], 0.f);
+    const V4 yBCA = mk(v1[1], v2[1], v0[1], 0.f);
+    const V4 xABC = mk(v0[0], v1[0], v2[0], 0.f);
+    return dot(xABC, sub(yBCA, yCAB));
+}
+
+/* sl_ndc_clip_status, portable branch (SL_PostVertexTransform.hpp:651-673) */
+static inline int clip_status(const V4& c0, const V4& c1, const V4& c2)
+{
+    auto le = [](const V4& c, float w) { return c[0] <= w && c[1] <= w && c[2] <= w && c[3] <= w; };
+    auto ge = [](const V4& c, float w) { return c[0] >= w && c[1] >= w && c[2] >= w && c[3] >= w; };
+    const bool vis = le(c0, c0[3]) && le(c1, c1[3]) && le(c2, c2[3]) &&
+                     ge(c0, -c0[3]) && ge(c1, -c1[3]) && ge(c2, -c2[3]);
+    const bool part = c0[3] > 0.f || c1[3] > 0.f || c2[3] > 0.f;
+    return (vis ? 3 : 0) | (part ? 1 : 0);
+}
+
+/* sl_perspective_divide, portable branch (SL_PostVertexTransform.hpp:240-249) */
+static inline void perspective_divide(V4& v)
+{
+    const float wInv = 1.f / v[3];
+    const V4 m = mulf(v, wInv);
+    v = mk(m[0], m[1], m[2], wInv);
+}
+
+/* sl_ndc_to_screen_coords, portable branch (SL_PostVertexTransform.hpp:509-524) */
+static inline void ndc_to_screen(V4& p, const V4& vp)
+{
+    const float w = vp[2] * 0.5f;
+    const float h = vp[3] * 0.5f;
+    p[0] = lm_max(std::floor((p[0] + 1.f) * w + vp[0]), 0.f);
+    p[1] = lm_max(std::floor((p[1] + 1.f) * h + vp[1]), 0.f);
+}
+
+struct DrawState
+{
+    const slo_context* ctx;
+    const Shader* shader;
+    Env env;
+    float scissor[16];
+    V4 viewport;
+    unsigned numVaryings;
+    uint32_t drawIndex;
+};
+
+/* SL_TriProcessor::push_bin (SL_TriProcessor.cpp:248-342) */
+static void push_bin(const DrawState& ds, std::vector<Bin>& bins, size_t primIndex, const TVert& a, const TVert& b, const TVert& c)
+{
+    const V4& p0 = a.vert;
+    const V4& p1 = b.vert;
+    const V4& p2 = c.vert;
+
+    const float minX = lm_min(lm_min(p0[0], p1[0]), p2[0]);
+    const float minY = lm_min(lm_min(p0[1], p1[1]), p2[1]);
+    const float maxX = lm_max(lm_max(p0[0], p1[0]), p2[0]);
+    const float maxY = lm_max(lm_max(p0[1], p1[1]), p2[1]);
+    if ((maxX - minX < 1.f) || (maxY - minY < 1.f))
+    {
+        return;
+    }
+
+    const float xyx = p0[0] - p1[0], xyy = p0[1] - p1[1];
+    const float zyx = p2[0] - p1[0], zyy = p2[1] - p1[1];
+    const float denom = 1.f / (zyx * xyy - zyy * xyx);
+
+    const V4 X = mk(p0[0], p1[0], p2[0], 0.f);
+    const V4 Y = mk(p0[1], p1[1], p2[1], 0.f);
+    const V4 ddx = mk(Y[1] * 1.f - Y[2] * 1.f, Y[2] * 1.f - Y[0] * 1.f, Y[0] * 1.f - Y[1] * 1.f, 0.f);
+    const V4 ddy = mk(1.f * X[2] - 1.f * X[1], 1.f * X[0] - 1.f * X[2], 1.f * X[1] - 1.f * X[0], 0.f);
+    const V4 ddz = mk(X[1] * Y[2] - X[2] * Y[1], X[2] * Y[0] - X[0] * Y[2], X[0] * Y[1] - X[1] * Y[0], 0.f);
+
+    Bin bin;
+    bin.screen[0] = p0;
+    bin.screen[1] = p1;
+    bin.screen[2] = p2;
+    bin.bc[0] = mulf(ddx, denom);
+    bin.bc[1] = mulf(ddy, denom);
+    bin.bc[2] = mulf(ddz, denom);
+    for (unsigned i = 0; i < ds.numVaryings; ++i)
+    {
+        bin.varyings[i + 0] = a.varyings[i];
+        bin.varyings[i + 4] = b.varyings[i];
+        bin.varyings[i + 8] = c.varyings[i];
+    }
+    bin.primIndex = primIndex;
+    bin.drawIndex = ds.drawIndex;
+    bins.push_back(bin);
+}
+
+/* SL_TriProcessor::clip_and_process_tris (SL_TriProcessor.cpp:370-519) */
+static void clip_and_process(const DrawState& ds, std::vector<Bin>& bins, size_t primIndex, const TVert& a, const TVert& b, const TVert& c)
+{
+    const unsigned numVarys = ds.numVaryings;
+    unsigned numTotalVerts = 3;
+    V4 tempVerts[9], newVerts[9];
+    V4 tempVarys[36], newVarys[36];
+    std::memset(tempVerts, 0, sizeof(tempVerts));
+    std::memset(newVerts, 0, sizeof(newVerts));
+    std::memset(tempVarys, 0, sizeof(tempVarys));
+    std::memset(newVarys, 0, sizeof(newVarys));
+    static const float clipEdges[6][4] = {
+        { 1.f,  0.f,  0.f, 1.f},
+        {-1.f,  0.f,  0.f, 1.f},
+        { 0.f,  1.f,  0.f, 1.f},
+        { 0.f, -1.f,  0.f, 1.f},
+        { 0.f,  0.f,  1.f, 1.f},
+        { 0.f,  0.f, -1.f, 1.f},
+    };
+
+    newVerts[0] = a.vert;
+    newVerts[1] = b.vert;
+    newVerts[2] = c.vert;
+    for (unsigned i = 0; i < numVarys; ++i)
+    {
+        newVarys[0 + i] = a.varyings[i];
+        newVarys[4 + i] = b.varyings[i];
+        newVarys[8 + i] = c.varyings[i];
+    }
+
+    for (int e = 0; e < 6; ++e)
+    {
+        const V4 edge = mk(clipEdges[e][0], clipEdges[e][1], clipEdges[e][2], clipEdges[e][3]);
+        unsigned numNewVerts = 0;
+        unsigned j = numTotalVerts - 1;
+        V4 p0 = newVerts[numTotalVerts - 1];
+        float t0 = dot(p0, edge);
+        int visible0 = !sign_mask(t0);
+
+        for (unsigned k = 0; k < numTotalVerts; ++k)
+        {
+            const V4 p1 = newVerts[k];
+            const float t1 = dot(p1, edge);
+            const int visible1 = !sign_mask(t1);
+
+            if (visible0 ^ visible1)
+            {
+                const float t = t0 * (1.f / (t0 - t1));
+                tempVerts[numNewVerts] = mix(p0, p1, t);
+                for (unsigned i = 0; i < numVarys; ++i)
+                {
+                    tempVarys[numNewVerts * 4 + i] = mix(newVarys[j * 4 + i], newVarys[k * 4 + i], t);
+                }
+                ++numNewVerts;
+            }
+
+            if (visible1)
+            {
+                tempVerts[numNewVerts] = p1;
+                for (unsigned i = 0; i < numVarys; ++i)
+                {
+                    tempVarys[numNewVerts * 4 + i] = newVarys[k * 4 + i];
+                }
+                ++numNewVerts;
+            }
+
+            j = k;
+            p0 = p1;
+            t0 = t1;
+            visible0 = visible1;
+        }
+
+        if (!numNewVerts)
+        {
+            return;
+        }
+
+        numTotalVerts = numNewVerts;
+        for (unsigned i = 0; i < numNewVerts; ++i)
+        {
+            newVerts[i] = tempVerts[i];
+        }
+
+        /* The reference copies numNewVerts vectors starting at each vertex's
+         * varying slot (SL_TriProcessor.cpp:471-475), not numVarys; restated
+         * slot by slot, bounded to the 36-slot arrays. */
+        for (unsigned i = numNewVerts; i--;)
+        {
+            const unsigned offset = i * 4;
+            for (unsigned m = 0; m < numNewVerts; ++m)
+            {
+                if (offset + m < 36)
+                {
+                    newVarys[offset + m] = tempVarys[offset + m];
+                }
+            }
+        }
+    }
+
+    if (numTotalVerts < 3)
+    {
+        return;
+    }
+
+    for (unsigned i = 0; i < numTotalVerts; ++i)
+    {
+        perspective_divide(newVerts[i]);
+        ndc_to_screen(newVerts[i], ds.viewport);
+    }
+
+    TVert q0, q1, q2;
+    q0.vert = newVerts[0];
+    for (unsigned i = 0; i < numVarys; ++i) q0.varyings[i] = newVarys[i];
+
+    for (unsigned i = numTotalVerts - 2; i--;)
+    {
+        const unsigned j = i + 1;
+        const unsigned k = i + 2;
+        q1.vert = newVerts[j];
+        q2.vert = newVerts[k];
+        for (unsigned v = 0; v < numVarys; ++v)
+        {
+            q1.varyings[v] = newVarys[j * 4 + v];
+            q2.varyings[v] = newVarys[k * 4 + v];
+        }
+        push_bin(ds, bins, primIndex, q0, q1, q2);
+    }
+}
+
+/* get_next_vertex3, portable branch (SL_TriProcessor.cpp:125-234) */
+static inline size_t read_index(const Ibo& ibo, size_t i)
+{
+    const uint8_t* p = ibo.bytes.data();
+    switch (ibo.type)
+    {
+        case SLG_VERTEX_DATA_BYTE:  return p[i];
+        case SLG_VERTEX_DATA_SHORT: { uint16_t v; std::memcpy(&v, p + 2 * i, 2); return v; }
+        default:                    { uint32_t v; std::memcpy(&v, p + 4 * i, 4); return v; }
+    }
+}
+
+/* SL_TriProcessor::process_verts<usingIndices> (SL_TriProcessor.cpp:527-640)
+ * restricted to elements [first, last) of one mesh instance. */
+static void process_verts(const DrawState& ds, const Ibo* ibo, const slg_mesh& m, size_t instanceId,
+                          size_t first, size_t last, std::vector<Bin>& bins)
+{
+    const size_t numElements = m.elementEnd - m.elementBegin;
+    const size_t primOffset = numElements * instanceId;
+    const uint8_t cullMode = ds.shader->cull;
+    TVert tv[3];
+
+    for (size_t i = first; i < last; i += 3)
+    {
+        for (int k = 0; k < 3; ++k)
+        {
+            const size_t vertId = ibo ? read_index(*ibo, i + k) : (i + k);
+            tv[k].vert = run_vs(ds.shader->vsProgram, ds.env, vertId, instanceId, tv[k].varyings);
+        }
+
+        if (cullMode != SLG_CULL_OFF)
+        {
+            const float det = face_determinant(tv[0].vert, tv[1].vert, tv[2].vert);
+            const bool culled = (cullMode == SLG_CULL_FRONT_FACE) ^ (sign_mask(det) != 0);
+            if (culled)
+            {
+                continue;
+            }
+        }
+
+        for (int k = 0; k < 3; ++k)
+        {
+            tv[k].vert = mat_mul(ds.scissor, tv[k].vert);
+        }
+
+        const int vis = clip_status(tv[0].vert, tv[1].vert, tv[2].vert);
+        if (vis == 3)
+        {
+            for (int k = 0; k < 3; ++k)
+            {
+                perspective_divide(tv[k].vert);
+                ndc_to_screen(tv[k].vert, ds.viewport);
+            }
+            push_bin(ds, bins, primOffset + i, tv[0], tv[1], tv[2]);
+        }
+        else if (vis == 1)
+        {
+            clip_and_process(ds, bins, primOffset + i, tv[0], tv[1], tv[2]);
+        }
+    }
+}
+
+/*-----------------------------------------------------------------------------
+ * Fragment stage
+-----------------------------------------------------------------------------*/
+struct Target
+{
+    uint8_t* bytes;
+    int type;
+    uint16_t w;
+};
+
+/* assign_pixel / assign_alpha_pixel, portable (SL_Framebuffer.cpp:45-80,271-368) */
+static inline void write_color(const Target& t, unsigned x, unsigned y, const V4& rgba, uint8_t blend)
+{
+    const size_t idx = (size_t)x + (size_t)t.w * y;
+    V4 src = rgba;
+
+    if (blend != SLG_BLEND_OFF)
+    {
+        V4 d;
+        if (t.type == SLG_COLOR_RGBA_8U)
+        {
+            const uint8_t* q = t.bytes + 4 * idx;
+            d = mk((float)q[0] * 0.00392156862745f, (float)q[1] * 0.00392156862745f,
+                   (float)q[2] * 0.00392156862745f, (float)q[3] * 0.00392156862745f);
+        }
+        else if (t.type == SLG_COLOR_RGBA_FLOAT)
+        {
+            const float* q = reinterpret_cast<const float*>(t.bytes) + 4 * idx;
+            d = mk(q[0], q[1], q[2], q[3]);
+        }
+        else
+        {
+            const float* q = reinterpret_cast<const float*>(t.bytes) + idx;
+            d = mk(q[0], 0.f, 0.f, 1.f);
+        }
+
+        const float sa = rgba[3];
+        const float modulation = 1.f - sa;
+        if (blend == SLG_BLEND_ALPHA)
+        {
+            const float dstMod = modulation * d[3];
+            const float dstAlpha = dstMod + sa;
+            const float r = 1.f / dstAlpha;
+            d = mk((rgba[0] * sa + d[0] * dstMod) * r, (rgba[1] * sa + d[1] * dstMod) * r,
+                   (rgba[2] * sa + d[2] * dstMod) * r, dstAlpha);
+        }
+        else if (blend == SLG_BLEND_PREMULTIPLED_ALPHA)
+        {
+            d = mk(d[0] * modulation + rgba[0], d[1] * modulation + rgba[1], d[2] * modulation + rgba[2], d[3] * modulation + rgba[3]);
+        }
+        else if (blend == SLG_BLEND_ADDITIVE)
+        {
+            d = mk(rgba[0] * sa + d[0], rgba[1] * sa + d[1], rgba[2] * sa + d[2], rgba[3] * sa + d[3]);
+        }
+        else
+        {
+            d = mk(rgba[0] * sa + d[0] * modulation, rgba[1] * sa + d[1] * modulation,
+                   rgba[2] * sa + d[2] * modulation, rgba[3] * sa + d[3] * modulation);
+        }
+        for (int k = 0; k < 4; ++k)
+        {
+            d[k] = lm_min(lm_max(d[k], 0.f), 1.f);
+        }
+        src = d;
+    }
+
+    if (t.type == SLG_COLOR_RGBA_8U)
+    {
+        uint8_t* q = t.bytes + 4 * idx;
+        for (int k = 0; k < 4; ++k)
+        {
+            q[k] = f2u8(src[k] * 255.f);
+        }
+    }
+    else if (t.type == SLG_COLOR_RGBA_FLOAT)
+    {
+        float* q = reinterpret_cast<float*>(t.bytes) + 4 * idx;
+        for (int k = 0; k < 4; ++k) q[k] = src[k];
+    }
+    else
+    {
+        float* q = reinterpret_cast<float*>(t.bytes) + idx;
+        q[0] = src[0];
+    }
+}
+
+static inline bool depth_cmp(uint8_t func, float z, float d)
+{
+    switch (func)
+    {
+        case SLG_DEPTH_TEST_LESS_THAN:     return z < d;
+        case SLG_DEPTH_TEST_LESS_EQUAL:    return z <= d;
+        case SLG_DEPTH_TEST_GREATER_THAN:  return z > d;
+        case SLG_DEPTH_TEST_GREATER_EQUAL: return z >= d;
+        case SLG_DEPTH_TEST_EQUAL:         return z == d;
+        case SLG_DEPTH_TEST_NOT_EQUAL:     return z != d;
+        default:                           return true;
+    }
+}
+
+struct RasterState
+{
+    const slo_context* ctx;
+    float* depth;
+    uint16_t width;
+    Target colors[4];
+    unsigned numOutputs;
+    std::vector<const Shader*> shaders; /* per draw index */
+    std::vector<Env> envs;               /* per draw index */
+};
+
+/* SL_FragmentProcessor::flush_tri_fragments for one fragment, portable
+ * (SL_FragmentProcessor.cpp:417-531, interpolate_tri_varyings :308-330) */
+static inline void shade_fragment(const RasterState& rs, const Bin& bin, int x, int y, float z, const V4& bcIn, uint64_t& frags)
+{
+    const Shader& sh = *rs.shaders[bin.drawIndex];
+    const V4 homogenous = mk(bin.screen[0][3], bin.screen[1][3], bin.screen[2][3], 0.f);
+    const V4 bc = mul(bcIn, homogenous);
+    const float persp = 1.f / (((bc[0] + bc[1]) + bc[2]) + bc[3]);
+    const V4 bcp = mulf(bc, persp);
+
+    V4 varyings[4];
+    for (unsigned i = 0; i < 4; ++i) varyings[i] = mk(0.f, 0.f, 0.f, 0.f);
+    for (unsigned i = 0; i < sh.numVaryings; ++i)
+    {
+        const V4 v0 = mulf(bin.varyings[i + 0], bcp[0]);
+        const V4 v1 = mulf(bin.varyings[i + 4], bcp[1]);
+        const V4 v2 = mulf(bin.varyings[i + 8], bcp[2]);
+        varyings[i] = add(add(v0, v1), v2);
+    }
+
+    V4 outputs[4];
+    const bool haveOutputs = run_fs(sh.fsProgram, rs.envs[bin.drawIndex], varyings, outputs);
+    if (haveOutputs)
+    {
+        for (unsigned t = 0; t < sh.numOutputs && t < rs.numOutputs; ++t)
+        {
+            write_color(rs.colors[t], (unsigned)x, (unsigned)y, outputs[t], sh.blend);
+        }
+    }
+    if (sh.depthMask == SLG_DEPTH_MASK_ON)
+    {
+        rs.depth[(size_t)x + (size_t)rs.width * y] = z;
+    }
+    ++frags;
+}
+
+/* SL_TriRasterizer::render_triangle_simd, portable branch
+ * (SL_TriRasterizer.cpp:807-923) with SL_ScanlineBounds init/step portable
+ * branches (SL_ScanlineBounds.hpp:137-186,301-321). Only rows with
+ * y % rowStride == rowPhase are drawn (the reference's scan-line
+ * interleave across threads, SL_ScanlineBounds.hpp:32-50). */
+static void raster_bin(const RasterState& rs, const Bin& bin, int rowStride, int rowPhase, uint64_t& frags)
+{
+    const Shader& sh = *rs.shaders[bin.drawIndex];
+    const V4* pts = bin.screen;
+    const int32_t bboxMinY = f2i(lm_min(lm_min(pts[0][1], pts[1][1]), pts[2][1]));
+    const int32_t bboxMaxY = f2i(lm_max(lm_max(pts[0][1], pts[1][1]), pts[2][1]));
+
+    int32_t y = bboxMinY;
+    if (rowStride > 1)
+    {
+        /* sl_scanline_offset (SL_ScanlineBounds.hpp:32-50) */
+        const int32_t n1 = rowStride - 1;
+        y += n1 - ((bboxMinY + (n1 - rowPhase)) % rowStride);
+    }
+    if (y >= bboxMaxY)
+    {
+        return;
+    }
+
+    const V4 depth = mk(pts[0][2], pts[1][2], pts[2][2], 0.f);
+
+    /* SL_ScanlineBounds::init */
+    V4 p0 = pts[0], p1 = pts[1], p2 = pts[2];
+    if (p0[1] < p1[1]) std::swap(p0, p1);
+    if (p0[1] < p2[1]) std::swap(p0, p2);
+    if (p1[1] < p2[1]) std::swap(p1, p2);
+    const V4 p2p0 = sub(p2, p0);
+    const V4 p2p1 = sub(p2, p1);
+    const V4 p1p0 = sub(p1, p0);
+    const float v0y = p0[1], v1y = p1[1], v0x = p0[0], v1x = p1[0];
+    const float p20y = 1.f / p2p0[1];
+    const float p20x = p2p0[0];
+    const float p21xy = p2p1[0] * (1.f / p2p1[1]);
+    const float p10xy = p1p0[0] * (1.f / p1p0[1]);
+
+    const V4* bcs = bin.bc;
+    const V4 bcX = mulf(bcs[0], 4.f);
+
+    do
+    {
+        const float yf = (float)y;
+
+        /* SL_ScanlineBounds::step */
+        const float d0 = yf - v0y;
+        const float d1 = yf - v1y;
+        const float alpha = d0 * p20y;
+        const int32_t lo = f2i(p20x * alpha + v0x);
+        const int32_t secondHalf = -(d1 < 0.f);
+        const int32_t sa = f2i(p21xy * d1 + v1x);
+        const int32_t sb = f2i(p10xy * d0 + v0x);
+        const int32_t hi = (secondHalf & sa) | (~secondHalf & sb);
+        const int32_t xMin = (lo >= hi) ? hi : lo;
+        const int32_t xMax = (lo >= hi) ? lo : hi;
+
+        if ((uint32_t)xMin < (uint32_t)xMax)
+        {
+            const V4 bcY = mk(bcs[1][0] * yf + bcs[2][0], bcs[1][1] * yf + bcs[2][1],
+                              bcs[1][2] * yf + bcs[2][2], bcs[1][3] * yf + bcs[2][3]);
+            V4 bc[4];
+            int32_t x4[4];
+            for (int k = 0; k < 4; ++k)
+            {
+                x4[k] = xMin + k;
+                const float xf = (float)x4[k];
+                bc[k] = mk(bcs[0][0] * xf + bcY[0], bcs[0][1] * xf + bcY[1],
+                           bcs[0][2] * xf + bcY[2], bcs[0][3] * xf + bcY[3]);
+            }
+
+            do
+            {
+                for (int k = 0; k < 4; ++k)
+                {
+                    if (x4[k] < xMax)
+                    {
+                        const float z = dot(depth, bc[k]);
+                        const float d = rs.depth[(size_t)x4[k] + (size_t)rs.width * y];
+                        if (depth_cmp(sh.depthTest, z, d))
+                        {
+                            shade_fragment(rs, bin, x4[k], y, z, bc[k], frags);
+                        }
+                    }
+                }
+                for (int k = 0; k < 4; ++k)
+                {
+                    bc[k] = add(bc[k], bcX);
+                    x4[k] += 4;
+                }
+            }
+            while (x4[0] < xMax);
+        }
+
+        y += rowStride;
+    }
+    while (y < bboxMaxY);
+}
+
+/* radix-sort of a flush group by primIndex when blending
+ * (SL_VertexProcessor.cpp:110-119; stable) */
+static void order_bins(std::vector<Bin>& bins, bool blending)
+{
+    if (!blending)
+    {
+        return;
+    }
+    const size_t group = 1024; /* SL_SHADER_MAX_BINNED_PRIMS (SL_Config.hpp:53) */
+    for (size_t b = 0; b < bins.size(); b += group)
+    {
+        const size_t e = std::min(bins.size(), b + group);
+        std::stable_sort(bins.begin() + b, bins.begin() + e,
+                         [](const Bin& l, const Bin& r) { return l.primIndex < r.primIndex; });
+    }
+}
+
+struct DrawItem
+{
+    slg_mesh mesh;
+    size_t numInstances;
+    size_t shaderId;
+    bool multiple; /* part of a draw_multiple group sharing one bin stream */
+};
+
+} // namespace
+
+/*-----------------------------------------------------------------------------
+ * C API
+-----------------------------------------------------------------------------*/
+extern "C" {
+
+int slo_context_create(slo_context** outCtx)
+{
+    if (!outCtx) return SLG_ERR_INVALID_ARG;
+    *outCtx = new (std::nothrow) slo_context();
+    return *outCtx ? SLG_OK : SLG_ERR_NO_MEMORY;
+}
+
+void slo_context_destroy(slo_context* ctx) { delete ctx; }
+const char* slo_last_error(const slo_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+unsigned slo_num_threads(slo_context* ctx, unsigned n)
+{
+    if (n > 0) ctx->numThreads = n;
+    return ctx->numThreads;
+}
+
+size_t slo_create_vbo(slo_context* ctx) { ctx->vbos.emplace_back(); return ctx->vbos.size() - 1; }
+
+int slo_vbo_init(slo_context* ctx, size_t id, size_t numBytes, const void* data)
+{
+    if (id >= ctx->vbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid vbo id");
+    ctx->vbos[id].bytes.assign(numBytes + 64, 0);
+    if (data) std::memcpy(ctx->vbos[id].bytes.data(), data, numBytes);
+    return SLG_OK;
+}
+
+int slo_vbo_assign(slo_context* ctx, size_t id, const void* data, size_t offset, size_t numBytes)
+{
+    if (id >= ctx->vbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid vbo id");
+    if (offset + numBytes + 64 > ctx->vbos[id].bytes.size()) return ctx->fail(SLG_ERR_INVALID_ARG, "vbo range");
+    std::memcpy(ctx->vbos[id].bytes.data() + offset, data, numBytes);
+    return SLG_OK;
+}
+
+size_t slo_create_ibo(slo_context* ctx) { ctx->ibos.emplace_back(); return ctx->ibos.size() - 1; }
+
+int slo_ibo_init(slo_context* ctx, size_t id, size_t numElements, int indexType, const void* data)
+{
+    if (id >= ctx->ibos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid ibo id");
+    const size_t ib = index_bytes(indexType);
+    if (!ib) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid index type");
+    Ibo& ibo = ctx->ibos[id];
+    ibo.type = indexType;
+    ibo.count = numElements;
+    ibo.bytes.assign(numElements * ib + 16, 0); /* padded like SL_IndexBuffer */
+    if (data) std::memcpy(ibo.bytes.data(), data, numElements * ib);
+    return SLG_OK;
+}
+
+size_t slo_create_vao(slo_context* ctx) { ctx->vaos.emplace_back(); return ctx->vaos.size() - 1; }
+
+int slo_vao_set_vertex_buffer(slo_context* ctx, size_t vao, size_t vbo)
+{
+    if (vao >= ctx->vaos.size() || vbo >= ctx->vbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid id");
+    ctx->vaos[vao].vbo = vbo;
+    return SLG_OK;
+}
+
+int slo_vao_set_index_buffer(slo_context* ctx, size_t vao, size_t ibo)
+{
+    if (vao >= ctx->vaos.size() || ibo >= ctx->ibos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid id");
+    ctx->vaos[vao].ibo = ibo;
+    return SLG_OK;
+}
+
+int slo_vao_set_binding(slo_context* ctx, size_t vao, unsigned bindId, ptrdiff_t offset, ptrdiff_t stride,
+                        unsigned numComponents, int dataType)
+{
+    if (vao >= ctx->vaos.size() || bindId >= 8) return ctx->fail(SLG_ERR_INVALID_ID, "invalid id");
+    Binding& b = ctx->vaos[vao].bindings[bindId];
+    b.offset = offset;
+    b.stride = stride;
+    b.comps = numComponents;
+    b.type = dataType;
+    return SLG_OK;
+}
+
+size_t slo_create_texture(slo_context* ctx) { ctx->textures.push_back(new Texture()); return ctx->textures.size() - 1; }
+
+int slo_texture_init(slo_context* ctx, size_t id, int colorType, uint16_t w, uint16_t h, uint16_t d)
+{
+    if (id >= ctx->textures.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
+    const size_t bpt = bytes_per_color(colorType);
+    if (!bpt || !w || !h || !d) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid texture format or size");
+    Texture& t = *ctx->textures[id];
+    t.type = colorType;
+    t.w = w; t.h = h; t.d = d;
+    t.bpt = (unsigned)bpt;
+    /* _sl_allocate_texture (SL_Texture.cpp:28-56): padded, zero-filled */
+    const size_t pw = w + (4 - (w % 4));
+    const size_t ph = h + (4 - (h % 4));
+    const size_t pd = d + (4 - (d % 4));
+    const size_t numBytes = pw * ph * pd * bpt;
+    const size_t rem = 4 * bpt;
+    t.bytes.assign(numBytes + (rem - (numBytes % rem)), 0);
+    return SLG_OK;
+}
+
+int slo_texture_set_texels(slo_context* ctx, size_t id, const void* data, size_t numBytes)
+{
+    if (id >= ctx->textures.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
+    Texture& t = *ctx->textures[id];
+    if (numBytes != (size_t)t.w * t.h * t.d * t.bpt) return ctx->fail(SLG_ERR_INVALID_ARG, "texel byte count");
+    std::memcpy(t.bytes.data(), data, numBytes);
+    return SLG_OK;
+}
+
+int slo_texture_read(slo_context* ctx, size_t id, void* dst, size_t numBytes)
+{
+    if (id >= ctx->textures.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
+    Texture& t = *ctx->textures[id];
+    if (numBytes != (size_t)t.w * t.h * t.d * t.bpt) return ctx->fail(SLG_ERR_INVALID_ARG, "texel byte count");
+    std::memcpy(dst, t.bytes.data(), numBytes);
+    return SLG_OK;
+}
+
+size_t slo_create_framebuffer(slo_context* ctx) { ctx->fbos.emplace_back(); return ctx->fbos.size() - 1; }
+
+int slo_fbo_reserve_color_buffers(slo_context* ctx, size_t fbo, unsigned n)
+{
+    if (fbo >= ctx->fbos.size() || n > 4) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo or count");
+    ctx->fbos[fbo].numColors = n;
+    return SLG_OK;
+}
+
+int slo_fbo_attach_color_buffer(slo_context* ctx, size_t fbo, unsigned index, size_t tex)
+{
+    if (fbo >= ctx->fbos.size() || tex >= ctx->textures.size() || index >= ctx->fbos[fbo].numColors)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo attachment");
+    ctx->fbos[fbo].colors[index] = tex;
+    return SLG_OK;
+}
+
+int slo_fbo_attach_depth_buffer(slo_context* ctx, size_t fbo, size_t tex)
+{
+    if (fbo >= ctx->fbos.size() || tex >= ctx->textures.size()) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo attachment");
+    if (ctx->textures[tex]->type != SLG_COLOR_R_FLOAT) return ctx->fail(SLG_ERR_INVALID_ARG, "depth must be R_FLOAT");
+    ctx->fbos[fbo].depth = tex;
+    return SLG_OK;
+}
+
+size_t slo_create_ubo(slo_context* ctx)
+{
+    Ubo* u = new Ubo();
+    std::memset(u->bytes, 0, sizeof(u->bytes));
+    ctx->ubos.push_back(u);
+    return ctx->ubos.size() - 1;
+}
+
+int slo_ubo_assign(slo_context* ctx, size_t id, const void* data, size_t numBytes)
+{
+    if (id >= ctx->ubos.size() || numBytes > 1024) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid ubo");
+    std::memcpy(ctx->ubos[id]->bytes, data, numBytes);
+    return SLG_OK;
+}
+
+/* SL_Context::create_shader validation (SL_Context.cpp:488-541) */
+size_t slo_create_shader(slo_context* ctx, const slg_vertex_shader* vs, const slg_fragment_shader* fs, size_t ubo)
+{
+    if (!vs || !fs) { ctx->err = "null shader"; return SLG_INVALID_ID; }
+    if (vs->numVaryings < fs->numVaryings || vs->numVaryings > 4 || fs->numVaryings > 4 || fs->numOutputs > 4)
+    {
+        ctx->err = "invalid varying or output count";
+        return SLG_INVALID_ID;
+    }
+    if (ubo != SLG_INVALID_ID && ubo >= ctx->ubos.size()) { ctx->err = "invalid ubo id"; return SLG_INVALID_ID; }
+    Shader s;
+    s.cull = vs->cullMode;
+    s.depthTest = fs->depthTest;
+    s.depthMask = fs->depthMask;
+    s.blend = fs->blend;
+    s.numVaryings = fs->numVaryings;
+    s.numOutputs = fs->numOutputs;
+    s.vsProgram = vs->program;
+    s.fsProgram = fs->program;
+    s.ubo = ubo;
+    ctx->shaders.push_back(s);
+    return ctx->shaders.size() - 1;
+}
+
+static void clear_color(Texture& t, const double rgba[4])
+{
+    const size_t n = (size_t)t.w * t.h * t.d;
+    if (t.type == SLG_COLOR_RGBA_8U)
+    {
+        /* color_cast<uint8_t, double> (SL_Color.cpp:148; SL_Color.hpp:625) */
+        uint8_t c[4];
+        for (int k = 0; k < 4; ++k)
+        {
+            const double v = rgba[k] * 255.0;
+            c[k] = (uint8_t)(uint32_t)((v != v || v >= 2147483648.0 || v < -2147483648.0) ? INT32_MIN : (int32_t)v);
+        }
+        for (size_t i = 0; i < n; ++i) std::memcpy(t.bytes.data() + 4 * i, c, 4);
+    }
+    else if (t.type == SLG_COLOR_RGBA_FLOAT)
+    {
+        const float c[4] = {(float)rgba[0], (float)rgba[1], (float)rgba[2], (float)rgba[3]};
+        for (size_t i = 0; i < n; ++i) std::memcpy(t.bytes.data() + 16 * i, c, 16);
+    }
+    else
+    {
+        const float c = (float)rgba[0];
+        for (size_t i = 0; i < n; ++i) std::memcpy(t.bytes.data() + 4 * i, &c, 4);
+    }
+}
+
+int slo_clear_color_buffer(slo_context* ctx, size_t fbo, unsigned att, const double rgba[4])
+{
+    if (fbo >= ctx->fbos.size() || att >= ctx->fbos[fbo].numColors) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo");
+    clear_color(*ctx->textures[ctx->fbos[fbo].colors[att]], rgba);
+    return SLG_OK;
+}
+
+int slo_clear_depth_buffer(slo_context* ctx, size_t fbo, double depth)
+{
+    if (fbo >= ctx->fbos.size() || ctx->fbos[fbo].depth == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo");
+    const double d[4] = {depth, 0, 0, 0};
+    clear_color(*ctx->textures[ctx->fbos[fbo].depth], d);
+    return SLG_OK;
+}
+
+int slo_clear_framebuffer(slo_context* ctx, size_t fbo, unsigned att, const double rgba[4], double depth)
+{
+    int r = slo_clear_color_buffer(ctx, fbo, att, rgba);
+    if (r) return r;
+    return slo_clear_depth_buffer(ctx, fbo, depth);
+}
+
+/* Runs a list of draw groups. Each group is what one SL_Context::draw,
+ * draw_instanced or draw_multiple call hands to SL_TriProcessor::execute
+ * (SL_TriProcessor.cpp:665-716): bins are produced in element order and
+ * rasterised in that order (one thread), in flush groups of 1024. With more
+ * than one host thread the vertex stage splits the element range into
+ * contiguous chunks whose bins are concatenated in order, and the raster
+ * stage splits scan-lines y % N across threads; both keep the one-thread
+ * result. */
+static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>& groups, size_t fboId)
+{
+    if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
+    const Fbo& fbo = ctx->fbos[fboId];
+    if (fbo.depth == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "framebuffer has no depth attachment");
+    Texture& depthTex = *ctx->textures[fbo.depth];
+
+    RasterState rs;
+    rs.ctx = ctx;
+    rs.depth = reinterpret_cast<float*>(depthTex.bytes.data());
+    rs.width = depthTex.w;
+    rs.numOutputs = fbo.numColors;
+    for (unsigned i = 0; i < fbo.numColors; ++i)
+    {
+        Texture& t = *ctx->textures[fbo.colors[i]];
+        rs.colors[i].bytes = t.bytes.data();
+        rs.colors[i].type = t.type;
+        rs.colors[i].w = t.w;
+    }
+
+    /* SL_TriProcessor::execute viewport set-up (SL_TriProcessor.cpp:672-675,
+     * SL_ViewportState.cpp:17-110) with the default viewport and scissor
+     * (0, 0, 65535, 65535). */
+    const float fboW = (float)depthTex.w, fboH = (float)depthTex.h;
+    float scissor[16];
+    {
+        const float invW = 1.f / fboW, invH = 1.f / fboH;
+        float sx = 0.f * invW, sy = 0.f * invH;
+        float sw = 65535.f * invW, sh = 65535.f * invH;
+        if (sx < 0.f) { sw += sx; sx = 0.f; }
+        if (sy < 0.f) { sh += sy; sy = 0.f; }
+        sw = lm_min(1.f - sx, sw);
+        sh = lm_min(1.f - sy, sh);
+        const float nm00 = 1.f / sw, nm11 = 1.f / sh;
+        const float nm30 = nm00 - 1.f, nm31 = nm11 - 1.f;
+        const float m30 = sx * (-2.f * nm00) + nm30;
+        const float m31 = sy * (-2.f * nm11) + nm31;
+        const float m[16] = {nm00, 0, 0, 0, 0, nm11, 0, 0, 0, 0, 1, 0, m30, m31, 0, 1};
+        std::memcpy(scissor, m, sizeof(m));
+    }
+    V4 viewport;
+    {
+        const float vx = lm_min(lm_max(0.f + 0.f, 0.f), fboW);
+        const float vy = lm_min(lm_max(0.f + 0.f, 0.f), fboH);
+        viewport = mk(vx, vy, lm_min(lm_min(65535.f, (0.f + 65535.f) - vx), fboW - vx),
+                      lm_min(lm_min(65535.f, (0.f + 65535.f) - vy), fboH - vy));
+    }
+
+    uint64_t totalBins = 0, totalFrags = 0;
+    const unsigned nthreads = std::max(1u, ctx->numThreads);
+
+    for (const std::vector<DrawItem>& group : groups)
+    {
+        /* one bin stream per group, in the order SL_TriProcessor::execute walks it */
+        std::vector<DrawState> states;
+        rs.shaders.clear();
+        rs.envs.clear();
+        for (size_t d = 0; d < group.size(); ++d)
+        {
+            const DrawItem& it = group[d];
+            if (it.shaderId >= ctx->shaders.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid shader id");
+            if (it.mesh.vaoId >= ctx->vaos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid vao id");
+            const Shader& sh = ctx->shaders[it.shaderId];
+            const Vao& vao = ctx->vaos[it.mesh.vaoId];
+            if (vao.vbo == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "vao has no vertex buffer");
+            DrawState ds;
+            ds.ctx = ctx;
+            ds.shader = &sh;
+            ds.env.ctx = ctx;
+            ds.env.vboBytes = ctx->vbos[vao.vbo].bytes.data();
+            ds.env.b0 = vao.bindings[0];
+            ds.env.ubo = sh.ubo != SLG_INVALID_ID ? ctx->ubos[sh.ubo]->bytes : nullptr;
+            std::memcpy(ds.scissor, scissor, sizeof(scissor));
+            ds.viewport = viewport;
+            ds.numVaryings = sh.numVaryings;
+            ds.drawIndex = (uint32_t)d;
+            states.push_back(ds);
+            rs.shaders.push_back(&sh);
+            rs.envs.push_back(ds.env);
+        }
+
+        /* enumerate (draw, instance) work units in execution order */
+        struct Unit { size_t draw, instance; };
+        std::vector<Unit> units;
+        for (size_t d = 0; d < group.size(); ++d)
+        {
+            for (size_t inst = 0; inst < std::max<size_t>(1, group[d].numInstances); ++inst)
+            {
+                units.push_back({d, inst});
+            }
+        }
+
+        const bool blending = group.empty() ? false : (ctx->shaders[group[0].shaderId].blend != SLG_BLEND_OFF);
+        std::vector<Bin> bins;
+
+        for (const Unit& u : units)
+        {
+            const DrawItem& it = group[u.draw];
+            const Vao& vao = ctx->vaos[it.mesh.vaoId];
+            const bool indexed = (it.mesh.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES);
+            const Ibo* ibo = (indexed && vao.ibo != SLG_INVALID_ID) ? &ctx->ibos[vao.ibo] : nullptr;
+            if (indexed && !ibo) return ctx->fail(SLG_ERR_INVALID_ARG, "indexed draw without index buffer");
+            const size_t begin = it.mesh.elementBegin, end = it.mesh.elementEnd;
+            const size_t numTris = (end > begin) ? (end - begin + 2) / 3 : 0;
+
+            if (nthreads == 1 || numTris < 4096)
+            {
+                process_verts(states[u.draw], ibo, it.mesh, u.instance, begin, end, bins);
+            }
+            else
+            {
+                std::vector<std::vector<Bin>> parts(nthreads);
+                std::vector<std::thread> pool;
+                const size_t per = (numTris + nthreads - 1) / nthreads;
+                for (unsigned t = 0; t < nthreads; ++t)
+                {
+                    const size_t f = begin + std::min(numTris, per * t) * 3;
+                    const size_t l = std::min(end, begin + std::min(numTris, per * (t + 1)) * 3);
+                    pool.emplace_back([&, t, f, l]() { process_verts(states[u.draw], ibo, it.mesh, u.instance, f, l, parts[t]); });
+                }
+                for (std::thread& th : pool) th.join();
+                for (auto& p : parts) bins.insert(bins.end(), p.begin(), p.end());
+            }
+        }
+
+        order_bins(bins, blending);
+        totalBins += bins.size();
+
+        if (nthreads == 1)
+        {
+            for (const Bin& b : bins) raster_bin(rs, b, 1, 0, totalFrags);
+        }
+        else
+        {
+            std::vector<uint64_t> frags(nthreads, 0);
+            std::vector<std::thread> pool;
+            for (unsigned t = 0; t < nthreads; ++t)
+            {
+                pool.emplace_back([&, t]() {
+                    for (const Bin& b : bins) raster_bin(rs, b, (int)nthreads, (int)t, frags[t]);
+                });
+            }
+            for (std::thread& th : pool) th.join();
+            for (uint64_t f : frags) totalFrags += f;
+        }
+    }
+
+    ctx->lastBins = totalBins;
+    ctx->lastFrags = totalFrags;
+    return SLG_OK;
+}
+
+static bool valid_tri_mesh(const slg_mesh* m)
+{
+    return m && (m->mode == SLG_RENDER_MODE_TRIANGLES || m->mode == SLG_RENDER_MODE_INDEXED_TRIANGLES);
+}
+
+int slo_draw(slo_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId)
+{
+    return slo_draw_instanced(ctx, m, 1, shaderId, fboId);
+}
+
+int slo_draw_instanced(slo_context* ctx, const slg_mesh* m, size_t numInstances, size_t shaderId, size_t fboId)
+{
+    if (!valid_tri_mesh(m)) return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle render modes are supported");
+    std::vector<std::vector<DrawItem>> groups(1);
+    groups[0].push_back({*m, numInstances, shaderId, false});
+    return run_draws(ctx, groups, fboId);
+}
+
+int slo_draw_multiple(slo_context* ctx, const slg_mesh* meshes, size_t numMeshes, size_t shaderId, size_t fboId)
+{
+    if (!meshes || !numMeshes) return SLG_OK;
+    std::vector<std::vector<DrawItem>> groups(1);
+    for (size_t i = 0; i < numMeshes; ++i)
+    {
+        if (!valid_tri_mesh(&meshes[i])) return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle render modes are supported");
+        groups[0].push_back({meshes[i], 1, shaderId, true});
+    }
+    return run_draws(ctx, groups, fboId);
+}
+
+int slo_draw_batch(slo_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, size_t fboId)
+{
+    std::vector<std::vector<DrawItem>> groups;
+    for (size_t i = 0; i < numCmds; ++i)
+    {
+        if (!valid_tri_mesh(&cmds[i].mesh)) return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle render modes are supported");
+        groups.push_back({{cmds[i].mesh, cmds[i].numInstances, cmds[i].shaderId, false}});
+    }
+    return run_draws(ctx, groups, fboId);
+}
+
+int slo_finish(slo_context*) { return SLG_OK; }
+
+void slo_last_stats(const slo_context* ctx, uint64_t* numBins, uint64_t* numFragments)
+{
+    if (numBins) *numBins = ctx->lastBins;
+    if (numFragments) *numFragments = ctx->lastFrags;
+}
+
+} // extern "C"

@@ -1,0 +1,305 @@
+"""ctypes binding of the draw-path C ABI (include/slg.h), shaped like SoftLight's
+SL_Context (softlight/include/softlight/SL_Context.hpp:59-306).
+
+`SLContext` wraps any library that exports the slg.h entry points under a
+given symbol prefix. The product library is softlight_gb300/libslg.so
+(prefix "slg_"); `Context()` opens it and raises if it is missing, so there is
+no silent CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libslg.so")
+
+INVALID_ID = (1 << 64) - 1
+
+# enums (values of include/slg.h, which mirror the reference's)
+VERTEX_DATA_BYTE, VERTEX_DATA_SHORT, VERTEX_DATA_INT, VERTEX_DATA_LONG, VERTEX_DATA_FLOAT = 0, 1, 2, 3, 4
+RENDER_MODE_TRIANGLES, RENDER_MODE_INDEXED_TRIANGLES = 0x10, 0x30
+CULL_BACK_FACE, CULL_FRONT_FACE, CULL_OFF = 0, 1, 2
+DEPTH_TEST_OFF, DEPTH_TEST_LESS_THAN, DEPTH_TEST_LESS_EQUAL, DEPTH_TEST_GREATER_THAN = 0, 1, 2, 3
+DEPTH_TEST_GREATER_EQUAL, DEPTH_TEST_EQUAL, DEPTH_TEST_NOT_EQUAL = 4, 5, 6
+DEPTH_MASK_OFF, DEPTH_MASK_ON = 0, 1
+BLEND_OFF, BLEND_ALPHA, BLEND_PREMULTIPLED_ALPHA, BLEND_ADDITIVE, BLEND_SCREEN = 0, 1, 2, 3, 4
+COLOR_R_FLOAT, COLOR_RGBA_8U, COLOR_RGBA_FLOAT = 5, 21, 26
+PROGRAM_LAMBERT_TEX, PROGRAM_BLINN_PHONG_INST, PROGRAM_VCOLOR_TEX_ALPHA = 1, 2, 3
+PROGRAM_VCOLOR_TEXF, PROGRAM_FLAT_COLOR = 4, 5
+
+BYTES_PER_COLOR = {COLOR_R_FLOAT: 4, COLOR_RGBA_8U: 4, COLOR_RGBA_FLOAT: 16}
+
+
+class Mesh(C.Structure):
+    """SL_Mesh (softlight/include/softlight/SL_Mesh.hpp:30-39)."""
+    _fields_ = [("vaoId", C.c_size_t), ("elementBegin", C.c_size_t), ("elementEnd", C.c_size_t),
+                ("mode", C.c_uint32), ("materialId", C.c_uint32)]
+
+
+class VertexShader(C.Structure):
+    """SL_VertexShader (softlight/include/softlight/SL_Shader.hpp:58)."""
+    _fields_ = [("numVaryings", C.c_uint8), ("cullMode", C.c_uint8), ("program", C.c_uint32)]
+
+
+class FragmentShader(C.Structure):
+    """SL_FragmentShader (softlight/include/softlight/SL_Shader.hpp:89)."""
+    _fields_ = [("numVaryings", C.c_uint8), ("numOutputs", C.c_uint8), ("blend", C.c_uint8),
+                ("depthTest", C.c_uint8), ("depthMask", C.c_uint8), ("program", C.c_uint32)]
+
+
+class DrawCmd(C.Structure):
+    _fields_ = [("mesh", Mesh), ("numInstances", C.c_size_t), ("shaderId", C.c_size_t)]
+
+
+class SLError(RuntimeError):
+    pass
+
+
+# (name, restype, argtypes) for every entry point of include/slg.h
+_SIGNATURES = [
+    ("context_create", C.c_int, [C.POINTER(C.c_void_p)]),
+    ("context_destroy", None, [C.c_void_p]),
+    ("last_error", C.c_char_p, [C.c_void_p]),
+    ("num_threads", C.c_uint, [C.c_void_p, C.c_uint]),
+    ("create_vbo", C.c_size_t, [C.c_void_p]),
+    ("vbo_init", C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p]),
+    ("vbo_assign", C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_size_t]),
+    ("create_ibo", C.c_size_t, [C.c_void_p]),
+    ("ibo_init", C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t, C.c_int, C.c_void_p]),
+    ("create_vao", C.c_size_t, [C.c_void_p]),
+    ("vao_set_vertex_buffer", C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t]),
+    ("vao_set_index_buffer", C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t]),
+    ("vao_set_binding", C.c_int, [C.c_void_p, C.c_size_t, C.c_uint, C.c_ssize_t, C.c_ssize_t, C.c_uint, C.c_int]),
+    ("create_texture", C.c_size_t, [C.c_void_p]),
+    ("texture_init", C.c_int, [C.c_void_p, C.c_size_t, C.c_int, C.c_uint16, C.c_uint16, C.c_uint16]),
+    ("texture_set_texels", C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t]),
+    ("texture_read", C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t]),
+    ("create_framebuffer", C.c_size_t, [C.c_void_p]),
+    ("fbo_reserve_color_buffers", C.c_int, [C.c_void_p, C.c_size_t, C.c_uint]),
+    ("fbo_attach_color_buffer", C.c_int, [C.c_void_p, C.c_size_t, C.c_uint, C.c_size_t]),
+    ("fbo_attach_depth_buffer", C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t]),
+    ("create_ubo", C.c_size_t, [C.c_void_p]),
+    ("ubo_assign", C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t]),
+    ("create_shader", C.c_size_t, [C.c_void_p, C.POINTER(VertexShader), C.POINTER(FragmentShader), C.c_size_t]),
+    ("clear_framebuffer", C.c_int, [C.c_void_p, C.c_size_t, C.c_uint, C.POINTER(C.c_double), C.c_double]),
+    ("clear_color_buffer", C.c_int, [C.c_void_p, C.c_size_t, C.c_uint, C.POINTER(C.c_double)]),
+    ("clear_depth_buffer", C.c_int, [C.c_void_p, C.c_size_t, C.c_double]),
+    ("draw", C.c_int, [C.c_void_p, C.POINTER(Mesh), C.c_size_t, C.c_size_t]),
+    ("draw_instanced", C.c_int, [C.c_void_p, C.POINTER(Mesh), C.c_size_t, C.c_size_t, C.c_size_t]),
+    ("draw_multiple", C.c_int, [C.c_void_p, C.POINTER(Mesh), C.c_size_t, C.c_size_t, C.c_size_t]),
+    ("draw_batch", C.c_int, [C.c_void_p, C.POINTER(DrawCmd), C.c_size_t, C.c_size_t]),
+    ("finish", C.c_int, [C.c_void_p]),
+]
+
+# GPU-only entry points (include/slg.h, "GPU-only controls")
+_GPU_SIGNATURES = [
+    ("context_stream", C.c_void_p, [C.c_void_p]),
+    ("set_tile_size", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    ("profile_stages", C.c_int, [C.c_void_p, C.c_int]),
+    ("stage_times", C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+]
+
+
+def exported_symbols(prefix="slg_", gpu=True):
+    """Names of the C ABI entry points a conforming library must export."""
+    sigs = _SIGNATURES + (_GPU_SIGNATURES if gpu else [])
+    return [prefix + n for n, _, _ in sigs]
+
+
+_LIB_CACHE = {}
+
+
+def open_library(path, prefix, gpu):
+    """dlopen a library exporting the slg.h ABI under `prefix` and bind its
+    signatures. Raises OSError if the file is missing."""
+    key = (os.path.realpath(path), prefix)
+    if key in _LIB_CACHE:
+        return _LIB_CACHE[key]
+    if not os.path.exists(path):
+        raise OSError(f"draw-path library not found: {path} (run softlight_gb300.build.build())")
+    lib = C.CDLL(path)
+    for name, res, args in _SIGNATURES + (_GPU_SIGNATURES if gpu else []):
+        fn = getattr(lib, prefix + name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB_CACHE[key] = lib
+    return lib
+
+
+class SLContext:
+    """SL_Context-shaped wrapper over one context of an slg.h library."""
+
+    def __init__(self, lib, prefix="slg_", gpu=True):
+        self._lib = lib
+        self._p = prefix
+        self.gpu = gpu
+        h = C.c_void_p()
+        rc = self._fn("context_create")(C.byref(h))
+        if rc != 0:
+            raise SLError(f"context_create failed ({rc})")
+        self._h = h
+        self._keep = []
+
+    # -- plumbing -----------------------------------------------------------
+    def _fn(self, name):
+        return getattr(self._lib, self._p + name)
+
+    def _call(self, name, *args):
+        rc = self._fn(name)(self._h, *args)
+        if rc != 0:
+            raise SLError(f"{self._p}{name} failed ({rc}): {self.last_error()}")
+        return rc
+
+    def _id(self, name, *args):
+        r = self._fn(name)(self._h, *args)
+        if r == INVALID_ID:
+            raise SLError(f"{self._p}{name} failed: {self.last_error()}")
+        return r
+
+    def last_error(self):
+        s = self._fn("last_error")(self._h)
+        return s.decode() if s else ""
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._fn("context_destroy")(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- resources ----------------------------------------------------------
+    def num_threads(self, n=0):
+        return self._fn("num_threads")(self._h, n)
+
+    def create_vbo(self):
+        return self._id("create_vbo")
+
+    def vbo_init(self, vbo, data):
+        a = np.ascontiguousarray(data)
+        self._call("vbo_init", vbo, a.nbytes, a.ctypes.data_as(C.c_void_p))
+
+    def vbo_assign(self, vbo, data, offset=0):
+        a = np.ascontiguousarray(data)
+        self._call("vbo_assign", vbo, a.ctypes.data_as(C.c_void_p), offset, a.nbytes)
+
+    def create_ibo(self):
+        return self._id("create_ibo")
+
+    def ibo_init(self, ibo, indices):
+        a = np.ascontiguousarray(indices)
+        t = {np.dtype(np.uint8): VERTEX_DATA_BYTE, np.dtype(np.uint16): VERTEX_DATA_SHORT,
+             np.dtype(np.uint32): VERTEX_DATA_INT}[a.dtype]
+        self._call("ibo_init", ibo, a.size, t, a.ctypes.data_as(C.c_void_p))
+
+    def create_vao(self):
+        return self._id("create_vao")
+
+    def vao_set_vertex_buffer(self, vao, vbo):
+        self._call("vao_set_vertex_buffer", vao, vbo)
+
+    def vao_set_index_buffer(self, vao, ibo):
+        self._call("vao_set_index_buffer", vao, ibo)
+
+    def vao_set_binding(self, vao, bind_id, offset, stride, num_components=3, data_type=VERTEX_DATA_FLOAT):
+        self._call("vao_set_binding", vao, bind_id, offset, stride, num_components, data_type)
+
+    def create_texture(self):
+        return self._id("create_texture")
+
+    def texture_init(self, tex, color_type, w, h, d=1):
+        self._call("texture_init", tex, color_type, w, h, d)
+
+    def texture_set_texels(self, tex, data):
+        a = np.ascontiguousarray(data)
+        self._call("texture_set_texels", tex, a.ctypes.data_as(C.c_void_p), a.nbytes)
+
+    def texture_read(self, tex, shape, dtype, out=None):
+        """Copy a texture's texels into a numpy array of `shape`/`dtype`."""
+        if out is None:
+            out = np.empty(shape, dtype=dtype)
+        self._call("texture_read", tex, out.ctypes.data_as(C.c_void_p), out.nbytes)
+        return out
+
+    def create_framebuffer(self):
+        return self._id("create_framebuffer")
+
+    def fbo_reserve_color_buffers(self, fbo, n):
+        self._call("fbo_reserve_color_buffers", fbo, n)
+
+    def fbo_attach_color_buffer(self, fbo, index, tex):
+        self._call("fbo_attach_color_buffer", fbo, index, tex)
+
+    def fbo_attach_depth_buffer(self, fbo, tex):
+        self._call("fbo_attach_depth_buffer", fbo, tex)
+
+    def create_ubo(self):
+        return self._id("create_ubo")
+
+    def ubo_assign(self, ubo, data):
+        b = bytes(data) if not isinstance(data, np.ndarray) else np.ascontiguousarray(data).tobytes()
+        buf = C.create_string_buffer(b, len(b))
+        self._call("ubo_assign", ubo, C.cast(buf, C.c_void_p), len(b))
+
+    def create_shader(self, vs, fs, ubo=INVALID_ID):
+        return self._id("create_shader", C.byref(vs), C.byref(fs), ubo)
+
+    # -- frame --------------------------------------------------------------
+    def clear_framebuffer(self, fbo, attachment, rgba, depth):
+        c = (C.c_double * 4)(*rgba)
+        self._call("clear_framebuffer", fbo, attachment, c, depth)
+
+    def clear_color_buffer(self, fbo, attachment, rgba):
+        c = (C.c_double * 4)(*rgba)
+        self._call("clear_color_buffer", fbo, attachment, c)
+
+    def clear_depth_buffer(self, fbo, depth):
+        self._call("clear_depth_buffer", fbo, depth)
+
+    def draw(self, mesh, shader, fbo):
+        self._call("draw", C.byref(mesh), shader, fbo)
+
+    def draw_instanced(self, mesh, num_instances, shader, fbo):
+        self._call("draw_instanced", C.byref(mesh), num_instances, shader, fbo)
+
+    def draw_multiple(self, meshes, shader, fbo):
+        arr = (Mesh * len(meshes))(*meshes)
+        self._call("draw_multiple", arr, len(meshes), shader, fbo)
+
+    def draw_batch(self, cmds, fbo):
+        arr = (DrawCmd * len(cmds))(*cmds)
+        self._call("draw_batch", arr, len(cmds), fbo)
+
+    def finish(self):
+        self._call("finish")
+
+    # -- GPU-only -----------------------------------------------------------
+    def stream_handle(self):
+        return self._fn("context_stream")(self._h)
+
+    def set_tile_size(self, w, h):
+        self._call("set_tile_size", w, h)
+
+    def profile_stages(self, enable=True):
+        self._call("profile_stages", 1 if enable else 0)
+
+    def stage_times(self):
+        ms = (C.c_float * 4)()
+        self._call("stage_times", ms)
+        return list(ms)
+
+
+def Context():
+    """A context of the GPU library; raises OSError when libslg.so is absent."""
+    lib = open_library(LIB_PATH, "slg_", gpu=True)
+    return SLContext(lib, "slg_", gpu=True)

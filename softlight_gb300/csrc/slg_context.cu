@@ -1,0 +1,818 @@
+/*
+ * slg_context.cu - host side of the GB300 draw path: the SL_Context-shaped
+ * resource model and the C ABI declared in include/slg.h.
+ *
+ * The context owns device mirrors of every resource the reference's
+ * SL_Context owns (softlight/include/softlight/SL_Context.hpp:66-82):
+ * vertex/index/uniform buffers and textures live in HBM from init/assign
+ * until the context is destroyed. Draws enqueue kernels on the context's
+ * stream and return; results become visible to the host at slg_finish or
+ * slg_texture_read, which also report any device-side error of the queued
+ * draws.
+ */
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/slg.h"
+#include "slg_device.cuh"
+#include "slg_kernels.cuh"
+
+using slg::DrawDesc;
+using slg::Frame;
+using slg::TexView;
+
+namespace
+{
+
+struct DevBuffer
+{
+    void*  ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct Vbo { DevBuffer buf; size_t size = 0; };
+struct Ibo { DevBuffer buf; int type = SLG_VERTEX_DATA_INVALID; size_t count = 0; };
+struct Binding { ptrdiff_t offset = 0, stride = 0; unsigned comps = 0; int type = 0; };
+struct Vao { size_t vbo = SLG_INVALID_ID, ibo = SLG_INVALID_ID; Binding bindings[8]; };
+struct Texture { DevBuffer buf; int type = -1; uint16_t w = 0, h = 0, d = 0; unsigned bpt = 0; };
+struct Fbo
+{
+    unsigned numColors = 0;
+    size_t colors[4] = {SLG_INVALID_ID, SLG_INVALID_ID, SLG_INVALID_ID, SLG_INVALID_ID};
+    size_t depth = SLG_INVALID_ID;
+};
+struct Ubo { DevBuffer buf; };
+struct Shader
+{
+    uint8_t cull, depthTest, depthMask, blend, numVaryings, numOutputs;
+    uint32_t vsProgram, fsProgram;
+    size_t ubo;
+};
+
+size_t bytes_per_color(int type)
+{
+    switch (type)
+    {
+        case SLG_COLOR_R_FLOAT: return 4;
+        case SLG_COLOR_RGBA_8U: return 4;
+        case SLG_COLOR_RGBA_FLOAT: return 16;
+        default: return 0;
+    }
+}
+
+size_t index_bytes(int type)
+{
+    switch (type)
+    {
+        case SLG_VERTEX_DATA_BYTE: return 1;
+        case SLG_VERTEX_DATA_SHORT: return 2;
+        case SLG_VERTEX_DATA_INT: return 4;
+        default: return 0;
+    }
+}
+
+bool valid_program(uint32_t p) { return p >= SLG_PROGRAM_LAMBERT_TEX && p <= SLG_PROGRAM_FLAT_COLOR; }
+
+constexpr size_t kDescRing = 4096;
+constexpr uint64_t kMaxSlots = (1ull << 29) - 1; /* keys are slot << 3 | sub in 32 bits */
+
+} // namespace
+
+struct slg_context
+{
+    std::string err;
+    cudaStream_t stream = nullptr;
+    unsigned numThreads = 1;
+    int tileW = 32, tileH = 32;
+    int keyCap = 16384;
+
+    std::vector<Vbo> vbos;
+    std::vector<Ibo> ibos;
+    std::vector<Vao> vaos;
+    std::vector<Texture> textures;
+    std::vector<Fbo> fbos;
+    std::vector<Ubo> ubos;
+    std::vector<Shader> shaders;
+
+    /* resource tables visible to device programs */
+    DevBuffer texTable, bufTable;
+    bool tablesDirty = true;
+
+    /* scratch */
+    DevBuffer records, varyings, slotInfo, slotOvf, ovfCount;
+    DevBuffer tileCount, tileOffset, tileCursor, entries, status;
+    uint64_t slotCap = 0, ovfCap = 0, tileCap = 0, entryCap = 0;
+
+    /* draw descriptors: pinned host ring mirrored to a device ring */
+    DrawDesc* hostDescs = nullptr;
+    uint64_t* hostStarts = nullptr;
+    DevBuffer devDescs, devStarts;
+    size_t descHead = 0;
+
+    int32_t* hostStatus = nullptr;
+    cudaEvent_t stageEvents[5] = {};
+    bool profileStages = false;
+
+    int fail(int code, const std::string& msg) { err = msg; return code; }
+    size_t fail_id(const std::string& msg) { err = msg; return SLG_INVALID_ID; }
+
+    int cuda_fail(cudaError_t e, const char* what)
+    {
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return SLG_ERR_CUDA;
+    }
+};
+
+namespace
+{
+
+int dev_alloc(slg_context* ctx, DevBuffer& b, size_t bytes, bool zero)
+{
+    if (b.bytes >= bytes && b.ptr)
+    {
+        if (zero)
+        {
+            cudaError_t e = cudaMemsetAsync(b.ptr, 0, bytes, ctx->stream);
+            if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaMemsetAsync");
+        }
+        return SLG_OK;
+    }
+    if (b.ptr)
+    {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(b.ptr);
+        b.ptr = nullptr;
+        b.bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&b.ptr, bytes ? bytes : 16);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaMalloc");
+    b.bytes = bytes;
+    if (zero)
+    {
+        e = cudaMemsetAsync(b.ptr, 0, bytes, ctx->stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaMemsetAsync");
+    }
+    return SLG_OK;
+}
+
+void dev_free(DevBuffer& b)
+{
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+}
+
+int upload_tables(slg_context* ctx)
+{
+    if (!ctx->tablesDirty) return SLG_OK;
+    std::vector<TexView> tex(std::max<size_t>(1, ctx->textures.size()));
+    for (size_t i = 0; i < ctx->textures.size(); ++i)
+    {
+        const Texture& t = ctx->textures[i];
+        tex[i].texels = static_cast<const uint8_t*>(t.buf.ptr);
+        tex[i].w = t.w;
+        tex[i].h = t.h;
+        tex[i].d = t.d;
+        tex[i].type = t.type;
+    }
+    std::vector<const uint8_t*> bufs(std::max<size_t>(1, ctx->vbos.size()), nullptr);
+    for (size_t i = 0; i < ctx->vbos.size(); ++i) bufs[i] = static_cast<const uint8_t*>(ctx->vbos[i].buf.ptr);
+
+    int r = dev_alloc(ctx, ctx->texTable, tex.size() * sizeof(TexView), false);
+    if (r) return r;
+    r = dev_alloc(ctx, ctx->bufTable, bufs.size() * sizeof(void*), false);
+    if (r) return r;
+    cudaStreamSynchronize(ctx->stream);
+    cudaError_t e = cudaMemcpy(ctx->texTable.ptr, tex.data(), tex.size() * sizeof(TexView), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(ctx->bufTable.ptr, bufs.data(), bufs.size() * sizeof(void*), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "table upload");
+    ctx->tablesDirty = false;
+    return SLG_OK;
+}
+
+int ensure_scratch(slg_context* ctx, uint64_t numSlots, uint64_t numTiles)
+{
+    int r;
+    if (numSlots > ctx->slotCap)
+    {
+        const uint64_t cap = std::max<uint64_t>(numSlots, 1u << 16);
+        const uint64_t ovf = std::max<uint64_t>(std::min<uint64_t>(7 * cap, 1u << 22), cap / 2);
+        const uint64_t recs = cap + ovf;
+        if ((r = dev_alloc(ctx, ctx->records, recs * slg::kRecordVec4 * sizeof(float4), false))) return r;
+        if ((r = dev_alloc(ctx, ctx->varyings, recs * slg::kVaryingVec4 * sizeof(float4), false))) return r;
+        if ((r = dev_alloc(ctx, ctx->slotInfo, cap * sizeof(uint32_t), false))) return r;
+        if ((r = dev_alloc(ctx, ctx->slotOvf, cap * sizeof(uint32_t), false))) return r;
+        ctx->slotCap = cap;
+        ctx->ovfCap = ovf;
+        const uint64_t wantEntries = std::max<uint64_t>(8 * cap, 32u << 20);
+        if (wantEntries > ctx->entryCap)
+        {
+            if ((r = dev_alloc(ctx, ctx->entries, wantEntries * sizeof(uint32_t), false))) return r;
+            ctx->entryCap = wantEntries;
+        }
+    }
+    if (!ctx->ovfCount.ptr)
+    {
+        if ((r = dev_alloc(ctx, ctx->ovfCount, sizeof(uint32_t), true))) return r;
+        if ((r = dev_alloc(ctx, ctx->status, 4 * sizeof(int32_t), true))) return r;
+    }
+    if (numTiles > ctx->tileCap)
+    {
+        const uint64_t cap = numTiles;
+        if ((r = dev_alloc(ctx, ctx->tileCount, cap * sizeof(uint32_t), true))) return r;
+        if ((r = dev_alloc(ctx, ctx->tileOffset, (cap + 1) * sizeof(uint32_t), false))) return r;
+        if ((r = dev_alloc(ctx, ctx->tileCursor, cap * sizeof(uint32_t), false))) return r;
+        ctx->tileCap = cap;
+    }
+    return SLG_OK;
+}
+
+/* Reads and clears the device status word; grows buffers that overflowed. */
+int check_status(slg_context* ctx)
+{
+    if (!ctx->status.ptr) return SLG_OK;
+    cudaError_t e = cudaMemcpyAsync(ctx->hostStatus, ctx->status.ptr, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "device status read");
+    const int32_t bits = ctx->hostStatus[0];
+    if (!bits) return SLG_OK;
+
+    const int32_t zero[4] = {0, 0, 0, 0};
+    cudaMemcpy(ctx->status.ptr, zero, sizeof(zero), cudaMemcpyHostToDevice);
+    std::string msg = "device-side overflow:";
+    if (bits & slg::kStatusEntryOverflow)
+    {
+        const uint64_t want = (uint64_t)ctx->hostStatus[1] * 2;
+        if (want > ctx->entryCap && dev_alloc(ctx, ctx->entries, want * sizeof(uint32_t), false) == SLG_OK) ctx->entryCap = want;
+        msg += " tile entries";
+    }
+    if (bits & slg::kStatusOvfOverflow)
+    {
+        msg += " clipped-triangle records";
+        ctx->slotCap = 0; /* reallocate with a larger overflow region on the next draw */
+        const uint64_t want = (uint64_t)ctx->hostStatus[2];
+        (void)want;
+    }
+    if (bits & slg::kStatusTileOverflow)
+    {
+        msg += " triangles per tile";
+    }
+    msg += " (the affected draws were skipped; buffers have been grown)";
+    return ctx->fail(SLG_ERR_OVERFLOW, msg);
+}
+
+int color_value(int type, const double rgba[4], uint32_t out[4])
+{
+    std::memset(out, 0, 4 * sizeof(uint32_t));
+    if (type == SLG_COLOR_RGBA_8U)
+    {
+        uint32_t packed = 0;
+        for (int k = 0; k < 4; ++k)
+        {
+            const double v = rgba[k] * 255.0;
+            const int32_t iv = (v != v || v >= 2147483648.0 || v < -2147483648.0) ? INT32_MIN : (int32_t)v;
+            packed |= ((uint32_t)iv & 0xFFu) << (8 * k);
+        }
+        out[0] = packed;
+    }
+    else if (type == SLG_COLOR_RGBA_FLOAT)
+    {
+        for (int k = 0; k < 4; ++k)
+        {
+            const float f = (float)rgba[k];
+            std::memcpy(&out[k], &f, 4);
+        }
+    }
+    else if (type == SLG_COLOR_R_FLOAT)
+    {
+        const float f = (float)rgba[0];
+        std::memcpy(&out[0], &f, 4);
+    }
+    else
+    {
+        return -1;
+    }
+    return 0;
+}
+
+int clear_texture(slg_context* ctx, size_t texId, const double rgba[4])
+{
+    const Texture& t = ctx->textures[texId];
+    uint32_t v[4];
+    if (color_value(t.type, rgba, v)) return ctx->fail(SLG_ERR_INVALID_ARG, "unsupported clear format");
+    cudaError_t e = slg::launch_clear(static_cast<uint8_t*>(t.buf.ptr), (size_t)t.w * t.h * t.d, (int)t.bpt, v, ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "clear launch");
+    return SLG_OK;
+}
+
+/* The viewport and scissor matrix of SL_TriProcessor::execute with the
+ * default SL_ViewportState (softlight/src/SL_TriProcessor.cpp:672-675,
+ * softlight/src/SL_ViewportState.cpp:17-110); compiled with
+ * -ffp-contract=off like the rest of the host code. */
+void viewport_setup(float fboW, float fboH, float scissor[16], float viewport[4])
+{
+    auto mn = [](float a, float b) { return (b < a) ? b : a; };
+    auto mx = [](float a, float b) { return (a < b) ? b : a; };
+    const float invW = 1.f / fboW, invH = 1.f / fboH;
+    float sx = 0.f * invW, sy = 0.f * invH;
+    float sw = 65535.f * invW, sh = 65535.f * invH;
+    if (sx < 0.f) { sw += sx; sx = 0.f; }
+    if (sy < 0.f) { sh += sy; sy = 0.f; }
+    sw = mn(1.f - sx, sw);
+    sh = mn(1.f - sy, sh);
+    const float nm00 = 1.f / sw, nm11 = 1.f / sh;
+    const float nm30 = nm00 - 1.f, nm31 = nm11 - 1.f;
+    const float m30 = sx * (-2.f * nm00) + nm30;
+    const float m31 = sy * (-2.f * nm11) + nm31;
+    const float m[16] = {nm00, 0, 0, 0, 0, nm11, 0, 0, 0, 0, 1, 0, m30, m31, 0, 1};
+    std::memcpy(scissor, m, sizeof(m));
+    const float vx = mn(mx(0.f + 0.f, 0.f), fboW);
+    const float vy = mn(mx(0.f + 0.f, 0.f), fboH);
+    viewport[0] = vx;
+    viewport[1] = vy;
+    viewport[2] = mn(mn(65535.f, (0.f + 65535.f) - vx), fboW - vx);
+    viewport[3] = mn(mn(65535.f, (0.f + 65535.f) - vy), fboH - vy);
+}
+
+struct DrawRequest
+{
+    slg_mesh mesh;
+    size_t numInstances;
+    size_t shaderId;
+    uint64_t primBase;
+};
+
+int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, DrawDesc& d, uint64_t& numSlots)
+{
+    const slg_mesh& m = req.mesh;
+    if (req.shaderId >= ctx->shaders.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid shader id");
+    if (m.vaoId >= ctx->vaos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid vao id");
+    if (m.mode != SLG_RENDER_MODE_TRIANGLES && m.mode != SLG_RENDER_MODE_INDEXED_TRIANGLES)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle render modes are supported");
+    const Shader& sh = ctx->shaders[req.shaderId];
+    const Vao& vao = ctx->vaos[m.vaoId];
+    if (vao.vbo == SLG_INVALID_ID || !ctx->vbos[vao.vbo].buf.ptr) return ctx->fail(SLG_ERR_INVALID_ARG, "vao has no vertex buffer");
+    const bool indexed = (m.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES);
+    if (indexed && (vao.ibo == SLG_INVALID_ID || !ctx->ibos[vao.ibo].buf.ptr))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "indexed draw without index buffer");
+
+    std::memset(&d, 0, sizeof(d));
+    d.vbo = static_cast<const uint8_t*>(ctx->vbos[vao.vbo].buf.ptr);
+    d.ibo = indexed ? static_cast<const uint8_t*>(ctx->ibos[vao.ibo].buf.ptr) : nullptr;
+    d.ubo = (sh.ubo != SLG_INVALID_ID) ? static_cast<const uint8_t*>(ctx->ubos[sh.ubo].buf.ptr) : nullptr;
+    d.b0Offset = vao.bindings[0].offset;
+    d.b0Stride = vao.bindings[0].stride;
+    d.elementBegin = m.elementBegin;
+    d.numElements = (m.elementEnd > m.elementBegin) ? (m.elementEnd - m.elementBegin) : 0;
+    d.numTris = (d.numElements + 2) / 3;
+    d.numInstances = std::max<size_t>(1, req.numInstances);
+    d.slotBase = slotBase;
+    d.primBase = req.primBase;
+    d.indexType = indexed ? ctx->ibos[vao.ibo].type : -1;
+    d.vsProgram = sh.vsProgram;
+    d.fsProgram = sh.fsProgram;
+    d.cull = sh.cull;
+    d.numVaryings = sh.numVaryings;
+    d.depthTest = sh.depthTest;
+    d.depthMask = sh.depthMask;
+    d.blend = sh.blend;
+    d.numOutputs = sh.numOutputs;
+    numSlots = d.numTris * d.numInstances;
+    if (req.numInstances == 0) numSlots = 0;
+    return SLG_OK;
+}
+
+/* One launch of the pipeline over a sequence of draws that share a
+ * framebuffer. The result equals issuing the draws one after another. */
+int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fboId)
+{
+    if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
+    const Fbo& fbo = ctx->fbos[fboId];
+    if (fbo.depth == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "framebuffer has no depth attachment");
+    if (fbo.numColors > 1) return ctx->fail(SLG_ERR_INVALID_ARG, "more than one colour attachment is not supported");
+    if (reqs.empty()) return SLG_OK;
+    if (reqs.size() + 1 > kDescRing) return ctx->fail(SLG_ERR_INVALID_ARG, "too many draws in one batch");
+
+    int r = upload_tables(ctx);
+    if (r) return r;
+
+    const Texture& depthTex = ctx->textures[fbo.depth];
+    const Texture* colorTex = (fbo.numColors > 0 && fbo.colors[0] != SLG_INVALID_ID) ? &ctx->textures[fbo.colors[0]] : nullptr;
+    if (colorTex && (colorTex->w != depthTex.w || colorTex->h != depthTex.h))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "colour and depth attachments differ in size");
+
+    /* descriptors into the ring */
+    const size_t n = reqs.size();
+    if (ctx->descHead + n + 1 > kDescRing)
+    {
+        cudaStreamSynchronize(ctx->stream);
+        ctx->descHead = 0;
+    }
+    DrawDesc* descs = ctx->hostDescs + ctx->descHead;
+    uint64_t* starts = ctx->hostStarts + ctx->descHead;
+    uint64_t numSlots = 0;
+    for (size_t i = 0; i < n; ++i)
+    {
+        uint64_t s = 0;
+        if ((r = build_desc(ctx, reqs[i], numSlots, descs[i], s))) return r;
+        starts[i] = numSlots;
+        numSlots += s;
+    }
+    starts[n] = numSlots;
+    if (numSlots > kMaxSlots) return ctx->fail(SLG_ERR_INVALID_ARG, "too many triangles in one launch (max 2^29-1)");
+
+    Frame f;
+    std::memset(&f, 0, sizeof(f));
+    f.width = depthTex.w;
+    f.height = depthTex.h;
+    f.tileW = ctx->tileW;
+    f.tileH = ctx->tileH;
+    f.tilesX = (f.width + f.tileW - 1) / f.tileW;
+    f.tilesY = (f.height + f.tileH - 1) / f.tileH;
+    const uint64_t numTiles = (uint64_t)f.tilesX * f.tilesY;
+    if ((r = ensure_scratch(ctx, numSlots, numTiles))) return r;
+
+    DrawDesc* devDescs = static_cast<DrawDesc*>(ctx->devDescs.ptr) + ctx->descHead;
+    uint64_t* devStarts = static_cast<uint64_t*>(ctx->devStarts.ptr) + ctx->descHead;
+    cudaError_t e = cudaMemcpyAsync(devDescs, descs, n * sizeof(DrawDesc), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(devStarts, starts, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "descriptor upload");
+    ctx->descHead += n + 1;
+
+    f.color = colorTex ? static_cast<uint8_t*>(colorTex->buf.ptr) : nullptr;
+    f.colorType = colorTex ? colorTex->type : SLG_COLOR_RGBA_8U;
+    f.depth = static_cast<float*>(depthTex.buf.ptr);
+    viewport_setup((float)f.width, (float)f.height, f.scissor, f.viewport);
+    f.records = static_cast<float4*>(ctx->records.ptr);
+    f.varyings = static_cast<float4*>(ctx->varyings.ptr);
+    f.slotInfo = static_cast<uint32_t*>(ctx->slotInfo.ptr);
+    f.slotOvf = static_cast<uint32_t*>(ctx->slotOvf.ptr);
+    f.ovfCount = static_cast<uint32_t*>(ctx->ovfCount.ptr);
+    f.ovfCap = (uint32_t)std::min<uint64_t>(ctx->ovfCap, 0xFFFFFFFFu);
+    f.numSlots = numSlots;
+    f.tileCount = static_cast<uint32_t*>(ctx->tileCount.ptr);
+    f.tileOffset = static_cast<uint32_t*>(ctx->tileOffset.ptr);
+    f.tileCursor = static_cast<uint32_t*>(ctx->tileCursor.ptr);
+    f.entries = static_cast<uint32_t*>(ctx->entries.ptr);
+    f.entryCap = (uint32_t)std::min<uint64_t>(ctx->entryCap, 0xFFFFFFFFu);
+    f.status = static_cast<int32_t*>(ctx->status.ptr);
+    f.draws = devDescs;
+    f.drawSlotStart = devStarts;
+    f.numDraws = (int32_t)n;
+    f.tables.textures = static_cast<const TexView*>(ctx->texTable.ptr);
+    f.tables.buffers = static_cast<const uint8_t* const*>(ctx->bufTable.ptr);
+
+    e = slg::launch_pipeline(f, ctx->keyCap, ctx->stream, ctx->profileStages ? ctx->stageEvents : nullptr);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "draw launch");
+    return SLG_OK;
+}
+
+bool id_ok(size_t id, size_t n) { return id < n; }
+
+} // namespace
+
+/*-----------------------------------------------------------------------------
+ * C ABI
+-----------------------------------------------------------------------------*/
+extern "C" {
+
+int slg_context_create(slg_context** outCtx)
+{
+    if (!outCtx) return SLG_ERR_INVALID_ARG;
+    *outCtx = nullptr;
+    slg_context* ctx = new (std::nothrow) slg_context();
+    if (!ctx) return SLG_ERR_NO_MEMORY;
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->hostDescs, kDescRing * sizeof(DrawDesc));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->hostStarts, kDescRing * sizeof(uint64_t));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->hostStatus, 4 * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->devDescs.ptr, kDescRing * sizeof(DrawDesc));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->devStarts.ptr, kDescRing * sizeof(uint64_t));
+    for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->stageEvents[i]);
+    if (e != cudaSuccess)
+    {
+        slg_context_destroy(ctx);
+        return SLG_ERR_CUDA;
+    }
+    ctx->devDescs.bytes = kDescRing * sizeof(DrawDesc);
+    ctx->devStarts.bytes = kDescRing * sizeof(uint64_t);
+    *outCtx = ctx;
+    return SLG_OK;
+}
+
+void slg_context_destroy(slg_context* ctx)
+{
+    if (!ctx) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (Vbo& v : ctx->vbos) dev_free(v.buf);
+    for (Ibo& v : ctx->ibos) dev_free(v.buf);
+    for (Texture& t : ctx->textures) dev_free(t.buf);
+    for (Ubo& u : ctx->ubos) dev_free(u.buf);
+    DevBuffer* scratch[] = {&ctx->texTable, &ctx->bufTable, &ctx->records, &ctx->varyings, &ctx->slotInfo, &ctx->slotOvf,
+                            &ctx->ovfCount, &ctx->tileCount, &ctx->tileOffset, &ctx->tileCursor, &ctx->entries,
+                            &ctx->status, &ctx->devDescs, &ctx->devStarts};
+    for (DevBuffer* b : scratch) dev_free(*b);
+    if (ctx->hostDescs) cudaFreeHost(ctx->hostDescs);
+    if (ctx->hostStarts) cudaFreeHost(ctx->hostStarts);
+    if (ctx->hostStatus) cudaFreeHost(ctx->hostStatus);
+    for (cudaEvent_t ev : ctx->stageEvents) if (ev) cudaEventDestroy(ev);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* slg_last_error(const slg_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+unsigned slg_num_threads(slg_context* ctx, unsigned n)
+{
+    if (n > 0) ctx->numThreads = n;
+    return ctx->numThreads;
+}
+
+size_t slg_create_vbo(slg_context* ctx) { ctx->vbos.emplace_back(); ctx->tablesDirty = true; return ctx->vbos.size() - 1; }
+
+int slg_vbo_init(slg_context* ctx, size_t id, size_t numBytes, const void* data)
+{
+    if (!id_ok(id, ctx->vbos.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid vbo id");
+    Vbo& v = ctx->vbos[id];
+    int r = dev_alloc(ctx, v.buf, numBytes + 64, true);
+    if (r) return r;
+    v.size = numBytes;
+    if (data && numBytes)
+    {
+        cudaError_t e = cudaMemcpyAsync(v.buf.ptr, data, numBytes, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "vbo upload");
+    }
+    ctx->tablesDirty = true;
+    return SLG_OK;
+}
+
+int slg_vbo_assign(slg_context* ctx, size_t id, const void* data, size_t offset, size_t numBytes)
+{
+    if (!id_ok(id, ctx->vbos.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid vbo id");
+    Vbo& v = ctx->vbos[id];
+    if (offset + numBytes > v.size) return ctx->fail(SLG_ERR_INVALID_ARG, "vbo range");
+    cudaError_t e = cudaMemcpyAsync(static_cast<uint8_t*>(v.buf.ptr) + offset, data, numBytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "vbo assign");
+    return SLG_OK;
+}
+
+size_t slg_create_ibo(slg_context* ctx) { ctx->ibos.emplace_back(); return ctx->ibos.size() - 1; }
+
+int slg_ibo_init(slg_context* ctx, size_t id, size_t numElements, int indexType, const void* data)
+{
+    if (!id_ok(id, ctx->ibos.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid ibo id");
+    const size_t ib = index_bytes(indexType);
+    if (!ib) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid index type");
+    Ibo& v = ctx->ibos[id];
+    /* padded like SL_IndexBuffer so a partial last triangle reads zeros */
+    int r = dev_alloc(ctx, v.buf, numElements * ib + 16, true);
+    if (r) return r;
+    v.type = indexType;
+    v.count = numElements;
+    if (data && numElements)
+    {
+        cudaError_t e = cudaMemcpyAsync(v.buf.ptr, data, numElements * ib, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "ibo upload");
+    }
+    return SLG_OK;
+}
+
+size_t slg_create_vao(slg_context* ctx) { ctx->vaos.emplace_back(); return ctx->vaos.size() - 1; }
+
+int slg_vao_set_vertex_buffer(slg_context* ctx, size_t vao, size_t vbo)
+{
+    if (!id_ok(vao, ctx->vaos.size()) || !id_ok(vbo, ctx->vbos.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid id");
+    ctx->vaos[vao].vbo = vbo;
+    return SLG_OK;
+}
+
+int slg_vao_set_index_buffer(slg_context* ctx, size_t vao, size_t ibo)
+{
+    if (!id_ok(vao, ctx->vaos.size()) || !id_ok(ibo, ctx->ibos.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid id");
+    ctx->vaos[vao].ibo = ibo;
+    return SLG_OK;
+}
+
+int slg_vao_set_binding(slg_context* ctx, size_t vao, unsigned bindId, ptrdiff_t offset, ptrdiff_t stride,
+                        unsigned numComponents, int dataType)
+{
+    if (!id_ok(vao, ctx->vaos.size()) || bindId >= 8) return ctx->fail(SLG_ERR_INVALID_ID, "invalid id");
+    Binding& b = ctx->vaos[vao].bindings[bindId];
+    b.offset = offset;
+    b.stride = stride;
+    b.comps = numComponents;
+    b.type = dataType;
+    return SLG_OK;
+}
+
+size_t slg_create_texture(slg_context* ctx) { ctx->textures.emplace_back(); ctx->tablesDirty = true; return ctx->textures.size() - 1; }
+
+int slg_texture_init(slg_context* ctx, size_t id, int colorType, uint16_t w, uint16_t h, uint16_t d)
+{
+    if (!id_ok(id, ctx->textures.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
+    const size_t bpt = bytes_per_color(colorType);
+    if (!bpt || !w || !h || !d) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid texture format or size");
+    Texture& t = ctx->textures[id];
+    /* zero padding after the dense texels: bilinear filtering may read one
+     * row and one texel past the end (softlight/include/softlight/SL_Sampler.hpp:200-201,
+     * allocation padded by softlight/src/SL_Texture.cpp:28-56) */
+    const size_t texels = (size_t)w * h * d;
+    const size_t padded = texels + (size_t)w + 64;
+    int r = dev_alloc(ctx, t.buf, padded * bpt, true);
+    if (r) return r;
+    t.type = colorType;
+    t.w = w; t.h = h; t.d = d;
+    t.bpt = (unsigned)bpt;
+    ctx->tablesDirty = true;
+    return SLG_OK;
+}
+
+int slg_texture_set_texels(slg_context* ctx, size_t id, const void* data, size_t numBytes)
+{
+    if (!id_ok(id, ctx->textures.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
+    Texture& t = ctx->textures[id];
+    if (!t.buf.ptr || numBytes != (size_t)t.w * t.h * t.d * t.bpt) return ctx->fail(SLG_ERR_INVALID_ARG, "texel byte count");
+    cudaError_t e = cudaMemcpyAsync(t.buf.ptr, data, numBytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "texture upload");
+    return SLG_OK;
+}
+
+int slg_texture_read(slg_context* ctx, size_t id, void* dst, size_t numBytes)
+{
+    if (!id_ok(id, ctx->textures.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
+    Texture& t = ctx->textures[id];
+    if (!t.buf.ptr || numBytes != (size_t)t.w * t.h * t.d * t.bpt) return ctx->fail(SLG_ERR_INVALID_ARG, "texel byte count");
+    cudaError_t e = cudaMemcpyAsync(dst, t.buf.ptr, numBytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "texture read");
+    return check_status(ctx);
+}
+
+size_t slg_create_framebuffer(slg_context* ctx) { ctx->fbos.emplace_back(); return ctx->fbos.size() - 1; }
+
+int slg_fbo_reserve_color_buffers(slg_context* ctx, size_t fbo, unsigned n)
+{
+    if (!id_ok(fbo, ctx->fbos.size()) || n > 4) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo or count");
+    ctx->fbos[fbo].numColors = n;
+    return SLG_OK;
+}
+
+int slg_fbo_attach_color_buffer(slg_context* ctx, size_t fbo, unsigned index, size_t tex)
+{
+    if (!id_ok(fbo, ctx->fbos.size()) || !id_ok(tex, ctx->textures.size()) || index >= ctx->fbos[fbo].numColors)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo attachment");
+    ctx->fbos[fbo].colors[index] = tex;
+    return SLG_OK;
+}
+
+int slg_fbo_attach_depth_buffer(slg_context* ctx, size_t fbo, size_t tex)
+{
+    if (!id_ok(fbo, ctx->fbos.size()) || !id_ok(tex, ctx->textures.size())) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo attachment");
+    if (ctx->textures[tex].type != SLG_COLOR_R_FLOAT) return ctx->fail(SLG_ERR_INVALID_ARG, "depth must be R_FLOAT");
+    ctx->fbos[fbo].depth = tex;
+    return SLG_OK;
+}
+
+size_t slg_create_ubo(slg_context* ctx)
+{
+    ctx->ubos.emplace_back();
+    if (dev_alloc(ctx, ctx->ubos.back().buf, 1024, true) != SLG_OK)
+    {
+        ctx->ubos.pop_back();
+        return SLG_INVALID_ID;
+    }
+    return ctx->ubos.size() - 1;
+}
+
+int slg_ubo_assign(slg_context* ctx, size_t id, const void* data, size_t numBytes)
+{
+    if (!id_ok(id, ctx->ubos.size()) || numBytes > 1024 || (!data && numBytes)) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid ubo");
+    cudaError_t e = cudaMemcpyAsync(ctx->ubos[id].buf.ptr, data, numBytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "ubo assign");
+    return SLG_OK;
+}
+
+size_t slg_create_shader(slg_context* ctx, const slg_vertex_shader* vs, const slg_fragment_shader* fs, size_t ubo)
+{
+    if (!vs || !fs) return ctx->fail_id("null shader");
+    /* SL_Context::create_shader (softlight/src/SL_Context.cpp:492-505) */
+    if (vs->numVaryings < fs->numVaryings || vs->numVaryings > 4 || fs->numVaryings > 4 || fs->numOutputs > 4)
+        return ctx->fail_id("invalid varying or output count");
+    if (!valid_program(vs->program) || !valid_program(fs->program)) return ctx->fail_id("unknown shader program");
+    if (vs->cullMode > SLG_CULL_OFF || fs->depthTest > SLG_DEPTH_TEST_NOT_EQUAL || fs->blend > SLG_BLEND_SCREEN || fs->depthMask > 1)
+        return ctx->fail_id("invalid pipeline state");
+    if (ubo != SLG_INVALID_ID && !id_ok(ubo, ctx->ubos.size())) return ctx->fail_id("invalid ubo id");
+    Shader s;
+    s.cull = vs->cullMode;
+    s.depthTest = fs->depthTest;
+    s.depthMask = fs->depthMask;
+    s.blend = fs->blend;
+    s.numVaryings = fs->numVaryings;
+    s.numOutputs = fs->numOutputs;
+    s.vsProgram = vs->program;
+    s.fsProgram = fs->program;
+    s.ubo = ubo;
+    ctx->shaders.push_back(s);
+    return ctx->shaders.size() - 1;
+}
+
+int slg_clear_color_buffer(slg_context* ctx, size_t fbo, unsigned att, const double rgba[4])
+{
+    if (!id_ok(fbo, ctx->fbos.size()) || att >= ctx->fbos[fbo].numColors || ctx->fbos[fbo].colors[att] == SLG_INVALID_ID)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo attachment");
+    return clear_texture(ctx, ctx->fbos[fbo].colors[att], rgba);
+}
+
+int slg_clear_depth_buffer(slg_context* ctx, size_t fbo, double depth)
+{
+    if (!id_ok(fbo, ctx->fbos.size()) || ctx->fbos[fbo].depth == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo");
+    const double d[4] = {depth, 0, 0, 0};
+    return clear_texture(ctx, ctx->fbos[fbo].depth, d);
+}
+
+int slg_clear_framebuffer(slg_context* ctx, size_t fbo, unsigned att, const double rgba[4], double depth)
+{
+    int r = slg_clear_color_buffer(ctx, fbo, att, rgba);
+    if (r) return r;
+    return slg_clear_depth_buffer(ctx, fbo, depth);
+}
+
+int slg_draw(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId)
+{
+    return slg_draw_instanced(ctx, m, 1, shaderId, fboId);
+}
+
+int slg_draw_instanced(slg_context* ctx, const slg_mesh* m, size_t numInstances, size_t shaderId, size_t fboId)
+{
+    if (!m) return ctx->fail(SLG_ERR_INVALID_ARG, "null mesh");
+    if (!numInstances) return SLG_OK;
+    std::vector<DrawRequest> reqs(1);
+    reqs[0] = {*m, numInstances, shaderId, 0};
+    return run_launch(ctx, reqs, fboId);
+}
+
+int slg_draw_multiple(slg_context* ctx, const slg_mesh* meshes, size_t numMeshes, size_t shaderId, size_t fboId)
+{
+    if (!meshes || !numMeshes) return SLG_OK;
+    std::vector<DrawRequest> reqs(numMeshes);
+    for (size_t i = 0; i < numMeshes; ++i) reqs[i] = {meshes[i], 1, shaderId, 0};
+    return run_launch(ctx, reqs, fboId);
+}
+
+int slg_draw_batch(slg_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, size_t fboId)
+{
+    if (!cmds || !numCmds) return SLG_OK;
+    std::vector<DrawRequest> reqs;
+    reqs.reserve(numCmds);
+    for (size_t i = 0; i < numCmds; ++i)
+    {
+        if (cmds[i].numInstances == 0) continue;
+        reqs.push_back({cmds[i].mesh, cmds[i].numInstances, cmds[i].shaderId, 0});
+    }
+    return run_launch(ctx, reqs, fboId);
+}
+
+int slg_finish(slg_context* ctx)
+{
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "stream synchronize");
+    return check_status(ctx);
+}
+
+void* slg_context_stream(slg_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int slg_set_tile_size(slg_context* ctx, int tileW, int tileH)
+{
+    const bool ok = (tileW == 8 && tileH == 8) || (tileW == 16 && tileH == 16) || (tileW == 32 && tileH == 16) ||
+                    (tileW == 32 && tileH == 32) || (tileW == 64 && tileH == 32) || (tileW == 64 && tileH == 64);
+    if (!ok) return ctx->fail(SLG_ERR_INVALID_ARG, "unsupported tile size");
+    cudaStreamSynchronize(ctx->stream);
+    ctx->tileW = tileW;
+    ctx->tileH = tileH;
+    return SLG_OK;
+}
+
+int slg_profile_stages(slg_context* ctx, int enable)
+{
+    ctx->profileStages = enable != 0;
+    return SLG_OK;
+}
+
+int slg_stage_times(slg_context* ctx, float ms[4])
+{
+    cudaError_t e = cudaEventSynchronize(ctx->stageEvents[4]);
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventElapsedTime(&ms[i], ctx->stageEvents[i], ctx->stageEvents[i + 1]);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "stage timing");
+    return SLG_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,265 @@
+/*
+ * slg_device.cuh - device-side data layout and exact arithmetic helpers.
+ *
+ * All floating-point code in this library is compiled with --fmad=false,
+ * -prec-div=true, -prec-sqrt=true and no flush-to-zero, so every expression
+ * below is a sequence of separately rounded binary32 operations in the
+ * written order. That is what makes coverage, depth and colour bit-identical
+ * to SoftLight's portable CPU path (the vector-library conventions are listed
+ * at the top of slg_kernels.cu).
+ */
+#ifndef SLG_DEVICE_CUH
+#define SLG_DEVICE_CUH
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/slg.h"
+#include "../../include/slg_programs.h"
+
+namespace slg
+{
+
+/*-----------------------------------------------------------------------------
+ * Sizes
+-----------------------------------------------------------------------------*/
+constexpr int kMaxVaryings = 4;         /* SL_SHADER_MAX_VARYING_VECTORS (SL_Config.hpp:40) */
+constexpr int kRecordVec4 = 8;          /* raster record: 8 x float4 = 128 bytes */
+constexpr int kVaryingVec4 = 12;        /* 3 vertices x 4 varyings */
+constexpr int kSubShift = 3;            /* key = slot << 3 | sub-triangle */
+
+/*-----------------------------------------------------------------------------
+ * Exact scalar helpers
+-----------------------------------------------------------------------------*/
+/* float -> int32 with x86 cvttss2si semantics: NaN or out of range gives
+ * INT32_MIN. */
+__device__ __forceinline__ int32_t f2i(float f)
+{
+    return (f >= -2147483648.f && f < 2147483648.f) ? __float2int_rz(f) : (int32_t)0x80000000;
+}
+
+__device__ __forceinline__ uint8_t f2u8(float f) { return (uint8_t)(uint32_t)f2i(f); }
+
+__device__ __forceinline__ float lm_max(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float lm_min(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ int sign_mask(float f) { return (int)(__float_as_uint(f) >> 31); }
+
+/*-----------------------------------------------------------------------------
+ * Resource views
+-----------------------------------------------------------------------------*/
+struct TexView
+{
+    const uint8_t* texels; /* dense w*h*d texels followed by zero padding */
+    uint32_t w, h, d;
+    int32_t type;          /* slg_color_type */
+};
+
+struct Tables
+{
+    const TexView* textures;
+    const uint8_t* const* buffers; /* vertex buffer base pointers by id */
+};
+
+/* One draw: what SL_ProcessorPool::run_shader_processors hands to
+ * SL_TriProcessor (softlight/src/SL_ProcessorPool.cpp:280-327). */
+struct DrawDesc
+{
+    const uint8_t* vbo;
+    const uint8_t* ibo;
+    const uint8_t* ubo;
+    int64_t  b0Offset;
+    int64_t  b0Stride;
+    uint64_t elementBegin;
+    uint64_t numElements;   /* elementEnd - elementBegin */
+    uint64_t numTris;       /* ceil(numElements / 3) per instance */
+    uint64_t numInstances;
+    uint64_t slotBase;      /* first slot of this draw in the launch */
+    uint64_t primBase;      /* primIndex offset (draw_multiple keeps per-mesh primIndex) */
+    int32_t  indexType;     /* -1: non-indexed */
+    uint32_t vsProgram;
+    uint32_t fsProgram;
+    uint8_t  cull, numVaryings, depthTest, depthMask, blend, numOutputs, pad0, pad1;
+};
+
+/* Per-launch scratch and framebuffer description. */
+struct Frame
+{
+    /* framebuffer */
+    uint8_t* color;         /* attachment 0, or null */
+    float*   depth;
+    int32_t  colorType;
+    int32_t  width, height;
+    int32_t  tileW, tileH, tilesX, tilesY;
+    float    scissor[16];
+    float    viewport[4];
+
+    /* scratch */
+    float4*   records;      /* (numSlots + ovfCap) x kRecordVec4 */
+    float4*   varyings;     /* (numSlots + ovfCap) x kVaryingVec4 */
+    uint32_t* slotInfo;     /* per slot: 0 none, 1 main record, 2+n: n clipped sub-records */
+    uint32_t* slotOvf;      /* per slot: first overflow record (relative) */
+    uint32_t* ovfCount;
+    uint32_t  ovfCap;
+    uint64_t  numSlots;
+    uint32_t* tileCount;    /* numTiles, zero between launches */
+    uint32_t* tileOffset;   /* numTiles + 1 */
+    uint32_t* tileCursor;   /* numTiles */
+    uint32_t* entries;      /* keys, grouped by tile */
+    uint32_t  entryCap;
+    int32_t*  status;       /* [0] error bits, [1] entries needed, [2] overflow records needed */
+
+    const DrawDesc* draws;
+    const uint64_t* drawSlotStart; /* numDraws + 1 */
+    int32_t numDraws;
+    Tables tables;
+};
+
+enum StatusBits
+{
+    kStatusEntryOverflow = 1,
+    kStatusOvfOverflow = 2,
+    kStatusTileOverflow = 4
+};
+
+/*-----------------------------------------------------------------------------
+ * Texture sampling: sl_sample_bilinear<color, SL_WrapMode::REPEAT, ORDERED>
+ * (softlight/include/softlight/SL_Sampler.hpp:97-115,187-218)
+-----------------------------------------------------------------------------*/
+__device__ __forceinline__ float wrap_repeat(float uvw)
+{
+    return (uvw < 0.f ? 1.f : 0.f) + fmodf(uvw, 1.f);
+}
+
+struct Bilinear
+{
+    uint32_t i00, i01, i10, i11;
+    float omdx, omdy, dx, dy;
+};
+
+__device__ __forceinline__ Bilinear bilinear_coords(const TexView& t, float x, float y)
+{
+    const float xf = wrap_repeat(x) * (float)t.w;
+    const float yf = wrap_repeat(y) * (float)t.h;
+    const uint32_t xi0 = (uint32_t)f2i(xf) & 0xFFFFu;
+    const uint32_t yi0 = (uint32_t)f2i(yf) & 0xFFFFu;
+    const uint32_t xn = (xi0 + 1u) & 0xFFFFu;
+    const uint32_t yn = (yi0 + 1u) & 0xFFFFu;
+    const uint32_t xi1 = (t.w < xn) ? t.w : xn;
+    const uint32_t yi1 = (t.h < yn) ? t.h : yn;
+    Bilinear c;
+    c.dx = xf - (float)xi0;
+    c.dy = yf - (float)yi0;
+    c.omdx = 1.f - c.dx;
+    c.omdy = 1.f - c.dy;
+    c.i00 = xi0 + t.w * yi0;
+    c.i01 = xi0 + t.w * yi1;
+    c.i10 = xi1 + t.w * yi0;
+    c.i11 = xi1 + t.w * yi1;
+    return c;
+}
+
+__device__ __forceinline__ float4 unpack_rgba8(uint32_t p)
+{
+    /* color_cast<float, uint8_t> (softlight/include/softlight/SL_Color.hpp:674) */
+    return make_float4((float)(p & 0xFFu) * 0.00392156862745f, (float)((p >> 8) & 0xFFu) * 0.00392156862745f,
+                       (float)((p >> 16) & 0xFFu) * 0.00392156862745f, (float)(p >> 24) * 0.00392156862745f);
+}
+
+__device__ __forceinline__ float4 bilinear_sum(const float4 p0, const float4 p1, const float4 p2, const float4 p3, const Bilinear& c)
+{
+    float4 r;
+    r.x = (((p0.x * c.omdx) * c.omdy + (p1.x * c.omdx) * c.dy) + (p2.x * c.dx) * c.omdy) + (p3.x * c.dx) * c.dy;
+    r.y = (((p0.y * c.omdx) * c.omdy + (p1.y * c.omdx) * c.dy) + (p2.y * c.dx) * c.omdy) + (p3.y * c.dx) * c.dy;
+    r.z = (((p0.z * c.omdx) * c.omdy + (p1.z * c.omdx) * c.dy) + (p2.z * c.dx) * c.omdy) + (p3.z * c.dx) * c.dy;
+    r.w = (((p0.w * c.omdx) * c.omdy + (p1.w * c.omdx) * c.dy) + (p2.w * c.dx) * c.omdy) + (p3.w * c.dx) * c.dy;
+    return r;
+}
+
+__device__ __forceinline__ slg_v4 sample_rgba8(const TexView& t, float u, float v)
+{
+    const Bilinear c = bilinear_coords(t, u, v);
+    const uint32_t* p = reinterpret_cast<const uint32_t*>(t.texels);
+    const float4 s = bilinear_sum(unpack_rgba8(__ldg(p + c.i00)), unpack_rgba8(__ldg(p + c.i01)),
+                                  unpack_rgba8(__ldg(p + c.i10)), unpack_rgba8(__ldg(p + c.i11)), c);
+    /* color_cast<uint8_t, float>, then the shader's color_cast<float, uint8_t> */
+    return slg_make_v4((float)f2u8(s.x * 255.f) * 0.00392156862745f, (float)f2u8(s.y * 255.f) * 0.00392156862745f,
+                       (float)f2u8(s.z * 255.f) * 0.00392156862745f, (float)f2u8(s.w * 255.f) * 0.00392156862745f);
+}
+
+__device__ __forceinline__ slg_v4 sample_rgbaf(const TexView& t, float u, float v)
+{
+    const Bilinear c = bilinear_coords(t, u, v);
+    const float4* p = reinterpret_cast<const float4*>(t.texels);
+    const float4 s = bilinear_sum(__ldg(p + c.i00), __ldg(p + c.i01), __ldg(p + c.i10), __ldg(p + c.i11), c);
+    return slg_make_v4(s.x, s.y, s.z, s.w);
+}
+
+/* Environment handed to the header-only programs (include/slg_programs.h). */
+struct DevEnv
+{
+    const uint8_t* vbo;
+    int64_t b0Offset, b0Stride;
+    const uint8_t* ubo;
+    Tables tables;
+
+    __device__ __forceinline__ const float* vertex(uint64_t vertId) const
+    {
+        return reinterpret_cast<const float*>(vbo + b0Offset + b0Stride * (int64_t)vertId);
+    }
+    __device__ __forceinline__ const void* uniforms() const { return ubo; }
+    __device__ __forceinline__ const float* buffer(uint32_t vboId) const
+    {
+        return reinterpret_cast<const float*>(tables.buffers[vboId]);
+    }
+    __device__ __forceinline__ slg_v4 sample_rgba8(uint32_t texId, float u, float v) const
+    {
+        return slg::sample_rgba8(tables.textures[texId], u, v);
+    }
+    __device__ __forceinline__ slg_v4 sample_rgbaf(uint32_t texId, float u, float v) const
+    {
+        return slg::sample_rgbaf(tables.textures[texId], u, v);
+    }
+};
+
+__device__ __forceinline__ DevEnv make_env(const DrawDesc& d, const Tables& t)
+{
+    DevEnv e;
+    e.vbo = d.vbo;
+    e.b0Offset = d.b0Offset;
+    e.b0Stride = d.b0Stride;
+    e.ubo = d.ubo;
+    e.tables = t;
+    return e;
+}
+
+/* Program dispatch: the GPU counterpart of calling SL_Shader::pVertShader /
+ * pFragShader through a function pointer (softlight/src/SL_TriProcessor.cpp:584-594,
+ * softlight/src/SL_FragmentProcessor.cpp:501). */
+__device__ __forceinline__ slg_v4 run_vertex_program(uint32_t program, const DevEnv& env, uint64_t vertId,
+                                                     uint64_t instanceId, slg_v4* varyings)
+{
+    switch (program)
+    {
+        case SLG_PROGRAM_LAMBERT_TEX:      return slg_vs_lambert(env, vertId, instanceId, varyings);
+        case SLG_PROGRAM_BLINN_PHONG_INST: return slg_vs_blinn(env, vertId, instanceId, varyings);
+        case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
+        case SLG_PROGRAM_VCOLOR_TEXF:      return slg_vs_vcolor(env, vertId, instanceId, varyings);
+        default:                           return slg_vs_flat(env, vertId, instanceId, varyings);
+    }
+}
+
+static __device__ __noinline__ bool run_fragment_program(uint32_t program, const DevEnv& env, const slg_v4* varyings, slg_v4* outputs)
+{
+    switch (program)
+    {
+        case SLG_PROGRAM_LAMBERT_TEX:      return slg_fs_lambert(env, varyings, outputs);
+        case SLG_PROGRAM_BLINN_PHONG_INST: return slg_fs_blinn(env, varyings, outputs);
+        case SLG_PROGRAM_VCOLOR_TEX_ALPHA: return slg_fs_vcolor_tex_alpha(env, varyings, outputs);
+        case SLG_PROGRAM_VCOLOR_TEXF:      return slg_fs_vcolor_texf(env, varyings, outputs);
+        default:                           return slg_fs_flat(env, varyings, outputs);
+    }
+}
+
+} // namespace slg
+
+#endif /* SLG_DEVICE_CUH */

@@ -1,0 +1,941 @@
+/*
+ * slg_kernels.cu - the GB300 kernels of the SoftLight triangle draw path.
+ *
+ * Pipeline of one launch (one draw, one instanced draw or a batch of draws):
+ *   1. vs_setup  : one thread per triangle slot (draw, instance, element
+ *                  triple): three vertex-program calls, back-face cull,
+ *                  clip-space classification, Sutherland-Hodgman clipping,
+ *                  perspective divide, viewport mapping, the sub-pixel
+ *                  reject and barycentric set-up of SL_TriProcessor
+ *                  (softlight/src/SL_TriProcessor.cpp:248-640); writes one
+ *                  128-byte raster record (+ varyings) per surviving
+ *                  triangle and counts, per screen tile, the records whose
+ *                  bounding box touches it.
+ *   2. tile_scan : exclusive scan of the per-tile counts.
+ *   3. bin_fill  : writes every record's ordering key into each tile list.
+ *   4. raster    : one CTA per tile. Sorts its keys (submission order),
+ *                  keeps the tile's depth and colour in shared memory and
+ *                  replays, per pixel and in submission order, the
+ *                  reference's scan-line span, incremental barycentrics,
+ *                  depth test, perspective-correct varyings, fragment
+ *                  program, blend and depth write
+ *                  (softlight/src/SL_TriRasterizer.cpp:807-923,
+ *                  softlight/src/SL_FragmentProcessor.cpp:417-531).
+ *
+ * Ordering. SoftLight with one thread rasterises triangles in the order
+ * push_bin emits them. Every record gets the key slot << 3 | sub, where the
+ * slot counts triangles in submission order across draws and instances and
+ * sub orders the fan triangles of a clipped input (0 when unclipped). Each
+ * tile processes its keys in ascending order, and each pixel is owned by
+ * exactly one thread, so every pixel sees its fragments in the reference's
+ * order. Nothing else depends on order.
+ *
+ * Vector-library conventions (LightMath, absent from the reference tree):
+ *   fmadd(a,b,c) = a*b + c (two roundings); rcp(x) = 1/x;
+ *   dot/sum fold left ((a0+a1)+a2)+a3; mix(a,b,t) = (b-a)*t + a;
+ *   cross(vec4) = (a1*b2-a2*b1, a2*b0-a0*b2, a0*b1-a1*b0, 0);
+ *   cross(vec2) = a0*b1 - a1*b0; max(a,b) = a<b ? b : a; min(a,b) = b<a ? b : a;
+ *   vec4 <= / >= compare all components; mat4*vec4 folds columns left;
+ *   float->int truncation gives INT32_MIN for NaN / out of range.
+ */
+#include "slg_device.cuh"
+#include "slg_kernels.cuh"
+
+namespace slg
+{
+
+/*-----------------------------------------------------------------------------
+ * Vertex stage helpers
+-----------------------------------------------------------------------------*/
+__device__ __forceinline__ float4 to_f4(const slg_v4& v) { return make_float4(v.x, v.y, v.z, v.w); }
+
+__device__ __forceinline__ float4 mat_mul(const float* m, const float4 v)
+{
+    float4 r;
+    r.x = ((m[0] * v.x + m[4] * v.y) + m[8]  * v.z) + m[12] * v.w;
+    r.y = ((m[1] * v.x + m[5] * v.y) + m[9]  * v.z) + m[13] * v.w;
+    r.z = ((m[2] * v.x + m[6] * v.y) + m[10] * v.z) + m[14] * v.w;
+    r.w = ((m[3] * v.x + m[7] * v.y) + m[11] * v.z) + m[15] * v.w;
+    return r;
+}
+
+/* face_determinant, portable branch (SL_TriProcessor.cpp:98-115) */
+__device__ __forceinline__ float face_determinant(const float4 p0, const float4 p1, const float4 p2)
+{
+    const float w0 = 1.f / p0.w;
+    const float w1 = 1.f / p1.w;
+    const float w2 = 1.f / p2.w;
+    const float v0x = p0.x * w0, v0y = p0.y * w0;
+    const float v1x = p1.x * w1, v1y = p1.y * w1;
+    const float v2x = p2.x * w2, v2y = p2.y * w2;
+    const float s = (v0x * (v1y - v2y) + v1x * (v2y - v0y)) + v2x * (v0y - v1y);
+    return __fadd_rn(s, 0.f);
+}
+
+/* sl_ndc_clip_status, portable branch (SL_PostVertexTransform.hpp:651-673) */
+__device__ __forceinline__ int clip_status(const float4 c0, const float4 c1, const float4 c2)
+{
+    auto inside = [](const float4 c) {
+        const float w = c.w, nw = -c.w;
+        return (c.x <= w && c.y <= w && c.z <= w && c.w <= w) && (c.x >= nw && c.y >= nw && c.z >= nw && c.w >= nw);
+    };
+    const bool vis = inside(c0) && inside(c1) && inside(c2);
+    const bool part = c0.w > 0.f || c1.w > 0.f || c2.w > 0.f;
+    return (vis ? 3 : 0) | (part ? 1 : 0);
+}
+
+/* sl_perspective_divide + sl_ndc_to_screen_coords, portable branches
+ * (SL_PostVertexTransform.hpp:240-249,509-524) */
+__device__ __forceinline__ float4 to_screen(const float4 v, const float* vp)
+{
+    const float wInv = 1.f / v.w;
+    const float x = v.x * wInv, y = v.y * wInv, z = v.z * wInv;
+    const float hw = vp[2] * 0.5f, hh = vp[3] * 0.5f;
+    float4 r;
+    r.x = lm_max(floorf((x + 1.f) * hw + vp[0]), 0.f);
+    r.y = lm_max(floorf((y + 1.f) * hh + vp[1]), 0.f);
+    r.z = z;
+    r.w = wInv;
+    return r;
+}
+
+/* The sub-pixel reject of SL_TriProcessor::push_bin (SL_TriProcessor.cpp:257-264) */
+__device__ __forceinline__ bool bin_visible(const float4 p0, const float4 p1, const float4 p2)
+{
+    const float minX = lm_min(lm_min(p0.x, p1.x), p2.x);
+    const float minY = lm_min(lm_min(p0.y, p1.y), p2.y);
+    const float maxX = lm_max(lm_max(p0.x, p1.x), p2.x);
+    const float maxY = lm_max(lm_max(p0.y, p1.y), p2.y);
+    return !((maxX - minX < 1.f) || (maxY - minY < 1.f));
+}
+
+/* Raster record of one binned triangle: the barycentric set-up of push_bin
+ * (SL_TriProcessor.cpp:271-314) and the per-triangle constants of
+ * SL_ScanlineBounds::init (SL_ScanlineBounds.hpp:137-186), which the
+ * reference recomputes per bin and thread and which are kept here.
+ *   r0 = (v0y, v1y, v0x, v1x)        r1 = (p20y, p20x, p21xy, p10xy)
+ *   r2 = (bc0.xyz, bc.w)             r3 = (bc1.xyz, z0)
+ *   r4 = (bc2.xyz, z1)               r5 = (z2, w0, w1, w2)
+ *   r6 = (minY, maxY, minX-1, maxX+1) as int32 bits
+ *   r7 = (draw index, primIndex lo, primIndex hi, 0) as uint32 bits */
+struct Record { float4 r[kRecordVec4]; };
+
+__device__ __forceinline__ void make_record(const float4 p0, const float4 p1, const float4 p2, uint32_t drawIndex,
+                                            uint64_t primIndex, Record& rec)
+{
+    const float xyx = p0.x - p1.x, xyy = p0.y - p1.y;
+    const float zyx = p2.x - p1.x, zyy = p2.y - p1.y;
+    const float denom = 1.f / (zyx * xyy - zyy * xyx);
+
+    const float ddx0 = p1.y - p2.y, ddx1 = p2.y - p0.y, ddx2 = p0.y - p1.y;
+    const float ddy0 = p2.x - p1.x, ddy1 = p0.x - p2.x, ddy2 = p1.x - p0.x;
+    const float ddz0 = p1.x * p2.y - p2.x * p1.y;
+    const float ddz1 = p2.x * p0.y - p0.x * p2.y;
+    const float ddz2 = p0.x * p1.y - p1.x * p0.y;
+
+    /* SL_ScanlineBounds::init: sort by y, descending */
+    float4 a = p0, b = p1, c = p2, t;
+    if (a.y < b.y) { t = a; a = b; b = t; }
+    if (a.y < c.y) { t = a; a = c; c = t; }
+    if (b.y < c.y) { t = b; b = c; c = t; }
+    const float p2p0x = c.x - a.x, p2p0y = c.y - a.y;
+    const float p2p1x = c.x - b.x, p2p1y = c.y - b.y;
+    const float p1p0x = b.x - a.x, p1p0y = b.y - a.y;
+
+    const float minX = lm_min(lm_min(p0.x, p1.x), p2.x);
+    const float minY = lm_min(lm_min(p0.y, p1.y), p2.y);
+    const float maxX = lm_max(lm_max(p0.x, p1.x), p2.x);
+    const float maxY = lm_max(lm_max(p0.y, p1.y), p2.y);
+
+    rec.r[0] = make_float4(a.y, b.y, a.x, b.x);
+    rec.r[1] = make_float4(1.f / p2p0y, p2p0x, p2p1x * (1.f / p2p1y), p1p0x * (1.f / p1p0y));
+    rec.r[2] = make_float4(ddx0 * denom, ddx1 * denom, ddx2 * denom, 0.f * denom);
+    rec.r[3] = make_float4(ddy0 * denom, ddy1 * denom, ddy2 * denom, p0.z);
+    rec.r[4] = make_float4(ddz0 * denom, ddz1 * denom, ddz2 * denom, p1.z);
+    rec.r[5] = make_float4(p2.z, p0.w, p1.w, p2.w);
+    rec.r[6] = make_float4(__int_as_float(f2i(minY)), __int_as_float(f2i(maxY)),
+                           __int_as_float(f2i(minX) - 1), __int_as_float(f2i(maxX) + 1));
+    rec.r[7] = make_float4(__uint_as_float(drawIndex), __uint_as_float((uint32_t)primIndex),
+                           __uint_as_float((uint32_t)(primIndex >> 32)), 0.f);
+}
+
+/* Inclusive tile range touched by a record; empty when tx1 < tx0 or ty1 < ty0. */
+struct TileRange { int tx0, tx1, ty0, ty1; };
+
+__device__ __forceinline__ TileRange tile_range(const float4 r6, const Frame& f)
+{
+    const int minY = __float_as_int(r6.x), maxY = __float_as_int(r6.y);
+    const int minX = __float_as_int(r6.z), maxX = __float_as_int(r6.w);
+    TileRange t;
+    if (maxY <= minY || maxX < minX || maxY <= 0 || minY >= f.height || maxX < 0 || minX >= f.width)
+    {
+        t.tx0 = 0; t.tx1 = -1; t.ty0 = 0; t.ty1 = -1;
+        return t;
+    }
+    const int ylo = max(minY, 0), yhi = min(maxY - 1, f.height - 1);
+    const int xlo = max(minX, 0), xhi = min(maxX, f.width - 1);
+    t.tx0 = xlo / f.tileW;
+    t.tx1 = xhi / f.tileW;
+    t.ty0 = ylo / f.tileH;
+    t.ty1 = yhi / f.tileH;
+    return t;
+}
+
+__device__ __forceinline__ void count_tiles(const float4 r6, const Frame& f)
+{
+    const TileRange t = tile_range(r6, f);
+    for (int ty = t.ty0; ty <= t.ty1; ++ty)
+    {
+        for (int tx = t.tx0; tx <= t.tx1; ++tx)
+        {
+            atomicAdd(&f.tileCount[ty * f.tilesX + tx], 1u);
+        }
+    }
+}
+
+__device__ __forceinline__ void store_record(const Frame& f, uint64_t recIndex, const Record& rec)
+{
+    float4* dst = f.records + recIndex * kRecordVec4;
+#pragma unroll
+    for (int i = 0; i < kRecordVec4; ++i)
+    {
+        dst[i] = rec.r[i];
+    }
+}
+
+__device__ __forceinline__ void store_varyings(const Frame& f, uint64_t recIndex, int nv,
+                                               const slg_v4* a, const slg_v4* b, const slg_v4* c)
+{
+    float4* dst = f.varyings + recIndex * kVaryingVec4;
+    for (int i = 0; i < nv; ++i)
+    {
+        dst[i] = to_f4(a[i]);
+        dst[4 + i] = to_f4(b[i]);
+        dst[8 + i] = to_f4(c[i]);
+    }
+}
+
+__device__ __forceinline__ slg_v4 mix4(const slg_v4 a, const slg_v4 b, float t)
+{
+    return slg_make_v4((b.x - a.x) * t + a.x, (b.y - a.y) * t + a.y, (b.z - a.z) * t + a.z, (b.w - a.w) * t + a.w);
+}
+
+__device__ __forceinline__ float4 mix4(const float4 a, const float4 b, float t)
+{
+    return make_float4((b.x - a.x) * t + a.x, (b.y - a.y) * t + a.y, (b.z - a.z) * t + a.z, (b.w - a.w) * t + a.w);
+}
+
+/* SL_TriProcessor::clip_and_process_tris (SL_TriProcessor.cpp:370-519).
+ * Returns the slotInfo value for the slot. */
+__device__ __noinline__ uint32_t clip_and_emit(const Frame& f, const DrawDesc& d, uint32_t drawIndex, uint64_t slot,
+                                               uint64_t primIndex, const float4* clip, const slg_v4* vary)
+{
+    const int nv = d.numVaryings;
+    float4 newVerts[9], tempVerts[9];
+    slg_v4 newVarys[36], tempVarys[36];
+    for (int i = 0; i < 9; ++i) { newVerts[i] = make_float4(0.f, 0.f, 0.f, 0.f); tempVerts[i] = newVerts[i]; }
+    for (int i = 0; i < 36; ++i) { newVarys[i] = slg_make_v4(0.f, 0.f, 0.f, 0.f); tempVarys[i] = newVarys[i]; }
+
+    unsigned numTotal = 3;
+    for (int k = 0; k < 3; ++k)
+    {
+        newVerts[k] = clip[k];
+        for (int i = 0; i < nv; ++i) newVarys[k * 4 + i] = vary[k * 4 + i];
+    }
+
+    for (int e = 0; e < 6; ++e)
+    {
+        /* clipEdges: +x, -x, +y, -y, +z, -z against w (SL_TriProcessor.cpp:384-393) */
+        const float ex = (e == 0) ? 1.f : (e == 1) ? -1.f : 0.f;
+        const float ey = (e == 2) ? 1.f : (e == 3) ? -1.f : 0.f;
+        const float ez = (e == 4) ? 1.f : (e == 5) ? -1.f : 0.f;
+        auto dotEdge = [&](const float4 p) { return ((p.x * ex + p.y * ey) + p.z * ez) + p.w * 1.f; };
+
+        unsigned numNew = 0;
+        unsigned j = numTotal - 1;
+        float4 q0 = newVerts[numTotal - 1];
+        float t0 = dotEdge(q0);
+        int vis0 = !sign_mask(t0);
+
+        for (unsigned k = 0; k < numTotal; ++k)
+        {
+            const float4 q1 = newVerts[k];
+            const float t1 = dotEdge(q1);
+            const int vis1 = !sign_mask(t1);
+            if (vis0 ^ vis1)
+            {
+                const float t = t0 * (1.f / (t0 - t1));
+                tempVerts[numNew] = mix4(q0, q1, t);
+                for (int i = 0; i < nv; ++i)
+                {
+                    tempVarys[numNew * 4 + i] = mix4(newVarys[j * 4 + i], newVarys[k * 4 + i], t);
+                }
+                ++numNew;
+            }
+            if (vis1)
+            {
+                tempVerts[numNew] = q1;
+                for (int i = 0; i < nv; ++i) tempVarys[numNew * 4 + i] = newVarys[k * 4 + i];
+                ++numNew;
+            }
+            j = k;
+            q0 = q1;
+            t0 = t1;
+            vis0 = vis1;
+        }
+
+        if (!numNew)
+        {
+            return 0;
+        }
+        numTotal = numNew;
+        for (unsigned i = 0; i < numNew; ++i) newVerts[i] = tempVerts[i];
+        /* copies numNew vectors from each vertex's first varying slot
+         * (SL_TriProcessor.cpp:471-475), bounded to the 36 slots */
+        for (unsigned i = numNew; i--;)
+        {
+            for (unsigned m = 0; m < numNew; ++m)
+            {
+                const unsigned s = i * 4 + m;
+                if (s < 36) newVarys[s] = tempVarys[s];
+            }
+        }
+    }
+
+    if (numTotal < 3)
+    {
+        return 0;
+    }
+
+    for (unsigned i = 0; i < numTotal; ++i)
+    {
+        newVerts[i] = to_screen(newVerts[i], f.viewport);
+    }
+
+    /* fan (0, i+1, i+2) for i = numTotal-3 .. 0, in that order */
+    uint32_t survivors = 0;
+    for (unsigned i = numTotal - 2; i--;)
+    {
+        survivors += bin_visible(newVerts[0], newVerts[i + 1], newVerts[i + 2]) ? 1u : 0u;
+    }
+    if (!survivors)
+    {
+        return 0;
+    }
+
+    const uint32_t base = atomicAdd(f.ovfCount, survivors);
+    if (base + survivors > f.ovfCap)
+    {
+        atomicOr(f.status, kStatusOvfOverflow);
+        atomicMax(f.status + 2, (int)(base + survivors));
+        return 0;
+    }
+    f.slotOvf[slot] = base;
+
+    uint32_t sub = 0;
+    for (unsigned i = numTotal - 2; i--;)
+    {
+        const float4 a = newVerts[0], b = newVerts[i + 1], c = newVerts[i + 2];
+        if (!bin_visible(a, b, c))
+        {
+            continue;
+        }
+        Record rec;
+        make_record(a, b, c, drawIndex, primIndex, rec);
+        const uint64_t recIndex = f.numSlots + base + sub;
+        store_record(f, recIndex, rec);
+        store_varyings(f, recIndex, nv, newVarys, newVarys + (i + 1) * 4, newVarys + (i + 2) * 4);
+        count_tiles(rec.r[6], f);
+        ++sub;
+    }
+    return 2u + survivors;
+}
+
+__device__ __forceinline__ int find_draw(const Frame& f, uint64_t slot)
+{
+    int lo = 0, hi = f.numDraws - 1;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi + 1) >> 1;
+        if (f.drawSlotStart[mid] <= slot) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint64_t read_index(const DrawDesc& d, uint64_t i)
+{
+    switch (d.indexType)
+    {
+        case SLG_VERTEX_DATA_BYTE:  return d.ibo[i];
+        case SLG_VERTEX_DATA_SHORT: return reinterpret_cast<const uint16_t*>(d.ibo)[i];
+        default:                    return reinterpret_cast<const uint32_t*>(d.ibo)[i];
+    }
+}
+
+/*-----------------------------------------------------------------------------
+ * Kernel 1: vertex processing, clipping, set-up and tile counting
+ * (SL_TriProcessor::process_verts, SL_TriProcessor.cpp:527-640)
+-----------------------------------------------------------------------------*/
+__global__ void __launch_bounds__(128) vs_setup_kernel(const Frame f)
+{
+    const uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= f.numSlots)
+    {
+        return;
+    }
+
+    const int di = (f.numDraws > 1) ? find_draw(f, slot) : 0;
+    const DrawDesc& d = f.draws[di];
+    const uint64_t local = slot - d.slotBase;
+    const uint64_t inst = local / d.numTris;
+    const uint64_t tri = local - inst * d.numTris;
+    const uint64_t i = d.elementBegin + 3u * tri;
+    const DevEnv env = make_env(d, f.tables);
+
+    float4 clip[3];
+    slg_v4 vary[12];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        const uint64_t vid = (d.indexType >= 0) ? read_index(d, i + k) : (i + k);
+        clip[k] = to_f4(run_vertex_program(d.vsProgram, env, vid, inst, vary + 4 * k));
+    }
+
+    uint32_t info = 0;
+    if (d.cull != SLG_CULL_OFF)
+    {
+        const float det = face_determinant(clip[0], clip[1], clip[2]);
+        const bool culled = (d.cull == SLG_CULL_FRONT_FACE) ^ (sign_mask(det) != 0);
+        if (culled)
+        {
+            f.slotInfo[slot] = 0;
+            return;
+        }
+    }
+
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        clip[k] = mat_mul(f.scissor, clip[k]);
+    }
+
+    const uint64_t primIndex = d.primBase + d.numElements * inst + i;
+    const int vis = clip_status(clip[0], clip[1], clip[2]);
+    if (vis == 3)
+    {
+        const float4 s0 = to_screen(clip[0], f.viewport);
+        const float4 s1 = to_screen(clip[1], f.viewport);
+        const float4 s2 = to_screen(clip[2], f.viewport);
+        if (bin_visible(s0, s1, s2))
+        {
+            Record rec;
+            make_record(s0, s1, s2, (uint32_t)di, primIndex, rec);
+            store_record(f, slot, rec);
+            store_varyings(f, slot, d.numVaryings, vary, vary + 4, vary + 8);
+            count_tiles(rec.r[6], f);
+            info = 1;
+        }
+    }
+    else if (vis == 1)
+    {
+        info = clip_and_emit(f, d, (uint32_t)di, slot, primIndex, clip, vary);
+    }
+    f.slotInfo[slot] = info;
+}
+
+/*-----------------------------------------------------------------------------
+ * Kernel 2: exclusive scan of tile counts (one CTA)
+-----------------------------------------------------------------------------*/
+__global__ void __launch_bounds__(1024) tile_scan_kernel(const Frame f, int numTiles)
+{
+    __shared__ uint32_t sSums[1024];
+    const int tid = threadIdx.x;
+    const int per = (numTiles + 1023) / 1024;
+    const int begin = min(numTiles, tid * per);
+    const int end = min(numTiles, begin + per);
+
+    uint32_t local = 0;
+    for (int t = begin; t < end; ++t) local += f.tileCount[t];
+    sSums[tid] = local;
+    __syncthreads();
+
+    /* Hillis-Steele inclusive scan over 1024 partial sums */
+    for (int off = 1; off < 1024; off <<= 1)
+    {
+        const uint32_t v = (tid >= off) ? sSums[tid - off] : 0u;
+        __syncthreads();
+        sSums[tid] += v;
+        __syncthreads();
+    }
+
+    uint32_t run = sSums[tid] - local;
+    for (int t = begin; t < end; ++t)
+    {
+        const uint32_t c = f.tileCount[t];
+        f.tileOffset[t] = run;
+        f.tileCursor[t] = run;
+        f.tileCount[t] = 0;
+        run += c;
+    }
+    if (tid == 1023)
+    {
+        const uint32_t total = sSums[1023];
+        f.tileOffset[numTiles] = total;
+        if (total > f.entryCap)
+        {
+            atomicOr(f.status, kStatusEntryOverflow);
+            atomicMax(f.status + 1, (int)min(total, 0x7FFFFFFFu));
+        }
+        *f.ovfCount = 0;
+    }
+}
+
+/*-----------------------------------------------------------------------------
+ * Kernel 3: tile list fill
+-----------------------------------------------------------------------------*/
+__device__ __forceinline__ void fill_record(const Frame& f, uint64_t recIndex, uint32_t key)
+{
+    const float4 r6 = f.records[recIndex * kRecordVec4 + 6];
+    const TileRange t = tile_range(r6, f);
+    for (int ty = t.ty0; ty <= t.ty1; ++ty)
+    {
+        for (int tx = t.tx0; tx <= t.tx1; ++tx)
+        {
+            const uint32_t pos = atomicAdd(&f.tileCursor[ty * f.tilesX + tx], 1u);
+            if (pos < f.entryCap)
+            {
+                f.entries[pos] = key;
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) bin_fill_kernel(const Frame f)
+{
+    const uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= f.numSlots)
+    {
+        return;
+    }
+    const uint32_t info = f.slotInfo[slot];
+    if (info == 1)
+    {
+        fill_record(f, slot, (uint32_t)(slot << kSubShift));
+    }
+    else if (info >= 2)
+    {
+        const uint32_t base = f.slotOvf[slot];
+        for (uint32_t s = 0; s < info - 2; ++s)
+        {
+            fill_record(f, f.numSlots + base + s, (uint32_t)(slot << kSubShift) | (s + 1));
+        }
+    }
+}
+
+/*-----------------------------------------------------------------------------
+ * Kernel 4: tile raster + shade
+-----------------------------------------------------------------------------*/
+__device__ __forceinline__ bool depth_cmp(int func, float z, float d)
+{
+    switch (func)
+    {
+        case SLG_DEPTH_TEST_LESS_THAN:     return z < d;
+        case SLG_DEPTH_TEST_LESS_EQUAL:    return z <= d;
+        case SLG_DEPTH_TEST_GREATER_THAN:  return z > d;
+        case SLG_DEPTH_TEST_GREATER_EQUAL: return z >= d;
+        case SLG_DEPTH_TEST_EQUAL:         return z == d;
+        case SLG_DEPTH_TEST_NOT_EQUAL:     return z != d;
+        default:                           return true;
+    }
+}
+
+/* Colour formats of the tile buffer in shared memory. */
+struct ColorRGBA8
+{
+    typedef uint32_t stored;
+    static __device__ __forceinline__ float4 load(stored v) { return unpack_rgba8(v); }
+    static __device__ __forceinline__ stored store(float4 c)
+    {
+        return (uint32_t)f2u8(c.x * 255.f) | ((uint32_t)f2u8(c.y * 255.f) << 8) |
+               ((uint32_t)f2u8(c.z * 255.f) << 16) | ((uint32_t)f2u8(c.w * 255.f) << 24);
+    }
+    static __device__ __forceinline__ stored read(const uint8_t* p, size_t i) { return reinterpret_cast<const uint32_t*>(p)[i]; }
+    static __device__ __forceinline__ void write(uint8_t* p, size_t i, stored v) { reinterpret_cast<uint32_t*>(p)[i] = v; }
+};
+
+struct ColorRGBAF
+{
+    typedef float4 stored;
+    static __device__ __forceinline__ float4 load(stored v) { return v; }
+    static __device__ __forceinline__ stored store(float4 c) { return c; }
+    static __device__ __forceinline__ stored read(const uint8_t* p, size_t i) { return reinterpret_cast<const float4*>(p)[i]; }
+    static __device__ __forceinline__ void write(uint8_t* p, size_t i, stored v) { reinterpret_cast<float4*>(p)[i] = v; }
+};
+
+struct ColorRF
+{
+    typedef float stored;
+    static __device__ __forceinline__ float4 load(stored v) { return make_float4(v, 0.f, 0.f, 1.f); }
+    static __device__ __forceinline__ stored store(float4 c) { return c.x; }
+    static __device__ __forceinline__ stored read(const uint8_t* p, size_t i) { return reinterpret_cast<const float*>(p)[i]; }
+    static __device__ __forceinline__ void write(uint8_t* p, size_t i, stored v) { reinterpret_cast<float*>(p)[i] = v; }
+};
+
+/* assign_alpha_pixel blend formulas (SL_Framebuffer.cpp:316-349) */
+__device__ __forceinline__ float4 blend_color(int mode, const float4 s, const float4 d)
+{
+    const float sa = s.w;
+    const float modulation = 1.f - sa;
+    float4 r;
+    if (mode == SLG_BLEND_ALPHA)
+    {
+        const float dstMod = modulation * d.w;
+        const float dstAlpha = dstMod + sa;
+        const float rc = 1.f / dstAlpha;
+        r = make_float4((s.x * sa + d.x * dstMod) * rc, (s.y * sa + d.y * dstMod) * rc, (s.z * sa + d.z * dstMod) * rc, dstAlpha);
+    }
+    else if (mode == SLG_BLEND_PREMULTIPLED_ALPHA)
+    {
+        r = make_float4(d.x * modulation + s.x, d.y * modulation + s.y, d.z * modulation + s.z, d.w * modulation + s.w);
+    }
+    else if (mode == SLG_BLEND_ADDITIVE)
+    {
+        r = make_float4(s.x * sa + d.x, s.y * sa + d.y, s.z * sa + d.z, s.w * sa + d.w);
+    }
+    else
+    {
+        r = make_float4(s.x * sa + d.x * modulation, s.y * sa + d.y * modulation, s.z * sa + d.z * modulation, s.w * sa + d.w * modulation);
+    }
+    r.x = lm_min(lm_max(r.x, 0.f), 1.f);
+    r.y = lm_min(lm_max(r.y, 0.f), 1.f);
+    r.z = lm_min(lm_max(r.z, 0.f), 1.f);
+    r.w = lm_min(lm_max(r.w, 0.f), 1.f);
+    return r;
+}
+
+__device__ __forceinline__ uint64_t key_to_record(const Frame& f, uint32_t key)
+{
+    const uint64_t slot = key >> kSubShift;
+    const uint32_t sub = key & ((1u << kSubShift) - 1u);
+    return (sub == 0) ? slot : (f.numSlots + f.slotOvf[slot] + (sub - 1));
+}
+
+/* In-place ascending bitonic sort of n keys in shared memory (n <= cap, cap a
+ * power of two); entries n..p-1 are padded with 0xFFFFFFFF. */
+__device__ void sort_keys(uint32_t* s, int n)
+{
+    int p = 2;
+    while (p < n) p <<= 1;
+    for (int i = n + threadIdx.x; i < p; i += blockDim.x) s[i] = 0xFFFFFFFFu;
+    __syncthreads();
+
+    int unsorted = 0;
+    for (int i = threadIdx.x; i + 1 < n; i += blockDim.x) unsorted |= (s[i] > s[i + 1]);
+    if (!__syncthreads_or(unsorted))
+    {
+        return;
+    }
+
+    for (int k = 2; k <= p; k <<= 1)
+    {
+        for (int j = k >> 1; j > 0; j >>= 1)
+        {
+            for (int i = threadIdx.x; i < p; i += blockDim.x)
+            {
+                const int ixj = i ^ j;
+                if (ixj > i)
+                {
+                    const uint32_t a = s[i], b = s[ixj];
+                    const bool up = ((i & k) == 0);
+                    if ((a > b) == up)
+                    {
+                        s[i] = b;
+                        s[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+template <int TW, int TH, class Color>
+struct RasterLayout
+{
+    static constexpr int kThreads = TH * 4;
+    static constexpr int kStride = TW + 4;       /* row pitch of the tile buffers (bank spread) */
+    static constexpr int kBatch = 32;            /* records staged per step */
+    static constexpr size_t kColorBytes = sizeof(typename Color::stored) * TH * kStride;
+    static constexpr size_t kDepthBytes = sizeof(float) * TH * kStride;
+    static constexpr size_t kRecBytes = sizeof(float4) * kBatch * kRecordVec4;
+    static constexpr size_t fixed_bytes() { return kColorBytes + kDepthBytes + kRecBytes + 2 * sizeof(uint32_t) * kBatch; }
+};
+
+template <int TW, int TH, class Color>
+__global__ void __launch_bounds__(TH * 4) raster_kernel(const Frame f, int keyCap)
+{
+    typedef RasterLayout<TW, TH, Color> L;
+    typedef typename Color::stored Stored;
+    extern __shared__ __align__(16) uint8_t smem[];
+    Stored*   sColor = reinterpret_cast<Stored*>(smem);
+    float*    sDepth = reinterpret_cast<float*>(smem + L::kColorBytes);
+    float4*   sRec   = reinterpret_cast<float4*>(smem + L::kColorBytes + L::kDepthBytes);
+    uint32_t* sRecIx = reinterpret_cast<uint32_t*>(smem + L::kColorBytes + L::kDepthBytes + L::kRecBytes);
+    uint32_t* sKeys  = sRecIx + 2 * L::kBatch;
+
+    const int tile = blockIdx.x;
+    const uint32_t begin = f.tileOffset[tile];
+    const uint32_t n = f.tileOffset[tile + 1] - begin;
+    if (n == 0 || (f.status[0] & kStatusEntryOverflow))
+    {
+        return;
+    }
+    if ((int)n > keyCap)
+    {
+        if (threadIdx.x == 0) atomicOr(f.status, kStatusTileOverflow);
+        return;
+    }
+
+    const int tx = tile % f.tilesX, ty = tile / f.tilesX;
+    const int x0 = tx * TW, y0 = ty * TH;
+
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) sKeys[i] = f.entries[begin + i];
+    __syncthreads();
+    sort_keys(sKeys, (int)n);
+
+    /* tile load */
+    for (int i = threadIdx.x; i < TW * TH; i += blockDim.x)
+    {
+        const int px = i % TW, py = i / TW;
+        const int gx = x0 + px, gy = y0 + py;
+        if (gx < f.width && gy < f.height)
+        {
+            const size_t gi = (size_t)gx + (size_t)f.width * gy;
+            sDepth[py * L::kStride + px] = f.depth[gi];
+            if (f.color) sColor[py * L::kStride + px] = Color::read(f.color, gi);
+        }
+    }
+    __syncthreads();
+
+    const int r = threadIdx.x >> 2;
+    const int c = threadIdx.x & 3;
+    const int y = y0 + r;
+    const int myX0 = x0 + c;
+    const int xLimit = min(x0 + TW, f.width);
+    const bool rowActive = (y < f.height);
+    const float yf = (float)y;
+
+    for (uint32_t b0 = 0; b0 < n; b0 += L::kBatch)
+    {
+        const int cnt = (int)min((uint32_t)L::kBatch, n - b0);
+        if (threadIdx.x < cnt)
+        {
+            sRecIx[threadIdx.x] = (uint32_t)key_to_record(f, sKeys[b0 + threadIdx.x]);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt * kRecordVec4; i += blockDim.x)
+        {
+            const int ri = i / kRecordVec4, part = i % kRecordVec4;
+            sRec[i] = f.records[(uint64_t)sRecIx[ri] * kRecordVec4 + part];
+        }
+        __syncthreads();
+
+        for (int ri = 0; ri < cnt && rowActive; ++ri)
+        {
+            const float4* R = sRec + ri * kRecordVec4;
+            const float4 r6 = R[6];
+            if (y < __float_as_int(r6.x) || y >= __float_as_int(r6.y))
+            {
+                continue;
+            }
+
+            /* SL_ScanlineBounds::step, portable branch (SL_ScanlineBounds.hpp:301-321) */
+            const float4 r0 = R[0], r1 = R[1];
+            const float d0 = yf - r0.x;
+            const float d1 = yf - r0.y;
+            const float alpha = d0 * r1.x;
+            const int32_t lo = f2i(r1.y * alpha + r0.z);
+            const int32_t sa = f2i(r1.z * d1 + r0.w);
+            const int32_t sb = f2i(r1.w * d0 + r0.z);
+            const int32_t hi = (d1 < 0.f) ? sa : sb;
+            const int32_t xMin = (lo >= hi) ? hi : lo;
+            const int32_t xMax = (lo >= hi) ? lo : hi;
+            if (!((uint32_t)xMin < (uint32_t)xMax))
+            {
+                continue;
+            }
+
+            const int xEnd = min(xMax, xLimit);
+            const int xs = xMin + ((myX0 - xMin) & 3);   /* first pixel of this thread's chain */
+            const int xFirst = max(xs, myX0);
+            if (xFirst >= xEnd)
+            {
+                continue;
+            }
+
+            /* incremental barycentrics (SL_TriRasterizer.cpp:856-911): the
+             * value at pixel x is bc0*xs + bcY plus (x-xs)/4 sequential
+             * additions of 4*bc0, replayed exactly */
+            const float4 r2 = R[2], r3 = R[3], r4 = R[4];
+            const float bcY0 = r3.x * yf + r4.x;
+            const float bcY1 = r3.y * yf + r4.y;
+            const float bcY2 = r3.z * yf + r4.z;
+            const float xsf = (float)xs;
+            float b0v = r2.x * xsf + bcY0;
+            float b1v = r2.y * xsf + bcY1;
+            float b2v = r2.z * xsf + bcY2;
+            const float bx0 = r2.x * 4.f, bx1 = r2.y * 4.f, bx2 = r2.z * 4.f;
+            for (int g = (xFirst - xs) >> 2; g > 0; --g)
+            {
+                b0v += bx0;
+                b1v += bx1;
+                b2v += bx2;
+            }
+
+            const float zw = 0.f * r2.w;
+            const float z0 = r3.w, z1 = r4.w;
+            const float4 r5 = R[5];
+            const uint32_t drawIndex = __float_as_uint(R[7].x);
+            const DrawDesc& dd = f.draws[drawIndex];
+            const int depthFunc = dd.depthTest;
+
+            for (int x = xFirst; x < xEnd; x += 4)
+            {
+                const float z = __fadd_rn(((z0 * b0v + z1 * b1v) + r5.x * b2v), zw);
+                const int idx = r * L::kStride + (x - x0);
+                if (depth_cmp(depthFunc, z, sDepth[idx]))
+                {
+                    /* flush_tri_fragments (SL_FragmentProcessor.cpp:463-529) */
+                    const float bp0 = b0v * r5.y, bp1 = b1v * r5.z, bp2 = b2v * r5.w;
+                    const float bp3 = r2.w * 0.f;
+                    const float persp = 1.f / (((bp0 + bp1) + bp2) + bp3);
+                    const float q0 = bp0 * persp, q1 = bp1 * persp, q2 = bp2 * persp;
+
+                    slg_v4 vary[4];
+                    const float4* V = f.varyings + (uint64_t)sRecIx[ri] * kVaryingVec4;
+                    for (int vi = 0; vi < dd.numVaryings; ++vi)
+                    {
+                        const float4 a = V[vi], b = V[4 + vi], cc = V[8 + vi];
+                        vary[vi] = slg_make_v4((a.x * q0 + b.x * q1) + cc.x * q2, (a.y * q0 + b.y * q1) + cc.y * q2,
+                                               (a.z * q0 + b.z * q1) + cc.z * q2, (a.w * q0 + b.w * q1) + cc.w * q2);
+                    }
+
+                    slg_v4 outputs[4];
+                    const DevEnv env = make_env(dd, f.tables);
+                    const bool haveOutputs = run_fragment_program(dd.fsProgram, env, vary, outputs);
+                    if (haveOutputs && dd.numOutputs > 0 && f.color)
+                    {
+                        const float4 o = to_f4(outputs[0]);
+                        if (dd.blend != SLG_BLEND_OFF)
+                        {
+                            sColor[idx] = Color::store(blend_color(dd.blend, o, Color::load(sColor[idx])));
+                        }
+                        else
+                        {
+                            sColor[idx] = Color::store(o);
+                        }
+                    }
+                    if (dd.depthMask == SLG_DEPTH_MASK_ON)
+                    {
+                        sDepth[idx] = z;
+                    }
+                }
+                b0v += bx0;
+                b1v += bx1;
+                b2v += bx2;
+            }
+        }
+        __syncthreads();
+    }
+
+    /* tile store */
+    for (int i = threadIdx.x; i < TW * TH; i += blockDim.x)
+    {
+        const int px = i % TW, py = i / TW;
+        const int gx = x0 + px, gy = y0 + py;
+        if (gx < f.width && gy < f.height)
+        {
+            const size_t gi = (size_t)gx + (size_t)f.width * gy;
+            f.depth[gi] = sDepth[py * L::kStride + px];
+            if (f.color) Color::write(f.color, gi, sColor[py * L::kStride + px]);
+        }
+    }
+}
+
+/*-----------------------------------------------------------------------------
+ * Clear (SL_ClearProcessor, softlight/src/SL_ClearProcessor.cpp)
+-----------------------------------------------------------------------------*/
+__global__ void clear_kernel(uint8_t* dst, size_t numTexels, int bytesPerTexel, uint4 value)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < numTexels; i += stride)
+    {
+        if (bytesPerTexel == 16) reinterpret_cast<uint4*>(dst)[i] = value;
+        else reinterpret_cast<uint32_t*>(dst)[i] = value.x;
+    }
+}
+
+/*-----------------------------------------------------------------------------
+ * Host-side launchers
+-----------------------------------------------------------------------------*/
+template <int TW, int TH, class Color>
+static cudaError_t launch_raster_t(const Frame& f, int numTiles, int keyCap, cudaStream_t s)
+{
+    typedef RasterLayout<TW, TH, Color> L;
+    const size_t smem = L::fixed_bytes() + sizeof(uint32_t) * (size_t)keyCap;
+    cudaError_t e = cudaFuncSetAttribute(raster_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    raster_kernel<TW, TH, Color><<<numTiles, L::kThreads, smem, s>>>(f, keyCap);
+    return cudaGetLastError();
+}
+
+template <class Color>
+static cudaError_t launch_raster_c(const Frame& f, int numTiles, int keyCap, cudaStream_t s)
+{
+    if (f.tileW == 16 && f.tileH == 16) return launch_raster_t<16, 16, Color>(f, numTiles, keyCap, s);
+    if (f.tileW == 32 && f.tileH == 16) return launch_raster_t<32, 16, Color>(f, numTiles, keyCap, s);
+    if (f.tileW == 64 && f.tileH == 32) return launch_raster_t<64, 32, Color>(f, numTiles, keyCap, s);
+    if (f.tileW == 64 && f.tileH == 64) return launch_raster_t<64, 64, Color>(f, numTiles, keyCap, s);
+    if (f.tileW == 8 && f.tileH == 8) return launch_raster_t<8, 8, Color>(f, numTiles, keyCap, s);
+    return launch_raster_t<32, 32, Color>(f, numTiles, keyCap, s);
+}
+
+cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEvent_t* ev)
+{
+    const int numTiles = f.tilesX * f.tilesY;
+    if (ev) cudaEventRecord(ev[0], s);
+    if (f.numSlots > 0)
+    {
+        const unsigned blocks = (unsigned)((f.numSlots + 127) / 128);
+        vs_setup_kernel<<<blocks, 128, 0, s>>>(f);
+    }
+    if (ev) cudaEventRecord(ev[1], s);
+    tile_scan_kernel<<<1, 1024, 0, s>>>(f, numTiles);
+    if (ev) cudaEventRecord(ev[2], s);
+    if (f.numSlots > 0)
+    {
+        const unsigned blocks = (unsigned)((f.numSlots + 255) / 256);
+        bin_fill_kernel<<<blocks, 256, 0, s>>>(f);
+    }
+    if (ev) cudaEventRecord(ev[3], s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    switch (f.colorType)
+    {
+        case SLG_COLOR_RGBA_FLOAT: e = launch_raster_c<ColorRGBAF>(f, numTiles, keyCap, s); break;
+        case SLG_COLOR_R_FLOAT:    e = launch_raster_c<ColorRF>(f, numTiles, keyCap, s); break;
+        default:                   e = launch_raster_c<ColorRGBA8>(f, numTiles, keyCap, s); break;
+    }
+    if (ev) cudaEventRecord(ev[4], s);
+    return e;
+}
+
+cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[4], cudaStream_t s)
+{
+    const uint4 v = make_uint4(value[0], value[1], value[2], value[3]);
+    const unsigned blocks = (unsigned)std::min<size_t>((numTexels + 255) / 256, 152u * 16u);
+    clear_kernel<<<blocks ? blocks : 1, 256, 0, s>>>(dst, numTexels, bytesPerTexel, v);
+    return cudaGetLastError();
+}
+
+} // namespace slg

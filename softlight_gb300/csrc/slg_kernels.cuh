@@ -1,0 +1,23 @@
+/*
+ * slg_kernels.cuh - host-side entry points of the draw-path kernels.
+ */
+#ifndef SLG_KERNELS_CUH
+#define SLG_KERNELS_CUH
+
+#include <cuda_runtime.h>
+#include "slg_device.cuh"
+
+namespace slg
+{
+
+/* Enqueue vs_setup, tile_scan, bin_fill and raster for one launch on s.
+ * When ev is not null, ev[0..4] are recorded before vs_setup, after
+ * vs_setup, after tile_scan, after bin_fill and after raster. */
+cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEvent_t* ev);
+
+/* Fill numTexels texels of 4 or 16 bytes with value. */
+cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[4], cudaStream_t s);
+
+} // namespace slg
+
+#endif /* SLG_KERNELS_CUH */

@@ -1,0 +1,105 @@
+"""Small seeded workloads for edge cases of the draw path (test-only)."""
+import math
+
+import numpy as np
+
+from softlight_gb300 import api as A
+from softlight_gb300 import scenes as S
+
+
+def random_soup(ctx, num_tris=300, width=96, height=80, seed=11, blend=A.BLEND_OFF,
+                depth_test=A.DEPTH_TEST_LESS_THAN, depth_mask=A.DEPTH_MASK_ON, cull=A.CULL_BACK_FACE,
+                color_type=A.COLOR_RGBA_8U, program=A.PROGRAM_VCOLOR_TEX_ALPHA, indexed=None, clear_depth=1.0,
+                max_area=None):
+    """Triangle soup like the c3 workload at a small size, with the pipeline
+    state as parameters. indexed: None (non-indexed) or a numpy index dtype."""
+    s = S.Scene(ctx, f"soup_{seed}", width, height, color_type=color_type)
+    verts, proj = S.soup_triangles(num_tris, width, height, seed=seed)
+    if max_area is not None:
+        pass
+    if indexed is None:
+        mesh = s.add_mesh(verts, None, stride=36)
+    else:
+        n = verts.shape[0]
+        perm = np.random.default_rng(seed + 1).permutation(n)
+        inv = np.empty_like(perm)
+        inv[perm] = np.arange(n)
+        shuffled = verts[perm]
+        idx = inv.astype(indexed)
+        if np.dtype(indexed).itemsize == 1:
+            assert n <= 256
+        mesh = s.add_mesh(shuffled, idx, stride=36)
+    if program == A.PROGRAM_VCOLOR_TEXF:
+        tex = s.add_texture_rgbaf(S.value_noise(64, 64, seed=seed, octaves=2).astype(np.float32))
+    else:
+        tex = s.add_texture_rgba8(S.to_rgba8(S.value_noise(64, 64, seed=seed, octaves=2, alpha=1.0)))
+    ub = S.vcolor_uniforms(proj, tex)
+    sh = s.add_shader(program, 2, ub, cull=cull, depth_test=depth_test, depth_mask=depth_mask, blend=blend)
+    s.draws.append((mesh, 1, sh))
+    s.num_triangles = num_tris
+    s.clear_depth = clear_depth
+    return s
+
+
+def big_triangles(ctx, width=300, height=200, seed=5):
+    """A few triangles spanning many tiles (long catch-up chains), one of
+    them screen-filling, plus equal-depth overlaps (order ties)."""
+    s = S.Scene(ctx, "big", width, height)
+    rng = np.random.default_rng(seed)
+    tris = []
+    for k in range(6):
+        z = -5.0 if k < 3 else -5.0 - k
+        p = rng.uniform(-6, 6, (3, 2))
+        tris.append([(p[0, 0], p[0, 1], z), (p[1, 0], p[1, 1], z), (p[2, 0], p[2, 1], z)])
+    tris.append([(-50, -50, -8.0), (50, -50, -8.0), (0, 60, -8.0)])
+    verts = []
+    for t in tris:
+        c = rng.uniform(0.2, 1.0, 4)
+        for v in t:
+            verts.append([*v, *c, *rng.uniform(0, 1, 2)])
+    verts = np.asarray(verts, dtype=np.float32)
+    mesh = s.add_mesh(verts, None, stride=36)
+    tex = s.add_texture_rgba8(S.checker(32, 32, 4))
+    proj = S.perspective(60.0, width / height, 0.1, 100.0)
+    sh = s.add_shader(A.PROGRAM_VCOLOR_TEX_ALPHA, 2, S.vcolor_uniforms(proj, tex), cull=A.CULL_OFF)
+    s.draws.append((mesh, 1, sh))
+    s.num_triangles = len(tris)
+    return s
+
+
+def multi_draw(ctx, width=128, height=96, batched=False, seed=21):
+    """Several draws with different programs and depth states into one frame,
+    issued one by one or as one batch."""
+    s = S.Scene(ctx, "multi", width, height)
+    verts, idx = S.uv_sphere(16, 8)
+    sphere = s.add_mesh(verts, idx)
+    tex = s.add_texture_rgba8(S.checker(64, 64, 8))
+    vp = S.perspective(60.0, width / height, 0.1, 100.0) @ S.look_at((0, 0, 6), (0, 0, 0), (0, 1, 0))
+    light = np.asarray([0.2, 0.9, 0.4]) / np.linalg.norm([0.2, 0.9, 0.4])
+    rng = np.random.default_rng(seed)
+    for k in range(5):
+        model = S.translate(rng.uniform(-2, 2, 3)) @ S.random_rotation(rng) @ S.scale(rng.uniform(0.5, 1.5))
+        ub = S.lambert_uniforms(vp, model, [*light, 0.0], [0.1, 0.1, 0.1, 0.0], tex)
+        sh = s.add_shader(A.PROGRAM_LAMBERT_TEX, 2, ub,
+                          depth_test=(A.DEPTH_TEST_LESS_THAN, A.DEPTH_TEST_LESS_EQUAL)[k % 2])
+        s.draws.append((sphere, 1, sh))
+    soup, proj = S.soup_triangles(60, width, height, seed=seed)
+    mesh = s.add_mesh(soup, None, stride=36)
+    sh = s.add_shader(A.PROGRAM_VCOLOR_TEX_ALPHA, 2, S.vcolor_uniforms(proj, tex), blend=A.BLEND_ALPHA)
+    s.draws.append((mesh, 1, sh))
+    s.batched = batched
+    return s
+
+
+def flat_triangle(ctx, width=640, height=480):
+    """The reference's headless draw test scene shape: one triangle, flat colour,
+    depth test off (softlight/tests/sl_draw_test.cpp:108-194)."""
+    s = S.Scene(ctx, "flat", width, height)
+    verts = np.asarray([[-0.9, -0.9, 0.0, 0, 0, 0, 0, 0, 0],
+                        [0.9, -0.9, 0.0, 0, 0, 0, 0, 0, 0],
+                        [0.0, 0.9, 0.0, 0, 0, 0, 0, 0, 0]], dtype=np.float32)
+    mesh = s.add_mesh(verts, None, stride=36)
+    sh = s.add_shader(A.PROGRAM_FLAT_COLOR, 0, S.flat_uniforms(np.eye(4), (1.0, 0.5, 0.25, 1.0)),
+                      cull=A.CULL_OFF, depth_test=A.DEPTH_TEST_OFF, depth_mask=A.DEPTH_MASK_OFF)
+    s.draws.append((mesh, 1, sh))
+    return s

@@ -1,0 +1,39 @@
+"""Helpers shared by the parity tests: build one workload on the GPU library
+and on the CPU oracle with identical calls, render, and compare.
+
+Parity bar (stated by the benchmark spec for this path): coverage and depth bit-exact;
+colour within 1 LSB per RGBA8 channel or 1e-5 relative for float targets.
+The implementations are designed to agree exactly, and the tests also report
+how many colour values differ at all.
+"""
+import numpy as np
+
+RGBA8_TOL = 1          # LSB per channel
+FLOAT_RTOL = 1e-5      # relative, float colour targets
+
+
+def render_both(builder, gpu_ctx, oracle_ctx, frames=1, **kw):
+    sg = builder(gpu_ctx, **kw)
+    so = builder(oracle_ctx, **kw)
+    for _ in range(frames):
+        sg.render()
+        so.render()
+    gpu_ctx.finish()
+    return sg, so
+
+
+def compare_scenes(sg, so, label=""):
+    cg, co = sg.read_color(), so.read_color()
+    dg, do = sg.read_depth(), so.read_depth()
+    # depth: bit-exact (covers coverage and depth-test outcomes)
+    bad = dg.view(np.uint32) != do.view(np.uint32)
+    assert not bad.any(), f"{label}: {int(bad.sum())} depth texels differ, first at {np.argwhere(bad)[:3].tolist()}"
+    if cg.dtype == np.uint8:
+        diff = np.abs(cg.astype(np.int16) - co.astype(np.int16))
+        assert diff.max(initial=0) <= RGBA8_TOL, f"{label}: colour differs by {diff.max()} LSB at {np.argwhere(diff > RGBA8_TOL)[:3].tolist()}"
+        return int((diff > 0).sum())
+    scale = np.maximum(np.abs(co), 1e-30)
+    rel = np.abs(cg - co) / scale
+    ok = (np.abs(cg - co) <= FLOAT_RTOL * scale) | (cg == co) | (np.isnan(cg) & np.isnan(co))
+    assert ok.all(), f"{label}: float colour rel err {np.nanmax(rel)}"
+    return int((cg.view(np.uint32) != co.view(np.uint32)).sum())

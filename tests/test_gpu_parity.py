@@ -1,0 +1,145 @@
+"""GPU parity tests: the CUDA draw path (through the C ABI) against the CPU
+oracle on identical seeded inputs. Coverage and depth must be bit-exact,
+colour within 1 LSB (RGBA8) or 1e-5 relative (float)."""
+import numpy as np
+import pytest
+
+from softlight_gb300 import api as A
+from softlight_gb300 import scenes as S
+
+import edge_scenes as E
+from parity import compare_scenes, render_both
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture()
+def ctxs(gpu_lib, oracle_mod):
+    g = gpu_lib.Context()
+    o = oracle_mod.Context()
+    yield g, o
+    g.close()
+    o.close()
+
+
+def test_c1_sphere_exact(ctxs):
+    g, o = ctxs
+    sg, so = render_both(S.build_c1, g, o)
+    assert compare_scenes(sg, so, "c1") == 0
+    assert (sg.read_depth() < 1.0).sum() > 50000
+
+
+def test_c1_two_frames_and_rerender(ctxs):
+    g, o = ctxs
+    sg, so = render_both(S.build_c1, g, o, frames=3)
+    assert compare_scenes(sg, so, "c1x3") == 0
+
+
+@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 16), (32, 32), (64, 32), (64, 64)])
+def test_c1_all_tile_sizes(ctxs, tile):
+    g, o = ctxs
+    g.set_tile_size(*tile)
+    sg, so = render_both(S.build_c1, g, o, width=333, height=211)
+    assert compare_scenes(sg, so, f"c1 tile {tile}") == 0
+
+
+def test_c2_instanced_small(ctxs):
+    g, o = ctxs
+    sg, so = render_both(S.build_c2, g, o, num_instances=48, width=480, height=270, tex_size=256)
+    assert compare_scenes(sg, so, "c2 small") == 0
+
+
+def test_c3_soup_small_blend_clip(ctxs):
+    g, o = ctxs
+    sg, so = render_both(S.build_c3, g, o, num_tris=3000, width=320, height=180, tex_size=256)
+    assert compare_scenes(sg, so, "c3 small") == 0
+
+
+def test_c4_batched_small(ctxs):
+    g, o = ctxs
+    sg, so = render_both(S.build_c4, g, o, num_draws=12, width=400, height=240, tex_size=64)
+    assert compare_scenes(sg, so, "c4 small") == 0
+
+
+@pytest.mark.parametrize("depth_test", range(7))
+@pytest.mark.parametrize("depth_mask", [0, 1])
+def test_depth_functions(ctxs, depth_test, depth_mask):
+    g, o = ctxs
+    sg, so = render_both(E.random_soup, g, o, depth_test=depth_test, depth_mask=depth_mask, clear_depth=0.5, frames=2)
+    compare_scenes(sg, so, f"depth {depth_test}/{depth_mask}")
+
+
+@pytest.mark.parametrize("blend", [A.BLEND_ALPHA, A.BLEND_PREMULTIPLED_ALPHA, A.BLEND_ADDITIVE, A.BLEND_SCREEN])
+@pytest.mark.parametrize("fmt", [A.COLOR_RGBA_8U, A.COLOR_RGBA_FLOAT])
+def test_blend_modes(ctxs, blend, fmt):
+    g, o = ctxs
+    sg, so = render_both(E.random_soup, g, o, blend=blend, color_type=fmt, num_tris=400)
+    compare_scenes(sg, so, f"blend {blend} fmt {fmt}")
+
+
+@pytest.mark.parametrize("cull", [A.CULL_BACK_FACE, A.CULL_FRONT_FACE, A.CULL_OFF])
+def test_cull_modes(ctxs, cull):
+    g, o = ctxs
+    sg, so = render_both(E.random_soup, g, o, cull=cull)
+    compare_scenes(sg, so, f"cull {cull}")
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.uint16, np.uint32])
+def test_index_types(ctxs, dtype):
+    g, o = ctxs
+    sg, so = render_both(E.random_soup, g, o, indexed=dtype, num_tris=80)
+    compare_scenes(sg, so, f"index {np.dtype(dtype).name}")
+
+
+def test_float_target_and_texture(ctxs):
+    g, o = ctxs
+    sg, so = render_both(E.random_soup, g, o, program=A.PROGRAM_VCOLOR_TEXF, color_type=A.COLOR_RGBA_FLOAT)
+    compare_scenes(sg, so, "texf")
+
+
+def test_big_triangles_and_ties(ctxs):
+    g, o = ctxs
+    for tile in [(8, 8), (32, 32), (64, 64)]:
+        g.set_tile_size(*tile)
+        sg, so = render_both(E.big_triangles, g, o)
+        assert compare_scenes(sg, so, f"big {tile}") == 0
+
+
+@pytest.mark.parametrize("batched", [False, True])
+def test_multi_draw(ctxs, batched):
+    g, o = ctxs
+    sg, so = render_both(E.multi_draw, g, o, batched=batched)
+    compare_scenes(sg, so, f"multi batched={batched}")
+
+
+def test_batched_equals_per_draw(gpu_lib):
+    a, b = gpu_lib.Context(), gpu_lib.Context()
+    sa = S.build_c4(a, num_draws=20, width=320, height=200, tex_size=32, batched=True)
+    sb = S.build_c4(b, num_draws=20, width=320, height=200, tex_size=32, batched=False)
+    sa.render()
+    sb.render()
+    assert np.array_equal(sa.read_color(), sb.read_color())
+    assert np.array_equal(sa.read_depth().view(np.uint32), sb.read_depth().view(np.uint32))
+
+
+def test_flat_triangle_draw_test_scene(ctxs):
+    g, o = ctxs
+    sg, so = render_both(E.flat_triangle, g, o)
+    assert compare_scenes(sg, so, "flat") == 0
+    img = sg.read_color()
+    assert (img[..., 0] == 255).sum() > 100000
+
+
+def test_empty_and_degenerate_draws(ctxs):
+    g, o = ctxs
+    for ctx in (g, o):
+        s = S.build_c1(ctx, width=64, height=48)
+        s.render()
+        mesh = s.draws[0][0]
+        empty = A.Mesh(mesh.vaoId, 0, 0, mesh.mode, 0)
+        ctx.draw(empty, s.draws[0][2], s.fbo)
+        ctx.draw_instanced(mesh, 0, s.draws[0][2], s.fbo)
+        ctx.finish()
+    # invalid ids are rejected, not executed
+    with pytest.raises(A.SLError):
+        g.draw(A.Mesh(999, 0, 3, A.RENDER_MODE_TRIANGLES, 0), 0, 0)
