@@ -11,6 +11,7 @@
  * draws.
  */
 #include <algorithm>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -37,7 +38,7 @@ struct DevBuffer
 };
 
 struct Vbo { DevBuffer buf; size_t size = 0; };
-struct Ibo { DevBuffer buf; int type = SLG_VERTEX_DATA_INVALID; size_t count = 0; };
+struct Ibo { DevBuffer buf; int type = SLG_VERTEX_DATA_INVALID; size_t count = 0; uint64_t maxIndex = 0; };
 struct Binding { ptrdiff_t offset = 0, stride = 0; unsigned comps = 0; int type = 0; };
 struct Vao { size_t vbo = SLG_INVALID_ID, ibo = SLG_INVALID_ID; Binding bindings[8]; };
 struct Texture { DevBuffer buf; int type = -1; uint16_t w = 0, h = 0, d = 0; unsigned bpt = 0; };
@@ -47,7 +48,7 @@ struct Fbo
     size_t colors[4] = {SLG_INVALID_ID, SLG_INVALID_ID, SLG_INVALID_ID, SLG_INVALID_ID};
     size_t depth = SLG_INVALID_ID;
 };
-struct Ubo { DevBuffer buf; };
+struct Ubo { DevBuffer buf; uint8_t shadow[1024] = {}; };
 struct Shader
 {
     uint8_t cull, depthTest, depthMask, blend, numVaryings, numOutputs;
@@ -340,6 +341,83 @@ void viewport_setup(float fboW, float fboH, float scissor[16], float viewport[4]
     viewport[3] = mn(mn(65535.f, (0.f + 65535.f) - vy), fboH - vy);
 }
 
+/* Bytes a program reads per vertex at binding 0 (include/slg_programs.h). */
+size_t program_vertex_bytes(uint32_t program)
+{
+    switch (program)
+    {
+        case SLG_PROGRAM_LAMBERT_TEX:
+        case SLG_PROGRAM_BLINN_PHONG_INST: return 32;
+        case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
+        case SLG_PROGRAM_VCOLOR_TEXF:      return 36;
+        default:                           return 12;
+    }
+}
+
+bool texture_ok(const slg_context* ctx, uint32_t id, int type)
+{
+    return id < ctx->textures.size() && ctx->textures[id].buf.ptr && ctx->textures[id].type == type;
+}
+
+/* Host-side bounds checks of everything a draw's kernels will read: the
+ * vertex range, the index range and the resource ids stored in the uniform
+ * block. The reference performs none (SL_Context::draw, SL_Context.cpp:714);
+ * here an invalid draw is rejected before any kernel is launched. */
+int validate_draw(slg_context* ctx, const Shader& sh, const Vao& vao, const slg_mesh& m, size_t numInstances, size_t numElements)
+{
+    const Vbo& vbo = ctx->vbos[vao.vbo];
+    const Binding& b0 = vao.bindings[0];
+    if (b0.offset < 0 || b0.stride <= 0) return ctx->fail(SLG_ERR_INVALID_ARG, "binding 0 needs offset >= 0 and stride > 0");
+    const uint64_t lastElement = m.elementBegin + 3 * ((numElements + 2) / 3) - 1;
+    uint64_t maxVertex;
+    if (m.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES)
+    {
+        const Ibo& ibo = ctx->ibos[vao.ibo];
+        if (m.elementEnd > ibo.count) return ctx->fail(SLG_ERR_INVALID_ARG, "element range exceeds the index buffer");
+        maxVertex = ibo.maxIndex;
+    }
+    else
+    {
+        maxVertex = lastElement;
+    }
+    const uint64_t need = (uint64_t)b0.offset + (uint64_t)b0.stride * maxVertex + program_vertex_bytes(sh.vsProgram);
+    if (need > vbo.size + 64) return ctx->fail(SLG_ERR_INVALID_ARG, "vertex range exceeds the vertex buffer");
+
+    if (sh.ubo == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "built-in programs need a uniform block");
+    const uint8_t* u = ctx->ubos[sh.ubo].shadow;
+    uint32_t tex = 0, buf = 0;
+    switch (sh.fsProgram)
+    {
+        case SLG_PROGRAM_LAMBERT_TEX:
+            std::memcpy(&tex, u + offsetof(slg_lambert_uniforms, textureId), 4);
+            if (!texture_ok(ctx, tex, SLG_COLOR_RGBA_8U)) return ctx->fail(SLG_ERR_INVALID_ARG, "uniform textureId is not an RGBA8 texture");
+            break;
+        case SLG_PROGRAM_BLINN_PHONG_INST:
+            std::memcpy(&tex, u + offsetof(slg_blinn_uniforms, textureId), 4);
+            if (!texture_ok(ctx, tex, SLG_COLOR_RGBA_8U)) return ctx->fail(SLG_ERR_INVALID_ARG, "uniform textureId is not an RGBA8 texture");
+            break;
+        case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
+            std::memcpy(&tex, u + offsetof(slg_vcolor_uniforms, textureId), 4);
+            if (!texture_ok(ctx, tex, SLG_COLOR_RGBA_8U)) return ctx->fail(SLG_ERR_INVALID_ARG, "uniform textureId is not an RGBA8 texture");
+            break;
+        case SLG_PROGRAM_VCOLOR_TEXF:
+            std::memcpy(&tex, u + offsetof(slg_vcolor_uniforms, textureId), 4);
+            if (!texture_ok(ctx, tex, SLG_COLOR_RGBA_FLOAT)) return ctx->fail(SLG_ERR_INVALID_ARG, "uniform textureId is not an RGBA float texture");
+            break;
+        default:
+            break;
+    }
+    if (sh.vsProgram == SLG_PROGRAM_BLINN_PHONG_INST)
+    {
+        std::memcpy(&buf, u + offsetof(slg_blinn_uniforms, instanceBufferId), 4);
+        if (buf >= ctx->vbos.size() || !ctx->vbos[buf].buf.ptr || ctx->vbos[buf].size < 64 * (uint64_t)numInstances)
+            return ctx->fail(SLG_ERR_INVALID_ARG, "uniform instanceBufferId does not hold one matrix per instance");
+    }
+    if (sh.vsProgram == SLG_PROGRAM_BLINN_PHONG_INST && sh.fsProgram != SLG_PROGRAM_BLINN_PHONG_INST)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "program pair not supported");
+    return SLG_OK;
+}
+
 struct DrawRequest
 {
     slg_mesh mesh;
@@ -361,6 +439,13 @@ int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, Draw
     const bool indexed = (m.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES);
     if (indexed && (vao.ibo == SLG_INVALID_ID || !ctx->ibos[vao.ibo].buf.ptr))
         return ctx->fail(SLG_ERR_INVALID_ARG, "indexed draw without index buffer");
+
+    const size_t numElements = (m.elementEnd > m.elementBegin) ? (m.elementEnd - m.elementBegin) : 0;
+    if (numElements && req.numInstances)
+    {
+        int r = validate_draw(ctx, sh, vao, m, req.numInstances, numElements);
+        if (r) return r;
+    }
 
     std::memset(&d, 0, sizeof(d));
     d.vbo = static_cast<const uint8_t*>(ctx->vbos[vao.vbo].buf.ptr);
@@ -576,6 +661,15 @@ int slg_ibo_init(slg_context* ctx, size_t id, size_t numElements, int indexType,
     if (r) return r;
     v.type = indexType;
     v.count = numElements;
+    v.maxIndex = 0;
+    for (size_t i = 0; data && i < numElements; ++i)
+    {
+        uint64_t x;
+        if (ib == 1) x = static_cast<const uint8_t*>(data)[i];
+        else if (ib == 2) { uint16_t t; std::memcpy(&t, static_cast<const uint8_t*>(data) + 2 * i, 2); x = t; }
+        else { uint32_t t; std::memcpy(&t, static_cast<const uint8_t*>(data) + 4 * i, 4); x = t; }
+        v.maxIndex = std::max(v.maxIndex, x);
+    }
     if (data && numElements)
     {
         cudaError_t e = cudaMemcpyAsync(v.buf.ptr, data, numElements * ib, cudaMemcpyHostToDevice, ctx->stream);
@@ -696,6 +790,7 @@ size_t slg_create_ubo(slg_context* ctx)
 int slg_ubo_assign(slg_context* ctx, size_t id, const void* data, size_t numBytes)
 {
     if (!id_ok(id, ctx->ubos.size()) || numBytes > 1024 || (!data && numBytes)) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid ubo");
+    std::memcpy(ctx->ubos[id].shadow, data, numBytes);
     cudaError_t e = cudaMemcpyAsync(ctx->ubos[id].buf.ptr, data, numBytes, cudaMemcpyHostToDevice, ctx->stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "ubo assign");
     return SLG_OK;
