@@ -38,6 +38,7 @@ def parse():
     p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    p.add_argument("--tile", default="32x32", help="screen tile WxH (8x8 .. 64x64)")
     return p.parse_args()
 
 
@@ -209,6 +210,8 @@ def run_gpu(args):
     sg.build()
     builder, kwargs, cfg = workload_config(args.workload)
     ctx = sg.Context()
+    tw, th = (int(v) for v in args.tile.split("x"))
+    ctx.set_tile_size(tw, th)
     scene = builder(ctx, **kwargs)
     stream = torch.cuda.ExternalStream(ctx.stream_handle())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -303,7 +306,7 @@ def run_gpu(args):
 
     if rank == 0:
         cfg = dict(cfg)
-        cfg.update({"l2": "flushed between timed frames (256 MiB write)", "tile": "32x32",
+        cfg.update({"l2": "flushed between timed frames (256 MiB write)", "tile": args.tile,
                     "triangles_per_frame": scene.num_triangles})
         line = {"metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,

@@ -243,6 +243,12 @@ int slg_set_tile_size(slg_context* ctx, int tileW, int tileH);
 int slg_profile_stages(slg_context* ctx, int enable);
 int slg_stage_times(slg_context* ctx, float ms[4]);
 
+/* Raster strategy: 0 (default) picks the order-free resolve for launches
+ * without blending and with one order-independent depth rule, else the
+ * ordered per-pixel replay; 1 forces the ordered replay. Both give the same
+ * image. */
+int slg_set_raster_mode(slg_context* ctx, int mode);
+
 #ifdef __cplusplus
 }
 #endif

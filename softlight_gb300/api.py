@@ -98,6 +98,7 @@ _GPU_SIGNATURES = [
     ("set_tile_size", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("profile_stages", C.c_int, [C.c_void_p, C.c_int]),
     ("stage_times", C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    ("set_raster_mode", C.c_int, [C.c_void_p, C.c_int]),
 ]
 
 
@@ -292,6 +293,9 @@ class SLContext:
 
     def profile_stages(self, enable=True):
         self._call("profile_stages", 1 if enable else 0)
+
+    def set_raster_mode(self, mode):
+        self._call("set_raster_mode", mode)
 
     def stage_times(self):
         ms = (C.c_float * 4)()

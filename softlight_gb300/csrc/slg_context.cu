@@ -92,6 +92,7 @@ struct slg_context
     unsigned numThreads = 1;
     int tileW = 32, tileH = 32;
     int keyCap = 16384;
+    bool forceOrdered = false;
 
     std::vector<Vbo> vbos;
     std::vector<Ibo> ibos;
@@ -550,6 +551,19 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     f.draws = devDescs;
     f.drawSlotStart = devStarts;
     f.numDraws = (int32_t)n;
+    /* order-free raster when nothing blends and every draw uses the same
+     * order-independent depth rule (NOT_EQUAL depends on order) */
+    f.orderFree = 1;
+    f.freeDepthFunc = descs[0].depthTest;
+    f.freeDepthMask = descs[0].depthMask;
+    for (size_t i = 0; i < n; ++i)
+    {
+        if (descs[i].blend != SLG_BLEND_OFF || descs[i].depthTest == SLG_DEPTH_TEST_NOT_EQUAL ||
+            descs[i].depthTest != f.freeDepthFunc || descs[i].depthMask != f.freeDepthMask || ctx->forceOrdered)
+        {
+            f.orderFree = 0;
+        }
+    }
     f.tables.textures = static_cast<const TexView*>(ctx->texTable.ptr);
     f.tables.buffers = static_cast<const uint8_t* const*>(ctx->bufTable.ptr);
 
@@ -893,6 +907,13 @@ int slg_set_tile_size(slg_context* ctx, int tileW, int tileH)
     cudaStreamSynchronize(ctx->stream);
     ctx->tileW = tileW;
     ctx->tileH = tileH;
+    return SLG_OK;
+}
+
+int slg_set_raster_mode(slg_context* ctx, int mode)
+{
+    if (mode != 0 && mode != 1) return ctx->fail(SLG_ERR_INVALID_ARG, "raster mode must be 0 or 1");
+    ctx->forceOrdered = (mode == 1);
     return SLG_OK;
 }
 

@@ -112,6 +112,12 @@ struct Frame
     const uint64_t* drawSlotStart; /* numDraws + 1 */
     int32_t numDraws;
     Tables tables;
+
+    /* raster mode of the launch: order-free when no draw blends and all
+     * draws share one order-independent depth rule */
+    int32_t orderFree;
+    int32_t freeDepthFunc;
+    int32_t freeDepthMask;
 };
 
 enum StatusBits

@@ -117,11 +117,11 @@ __device__ __forceinline__ bool bin_visible(const float4 p0, const float4 p1, co
  *   r2 = (bc0.xyz, bc.w)             r3 = (bc1.xyz, z0)
  *   r4 = (bc2.xyz, z1)               r5 = (z2, w0, w1, w2)
  *   r6 = (minY, maxY, minX-1, maxX+1) as int32 bits
- *   r7 = (draw index, primIndex lo, primIndex hi, 0) as uint32 bits */
+ *   r7 = (draw index, primIndex lo, primIndex hi, depth test | mask << 4) as uint32 bits */
 struct Record { float4 r[kRecordVec4]; };
 
 __device__ __forceinline__ void make_record(const float4 p0, const float4 p1, const float4 p2, uint32_t drawIndex,
-                                            uint64_t primIndex, Record& rec)
+                                            uint64_t primIndex, uint32_t depthFlags, Record& rec)
 {
     const float xyx = p0.x - p1.x, xyy = p0.y - p1.y;
     const float zyx = p2.x - p1.x, zyy = p2.y - p1.y;
@@ -156,7 +156,7 @@ __device__ __forceinline__ void make_record(const float4 p0, const float4 p1, co
     rec.r[6] = make_float4(__int_as_float(f2i(minY)), __int_as_float(f2i(maxY)),
                            __int_as_float(f2i(minX) - 1), __int_as_float(f2i(maxX) + 1));
     rec.r[7] = make_float4(__uint_as_float(drawIndex), __uint_as_float((uint32_t)primIndex),
-                           __uint_as_float((uint32_t)(primIndex >> 32)), 0.f);
+                           __uint_as_float((uint32_t)(primIndex >> 32)), __uint_as_float(depthFlags));
 }
 
 /* Inclusive tile range touched by a record; empty when tx1 < tx0 or ty1 < ty0. */
@@ -341,7 +341,7 @@ __device__ __noinline__ uint32_t clip_and_emit(const Frame& f, const DrawDesc& d
             continue;
         }
         Record rec;
-        make_record(a, b, c, drawIndex, primIndex, rec);
+        make_record(a, b, c, drawIndex, primIndex, (uint32_t)d.depthTest | ((uint32_t)d.depthMask << 4), rec);
         const uint64_t recIndex = f.numSlots + base + sub;
         store_record(f, recIndex, rec);
         store_varyings(f, recIndex, nv, newVarys, newVarys + (i + 1) * 4, newVarys + (i + 2) * 4);
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(128) vs_setup_kernel(const Frame f)
         if (bin_visible(s0, s1, s2))
         {
             Record rec;
-            make_record(s0, s1, s2, (uint32_t)di, primIndex, rec);
+            make_record(s0, s1, s2, (uint32_t)di, primIndex, (uint32_t)d.depthTest | ((uint32_t)d.depthMask << 4), rec);
             store_record(f, slot, rec);
             store_varyings(f, slot, d.numVaryings, vary, vary + 4, vary + 8);
             count_tiles(rec.r[6], f);
@@ -659,29 +659,185 @@ __device__ void sort_keys(uint32_t* s, int n)
     }
 }
 
+/* Per-triangle constants a thread needs for one scan-line. */
+struct Span
+{
+    int32_t xMin, xMax;
+};
+
+/* SL_ScanlineBounds::step, portable branch (SL_ScanlineBounds.hpp:301-321) */
+__device__ __forceinline__ Span scanline_span(const float4 r0, const float4 r1, float yf)
+{
+    const float d0 = yf - r0.x;
+    const float d1 = yf - r0.y;
+    const float alpha = d0 * r1.x;
+    const int32_t lo = f2i(r1.y * alpha + r0.z);
+    const int32_t sa = f2i(r1.z * d1 + r0.w);
+    const int32_t sb = f2i(r1.w * d0 + r0.z);
+    const int32_t hi = (d1 < 0.f) ? sa : sb;
+    Span s;
+    s.xMin = (lo >= hi) ? hi : lo;
+    s.xMax = (lo >= hi) ? lo : hi;
+    return s;
+}
+
+/* One thread's walk over the pixels x = xs + 4g of a scan-line span that lie
+ * in [xFirst, xEnd): the incremental barycentrics of
+ * SL_TriRasterizer.cpp:856-911 replayed exactly (bc0*xs + bcY, then one
+ * addition of 4*bc0 per step, including the steps left of the tile). */
+struct Chain
+{
+    float b0, b1, b2;       /* barycentrics at the current pixel */
+    float s0, s1, s2;       /* 4 * bc0 */
+    int x, xEnd;
+};
+
+__device__ __forceinline__ bool chain_begin(const float4* R, float yf, int myX0, int xLimit, Chain& ch)
+{
+    const Span sp = scanline_span(R[0], R[1], yf);
+    if (!((uint32_t)sp.xMin < (uint32_t)sp.xMax))
+    {
+        return false;
+    }
+    const int xEnd = min(sp.xMax, xLimit);
+    const int xs = sp.xMin + ((myX0 - sp.xMin) & 3);
+    const int xFirst = max(xs, myX0);
+    if (xFirst >= xEnd)
+    {
+        return false;
+    }
+    const float4 r2 = R[2], r3 = R[3], r4 = R[4];
+    const float bcY0 = r3.x * yf + r4.x;
+    const float bcY1 = r3.y * yf + r4.y;
+    const float bcY2 = r3.z * yf + r4.z;
+    const float xsf = (float)xs;
+    ch.b0 = r2.x * xsf + bcY0;
+    ch.b1 = r2.y * xsf + bcY1;
+    ch.b2 = r2.z * xsf + bcY2;
+    ch.s0 = r2.x * 4.f;
+    ch.s1 = r2.y * 4.f;
+    ch.s2 = r2.z * 4.f;
+    for (int g = (xFirst - xs) >> 2; g > 0; --g)
+    {
+        ch.b0 += ch.s0;
+        ch.b1 += ch.s1;
+        ch.b2 += ch.s2;
+    }
+    ch.x = xFirst;
+    ch.xEnd = xEnd;
+    return true;
+}
+
+__device__ __forceinline__ void chain_step(Chain& ch)
+{
+    ch.b0 += ch.s0;
+    ch.b1 += ch.s1;
+    ch.b2 += ch.s2;
+    ch.x += 4;
+}
+
+/* z = dot(depth, bc) with depth.w = 0 (SL_TriRasterizer.cpp:880) */
+__device__ __forceinline__ float chain_depth(const float4* R, const Chain& ch)
+{
+    const float4 r2 = R[2], r3 = R[3], r4 = R[4], r5 = R[5];
+    return __fadd_rn((r3.w * ch.b0 + r4.w * ch.b1) + r5.x * ch.b2, 0.f * r2.w);
+}
+
+/* Perspective correction, varying interpolation and the fragment program of
+ * SL_FragmentProcessor::flush_tri_fragments (SL_FragmentProcessor.cpp:463-529,
+ * interpolate_tri_varyings :308-330). Returns whether colour is written. */
+__device__ __forceinline__ bool shade(const Frame& f, const DrawDesc& dd, uint64_t rec, float bcw, const float4 r5,
+                                      float b0, float b1, float b2, float4& out)
+{
+    const float bp0 = b0 * r5.y, bp1 = b1 * r5.z, bp2 = b2 * r5.w;
+    const float bp3 = bcw * 0.f;
+    const float persp = 1.f / (((bp0 + bp1) + bp2) + bp3);
+    const float q0 = bp0 * persp, q1 = bp1 * persp, q2 = bp2 * persp;
+
+    slg_v4 vary[4];
+    const float4* V = f.varyings + rec * kVaryingVec4;
+    for (int vi = 0; vi < dd.numVaryings; ++vi)
+    {
+        const float4 a = V[vi], b = V[4 + vi], c = V[8 + vi];
+        vary[vi] = slg_make_v4((a.x * q0 + b.x * q1) + c.x * q2, (a.y * q0 + b.y * q1) + c.y * q2,
+                               (a.z * q0 + b.z * q1) + c.z * q2, (a.w * q0 + b.w * q1) + c.w * q2);
+    }
+    slg_v4 outputs[4];
+    const DevEnv env = make_env(dd, f.tables);
+    const bool have = run_fragment_program(dd.fsProgram, env, vary, outputs);
+    out = to_f4(outputs[0]);
+    return have && dd.numOutputs > 0;
+}
+
 template <int TW, int TH, class Color>
 struct RasterLayout
 {
     static constexpr int kThreads = TH * 4;
     static constexpr int kStride = TW + 4;       /* row pitch of the tile buffers (bank spread) */
-    static constexpr int kBatch = 32;            /* records staged per step */
-    static constexpr size_t kColorBytes = sizeof(typename Color::stored) * TH * kStride;
-    static constexpr size_t kDepthBytes = sizeof(float) * TH * kStride;
+    static constexpr int kBatch = 64;            /* records staged per step */
+    static constexpr int kPix = TH * kStride;
     static constexpr size_t kRecBytes = sizeof(float4) * kBatch * kRecordVec4;
-    static constexpr size_t fixed_bytes() { return kColorBytes + kDepthBytes + kRecBytes + 2 * sizeof(uint32_t) * kBatch; }
+    /* ordered path: colour + depth tile, records, record ids, then keys */
+    static constexpr size_t ordered_bytes() { return sizeof(typename Color::stored) * kPix + sizeof(float) * kPix + kRecBytes + 2 * sizeof(uint32_t) * kBatch; }
+    /* order-free path: records + keys, then d0, z, key, b0, b1, b2 per pixel */
+    static constexpr size_t free_bytes() { return kRecBytes + sizeof(uint32_t) * kBatch + 6 * sizeof(float) * kPix; }
 };
 
+/* Stages records [b0, b0+cnt) of the tile list into shared memory. */
+template <int Batch>
+__device__ __forceinline__ void stage_records(const Frame& f, const uint32_t* keys, int cnt, float4* sRec, uint32_t* sKey)
+{
+    for (int i = threadIdx.x; i < cnt * kRecordVec4; i += blockDim.x)
+    {
+        const int ri = i / kRecordVec4, part = i % kRecordVec4;
+        const uint32_t key = keys[ri];
+        if (part == 0) sKey[ri] = key;
+        sRec[i] = f.records[key_to_record(f, key) * kRecordVec4 + part];
+    }
+}
+
+/* The warp owns rows [bandY0, bandY0 + 8): the 32 lanes test 32 staged
+ * records at once against that band and the warp walks only the hits, in
+ * order (ballot + find-first-set compaction). */
+template <class Fn>
+__device__ __forceinline__ void for_band_records(const float4* sRec, int cnt, int bandY0, Fn&& fn)
+{
+    const int lane = threadIdx.x & 31;
+    for (int base = 0; base < cnt; base += 32)
+    {
+        const int ri = base + lane;
+        bool hit = false;
+        if (ri < cnt)
+        {
+            const float4 r6 = sRec[ri * kRecordVec4 + 6];
+            hit = __float_as_int(r6.x) < bandY0 + 8 && __float_as_int(r6.y) > bandY0;
+        }
+        unsigned mask = __ballot_sync(0xFFFFFFFFu, hit);
+        while (mask)
+        {
+            const int j = __ffs(mask) - 1;
+            mask &= mask - 1;
+            fn(base + j);
+        }
+    }
+}
+
+/*-----------------------------------------------------------------------------
+ * Ordered raster: blending or order-dependent depth state. Keys are sorted
+ * and every thread applies, for the pixels it owns, each fragment in
+ * submission order: depth test, fragment program, blend, depth write.
+-----------------------------------------------------------------------------*/
 template <int TW, int TH, class Color>
-__global__ void __launch_bounds__(TH * 4) raster_kernel(const Frame f, int keyCap)
+__global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f, int keyCap)
 {
     typedef RasterLayout<TW, TH, Color> L;
     typedef typename Color::stored Stored;
     extern __shared__ __align__(16) uint8_t smem[];
     Stored*   sColor = reinterpret_cast<Stored*>(smem);
-    float*    sDepth = reinterpret_cast<float*>(smem + L::kColorBytes);
-    float4*   sRec   = reinterpret_cast<float4*>(smem + L::kColorBytes + L::kDepthBytes);
-    uint32_t* sRecIx = reinterpret_cast<uint32_t*>(smem + L::kColorBytes + L::kDepthBytes + L::kRecBytes);
-    uint32_t* sKeys  = sRecIx + 2 * L::kBatch;
+    float*    sDepth = reinterpret_cast<float*>(smem + sizeof(Stored) * L::kPix);
+    float4*   sRec   = reinterpret_cast<float4*>(smem + sizeof(Stored) * L::kPix + sizeof(float) * L::kPix);
+    uint32_t* sRecKey = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(sRec) + L::kRecBytes);
+    uint32_t* sKeys  = sRecKey + 2 * L::kBatch;
 
     const int tile = blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
@@ -703,7 +859,6 @@ __global__ void __launch_bounds__(TH * 4) raster_kernel(const Frame f, int keyCa
     __syncthreads();
     sort_keys(sKeys, (int)n);
 
-    /* tile load */
     for (int i = threadIdx.x; i < TW * TH; i += blockDim.x)
     {
         const int px = i % TW, py = i / TW;
@@ -724,131 +879,53 @@ __global__ void __launch_bounds__(TH * 4) raster_kernel(const Frame f, int keyCa
     const int xLimit = min(x0 + TW, f.width);
     const bool rowActive = (y < f.height);
     const float yf = (float)y;
+    const int bandY0 = y0 + ((threadIdx.x >> 5) << 3);
 
     for (uint32_t b0 = 0; b0 < n; b0 += L::kBatch)
     {
         const int cnt = (int)min((uint32_t)L::kBatch, n - b0);
-        if (threadIdx.x < cnt)
-        {
-            sRecIx[threadIdx.x] = (uint32_t)key_to_record(f, sKeys[b0 + threadIdx.x]);
-        }
-        __syncthreads();
-        for (int i = threadIdx.x; i < cnt * kRecordVec4; i += blockDim.x)
-        {
-            const int ri = i / kRecordVec4, part = i % kRecordVec4;
-            sRec[i] = f.records[(uint64_t)sRecIx[ri] * kRecordVec4 + part];
-        }
+        stage_records<L::kBatch>(f, sKeys + b0, cnt, sRec, sRecKey);
         __syncthreads();
 
-        for (int ri = 0; ri < cnt && rowActive; ++ri)
-        {
+        for_band_records(sRec, cnt, bandY0, [&](int ri) {
             const float4* R = sRec + ri * kRecordVec4;
             const float4 r6 = R[6];
-            if (y < __float_as_int(r6.x) || y >= __float_as_int(r6.y))
+            if (!rowActive || y < __float_as_int(r6.x) || y >= __float_as_int(r6.y))
             {
-                continue;
+                return;
             }
-
-            /* SL_ScanlineBounds::step, portable branch (SL_ScanlineBounds.hpp:301-321) */
-            const float4 r0 = R[0], r1 = R[1];
-            const float d0 = yf - r0.x;
-            const float d1 = yf - r0.y;
-            const float alpha = d0 * r1.x;
-            const int32_t lo = f2i(r1.y * alpha + r0.z);
-            const int32_t sa = f2i(r1.z * d1 + r0.w);
-            const int32_t sb = f2i(r1.w * d0 + r0.z);
-            const int32_t hi = (d1 < 0.f) ? sa : sb;
-            const int32_t xMin = (lo >= hi) ? hi : lo;
-            const int32_t xMax = (lo >= hi) ? lo : hi;
-            if (!((uint32_t)xMin < (uint32_t)xMax))
+            Chain ch;
+            if (!chain_begin(R, yf, myX0, xLimit, ch))
             {
-                continue;
+                return;
             }
-
-            const int xEnd = min(xMax, xLimit);
-            const int xs = xMin + ((myX0 - xMin) & 3);   /* first pixel of this thread's chain */
-            const int xFirst = max(xs, myX0);
-            if (xFirst >= xEnd)
-            {
-                continue;
-            }
-
-            /* incremental barycentrics (SL_TriRasterizer.cpp:856-911): the
-             * value at pixel x is bc0*xs + bcY plus (x-xs)/4 sequential
-             * additions of 4*bc0, replayed exactly */
-            const float4 r2 = R[2], r3 = R[3], r4 = R[4];
-            const float bcY0 = r3.x * yf + r4.x;
-            const float bcY1 = r3.y * yf + r4.y;
-            const float bcY2 = r3.z * yf + r4.z;
-            const float xsf = (float)xs;
-            float b0v = r2.x * xsf + bcY0;
-            float b1v = r2.y * xsf + bcY1;
-            float b2v = r2.z * xsf + bcY2;
-            const float bx0 = r2.x * 4.f, bx1 = r2.y * 4.f, bx2 = r2.z * 4.f;
-            for (int g = (xFirst - xs) >> 2; g > 0; --g)
-            {
-                b0v += bx0;
-                b1v += bx1;
-                b2v += bx2;
-            }
-
-            const float zw = 0.f * r2.w;
-            const float z0 = r3.w, z1 = r4.w;
-            const float4 r5 = R[5];
+            const uint32_t flags = __float_as_uint(R[7].w);
+            const int depthFunc = flags & 0xF;
+            const bool depthMask = (flags >> 4) & 1;
             const uint32_t drawIndex = __float_as_uint(R[7].x);
-            const DrawDesc& dd = f.draws[drawIndex];
-            const int depthFunc = dd.depthTest;
-
-            for (int x = xFirst; x < xEnd; x += 4)
+            for (; ch.x < ch.xEnd; chain_step(ch))
             {
-                const float z = __fadd_rn(((z0 * b0v + z1 * b1v) + r5.x * b2v), zw);
-                const int idx = r * L::kStride + (x - x0);
+                const float z = chain_depth(R, ch);
+                const int idx = r * L::kStride + (ch.x - x0);
                 if (depth_cmp(depthFunc, z, sDepth[idx]))
                 {
-                    /* flush_tri_fragments (SL_FragmentProcessor.cpp:463-529) */
-                    const float bp0 = b0v * r5.y, bp1 = b1v * r5.z, bp2 = b2v * r5.w;
-                    const float bp3 = r2.w * 0.f;
-                    const float persp = 1.f / (((bp0 + bp1) + bp2) + bp3);
-                    const float q0 = bp0 * persp, q1 = bp1 * persp, q2 = bp2 * persp;
-
-                    slg_v4 vary[4];
-                    const float4* V = f.varyings + (uint64_t)sRecIx[ri] * kVaryingVec4;
-                    for (int vi = 0; vi < dd.numVaryings; ++vi)
+                    const DrawDesc& dd = f.draws[drawIndex];
+                    float4 o;
+                    if (shade(f, dd, key_to_record(f, sRecKey[ri]), R[2].w, R[5], ch.b0, ch.b1, ch.b2, o) && f.color)
                     {
-                        const float4 a = V[vi], b = V[4 + vi], cc = V[8 + vi];
-                        vary[vi] = slg_make_v4((a.x * q0 + b.x * q1) + cc.x * q2, (a.y * q0 + b.y * q1) + cc.y * q2,
-                                               (a.z * q0 + b.z * q1) + cc.z * q2, (a.w * q0 + b.w * q1) + cc.w * q2);
+                        sColor[idx] = (dd.blend != SLG_BLEND_OFF) ? Color::store(blend_color(dd.blend, o, Color::load(sColor[idx])))
+                                                                  : Color::store(o);
                     }
-
-                    slg_v4 outputs[4];
-                    const DevEnv env = make_env(dd, f.tables);
-                    const bool haveOutputs = run_fragment_program(dd.fsProgram, env, vary, outputs);
-                    if (haveOutputs && dd.numOutputs > 0 && f.color)
-                    {
-                        const float4 o = to_f4(outputs[0]);
-                        if (dd.blend != SLG_BLEND_OFF)
-                        {
-                            sColor[idx] = Color::store(blend_color(dd.blend, o, Color::load(sColor[idx])));
-                        }
-                        else
-                        {
-                            sColor[idx] = Color::store(o);
-                        }
-                    }
-                    if (dd.depthMask == SLG_DEPTH_MASK_ON)
+                    if (depthMask)
                     {
                         sDepth[idx] = z;
                     }
                 }
-                b0v += bx0;
-                b1v += bx1;
-                b2v += bx2;
             }
-        }
+        });
         __syncthreads();
     }
 
-    /* tile store */
     for (int i = threadIdx.x; i < TW * TH; i += blockDim.x)
     {
         const int px = i % TW, py = i / TW;
@@ -858,6 +935,155 @@ __global__ void __launch_bounds__(TH * 4) raster_kernel(const Frame f, int keyCa
             const size_t gi = (size_t)gx + (size_t)f.width * gy;
             f.depth[gi] = sDepth[py * L::kStride + px];
             if (f.color) Color::write(f.color, gi, sColor[py * L::kStride + px]);
+        }
+    }
+}
+
+/*-----------------------------------------------------------------------------
+ * Order-free raster: no blending and one of the depth rules below for every
+ * draw of the launch. The outcome of SoftLight's sequential per-pixel loop
+ * (test against the current depth, write depth, overwrite colour) is then a
+ * function of the fragment set alone:
+ *   depth mask on,  LESS          : min z, ties -> earliest key
+ *   depth mask on,  LESS_EQUAL    : min z, ties -> latest key
+ *   depth mask on,  GREATER       : max z, ties -> earliest key
+ *   depth mask on,  GREATER_EQUAL : max z, ties -> latest key
+ *   depth mask on,  EQUAL         : latest key with z == d0
+ *   any mask,       OFF           : latest key
+ *   depth mask off, LT/LE/GT/GE/EQ: latest key passing against d0
+ * (every built-in program writes colour unconditionally). Each thread keeps
+ * the winning (z, key, barycentrics) of the pixels it owns while the records
+ * stream by in any order, and shades each pixel once at the end.
+-----------------------------------------------------------------------------*/
+__device__ __forceinline__ bool free_wins(int func, bool mask, float z, uint32_t key, float d0, float bz, uint32_t bkey)
+{
+    const bool none = (bkey == 0xFFFFFFFFu);
+    if (func == SLG_DEPTH_TEST_OFF)
+    {
+        return none || key > bkey;
+    }
+    if (!mask)
+    {
+        return depth_cmp(func, z, d0) && (none || key > bkey);
+    }
+    switch (func)
+    {
+        case SLG_DEPTH_TEST_LESS_THAN:     return none ? (z < d0) : (z < bz || (z == bz && key < bkey));
+        case SLG_DEPTH_TEST_LESS_EQUAL:    return none ? (z <= d0) : (z < bz || (z == bz && key > bkey));
+        case SLG_DEPTH_TEST_GREATER_THAN:  return none ? (z > d0) : (z > bz || (z == bz && key < bkey));
+        case SLG_DEPTH_TEST_GREATER_EQUAL: return none ? (z >= d0) : (z > bz || (z == bz && key > bkey));
+        default:                           return (z == d0) && (none || key > bkey);
+    }
+}
+
+template <int TW, int TH, class Color>
+__global__ void __launch_bounds__(TH * 4) raster_free_kernel(const Frame f, int depthFunc, int depthMask)
+{
+    typedef RasterLayout<TW, TH, Color> L;
+    extern __shared__ __align__(16) uint8_t smem[];
+    float4*   sRec  = reinterpret_cast<float4*>(smem);
+    uint32_t* sRecKey = reinterpret_cast<uint32_t*>(smem + L::kRecBytes);
+    float*    sD0   = reinterpret_cast<float*>(sRecKey + L::kBatch);
+    float*    sZ    = sD0 + L::kPix;
+    uint32_t* sBest = reinterpret_cast<uint32_t*>(sZ + L::kPix);
+    float*    sB0   = reinterpret_cast<float*>(sBest + L::kPix);
+    float*    sB1   = sB0 + L::kPix;
+    float*    sB2   = sB1 + L::kPix;
+
+    const int tile = blockIdx.x;
+    const uint32_t begin = f.tileOffset[tile];
+    const uint32_t n = f.tileOffset[tile + 1] - begin;
+    if (n == 0 || (f.status[0] & kStatusEntryOverflow))
+    {
+        return;
+    }
+    const int tx = tile % f.tilesX, ty = tile / f.tilesX;
+    const int x0 = tx * TW, y0 = ty * TH;
+    const int r = threadIdx.x >> 2;
+    const int c = threadIdx.x & 3;
+    const int y = y0 + r;
+    const int myX0 = x0 + c;
+    const int xLimit = min(x0 + TW, f.width);
+    const bool rowActive = (y < f.height);
+    const float yf = (float)y;
+    const int bandY0 = y0 + ((threadIdx.x >> 5) << 3);
+    const bool mask = depthMask != 0;
+
+    /* each thread initialises the pixels it owns */
+    if (rowActive)
+    {
+        for (int x = myX0; x < xLimit; x += 4)
+        {
+            const int idx = r * L::kStride + (x - x0);
+            sD0[idx] = f.depth[(size_t)x + (size_t)f.width * y];
+            sBest[idx] = 0xFFFFFFFFu;
+        }
+    }
+
+    for (uint32_t b0 = 0; b0 < n; b0 += L::kBatch)
+    {
+        const int cnt = (int)min((uint32_t)L::kBatch, n - b0);
+        __syncthreads();
+        stage_records<L::kBatch>(f, f.entries + begin + b0, cnt, sRec, sRecKey);
+        __syncthreads();
+
+        for_band_records(sRec, cnt, bandY0, [&](int ri) {
+            const float4* R = sRec + ri * kRecordVec4;
+            const float4 r6 = R[6];
+            if (!rowActive || y < __float_as_int(r6.x) || y >= __float_as_int(r6.y))
+            {
+                return;
+            }
+            Chain ch;
+            if (!chain_begin(R, yf, myX0, xLimit, ch))
+            {
+                return;
+            }
+            const uint32_t key = sRecKey[ri];
+            for (; ch.x < ch.xEnd; chain_step(ch))
+            {
+                const float z = chain_depth(R, ch);
+                const int idx = r * L::kStride + (ch.x - x0);
+                if (free_wins(depthFunc, mask, z, key, sD0[idx], sZ[idx], sBest[idx]))
+                {
+                    sZ[idx] = z;
+                    sBest[idx] = key;
+                    sB0[idx] = ch.b0;
+                    sB1[idx] = ch.b1;
+                    sB2[idx] = ch.b2;
+                }
+            }
+        });
+    }
+
+    /* resolve: shade each owned pixel's winner once */
+    if (!rowActive)
+    {
+        return;
+    }
+    for (int x = myX0; x < xLimit; x += 4)
+    {
+        const int idx = r * L::kStride + (x - x0);
+        const uint32_t key = sBest[idx];
+        if (key == 0xFFFFFFFFu)
+        {
+            continue;
+        }
+        const size_t gi = (size_t)x + (size_t)f.width * y;
+        const uint64_t rec = key_to_record(f, key);
+        const float4* R = f.records + rec * kRecordVec4;
+        const DrawDesc& dd = f.draws[__float_as_uint(R[7].x)];
+        if (f.color && dd.numOutputs > 0)
+        {
+            float4 o;
+            if (shade(f, dd, rec, R[2].w, R[5], sB0[idx], sB1[idx], sB2[idx], o))
+            {
+                Color::write(f.color, gi, Color::store(o));
+            }
+        }
+        if (mask)
+        {
+            f.depth[gi] = sZ[idx];
         }
     }
 }
@@ -882,10 +1108,21 @@ template <int TW, int TH, class Color>
 static cudaError_t launch_raster_t(const Frame& f, int numTiles, int keyCap, cudaStream_t s)
 {
     typedef RasterLayout<TW, TH, Color> L;
-    const size_t smem = L::fixed_bytes() + sizeof(uint32_t) * (size_t)keyCap;
-    cudaError_t e = cudaFuncSetAttribute(raster_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    raster_kernel<TW, TH, Color><<<numTiles, L::kThreads, smem, s>>>(f, keyCap);
+    cudaError_t e;
+    if (f.orderFree)
+    {
+        const size_t smem = L::free_bytes();
+        e = cudaFuncSetAttribute(raster_free_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        raster_free_kernel<TW, TH, Color><<<numTiles, L::kThreads, smem, s>>>(f, f.freeDepthFunc, f.freeDepthMask);
+    }
+    else
+    {
+        const size_t smem = L::ordered_bytes() + sizeof(uint32_t) * (size_t)keyCap;
+        e = cudaFuncSetAttribute(raster_ordered_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        raster_ordered_kernel<TW, TH, Color><<<numTiles, L::kThreads, smem, s>>>(f, keyCap);
+    }
     return cudaGetLastError();
 }
 

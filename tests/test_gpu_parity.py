@@ -29,6 +29,30 @@ def test_c1_sphere_exact(ctxs):
     assert (sg.read_depth() < 1.0).sum() > 50000
 
 
+@pytest.mark.parametrize("mode", [0, 1])
+def test_raster_modes_agree(ctxs, mode):
+    """Order-free resolve (mode 0) and the ordered replay (mode 1) both match."""
+    g, o = ctxs
+    g.set_raster_mode(mode)
+    sg, so = render_both(S.build_c2, g, o, num_instances=24, width=320, height=200, tex_size=128)
+    assert compare_scenes(sg, so, f"c2 mode {mode}") == 0
+    sg, so = render_both(E.multi_draw, g, o)
+    compare_scenes(sg, so, f"multi mode {mode}")
+
+
+@pytest.mark.parametrize("depth_test", [1, 2, 3, 4, 5, 0])
+@pytest.mark.parametrize("depth_mask", [0, 1])
+def test_order_free_depth_rules(ctxs, depth_test, depth_mask):
+    """Opaque draws take the order-free path; every depth rule it accepts must
+    reproduce the sequential result, ties included."""
+    g, o = ctxs
+    sg, so = render_both(E.random_soup, g, o, depth_test=depth_test, depth_mask=depth_mask, clear_depth=0.5,
+                         frames=2, num_tris=500)
+    compare_scenes(sg, so, f"free depth {depth_test}/{depth_mask}")
+    sg, so = render_both(E.big_triangles, g, o)
+    compare_scenes(sg, so, "free big")
+
+
 def test_c1_two_frames_and_rerender(ctxs):
     g, o = ctxs
     sg, so = render_both(S.build_c1, g, o, frames=3)
