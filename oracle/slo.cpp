@@ -181,6 +181,7 @@ struct slo_context
     std::vector<Ubo*> ubos;
     std::vector<Shader> shaders;
     uint64_t lastBins = 0, lastFrags = 0;
+    std::vector<Bin> lastBinList; /* bins of the last draw group, kept for debugging */
 
     ~slo_context()
     {
@@ -1274,6 +1275,7 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
         }
 
         order_bins(bins, blending);
+        ctx->lastBinList = bins;
         totalBins += bins.size();
 
         if (nthreads == 1)
@@ -1342,6 +1344,22 @@ int slo_draw_batch(slo_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, s
 }
 
 int slo_finish(slo_context*) { return SLG_OK; }
+
+/* Copies the last draw group's bins: per bin 12 floats of screen
+ * coordinates (x, y, z, w for the three vertices) and the primIndex as a
+ * float. Returns the number of bins available. */
+size_t slo_debug_bins(const slo_context* ctx, float* out, size_t maxBins)
+{
+    const size_t n = ctx->lastBinList.size();
+    for (size_t i = 0; i < n && i < maxBins; ++i)
+    {
+        const Bin& b = ctx->lastBinList[i];
+        for (int v = 0; v < 3; ++v)
+            for (int c = 0; c < 4; ++c) out[i * 13 + v * 4 + c] = b.screen[v][c];
+        out[i * 13 + 12] = (float)b.primIndex;
+    }
+    return n;
+}
 
 void slo_last_stats(const slo_context* ctx, uint64_t* numBins, uint64_t* numFragments)
 {
