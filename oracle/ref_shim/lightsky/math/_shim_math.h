@@ -155,6 +155,8 @@ inline int sign_mask(int32_t i) noexcept { return (int)((uint32_t)i >> 31); }
 /*-----------------------------------------------------------------------------
  * vectors
 -----------------------------------------------------------------------------*/
+#define LS_EPSILON 1.0e-6f
+
 #define LS_SHIM_VEC_COMMON(N)                                                                          \
     typedef T value_type;                                                                              \
     static constexpr unsigned num_components() noexcept { return N; }                                 \
@@ -203,7 +205,7 @@ struct vec3_t
 };
 
 template <typename T>
-struct vec4_t
+union vec4_t
 {
     typedef vec4_t vecN_t;
     T v[4];
@@ -211,6 +213,10 @@ struct vec4_t
     constexpr vec4_t(T s) noexcept : v{s, s, s, s} {}
     constexpr vec4_t(T a, T b, T c, T d) noexcept : v{a, b, c, d} {}
     template <typename U> explicit constexpr operator vec4_t<U>() const noexcept { return vec4_t<U>{(U)v[0], (U)v[1], (U)v[2], (U)v[3]}; }
+    /* the address of a vec4 is the address of its first component (the
+     * reference passes &vec4 where a float pointer is expected) */
+    T* operator&() noexcept { return v; }
+    const T* operator&() const noexcept { return v; }
     LS_SHIM_VEC_COMMON(4)
 };
 
@@ -315,17 +321,17 @@ inline int sign_mask(const vec4_t<int>& a) noexcept
 }
 
 /* vector casts */
-template <typename T> constexpr vec2_t<T> vec2_cast(const vec3_t<T>& a) noexcept { return vec2_t<T>{a.v[0], a.v[1]}; }
-template <typename T> constexpr vec2_t<T> vec2_cast(const vec4_t<T>& a) noexcept { return vec2_t<T>{a.v[0], a.v[1]}; }
-template <typename U, typename T> constexpr vec2_t<U> vec2_cast(const vec4_t<T>& a) noexcept { return vec2_t<U>{(U)a.v[0], (U)a.v[1]}; }
-template <typename U, typename T> constexpr vec2_t<U> vec2_cast(const vec3_t<T>& a) noexcept { return vec2_t<U>{(U)a.v[0], (U)a.v[1]}; }
-template <typename T> constexpr vec3_t<T> vec3_cast(const vec4_t<T>& a) noexcept { return vec3_t<T>{a.v[0], a.v[1], a.v[2]}; }
+template <typename U, typename T> using ls_cast_t = typename std::conditional<std::is_void<U>::value, T, U>::type;
+template <typename U = void, typename T> constexpr vec2_t<ls_cast_t<U, T>> vec2_cast(const vec3_t<T>& a) noexcept
+{ return vec2_t<ls_cast_t<U, T>>{(ls_cast_t<U, T>)a.v[0], (ls_cast_t<U, T>)a.v[1]}; }
+template <typename U = void, typename T> constexpr vec2_t<ls_cast_t<U, T>> vec2_cast(const vec4_t<T>& a) noexcept
+{ return vec2_t<ls_cast_t<U, T>>{(ls_cast_t<U, T>)a.v[0], (ls_cast_t<U, T>)a.v[1]}; }
+template <typename U = void, typename T> constexpr vec3_t<ls_cast_t<U, T>> vec3_cast(const vec4_t<T>& a) noexcept
+{ return vec3_t<ls_cast_t<U, T>>{(ls_cast_t<U, T>)a.v[0], (ls_cast_t<U, T>)a.v[1], (ls_cast_t<U, T>)a.v[2]}; }
 template <typename T> constexpr vec3_t<T> vec3_cast(const vec2_t<T>& a, typename ls_ident<T>::type z) noexcept { return vec3_t<T>{a.v[0], a.v[1], z}; }
-template <typename U, typename T> constexpr vec3_t<U> vec3_cast(const vec4_t<T>& a) noexcept { return vec3_t<U>{(U)a.v[0], (U)a.v[1], (U)a.v[2]}; }
 template <typename T> constexpr vec4_t<T> vec4_cast(const vec3_t<T>& a, typename ls_ident<T>::type w) noexcept { return vec4_t<T>{a.v[0], a.v[1], a.v[2], w}; }
 template <typename T> constexpr vec4_t<T> vec4_cast(const vec2_t<T>& a, typename ls_ident<T>::type z, typename ls_ident<T>::type w) noexcept { return vec4_t<T>{a.v[0], a.v[1], z, w}; }
 template <typename T> constexpr vec4_t<T> vec4_cast(typename ls_ident<T>::type x, const vec2_t<T>& a, typename ls_ident<T>::type w) noexcept { return vec4_t<T>{x, a.v[0], a.v[1], w}; }
-template <typename U, typename T> constexpr vec4_t<U> vec4_cast(const vec3_t<T>& a, U w) noexcept { return vec4_t<U>{(U)a.v[0], (U)a.v[1], (U)a.v[2], w}; }
 
 /*-----------------------------------------------------------------------------
  * matrices (column-major)

@@ -15,7 +15,7 @@
 #include <type_traits>
 #include <utility>
 
-#define LS_INLINE inline
+#define LS_INLINE __attribute__((always_inline))
 #define LS_IMPERATIVE
 #define LS_API
 #define LS_RESTRICT_PTR __restrict__

@@ -70,6 +70,24 @@ template <typename T> struct AlignedPointerDeleter
 template <typename T, typename D = std::default_delete<T>>
 using Pointer = std::unique_ptr<T, D>;
 
+/* std allocator returning 64-byte aligned storage */
+template <typename T>
+struct AlignedAllocator
+{
+    typedef T value_type;
+    AlignedAllocator() noexcept = default;
+    template <typename U> AlignedAllocator(const AlignedAllocator<U>&) noexcept {}
+    T* allocate(std::size_t n)
+    {
+        void* p = aligned_malloc(sizeof(T) * n);
+        if (!p) throw std::bad_alloc();
+        return static_cast<T*>(p);
+    }
+    void deallocate(T* p, std::size_t) noexcept { aligned_free(p); }
+    template <typename U> bool operator==(const AlignedAllocator<U>&) const noexcept { return true; }
+    template <typename U> bool operator!=(const AlignedAllocator<U>&) const noexcept { return false; }
+};
+
 template <typename T>
 using UniqueAlignedArray = std::unique_ptr<T[], AlignedArrayDeleter<T>>;
 
@@ -146,8 +164,6 @@ class WorkerThread
     {
         mThread = std::thread([this]() { run(); });
     }
-
-    WorkerThread() : WorkerThread(0) {}
 
     ~WorkerThread()
     {

@@ -1,0 +1,86 @@
+"""The CPU oracle against golden fixtures produced by SoftLight's own draw-path
+sources (tests/golden/make_golden.py), and - where the reference tree is
+present - against the reference build directly. These pin the oracle: the
+fixtures are the reference's outputs on the same seeded inputs."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import golden_scenes as G
+from golden.make_golden import digest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+REF_TREE = "/root/reference/softlight"
+
+
+def load(name):
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return d["color"], d["depth"]
+
+
+def same(a, b):
+    if a.dtype == np.float32:
+        return np.array_equal(a.view(np.uint32), b.view(np.uint32)) or \
+            (np.array_equal(np.isnan(a), np.isnan(b)) and
+             np.array_equal(np.where(np.isnan(a), 0, a).view(np.uint32), np.where(np.isnan(b), 0, b).view(np.uint32)))
+    return np.array_equal(a, b)
+
+
+def test_index_matches_fixtures():
+    with open(os.path.join(GOLDEN, "index.json")) as fh:
+        index = json.load(fh)
+    assert set(index) == set(G.SCENES)
+    for name, meta in index.items():
+        c, d = load(name)
+        assert digest(c) == meta["color_sha256"], name
+        assert digest(d) == meta["depth_sha256"], name
+
+
+@pytest.mark.parametrize("name", sorted(G.SCENES))
+def test_oracle_matches_reference_golden(oracle_mod, name):
+    builder, kw = G.SCENES[name]
+    ctx = oracle_mod.Context()
+    scene = builder(ctx, **kw)
+    scene.render()
+    gc, gd = load(name)
+    c, d = scene.read_color(), scene.read_depth()
+    assert same(d, gd), f"{name}: depth differs from the reference in {int((d != gd).sum())} texels"
+    assert same(c, gc), f"{name}: colour differs from the reference"
+    ctx.close()
+
+
+@pytest.mark.parametrize("threads", [2, 5])
+def test_oracle_threads_match_one_thread(oracle_mod, threads):
+    """The oracle's multi-threaded mode (used for the CPU baseline timing)
+    reproduces the one-thread result."""
+    from softlight_gb300 import scenes as S
+    ref = oracle_mod.Context(num_threads=1)
+    par = oracle_mod.Context(num_threads=threads)
+    a = S.build_c2(ref, num_instances=4, width=200, height=120, tex_size=64)
+    b = S.build_c2(par, num_instances=4, width=200, height=120, tex_size=64)
+    a.render()
+    b.render()
+    assert np.array_equal(a.read_color(), b.read_color())
+    assert same(a.read_depth(), b.read_depth())
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_TREE), reason="reference tree not present")
+@pytest.mark.parametrize("name", ["c1_sphere_160x120", "c3_soup_2000_160x96", "multi_draw", "soup_not_equal"])
+def test_reference_build_matches_oracle_live(oracle_mod, name):
+    """Builds the reference sources (oracle/ref_build.py) and renders live."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(HERE), "oracle"))
+    import ref_build
+    from softlight_gb300.api import SLContext, open_library
+    lib = open_library(ref_build.build_ref(), "slr_", gpu=False)
+    builder, kw = G.SCENES[name]
+    r = SLContext(lib, "slr_", gpu=False)
+    o = oracle_mod.Context()
+    sr, so = builder(r, **kw), builder(o, **kw)
+    sr.render()
+    so.render()
+    assert same(sr.read_depth(), so.read_depth())
+    assert same(sr.read_color(), so.read_color())
