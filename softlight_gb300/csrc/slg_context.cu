@@ -91,7 +91,7 @@ struct slg_context
     cudaStream_t stream = nullptr;
     unsigned numThreads = 1;
     int tileW = 32, tileH = 32;
-    int keyCap = 16384;
+    int keyCap = 32768;   /* largest sortable tile list (128 KB of shared memory) */
     bool forceOrdered = false;
 
     std::vector<Vbo> vbos;

@@ -193,6 +193,38 @@ __device__ __forceinline__ void count_tiles(const float4 r6, const Frame& f)
     }
 }
 
+/* Walks each lane's tile range in lock-step; lanes that hit the same tile in
+ * the same step are grouped with __match_any_sync and one atomic per group
+ * adds (or reserves) the group's size. fn(tile, groupBase + rankInGroup) is
+ * called per lane and tile when `reserve` points at per-tile cursors; with
+ * reserve == nullptr only the counts are added. Every lane of the warp must
+ * call this. */
+template <class Fn>
+__device__ __forceinline__ void warp_tile_walk(const Frame& f, TileRange t, bool valid, uint32_t* counters, Fn&& fn)
+{
+    const unsigned lane = threadIdx.x & 31;
+    bool active = valid && t.tx1 >= t.tx0 && t.ty1 >= t.ty0;
+    int tx = t.tx0, ty = t.ty0;
+    while (__any_sync(0xFFFFFFFFu, active))
+    {
+        const uint32_t tile = active ? (uint32_t)(ty * f.tilesX + tx) : 0xFFFFFFFFu;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, tile);
+        if (active)
+        {
+            const unsigned leader = __ffs(peers) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(&counters[tile], (uint32_t)__popc(peers));
+            base = __shfl_sync(peers, base, leader);
+            fn(tile, base + __popc(peers & ((1u << lane) - 1u)));
+            if (++tx > t.tx1)
+            {
+                tx = t.tx0;
+                if (++ty > t.ty1) active = false;
+            }
+        }
+    }
+}
+
 __device__ __forceinline__ void store_record(const Frame& f, uint64_t recIndex, const Record& rec)
 {
     float4* dst = f.records + recIndex * kRecordVec4;
@@ -376,14 +408,8 @@ __device__ __forceinline__ uint64_t read_index(const DrawDesc& d, uint64_t i)
  * Kernel 1: vertex processing, clipping, set-up and tile counting
  * (SL_TriProcessor::process_verts, SL_TriProcessor.cpp:527-640)
 -----------------------------------------------------------------------------*/
-__global__ void __launch_bounds__(128) vs_setup_kernel(const Frame f)
+__device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, TileRange& tr, bool& counted)
 {
-    const uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= f.numSlots)
-    {
-        return;
-    }
-
     const int di = (f.numDraws > 1) ? find_draw(f, slot) : 0;
     const DrawDesc& d = f.draws[di];
     const uint64_t local = slot - d.slotBase;
@@ -401,15 +427,13 @@ __global__ void __launch_bounds__(128) vs_setup_kernel(const Frame f)
         clip[k] = to_f4(run_vertex_program(d.vsProgram, env, vid, inst, vary + 4 * k));
     }
 
-    uint32_t info = 0;
     if (d.cull != SLG_CULL_OFF)
     {
         const float det = face_determinant(clip[0], clip[1], clip[2]);
         const bool culled = (d.cull == SLG_CULL_FRONT_FACE) ^ (sign_mask(det) != 0);
         if (culled)
         {
-            f.slotInfo[slot] = 0;
-            return;
+            return 0;
         }
     }
 
@@ -432,15 +456,32 @@ __global__ void __launch_bounds__(128) vs_setup_kernel(const Frame f)
             make_record(s0, s1, s2, (uint32_t)di, primIndex, (uint32_t)d.depthTest | ((uint32_t)d.depthMask << 4), rec);
             store_record(f, slot, rec);
             store_varyings(f, slot, d.numVaryings, vary, vary + 4, vary + 8);
-            count_tiles(rec.r[6], f);
-            info = 1;
+            tr = tile_range(rec.r[6], f);
+            counted = true;
+            return 1;
         }
+        return 0;
     }
-    else if (vis == 1)
+    if (vis == 1)
     {
-        info = clip_and_emit(f, d, (uint32_t)di, slot, primIndex, clip, vary);
+        return clip_and_emit(f, d, (uint32_t)di, slot, primIndex, clip, vary);
     }
-    f.slotInfo[slot] = info;
+    return 0;
+}
+
+__global__ void __launch_bounds__(128) vs_setup_kernel(const Frame f)
+{
+    const uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    TileRange tr;
+    tr.tx0 = 0; tr.tx1 = -1; tr.ty0 = 0; tr.ty1 = -1;
+    bool counted = false;
+    if (slot < f.numSlots)
+    {
+        f.slotInfo[slot] = setup_slot(f, slot, tr, counted);
+    }
+    /* per-tile counts of the unclipped records, one atomic per group of
+     * lanes touching the same tile (clipped records count themselves) */
+    warp_tile_walk(f, tr, counted, f.tileCount, [](uint32_t, uint32_t) {});
 }
 
 /*-----------------------------------------------------------------------------
@@ -448,38 +489,54 @@ __global__ void __launch_bounds__(128) vs_setup_kernel(const Frame f)
 -----------------------------------------------------------------------------*/
 __global__ void __launch_bounds__(1024) tile_scan_kernel(const Frame f, int numTiles)
 {
-    __shared__ uint32_t sSums[1024];
+    __shared__ uint32_t sWarp[32];
+    __shared__ uint32_t sCarry;
     const int tid = threadIdx.x;
-    const int per = (numTiles + 1023) / 1024;
-    const int begin = min(numTiles, tid * per);
-    const int end = min(numTiles, begin + per);
-
-    uint32_t local = 0;
-    for (int t = begin; t < end; ++t) local += f.tileCount[t];
-    sSums[tid] = local;
+    const int lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) sCarry = 0;
     __syncthreads();
 
-    /* Hillis-Steele inclusive scan over 1024 partial sums */
-    for (int off = 1; off < 1024; off <<= 1)
+    /* 1024 tiles per step: coalesced load, warp-shuffle scan, warp sums */
+    for (int base = 0; base < numTiles; base += 1024)
     {
-        const uint32_t v = (tid >= off) ? sSums[tid - off] : 0u;
+        const int t = base + tid;
+        const uint32_t c = (t < numTiles) ? f.tileCount[t] : 0u;
+        uint32_t v = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, v, o);
+            if (lane >= o) v += n;
+        }
+        if (lane == 31) sWarp[warp] = v;
         __syncthreads();
-        sSums[tid] += v;
+        if (warp == 0)
+        {
+            uint32_t w = sWarp[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, w, o);
+                if (lane >= o) w += n;
+            }
+            sWarp[lane] = w;
+        }
+        __syncthreads();
+        const uint32_t carry = sCarry;
+        const uint32_t excl = carry + (warp ? sWarp[warp - 1] : 0u) + v - c;
+        if (t < numTiles)
+        {
+            f.tileOffset[t] = excl;
+            f.tileCursor[t] = excl;
+            f.tileCount[t] = 0;
+        }
+        __syncthreads();
+        if (tid == 1023) sCarry = carry + sWarp[31];
         __syncthreads();
     }
-
-    uint32_t run = sSums[tid] - local;
-    for (int t = begin; t < end; ++t)
+    if (tid == 0)
     {
-        const uint32_t c = f.tileCount[t];
-        f.tileOffset[t] = run;
-        f.tileCursor[t] = run;
-        f.tileCount[t] = 0;
-        run += c;
-    }
-    if (tid == 1023)
-    {
-        const uint32_t total = sSums[1023];
+        const uint32_t total = sCarry;
         f.tileOffset[numTiles] = total;
         if (total > f.entryCap)
         {
@@ -513,21 +570,23 @@ __device__ __forceinline__ void fill_record(const Frame& f, uint64_t recIndex, u
 __global__ void __launch_bounds__(256) bin_fill_kernel(const Frame f)
 {
     const uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= f.numSlots)
-    {
-        return;
-    }
-    const uint32_t info = f.slotInfo[slot];
+    const uint32_t info = (slot < f.numSlots) ? f.slotInfo[slot] : 0u;
+    TileRange tr;
+    tr.tx0 = 0; tr.tx1 = -1; tr.ty0 = 0; tr.ty1 = -1;
     if (info == 1)
     {
-        fill_record(f, slot, (uint32_t)(slot << kSubShift));
+        tr = tile_range(f.records[slot * kRecordVec4 + 6], f);
     }
-    else if (info >= 2)
+    const uint32_t key = (uint32_t)(slot << kSubShift);
+    warp_tile_walk(f, tr, info == 1, f.tileCursor, [&](uint32_t, uint32_t pos) {
+        if (pos < f.entryCap) f.entries[pos] = key;
+    });
+    if (info >= 2)
     {
         const uint32_t base = f.slotOvf[slot];
         for (uint32_t s = 0; s < info - 2; ++s)
         {
-            fill_record(f, f.numSlots + base + s, (uint32_t)(slot << kSubShift) | (s + 1));
+            fill_record(f, f.numSlots + base + s, key | (s + 1));
         }
     }
 }
@@ -827,8 +886,33 @@ __device__ __forceinline__ void for_band_records(const float4* sRec, int cnt, in
  * and every thread applies, for the pixels it owns, each fragment in
  * submission order: depth test, fragment program, blend, depth write.
 -----------------------------------------------------------------------------*/
+/* Sorts each tile's key list in place (ascending = submission order) for
+ * the ordered raster; one CTA per tile, the list staged in shared memory. */
+__global__ void __launch_bounds__(1024) tile_sort_kernel(const Frame f, int sortCap)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint32_t* sKeys = reinterpret_cast<uint32_t*>(smem);
+    const int tile = blockIdx.x;
+    const uint32_t begin = f.tileOffset[tile];
+    const uint32_t n = f.tileOffset[tile + 1] - begin;
+    if (n < 2 || (f.status[0] & kStatusEntryOverflow))
+    {
+        return;
+    }
+    if ((int)n > sortCap)
+    {
+        if (threadIdx.x == 0) atomicOr(f.status, kStatusTileOverflow);
+        return;
+    }
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) sKeys[i] = f.entries[begin + i];
+    __syncthreads();
+    sort_keys(sKeys, (int)n);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) f.entries[begin + i] = sKeys[i];
+}
+
 template <int TW, int TH, class Color>
-__global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f, int keyCap)
+__global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
 {
     typedef RasterLayout<TW, TH, Color> L;
     typedef typename Color::stored Stored;
@@ -837,27 +921,18 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f, i
     float*    sDepth = reinterpret_cast<float*>(smem + sizeof(Stored) * L::kPix);
     float4*   sRec   = reinterpret_cast<float4*>(smem + sizeof(Stored) * L::kPix + sizeof(float) * L::kPix);
     uint32_t* sRecKey = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(sRec) + L::kRecBytes);
-    uint32_t* sKeys  = sRecKey + 2 * L::kBatch;
 
     const int tile = blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
     const uint32_t n = f.tileOffset[tile + 1] - begin;
-    if (n == 0 || (f.status[0] & kStatusEntryOverflow))
+    if (n == 0 || (f.status[0] & (kStatusEntryOverflow | kStatusTileOverflow)))
     {
         return;
     }
-    if ((int)n > keyCap)
-    {
-        if (threadIdx.x == 0) atomicOr(f.status, kStatusTileOverflow);
-        return;
-    }
+    const uint32_t* sKeys = f.entries + begin; /* sorted by tile_sort_kernel */
 
     const int tx = tile % f.tilesX, ty = tile / f.tilesX;
     const int x0 = tx * TW, y0 = ty * TH;
-
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) sKeys[i] = f.entries[begin + i];
-    __syncthreads();
-    sort_keys(sKeys, (int)n);
 
     for (int i = threadIdx.x; i < TW * TH; i += blockDim.x)
     {
@@ -1118,10 +1193,15 @@ static cudaError_t launch_raster_t(const Frame& f, int numTiles, int keyCap, cud
     }
     else
     {
-        const size_t smem = L::ordered_bytes() + sizeof(uint32_t) * (size_t)keyCap;
+        /* keyCap keys of 4 bytes per tile for the sort (<= 227 KB) */
+        const size_t sortSmem = sizeof(uint32_t) * (size_t)keyCap;
+        e = cudaFuncSetAttribute(tile_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sortSmem);
+        if (e != cudaSuccess) return e;
+        tile_sort_kernel<<<numTiles, 1024, sortSmem, s>>>(f, keyCap);
+        const size_t smem = L::ordered_bytes();
         e = cudaFuncSetAttribute(raster_ordered_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        raster_ordered_kernel<TW, TH, Color><<<numTiles, L::kThreads, smem, s>>>(f, keyCap);
+        raster_ordered_kernel<TW, TH, Color><<<numTiles, L::kThreads, smem, s>>>(f);
     }
     return cudaGetLastError();
 }
