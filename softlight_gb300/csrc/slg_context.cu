@@ -107,7 +107,7 @@ struct slg_context
     bool tablesDirty = true;
 
     /* scratch */
-    DevBuffer records, varyings, slotInfo, slotOvf, ovfCount;
+    DevBuffer records, varyings, slotInfo, slotOvf, ovfCount, clipQueue, clipCount;
     DevBuffer tileCount, tileOffset, tileCursor, entries, status;
     uint64_t slotCap = 0, ovfCap = 0, tileCap = 0, entryCap = 0;
 
@@ -210,6 +210,7 @@ int ensure_scratch(slg_context* ctx, uint64_t numSlots, uint64_t numTiles)
         if ((r = dev_alloc(ctx, ctx->varyings, recs * slg::kVaryingVec4 * sizeof(float4), false))) return r;
         if ((r = dev_alloc(ctx, ctx->slotInfo, cap * sizeof(uint32_t), false))) return r;
         if ((r = dev_alloc(ctx, ctx->slotOvf, cap * sizeof(uint32_t), false))) return r;
+        if ((r = dev_alloc(ctx, ctx->clipQueue, cap * sizeof(uint32_t), false))) return r;
         ctx->slotCap = cap;
         ctx->ovfCap = ovf;
         const uint64_t wantEntries = std::max<uint64_t>(8 * cap, 32u << 20);
@@ -222,6 +223,7 @@ int ensure_scratch(slg_context* ctx, uint64_t numSlots, uint64_t numTiles)
     if (!ctx->ovfCount.ptr)
     {
         if ((r = dev_alloc(ctx, ctx->ovfCount, sizeof(uint32_t), true))) return r;
+        if ((r = dev_alloc(ctx, ctx->clipCount, sizeof(uint32_t), true))) return r;
         if ((r = dev_alloc(ctx, ctx->status, 4 * sizeof(int32_t), true))) return r;
     }
     if (numTiles > ctx->tileCap)
@@ -540,6 +542,8 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     f.slotInfo = static_cast<uint32_t*>(ctx->slotInfo.ptr);
     f.slotOvf = static_cast<uint32_t*>(ctx->slotOvf.ptr);
     f.ovfCount = static_cast<uint32_t*>(ctx->ovfCount.ptr);
+    f.clipQueue = static_cast<uint32_t*>(ctx->clipQueue.ptr);
+    f.clipCount = static_cast<uint32_t*>(ctx->clipCount.ptr);
     f.ovfCap = (uint32_t)std::min<uint64_t>(ctx->ovfCap, 0xFFFFFFFFu);
     f.numSlots = numSlots;
     f.tileCount = static_cast<uint32_t*>(ctx->tileCount.ptr);
@@ -614,7 +618,8 @@ void slg_context_destroy(slg_context* ctx)
     for (Texture& t : ctx->textures) dev_free(t.buf);
     for (Ubo& u : ctx->ubos) dev_free(u.buf);
     DevBuffer* scratch[] = {&ctx->texTable, &ctx->bufTable, &ctx->records, &ctx->varyings, &ctx->slotInfo, &ctx->slotOvf,
-                            &ctx->ovfCount, &ctx->tileCount, &ctx->tileOffset, &ctx->tileCursor, &ctx->entries,
+                            &ctx->ovfCount, &ctx->clipQueue, &ctx->clipCount, &ctx->tileCount, &ctx->tileOffset,
+                            &ctx->tileCursor, &ctx->entries,
                             &ctx->status, &ctx->devDescs, &ctx->devStarts};
     for (DevBuffer* b : scratch) dev_free(*b);
     if (ctx->hostDescs) cudaFreeHost(ctx->hostDescs);

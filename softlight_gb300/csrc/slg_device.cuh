@@ -100,6 +100,8 @@ struct Frame
     uint32_t* slotOvf;      /* per slot: first overflow record (relative) */
     uint32_t* ovfCount;
     uint32_t  ovfCap;
+    uint32_t* clipQueue;    /* slots of partially visible triangles (capacity numSlots) */
+    uint32_t* clipCount;
     uint64_t  numSlots;
     uint32_t* tileCount;    /* numTiles, zero between launches */
     uint32_t* tileOffset;   /* numTiles + 1 */
@@ -254,7 +256,7 @@ __device__ __forceinline__ slg_v4 run_vertex_program(uint32_t program, const Dev
     }
 }
 
-static __device__ __noinline__ bool run_fragment_program(uint32_t program, const DevEnv& env, const slg_v4* varyings, slg_v4* outputs)
+__device__ __forceinline__ bool run_fragment_program(uint32_t program, const DevEnv& env, const slg_v4* varyings, slg_v4* outputs)
 {
     switch (program)
     {

@@ -239,11 +239,15 @@ __device__ __forceinline__ void store_varyings(const Frame& f, uint64_t recIndex
                                                const slg_v4* a, const slg_v4* b, const slg_v4* c)
 {
     float4* dst = f.varyings + recIndex * kVaryingVec4;
-    for (int i = 0; i < nv; ++i)
+#pragma unroll
+    for (int i = 0; i < kMaxVaryings; ++i)
     {
-        dst[i] = to_f4(a[i]);
-        dst[4 + i] = to_f4(b[i]);
-        dst[8 + i] = to_f4(c[i]);
+        if (i < nv)
+        {
+            dst[i] = to_f4(a[i]);
+            dst[4 + i] = to_f4(b[i]);
+            dst[8 + i] = to_f4(c[i]);
+        }
     }
 }
 
@@ -259,8 +263,13 @@ __device__ __forceinline__ float4 mix4(const float4 a, const float4 b, float t)
 
 /* SL_TriProcessor::clip_and_process_tris (SL_TriProcessor.cpp:370-519).
  * Returns the slotInfo value for the slot. */
+struct ClipTri { float4 p[3]; uint64_t vid[3]; };
+
+/* The varyings of a clipped triangle's vertices are recomputed here (the
+ * vertex program is a pure function of vertex and instance id), so the
+ * common unclipped path keeps them in registers. */
 __device__ __noinline__ uint32_t clip_and_emit(const Frame& f, const DrawDesc& d, uint32_t drawIndex, uint64_t slot,
-                                               uint64_t primIndex, const float4* clip, const slg_v4* vary)
+                                               uint64_t primIndex, uint64_t inst, const ClipTri tri)
 {
     const int nv = d.numVaryings;
     float4 newVerts[9], tempVerts[9];
@@ -269,10 +278,13 @@ __device__ __noinline__ uint32_t clip_and_emit(const Frame& f, const DrawDesc& d
     for (int i = 0; i < 36; ++i) { newVarys[i] = slg_make_v4(0.f, 0.f, 0.f, 0.f); tempVarys[i] = newVarys[i]; }
 
     unsigned numTotal = 3;
+    const DevEnv env = make_env(d, f.tables);
     for (int k = 0; k < 3; ++k)
     {
-        newVerts[k] = clip[k];
-        for (int i = 0; i < nv; ++i) newVarys[k * 4 + i] = vary[k * 4 + i];
+        newVerts[k] = tri.p[k];
+        slg_v4 vary[4];
+        (void)run_vertex_program(d.vsProgram, env, tri.vid[k], inst, vary);
+        for (int i = 0; i < nv; ++i) newVarys[k * 4 + i] = vary[i];
     }
 
     for (int e = 0; e < 6; ++e)
@@ -420,11 +432,12 @@ __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, Ti
 
     float4 clip[3];
     slg_v4 vary[12];
+    uint64_t vids[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
     {
-        const uint64_t vid = (d.indexType >= 0) ? read_index(d, i + k) : (i + k);
-        clip[k] = to_f4(run_vertex_program(d.vsProgram, env, vid, inst, vary + 4 * k));
+        vids[k] = (d.indexType >= 0) ? read_index(d, i + k) : (i + k);
+        clip[k] = to_f4(run_vertex_program(d.vsProgram, env, vids[k], inst, vary + 4 * k));
     }
 
     if (d.cull != SLG_CULL_OFF)
@@ -464,9 +477,41 @@ __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, Ti
     }
     if (vis == 1)
     {
-        return clip_and_emit(f, d, (uint32_t)di, slot, primIndex, clip, vary);
+        /* partially visible: queued for clip_kernel */
+        const uint32_t q = atomicAdd(f.clipCount, 1u);
+        f.clipQueue[q] = (uint32_t)slot;
+        return 0;
     }
     return 0;
+}
+
+/*-----------------------------------------------------------------------------
+ * Kernel 1b: clipping of the queued partially visible triangles
+ * (SL_TriProcessor::clip_and_process_tris, SL_TriProcessor.cpp:370-519)
+-----------------------------------------------------------------------------*/
+__global__ void __launch_bounds__(128) clip_kernel(const Frame f)
+{
+    const uint32_t count = *f.clipCount;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x)
+    {
+        const uint64_t slot = f.clipQueue[q];
+        const int di = (f.numDraws > 1) ? find_draw(f, slot) : 0;
+        const DrawDesc& d = f.draws[di];
+        const uint64_t local = slot - d.slotBase;
+        const uint64_t inst = local / d.numTris;
+        const uint64_t tri = local - inst * d.numTris;
+        const uint64_t i = d.elementBegin + 3u * tri;
+        const DevEnv env = make_env(d, f.tables);
+        ClipTri ct;
+        for (int k = 0; k < 3; ++k)
+        {
+            ct.vid[k] = (d.indexType >= 0) ? read_index(d, i + k) : (i + k);
+            slg_v4 vary[4];
+            ct.p[k] = mat_mul(f.scissor, to_f4(run_vertex_program(d.vsProgram, env, ct.vid[k], inst, vary)));
+        }
+        const uint64_t primIndex = d.primBase + d.numElements * inst + i;
+        f.slotInfo[slot] = clip_and_emit(f, d, (uint32_t)di, slot, primIndex, inst, ct);
+    }
 }
 
 __global__ void __launch_bounds__(128) vs_setup_kernel(const Frame f)
@@ -544,6 +589,7 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const Frame f, int numT
             atomicMax(f.status + 1, (int)min(total, 0x7FFFFFFFu));
         }
         *f.ovfCount = 0;
+        *f.clipCount = 0;
     }
 }
 
@@ -815,11 +861,20 @@ __device__ __forceinline__ bool shade(const Frame& f, const DrawDesc& dd, uint64
 
     slg_v4 vary[4];
     const float4* V = f.varyings + rec * kVaryingVec4;
-    for (int vi = 0; vi < dd.numVaryings; ++vi)
+    const int nv = dd.numVaryings;
+#pragma unroll
+    for (int vi = 0; vi < kMaxVaryings; ++vi)
     {
-        const float4 a = V[vi], b = V[4 + vi], c = V[8 + vi];
-        vary[vi] = slg_make_v4((a.x * q0 + b.x * q1) + c.x * q2, (a.y * q0 + b.y * q1) + c.y * q2,
-                               (a.z * q0 + b.z * q1) + c.z * q2, (a.w * q0 + b.w * q1) + c.w * q2);
+        if (vi < nv)
+        {
+            const float4 a = V[vi], b = V[4 + vi], c = V[8 + vi];
+            vary[vi] = slg_make_v4((a.x * q0 + b.x * q1) + c.x * q2, (a.y * q0 + b.y * q1) + c.y * q2,
+                                   (a.z * q0 + b.z * q1) + c.z * q2, (a.w * q0 + b.w * q1) + c.w * q2);
+        }
+        else
+        {
+            vary[vi] = slg_make_v4(0.f, 0.f, 0.f, 0.f);
+        }
     }
     slg_v4 outputs[4];
     const DevEnv env = make_env(dd, f.tables);
@@ -1225,6 +1280,7 @@ cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEven
     {
         const unsigned blocks = (unsigned)((f.numSlots + 127) / 128);
         vs_setup_kernel<<<blocks, 128, 0, s>>>(f);
+        clip_kernel<<<152 * 4, 128, 0, s>>>(f);
     }
     if (ev) cudaEventRecord(ev[1], s);
     tile_scan_kernel<<<1, 1024, 0, s>>>(f, numTiles);
