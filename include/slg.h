@@ -249,6 +249,22 @@ int slg_stage_times(slg_context* ctx, float ms[4]);
  * image. */
 int slg_set_raster_mode(slg_context* ctx, int mode);
 
+/* Threads per block of the vertex/set-up stage, i.e. triangles per CTA: 64,
+ * 128 (default) or 256. */
+int slg_set_vertex_block(slg_context* ctx, int threads);
+
+/* When enabled, slg_draw_batch captures its launch sequence into a CUDA
+ * graph and replays it on later calls with the same draws and launch
+ * parameters (uniform-block contents may change between replays). */
+int slg_set_batch_graphs(slg_context* ctx, int enable);
+
+/* Autotuner: renders clear(rgba, depth) + slg_draw_batch(cmds) with every
+ * supported tile size and vertex block size, keeps the fastest for the
+ * context and returns it in out = {tileW, tileH, vertex block}. The
+ * framebuffer holds the last trial's frame afterwards. */
+int slg_autotune(slg_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, size_t fboId,
+                 const double rgba[4], double depth, int out[3]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,6 +99,10 @@ _GPU_SIGNATURES = [
     ("profile_stages", C.c_int, [C.c_void_p, C.c_int]),
     ("stage_times", C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     ("set_raster_mode", C.c_int, [C.c_void_p, C.c_int]),
+    ("set_vertex_block", C.c_int, [C.c_void_p, C.c_int]),
+    ("set_batch_graphs", C.c_int, [C.c_void_p, C.c_int]),
+    ("autotune", C.c_int, [C.c_void_p, C.POINTER(DrawCmd), C.c_size_t, C.c_size_t, C.POINTER(C.c_double),
+                           C.c_double, C.POINTER(C.c_int)]),
 ]
 
 
@@ -296,6 +300,21 @@ class SLContext:
 
     def set_raster_mode(self, mode):
         self._call("set_raster_mode", mode)
+
+    def set_vertex_block(self, threads):
+        self._call("set_vertex_block", threads)
+
+    def set_batch_graphs(self, enable=True):
+        self._call("set_batch_graphs", 1 if enable else 0)
+
+    def autotune(self, cmds, fbo, rgba=(0.0, 0.0, 0.0, 1.0), depth=1.0):
+        """Picks the fastest tile size and vertex block for clear + draw_batch;
+        returns (tileW, tileH, vertex block)."""
+        arr = (DrawCmd * len(cmds))(*cmds)
+        c = (C.c_double * 4)(*rgba)
+        out = (C.c_int * 3)()
+        self._call("autotune", arr, len(cmds), fbo, c, depth, out)
+        return tuple(out)
 
     def stage_times(self):
         ms = (C.c_float * 4)()

@@ -93,6 +93,18 @@ struct slg_context
     int tileW = 32, tileH = 32;
     int keyCap = 32768;   /* largest sortable tile list (128 KB of shared memory) */
     bool forceOrdered = false;
+    int vsBlock = 128;          /* triangles per CTA of the vertex stage */
+    bool batchGraphs = false;   /* replay slg_draw_batch launches as a CUDA graph */
+
+    /* the last captured batch launch */
+    struct GraphCache
+    {
+        cudaGraphExec_t exec = nullptr;
+        std::vector<DrawDesc> descs;
+        std::vector<uint64_t> starts;
+        Frame frame;
+        DevBuffer devDescs, devStarts;
+    } graph;
 
     std::vector<Vbo> vbos;
     std::vector<Ibo> ibos;
@@ -476,9 +488,63 @@ int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, Draw
     return SLG_OK;
 }
 
+/* Replays the cached CUDA graph of a batch launch when the descriptors and
+ * the launch parameters are unchanged (uniform-block contents may change:
+ * they are read from device memory and were validated again on the host),
+ * otherwise captures the pipeline of this launch into a new graph. */
+int launch_batch_graph(slg_context* ctx, const Frame& frame, const DrawDesc* descs, const uint64_t* starts, size_t n)
+{
+    slg_context::GraphCache& g = ctx->graph;
+    int r;
+    if ((r = dev_alloc(ctx, g.devDescs, n * sizeof(DrawDesc), false))) return r;
+    if ((r = dev_alloc(ctx, g.devStarts, (n + 1) * sizeof(uint64_t), false))) return r;
+    Frame f = frame;
+    f.draws = static_cast<const DrawDesc*>(g.devDescs.ptr);
+    f.drawSlotStart = static_cast<const uint64_t*>(g.devStarts.ptr);
+
+    const bool same = g.exec && g.descs.size() == n &&
+                      std::memcmp(g.descs.data(), descs, n * sizeof(DrawDesc)) == 0 &&
+                      std::memcmp(g.starts.data(), starts, (n + 1) * sizeof(uint64_t)) == 0 &&
+                      std::memcmp(&g.frame, &f, sizeof(Frame)) == 0;
+    cudaError_t e = cudaSuccess;
+    if (!same)
+    {
+        if (g.exec)
+        {
+            cudaStreamSynchronize(ctx->stream);
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+        e = cudaMemcpyAsync(g.devDescs.ptr, descs, n * sizeof(DrawDesc), cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(g.devStarts.ptr, starts, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "graph descriptor upload");
+
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaStreamBeginCapture");
+        const cudaError_t le = slg::launch_pipeline(f, ctx->keyCap, ctx->stream, nullptr);
+        e = cudaStreamEndCapture(ctx->stream, &graph);
+        if (le != cudaSuccess) e = le;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&g.exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess)
+        {
+            g.exec = nullptr;
+            return ctx->cuda_fail(e, "batch graph capture");
+        }
+        g.descs.assign(descs, descs + n);
+        g.starts.assign(starts, starts + n + 1);
+        g.frame = f;
+    }
+    e = cudaGraphLaunch(g.exec, ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaGraphLaunch");
+    return SLG_OK;
+}
+
 /* One launch of the pipeline over a sequence of draws that share a
  * framebuffer. The result equals issuing the draws one after another. */
-int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fboId)
+int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fboId, bool batch = false)
 {
     if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
     const Fbo& fbo = ctx->fbos[fboId];
@@ -528,10 +594,7 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
 
     DrawDesc* devDescs = static_cast<DrawDesc*>(ctx->devDescs.ptr) + ctx->descHead;
     uint64_t* devStarts = static_cast<uint64_t*>(ctx->devStarts.ptr) + ctx->descHead;
-    cudaError_t e = cudaMemcpyAsync(devDescs, descs, n * sizeof(DrawDesc), cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(devStarts, starts, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream);
-    if (e != cudaSuccess) return ctx->cuda_fail(e, "descriptor upload");
-    ctx->descHead += n + 1;
+    cudaError_t e = cudaSuccess;
 
     f.color = colorTex ? static_cast<uint8_t*>(colorTex->buf.ptr) : nullptr;
     f.colorType = colorTex ? colorTex->type : SLG_COLOR_RGBA_8U;
@@ -571,6 +634,18 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     f.tables.textures = static_cast<const TexView*>(ctx->texTable.ptr);
     f.tables.buffers = static_cast<const uint8_t* const*>(ctx->bufTable.ptr);
 
+    f.vsBlock = ctx->vsBlock;
+
+    if (batch && ctx->batchGraphs && !ctx->profileStages)
+    {
+        return launch_batch_graph(ctx, f, descs, starts, n);
+    }
+
+    e = cudaMemcpyAsync(devDescs, descs, n * sizeof(DrawDesc), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(devStarts, starts, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "descriptor upload");
+    ctx->descHead += n + 1;
+
     e = slg::launch_pipeline(f, ctx->keyCap, ctx->stream, ctx->profileStages ? ctx->stageEvents : nullptr);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "draw launch");
     return SLG_OK;
@@ -598,6 +673,7 @@ int slg_context_create(slg_context** outCtx)
     if (e == cudaSuccess) e = cudaMalloc(&ctx->devDescs.ptr, kDescRing * sizeof(DrawDesc));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->devStarts.ptr, kDescRing * sizeof(uint64_t));
     for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->stageEvents[i]);
+    if (e == cudaSuccess) e = slg::init_kernel_attributes(ctx->keyCap);
     if (e != cudaSuccess)
     {
         slg_context_destroy(ctx);
@@ -622,6 +698,9 @@ void slg_context_destroy(slg_context* ctx)
                             &ctx->tileCursor, &ctx->entries,
                             &ctx->status, &ctx->devDescs, &ctx->devStarts};
     for (DevBuffer* b : scratch) dev_free(*b);
+    if (ctx->graph.exec) cudaGraphExecDestroy(ctx->graph.exec);
+    dev_free(ctx->graph.devDescs);
+    dev_free(ctx->graph.devStarts);
     if (ctx->hostDescs) cudaFreeHost(ctx->hostDescs);
     if (ctx->hostStarts) cudaFreeHost(ctx->hostStarts);
     if (ctx->hostStatus) cudaFreeHost(ctx->hostStatus);
@@ -892,7 +971,77 @@ int slg_draw_batch(slg_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, s
         if (cmds[i].numInstances == 0) continue;
         reqs.push_back({cmds[i].mesh, cmds[i].numInstances, cmds[i].shaderId, 0});
     }
-    return run_launch(ctx, reqs, fboId);
+    return run_launch(ctx, reqs, fboId, true);
+}
+
+int slg_set_vertex_block(slg_context* ctx, int threads)
+{
+    if (threads != 64 && threads != 128 && threads != 256) return ctx->fail(SLG_ERR_INVALID_ARG, "vertex block must be 64, 128 or 256");
+    ctx->vsBlock = threads;
+    return SLG_OK;
+}
+
+int slg_set_batch_graphs(slg_context* ctx, int enable)
+{
+    ctx->batchGraphs = enable != 0;
+    return SLG_OK;
+}
+
+/* Times clear + slg_draw_batch for every supported tile size and vertex
+ * block size and keeps the fastest; out = {tileW, tileH, vertex block}. */
+int slg_autotune(slg_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, size_t fboId,
+                 const double rgba[4], double depth, int out[3])
+{
+    if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
+    static const int tiles[][2] = {{8, 8}, {16, 16}, {32, 16}, {32, 32}, {64, 32}, {64, 64}};
+    static const int blocks[] = {64, 128, 256};
+    const bool graphs = ctx->batchGraphs, prof = ctx->profileStages;
+    ctx->batchGraphs = false;
+    ctx->profileStages = false;
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    float best = 1e30f;
+    int bw = ctx->tileW, bh = ctx->tileH, bb = ctx->vsBlock;
+    const bool hasColor = ctx->fbos[fboId].numColors > 0;
+    auto frame = [&]() -> int {
+        const int c = hasColor ? slg_clear_framebuffer(ctx, fboId, 0, rgba, depth) : slg_clear_depth_buffer(ctx, fboId, depth);
+        return c ? c : slg_draw_batch(ctx, cmds, numCmds, fboId);
+    };
+    int status = SLG_OK;
+    for (const auto& t : tiles)
+    {
+        for (int b : blocks)
+        {
+            ctx->tileW = t[0];
+            ctx->tileH = t[1];
+            ctx->vsBlock = b;
+            int r = frame();
+            if (!r) r = frame();
+            if (!r) r = slg_finish(ctx);
+            if (r == SLG_ERR_OVERFLOW) continue; /* this tile size overflows its lists */
+            if (r) { status = r; break; }
+            cudaEventRecord(t0, ctx->stream);
+            for (int k = 0; k < 3 && !r; ++k) r = frame();
+            cudaEventRecord(t1, ctx->stream);
+            if (!r) r = slg_finish(ctx);
+            if (r == SLG_ERR_OVERFLOW) continue;
+            if (r) { status = r; break; }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, t0, t1);
+            if (ms < best) { best = ms; bw = t[0]; bh = t[1]; bb = b; }
+        }
+        if (status) break;
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    ctx->tileW = bw;
+    ctx->tileH = bh;
+    ctx->vsBlock = bb;
+    ctx->batchGraphs = graphs;
+    ctx->profileStages = prof;
+    if (out) { out[0] = bw; out[1] = bh; out[2] = bb; }
+    return status;
 }
 
 int slg_finish(slg_context* ctx)

@@ -120,6 +120,9 @@ struct Frame
     int32_t orderFree;
     int32_t freeDepthFunc;
     int32_t freeDepthMask;
+
+    /* threads per block of the vertex stage (64, 128 or 256): triangles per CTA */
+    int32_t vsBlock;
 };
 
 enum StatusBits

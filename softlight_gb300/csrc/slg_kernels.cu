@@ -514,7 +514,7 @@ __global__ void __launch_bounds__(128) clip_kernel(const Frame f)
     }
 }
 
-__global__ void __launch_bounds__(128) vs_setup_kernel(const Frame f)
+__global__ void __launch_bounds__(256) vs_setup_kernel(const Frame f)
 {
     const uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     TileRange tr;
@@ -1238,27 +1238,48 @@ template <int TW, int TH, class Color>
 static cudaError_t launch_raster_t(const Frame& f, int numTiles, int keyCap, cudaStream_t s)
 {
     typedef RasterLayout<TW, TH, Color> L;
-    cudaError_t e;
     if (f.orderFree)
     {
-        const size_t smem = L::free_bytes();
-        e = cudaFuncSetAttribute(raster_free_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        raster_free_kernel<TW, TH, Color><<<numTiles, L::kThreads, smem, s>>>(f, f.freeDepthFunc, f.freeDepthMask);
+        raster_free_kernel<TW, TH, Color><<<numTiles, L::kThreads, L::free_bytes(), s>>>(f, f.freeDepthFunc, f.freeDepthMask);
     }
     else
     {
         /* keyCap keys of 4 bytes per tile for the sort (<= 227 KB) */
-        const size_t sortSmem = sizeof(uint32_t) * (size_t)keyCap;
-        e = cudaFuncSetAttribute(tile_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sortSmem);
-        if (e != cudaSuccess) return e;
-        tile_sort_kernel<<<numTiles, 1024, sortSmem, s>>>(f, keyCap);
-        const size_t smem = L::ordered_bytes();
-        e = cudaFuncSetAttribute(raster_ordered_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        raster_ordered_kernel<TW, TH, Color><<<numTiles, L::kThreads, smem, s>>>(f);
+        tile_sort_kernel<<<numTiles, 1024, sizeof(uint32_t) * (size_t)keyCap, s>>>(f, keyCap);
+        raster_ordered_kernel<TW, TH, Color><<<numTiles, L::kThreads, L::ordered_bytes(), s>>>(f);
     }
     return cudaGetLastError();
+}
+
+template <int TW, int TH, class Color>
+static cudaError_t attributes_t()
+{
+    typedef RasterLayout<TW, TH, Color> L;
+    cudaError_t e = cudaFuncSetAttribute(raster_free_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::free_bytes());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(raster_ordered_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::ordered_bytes());
+    return e;
+}
+
+template <class Color>
+static cudaError_t attributes_c()
+{
+    cudaError_t e = attributes_t<8, 8, Color>();
+    if (e == cudaSuccess) e = attributes_t<16, 16, Color>();
+    if (e == cudaSuccess) e = attributes_t<32, 16, Color>();
+    if (e == cudaSuccess) e = attributes_t<32, 32, Color>();
+    if (e == cudaSuccess) e = attributes_t<64, 32, Color>();
+    if (e == cudaSuccess) e = attributes_t<64, 64, Color>();
+    return e;
+}
+
+cudaError_t init_kernel_attributes(int keyCap)
+{
+    cudaError_t e = cudaFuncSetAttribute(tile_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(uint32_t) * keyCap));
+    if (e == cudaSuccess) e = attributes_c<ColorRGBA8>();
+    if (e == cudaSuccess) e = attributes_c<ColorRGBAF>();
+    if (e == cudaSuccess) e = attributes_c<ColorRF>();
+    return e;
 }
 
 template <class Color>
@@ -1275,11 +1296,12 @@ static cudaError_t launch_raster_c(const Frame& f, int numTiles, int keyCap, cud
 cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEvent_t* ev)
 {
     const int numTiles = f.tilesX * f.tilesY;
+    const int vsBlock = (f.vsBlock == 64 || f.vsBlock == 256) ? f.vsBlock : 128;
     if (ev) cudaEventRecord(ev[0], s);
     if (f.numSlots > 0)
     {
-        const unsigned blocks = (unsigned)((f.numSlots + 127) / 128);
-        vs_setup_kernel<<<blocks, 128, 0, s>>>(f);
+        const unsigned blocks = (unsigned)((f.numSlots + vsBlock - 1) / vsBlock);
+        vs_setup_kernel<<<blocks, vsBlock, 0, s>>>(f);
         clip_kernel<<<152 * 4, 128, 0, s>>>(f);
     }
     if (ev) cudaEventRecord(ev[1], s);

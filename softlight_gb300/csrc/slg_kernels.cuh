@@ -15,6 +15,10 @@ namespace slg
  * vs_setup, after tile_scan, after bin_fill and after raster. */
 cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEvent_t* ev);
 
+/* Raises the dynamic shared-memory limits of the raster and sort kernels
+ * once, so launches (and stream captures) need no attribute calls. */
+cudaError_t init_kernel_attributes(int keyCap);
+
 /* Fill numTexels texels of 4 or 16 bytes with value. */
 cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[4], cudaStream_t s);
 

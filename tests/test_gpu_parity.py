@@ -167,3 +167,52 @@ def test_empty_and_degenerate_draws(ctxs):
     # invalid ids are rejected, not executed
     with pytest.raises(A.SLError):
         g.draw(A.Mesh(999, 0, 3, A.RENDER_MODE_TRIANGLES, 0), 0, 0)
+
+
+@pytest.mark.parametrize("vs_block", [64, 128, 256])
+def test_vertex_block_sizes(ctxs, vs_block):
+    g, o = ctxs
+    g.set_vertex_block(vs_block)
+    sg, so = render_both(S.build_c4, g, o, num_draws=8, width=256, height=160, tex_size=32)
+    assert compare_scenes(sg, so, f"vs block {vs_block}") == 0
+
+
+def test_batch_graph_replay_tracks_uniforms(ctxs):
+    """Graph replays of a batch pick up uniform-block updates and match the
+    oracle frame by frame; a changed draw list is recaptured."""
+    import numpy as np
+    g, o = ctxs
+    g.set_batch_graphs(True)
+    sg = S.build_c4(g, num_draws=10, width=256, height=160, tex_size=32)
+    so = S.build_c4(o, num_draws=10, width=256, height=160, tex_size=32)
+    rng = np.random.default_rng(9)
+    for frame in range(4):
+        if frame >= 2:
+            # move one mesh: rewrite its uniform block on both sides
+            ubo, data = sg.frame_ubos[frame]
+            arr = np.frombuffer(data, dtype=np.uint8).copy()
+            model = arr[64:128].view(np.float32).copy()
+            model[12:15] += rng.uniform(-3, 3, 3).astype(np.float32)
+            arr[64:128] = model.view(np.uint8)
+            g.ubo_assign(ubo, arr.tobytes())
+            o.ubo_assign(so.frame_ubos[frame][0], arr.tobytes())
+        if frame == 3:
+            sg.draws = sg.draws[:-2]
+            so.draws = so.draws[:-2]
+        sg.render()
+        so.render()
+        g.finish()
+        assert compare_scenes(sg, so, f"graph frame {frame}") == 0
+
+
+def test_autotune_picks_a_valid_config(ctxs):
+    g, o = ctxs
+    sg = S.build_c4(g, num_draws=12, width=320, height=200, tex_size=32)
+    so = S.build_c4(o, num_draws=12, width=320, height=200, tex_size=32)
+    from softlight_gb300 import api as A2
+    cmds = [A2.DrawCmd(m, n, s) for (m, n, s) in sg.draws]
+    tw, th, vb = g.autotune(cmds, sg.fbo)
+    assert (tw, th) in [(8, 8), (16, 16), (32, 16), (32, 32), (64, 32), (64, 64)] and vb in (64, 128, 256)
+    sg.render()
+    so.render()
+    assert compare_scenes(sg, so, "autotuned") == 0
