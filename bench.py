@@ -38,7 +38,7 @@ def parse():
     p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-seconds", type=float, default=15.0)
-    p.add_argument("--tile", default="32x32", help="screen tile WxH (8x8 .. 64x64)")
+    p.add_argument("--tile", default="auto", help="screen tile WxH (8x8 .. 64x64) or auto (autotuner)")
     return p.parse_args()
 
 
@@ -197,6 +197,14 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def launches_per_frame(scene):
+    """Kernels one frame launches: two clears, then vs_setup, clip, tile_scan,
+    bin_fill and raster per launch, plus tile_sort on the ordered path."""
+    per_launch = 5 + (1 if scene.blending else 0)
+    launches = 1 if scene.batched else len(scene.draws)
+    return 2 + per_launch * launches
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -210,23 +218,25 @@ def run_gpu(args):
     sg.build()
     builder, kwargs, cfg = workload_config(args.workload)
     ctx = sg.Context()
-    tw, th = (int(v) for v in args.tile.split("x"))
-    ctx.set_tile_size(tw, th)
     scene = builder(ctx, **kwargs)
     stream = torch.cuda.ExternalStream(ctx.stream_handle())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    cmds = [sg.api.DrawCmd(m, n, sh) for (m, n, sh) in scene.draws]
+    if args.tile == "auto":
+        tw, th, vb = ctx.autotune(cmds, scene.fbo, scene.clear_color, scene.clear_depth)
+    else:
+        tw, th = (int(v) for v in args.tile.split("x"))
+        vb = 128
+        ctx.set_tile_size(tw, th)
+    if scene.batched:
+        ctx.set_batch_graphs(True)
 
-    for _ in range(max(3, args.warmup)):
-        scene.render()
-    ctx.finish()
-
-    ctx.profile_stages(True)
-    step_ms, stage_ms = [], []
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clocks:
-        for i in range(args.steps):
+    def timed_frames(k, profile):
+        """k frames, each timed with CUDA events on the context's stream,
+        L2 flushed before each; optional per-stage event times."""
+        ctx.profile_stages(profile)
+        ms, stages = [], []
+        for i in range(k):
             with torch.cuda.stream(stream):
                 flush.fill_(i & 0xFF)
                 ev0 = torch.cuda.Event(enable_timing=True)
@@ -236,11 +246,24 @@ def run_gpu(args):
             with torch.cuda.stream(stream):
                 ev1.record(stream)
             ev1.synchronize()
-            step_ms.append(ev0.elapsed_time(ev1))
-            stage_ms.append(ctx.stage_times())
+            ms.append(ev0.elapsed_time(ev1))
+            if profile:
+                stages.append(ctx.stage_times())
+        ctx.finish()
+        ctx.profile_stages(False)
+        return ms, stages
+
+    for _ in range(max(3, args.warmup)):
+        scene.render()
     ctx.finish()
+
+    if world > 1:
+        torch.distributed.barrier()
     torch.cuda.synchronize()
-    ctx.profile_stages(False)
+    with ClockSampler(local) as clocks:
+        step_ms, _ = timed_frames(args.steps, False)
+        _, stage_ms = timed_frames(max(3, min(args.steps, 10)), True)
+    torch.cuda.synchronize()
     total_ms = sum(step_ms)
     if world > 1:
         t = torch.tensor([total_ms], device="cuda")
@@ -248,11 +271,26 @@ def run_gpu(args):
         total_ms = float(t.item())
     fps = world * args.steps / (total_ms / 1000.0)
 
+    per_draw = None
+    if scene.batched:
+        # the same frames issued as one slg_draw call per mesh
+        scene.batched = False
+        for _ in range(2):
+            scene.render()
+        pd_ms, _ = timed_frames(args.steps, False)
+        scene.batched = True
+        per_draw = {"value": args.steps / (sum(pd_ms) / 1000.0), "unit": "frames/s",
+                    "launches_per_frame": 2 + 6 * len(scene.draws),
+                    "batched_speedup": (sum(pd_ms) / max(total_ms, 1e-9))}
+
     # end to end through the C ABI with pinned host buffers
-    ubo_id, ubo_bytes = scene.frame_ubos[0]
-    ubo_host = torch.empty(len(ubo_bytes), dtype=torch.uint8, pin_memory=True).numpy()
-    ubo_host[:] = np.frombuffer(ubo_bytes, dtype=np.uint8)
-    h2d = len(ubo_bytes)
+    ubos = []
+    h2d = 0
+    for ubo_id, ubo_bytes in scene.frame_ubos:
+        ubo_host = torch.empty(len(ubo_bytes), dtype=torch.uint8, pin_memory=True).numpy()
+        ubo_host[:] = np.frombuffer(ubo_bytes, dtype=np.uint8)
+        ubos.append((ubo_id, ubo_host))
+        h2d += len(ubo_bytes)
     inst = getattr(scene, "instance_matrices", None)
     if inst is not None:
         inst_host = torch.empty(inst[1].nbytes, dtype=torch.uint8, pin_memory=True).numpy()
@@ -266,7 +304,8 @@ def run_gpu(args):
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        ctx.ubo_assign(ubo_id, ubo_host)
+        for ubo_id, ubo_host in ubos:
+            ctx.ubo_assign(ubo_id, ubo_host)
         if inst is not None:
             ctx.vbo_assign(inst[0], inst_host)
         scene.render()
@@ -306,7 +345,8 @@ def run_gpu(args):
 
     if rank == 0:
         cfg = dict(cfg)
-        cfg.update({"l2": "flushed between timed frames (256 MiB write)", "tile": args.tile,
+        cfg.update({"l2": "flushed between timed frames (256 MiB write)", "tile": f"{tw}x{th}",
+                    "vertex_block": vb, "tuned": args.tile == "auto", "batched_graph": bool(scene.batched),
                     "triangles_per_frame": scene.num_triangles})
         line = {"metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -315,7 +355,9 @@ def run_gpu(args):
                 "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": scene.height * scene.width * 4},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks.summary(),
-                "gpu_launches": args.steps * 6}
+                "gpu_launches": args.steps * (launches_per_frame(scene))}
+        if per_draw is not None:
+            line["per_draw"] = per_draw
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:

@@ -263,6 +263,7 @@ class Scene:
         self.frame_ubos = []     # (ubo id, bytes) re-uploaded per frame in e2e timing
         self.texture_bytes = 0
         self.geometry_bytes = 0
+        self.blending = False
 
     def add_texture_rgba8(self, img):
         t = self.ctx.create_texture()
@@ -304,6 +305,7 @@ class Scene:
         ubo = ctx.create_ubo()
         ctx.ubo_assign(ubo, ubo_bytes)
         self.frame_ubos.append((ubo, ubo_bytes))
+        self.blending = self.blending or blend != A.BLEND_OFF
         vs = A.VertexShader(num_varyings, cull, program)
         fs = A.FragmentShader(num_varyings, num_outputs, blend, depth_test, depth_mask, program)
         return ctx.create_shader(vs, fs, ubo)
