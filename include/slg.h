@@ -216,6 +216,34 @@ int slg_draw(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId)
 int slg_draw_instanced(slg_context* ctx, const slg_mesh* m, size_t numInstances, size_t shaderId, size_t fboId);
 int slg_draw_multiple(slg_context* ctx, const slg_mesh* meshes, size_t numMeshes, size_t shaderId, size_t fboId);
 
+/* slg_draw that allocates nothing. No counterpart in the reference: SoftLight
+ * draws on the host and has no device scratch to allocate.
+ *
+ * slg_draw grows its scratch buffers with cudaMalloc when a draw needs more;
+ * callers that must not allocate mid-frame (a fixed device-memory budget, a
+ * thread that must not meet cudaMalloc's implicit device synchronisation, an
+ * allocator hook that forbids new allocations) use this variant, whose
+ * scratch is one file-scope device array of about 4.3 MiB sized for the
+ * worst case of the limits below. Same arguments, results and errors as
+ * slg_draw, plus:
+ *  - limits: at most SLG_NOALLOC_MAX_TRIANGLES triangles per call and a
+ *    framebuffer of at most SLG_NOALLOC_MAX_TILES tiles of the context's tile
+ *    size (256x256 pixels at the default 32x32); larger draws are rejected
+ *    with SLG_ERR_INVALID_ARG and a message naming the limit, before any work
+ *    is queued;
+ *  - the first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress, with that device current) and caches it; make
+ *    that first call before any stream capture;
+ *  - the pipeline's counters (overflow and clip counts, status words, per-tile
+ *    triangle counts) must start at zero; each call clears them itself with
+ *    one cudaMemsetAsync on the context's stream before its kernels;
+ *  - all contexts on a device share the one array: calls whose work overlaps
+ *    on the device (two contexts, or two host threads) race on it and must be
+ *    serialised by the caller. */
+#define SLG_NOALLOC_MAX_TRIANGLES 1024
+#define SLG_NOALLOC_MAX_TILES 64
+int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId);
+
 /* Many draws (each possibly instanced, each with its own shader/uniforms) in
  * one launch sequence with the same result as issuing them one by one with
  * slg_draw / slg_draw_instanced. No single reference counterpart: it replaces

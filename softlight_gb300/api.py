@@ -103,6 +103,7 @@ _GPU_SIGNATURES = [
     ("set_batch_graphs", C.c_int, [C.c_void_p, C.c_int]),
     ("autotune", C.c_int, [C.c_void_p, C.POINTER(DrawCmd), C.c_size_t, C.c_size_t, C.POINTER(C.c_double),
                            C.c_double, C.POINTER(C.c_int)]),
+    ("draw_noalloc", C.c_int, [C.c_void_p, C.POINTER(Mesh), C.c_size_t, C.c_size_t]),
 ]
 
 
@@ -284,6 +285,10 @@ class SLContext:
     def draw_batch(self, cmds, fbo):
         arr = (DrawCmd * len(cmds))(*cmds)
         self._call("draw_batch", arr, len(cmds), fbo)
+
+    def draw_noalloc(self, mesh, shader, fbo):
+        """slg_draw with its scratch in a fixed device array (no allocation)."""
+        self._call("draw_noalloc", C.byref(mesh), shader, fbo)
 
     def finish(self):
         self._call("finish")

@@ -14,6 +14,7 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -1086,3 +1087,199 @@ int slg_stage_times(slg_context* ctx, float ms[4])
 }
 
 } // extern "C"
+
+/*-----------------------------------------------------------------------------
+ * slg_draw_noalloc: slg_draw with its per-launch scratch in one fixed device
+ * array that exists from the moment the library is loaded.
+ *
+ * slg_draw keeps its scratch (triangle records, varyings, tile lists) in
+ * context buffers that grow with cudaMalloc when a draw needs more. Some
+ * callers cannot let a draw allocate: a render loop running under a fixed
+ * device-memory budget, a thread that must not meet cudaMalloc/cudaFree's
+ * implicit device-wide synchronisation in the middle of a frame, or code
+ * running under an allocator hook that forbids new allocations once set-up
+ * is over. For them this variant sizes every scratch array for a stated
+ * worst case, rejects larger draws up front, and never allocates.
+-----------------------------------------------------------------------------*/
+namespace
+{
+
+constexpr uint64_t kNoAllocTris = SLG_NOALLOC_MAX_TRIANGLES;
+constexpr uint64_t kNoAllocTiles = SLG_NOALLOC_MAX_TILES;
+/* a clipped triangle is replaced by at most 7 sub-triangles, which live in
+ * the overflow region behind the per-triangle records */
+constexpr uint64_t kNoAllocOvf = 7 * kNoAllocTris;
+constexpr uint64_t kNoAllocRecords = kNoAllocTris + kNoAllocOvf;
+/* every record lands in at most every tile: no tile list can overflow */
+constexpr uint64_t kNoAllocEntries = kNoAllocOvf * kNoAllocTiles;
+constexpr size_t kNoAllocTextures = 256, kNoAllocBuffers = 256;
+
+constexpr size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
+
+/* layout of the static scratch; the first kNoAllocZeroBytes must be zero
+ * when the pipeline starts: ovfCount (+0), clipCount (+4), the status words
+ * (+16..+31) and the per-tile triangle counters (+256) */
+constexpr size_t kOffCounters = 0;
+constexpr size_t kOffTileCount = 256;
+constexpr size_t kNoAllocZeroBytes = kOffTileCount + align256(kNoAllocTiles * sizeof(uint32_t));
+constexpr size_t kOffTileOffset = kNoAllocZeroBytes;
+constexpr size_t kOffTileCursor = kOffTileOffset + align256((kNoAllocTiles + 1) * sizeof(uint32_t));
+constexpr size_t kOffSlotInfo = kOffTileCursor + align256(kNoAllocTiles * sizeof(uint32_t));
+constexpr size_t kOffSlotOvf = kOffSlotInfo + align256(kNoAllocTris * sizeof(uint32_t));
+constexpr size_t kOffClipQueue = kOffSlotOvf + align256(kNoAllocTris * sizeof(uint32_t));
+constexpr size_t kOffTexTable = kOffClipQueue + align256(kNoAllocTris * sizeof(uint32_t));
+constexpr size_t kOffBufTable = kOffTexTable + align256(kNoAllocTextures * sizeof(TexView));
+constexpr size_t kOffRecords = kOffBufTable + align256(kNoAllocBuffers * sizeof(void*));
+constexpr size_t kOffVaryings = kOffRecords + align256(kNoAllocRecords * slg::kRecordVec4 * sizeof(float4));
+constexpr size_t kOffEntries = kOffVaryings + align256(kNoAllocRecords * slg::kVaryingVec4 * sizeof(float4));
+constexpr size_t kNoAllocBytes = kOffEntries + align256(kNoAllocEntries * sizeof(uint32_t));
+static_assert(kNoAllocBytes < (8u << 20), "static draw scratch stays under 8 MiB");
+
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noallocMutex;
+unsigned char* g_noallocPtr[kNoAllocMaxDevices] = {};
+
+/* Device address of the static scratch on the current device, looked up
+ * once per device (with that device current) and cached. */
+int noalloc_scratch(slg_context* ctx, unsigned char** out)
+{
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return ctx->fail(SLG_ERR_INVALID_ARG, "slg_draw_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    if (!g_noallocPtr[dev])
+    {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noallocScratch);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaGetSymbolAddress(static draw scratch)");
+        g_noallocPtr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noallocPtr[dev];
+    return SLG_OK;
+}
+
+} // namespace
+
+extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId)
+{
+    if (!m) return ctx->fail(SLG_ERR_INVALID_ARG, "null mesh");
+    if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
+    const Fbo& fbo = ctx->fbos[fboId];
+    if (fbo.depth == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "framebuffer has no depth attachment");
+    if (fbo.numColors > 1) return ctx->fail(SLG_ERR_INVALID_ARG, "more than one colour attachment is not supported");
+    const Texture& depthTex = ctx->textures[fbo.depth];
+    const Texture* colorTex = (fbo.numColors > 0 && fbo.colors[0] != SLG_INVALID_ID) ? &ctx->textures[fbo.colors[0]] : nullptr;
+    if (colorTex && (colorTex->w != depthTex.w || colorTex->h != depthTex.h))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "colour and depth attachments differ in size");
+
+    unsigned char* scratch = nullptr;
+    int r = noalloc_scratch(ctx, &scratch);
+    if (r) return r;
+
+    /* the descriptor goes through the context's pinned ring, as for slg_draw */
+    if (ctx->descHead + 2 > kDescRing)
+    {
+        cudaStreamSynchronize(ctx->stream);
+        ctx->descHead = 0;
+    }
+    DrawDesc* desc = ctx->hostDescs + ctx->descHead;
+    uint64_t* starts = ctx->hostStarts + ctx->descHead;
+    uint64_t numSlots = 0;
+    const DrawRequest req = {*m, 1, shaderId, 0};
+    if ((r = build_desc(ctx, req, 0, *desc, numSlots))) return r;
+    if (numSlots == 0) return SLG_OK;
+    if (numSlots > kNoAllocTris)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "slg_draw_noalloc: " + std::to_string(numSlots) + " triangles exceed the static limit of " +
+                                                  std::to_string(kNoAllocTris));
+
+    Frame f;
+    std::memset(&f, 0, sizeof(f));
+    f.width = depthTex.w;
+    f.height = depthTex.h;
+    f.tileW = ctx->tileW;
+    f.tileH = ctx->tileH;
+    f.tilesX = (f.width + f.tileW - 1) / f.tileW;
+    f.tilesY = (f.height + f.tileH - 1) / f.tileH;
+    const uint64_t numTiles = (uint64_t)f.tilesX * f.tilesY;
+    if (numTiles > kNoAllocTiles)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "slg_draw_noalloc: a " + std::to_string(f.width) + "x" + std::to_string(f.height) +
+                                                  " framebuffer is " + std::to_string(numTiles) + " tiles of " + std::to_string(f.tileW) + "x" +
+                                                  std::to_string(f.tileH) + ", over the static limit of " + std::to_string(kNoAllocTiles));
+
+    /* resource tables: the context's when they are current, else a copy of
+     * them into the static scratch */
+    const size_t numTex = ctx->textures.size(), numBuf = ctx->vbos.size();
+    cudaError_t e = cudaSuccess;
+    if (!ctx->tablesDirty && ctx->texTable.ptr && ctx->bufTable.ptr)
+    {
+        f.tables.textures = static_cast<const TexView*>(ctx->texTable.ptr);
+        f.tables.buffers = static_cast<const uint8_t* const*>(ctx->bufTable.ptr);
+    }
+    else
+    {
+        if (numTex > kNoAllocTextures || numBuf > kNoAllocBuffers)
+            return ctx->fail(SLG_ERR_INVALID_ARG, "slg_draw_noalloc: more than 256 textures or vertex buffers since the last slg_draw");
+        TexView tex[kNoAllocTextures];
+        const uint8_t* bufs[kNoAllocBuffers];
+        for (size_t i = 0; i < numTex; ++i)
+        {
+            const Texture& t = ctx->textures[i];
+            tex[i].texels = static_cast<const uint8_t*>(t.buf.ptr);
+            tex[i].w = t.w;
+            tex[i].h = t.h;
+            tex[i].d = t.d;
+            tex[i].type = t.type;
+        }
+        for (size_t i = 0; i < numBuf; ++i) bufs[i] = static_cast<const uint8_t*>(ctx->vbos[i].buf.ptr);
+        if (numTex) e = cudaMemcpyAsync(scratch + kOffTexTable, tex, numTex * sizeof(TexView), cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess && numBuf)
+            e = cudaMemcpyAsync(scratch + kOffBufTable, bufs, numBuf * sizeof(void*), cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "slg_draw_noalloc: table upload");
+        f.tables.textures = reinterpret_cast<const TexView*>(scratch + kOffTexTable);
+        f.tables.buffers = reinterpret_cast<const uint8_t* const*>(scratch + kOffBufTable);
+    }
+
+    starts[0] = 0;
+    starts[1] = numSlots;
+    DrawDesc* devDesc = static_cast<DrawDesc*>(ctx->devDescs.ptr) + ctx->descHead;
+    uint64_t* devStarts = static_cast<uint64_t*>(ctx->devStarts.ptr) + ctx->descHead;
+    e = cudaMemcpyAsync(devDesc, desc, sizeof(DrawDesc), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(devStarts, starts, 2 * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(scratch + kOffCounters, 0, kNoAllocZeroBytes, ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "slg_draw_noalloc: descriptor upload");
+    ctx->descHead += 2;
+
+    f.color = colorTex ? static_cast<uint8_t*>(colorTex->buf.ptr) : nullptr;
+    f.colorType = colorTex ? colorTex->type : SLG_COLOR_RGBA_8U;
+    f.depth = static_cast<float*>(depthTex.buf.ptr);
+    viewport_setup((float)f.width, (float)f.height, f.scissor, f.viewport);
+    f.records = reinterpret_cast<float4*>(scratch + kOffRecords);
+    f.varyings = reinterpret_cast<float4*>(scratch + kOffVaryings);
+    f.slotInfo = reinterpret_cast<uint32_t*>(scratch + kOffSlotInfo);
+    f.slotOvf = reinterpret_cast<uint32_t*>(scratch + kOffSlotOvf);
+    f.ovfCount = reinterpret_cast<uint32_t*>(scratch + kOffCounters);
+    f.clipCount = reinterpret_cast<uint32_t*>(scratch + kOffCounters + 4);
+    f.status = reinterpret_cast<int32_t*>(scratch + kOffCounters + 16);
+    f.clipQueue = reinterpret_cast<uint32_t*>(scratch + kOffClipQueue);
+    f.ovfCap = (uint32_t)kNoAllocOvf;
+    f.numSlots = numSlots;
+    f.tileCount = reinterpret_cast<uint32_t*>(scratch + kOffTileCount);
+    f.tileOffset = reinterpret_cast<uint32_t*>(scratch + kOffTileOffset);
+    f.tileCursor = reinterpret_cast<uint32_t*>(scratch + kOffTileCursor);
+    f.entries = reinterpret_cast<uint32_t*>(scratch + kOffEntries);
+    f.entryCap = (uint32_t)kNoAllocEntries;
+    f.draws = devDesc;
+    f.drawSlotStart = devStarts;
+    f.numDraws = 1;
+    f.orderFree = (desc->blend == SLG_BLEND_OFF && desc->depthTest != SLG_DEPTH_TEST_NOT_EQUAL && !ctx->forceOrdered) ? 1 : 0;
+    f.freeDepthFunc = desc->depthTest;
+    f.freeDepthMask = desc->depthMask;
+    f.vsBlock = ctx->vsBlock;
+
+    e = slg::launch_pipeline(f, ctx->keyCap, ctx->stream, nullptr);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "slg_draw_noalloc: launch");
+    return SLG_OK;
+}

@@ -1,0 +1,108 @@
+"""slg_draw_noalloc, the draw whose scratch is one fixed device array, against
+slg_draw on the same scenes: two no-allocation calls in a row, then slg_draw,
+then one more no-allocation call, each frame compared with slg_draw's.
+Tolerance: depth bit-exact (NaN matches NaN), RGBA8 colour within 1 LSB,
+float colour within 1e-5 relative -- the same bar as the oracle parity tests.
+The file name sorts last so that it also runs after every other GPU test."""
+import numpy as np
+import pytest
+
+from softlight_gb300 import api as A
+
+import edge_scenes as E
+
+pytestmark = pytest.mark.gpu
+
+MAX_TRIS = 1024   # SLG_NOALLOC_MAX_TRIANGLES
+MAX_TILES = 64    # SLG_NOALLOC_MAX_TILES
+
+
+@pytest.fixture()
+def ctx(gpu_lib):
+    c = gpu_lib.Context()
+    yield c
+    c.close()
+
+
+def frame(scene, noalloc):
+    c = scene.ctx
+    c.clear_framebuffer(scene.fbo, 0, scene.clear_color, scene.clear_depth)
+    for (mesh, n, shader) in scene.draws:
+        assert n == 1
+        if noalloc:
+            c.draw_noalloc(mesh, shader, scene.fbo)
+        else:
+            c.draw(mesh, shader, scene.fbo)
+    c.finish()
+    return scene.read_color(), scene.read_depth()
+
+
+def assert_same(got, want, label):
+    cg, dg = got
+    cw, dw = want
+    bad = (dg.view(np.uint32) != dw.view(np.uint32)) & ~(np.isnan(dg) & np.isnan(dw))
+    assert not bad.any(), f"{label}: {int(bad.sum())} depth texels differ"
+    if cg.dtype == np.uint8:
+        diff = np.abs(cg.astype(np.int16) - cw.astype(np.int16))
+        assert diff.max(initial=0) <= 1, f"{label}: colour differs by {diff.max()} LSB"
+    else:
+        scale = np.maximum(np.abs(cw), 1e-30)
+        ok = (np.abs(cg - cw) <= 1e-5 * scale) | (cg == cw) | (np.isnan(cg) & np.isnan(cw))
+        assert ok.all(), f"{label}: float colour differs"
+
+
+def check_scene(scene, label):
+    first = frame(scene, noalloc=True)
+    second = frame(scene, noalloc=True)
+    want = frame(scene, noalloc=False)
+    third = frame(scene, noalloc=True)   # now with the context's uploaded resource tables
+    scene.ctx.clear_framebuffer(scene.fbo, 0, scene.clear_color, scene.clear_depth)
+    scene.ctx.finish()
+    blank = scene.read_color()
+    touched = np.any(want[0] != blank, axis=-1) if want[0].ndim == 3 else (want[0] != blank)
+    assert touched.sum() > 100, f"{label}: scene covers too little"
+    assert_same(first, want, f"{label} call 1")
+    assert_same(second, want, f"{label} call 2")
+    assert_same(third, want, f"{label} call 3")
+
+
+def test_opaque_soup_with_clipping(ctx):
+    s = E.random_soup(ctx, num_tris=MAX_TRIS, width=256, height=256, seed=31)
+    check_scene(s, "opaque soup")
+
+
+def test_blended_soup_ordered_path(ctx):
+    s = E.random_soup(ctx, num_tris=600, width=200, height=160, seed=32,
+                      blend=A.BLEND_ALPHA, depth_mask=A.DEPTH_MASK_OFF)
+    check_scene(s, "blended soup")
+
+
+def test_float_target(ctx):
+    s = E.random_soup(ctx, num_tris=400, width=128, height=96, seed=33,
+                      color_type=A.COLOR_RGBA_FLOAT, program=A.PROGRAM_VCOLOR_TEXF)
+    check_scene(s, "float target")
+
+
+def test_largest_framebuffer_at_64px_tiles(ctx):
+    ctx.set_tile_size(64, 64)
+    s = E.random_soup(ctx, num_tris=800, width=512, height=512, seed=34)
+    check_scene(s, "512x512 at 64x64 tiles")
+
+
+def test_limits_rejected_before_any_work(ctx):
+    s = E.random_soup(ctx, num_tris=MAX_TRIS + 1, width=64, height=64, seed=35)
+    c = s.ctx
+    c.clear_framebuffer(s.fbo, 0, s.clear_color, s.clear_depth)
+    mesh, _, shader = s.draws[0]
+    with pytest.raises(A.SLError, match=str(MAX_TRIS)):
+        c.draw_noalloc(mesh, shader, s.fbo)
+    c.finish()
+    assert (s.read_depth() == s.clear_depth).all()
+
+    big = E.random_soup(ctx, num_tris=100, width=257, height=256, seed=36)  # 9 x 8 tiles of 32 x 32
+    big.ctx.clear_framebuffer(big.fbo, 0, big.clear_color, big.clear_depth)
+    mesh, _, shader = big.draws[0]
+    with pytest.raises(A.SLError, match=str(MAX_TILES)):
+        big.ctx.draw_noalloc(mesh, shader, big.fbo)
+    big.ctx.finish()
+    assert (big.read_depth() == big.clear_depth).all()
