@@ -293,6 +293,45 @@ int slg_set_batch_graphs(slg_context* ctx, int enable);
 int slg_autotune(slg_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, size_t fboId,
                  const double rgba[4], double depth, int out[3]);
 
+/*-----------------------------------------------------------------------------
+ * Differentiable rendering (no reference counterpart: SoftLight has no
+ * adjoint). Covers one opaque SLG_PROGRAM_VCOLOR_TEXF draw per framebuffer
+ * frame. The model: the draw's exact coverage is frozen as a visibility map;
+ * at each covered pixel (x, y) the perspective-correct barycentrics of the
+ * visible triangle's unsnapped clip-space vertices at the pixel's NDC point
+ * interpolate vertex colour and uv, the float texture is sampled bilinearly
+ * (REPEAT, the draw path's texel addressing), and out = colour * texel.
+ * Device buffers below are plain device (or managed, or pinned host)
+ * pointers; work is queued on the context's stream (slg_context_stream).
+-----------------------------------------------------------------------------*/
+/* Attach (enable != 0) or drop a visibility map: one uint32 per pixel of the
+ * depth attachment, cleared to 0 with the depth buffer; every opaque draw
+ * into the framebuffer then writes, where its fragment wins the depth test,
+ * 1 + the index of the winning triangle within the draw. Draws that blend or
+ * mix depth rules are rejected while it is attached. */
+int slg_fbo_enable_visibility(slg_context* ctx, size_t fboId, int enable);
+int slg_fbo_read_visibility(slg_context* ctx, size_t fboId, uint32_t* dst, size_t count);
+
+/* The model's image for the draw (mesh, shader) over the framebuffer's
+ * visibility map: width*height RGBA floats into `image` (device, 16-byte
+ * aligned). The model covers a pixel when its visible triangle's
+ * barycentrics there are all >= -1 (within one triangle height of the
+ * unsnapped triangle; snapping lets slivers cover pixels far outside it);
+ * every other pixel takes the framebuffer's colour when colour attachment 0
+ * is RGBA float, else 0, and carries no gradient. */
+int slg_diff_shade(slg_context* ctx, const slg_mesh* mesh, size_t shaderId, size_t fboId, float* image, size_t count);
+
+/* Adjoint of slg_diff_shade: for dL/d image (width*height RGBA floats),
+ * ADDS dL/d vertex position, colour and uv into dVertices -- floats laid
+ * out like the draw's vertex buffer (pos[3], rgba[4], uv[2] at binding 0's
+ * offset and stride) -- and dL/d texel into dTexels (texW*texH RGBA floats).
+ * Recomputes every pixel's barycentrics, varyings and texture footprint
+ * from the buffers; stores nothing from the forward but the visibility map.
+ * Accumulates with FP32 atomics staged per 16x16 pixel tile in shared
+ * memory, so the summation order (and the last bits) vary between runs. */
+int slg_draw_adjoint(slg_context* ctx, const slg_mesh* mesh, size_t shaderId, size_t fboId, const float* dImage,
+                     size_t dImageCount, float* dVertices, size_t dVertexCount, float* dTexels, size_t dTexelCount);
+
 #ifdef __cplusplus
 }
 #endif

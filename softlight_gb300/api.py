@@ -104,6 +104,11 @@ _GPU_SIGNATURES = [
     ("autotune", C.c_int, [C.c_void_p, C.POINTER(DrawCmd), C.c_size_t, C.c_size_t, C.POINTER(C.c_double),
                            C.c_double, C.POINTER(C.c_int)]),
     ("draw_noalloc", C.c_int, [C.c_void_p, C.POINTER(Mesh), C.c_size_t, C.c_size_t]),
+    ("fbo_enable_visibility", C.c_int, [C.c_void_p, C.c_size_t, C.c_int]),
+    ("fbo_read_visibility", C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t]),
+    ("diff_shade", C.c_int, [C.c_void_p, C.POINTER(Mesh), C.c_size_t, C.c_size_t, C.c_void_p, C.c_size_t]),
+    ("draw_adjoint", C.c_int, [C.c_void_p, C.POINTER(Mesh), C.c_size_t, C.c_size_t, C.c_void_p, C.c_size_t,
+                               C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t]),
 ]
 
 
@@ -289,6 +294,23 @@ class SLContext:
     def draw_noalloc(self, mesh, shader, fbo):
         """slg_draw with its scratch in a fixed device array (no allocation)."""
         self._call("draw_noalloc", C.byref(mesh), shader, fbo)
+
+    # -- differentiable rendering (device pointers as integers) -------------
+    def fbo_enable_visibility(self, fbo, enable=True):
+        self._call("fbo_enable_visibility", fbo, 1 if enable else 0)
+
+    def fbo_read_visibility(self, fbo, shape):
+        out = np.empty(shape, np.uint32)
+        self._call("fbo_read_visibility", fbo, out.ctypes.data_as(C.c_void_p), out.size)
+        return out
+
+    def diff_shade(self, mesh, shader, fbo, image_ptr, count):
+        self._call("diff_shade", C.byref(mesh), shader, fbo, C.c_void_p(image_ptr), count)
+
+    def draw_adjoint(self, mesh, shader, fbo, d_image_ptr, d_image_count, d_vertices_ptr, d_vertex_count,
+                     d_texels_ptr, d_texel_count):
+        self._call("draw_adjoint", C.byref(mesh), shader, fbo, C.c_void_p(d_image_ptr), d_image_count,
+                   C.c_void_p(d_vertices_ptr), d_vertex_count, C.c_void_p(d_texels_ptr), d_texel_count)
 
     def finish(self):
         self._call("finish")

@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/slg.h"
+#include "slg_adjoint.cuh"
 #include "slg_device.cuh"
 #include "slg_kernels.cuh"
 
@@ -48,6 +49,8 @@ struct Fbo
     unsigned numColors = 0;
     size_t colors[4] = {SLG_INVALID_ID, SLG_INVALID_ID, SLG_INVALID_ID, SLG_INVALID_ID};
     size_t depth = SLG_INVALID_ID;
+    DevBuffer vis;          /* visibility map, when enabled */
+    bool visEnabled = false;
 };
 struct Ubo { DevBuffer buf; uint8_t shadow[1024] = {}; };
 struct Shader
@@ -637,6 +640,15 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
 
     f.vsBlock = ctx->vsBlock;
 
+    if (fbo.visEnabled)
+    {
+        if (!f.orderFree)
+            return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map takes opaque draws only (no blending, one depth rule)");
+        if (fbo.vis.bytes < (size_t)f.width * f.height * sizeof(uint32_t))
+            return ctx->fail(SLG_ERR_INVALID_ARG, "visibility map is smaller than the framebuffer (enable it again after resizing)");
+        f.ids = static_cast<uint32_t*>(fbo.vis.ptr);
+    }
+
     if (batch && ctx->batchGraphs && !ctx->profileStages)
     {
         return launch_batch_graph(ctx, f, descs, starts, n);
@@ -694,6 +706,7 @@ void slg_context_destroy(slg_context* ctx)
     for (Ibo& v : ctx->ibos) dev_free(v.buf);
     for (Texture& t : ctx->textures) dev_free(t.buf);
     for (Ubo& u : ctx->ubos) dev_free(u.buf);
+    for (Fbo& f : ctx->fbos) dev_free(f.vis);
     DevBuffer* scratch[] = {&ctx->texTable, &ctx->bufTable, &ctx->records, &ctx->varyings, &ctx->slotInfo, &ctx->slotOvf,
                             &ctx->ovfCount, &ctx->clipQueue, &ctx->clipCount, &ctx->tileCount, &ctx->tileOffset,
                             &ctx->tileCursor, &ctx->entries,
@@ -930,7 +943,10 @@ int slg_clear_depth_buffer(slg_context* ctx, size_t fbo, double depth)
 {
     if (!id_ok(fbo, ctx->fbos.size()) || ctx->fbos[fbo].depth == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo");
     const double d[4] = {depth, 0, 0, 0};
-    return clear_texture(ctx, ctx->fbos[fbo].depth, d);
+    int r = clear_texture(ctx, ctx->fbos[fbo].depth, d);
+    if (r || !ctx->fbos[fbo].visEnabled) return r;
+    cudaError_t e = cudaMemsetAsync(ctx->fbos[fbo].vis.ptr, 0, ctx->fbos[fbo].vis.bytes, ctx->stream);
+    return (e == cudaSuccess) ? SLG_OK : ctx->cuda_fail(e, "visibility clear");
 }
 
 int slg_clear_framebuffer(slg_context* ctx, size_t fbo, unsigned att, const double rgba[4], double depth)
@@ -1283,3 +1299,145 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
     if (e != cudaSuccess) return ctx->cuda_fail(e, "slg_draw_noalloc: launch");
     return SLG_OK;
 }
+
+/*-----------------------------------------------------------------------------
+ * Differentiable rendering (no reference counterpart; the reference has no
+ * adjoint). An opaque draw into a framebuffer with a visibility map records,
+ * per pixel, which triangle won the depth test; given that map,
+ * slg_diff_shade evaluates the differentiable shading model of the
+ * vertex-colour x float-texture program and slg_draw_adjoint its gradients
+ * (model and layout: softlight_gb300/csrc/slg_adjoint.cu).
+-----------------------------------------------------------------------------*/
+namespace
+{
+
+bool device_visible(const void* p)
+{
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged || attr.type == cudaMemoryTypeHost;
+}
+
+int diff_args(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId, slg::DiffArgs& a, uint64_t& vertexBytes)
+{
+    if (!m) return ctx->fail(SLG_ERR_INVALID_ARG, "null mesh");
+    if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
+    const Fbo& fbo = ctx->fbos[fboId];
+    if (!fbo.visEnabled || fbo.depth == SLG_INVALID_ID)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "framebuffer has no visibility map (slg_fbo_enable_visibility)");
+    const Texture& depthTex = ctx->textures[fbo.depth];
+    if (fbo.vis.bytes < (size_t)depthTex.w * depthTex.h * sizeof(uint32_t))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "visibility map is smaller than the framebuffer");
+
+    const DrawRequest req = {*m, 1, shaderId, 0};
+    DrawDesc d;
+    uint64_t numSlots = 0;
+    int r = build_desc(ctx, req, 0, d, numSlots);
+    if (r) return r;
+    const Shader& sh = ctx->shaders[shaderId];
+    if (sh.vsProgram != SLG_PROGRAM_VCOLOR_TEXF || sh.fsProgram != SLG_PROGRAM_VCOLOR_TEXF)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "the differentiable model covers SLG_PROGRAM_VCOLOR_TEXF draws only");
+    if ((d.b0Offset & 3) || (d.b0Stride & 3)) return ctx->fail(SLG_ERR_INVALID_ARG, "binding 0 offset and stride must be multiples of 4 bytes");
+    if (d.numElements / 3 > 0xFFFFFFFEull) return ctx->fail(SLG_ERR_INVALID_ARG, "too many triangles");
+    uint32_t texId = 0;
+    std::memcpy(&texId, ctx->ubos[sh.ubo].shadow + offsetof(slg_vcolor_uniforms, textureId), 4);
+    const Texture& tex = ctx->textures[texId];   /* validated by build_desc */
+
+    const Vao& vao = ctx->vaos[m->vaoId];
+    const uint64_t maxVertex = (d.indexType >= 0) ? ctx->ibos[vao.ibo].maxIndex : (d.elementBegin + 3 * d.numTris - 1);
+    vertexBytes = (uint64_t)d.b0Offset + (uint64_t)d.b0Stride * maxVertex + 9 * sizeof(float);
+
+    std::memset(&a, 0, sizeof(a));
+    a.vbo = d.vbo;
+    a.b0Offset = d.b0Offset;
+    a.b0Stride = d.b0Stride;
+    a.ibo = d.ibo;
+    a.indexType = d.indexType;
+    a.elementBegin = d.elementBegin;
+    a.numTris = (uint32_t)(d.numElements / 3);
+    a.mvp = reinterpret_cast<const float*>(d.ubo + offsetof(slg_vcolor_uniforms, mvpMatrix));
+    a.texels = static_cast<const float4*>(tex.buf.ptr);
+    a.texW = tex.w;
+    a.texH = tex.h;
+    a.vis = static_cast<const uint32_t*>(fbo.vis.ptr);
+    if (fbo.numColors > 0 && fbo.colors[0] != SLG_INVALID_ID && ctx->textures[fbo.colors[0]].type == SLG_COLOR_RGBA_FLOAT &&
+        ctx->textures[fbo.colors[0]].w == depthTex.w && ctx->textures[fbo.colors[0]].h == depthTex.h)
+        a.exact = static_cast<const float4*>(ctx->textures[fbo.colors[0]].buf.ptr);
+    a.width = depthTex.w;
+    a.height = depthTex.h;
+    return SLG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int slg_fbo_enable_visibility(slg_context* ctx, size_t fboId, int enable)
+{
+    if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
+    Fbo& fbo = ctx->fbos[fboId];
+    if (!enable)
+    {
+        cudaStreamSynchronize(ctx->stream);
+        dev_free(fbo.vis);
+        fbo.visEnabled = false;
+        return SLG_OK;
+    }
+    if (fbo.depth == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "a visibility map needs a depth attachment");
+    const Texture& d = ctx->textures[fbo.depth];
+    int r = dev_alloc(ctx, fbo.vis, (size_t)d.w * d.h * sizeof(uint32_t), true);
+    if (r) return r;
+    fbo.visEnabled = true;
+    return SLG_OK;
+}
+
+int slg_fbo_read_visibility(slg_context* ctx, size_t fboId, uint32_t* dst, size_t count)
+{
+    if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
+    const Fbo& fbo = ctx->fbos[fboId];
+    if (!fbo.visEnabled) return ctx->fail(SLG_ERR_INVALID_ARG, "framebuffer has no visibility map");
+    if (!dst || count * sizeof(uint32_t) > fbo.vis.bytes) return ctx->fail(SLG_ERR_INVALID_ARG, "bad destination size");
+    cudaError_t e = cudaMemcpyAsync(dst, fbo.vis.ptr, count * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "visibility read");
+    return check_status(ctx);
+}
+
+int slg_diff_shade(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId, float* image, size_t count)
+{
+    slg::DiffArgs a;
+    uint64_t vertexBytes = 0;
+    int r = diff_args(ctx, m, shaderId, fboId, a, vertexBytes);
+    if (r) return r;
+    if (!image || ((uintptr_t)image & 15) || count < (size_t)a.width * a.height * 4 || !device_visible(image))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "image must be a 16-byte aligned device buffer of width*height*4 floats");
+    a.image = reinterpret_cast<float4*>(image);
+    cudaError_t e = slg::launch_diff_shade(a, ctx->stream);
+    return (e == cudaSuccess) ? SLG_OK : ctx->cuda_fail(e, "diff shade launch");
+}
+
+int slg_draw_adjoint(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId, const float* dImage, size_t dImageCount,
+                     float* dVertices, size_t dVertexCount, float* dTexels, size_t dTexelCount)
+{
+    slg::DiffArgs a;
+    uint64_t vertexBytes = 0;
+    int r = diff_args(ctx, m, shaderId, fboId, a, vertexBytes);
+    if (r) return r;
+    if (!dImage || ((uintptr_t)dImage & 15) || dImageCount < (size_t)a.width * a.height * 4 || !device_visible(dImage))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "dImage must be a 16-byte aligned device buffer of width*height*4 floats");
+    if (!dVertices || ((uintptr_t)dVertices & 3) || (uint64_t)dVertexCount * sizeof(float) < vertexBytes || !device_visible(dVertices))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "dVertices must be a device buffer covering the draw's vertices in the vertex buffer's layout");
+    if (!dTexels || ((uintptr_t)dTexels & 15) || dTexelCount < (size_t)a.texW * a.texH * 4 || !device_visible(dTexels))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "dTexels must be a 16-byte aligned device buffer of texW*texH*4 floats");
+    a.dImage = reinterpret_cast<const float4*>(dImage);
+    a.dVertices = dVertices;
+    a.dTexels = reinterpret_cast<float4*>(dTexels);
+    cudaError_t e = slg::launch_diff_adjoint(a, ctx->stream);
+    return (e == cudaSuccess) ? SLG_OK : ctx->cuda_fail(e, "adjoint launch");
+}
+
+} // extern "C"

@@ -123,6 +123,10 @@ struct Frame
 
     /* threads per block of the vertex stage (64, 128 or 256): triangles per CTA */
     int32_t vsBlock;
+
+    /* optional visibility map (order-free raster only): per pixel written,
+     * 1 + the launch slot (triangle) of the winning fragment; null: off */
+    uint32_t* ids;
 };
 
 enum StatusBits

@@ -1215,6 +1215,10 @@ __global__ void __launch_bounds__(TH * 4) raster_free_kernel(const Frame f, int 
         {
             f.depth[gi] = sZ[idx];
         }
+        if (f.ids)
+        {
+            f.ids[gi] = (key >> kSubShift) + 1u;
+        }
     }
 }
 

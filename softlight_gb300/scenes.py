@@ -12,6 +12,8 @@ Configurations (BASELINE workloads):
   c2  the sphere x1024 instances, 1024^2 noise texture, Blinn-Phong 4 lights, 1920x1080
   c3  2M-triangle soup, 30% back-facing, 10% crossing the near plane, alpha blend, 1920x1080
   c4  256 uneven meshes (12..65k tris) each with its own 512^2 texture, Lambert+ambient, 3840x2160
+  c5  10k-triangle noise-displaced sphere, per-vertex colours x 256^2 float RGBA texture,
+      512x512 float target with a visibility map (the differentiable render)
 """
 import math
 import struct
@@ -501,4 +503,99 @@ def build_c4(ctx, num_draws=256, width=3840, height=2160, tex_size=512, batched=
     return s
 
 
-BUILDERS = {"c1": build_c1, "c2": build_c2, "c3": build_c3, "c4": build_c4}
+def displaced_sphere(lon=100, lat=50, seed=5, amplitude=0.12, waves=6):
+    """UV sphere (lon*lat*2 triangles) with radius 1 + amplitude * noise(n),
+    noise a seeded sum of sinusoids of the direction: positions (V x 3),
+    uvs (V x 2), triangle indices."""
+    verts, idx = uv_sphere(lon, lat)
+    n = verts[:, 5:8].astype(np.float64)
+    rng = np.random.default_rng(seed)
+    freq = rng.normal(size=(waves, 3)) * 2.5
+    phase = rng.uniform(0.0, 2.0 * math.pi, waves)
+    amp = rng.uniform(0.3, 1.0, waves)
+    noise = (amp[None, :] * np.sin(n @ freq.T + phase[None, :])).sum(1) / amp.sum()
+    pos = n * (1.0 + amplitude * noise)[:, None]
+    return pos.astype(np.float32), verts[:, 3:5].copy(), idx
+
+
+def c5_uv(uv):
+    """The differentiable scene's texture coordinates: the sphere's (j/lon,
+    i/lat) grid scaled and offset so that no mesh edge lies on a texel
+    boundary (where the bilinear derivative jumps) and no triangle spans the
+    repeat seam."""
+    return (np.asarray(uv, np.float64) * [0.97, 0.93] + [0.0157, 0.0347]).astype(np.float32)
+
+
+class DiffScene(Scene):
+    """One opaque vertex-colour x float-texture draw whose per-vertex
+    positions and colours and whose texels are parameters: the scene of the
+    differentiable render."""
+
+    def set_params(self, pos=None, col=None, tex=None):
+        if pos is not None:
+            self.pos = np.ascontiguousarray(pos, np.float32)
+        if col is not None:
+            self.col = np.ascontiguousarray(col, np.float32)
+        if tex is not None:
+            self.tex = np.ascontiguousarray(tex, np.float32)
+            self.ctx.texture_set_texels(self.tex_id, self.tex)
+        if pos is not None or col is not None:
+            self.ctx.vbo_assign(self.vbo, self.vertex_array())
+
+    def vertex_array(self):
+        return np.concatenate([self.pos, self.col, self.uv], 1).astype(np.float32)
+
+
+def build_c5(ctx, width=512, height=512, tex_size=256, lon=100, lat=50, seed=5, index_dtype=np.uint32):
+    """Differentiable render: a 10k-triangle noise-displaced sphere with
+    float32 per-vertex colours and a tex_size^2 float32 RGBA texture,
+    vertex colour x texture, depth LESS, 512x512 RGBA float target.
+    index_dtype None draws the triangles non-indexed (vertices expanded)."""
+    s = DiffScene(ctx, f"c5_diff_{width}x{height}", width, height, color_type=A.COLOR_RGBA_FLOAT)
+    s.clear_color = (0.0, 0.0, 0.0, 0.0)
+    pos, uv, idx = displaced_sphere(lon, lat, seed)
+    uv = c5_uv(uv)
+    if index_dtype is None:
+        pos, uv, idx = pos[idx], uv[idx], None
+    rng = np.random.default_rng(seed + 1)
+    col = np.concatenate([rng.uniform(0.3, 1.0, (pos.shape[0], 3)), np.ones((pos.shape[0], 1))], 1)
+    ntri = pos.shape[0] // 3 if idx is None else idx.size // 3
+    s.tri = np.arange(3 * ntri).reshape(-1, 3) if idx is None else idx.reshape(-1, 3).astype(np.int64)
+    s.pos, s.uv = pos, uv.astype(np.float32)
+    s.col = col.astype(np.float32)
+    s.tex = value_noise(tex_size, tex_size, seed=seed + 2, octaves=3).astype(np.float32)
+    s.vbo = ctx.create_vbo()
+    ctx.vbo_init(s.vbo, s.vertex_array())
+    vao = ctx.create_vao()
+    ctx.vao_set_vertex_buffer(vao, s.vbo)
+    ctx.vao_set_binding(vao, 0, 0, 36, 3, A.VERTEX_DATA_FLOAT)
+    if idx is None:
+        mesh = A.Mesh(vao, 0, 3 * ntri, A.RENDER_MODE_TRIANGLES, 0)
+        s.geometry_bytes = s.vertex_array().nbytes
+    else:
+        ibo = ctx.create_ibo()
+        ctx.ibo_init(ibo, idx.astype(index_dtype))
+        ctx.vao_set_index_buffer(vao, ibo)
+        mesh = A.Mesh(vao, 0, idx.size, A.RENDER_MODE_INDEXED_TRIANGLES, 0)
+        s.geometry_bytes = s.vertex_array().nbytes + idx.astype(index_dtype).nbytes
+    s.tex_id = s.add_texture_rgbaf(s.tex)
+    s.mvp = perspective(60.0, width / height, 0.1, 100.0) @ look_at((0, 0, 2.5), (0, 0, 0), (0, 1, 0))
+    sh = s.add_shader(A.PROGRAM_VCOLOR_TEXF, 2, vcolor_uniforms(s.mvp, s.tex_id))
+    s.mesh, s.shader = mesh, sh
+    s.draws.append((mesh, 1, sh))
+    s.num_triangles = ntri
+    if ctx.gpu:
+        ctx.fbo_enable_visibility(s.fbo)   # the CPU restatement has no visibility map
+    return s
+
+
+def c5_perturbed(s, seed=6, col_sigma=0.05, tex_sigma=0.05, pos_sigma=0.01):
+    """Seeded perturbation of a c5 scene's parameters (the target's)."""
+    rng = np.random.default_rng(seed)
+    pos = s.pos + rng.normal(0.0, pos_sigma, s.pos.shape).astype(np.float32)
+    col = s.col + rng.normal(0.0, col_sigma, s.col.shape).astype(np.float32)
+    tex = s.tex + rng.normal(0.0, tex_sigma, s.tex.shape).astype(np.float32)
+    return pos, col, tex
+
+
+BUILDERS = {"c1": build_c1, "c2": build_c2, "c3": build_c3, "c4": build_c4, "c5": build_c5}

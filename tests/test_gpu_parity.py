@@ -121,6 +121,15 @@ def test_float_target_and_texture(ctxs):
     compare_scenes(sg, so, "texf")
 
 
+def test_c5_differentiable_scene_exact(ctxs):
+    """The differentiable-render scene (its framebuffer records a visibility
+    map on the GPU) renders exactly like the oracle."""
+    g, o = ctxs
+    sg, so = render_both(S.build_c5, g, o)
+    compare_scenes(sg, so, "c5")
+    assert (sg.read_depth() < 1.0).sum() > 100000
+
+
 def test_big_triangles_and_ties(ctxs):
     g, o = ctxs
     for tile in [(8, 8), (32, 32), (64, 64)]:
