@@ -35,7 +35,8 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
+    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    p.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-render timing")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     p.add_argument("--tile", default="auto", help="screen tile WxH (8x8 .. 64x64) or auto (autotuner)")
@@ -59,6 +60,9 @@ def workload_config(name):
     if name == "c3":
         return S.build_c3, {}, {"workload": "2M-triangle soup, 30% back-facing, 10% near-plane clipped, alpha blend, 2048^2 texture",
                                  "resolution": "1920x1080"}
+    if name == "c5":
+        return S.build_c5, {}, {"workload": "10k-triangle noise-displaced sphere, float32 vertex colours x 256^2 float32 texture, "
+                                             "visibility map recorded", "resolution": "512x512"}
     return S.build_c4, {}, {"workload": "256 uneven meshes (12..65k tris), per-draw 512^2 textures, Lambert+ambient, one batched launch",
                              "resolution": "3840x2160", "draws": 256}
 
@@ -197,6 +201,69 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def adjoint_timing(sg, torch, flush, steps, warmup):
+    """Differentiable render (512x512, 10k-triangle displaced sphere, vertex
+    colours x 256^2 float texture): device time of the forward (clear + exact
+    draw recording the visibility map + model image) and of the adjoint
+    (gradient buffers zeroed + adjoint kernel), each frame timed with CUDA
+    events on the context's stream after an L2 flush."""
+    from softlight_gb300 import scenes as S
+    ctx = sg.Context()
+    s = S.build_c5(ctx)
+    tw, th, vb = ctx.autotune([sg.api.DrawCmd(s.mesh, 1, s.shader)], s.fbo, s.clear_color, s.clear_depth)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+    img = torch.empty(s.height, s.width, 4, device="cuda")
+    target = torch.rand(s.height, s.width, 4, device="cuda", generator=torch.Generator("cuda").manual_seed(5))
+    nv = s.pos.shape[0]
+    dvert = torch.zeros(nv * 9, device="cuda")
+    dtex = torch.zeros(s.tex.size, device="cuda")
+    d_img = torch.empty_like(img)
+
+    def forward():
+        s.render()
+        ctx.diff_shade(s.mesh, s.shader, s.fbo, img.data_ptr(), img.numel())
+
+    def backward():
+        with torch.cuda.stream(stream):
+            dvert.zero_()
+            dtex.zero_()
+        ctx.draw_adjoint(s.mesh, s.shader, s.fbo, d_img.data_ptr(), d_img.numel(), dvert.data_ptr(), dvert.numel(),
+                         dtex.data_ptr(), dtex.numel())
+
+    def timed(fn, k):
+        out = []
+        for i in range(k):
+            with torch.cuda.stream(stream):
+                flush.fill_(i & 0xFF)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            fn()
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return out
+
+    for _ in range(max(3, warmup)):
+        forward()
+    ctx.finish()
+    with torch.cuda.stream(stream):
+        d_img.copy_(2.0 * (img - target))
+    for _ in range(max(3, warmup)):
+        backward()
+    ctx.finish()
+    f_ms = statistics.median(timed(forward, steps))
+    b_ms = statistics.median(timed(backward, steps))
+    ctx.close()
+    return {"workload": "differentiable render 512x512: 10k-triangle noise-displaced sphere, float32 vertex colours "
+                        "x 256^2 float32 RGBA texture, L2 image loss",
+            "unit": "ms/frame", "forward_ms": f_ms, "adjoint_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
+            "forward": "clear + exact draw recording the visibility map + model image (slg_diff_shade)",
+            "adjoint": "gradient buffers zeroed + slg_draw_adjoint (forward recomputed per pixel)",
+            "tile": f"{tw}x{th}", "vertex_block": vb, "l2": "flushed before each timed frame"}
+
+
 def launches_per_frame(scene):
     """Kernels one frame launches: two clears, then vs_setup, clip, tile_scan,
     bin_fill and raster per launch, plus tile_sort on the ordered path."""
@@ -296,10 +363,14 @@ def run_gpu(args):
         inst_host = torch.empty(inst[1].nbytes, dtype=torch.uint8, pin_memory=True).numpy()
         inst_host[:] = inst[1].view(np.uint8).reshape(-1)
         h2d += inst_host.nbytes
-    color_host = torch.empty(scene.height * scene.width * 4, dtype=torch.uint8, pin_memory=True).numpy()
+    color_bytes = scene.height * scene.width * sg.api.BYTES_PER_COLOR[scene.color_type]
+    color_host = torch.empty(color_bytes, dtype=torch.uint8, pin_memory=True).numpy()
+
+    def read_color():
+        ctx.texture_read(scene.color_tex, (color_bytes,), np.uint8, out=color_host)
     for _ in range(2):
         scene.render()
-        ctx.texture_read(scene.color_tex, (scene.height, scene.width, 4), np.uint8, out=color_host.reshape(scene.height, scene.width, 4))
+        read_color()
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
@@ -309,7 +380,7 @@ def run_gpu(args):
         if inst is not None:
             ctx.vbo_assign(inst[0], inst_host)
         scene.render()
-        ctx.texture_read(scene.color_tex, (scene.height, scene.width, 4), np.uint8, out=color_host.reshape(scene.height, scene.width, 4))
+        read_color()
     e2e_s = time.perf_counter() - t0
     if world > 1:
         t = torch.tensor([e2e_s], device="cuda")
@@ -353,11 +424,13 @@ def run_gpu(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": cfg,
                 "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d,
-                        "d2h_bytes_per_step": scene.height * scene.width * 4},
+                        "d2h_bytes_per_step": color_bytes},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks.summary(),
                 "gpu_launches": args.steps * (launches_per_frame(scene))}
         if per_draw is not None:
             line["per_draw"] = per_draw
+        if not args.no_adjoint and world == 1:
+            line["adjoint"] = adjoint_timing(sg, torch, flush, max(args.steps, 5), args.warmup)
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:

@@ -327,7 +327,7 @@ int slg_diff_shade(slg_context* ctx, const slg_mesh* mesh, size_t shaderId, size
  * offset and stride) -- and dL/d texel into dTexels (texW*texH RGBA floats).
  * Recomputes every pixel's barycentrics, varyings and texture footprint
  * from the buffers; stores nothing from the forward but the visibility map.
- * Accumulates with FP32 atomics staged per 16x16 pixel tile in shared
+ * Accumulates with FP32 atomics staged per 32x8 pixel tile in shared
  * memory, so the summation order (and the last bits) vary between runs. */
 int slg_draw_adjoint(slg_context* ctx, const slg_mesh* mesh, size_t shaderId, size_t fboId, const float* dImage,
                      size_t dImageCount, float* dVertices, size_t dVertexCount, float* dTexels, size_t dTexelCount);

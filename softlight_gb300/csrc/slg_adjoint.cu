@@ -32,10 +32,13 @@
  * Nothing from the forward pass is stored but the visibility map (4 bytes a
  * pixel): the adjoint recomputes each pixel's barycentrics, varyings and
  * texture footprint from the vertex buffer and the texture, then runs the
- * chain rule backwards. Gradients are accumulated per 16x16 pixel tile in
- * shared-memory hash tables (one for vertices, one for texels) with shared
- * FP32 atomics, then flushed to HBM with one global FP32 atomic per touched
- * vertex or texel component and tile.
+ * chain rule backwards. A warp owns 32 consecutive pixels of a row; their
+ * contributions are first summed over runs of lanes that share a triangle
+ * (vertex gradients) or a bilinear cell (texel gradients) with warp
+ * shuffles, then the last lane of each run adds the sums into per-tile
+ * (32x8 pixels) shared-memory hash tables, one for vertices and one for
+ * texels, with shared FP32 atomics; each tile flushes its tables to HBM
+ * with one global FP32 atomic per touched vertex or texel component.
  */
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -49,7 +52,7 @@ namespace slg
 namespace
 {
 
-constexpr int kTileX = 16, kTileY = 16, kThreads = kTileX * kTileY;
+constexpr int kTileX = 32, kTileY = 8, kThreads = kTileX * kTileY;   /* one warp per row */
 constexpr int kVertSlots = 512;   /* distinct vertices a tile can stage */
 constexpr int kTexSlots = 1024;   /* distinct texels a tile can stage */
 constexpr int kProbes = 16;       /* linear-probe bound; then the update goes straight to HBM */
@@ -209,6 +212,36 @@ __device__ __forceinline__ int stage_slot(uint32_t* keys, int mask, uint32_t key
     return -1;
 }
 
+/* Segmented inclusive sum of v over runs of equal `key` in consecutive lanes
+ * (lane i and i + 1 in one run when their keys match): afterwards the last
+ * lane of each run holds the run's totals. Returns whether this lane is the
+ * last of its run. All 32 lanes must call it. */
+template <int N>
+__device__ __forceinline__ bool run_reduce(uint32_t key, float (&v)[N])
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t prev = __shfl_up_sync(0xFFFFFFFFu, key, 1);
+    const uint32_t heads = __ballot_sync(0xFFFFFFFFu, lane == 0 || key != prev);
+    const int start = 31 - __clz(heads & (0xFFFFFFFFu >> (31 - lane)));
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1)
+    {
+        const bool take = lane - off >= start;
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+        {
+            const float t = __shfl_up_sync(0xFFFFFFFFu, v[i], off);
+            if (take) v[i] += t;
+        }
+    }
+    return lane == 31 || ((heads >> (lane + 1)) & 1u);
+}
+
+/* One warp per 32-pixel row segment. Each pixel's contributions are summed
+ * over runs of lanes with the same triangle (vertex gradients) and the same
+ * bilinear cell (texel gradients) with warp shuffles; the last lane of each
+ * run adds the run's sums into the tile's shared tables, which are flushed
+ * to HBM with global FP32 atomics once per tile. */
 __global__ void __launch_bounds__(kThreads) diff_adjoint_kernel(const DiffArgs a)
 {
     __shared__ uint32_t vKey[kVertSlots];
@@ -229,8 +262,20 @@ __global__ void __launch_bounds__(kThreads) diff_adjoint_kernel(const DiffArgs a
     const int x = blockIdx.x * kTileX + (tid % kTileX);
     const int y = blockIdx.y * kTileY + (tid / kTileX);
     PixelModel m;
-    if (x < a.width && y < a.height && pixel_model(a, x, y, a.vis[(size_t)x + (size_t)a.width * y], m))
+    const bool live = x < a.width && y < a.height && pixel_model(a, x, y, a.vis[(size_t)x + (size_t)a.width * y], m);
+
+    float vv[3 * kVertFloats];
+    float tv[16];
+#pragma unroll
+    for (int i = 0; i < 3 * kVertFloats; ++i) vv[i] = 0.f;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) tv[i] = 0.f;
+    uint32_t triKey = kEmpty, cellKey = kEmpty;
+
+    if (live)
     {
+        triKey = a.vis[(size_t)x + (size_t)a.width * y];
+        cellKey = m.ti[0];
         const float4 g = a.dImage[(size_t)x + (size_t)a.width * y];
         const float4 gc = f4_mul(g, m.texel);    /* dL/d colour varying */
         const float4 gt = f4_mul(g, m.colour);   /* dL/d texture sample */
@@ -272,36 +317,56 @@ __global__ void __launch_bounds__(kThreads) diff_adjoint_kernel(const DiffArgs a
             /* clip gradient (x, y, 0, w), then positions: dp_c = sum_r M[r][c] dclip_r */
             const float dcx = dhp[k].x, dcy = dhp[k].y;
             const float dcw = -(m.nx * dcx + m.ny * dcy);
-            float vals[kVertFloats];
-            vals[0] = (M[0] * dcx + M[1] * dcy) + M[3] * dcw;
-            vals[1] = (M[4] * dcx + M[5] * dcy) + M[7] * dcw;
-            vals[2] = (M[8] * dcx + M[9] * dcy) + M[11] * dcw;
-            vals[3] = gc.x * m.lam[k];
-            vals[4] = gc.y * m.lam[k];
-            vals[5] = gc.z * m.lam[k];
-            vals[6] = gc.w * m.lam[k];
-            vals[7] = du * m.lam[k];
-            vals[8] = dv * m.lam[k];
+            float* o = vv + k * kVertFloats;
+            o[0] = (M[0] * dcx + M[1] * dcy) + M[3] * dcw;
+            o[1] = (M[4] * dcx + M[5] * dcy) + M[7] * dcw;
+            o[2] = (M[8] * dcx + M[9] * dcy) + M[11] * dcw;
+            o[3] = gc.x * m.lam[k];
+            o[4] = gc.y * m.lam[k];
+            o[5] = gc.z * m.lam[k];
+            o[6] = gc.w * m.lam[k];
+            o[7] = du * m.lam[k];
+            o[8] = dv * m.lam[k];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+        {
+            tv[4 * j + 0] = gt.x * m.w[j];
+            tv[4 * j + 1] = gt.y * m.w[j];
+            tv[4 * j + 2] = gt.z * m.w[j];
+            tv[4 * j + 3] = gt.w * m.w[j];
+        }
+    }
+
+    if (run_reduce(triKey, vv) && triKey != kEmpty)
+    {
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            const float* o = vv + k * kVertFloats;
             const int s = stage_slot(vKey, kVertSlots - 1, m.vid[k]);
             if (s >= 0)
             {
 #pragma unroll
-                for (int c = 0; c < kVertFloats; ++c) atomicAdd(&vVal[s * kVertFloats + c], vals[c]);
+                for (int c = 0; c < kVertFloats; ++c) atomicAdd(&vVal[s * kVertFloats + c], o[c]);
             }
             else
             {
                 float* dst = a.dVertices + (a.b0Offset + a.b0Stride * (int64_t)m.vid[k]) / 4;
 #pragma unroll
-                for (int c = 0; c < kVertFloats; ++c) atomicAdd(dst + c, vals[c]);
+                for (int c = 0; c < kVertFloats; ++c) atomicAdd(dst + c, o[c]);
             }
         }
+    }
 
+    if (run_reduce(cellKey, tv) && cellKey != kEmpty)
+    {
         const uint32_t numTexels = a.texW * a.texH;
 #pragma unroll
         for (int j = 0; j < 4; ++j)
         {
             if (m.ti[j] >= numTexels) continue;   /* zero padding: a constant */
-            const float4 v = f4_scale(gt, m.w[j]);
+            const float4 v = make_float4(tv[4 * j], tv[4 * j + 1], tv[4 * j + 2], tv[4 * j + 3]);
             const int s = stage_slot(tKey, kTexSlots - 1, m.ti[j]);
             if (s >= 0)
             {

@@ -797,13 +797,10 @@ struct Chain
     int x, xEnd;
 };
 
-__device__ __forceinline__ bool chain_begin(const float4* R, float yf, int myX0, int xLimit, Chain& ch)
+/* The chain of the column class of myX0 (pixels myX0 + 4k below xLimit) on
+ * a scan-line whose span sp is known to be non-empty. */
+__device__ __forceinline__ bool chain_begin_span(const float4* R, float yf, const Span sp, int myX0, int xLimit, Chain& ch)
 {
-    const Span sp = scanline_span(R[0], R[1], yf);
-    if (!((uint32_t)sp.xMin < (uint32_t)sp.xMax))
-    {
-        return false;
-    }
     const int xEnd = min(sp.xMax, xLimit);
     const int xs = sp.xMin + ((myX0 - sp.xMin) & 3);
     const int xFirst = max(xs, myX0);
@@ -831,6 +828,16 @@ __device__ __forceinline__ bool chain_begin(const float4* R, float yf, int myX0,
     ch.x = xFirst;
     ch.xEnd = xEnd;
     return true;
+}
+
+__device__ __forceinline__ bool chain_begin(const float4* R, float yf, int myX0, int xLimit, Chain& ch)
+{
+    const Span sp = scanline_span(R[0], R[1], yf);
+    if (!((uint32_t)sp.xMin < (uint32_t)sp.xMax))
+    {
+        return false;
+    }
+    return chain_begin_span(R, yf, sp, myX0, xLimit, ch);
 }
 
 __device__ __forceinline__ void chain_step(Chain& ch)
@@ -893,8 +900,6 @@ struct RasterLayout
     static constexpr size_t kRecBytes = sizeof(float4) * kBatch * kRecordVec4;
     /* ordered path: colour + depth tile, records, record ids, then keys */
     static constexpr size_t ordered_bytes() { return sizeof(typename Color::stored) * kPix + sizeof(float) * kPix + kRecBytes + 2 * sizeof(uint32_t) * kBatch; }
-    /* order-free path: records + keys, then d0, z, key, b0, b1, b2 per pixel */
-    static constexpr size_t free_bytes() { return kRecBytes + sizeof(uint32_t) * kBatch + 6 * sizeof(float) * kPix; }
 };
 
 /* Stages records [b0, b0+cnt) of the tile list into shared memory. */
@@ -1081,44 +1086,131 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
  *   depth mask on,  EQUAL         : latest key with z == d0
  *   any mask,       OFF           : latest key
  *   depth mask off, LT/LE/GT/GE/EQ: latest key passing against d0
- * (every built-in program writes colour unconditionally). Each thread keeps
- * the winning (z, key, barycentrics) of the pixels it owns while the records
- * stream by in any order, and shades each pixel once at the end.
+ * (every built-in program writes colour unconditionally), so fragments may
+ * be visited in any order and each pixel shaded once at the end.
+ *
+ * Task-parallel. A task is one scan-line of one staged
+ * record inside the tile; a block-wide prefix sum over the records' row
+ * counts deals the tasks to the threads densely, so triangles a few pixels
+ * tall do not leave lanes idle. Each task walks its span with the four
+ * column chains of the reference's 4-wide scan-line loop (chain_begin_span),
+ * so every fragment's barycentrics and depth are the reference's bit for bit.
+ *
+ * Pass 1 folds each fragment that passes the depth test against the
+ * pre-launch depth into the pixel's best word with a shared 64-bit
+ * atomicMin; the word packs (depth order, key) so that its minimum is the
+ * fragment the table above keeps. Pass 2 walks
+ * the batch again and the pixel's winning fragment, unique by its key,
+ * stores its barycentrics and depth; the resolve shades each pixel once.
 -----------------------------------------------------------------------------*/
-__device__ __forceinline__ bool free_wins(int func, bool mask, float z, uint32_t key, float d0, float bz, uint32_t bkey)
+constexpr int kFreeThreads = 128;
+constexpr int kFreeBatch = 128;   /* records staged per step */
+
+template <int TW, int TH>
+struct FreeLayout
 {
-    const bool none = (bkey == 0xFFFFFFFFu);
-    if (func == SLG_DEPTH_TEST_OFF)
+    static constexpr int kPix = TW * TH;
+    static constexpr size_t kRecOff = 0;                                                   /* float4 [batch][8] */
+    static constexpr size_t kBOff = kRecOff + sizeof(float4) * kFreeBatch * kRecordVec4;    /* float4 (b0, b1, b2, z) per pixel */
+    static constexpr size_t kBestOff = kBOff + sizeof(float4) * kPix;                      /* u64 per pixel */
+    static constexpr size_t kD0Off = kBestOff + sizeof(unsigned long long) * kPix;         /* pre-launch depth per pixel */
+    static constexpr size_t kKeyOff = kD0Off + sizeof(float) * kPix;                       /* u32 per staged record */
+    static constexpr size_t kPreOff = kKeyOff + sizeof(uint32_t) * kFreeBatch;             /* u32 [batch + 1] row prefix */
+    static constexpr size_t kWarpOff = kPreOff + sizeof(uint32_t) * (kFreeBatch + 4);      /* u32 per warp */
+    static constexpr size_t bytes() { return kWarpOff + sizeof(uint32_t) * (kFreeThreads / 32); }
+};
+
+/* Total order of depths as unsigned words (-0 and +0 equal, as they compare). */
+__device__ __forceinline__ uint32_t depth_order(float z)
+{
+    const uint32_t u = __float_as_uint(z + 0.f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+/* Whether the depth rule prefers the larger key among equal depths (or
+ * whenever depth does not decide). */
+__device__ __forceinline__ bool free_key_max(int func, bool mask)
+{
+    return !mask || !(func == SLG_DEPTH_TEST_LESS_THAN || func == SLG_DEPTH_TEST_GREATER_THAN);
+}
+
+__device__ __forceinline__ unsigned long long free_pack(int func, bool mask, float z, uint32_t key)
+{
+    uint32_t zp = 0u;
+    if (mask && (func == SLG_DEPTH_TEST_LESS_THAN || func == SLG_DEPTH_TEST_LESS_EQUAL)) zp = depth_order(z);
+    if (mask && (func == SLG_DEPTH_TEST_GREATER_THAN || func == SLG_DEPTH_TEST_GREATER_EQUAL)) zp = ~depth_order(z);
+    return ((unsigned long long)zp << 32) | (free_key_max(func, mask) ? ~key : key);
+}
+
+/* Walks the scan-line tasks of the staged batch. kStore false: fold every
+ * passing fragment into sBest; true: the fragment equal to its pixel's
+ * sBest stores (b0, b1, b2, z). */
+template <int TW, int TH, bool kStore>
+__device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sKey, const uint32_t* sPre, int cnt, int x0, int y0,
+                                          int xLimit, int func, bool mask, const float* sD0, unsigned long long* sBest, float4* sB)
+{
+    const uint32_t total = sPre[cnt];
+    for (uint32_t i = threadIdx.x; i < total; i += kFreeThreads)
     {
-        return none || key > bkey;
-    }
-    if (!mask)
-    {
-        return depth_cmp(func, z, d0) && (none || key > bkey);
-    }
-    switch (func)
-    {
-        case SLG_DEPTH_TEST_LESS_THAN:     return none ? (z < d0) : (z < bz || (z == bz && key < bkey));
-        case SLG_DEPTH_TEST_LESS_EQUAL:    return none ? (z <= d0) : (z < bz || (z == bz && key > bkey));
-        case SLG_DEPTH_TEST_GREATER_THAN:  return none ? (z > d0) : (z > bz || (z == bz && key < bkey));
-        case SLG_DEPTH_TEST_GREATER_EQUAL: return none ? (z >= d0) : (z > bz || (z == bz && key > bkey));
-        default:                           return (z == d0) && (none || key > bkey);
+        int lo = 0, hi = cnt;
+        while (hi - lo > 1)
+        {
+            const int mid = (lo + hi) >> 1;
+            if (sPre[mid] <= i) lo = mid;
+            else hi = mid;
+        }
+        const float4* R = sRec + lo * kRecordVec4;
+        const int y = max(__float_as_int(R[6].x), y0) + (int)(i - sPre[lo]);
+        const float yf = (float)y;
+        const Span sp = scanline_span(R[0], R[1], yf);
+        if (!((uint32_t)sp.xMin < (uint32_t)sp.xMax))
+        {
+            continue;
+        }
+        const uint32_t key = sKey[lo];
+        const int rowBase = (y - y0) * TW - x0;
+#pragma unroll 1
+        for (int l = 0; l < 4; ++l)
+        {
+            Chain ch;
+            if (!chain_begin_span(R, yf, sp, x0 + l, xLimit, ch))
+            {
+                continue;
+            }
+            for (; ch.x < ch.xEnd; chain_step(ch))
+            {
+                const float z = chain_depth(R, ch);
+                const int idx = rowBase + ch.x;
+                if (!depth_cmp(func, z, sD0[idx]))
+                {
+                    continue;
+                }
+                const unsigned long long p = free_pack(func, mask, z, key);
+                if (kStore)
+                {
+                    if (sBest[idx] == p) sB[idx] = make_float4(ch.b0, ch.b1, ch.b2, z);
+                }
+                else
+                {
+                    atomicMin(sBest + idx, p);
+                }
+            }
+        }
     }
 }
 
 template <int TW, int TH, class Color>
-__global__ void __launch_bounds__(TH * 4) raster_free_kernel(const Frame f, int depthFunc, int depthMask)
+__global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Frame f, int depthFunc, int depthMask)
 {
-    typedef RasterLayout<TW, TH, Color> L;
+    typedef FreeLayout<TW, TH> L;
     extern __shared__ __align__(16) uint8_t smem[];
-    float4*   sRec  = reinterpret_cast<float4*>(smem);
-    uint32_t* sRecKey = reinterpret_cast<uint32_t*>(smem + L::kRecBytes);
-    float*    sD0   = reinterpret_cast<float*>(sRecKey + L::kBatch);
-    float*    sZ    = sD0 + L::kPix;
-    uint32_t* sBest = reinterpret_cast<uint32_t*>(sZ + L::kPix);
-    float*    sB0   = reinterpret_cast<float*>(sBest + L::kPix);
-    float*    sB1   = sB0 + L::kPix;
-    float*    sB2   = sB1 + L::kPix;
+    float4* sRec = reinterpret_cast<float4*>(smem + L::kRecOff);
+    float4* sB = reinterpret_cast<float4*>(smem + L::kBOff);
+    unsigned long long* sBest = reinterpret_cast<unsigned long long*>(smem + L::kBestOff);
+    float* sD0 = reinterpret_cast<float*>(smem + L::kD0Off);
+    uint32_t* sKey = reinterpret_cast<uint32_t*>(smem + L::kKeyOff);
+    uint32_t* sPre = reinterpret_cast<uint32_t*>(smem + L::kPreOff);
+    uint32_t* sWarp = reinterpret_cast<uint32_t*>(smem + L::kWarpOff);
 
     const int tile = blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
@@ -1129,91 +1221,81 @@ __global__ void __launch_bounds__(TH * 4) raster_free_kernel(const Frame f, int 
     }
     const int tx = tile % f.tilesX, ty = tile / f.tilesX;
     const int x0 = tx * TW, y0 = ty * TH;
-    const int r = threadIdx.x >> 2;
-    const int c = threadIdx.x & 3;
-    const int y = y0 + r;
-    const int myX0 = x0 + c;
     const int xLimit = min(x0 + TW, f.width);
-    const bool rowActive = (y < f.height);
-    const float yf = (float)y;
-    const int bandY0 = y0 + ((threadIdx.x >> 5) << 3);
+    const int yLimit = min(y0 + TH, f.height);
     const bool mask = depthMask != 0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-    /* each thread initialises the pixels it owns */
-    if (rowActive)
+    for (int i = threadIdx.x; i < L::kPix; i += kFreeThreads)
     {
-        for (int x = myX0; x < xLimit; x += 4)
+        const int x = x0 + i % TW, y = y0 + i / TW;
+        sBest[i] = ~0ull;
+        sD0[i] = (x < xLimit && y < yLimit) ? f.depth[(size_t)x + (size_t)f.width * y] : 0.f;
+    }
+
+    for (uint32_t b0 = 0; b0 < n; b0 += kFreeBatch)
+    {
+        const int cnt = (int)min((uint32_t)kFreeBatch, n - b0);
+        __syncthreads();
+        stage_records<kFreeBatch>(f, f.entries + begin + b0, cnt, sRec, sKey);
+        __syncthreads();
+
+        /* rows of each staged record inside the tile, prefix-summed */
+        uint32_t rows = 0;
+        if ((int)threadIdx.x < cnt)
         {
-            const int idx = r * L::kStride + (x - x0);
-            sD0[idx] = f.depth[(size_t)x + (size_t)f.width * y];
-            sBest[idx] = 0xFFFFFFFFu;
+            const float4 r6 = sRec[threadIdx.x * kRecordVec4 + 6];
+            const int ry0 = max(__float_as_int(r6.x), y0);
+            const int ry1 = min(__float_as_int(r6.y), yLimit);
+            rows = (ry1 > ry0) ? (uint32_t)(ry1 - ry0) : 0u;
         }
-    }
-
-    for (uint32_t b0 = 0; b0 < n; b0 += L::kBatch)
-    {
-        const int cnt = (int)min((uint32_t)L::kBatch, n - b0);
+        uint32_t incl = rows;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1)
+        {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+            if (lane >= off) incl += t;
+        }
+        if (lane == 31) sWarp[warp] = incl;
         __syncthreads();
-        stage_records<L::kBatch>(f, f.entries + begin + b0, cnt, sRec, sRecKey);
+        for (int w = 0; w < warp; ++w) incl += sWarp[w];
+        sPre[threadIdx.x + 1] = incl;
+        if (threadIdx.x == 0) sPre[0] = 0u;
         __syncthreads();
 
-        for_band_records(sRec, cnt, bandY0, [&](int ri) {
-            const float4* R = sRec + ri * kRecordVec4;
-            const float4 r6 = R[6];
-            if (!rowActive || y < __float_as_int(r6.x) || y >= __float_as_int(r6.y))
-            {
-                return;
-            }
-            Chain ch;
-            if (!chain_begin(R, yf, myX0, xLimit, ch))
-            {
-                return;
-            }
-            const uint32_t key = sRecKey[ri];
-            for (; ch.x < ch.xEnd; chain_step(ch))
-            {
-                const float z = chain_depth(R, ch);
-                const int idx = r * L::kStride + (ch.x - x0);
-                if (free_wins(depthFunc, mask, z, key, sD0[idx], sZ[idx], sBest[idx]))
-                {
-                    sZ[idx] = z;
-                    sBest[idx] = key;
-                    sB0[idx] = ch.b0;
-                    sB1[idx] = ch.b1;
-                    sB2[idx] = ch.b2;
-                }
-            }
-        });
+        free_walk<TW, TH, false>(sRec, sKey, sPre, cnt, x0, y0, xLimit, depthFunc, mask, sD0, sBest, sB);
+        __syncthreads();
+        free_walk<TW, TH, true>(sRec, sKey, sPre, cnt, x0, y0, xLimit, depthFunc, mask, sD0, sBest, sB);
     }
+    __syncthreads();
 
-    /* resolve: shade each owned pixel's winner once */
-    if (!rowActive)
+    /* resolve: shade each pixel's winner once */
+    const bool keyMax = free_key_max(depthFunc, mask);
+    for (int i = threadIdx.x; i < L::kPix; i += kFreeThreads)
     {
-        return;
-    }
-    for (int x = myX0; x < xLimit; x += 4)
-    {
-        const int idx = r * L::kStride + (x - x0);
-        const uint32_t key = sBest[idx];
-        if (key == 0xFFFFFFFFu)
+        const unsigned long long p = sBest[i];
+        if (p == ~0ull)
         {
             continue;
         }
+        const int x = x0 + i % TW, y = y0 + i / TW;
+        const uint32_t key = keyMax ? ~(uint32_t)p : (uint32_t)p;
         const size_t gi = (size_t)x + (size_t)f.width * y;
         const uint64_t rec = key_to_record(f, key);
         const float4* R = f.records + rec * kRecordVec4;
         const DrawDesc& dd = f.draws[__float_as_uint(R[7].x)];
+        const float4 b = sB[i];
         if (f.color && dd.numOutputs > 0)
         {
             float4 o;
-            if (shade(f, dd, rec, R[2].w, R[5], sB0[idx], sB1[idx], sB2[idx], o))
+            if (shade(f, dd, rec, R[2].w, R[5], b.x, b.y, b.z, o))
             {
                 Color::write(f.color, gi, Color::store(o));
             }
         }
         if (mask)
         {
-            f.depth[gi] = sZ[idx];
+            f.depth[gi] = b.w;
         }
         if (f.ids)
         {
@@ -1244,7 +1326,7 @@ static cudaError_t launch_raster_t(const Frame& f, int numTiles, int keyCap, cud
     typedef RasterLayout<TW, TH, Color> L;
     if (f.orderFree)
     {
-        raster_free_kernel<TW, TH, Color><<<numTiles, L::kThreads, L::free_bytes(), s>>>(f, f.freeDepthFunc, f.freeDepthMask);
+        raster_free_kernel<TW, TH, Color><<<numTiles, kFreeThreads, FreeLayout<TW, TH>::bytes(), s>>>(f, f.freeDepthFunc, f.freeDepthMask);
     }
     else
     {
@@ -1259,7 +1341,7 @@ template <int TW, int TH, class Color>
 static cudaError_t attributes_t()
 {
     typedef RasterLayout<TW, TH, Color> L;
-    cudaError_t e = cudaFuncSetAttribute(raster_free_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::free_bytes());
+    cudaError_t e = cudaFuncSetAttribute(raster_free_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FreeLayout<TW, TH>::bytes());
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(raster_ordered_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::ordered_bytes());
     return e;
