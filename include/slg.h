@@ -316,9 +316,11 @@ int slg_fbo_read_visibility(slg_context* ctx, size_t fboId, uint32_t* dst, size_
  * visibility map: width*height RGBA floats into `image` (device, 16-byte
  * aligned). The model covers a pixel when its visible triangle's
  * barycentrics there are all >= -1 (within one triangle height of the
- * unsnapped triangle; snapping lets slivers cover pixels far outside it);
- * every other pixel takes the framebuffer's colour when colour attachment 0
- * is RGBA float, else 0, and carries no gradient. */
+ * unsnapped triangle; snapping lets slivers cover pixels far outside it)
+ * and the triangle is not a sliver (twice its area in clip-space xy/w at
+ * the pixel >= 0.02 x the sum of its squared edge lengths there); every
+ * other pixel takes the framebuffer's colour when colour attachment 0 is
+ * RGBA float, else 0, and carries no gradient. */
 int slg_diff_shade(slg_context* ctx, const slg_mesh* mesh, size_t shaderId, size_t fboId, float* image, size_t count);
 
 /* Adjoint of slg_diff_shade: for dL/d image (width*height RGBA floats),

@@ -27,10 +27,13 @@ coverage the exact rasteriser produced (the per-pixel visible triangle):
     (softlight/include/softlight/SL_Sampler.hpp:97-218);
   * output = colour * texel (componentwise);
   * domain: a visible pixel is modelled when every barycentric is >= -1
-    (within one triangle height of the unsnapped triangle); snapping lets
+    (within one triangle height of the unsnapped triangle; snapping lets
     slivers own pixels far outside their unsnapped shape, where the
-    extrapolation is ill-conditioned. Other pixels keep the framebuffer's
-    colour and carry no gradient.
+    extrapolation is ill-conditioned) and its triangle is not a sliver in the
+    h' frame: |sum e_k| >= 0.02 x the sum of its squared edge lengths
+    (barycentrics vary as 1/area, so near-degenerate and edge-on triangles
+    have unbounded sensitivity). Other pixels keep the framebuffer's colour
+    and carry no gradient.
 
 The adjoint takes dL/d(output) per pixel and returns dL/d positions (V x 3),
 colours (V x 4), uvs (V x 2) and texels (H x W x 4). Texel indices that fall
@@ -47,6 +50,7 @@ def clip_positions(pos, mvp):
 
 
 MIN_BARYCENTRIC = -1.0
+MIN_SHAPE = 0.02   # |2 x area| / (sum of squared edge lengths); 0.29 for an equilateral triangle
 
 
 def wrap_repeat(t):
@@ -90,8 +94,11 @@ class Model:
         e = a[:, :, 0] * b[:, :, 1] - a[:, :, 1] * b[:, :, 0]
         S = e.sum(1)
         if frozen is None:
+            # squared edge lengths of the triangle in the h' frame
+            e2 = sum(((np.roll(hp, -1, axis=1) - hp) ** 2).sum(2).T)
             with np.errstate(divide="ignore", invalid="ignore"):
-                ok = (S != 0.0) & ((e / np.where(S == 0.0, 1.0, S)[:, None]).min(1) >= MIN_BARYCENTRIC)
+                ok = ((S != 0.0) & ((e / np.where(S == 0.0, 1.0, S)[:, None]).min(1) >= MIN_BARYCENTRIC)
+                      & (np.abs(S) >= MIN_SHAPE * e2))
         else:
             ok = np.isin(pix, frozen.pix)
         self.pix, self.t, v, h, hp, a, b, e, S = pix[ok], t[ok], v[ok], h[ok], hp[ok], a[ok], b[ok], e[ok], S[ok]

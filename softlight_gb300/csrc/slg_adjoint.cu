@@ -23,11 +23,13 @@
  *              x + W y into the padded texel array)
  *   out      = colour * texel
  *
- * The model covers a visible pixel when min l_k >= -1. The exact rasteriser
- * snaps vertices to whole pixels, so a sliver can own pixels well outside
- * its unsnapped shape, where l_k reach tens and the extrapolation is
- * ill-conditioned; such pixels (about 0.5% of the 512x512 sphere's) keep the
- * framebuffer's colour and carry no gradient.
+ * The model covers a visible pixel when min l_k >= -1 and its triangle is
+ * not a sliver: |e_0 + e_1 + e_2| >= 0.02 x the sum of the squared edge
+ * lengths in the h' frame. The exact rasteriser snaps vertices to whole
+ * pixels, so a sliver can own pixels well outside its unsnapped shape, where
+ * l_k reach tens; and near-degenerate or edge-on triangles have barycentrics
+ * that vary as 1/area. Such pixels (about 0.6% of the 512x512 sphere's) keep
+ * the framebuffer's colour and carry no gradient.
  *
  * Nothing from the forward pass is stored but the visibility map (4 bytes a
  * pixel): the adjoint recomputes each pixel's barycentrics, varyings and
@@ -59,6 +61,7 @@ constexpr int kProbes = 16;       /* linear-probe bound; then the update goes st
 constexpr int kVertFloats = 9;    /* pos[3], rgba[4], uv[2] */
 constexpr uint32_t kEmpty = 0xFFFFFFFFu;
 constexpr float kMinBarycentric = -1.f;
+constexpr float kMinShape = 0.02f;   /* 0.29 for an equilateral triangle */
 
 struct PixelModel
 {
@@ -129,6 +132,16 @@ __device__ bool pixel_model(const DiffArgs& a, int x, int y, uint32_t id, PixelM
     }
     m.S = (e[0] + e[1]) + e[2];
     if (!(m.S != 0.f) || !isfinite(m.S)) return false;
+    /* slivers and edge-on triangles (barycentrics vary as 1/area) are
+     * outside the model: |2 x area| >= kMinShape x sum of squared edges */
+    float e2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        const float2 p = m.hp[(k + 1) % 3], q = m.hp[k];
+        e2 += (p.x - q.x) * (p.x - q.x) + (p.y - q.y) * (p.y - q.y);
+    }
+    if (fabsf(m.S) < kMinShape * e2) return false;
 #pragma unroll
     for (int k = 0; k < 3; ++k) m.lam[k] = e[k] / m.S;
     /* the model's domain: pixels within one triangle height of every edge of

@@ -503,7 +503,7 @@ def build_c4(ctx, num_draws=256, width=3840, height=2160, tex_size=512, batched=
     return s
 
 
-def displaced_sphere(lon=100, lat=50, seed=5, amplitude=0.12, waves=6):
+def displaced_sphere(lon=100, lat=50, seed=5, amplitude=0.1, waves=6):
     """UV sphere (lon*lat*2 triangles) with radius 1 + amplitude * noise(n),
     noise a seeded sum of sinusoids of the direction: positions (V x 3),
     uvs (V x 2), triangle indices."""
@@ -589,7 +589,7 @@ def build_c5(ctx, width=512, height=512, tex_size=256, lon=100, lat=50, seed=5, 
     return s
 
 
-def c5_perturbed(s, seed=6, col_sigma=0.05, tex_sigma=0.05, pos_sigma=0.01):
+def c5_perturbed(s, seed=6, col_sigma=0.05, tex_sigma=0.05, pos_sigma=0.05):
     """Seeded perturbation of a c5 scene's parameters (the target's)."""
     rng = np.random.default_rng(seed)
     pos = s.pos + rng.normal(0.0, pos_sigma, s.pos.shape).astype(np.float32)

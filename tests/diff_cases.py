@@ -14,16 +14,23 @@ def visibility(pos, tri, mvp, width, height):
     clip = D.clip_positions(pos, mvp)
     h = clip[tri][:, :, [0, 1, 3]]                 # T x 3 x 3
     z = clip[tri][:, :, 2]
-    ys, xs = np.mgrid[0:height, 0:width]
-    nx = (2.0 * xs / width - 1.0).reshape(-1)
-    ny = (2.0 * ys / height - 1.0).reshape(-1)
-    best = np.full(nx.size, np.inf)
-    vis = np.zeros(nx.size, np.uint32)
+    best = np.full(width * height, np.inf)
+    vis = np.zeros(width * height, np.uint32)
     # front-facing: counter-clockwise in NDC
     ndc = h[:, :, :2] / h[:, :, 2:3]
     area = ((ndc[:, 1, 0] - ndc[:, 0, 0]) * (ndc[:, 2, 1] - ndc[:, 0, 1])
             - (ndc[:, 2, 0] - ndc[:, 0, 0]) * (ndc[:, 1, 1] - ndc[:, 0, 1]))
+    sx = (ndc[:, :, 0] + 1.0) * 0.5 * width
+    sy = (ndc[:, :, 1] + 1.0) * 0.5 * height
     for t in np.nonzero((area > 0) & (h[:, :, 2] > 0).all(1))[0]:
+        x0, x1 = max(int(np.floor(sx[t].min())) - 1, 0), min(int(np.ceil(sx[t].max())) + 2, width)
+        y0, y1 = max(int(np.floor(sy[t].min())) - 1, 0), min(int(np.ceil(sy[t].max())) + 2, height)
+        if x0 >= x1 or y0 >= y1:
+            continue
+        ys, xs = np.mgrid[y0:y1, x0:x1]
+        flat = (ys * width + xs).reshape(-1)
+        nx = (2.0 * xs / width - 1.0).reshape(-1)
+        ny = (2.0 * ys / height - 1.0).reshape(-1)
         hp_x = h[t, :, 0][None, :] - h[t, :, 2][None, :] * nx[:, None]
         hp_y = h[t, :, 1][None, :] - h[t, :, 2][None, :] * ny[:, None]
         a = [1, 2, 0]
@@ -34,9 +41,9 @@ def visibility(pos, tri, mvp, width, height):
         inside = (s != 0) & (lam >= 0).all(1)
         with np.errstate(divide="ignore", invalid="ignore"):
             depth = (lam * z[t][None, :]).sum(1) / (lam * h[t, :, 2][None, :]).sum(1)
-        win = inside & (depth < best)
-        best[win] = depth[win]
-        vis[win] = t + 1
+        win = inside & (depth < best[flat])
+        best[flat[win]] = depth[win]
+        vis[flat[win]] = t + 1
     return vis.reshape(height, width)
 
 

@@ -8,11 +8,15 @@ Tolerances, all norm-wise relative errors:
   * gradients (positions, colours, uvs, texels), GPU FP32 adjoint vs FP64
     adjoint: 1e-4;
   * GPU gradients vs central differences (h = 1e-3) of the FP64 loss with
-    coverage, uv repeat offsets and texel cells frozen: colours and texels
-    1e-4 (the loss is quadratic in them, so the differences are exact);
-    positions 2e-2 (O(h^2) truncation of the non-linear barycentrics, largest
-    at the poles' sliver triangles), and 1e-4 for the Richardson combination
-    of h and h/2, which cancels the h^2 term."""
+    coverage, uv repeat offsets and texel cells frozen, on 64 sampled
+    parameters: colours and texels 1e-4 (the loss is quadratic in them, so
+    the differences are exact). Positions enter through barycentrics that
+    vary as 1/area, and triangles near the silhouette and the poles project
+    to a few pixels, where a 1e-3 step changes their screen area by tens of
+    percent: h = 1e-3 carries up to ~4% O(h^2) truncation error there, so
+    its bound is 0.1, the Richardson combination of h and h/2 is held to
+    1e-2, and FP64 central differences at h = 1e-5 (truncation ~1e-6,
+    rounding ~1e-10) to 1e-4."""
 import numpy as np
 import pytest
 
@@ -155,19 +159,22 @@ def test_autograd_harness_against_fp64_and_differences(c5):
     for name, w in (("pos", want[0]), ("col", want[1]), ("tex", want[3])):
         assert rel(grads[name], w) <= 1e-4, f"{name}: autograd vs FP64 adjoint {rel(grads[name], w):.3e}"
 
+    # 64 sampled parameters: 22 colour, 21 texel and 21 position components
     rng = np.random.default_rng(7)
-    for name, tol in (("col", 1e-4), ("tex", 1e-4), ("pos", 2e-2)):
+    for name, tol, count in (("col", 1e-4, 22), ("tex", 1e-4, 21), ("pos", 0.1, 21)):
         g = grads[name].reshape(-1)
         cand = np.nonzero(np.abs(g) > 1e-2 * np.abs(g).max())[0]
-        idx = rng.choice(cand, size=8, replace=False)
+        idx = rng.choice(cand, size=count, replace=False)
         num = np.array([fd(s, vis, tgt, base, name, i, 1e-3) for i in idx])
         err = rel(g[idx], num)
         assert err <= tol, f"{name}: GPU gradient vs central differences {err:.3e}"
         if name == "pos":
             num2 = np.array([fd(s, vis, tgt, base, name, i, 5e-4) for i in idx])
-            rich = (4.0 * num2 - num) / 3.0
-            err = rel(g[idx], rich)
-            assert err <= 1e-4, f"pos: GPU gradient vs Richardson differences {err:.3e}"
+            err = rel(g[idx], (4.0 * num2 - num) / 3.0)
+            assert err <= 1e-2, f"pos: GPU gradient vs Richardson differences {err:.3e}"
+            fine = np.array([fd(s, vis, tgt, base, name, i, 1e-5) for i in idx])
+            err = rel(g[idx], fine)
+            assert err <= 1e-4, f"pos: GPU gradient vs central differences at h=1e-5 {err:.3e}"
 
 
 @pytest.mark.parametrize("index_dtype", [np.uint8, np.uint16, np.uint32, None])
