@@ -430,14 +430,17 @@ __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, Ti
     const uint64_t i = d.elementBegin + 3u * tri;
     const DevEnv env = make_env(d, f.tables);
 
+    /* positions first; the varyings are produced again per vertex only for
+     * triangles that are stored (keeps three vertices' varyings out of the
+     * registers while culling and set-up run) */
     float4 clip[3];
-    slg_v4 vary[12];
     uint64_t vids[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
     {
+        slg_v4 unused[kMaxVaryings];
         vids[k] = (d.indexType >= 0) ? read_index(d, i + k) : (i + k);
-        clip[k] = to_f4(run_vertex_program(d.vsProgram, env, vids[k], inst, vary + 4 * k));
+        clip[k] = to_f4(run_vertex_program(d.vsProgram, env, vids[k], inst, unused));
     }
 
     if (d.cull != SLG_CULL_OFF)
@@ -468,8 +471,20 @@ __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, Ti
             Record rec;
             make_record(s0, s1, s2, (uint32_t)di, primIndex, (uint32_t)d.depthTest | ((uint32_t)d.depthMask << 4), rec);
             store_record(f, slot, rec);
-            store_varyings(f, slot, d.numVaryings, vary, vary + 4, vary + 8);
             tr = tile_range(rec.r[6], f);
+            float4* dst = f.varyings + slot * kVaryingVec4;
+            const int nv = d.numVaryings;
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+            {
+                slg_v4 vary[kMaxVaryings];
+                (void)run_vertex_program(d.vsProgram, env, vids[k], inst, vary);
+#pragma unroll
+                for (int vi = 0; vi < kMaxVaryings; ++vi)
+                {
+                    if (vi < nv) dst[4 * k + vi] = to_f4(vary[vi]);
+                }
+            }
             counted = true;
             return 1;
         }
