@@ -91,7 +91,7 @@ __device__ __forceinline__ uint32_t vertex_id(const DiffArgs& a, uint64_t e)
 
 __device__ __forceinline__ float wrap_unit(float t)
 {
-    return (t < 0.f ? 1.f : 0.f) + fmodf(t, 1.f);
+    return wrap_repeat(t);
 }
 
 __device__ __forceinline__ float4 f4_scale(float4 v, float s) { return make_float4(v.x * s, v.y * s, v.z * s, v.w * s); }
