@@ -185,6 +185,23 @@ int    slg_texture_set_texels(slg_context* ctx, size_t texId, const void* data, 
  * softlight/src/SL_Context.cpp:747-880): copies w*h*d texels. */
 int    slg_texture_read(slg_context* ctx, size_t texId, void* dst, size_t numBytes);
 
+/* SL_Context::blit(outTextureId, inTextureId) and its rectangle form
+ * (softlight/src/SL_Context.cpp:747-812; SL_BlitProcessor::blit_nearest,
+ * softlight/src/SL_BlitProcessor.cpp:621-660): nearest-neighbour scaled copy
+ * with a vertical flip and the reference's colour-format conversions between
+ * any two of the supported texture types. Rectangles whose reads would fall
+ * outside the source texture, or writes outside the destination, are
+ * rejected (the reference does not check them). */
+int slg_blit(slg_context* ctx, size_t outTextureId, size_t inTextureId);
+int slg_blit_rect(slg_context* ctx, size_t outTextureId, size_t inTextureId, uint16_t srcX0, uint16_t srcY0,
+                  uint16_t srcX1, uint16_t srcY1, uint16_t dstX0, uint16_t dstY0, uint16_t dstX1, uint16_t dstY1);
+/* SL_Context::blit(SL_TextureView& buffer, textureId) (softlight/src/SL_Context.cpp:816-880)
+ * into host memory: the whole texture scaled into a dstW x dstH buffer of
+ * dstColorType texels (a window's back buffer in the reference), read back
+ * at once. */
+int slg_blit_read(slg_context* ctx, size_t inTextureId, int dstColorType, uint16_t dstW, uint16_t dstH, void* dst,
+                  size_t numBytes);
+
 /* SL_Context::create_framebuffer + SL_Framebuffer::reserve_color_buffers /
  * attach_color_buffer / attach_depth_buffer (softlight/src/SL_Context.cpp:284;
  * softlight/src/SL_Framebuffer.cpp:823,855,908) */

@@ -143,6 +143,19 @@ class Context
     void draw_instanced(const slg_mesh& m, size_t n, size_t shaderId, size_t fboId) noexcept { note(slg_draw_instanced(mCtx, &m, n, shaderId, fboId)); }
     void draw_batch(const slg_draw_cmd* cmds, size_t n, size_t fboId) noexcept { note(slg_draw_batch(mCtx, cmds, n, fboId)); }
 
+    /* SL_Context::blit (softlight/src/SL_Context.cpp:747-880); the window
+     * buffer form becomes a read into host memory of the given format */
+    void blit(size_t outTextureId, size_t inTextureId) noexcept { note(slg_blit(mCtx, outTextureId, inTextureId)); }
+    void blit(size_t outTextureId, size_t inTextureId, uint16_t srcX0, uint16_t srcY0, uint16_t srcX1, uint16_t srcY1,
+              uint16_t dstX0, uint16_t dstY0, uint16_t dstX1, uint16_t dstY1) noexcept
+    {
+        note(slg_blit_rect(mCtx, outTextureId, inTextureId, srcX0, srcY0, srcX1, srcY1, dstX0, dstY0, dstX1, dstY1));
+    }
+    int blit_read(size_t textureId, int colorType, uint16_t w, uint16_t h, void* dst, size_t numBytes) noexcept
+    {
+        return slg_blit_read(mCtx, textureId, colorType, w, h, dst, numBytes);
+    }
+
     void clear_color_buffer(size_t fboId, unsigned attachment, const double rgba[4]) noexcept { note(slg_clear_color_buffer(mCtx, fboId, attachment, rgba)); }
     void clear_depth_buffer(size_t fboId, double depth) noexcept { note(slg_clear_depth_buffer(mCtx, fboId, depth)); }
     void clear_framebuffer(size_t fboId, unsigned attachment, const double rgba[4], double depth) noexcept

@@ -242,6 +242,25 @@ int slr_texture_read(slr_context* c, size_t id, void* dst, size_t n)
     std::memcpy(dst, t.data(), n);
     return SLG_OK;
 }
+int slr_blit(slr_context* c, size_t out, size_t in)
+{
+    c->ctx.blit(out, in);
+    return SLG_OK;
+}
+int slr_blit_rect(slr_context* c, size_t out, size_t in, uint16_t sx0, uint16_t sy0, uint16_t sx1, uint16_t sy1,
+                  uint16_t dx0, uint16_t dy0, uint16_t dx1, uint16_t dy1)
+{
+    c->ctx.blit(out, in, sx0, sy0, sx1, sy1, dx0, dy0, dx1, dy1);
+    return SLG_OK;
+}
+int slr_blit_read(slr_context* c, size_t in, int type, uint16_t w, uint16_t h, void* dst, size_t n)
+{
+    (void)n;
+    SL_TextureView view;
+    sl_texture_view_from_buffer(view, w, h, 1, (SL_ColorDataType)type, dst);
+    c->ctx.blit(view, in);
+    return SLG_OK;
+}
 size_t slr_create_framebuffer(slr_context* c) { return c->ctx.create_framebuffer(); }
 int slr_fbo_reserve_color_buffers(slr_context* c, size_t fbo, unsigned n)
 {

@@ -1029,6 +1029,106 @@ int slo_texture_read(slo_context* ctx, size_t id, void* dst, size_t numBytes)
     return SLG_OK;
 }
 
+/* SL_BlitProcessor::blit_nearest (softlight/src/SL_BlitProcessor.cpp:621-660) over a
+ * destination of dstType texels, dstW x dstH, with the blit operators of
+ * :20-420 (color_cast, softlight/include/softlight/SL_Color.hpp:600-690).
+ * Index arithmetic is 64-bit unsigned (uint_fast32_t on LP64). */
+static int blit_into(slo_context* ctx, const Texture& src, int dstType, uint64_t dstW, uint64_t dstH, uint8_t* out,
+                     uint16_t srcX0, uint16_t srcY0, uint16_t srcX1, uint16_t srcY1, uint16_t dstX0, uint16_t dstY0,
+                     uint16_t dstX1, uint16_t dstY1)
+{
+    if (srcX1 <= srcX0 || srcY1 <= srcY0 || dstX1 <= dstX0 || dstY1 <= dstY0)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "empty or inverted blit rectangle");
+    if (dstY1 > dstH) return ctx->fail(SLG_ERR_INVALID_ARG, "blit rectangle extends below the destination");
+    const uint64_t inW = (uint64_t)srcX1 - srcX0, inH = (uint64_t)srcY1 - srcY0, outW = (uint64_t)dstX1 - dstX0;
+    const uint64_t x0 = dstX0, x1 = std::min<uint64_t>(dstW, x0 + outW);
+    const uint64_t y0 = dstY0, y1 = dstY1;
+    const uint64_t foutW = ((inW << 16) / dstW) + 1u;
+    const uint64_t foutH = ((inH << 16) / dstH) + 1u;
+    if (x1 <= x0) return SLG_OK;
+    if (((x1 - 1u) * foutW >> 16) >= src.w || srcY0 + (((y1 - 1u) * foutH) >> 16) + 1u > srcY1 ||
+        srcY1 - (srcY0 + ((y0 * foutH) >> 16)) - 1u >= src.h)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "blit rectangle reads outside the source texture");
+    for (uint64_t y = y0; y < y1; ++y)
+    {
+        const uint64_t yf = (y * foutH) >> 16;
+        const uint64_t srcY = srcY1 - (srcY0 + yf) - 1u;
+        for (uint64_t x = x0; x < x1; ++x)
+        {
+            const uint64_t srcX = (x * foutW) >> 16;
+            const uint64_t si = srcX + (uint64_t)src.w * srcY;
+            const uint64_t di = x + dstW * y;
+            float c[4];
+            if (src.type == SLG_COLOR_RGBA_8U)
+            {
+                const uint8_t* q = &src.bytes[si * 4];
+                for (int k = 0; k < 4; ++k) c[k] = (float)q[k] * 0.00392156862745f;
+                if (dstType == SLG_COLOR_RGBA_8U) { std::memcpy(out + di * 4, q, 4); continue; }
+            }
+            else if (src.type == SLG_COLOR_RGBA_FLOAT)
+            {
+                std::memcpy(c, &src.bytes[si * 16], 16);
+            }
+            else
+            {
+                /* SL_Blit_R_to_*: (min, min, r, max) of the source type */
+                float r;
+                std::memcpy(&r, &src.bytes[si * 4], 4);
+                if (dstType == SLG_COLOR_R_FLOAT) { std::memcpy(out + di * 4, &r, 4); continue; }
+                c[0] = 0.f; c[1] = 0.f; c[2] = r; c[3] = 1.f;
+            }
+            if (dstType == SLG_COLOR_RGBA_8U)
+            {
+                uint8_t q[4];
+                for (int k = 0; k < 4; ++k) q[k] = f2u8(c[k] * 255.f);
+                std::memcpy(out + di * 4, q, 4);
+            }
+            else if (dstType == SLG_COLOR_RGBA_FLOAT)
+            {
+                std::memcpy(out + di * 16, c, 16);
+            }
+            else
+            {
+                std::memcpy(out + di * 4, &c[0], 4);
+            }
+        }
+    }
+    return SLG_OK;
+}
+
+static bool blit_type_ok(int t) { return t == SLG_COLOR_RGBA_8U || t == SLG_COLOR_RGBA_FLOAT || t == SLG_COLOR_R_FLOAT; }
+
+int slo_blit_rect(slo_context* ctx, size_t outId, size_t inId, uint16_t srcX0, uint16_t srcY0, uint16_t srcX1,
+                  uint16_t srcY1, uint16_t dstX0, uint16_t dstY0, uint16_t dstX1, uint16_t dstY1)
+{
+    if (outId >= ctx->textures.size() || inId >= ctx->textures.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
+    const Texture& src = *ctx->textures[inId];
+    Texture& dst = *ctx->textures[outId];
+    if (src.bytes.empty() || dst.bytes.empty() || !blit_type_ok(src.type) || !blit_type_ok(dst.type))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "blit needs initialised R float, RGBA8 or RGBA float textures");
+    if (outId == inId) return ctx->fail(SLG_ERR_INVALID_ARG, "blit source and destination are the same texture");
+    return blit_into(ctx, src, dst.type, dst.w, dst.h, dst.bytes.data(), srcX0, srcY0, srcX1, srcY1, dstX0, dstY0, dstX1, dstY1);
+}
+
+int slo_blit(slo_context* ctx, size_t outId, size_t inId)
+{
+    if (outId >= ctx->textures.size() || inId >= ctx->textures.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
+    const Texture& src = *ctx->textures[inId];
+    const Texture& dst = *ctx->textures[outId];
+    return slo_blit_rect(ctx, outId, inId, 0, 0, src.w, src.h, 0, 0, dst.w, dst.h);
+}
+
+int slo_blit_read(slo_context* ctx, size_t inId, int dstType, uint16_t dstW, uint16_t dstH, void* dst, size_t numBytes)
+{
+    if (inId >= ctx->textures.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
+    const Texture& src = *ctx->textures[inId];
+    if (src.bytes.empty() || !blit_type_ok(src.type) || !blit_type_ok(dstType))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "blit needs R float, RGBA8 or RGBA float formats");
+    const size_t bytes = (size_t)dstW * dstH * (dstType == SLG_COLOR_RGBA_FLOAT ? 16u : 4u);
+    if (!dst || numBytes != bytes || bytes == 0) return ctx->fail(SLG_ERR_INVALID_ARG, "destination byte count");
+    return blit_into(ctx, src, dstType, dstW, dstH, static_cast<uint8_t*>(dst), 0, 0, src.w, src.h, 0, 0, dstW, dstH);
+}
+
 size_t slo_create_framebuffer(slo_context* ctx) { ctx->fbos.emplace_back(); return ctx->fbos.size() - 1; }
 
 int slo_fbo_reserve_color_buffers(slo_context* ctx, size_t fbo, unsigned n)

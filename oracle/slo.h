@@ -37,6 +37,11 @@ size_t slo_create_texture(slo_context* ctx);
 int    slo_texture_init(slo_context* ctx, size_t texId, int colorType, uint16_t w, uint16_t h, uint16_t d);
 int    slo_texture_set_texels(slo_context* ctx, size_t texId, const void* data, size_t numBytes);
 int    slo_texture_read(slo_context* ctx, size_t texId, void* dst, size_t numBytes);
+int    slo_blit(slo_context* ctx, size_t outTextureId, size_t inTextureId);
+int    slo_blit_rect(slo_context* ctx, size_t outTextureId, size_t inTextureId, uint16_t srcX0, uint16_t srcY0,
+                     uint16_t srcX1, uint16_t srcY1, uint16_t dstX0, uint16_t dstY0, uint16_t dstX1, uint16_t dstY1);
+int    slo_blit_read(slo_context* ctx, size_t inTextureId, int dstColorType, uint16_t dstW, uint16_t dstH, void* dst,
+                     size_t numBytes);
 size_t slo_create_framebuffer(slo_context* ctx);
 int    slo_fbo_reserve_color_buffers(slo_context* ctx, size_t fboId, unsigned numColorBuffers);
 int    slo_fbo_attach_color_buffer(slo_context* ctx, size_t fboId, unsigned index, size_t texId);

@@ -89,6 +89,9 @@ _SIGNATURES = [
     ("draw_instanced", C.c_int, [C.c_void_p, C.POINTER(Mesh), C.c_size_t, C.c_size_t, C.c_size_t]),
     ("draw_multiple", C.c_int, [C.c_void_p, C.POINTER(Mesh), C.c_size_t, C.c_size_t, C.c_size_t]),
     ("draw_batch", C.c_int, [C.c_void_p, C.POINTER(DrawCmd), C.c_size_t, C.c_size_t]),
+    ("blit", C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t]),
+    ("blit_rect", C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t] + [C.c_uint16] * 8),
+    ("blit_read", C.c_int, [C.c_void_p, C.c_size_t, C.c_int, C.c_uint16, C.c_uint16, C.c_void_p, C.c_size_t]),
     ("finish", C.c_int, [C.c_void_p]),
 ]
 
@@ -311,6 +314,21 @@ class SLContext:
                      d_texels_ptr, d_texel_count):
         self._call("draw_adjoint", C.byref(mesh), shader, fbo, C.c_void_p(d_image_ptr), d_image_count,
                    C.c_void_p(d_vertices_ptr), d_vertex_count, C.c_void_p(d_texels_ptr), d_texel_count)
+
+    def blit(self, out_tex, in_tex):
+        self._call("blit", out_tex, in_tex)
+
+    def blit_rect(self, out_tex, in_tex, src, dst):
+        """src = (x0, y0, x1, y1) in the input texture, dst likewise in the output."""
+        self._call("blit_rect", out_tex, in_tex, *src, *dst)
+
+    def blit_read(self, in_tex, color_type, width, height):
+        """The texture scaled into a width x height host image of color_type."""
+        shape = (height, width) if color_type == COLOR_R_FLOAT else (height, width, 4)
+        dtype = np.uint8 if color_type == COLOR_RGBA_8U else np.float32
+        out = np.empty(shape, dtype)
+        self._call("blit_read", in_tex, color_type, width, height, out.ctypes.data_as(C.c_void_p), out.nbytes)
+        return out
 
     def finish(self):
         self._call("finish")

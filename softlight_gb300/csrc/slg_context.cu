@@ -125,6 +125,7 @@ struct slg_context
     /* scratch */
     DevBuffer records, varyings, slotInfo, slotOvf, ovfCount, clipQueue, clipCount;
     DevBuffer tileCount, tileOffset, tileCursor, entries, status;
+    DevBuffer blitBuf;      /* destination of slg_blit_read */
     uint64_t slotCap = 0, ovfCap = 0, tileCap = 0, entryCap = 0;
 
     /* draw descriptors: pinned host ring mirrored to a device ring */
@@ -709,7 +710,7 @@ void slg_context_destroy(slg_context* ctx)
     for (Fbo& f : ctx->fbos) dev_free(f.vis);
     DevBuffer* scratch[] = {&ctx->texTable, &ctx->bufTable, &ctx->records, &ctx->varyings, &ctx->slotInfo, &ctx->slotOvf,
                             &ctx->ovfCount, &ctx->clipQueue, &ctx->clipCount, &ctx->tileCount, &ctx->tileOffset,
-                            &ctx->tileCursor, &ctx->entries,
+                            &ctx->tileCursor, &ctx->entries, &ctx->blitBuf,
                             &ctx->status, &ctx->devDescs, &ctx->devStarts};
     for (DevBuffer* b : scratch) dev_free(*b);
     if (ctx->graph.exec) cudaGraphExecDestroy(ctx->graph.exec);
@@ -860,6 +861,101 @@ int slg_texture_read(slg_context* ctx, size_t id, void* dst, size_t numBytes)
     cudaError_t e = cudaMemcpyAsync(dst, t.buf.ptr, numBytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "texture read");
+    return check_status(ctx);
+}
+
+} // extern "C"
+
+namespace
+{
+
+/* Geometry of SL_BlitProcessor::blit_nearest (softlight/src/SL_BlitProcessor.cpp:621-660)
+ * for a source texture and a dstW x dstH destination, in the reference's
+ * 64-bit unsigned arithmetic; rejects rectangles whose reads or writes the
+ * reference would make out of bounds. */
+int blit_geometry(slg_context* ctx, const Texture& src, uint64_t dstW, uint64_t dstH, uint16_t srcX0, uint16_t srcY0,
+                  uint16_t srcX1, uint16_t srcY1, uint16_t dstX0, uint16_t dstY0, uint16_t dstX1, uint16_t dstY1,
+                  slg::BlitArgs& a)
+{
+    if (srcX1 <= srcX0 || srcY1 <= srcY0 || dstX1 <= dstX0 || dstY1 <= dstY0)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "empty or inverted blit rectangle");
+    if (dstY1 > dstH) return ctx->fail(SLG_ERR_INVALID_ARG, "blit rectangle extends below the destination");
+    const uint64_t inW = (uint64_t)srcX1 - srcX0, inH = (uint64_t)srcY1 - srcY0;
+    const uint64_t x0 = dstX0, x1 = std::min<uint64_t>(dstW, x0 + ((uint64_t)dstX1 - dstX0));
+    const uint64_t y0 = dstY0, y1 = dstY1;
+    std::memset(&a, 0, sizeof(a));
+    a.foutW = ((inW << 16) / dstW) + 1u;
+    a.foutH = ((inH << 16) / dstH) + 1u;
+    a.x0 = x0;
+    a.y0 = y0;
+    a.nx = (x1 > x0) ? x1 - x0 : 0u;
+    a.ny = y1 - y0;
+    a.srcY0 = srcY0;
+    a.srcY1 = srcY1;
+    a.srcW = src.w;
+    a.dstW = dstW;
+    if (a.nx == 0u) return SLG_OK;
+    const uint64_t maxSrcX = ((x1 - 1u) * a.foutW) >> 16;
+    const uint64_t yfMin = (y0 * a.foutH) >> 16, yfMax = ((y1 - 1u) * a.foutH) >> 16;
+    if (maxSrcX >= src.w || srcY0 + yfMax + 1u > srcY1 || srcY1 - (srcY0 + yfMin) - 1u >= src.h)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "blit rectangle reads outside the source texture");
+    return SLG_OK;
+}
+
+bool blit_type_ok(int t) { return t == SLG_COLOR_RGBA_8U || t == SLG_COLOR_RGBA_FLOAT || t == SLG_COLOR_R_FLOAT; }
+
+} // namespace
+
+extern "C" {
+
+int slg_blit_rect(slg_context* ctx, size_t outId, size_t inId, uint16_t srcX0, uint16_t srcY0, uint16_t srcX1,
+                  uint16_t srcY1, uint16_t dstX0, uint16_t dstY0, uint16_t dstX1, uint16_t dstY1)
+{
+    if (!id_ok(outId, ctx->textures.size()) || !id_ok(inId, ctx->textures.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
+    const Texture& src = ctx->textures[inId];
+    Texture& dst = ctx->textures[outId];
+    if (!src.buf.ptr || !dst.buf.ptr || !blit_type_ok(src.type) || !blit_type_ok(dst.type))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "blit needs initialised R float, RGBA8 or RGBA float textures");
+    if (outId == inId) return ctx->fail(SLG_ERR_INVALID_ARG, "blit source and destination are the same texture");
+    slg::BlitArgs a;
+    int r = blit_geometry(ctx, src, dst.w, dst.h, srcX0, srcY0, srcX1, srcY1, dstX0, dstY0, dstX1, dstY1, a);
+    if (r || a.nx == 0u) return r;
+    a.src = static_cast<const uint8_t*>(src.buf.ptr);
+    a.dst = static_cast<uint8_t*>(dst.buf.ptr);
+    a.srcType = src.type;
+    a.dstType = dst.type;
+    cudaError_t e = slg::launch_blit(a, ctx->stream);
+    return (e == cudaSuccess) ? SLG_OK : ctx->cuda_fail(e, "blit launch");
+}
+
+int slg_blit(slg_context* ctx, size_t outId, size_t inId)
+{
+    if (!id_ok(outId, ctx->textures.size()) || !id_ok(inId, ctx->textures.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
+    const Texture& src = ctx->textures[inId];
+    const Texture& dst = ctx->textures[outId];
+    return slg_blit_rect(ctx, outId, inId, 0, 0, src.w, src.h, 0, 0, dst.w, dst.h);
+}
+
+int slg_blit_read(slg_context* ctx, size_t inId, int dstType, uint16_t dstW, uint16_t dstH, void* out, size_t numBytes)
+{
+    if (!id_ok(inId, ctx->textures.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
+    const Texture& src = ctx->textures[inId];
+    if (!src.buf.ptr || !blit_type_ok(src.type) || !blit_type_ok(dstType))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "blit needs R float, RGBA8 or RGBA float formats");
+    const size_t bytes = (size_t)dstW * dstH * bytes_per_color(dstType);
+    if (!out || numBytes != bytes || bytes == 0) return ctx->fail(SLG_ERR_INVALID_ARG, "destination byte count");
+    slg::BlitArgs a;
+    int r = blit_geometry(ctx, src, dstW, dstH, 0, 0, src.w, src.h, 0, 0, dstW, dstH, a);
+    if (r) return r;
+    if ((r = dev_alloc(ctx, ctx->blitBuf, bytes, false))) return r;
+    a.src = static_cast<const uint8_t*>(src.buf.ptr);
+    a.dst = static_cast<uint8_t*>(ctx->blitBuf.ptr);
+    a.srcType = src.type;
+    a.dstType = dstType;
+    cudaError_t e = slg::launch_blit(a, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, ctx->blitBuf.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "blit read");
     return check_status(ctx);
 }
 

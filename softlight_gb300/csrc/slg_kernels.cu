@@ -1426,6 +1426,79 @@ cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEven
     return e;
 }
 
+/*-----------------------------------------------------------------------------
+ * Blit (SL_BlitProcessor::blit_nearest, softlight/src/SL_BlitProcessor.cpp:621-660,
+ * with the blit operators of :20-420 and color_cast of SL_Color.hpp:600-690)
+-----------------------------------------------------------------------------*/
+__device__ __forceinline__ float4 blit_src_rgbaf(const BlitArgs& a, uint64_t i)
+{
+    switch (a.srcType)
+    {
+        case SLG_COLOR_RGBA_8U:
+            return unpack_rgba8(reinterpret_cast<const uint32_t*>(a.src)[i]);
+        case SLG_COLOR_RGBA_FLOAT:
+            return reinterpret_cast<const float4*>(a.src)[i];
+        default:
+            /* SL_Blit_R_to_RGBA: (min, min, r, max) in the source type */
+            return make_float4(0.f, 0.f, reinterpret_cast<const float*>(a.src)[i], 1.f);
+    }
+}
+
+__global__ void blit_kernel(const BlitArgs a)
+{
+    const uint64_t n = a.nx * a.ny;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride)
+    {
+        const uint64_t x = a.x0 + t % a.nx;
+        const uint64_t y = a.y0 + t / a.nx;
+        const uint64_t srcX = (x * a.foutW) >> 16;
+        const uint64_t yf = (y * a.foutH) >> 16;
+        const uint64_t srcY = a.srcY1 - (a.srcY0 + yf) - 1u;
+        const uint64_t si = srcX + a.srcW * srcY;
+        const uint64_t di = x + a.dstW * y;
+        if (a.srcType == a.dstType)
+        {
+            /* same format: a plain copy (SL_Blit_RGBA_to_RGBA<u8, u8> copies
+             * the 32-bit word; float to float is the identity cast) */
+            if (a.dstType == SLG_COLOR_RGBA_FLOAT) reinterpret_cast<float4*>(a.dst)[di] = reinterpret_cast<const float4*>(a.src)[si];
+            else reinterpret_cast<uint32_t*>(a.dst)[di] = reinterpret_cast<const uint32_t*>(a.src)[si];
+            continue;
+        }
+        if (a.srcType == SLG_COLOR_RGBA_8U && a.dstType == SLG_COLOR_R_FLOAT)
+        {
+            /* SL_Blit_RGBA_to_R<uint8_t, float>: the red channel of the cast */
+            reinterpret_cast<float*>(a.dst)[di] = (float)(reinterpret_cast<const uint32_t*>(a.src)[si] & 0xFFu) * 0.00392156862745f;
+            continue;
+        }
+        const float4 c = blit_src_rgbaf(a, si);
+        switch (a.dstType)
+        {
+            case SLG_COLOR_RGBA_8U:
+            {
+                /* color_cast<uint8_t, float>: (uint8_t)(c * 255) per channel */
+                const uint32_t r = f2u8(c.x * 255.f), g = f2u8(c.y * 255.f), b = f2u8(c.z * 255.f), w = f2u8(c.w * 255.f);
+                reinterpret_cast<uint32_t*>(a.dst)[di] = r | (g << 8) | (b << 16) | (w << 24);
+                break;
+            }
+            case SLG_COLOR_RGBA_FLOAT:
+                reinterpret_cast<float4*>(a.dst)[di] = c;
+                break;
+            default:
+                reinterpret_cast<float*>(a.dst)[di] = c.x;
+                break;
+        }
+    }
+}
+
+cudaError_t launch_blit(const BlitArgs& a, cudaStream_t s)
+{
+    const uint64_t n = a.nx * a.ny;
+    const unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 152u * 16u);
+    blit_kernel<<<blocks ? blocks : 1, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[4], cudaStream_t s)
 {
     const uint4 v = make_uint4(value[0], value[1], value[2], value[3]);

@@ -22,6 +22,20 @@ cudaError_t init_kernel_attributes(int keyCap);
 /* Fill numTexels texels of 4 or 16 bytes with value. */
 cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[4], cudaStream_t s);
 
+/* Nearest-neighbour blit of SL_BlitProcessor::blit_nearest over destination
+ * pixels [x0, x0 + nx) x [y0, y0 + ny); all reads were checked in bounds. */
+struct BlitArgs
+{
+    const uint8_t* src;
+    uint8_t* dst;
+    int32_t srcType, dstType;          /* slg_color_type */
+    uint64_t srcW, dstW;
+    uint64_t x0, y0, nx, ny;
+    uint64_t foutW, foutH;             /* 16.16 source steps per destination pixel */
+    uint64_t srcY0, srcY1;
+};
+cudaError_t launch_blit(const BlitArgs& a, cudaStream_t s);
+
 } // namespace slg
 
 #endif /* SLG_KERNELS_CUH */

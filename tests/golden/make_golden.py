@@ -6,7 +6,8 @@ oracle/ref_shim, portable branches, one thread).
 Each fixture is <name>.npz holding the colour and depth attachments after
 one frame of a seeded workload (tests/golden_scenes.py), plus SHA-256 digests
 of both arrays with every NaN replaced by one canonical NaN (x86 and aarch64
-produce different NaN payloads). Run from the repository root:
+produce different NaN payloads); blits.npz holds the results of the blit
+cases of tests/golden_scenes.py (blit_cases). Run from the repository root:
 
     python tests/golden/make_golden.py
 """
@@ -54,6 +55,13 @@ def main():
         print(name, index[name]["covered"])
     with open(os.path.join(HERE, "index.json"), "w") as fh:
         json.dump(index, fh, indent=1, sort_keys=True)
+
+    # blits (SL_Context::blit) of rendered attachments
+    ctx = SLContext(lib, "slr_", gpu=False)
+    blits = G.blit_cases(ctx)
+    ctx.close()
+    np.savez_compressed(os.path.join(HERE, "blits.npz"), **blits)
+    print("blits", sorted(blits))
 
 
 if __name__ == "__main__":

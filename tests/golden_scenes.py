@@ -28,3 +28,44 @@ SCENES = {
     "multi_draw": (E.multi_draw, dict()),
     "flat_triangle": (E.flat_triangle, dict(width=128, height=96)),
 }
+
+
+# (name, source: "color" | "depth" | "colorf", destination type, width, height)
+BLIT_READS = [
+    ("rgba8_to_rgba8_80x50", "color", A.COLOR_RGBA_8U, 80, 50),
+    ("rgba8_to_rgbaf_213x97", "color", A.COLOR_RGBA_FLOAT, 213, 97),
+    ("rgba8_to_rf_100x75", "color", A.COLOR_R_FLOAT, 100, 75),
+    ("rf_to_rgba8_160x120", "depth", A.COLOR_RGBA_8U, 160, 120),
+    ("rf_to_rgbaf_57x33", "depth", A.COLOR_RGBA_FLOAT, 57, 33),
+    ("rf_to_rf_320x240", "depth", A.COLOR_R_FLOAT, 320, 240),
+    ("rgbaf_to_rgba8_120x90", "colorf", A.COLOR_RGBA_8U, 120, 90),
+    ("rgbaf_to_rf_96x80", "colorf", A.COLOR_R_FLOAT, 96, 80),
+    ("rgbaf_to_rgbaf_50x40", "colorf", A.COLOR_RGBA_FLOAT, 50, 40),
+]
+
+
+def blit_cases(ctx):
+    """Blits (SL_Context::blit) of rendered attachments through ctx: scaled
+    reads into host buffers of every supported format, a rectangle blit into
+    a patterned texture and a whole-texture blit. Returns {name: array}."""
+    out = {}
+    s = S.build_c1(ctx, width=160, height=120)
+    s.render()
+    f = E.random_soup(ctx, program=A.PROGRAM_VCOLOR_TEXF, color_type=A.COLOR_RGBA_FLOAT)
+    f.render()
+    src = {"color": s.color_tex, "depth": s.depth_tex, "colorf": f.color_tex}
+    for name, which, ctype, w, h in BLIT_READS:
+        out[name] = ctx.blit_read(src[which], ctype, w, h)
+
+    dst = ctx.create_texture()
+    ctx.texture_init(dst, A.COLOR_RGBA_8U, 200, 150, 1)
+    ctx.texture_set_texels(dst, (np.arange(200 * 150 * 4) % 251).astype(np.uint8).reshape(150, 200, 4))
+    ctx.blit_rect(dst, s.color_tex, (10, 5, 150, 100), (20, 30, 180, 140))
+    out["rect_rgba8_into_pattern"] = ctx.texture_read(dst, (150, 200, 4), np.uint8)
+
+    dstf = ctx.create_texture()
+    ctx.texture_init(dstf, A.COLOR_RGBA_FLOAT, 64, 48, 1)
+    ctx.texture_set_texels(dstf, np.full((48, 64, 4), 0.25, np.float32))
+    ctx.blit(dstf, s.depth_tex)
+    out["whole_rf_to_rgbaf_64x48"] = ctx.texture_read(dstf, (48, 64, 4), np.float32)
+    return out

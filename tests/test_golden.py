@@ -52,6 +52,18 @@ def test_oracle_matches_reference_golden(oracle_mod, name):
     ctx.close()
 
 
+def test_oracle_blits_match_reference_golden(oracle_mod):
+    """SL_Context::blit: scaled reads in every format pair, a rectangle blit
+    and a whole-texture blit, against the reference's outputs."""
+    want = np.load(os.path.join(GOLDEN, "blits.npz"))
+    ctx = oracle_mod.Context()
+    got = G.blit_cases(ctx)
+    ctx.close()
+    assert set(got) == set(want.files)
+    for name in want.files:
+        assert same(got[name], want[name]), f"blit {name} differs from the reference"
+
+
 @pytest.mark.parametrize("threads", [2, 5])
 def test_oracle_threads_match_one_thread(oracle_mod, threads):
     """The oracle's multi-threaded mode (used for the CPU baseline timing)
