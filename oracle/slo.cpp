@@ -1342,6 +1342,56 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
         }
 
         const bool blending = group.empty() ? false : (ctx->shaders[group[0].shaderId].blend != SLG_BLEND_OFF);
+
+        if (!group.empty() && (group[0].mesh.mode == SLG_RENDER_MODE_POINTS || group[0].mesh.mode == SLG_RENDER_MODE_INDEXED_POINTS))
+        {
+            /* SL_PointProcessor::process_verts and SL_PointRasterizer::render_point
+             * (softlight/src/SL_PointProcessor.cpp:63-110, SL_PointRasterizer.cpp:26-90),
+             * one thread: points in element order, each depth-tested and
+             * written at once, at linear index x + W*y of its 16-bit screen
+             * coordinates (an index past the buffer is dropped). */
+            const size_t W = depthTex.w, H = depthTex.h;
+            for (const Unit& u : units)
+            {
+                const DrawItem& it = group[u.draw];
+                const DrawState& ds = states[u.draw];
+                const Shader& sh = *ds.shader;
+                const Vao& vao = ctx->vaos[it.mesh.vaoId];
+                const bool indexed = (it.mesh.mode == SLG_RENDER_MODE_INDEXED_POINTS);
+                const Ibo* ibo = (indexed && vao.ibo != SLG_INVALID_ID) ? &ctx->ibos[vao.ibo] : nullptr;
+                if (indexed && !ibo) return ctx->fail(SLG_ERR_INVALID_ARG, "indexed draw without index buffer");
+                for (size_t i = it.mesh.elementBegin; i < it.mesh.elementEnd; ++i)
+                {
+                    const size_t vertId = ibo ? read_index(*ibo, i) : i;
+                    V4 vary[4];
+                    for (int k = 0; k < 4; ++k) vary[k] = mk(0.f, 0.f, 0.f, 0.f);
+                    V4 v = mat_mul(ds.scissor, run_vs(sh.vsProgram, ds.env, vertId, u.instance, vary));
+                    const float w = v[3], nw = -v[3];
+                    const bool visible = (w > 0.f) && (v[0] <= w && v[1] <= w && v[2] <= w && v[3] <= w) &&
+                                         (v[0] >= nw && v[1] >= nw && v[2] >= nw && v[3] >= nw);
+                    if (!visible) continue;
+                    perspective_divide(v);
+                    ndc_to_screen(v, ds.viewport);
+                    const size_t x = (uint32_t)f2i(v[0]) & 0xFFFFu, y = (uint32_t)f2i(v[1]) & 0xFFFFu;
+                    const size_t lin = x + W * y;
+                    if (lin >= W * H) continue;
+                    const float z = v[2];
+                    if (!depth_cmp(sh.depthTest, z, rs.depth[lin])) continue;
+                    V4 outputs[4];
+                    if (run_fs(sh.fsProgram, ds.env, vary, outputs))
+                    {
+                        for (unsigned t = 0; t < sh.numOutputs && t < rs.numOutputs; ++t)
+                        {
+                            write_color(rs.colors[t], (unsigned)(lin % W), (unsigned)(lin / W), outputs[t], sh.blend);
+                        }
+                    }
+                    if (sh.depthMask == SLG_DEPTH_MASK_ON) rs.depth[lin] = z;
+                    ++totalFrags;
+                }
+            }
+            continue;
+        }
+
         std::vector<Bin> bins;
 
         for (const Unit& u : units)
@@ -1404,7 +1454,8 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
 
 static bool valid_tri_mesh(const slg_mesh* m)
 {
-    return m && (m->mode == SLG_RENDER_MODE_TRIANGLES || m->mode == SLG_RENDER_MODE_INDEXED_TRIANGLES);
+    return m && (m->mode == SLG_RENDER_MODE_TRIANGLES || m->mode == SLG_RENDER_MODE_INDEXED_TRIANGLES ||
+                 m->mode == SLG_RENDER_MODE_POINTS || m->mode == SLG_RENDER_MODE_INDEXED_POINTS);
 }
 
 int slo_draw(slo_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId)
@@ -1414,7 +1465,7 @@ int slo_draw(slo_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId)
 
 int slo_draw_instanced(slo_context* ctx, const slg_mesh* m, size_t numInstances, size_t shaderId, size_t fboId)
 {
-    if (!valid_tri_mesh(m)) return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle render modes are supported");
+    if (!valid_tri_mesh(m)) return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle and point render modes are supported");
     std::vector<std::vector<DrawItem>> groups(1);
     groups[0].push_back({*m, numInstances, shaderId, false});
     return run_draws(ctx, groups, fboId);
@@ -1426,7 +1477,7 @@ int slo_draw_multiple(slo_context* ctx, const slg_mesh* meshes, size_t numMeshes
     std::vector<std::vector<DrawItem>> groups(1);
     for (size_t i = 0; i < numMeshes; ++i)
     {
-        if (!valid_tri_mesh(&meshes[i])) return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle render modes are supported");
+        if (!valid_tri_mesh(&meshes[i])) return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle and point render modes are supported");
         groups[0].push_back({meshes[i], 1, shaderId, true});
     }
     return run_draws(ctx, groups, fboId);
@@ -1437,7 +1488,7 @@ int slo_draw_batch(slo_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, s
     std::vector<std::vector<DrawItem>> groups;
     for (size_t i = 0; i < numCmds; ++i)
     {
-        if (!valid_tri_mesh(&cmds[i].mesh)) return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle render modes are supported");
+        if (!valid_tri_mesh(&cmds[i].mesh)) return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle and point render modes are supported");
         groups.push_back({{cmds[i].mesh, cmds[i].numInstances, cmds[i].shaderId, false}});
     }
     return run_draws(ctx, groups, fboId);

@@ -388,9 +388,10 @@ int validate_draw(slg_context* ctx, const Shader& sh, const Vao& vao, const slg_
     const Vbo& vbo = ctx->vbos[vao.vbo];
     const Binding& b0 = vao.bindings[0];
     if (b0.offset < 0 || b0.stride <= 0) return ctx->fail(SLG_ERR_INVALID_ARG, "binding 0 needs offset >= 0 and stride > 0");
-    const uint64_t lastElement = m.elementBegin + 3 * ((numElements + 2) / 3) - 1;
+    const bool points = (m.mode == SLG_RENDER_MODE_POINTS || m.mode == SLG_RENDER_MODE_INDEXED_POINTS);
+    const uint64_t lastElement = points ? m.elementBegin + numElements - 1 : m.elementBegin + 3 * ((numElements + 2) / 3) - 1;
     uint64_t maxVertex;
-    if (m.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES)
+    if (m.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES || m.mode == SLG_RENDER_MODE_INDEXED_POINTS)
     {
         const Ibo& ibo = ctx->ibos[vao.ibo];
         if (m.elementEnd > ibo.count) return ctx->fail(SLG_ERR_INVALID_ARG, "element range exceeds the index buffer");
@@ -451,12 +452,13 @@ int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, Draw
     const slg_mesh& m = req.mesh;
     if (req.shaderId >= ctx->shaders.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid shader id");
     if (m.vaoId >= ctx->vaos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid vao id");
-    if (m.mode != SLG_RENDER_MODE_TRIANGLES && m.mode != SLG_RENDER_MODE_INDEXED_TRIANGLES)
-        return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle render modes are supported");
+    const bool points = (m.mode == SLG_RENDER_MODE_POINTS || m.mode == SLG_RENDER_MODE_INDEXED_POINTS);
+    if (m.mode != SLG_RENDER_MODE_TRIANGLES && m.mode != SLG_RENDER_MODE_INDEXED_TRIANGLES && !points)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle and point render modes are supported");
     const Shader& sh = ctx->shaders[req.shaderId];
     const Vao& vao = ctx->vaos[m.vaoId];
     if (vao.vbo == SLG_INVALID_ID || !ctx->vbos[vao.vbo].buf.ptr) return ctx->fail(SLG_ERR_INVALID_ARG, "vao has no vertex buffer");
-    const bool indexed = (m.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES);
+    const bool indexed = (m.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES || m.mode == SLG_RENDER_MODE_INDEXED_POINTS);
     if (indexed && (vao.ibo == SLG_INVALID_ID || !ctx->ibos[vao.ibo].buf.ptr))
         return ctx->fail(SLG_ERR_INVALID_ARG, "indexed draw without index buffer");
 
@@ -475,7 +477,8 @@ int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, Draw
     d.b0Stride = vao.bindings[0].stride;
     d.elementBegin = m.elementBegin;
     d.numElements = (m.elementEnd > m.elementBegin) ? (m.elementEnd - m.elementBegin) : 0;
-    d.numTris = (d.numElements + 2) / 3;
+    d.numTris = points ? d.numElements : (d.numElements + 2) / 3;
+    d.prim = points ? slg::kPrimPoint : slg::kPrimTriangle;
     d.numInstances = std::max<size_t>(1, req.numInstances);
     d.slotBase = slotBase;
     d.primBase = req.primBase;
@@ -1435,6 +1438,7 @@ int diff_args(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId
     int r = build_desc(ctx, req, 0, d, numSlots);
     if (r) return r;
     const Shader& sh = ctx->shaders[shaderId];
+    if (d.prim != slg::kPrimTriangle) return ctx->fail(SLG_ERR_INVALID_ARG, "the differentiable model covers triangle draws only");
     if (sh.vsProgram != SLG_PROGRAM_VCOLOR_TEXF || sh.fsProgram != SLG_PROGRAM_VCOLOR_TEXF)
         return ctx->fail(SLG_ERR_INVALID_ARG, "the differentiable model covers SLG_PROGRAM_VCOLOR_TEXF draws only");
     if ((d.b0Offset & 3) || (d.b0Stride & 3)) return ctx->fail(SLG_ERR_INVALID_ARG, "binding 0 offset and stride must be multiples of 4 bytes");

@@ -71,15 +71,25 @@ struct DrawDesc
     int64_t  b0Stride;
     uint64_t elementBegin;
     uint64_t numElements;   /* elementEnd - elementBegin */
-    uint64_t numTris;       /* ceil(numElements / 3) per instance */
+    uint64_t numTris;       /* primitives per instance: ceil(numElements / 3) triangles, or numElements points */
     uint64_t numInstances;
     uint64_t slotBase;      /* first slot of this draw in the launch */
     uint64_t primBase;      /* primIndex offset (draw_multiple keeps per-mesh primIndex) */
     int32_t  indexType;     /* -1: non-indexed */
     uint32_t vsProgram;
     uint32_t fsProgram;
-    uint8_t  cull, numVaryings, depthTest, depthMask, blend, numOutputs, pad0, pad1;
+    uint8_t  cull, numVaryings, depthTest, depthMask, blend, numOutputs, prim, pad1;
 };
+
+/* DrawDesc::prim */
+enum PrimKind
+{
+    kPrimTriangle = 0,
+    kPrimPoint = 1
+};
+
+/* record r7.w: depth test | depth mask << 4 | this bit for a point record */
+constexpr uint32_t kRecordPoint = 1u << 5;
 
 /* Per-launch scratch and framebuffer description. */
 struct Frame

@@ -420,11 +420,63 @@ __device__ __forceinline__ uint64_t read_index(const DrawDesc& d, uint64_t i)
  * Kernel 1: vertex processing, clipping, set-up and tile counting
  * (SL_TriProcessor::process_verts, SL_TriProcessor.cpp:527-640)
 -----------------------------------------------------------------------------*/
+/* SL_PointProcessor::process_verts for one point (softlight/src/SL_PointProcessor.cpp:63-110):
+ * vertex program, scissor, the one-vertex clip status (fully inside
+ * [-w, w] with w > 0, SL_PostVertexTransform.hpp:536-552), divide and
+ * viewport. The fragment lands where SL_PointRasterizer addresses it: the
+ * 16-bit screen coordinates at linear index x + W*y (SL_PointRasterizer.cpp:
+ * 45-57), so x == W wraps to the next row; an index past the buffer (which
+ * the reference would write out of bounds) is dropped. */
+__device__ __forceinline__ uint32_t setup_point(const Frame& f, const DrawDesc& d, int di, uint64_t slot, uint64_t local,
+                                                TileRange& tr, bool& counted)
+{
+    const uint64_t inst = local / d.numTris;
+    const uint64_t e = d.elementBegin + (local - inst * d.numTris);
+    const DevEnv env = make_env(d, f.tables);
+    const uint64_t vid = (d.indexType >= 0) ? read_index(d, e) : e;
+    slg_v4 vary[kMaxVaryings];
+    float4 c = mat_mul(f.scissor, to_f4(run_vertex_program(d.vsProgram, env, vid, inst, vary)));
+    const float w = c.w, nw = -c.w;
+    const bool visible = (w > 0.f) && (c.x <= w && c.y <= w && c.z <= w && c.w <= w) &&
+                         (c.x >= nw && c.y >= nw && c.z >= nw && c.w >= nw);
+    if (!visible)
+    {
+        return 0;
+    }
+    const float4 sc = to_screen(c, f.viewport);
+    const uint64_t lin = (uint64_t)((uint32_t)f2i(sc.x) & 0xFFFFu) + (uint64_t)f.width * ((uint32_t)f2i(sc.y) & 0xFFFFu);
+    if (lin >= (uint64_t)f.width * (uint64_t)f.height)
+    {
+        return 0;
+    }
+    const int px = (int)(lin % (uint64_t)f.width), py = (int)(lin / (uint64_t)f.width);
+    Record rec;
+    rec.r[0] = sc;
+    rec.r[1] = rec.r[2] = rec.r[3] = rec.r[4] = rec.r[5] = make_float4(0.f, 0.f, 0.f, 0.f);
+    rec.r[6] = make_float4(__int_as_float(py), __int_as_float(py + 1), __int_as_float(px), __int_as_float(px));
+    rec.r[7] = make_float4(__uint_as_float((uint32_t)di), __uint_as_float((uint32_t)e), __uint_as_float((uint32_t)(e >> 32)),
+                           __uint_as_float((uint32_t)d.depthTest | ((uint32_t)d.depthMask << 4) | kRecordPoint));
+    store_record(f, slot, rec);
+    float4* dst = f.varyings + slot * kVaryingVec4;
+#pragma unroll
+    for (int vi = 0; vi < kMaxVaryings; ++vi)
+    {
+        if (vi < d.numVaryings) dst[vi] = to_f4(vary[vi]);
+    }
+    tr = tile_range(rec.r[6], f);
+    counted = true;
+    return 1;
+}
+
 __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, TileRange& tr, bool& counted)
 {
     const int di = (f.numDraws > 1) ? find_draw(f, slot) : 0;
     const DrawDesc& d = f.draws[di];
     const uint64_t local = slot - d.slotBase;
+    if (d.prim == kPrimPoint)
+    {
+        return setup_point(f, d, di, slot, local, tr, counted);
+    }
     const uint64_t inst = local / d.numTris;
     const uint64_t tri = local - inst * d.numTris;
     const uint64_t i = d.elementBegin + 3u * tri;
@@ -905,6 +957,25 @@ __device__ __forceinline__ bool shade(const Frame& f, const DrawDesc& dd, uint64
     return have && dd.numOutputs > 0;
 }
 
+/* SL_PointRasterizer::render_point's shading (SL_PointRasterizer.cpp:59-90):
+ * the point's varyings are handed to the fragment program unchanged. */
+__device__ __forceinline__ bool shade_point(const Frame& f, const DrawDesc& dd, uint64_t rec, float4& out)
+{
+    slg_v4 vary[kMaxVaryings];
+    const float4* V = f.varyings + rec * kVaryingVec4;
+#pragma unroll
+    for (int vi = 0; vi < kMaxVaryings; ++vi)
+    {
+        const float4 v = (vi < dd.numVaryings) ? V[vi] : make_float4(0.f, 0.f, 0.f, 0.f);
+        vary[vi] = slg_make_v4(v.x, v.y, v.z, v.w);
+    }
+    slg_v4 outputs[4];
+    const DevEnv env = make_env(dd, f.tables);
+    const bool have = run_fragment_program(dd.fsProgram, env, vary, outputs);
+    out = to_f4(outputs[0]);
+    return have && dd.numOutputs > 0;
+}
+
 template <int TW, int TH, class Color>
 struct RasterLayout
 {
@@ -1044,12 +1115,37 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
             {
                 return;
             }
+            const uint32_t flags = __float_as_uint(R[7].w);
+            if (flags & kRecordPoint)
+            {
+                const int px = __float_as_int(r6.z);
+                if (px < myX0 || px >= xLimit || ((px - myX0) & 3) != 0)
+                {
+                    return;
+                }
+                const int idx = r * L::kStride + (px - x0);
+                const float z = R[0].z;
+                if (depth_cmp(flags & 0xF, z, sDepth[idx]))
+                {
+                    const DrawDesc& dd = f.draws[__float_as_uint(R[7].x)];
+                    float4 o;
+                    if (shade_point(f, dd, key_to_record(f, sRecKey[ri]), o) && f.color)
+                    {
+                        sColor[idx] = (dd.blend != SLG_BLEND_OFF) ? Color::store(blend_color(dd.blend, o, Color::load(sColor[idx])))
+                                                                  : Color::store(o);
+                    }
+                    if ((flags >> 4) & 1)
+                    {
+                        sDepth[idx] = z;
+                    }
+                }
+                return;
+            }
             Chain ch;
             if (!chain_begin(R, yf, myX0, xLimit, ch))
             {
                 return;
             }
-            const uint32_t flags = __float_as_uint(R[7].w);
             const int depthFunc = flags & 0xF;
             const bool depthMask = (flags >> 4) & 1;
             const uint32_t drawIndex = __float_as_uint(R[7].x);
@@ -1176,6 +1272,26 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
         }
         const float4* R = sRec + lo * kRecordVec4;
         const int y = max(__float_as_int(R[6].x), y0) + (int)(i - sPre[lo]);
+        if (__float_as_uint(R[7].w) & kRecordPoint)
+        {
+            const int px = __float_as_int(R[6].z);
+            const int idx = (y - y0) * TW + (px - x0);
+            const float z = R[0].z;
+            if (px < x0 || px >= xLimit || !depth_cmp(func, z, sD0[idx]))
+            {
+                continue;
+            }
+            const unsigned long long p = free_pack(func, mask, z, sKey[lo]);
+            if (kStore)
+            {
+                if (sBest[idx] == p) sB[idx] = make_float4(0.f, 0.f, 0.f, z);
+            }
+            else
+            {
+                atomicMin(sBest + idx, p);
+            }
+            continue;
+        }
         const float yf = (float)y;
         const Span sp = scanline_span(R[0], R[1], yf);
         if (!((uint32_t)sp.xMin < (uint32_t)sp.xMax))
@@ -1303,7 +1419,8 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
         if (f.color && dd.numOutputs > 0)
         {
             float4 o;
-            if (shade(f, dd, rec, R[2].w, R[5], b.x, b.y, b.z, o))
+            const bool point = (__float_as_uint(R[7].w) & kRecordPoint) != 0;
+            if (point ? shade_point(f, dd, rec, o) : shade(f, dd, rec, R[2].w, R[5], b.x, b.y, b.z, o))
             {
                 Color::write(f.color, gi, Color::store(o));
             }

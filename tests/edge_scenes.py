@@ -103,3 +103,50 @@ def flat_triangle(ctx, width=640, height=480):
                       cull=A.CULL_OFF, depth_test=A.DEPTH_TEST_OFF, depth_mask=A.DEPTH_MASK_OFF)
     s.draws.append((mesh, 1, sh))
     return s
+
+
+def random_points(ctx, num_points=3000, width=64, height=48, seed=41, blend=A.BLEND_OFF,
+                  depth_test=A.DEPTH_TEST_LESS_THAN, depth_mask=A.DEPTH_MASK_ON, indexed=None,
+                  color_type=A.COLOR_RGBA_8U, clear_depth=1.0, num_instances=1):
+    """Point draw (SL_RENDER_MODE_POINTS): seeded points in and around the
+    view volume, dense enough that many share a pixel; vertex colour x RGBA8
+    texture program with vertex alpha."""
+    rng = np.random.default_rng(seed)
+    s = S.Scene(ctx, f"points_{seed}", width, height, color_type=color_type)
+    pos = np.stack([rng.uniform(-1.3, 1.3, num_points), rng.uniform(-1.3, 1.3, num_points),
+                    rng.uniform(-1.2, 1.2, num_points)], 1)
+    col = np.concatenate([rng.uniform(0.0, 1.0, (num_points, 3)), rng.uniform(0.2, 1.0, (num_points, 1))], 1)
+    uv = rng.uniform(-0.5, 1.5, (num_points, 2))
+    verts = np.concatenate([pos, col, uv], 1).astype(np.float32)
+    tex = s.add_texture_rgba8(S.to_rgba8(S.value_noise(32, 32, seed=seed, octaves=2, alpha=1.0)))
+    if indexed is None:
+        mesh = s.add_mesh(verts, None, stride=36)
+        mesh.mode = A.RENDER_MODE_POINTS
+    else:
+        order = rng.permutation(num_points)
+        mesh = s.add_mesh(verts, order.astype(indexed), stride=36)
+        mesh.mode = A.RENDER_MODE_INDEXED_POINTS
+    sh = s.add_shader(A.PROGRAM_VCOLOR_TEX_ALPHA, 2, S.vcolor_uniforms(np.eye(4), tex), cull=A.CULL_OFF,
+                      depth_test=depth_test, depth_mask=depth_mask, blend=blend)
+    s.draws.append((mesh, num_instances, sh))
+    s.num_triangles = num_points
+    s.clear_depth = clear_depth
+    return s
+
+
+def point_edges(ctx, width=40, height=30):
+    """Points placed at the edges of the reference's point addressing: x = W
+    lands on the next row's first pixel (linear index x + W*y), x = W on the
+    last row falls past the buffer and is dropped, w <= 0 and |x| > w are
+    culled; identity transform, flat colour, depth off."""
+    s = S.Scene(ctx, "point_edges", width, height)
+    pts = [(1.0, 0.0, 0.0), (1.0, -1.0, 0.0), (1.0, 1.0, 0.0), (-1.0, -1.0, 0.0), (0.999, 0.999, 0.0),
+           (1.0001, 0.0, 0.0), (0.0, 0.0, 1.0), (0.0, 0.0, -1.0), (0.5, -0.5, 0.5), (-1.0, 1.0, 0.0)]
+    verts = np.zeros((len(pts), 9), np.float32)
+    verts[:, :3] = pts
+    mesh = s.add_mesh(verts, None, stride=36)
+    mesh.mode = A.RENDER_MODE_POINTS
+    sh = s.add_shader(A.PROGRAM_FLAT_COLOR, 0, S.flat_uniforms(np.eye(4), (1.0, 0.5, 0.25, 1.0)),
+                      cull=A.CULL_OFF, depth_test=A.DEPTH_TEST_OFF, depth_mask=A.DEPTH_MASK_OFF)
+    s.draws.append((mesh, 1, sh))
+    return s

@@ -27,6 +27,13 @@ SCENES = {
     "big_triangles": (E.big_triangles, dict()),
     "multi_draw": (E.multi_draw, dict()),
     "flat_triangle": (E.flat_triangle, dict(width=128, height=96)),
+    "points_less": (E.random_points, dict()),
+    "points_blend_alpha": (E.random_points, dict(blend=A.BLEND_ALPHA, depth_mask=A.DEPTH_MASK_OFF, seed=42)),
+    "points_u16_depth_off": (E.random_points, dict(indexed=np.uint16, depth_test=A.DEPTH_TEST_OFF, seed=43)),
+    "points_gequal_float": (E.random_points, dict(depth_test=A.DEPTH_TEST_GREATER_EQUAL, clear_depth=-1.0,
+                                                  color_type=A.COLOR_RGBA_FLOAT, seed=44)),
+    "points_not_equal": (E.random_points, dict(depth_test=A.DEPTH_TEST_NOT_EQUAL, clear_depth=0.5, seed=45)),
+    "point_edges": (E.point_edges, dict()),
 }
 
 

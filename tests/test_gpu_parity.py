@@ -225,3 +225,25 @@ def test_autotune_picks_a_valid_config(ctxs):
     sg.render()
     so.render()
     assert compare_scenes(sg, so, "autotuned") == 0
+
+
+@pytest.mark.parametrize("kw", [
+    dict(num_points=200000, width=320, height=240),
+    dict(num_points=100000, width=256, height=192, blend=A.BLEND_ALPHA, depth_mask=A.DEPTH_MASK_OFF, seed=52),
+    dict(num_points=50000, width=200, height=150, num_instances=3, seed=53),
+    dict(num_points=50000, width=200, height=150, depth_test=A.DEPTH_TEST_LESS_EQUAL, indexed=np.uint32, seed=54),
+], ids=["less_200k", "blend_100k", "instanced_3x50k", "lequal_indexed"])
+def test_points(ctxs, kw):
+    """SL_RENDER_MODE_POINTS: order-free (depth rules) and ordered (blending)
+    resolution of many points per pixel, against the oracle."""
+    g, o = ctxs
+    sg, so = render_both(E.random_points, g, o, **kw)
+    compare_scenes(sg, so, "points")
+
+
+@pytest.mark.parametrize("tile", [(8, 8), (64, 64)])
+def test_points_all_tiles(ctxs, tile):
+    g, o = ctxs
+    g.set_tile_size(*tile)
+    sg, so = render_both(E.random_points, g, o, num_points=30000, width=300, height=200, seed=55)
+    compare_scenes(sg, so, f"points {tile}")
