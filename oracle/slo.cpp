@@ -739,6 +739,7 @@ struct RasterState
     const slo_context* ctx;
     float* depth;
     uint16_t width;
+    uint16_t height;
     Target colors[4];
     unsigned numOutputs;
     std::vector<const Shader*> shaders; /* per draw index */
@@ -884,6 +885,200 @@ static void raster_bin(const RasterState& rs, const Bin& bin, int rowStride, int
 
 /* radix-sort of a flush group by primIndex when blending
  * (SL_VertexProcessor.cpp:110-119; stable) */
+/*-----------------------------------------------------------------------------
+ * Lines: SL_LineProcessor (softlight/src/SL_LineProcessor.cpp:25-279) and
+ * SL_LineRasterizer::render_line (softlight/src/SL_LineRasterizer.cpp:26-90),
+ * one thread, the bins in element order.
+-----------------------------------------------------------------------------*/
+struct LineVert
+{
+    V4 vert;
+    V4 varyings[4];
+};
+
+/* sl_draw_line_bresenham (softlight/include/softlight/SL_Geometry.hpp:313-366),
+ * sl_lowp_t = int16_t */
+template <typename Fn>
+static void line_bresenham(int16_t x1, int16_t y1, int16_t x2, int16_t y2, Fn&& fn)
+{
+    const bool steep = std::abs(x1 - x2) < std::abs(y1 - y2);
+    if (steep)
+    {
+        std::swap(x1, y1);
+        std::swap(x2, y2);
+    }
+    if (x1 > x2)
+    {
+        std::swap(x1, x2);
+        std::swap(y1, y2);
+    }
+    const int16_t dx = (int16_t)(x2 - x1);
+    const int16_t dy = (int16_t)(y2 - y1);
+    const int16_t dErr = (int16_t)((dy < 0 ? -dy : dy) * 2);
+    const int16_t yErr = (y2 > y1) ? 1 : -1;
+    int16_t err = 0;
+    int16_t y = y1;
+    for (int16_t x = x1; x <= x2; ++x)
+    {
+        if (steep) fn((uint16_t)y, (uint16_t)x);
+        else fn((uint16_t)x, (uint16_t)y);
+        err = (int16_t)(err + dErr);
+        if (err > dx)
+        {
+            y = (int16_t)(y + yErr);
+            err = (int16_t)(err - 2 * dx);
+        }
+    }
+}
+
+/* SL_LineRasterizer::render_line + SL_FragmentProcessor::flush_line_fragments
+ * (SL_FragmentProcessor.cpp:346-402): fragments are depth-tested when they
+ * are queued and written when the queue of SL_SHADER_MAX_QUEUED_FRAGS (600)
+ * is flushed or the line ends. */
+static void render_line(const RasterState& rs, const DrawState& ds, const LineVert& a, const LineVert& b, uint64_t& frags)
+{
+    const Shader& sh = *ds.shader;
+    const float z0 = a.vert[2], z1 = b.vert[2];
+    const float sc0x = a.vert[0], sc0y = a.vert[1], sc1x = b.vert[0], sc1y = b.vert[1];
+    const float ex = sc1x - sc0x, ey = sc1y - sc0y;
+    const float dist = 1.f / std::sqrt(ex * ex + ey * ey);
+    const size_t W = rs.width, H = rs.height;
+
+    struct Frag { float interp, z; uint16_t x, y; };
+    std::vector<Frag> queue;
+    queue.reserve(600);
+    const auto flush = [&]() {
+        for (const Frag& q : queue)
+        {
+            V4 vary[4];
+            for (unsigned i = 0; i < 4; ++i) vary[i] = mk(0.f, 0.f, 0.f, 0.f);
+            for (unsigned i = 0; i < ds.numVaryings; ++i) vary[i] = mix(a.varyings[i], b.varyings[i], q.interp);
+            V4 outputs[4];
+            const size_t lin = (size_t)q.x + W * q.y;
+            if (run_fs(sh.fsProgram, ds.env, vary, outputs))
+            {
+                for (unsigned t = 0; t < sh.numOutputs && t < rs.numOutputs; ++t)
+                {
+                    write_color(rs.colors[t], (unsigned)(lin % W), (unsigned)(lin / W), outputs[t], sh.blend);
+                }
+            }
+            if (sh.depthMask == SLG_DEPTH_MASK_ON) rs.depth[lin] = q.z;
+            ++frags;
+        }
+        queue.clear();
+    };
+    const auto to_u16 = [](float v) { return (uint16_t)((uint32_t)f2i(v) & 0xFFFFu); };
+    line_bresenham((int16_t)to_u16(sc0x), (int16_t)to_u16(sc0y), (int16_t)to_u16(sc1x), (int16_t)to_u16(sc1y),
+                   [&](uint16_t x, uint16_t y) {
+                       const float px = (float)x - sc0x, py = (float)y - sc0y;
+                       const float currLen = std::sqrt(((px * px + py * py) + 0.f * 0.f) + 0.f * 0.f);
+                       const float interp = currLen * dist;
+                       const float z = (z1 - z0) * interp + z0;
+                       const size_t lin = (size_t)x + W * y;
+                       if (lin >= W * H) return; /* past the buffer: out of bounds in the reference */
+                       if (!depth_cmp(sh.depthTest, z, rs.depth[lin])) return;
+                       queue.push_back({interp, z, x, y});
+                       if (queue.size() == 600) flush();
+                   });
+    flush();
+}
+
+/* _clip_segment of SL_LineProcessor::clip_and_process_lines (SL_LineProcessor.cpp:94-126) */
+static bool clip_segment(float num, float denom, float& tE, float& tL)
+{
+    if (std::fabs(denom) < 1.0e-6f) return num < 0.f;
+    const float t = num / denom;
+    if (denom > 0.f)
+    {
+        if (t > tL) return false;
+        if (t > tE) tE = t;
+    }
+    else
+    {
+        if (t < tE) return false;
+        if (t < tL) tL = t;
+    }
+    return true;
+}
+
+/* SL_LineProcessor::clip_and_process_lines (SL_LineProcessor.cpp:63-166) */
+static void clip_and_render_line(const RasterState& rs, const DrawState& ds, const LineVert& a, const LineVert& b, uint64_t& frags)
+{
+    const float dx = b.vert[0] - a.vert[0], dy = b.vert[1] - a.vert[1];
+    const float xMin = ds.viewport[0], yMin = ds.viewport[1], xMax = ds.viewport[2], yMax = ds.viewport[3];
+    if (std::fabs(dx) < 1.0e-6f && std::fabs(dy) < 1.0e-6f)
+    {
+        if (a.vert[0] >= xMin && a.vert[0] <= xMax && a.vert[1] >= yMin && a.vert[1] <= yMax)
+        {
+            render_line(rs, ds, a, b, frags);
+            return;
+        }
+    }
+    LineVert p0 = a, p1 = b;
+    const float lx = p0.vert[0] - p1.vert[0], ly = p0.vert[1] - p1.vert[1];
+    const float dist = 1.f / std::sqrt(lx * lx + ly * ly);
+    float tE = 0.f, tL = 1.f;
+    const float x1 = p0.vert[0], y1 = p0.vert[1];
+    if (!(clip_segment(xMin - x1, dx, tE, tL) && clip_segment(x1 - xMax, -dx, tE, tL) &&
+          clip_segment(yMin - y1, dy, tE, tL) && clip_segment(y1 - yMax, -dy, tE, tL)))
+    {
+        return;
+    }
+    if (tL < 1.f)
+    {
+        p1.vert[0] = x1 + tL * dx;
+        p1.vert[1] = y1 + tL * dy;
+    }
+    if (tE > 0.f)
+    {
+        p0.vert[0] = x1 + tE * dx;
+        p0.vert[1] = y1 + tE * dy;
+    }
+    const V4 d0 = sub(p0.vert, a.vert), d1 = sub(p1.vert, b.vert);
+    const float interp0 = std::sqrt(dot(d0, d0)) * dist;
+    const float interp1 = std::sqrt(dot(d1, d1)) * dist;
+    p0.vert[2] = (b.vert[2] - a.vert[2]) * interp0 + a.vert[2];
+    p0.vert[3] = (b.vert[3] - a.vert[3]) * interp0 + a.vert[3];
+    p1.vert[2] = (a.vert[2] - b.vert[2]) * interp1 + b.vert[2];
+    p1.vert[3] = (a.vert[3] - b.vert[3]) * interp1 + b.vert[3];
+    for (unsigned i = 0; i < ds.numVaryings; ++i)
+    {
+        p0.varyings[i] = mix(a.varyings[i], b.varyings[i], interp0);
+        p1.varyings[i] = mix(b.varyings[i], a.varyings[i], interp1);
+    }
+    render_line(rs, ds, p0, p1, frags);
+}
+
+/* SL_LineProcessor::process_verts (SL_LineProcessor.cpp:172-279), one thread */
+static void process_lines(const RasterState& rs, const DrawState& ds, const Ibo* ibo, const slg_mesh& m, size_t instanceId, uint64_t& frags)
+{
+    const Shader& sh = *ds.shader;
+    for (size_t i = m.elementBegin; i < m.elementEnd; i += 2)
+    {
+        LineVert v0, v1;
+        for (unsigned k = 0; k < 4; ++k) v0.varyings[k] = v1.varyings[k] = mk(0.f, 0.f, 0.f, 0.f);
+        v0.vert = mat_mul(ds.scissor, run_vs(sh.vsProgram, ds.env, ibo ? read_index(*ibo, i) : i, instanceId, v0.varyings));
+        v1.vert = mat_mul(ds.scissor, run_vs(sh.vsProgram, ds.env, ibo ? read_index(*ibo, i + 1) : i + 1, instanceId, v1.varyings));
+        if (v0.vert[3] < 0.f || v1.vert[3] < 0.f) continue;
+        /* sl_ndc_clip_status of two vertices (SL_PostVertexTransform.hpp:560-585) */
+        const V4& c0 = v0.vert;
+        const V4& c1 = v1.vert;
+        const float w0 = c0[3], w1 = c1[3];
+        const bool inside = (c0[0] <= w0 && c0[1] <= w0 && c0[2] <= w0 && c0[3] <= w0) &&
+                            (c1[0] <= w1 && c1[1] <= w1 && c1[2] <= w1 && c1[3] <= w1) &&
+                            (c0[0] >= -w0 && c0[1] >= -w0 && c0[2] >= -w0 && c0[3] >= -w0) &&
+                            (c1[0] >= -w1 && c1[1] >= -w1 && c1[2] >= -w1 && c1[3] >= -w1);
+        const int status = (inside ? 3 : 0) | ((w0 > 0.f || w1 > 0.f) ? 1 : 0);
+        if (status == 0) continue;
+        perspective_divide(v0.vert);
+        perspective_divide(v1.vert);
+        ndc_to_screen(v0.vert, ds.viewport);
+        ndc_to_screen(v1.vert, ds.viewport);
+        if (status == 3) render_line(rs, ds, v0, v1, frags);
+        else clip_and_render_line(rs, ds, v0, v1, frags);
+    }
+}
+
 static void order_bins(std::vector<Bin>& bins, bool blending)
 {
     if (!blending)
@@ -1260,6 +1455,7 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
     rs.ctx = ctx;
     rs.depth = reinterpret_cast<float*>(depthTex.bytes.data());
     rs.width = depthTex.w;
+    rs.height = depthTex.h;
     rs.numOutputs = fbo.numColors;
     for (unsigned i = 0; i < fbo.numColors; ++i)
     {
@@ -1392,6 +1588,20 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
             continue;
         }
 
+        if (!group.empty() && (group[0].mesh.mode == SLG_RENDER_MODE_LINES || group[0].mesh.mode == SLG_RENDER_MODE_INDEXED_LINES))
+        {
+            for (const Unit& u : units)
+            {
+                const DrawItem& it = group[u.draw];
+                const Vao& vao = ctx->vaos[it.mesh.vaoId];
+                const bool indexed = (it.mesh.mode == SLG_RENDER_MODE_INDEXED_LINES);
+                const Ibo* ibo = (indexed && vao.ibo != SLG_INVALID_ID) ? &ctx->ibos[vao.ibo] : nullptr;
+                if (indexed && !ibo) return ctx->fail(SLG_ERR_INVALID_ARG, "indexed draw without index buffer");
+                process_lines(rs, states[u.draw], ibo, it.mesh, u.instance, totalFrags);
+            }
+            continue;
+        }
+
         std::vector<Bin> bins;
 
         for (const Unit& u : units)
@@ -1455,7 +1665,8 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
 static bool valid_tri_mesh(const slg_mesh* m)
 {
     return m && (m->mode == SLG_RENDER_MODE_TRIANGLES || m->mode == SLG_RENDER_MODE_INDEXED_TRIANGLES ||
-                 m->mode == SLG_RENDER_MODE_POINTS || m->mode == SLG_RENDER_MODE_INDEXED_POINTS);
+                 m->mode == SLG_RENDER_MODE_POINTS || m->mode == SLG_RENDER_MODE_INDEXED_POINTS ||
+                 m->mode == SLG_RENDER_MODE_LINES || m->mode == SLG_RENDER_MODE_INDEXED_LINES);
 }
 
 int slo_draw(slo_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId)
@@ -1465,7 +1676,7 @@ int slo_draw(slo_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId)
 
 int slo_draw_instanced(slo_context* ctx, const slg_mesh* m, size_t numInstances, size_t shaderId, size_t fboId)
 {
-    if (!valid_tri_mesh(m)) return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle and point render modes are supported");
+    if (!valid_tri_mesh(m)) return ctx->fail(SLG_ERR_INVALID_ARG, "only point, line and triangle render modes are supported");
     std::vector<std::vector<DrawItem>> groups(1);
     groups[0].push_back({*m, numInstances, shaderId, false});
     return run_draws(ctx, groups, fboId);
@@ -1477,7 +1688,7 @@ int slo_draw_multiple(slo_context* ctx, const slg_mesh* meshes, size_t numMeshes
     std::vector<std::vector<DrawItem>> groups(1);
     for (size_t i = 0; i < numMeshes; ++i)
     {
-        if (!valid_tri_mesh(&meshes[i])) return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle and point render modes are supported");
+        if (!valid_tri_mesh(&meshes[i])) return ctx->fail(SLG_ERR_INVALID_ARG, "only point, line and triangle render modes are supported");
         groups[0].push_back({meshes[i], 1, shaderId, true});
     }
     return run_draws(ctx, groups, fboId);
@@ -1488,7 +1699,7 @@ int slo_draw_batch(slo_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, s
     std::vector<std::vector<DrawItem>> groups;
     for (size_t i = 0; i < numCmds; ++i)
     {
-        if (!valid_tri_mesh(&cmds[i].mesh)) return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle and point render modes are supported");
+        if (!valid_tri_mesh(&cmds[i].mesh)) return ctx->fail(SLG_ERR_INVALID_ARG, "only point, line and triangle render modes are supported");
         groups.push_back({{cmds[i].mesh, cmds[i].numInstances, cmds[i].shaderId, false}});
     }
     return run_draws(ctx, groups, fboId);

@@ -86,6 +86,7 @@ bool valid_program(uint32_t p) { return p >= SLG_PROGRAM_LAMBERT_TEX && p <= SLG
 
 constexpr size_t kDescRing = 4096;
 constexpr uint64_t kMaxSlots = (1ull << 29) - 1; /* keys are slot << 3 | sub in 32 bits */
+constexpr int kMaxLineExtent = 10922;            /* 3 * 10922 < 32768 */
 
 } // namespace
 
@@ -379,6 +380,26 @@ bool texture_ok(const slg_context* ctx, uint32_t id, int type)
     return id < ctx->textures.size() && ctx->textures[id].buf.ptr && ctx->textures[id].type == type;
 }
 
+/* Vertices per primitive of the supported render modes (0 = unsupported). */
+uint64_t render_mode_vertices(int mode)
+{
+    switch (mode)
+    {
+        case SLG_RENDER_MODE_POINTS:
+        case SLG_RENDER_MODE_INDEXED_POINTS:    return 1;
+        case SLG_RENDER_MODE_LINES:
+        case SLG_RENDER_MODE_INDEXED_LINES:     return 2;
+        case SLG_RENDER_MODE_TRIANGLES:
+        case SLG_RENDER_MODE_INDEXED_TRIANGLES: return 3;
+        default:                                return 0;
+    }
+}
+
+bool render_mode_indexed(int mode)
+{
+    return mode == SLG_RENDER_MODE_INDEXED_POINTS || mode == SLG_RENDER_MODE_INDEXED_LINES || mode == SLG_RENDER_MODE_INDEXED_TRIANGLES;
+}
+
 /* Host-side bounds checks of everything a draw's kernels will read: the
  * vertex range, the index range and the resource ids stored in the uniform
  * block. The reference performs none (SL_Context::draw, SL_Context.cpp:714);
@@ -388,13 +409,15 @@ int validate_draw(slg_context* ctx, const Shader& sh, const Vao& vao, const slg_
     const Vbo& vbo = ctx->vbos[vao.vbo];
     const Binding& b0 = vao.bindings[0];
     if (b0.offset < 0 || b0.stride <= 0) return ctx->fail(SLG_ERR_INVALID_ARG, "binding 0 needs offset >= 0 and stride > 0");
-    const bool points = (m.mode == SLG_RENDER_MODE_POINTS || m.mode == SLG_RENDER_MODE_INDEXED_POINTS);
-    const uint64_t lastElement = points ? m.elementBegin + numElements - 1 : m.elementBegin + 3 * ((numElements + 2) / 3) - 1;
+    /* the reference reads whole primitives: a partial last line or triangle
+     * reads the elements after elementEnd */
+    const uint64_t perPrim = render_mode_vertices(m.mode);
+    const uint64_t lastElement = m.elementBegin + perPrim * ((numElements + perPrim - 1) / perPrim) - 1;
     uint64_t maxVertex;
-    if (m.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES || m.mode == SLG_RENDER_MODE_INDEXED_POINTS)
+    if (render_mode_indexed(m.mode))
     {
         const Ibo& ibo = ctx->ibos[vao.ibo];
-        if (m.elementEnd > ibo.count) return ctx->fail(SLG_ERR_INVALID_ARG, "element range exceeds the index buffer");
+        if (lastElement >= ibo.count) return ctx->fail(SLG_ERR_INVALID_ARG, "element range exceeds the index buffer");
         maxVertex = ibo.maxIndex;
     }
     else
@@ -452,13 +475,13 @@ int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, Draw
     const slg_mesh& m = req.mesh;
     if (req.shaderId >= ctx->shaders.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid shader id");
     if (m.vaoId >= ctx->vaos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid vao id");
-    const bool points = (m.mode == SLG_RENDER_MODE_POINTS || m.mode == SLG_RENDER_MODE_INDEXED_POINTS);
-    if (m.mode != SLG_RENDER_MODE_TRIANGLES && m.mode != SLG_RENDER_MODE_INDEXED_TRIANGLES && !points)
-        return ctx->fail(SLG_ERR_INVALID_ARG, "only triangle and point render modes are supported");
+    const uint64_t perPrim = render_mode_vertices(m.mode);
+    if (perPrim == 0)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "only point, line and triangle render modes are supported");
     const Shader& sh = ctx->shaders[req.shaderId];
     const Vao& vao = ctx->vaos[m.vaoId];
     if (vao.vbo == SLG_INVALID_ID || !ctx->vbos[vao.vbo].buf.ptr) return ctx->fail(SLG_ERR_INVALID_ARG, "vao has no vertex buffer");
-    const bool indexed = (m.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES || m.mode == SLG_RENDER_MODE_INDEXED_POINTS);
+    const bool indexed = render_mode_indexed(m.mode);
     if (indexed && (vao.ibo == SLG_INVALID_ID || !ctx->ibos[vao.ibo].buf.ptr))
         return ctx->fail(SLG_ERR_INVALID_ARG, "indexed draw without index buffer");
 
@@ -477,8 +500,8 @@ int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, Draw
     d.b0Stride = vao.bindings[0].stride;
     d.elementBegin = m.elementBegin;
     d.numElements = (m.elementEnd > m.elementBegin) ? (m.elementEnd - m.elementBegin) : 0;
-    d.numTris = points ? d.numElements : (d.numElements + 2) / 3;
-    d.prim = points ? slg::kPrimPoint : slg::kPrimTriangle;
+    d.numTris = (d.numElements + perPrim - 1) / perPrim;
+    d.prim = (perPrim == 1) ? slg::kPrimPoint : (perPrim == 2) ? slg::kPrimLine : slg::kPrimTriangle;
     d.numInstances = std::max<size_t>(1, req.numInstances);
     d.slotBase = slotBase;
     d.primBase = req.primBase;
@@ -638,6 +661,14 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
         {
             f.orderFree = 0;
         }
+    }
+    for (size_t i = 0; i < n; ++i)
+    {
+        /* the reference's Bresenham error term is int16: it stays exact while
+         * 3 * dx fits, dx <= max(W, H) */
+        if (descs[i].prim == slg::kPrimLine && std::max(f.width, f.height) > kMaxLineExtent)
+            return ctx->fail(SLG_ERR_INVALID_ARG, "line draws need a framebuffer of at most 10922 x 10922");
+        if (descs[i].prim == slg::kPrimLine) f.hasLines = 1;
     }
     f.tables.textures = static_cast<const TexView*>(ctx->texTable.ptr);
     f.tables.buffers = static_cast<const uint8_t* const*>(ctx->bufTable.ptr);
@@ -1323,6 +1354,12 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
         return ctx->fail(SLG_ERR_INVALID_ARG, "slg_draw_noalloc: a " + std::to_string(f.width) + "x" + std::to_string(f.height) +
                                                   " framebuffer is " + std::to_string(numTiles) + " tiles of " + std::to_string(f.tileW) + "x" +
                                                   std::to_string(f.tileH) + ", over the static limit of " + std::to_string(kNoAllocTiles));
+    if (desc->prim == slg::kPrimLine)
+    {
+        if (std::max(f.width, f.height) > kMaxLineExtent)
+            return ctx->fail(SLG_ERR_INVALID_ARG, "line draws need a framebuffer of at most 10922 x 10922");
+        f.hasLines = 1;
+    }
 
     /* resource tables: the context's when they are current, else a copy of
      * them into the static scratch */

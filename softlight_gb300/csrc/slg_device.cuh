@@ -85,11 +85,14 @@ struct DrawDesc
 enum PrimKind
 {
     kPrimTriangle = 0,
-    kPrimPoint = 1
+    kPrimPoint = 1,
+    kPrimLine = 2
 };
 
-/* record r7.w: depth test | depth mask << 4 | this bit for a point record */
+/* record r7.w: depth test | depth mask << 4 | one of these bits for a point
+ * or a line record (none for a triangle) */
 constexpr uint32_t kRecordPoint = 1u << 5;
+constexpr uint32_t kRecordLine = 1u << 6;
 
 /* Per-launch scratch and framebuffer description. */
 struct Frame
@@ -133,6 +136,10 @@ struct Frame
 
     /* threads per block of the vertex stage (64, 128 or 256): triangles per CTA */
     int32_t vsBlock;
+
+    /* some draw of the launch is a line draw: the vertex stage variant with
+     * the line set-up runs (kept apart from the triangle variant's registers) */
+    int32_t hasLines;
 
     /* optional visibility map (order-free raster only): per pixel written,
      * 1 + the launch slot (triangle) of the winning fragment; null: off */

@@ -468,6 +468,297 @@ __device__ __forceinline__ uint32_t setup_point(const Frame& f, const DrawDesc& 
     return 1;
 }
 
+/*-----------------------------------------------------------------------------
+ * Lines (SL_LineProcessor, softlight/src/SL_LineProcessor.cpp:51-279;
+ * SL_LineRasterizer, softlight/src/SL_LineRasterizer.cpp:26-96). A line record:
+ *   r0, r1 = screen positions of the two ends (x, y, z, w)
+ *   r2     = (1 / |end1 - end0|, 0, 0, 0)
+ *   r3     = Bresenham walk as int32 bits: (x1, x2, y1, steep | (yErr < 0) << 1)
+ *   r4     = (dx, dErr, wraps, 0) as int32 bits
+ *   r6     = pixel bounds, r7 = (draw, primIndex lo, hi, flags | kRecordLine)
+-----------------------------------------------------------------------------*/
+constexpr float kLineEpsilon = 1.0e-6f;   /* LS_EPSILON */
+
+__device__ __forceinline__ float mixf(float a, float b, float t) { return (b - a) * t + a; }
+
+/* _clip_segment of SL_LineProcessor::clip_and_process_lines (SL_LineProcessor.cpp:94-126) */
+__device__ __forceinline__ bool clip_segment(float num, float denom, float& tE, float& tL)
+{
+    if (fabsf(denom) < kLineEpsilon) return num < 0.f;
+    const float t = num / denom;
+    if (denom > 0.f)
+    {
+        if (t > tL) return false;
+        if (t > tE) tE = t;
+    }
+    else
+    {
+        if (t < tE) return false;
+        if (t < tL) tL = t;
+    }
+    return true;
+}
+
+/* Screen-space clip of a partially visible line against the viewport
+ * (SL_LineProcessor.cpp:63-166); false when nothing is left. */
+__device__ __forceinline__ bool clip_line(const float* vp, float4& p0, float4& p1, slg_v4* va, slg_v4* vb, int nv)
+{
+    const float4 a = p0, b = p1;
+    const float dx = b.x - a.x, dy = b.y - a.y;
+    const float xMin = vp[0], yMin = vp[1], xMax = vp[2], yMax = vp[3];
+    if (fabsf(dx) < kLineEpsilon && fabsf(dy) < kLineEpsilon)
+    {
+        if (a.x >= xMin && a.x <= xMax && a.y >= yMin && a.y <= yMax) return true;
+    }
+    const float ex = a.x - b.x, ey = a.y - b.y;
+    const float dist = 1.f / sqrtf(ex * ex + ey * ey);
+    float tE = 0.f, tL = 1.f;
+    if (!(clip_segment(xMin - a.x, dx, tE, tL) && clip_segment(a.x - xMax, -dx, tE, tL) &&
+          clip_segment(yMin - a.y, dy, tE, tL) && clip_segment(a.y - yMax, -dy, tE, tL)))
+    {
+        return false;
+    }
+    if (tL < 1.f)
+    {
+        p1.x = a.x + tL * dx;
+        p1.y = a.y + tL * dy;
+    }
+    if (tE > 0.f)
+    {
+        p0.x = a.x + tE * dx;
+        p0.y = a.y + tE * dy;
+    }
+    const float l0x = p0.x - a.x, l0y = p0.y - a.y, l1x = p1.x - b.x, l1y = p1.y - b.y;
+    const float interp0 = sqrtf(((l0x * l0x + l0y * l0y) + 0.f) + 0.f) * dist;
+    const float interp1 = sqrtf(((l1x * l1x + l1y * l1y) + 0.f) + 0.f) * dist;
+    p0.z = mixf(a.z, b.z, interp0);
+    p0.w = mixf(a.w, b.w, interp0);
+    p1.z = mixf(b.z, a.z, interp1);
+    p1.w = mixf(b.w, a.w, interp1);
+#pragma unroll
+    for (int vi = 0; vi < kMaxVaryings; ++vi)
+    {
+        if (vi < nv)
+        {
+            const slg_v4 u = va[vi], v = vb[vi];
+            va[vi] = slg_make_v4(mixf(u.x, v.x, interp0), mixf(u.y, v.y, interp0), mixf(u.z, v.z, interp0), mixf(u.w, v.w, interp0));
+            vb[vi] = slg_make_v4(mixf(v.x, u.x, interp1), mixf(v.y, u.y, interp1), mixf(v.z, u.z, interp1), mixf(v.w, u.w, interp1));
+        }
+    }
+    return true;
+}
+
+/* float screen coordinate -> the int16 the Bresenham walk takes ((uint16_t) cast, then sl_lowp_t) */
+__device__ __forceinline__ int lowp(float v) { return (int)(int16_t)(uint16_t)((uint32_t)f2i(v) & 0xFFFFu); }
+
+/* SL_LineProcessor::process_verts for one segment (SL_LineProcessor.cpp:172-279). */
+__device__ __forceinline__ uint32_t setup_line(const Frame& f, const DrawDesc& d, int di, uint64_t slot, uint64_t local,
+                                               TileRange& tr, bool& counted)
+{
+    const uint64_t inst = local / d.numTris;
+    const uint64_t i = d.elementBegin + 2u * (local - inst * d.numTris);
+    const DevEnv env = make_env(d, f.tables);
+    slg_v4 va[kMaxVaryings], vb[kMaxVaryings];
+    const uint64_t vid0 = (d.indexType >= 0) ? read_index(d, i) : i;
+    const uint64_t vid1 = (d.indexType >= 0) ? read_index(d, i + 1) : (i + 1);
+    const float4 c0 = mat_mul(f.scissor, to_f4(run_vertex_program(d.vsProgram, env, vid0, inst, va)));
+    const float4 c1 = mat_mul(f.scissor, to_f4(run_vertex_program(d.vsProgram, env, vid1, inst, vb)));
+    if (c0.w < 0.f || c1.w < 0.f)
+    {
+        return 0;
+    }
+    /* sl_ndc_clip_status of two vertices (SL_PostVertexTransform.hpp:560-585) */
+    const float w0 = c0.w, w1 = c1.w;
+    const bool inside = (c0.x <= w0 && c0.y <= w0 && c0.z <= w0 && c0.w <= w0) && (c1.x <= w1 && c1.y <= w1 && c1.z <= w1 && c1.w <= w1) &&
+                        (c0.x >= -w0 && c0.y >= -w0 && c0.z >= -w0 && c0.w >= -w0) && (c1.x >= -w1 && c1.y >= -w1 && c1.z >= -w1 && c1.w >= -w1);
+    const int status = (inside ? 3 : 0) | ((w0 > 0.f || w1 > 0.f) ? 1 : 0);
+    if (status == 0)
+    {
+        return 0;
+    }
+    float4 s0 = to_screen(c0, f.viewport), s1 = to_screen(c1, f.viewport);
+    uint64_t primIndex = i;
+    if (status == 1)
+    {
+        if (!clip_line(f.viewport, s0, s1, va, vb, d.numVaryings)) return 0;
+        primIndex = i * inst + i;
+    }
+
+    /* sl_draw_line_bresenham set-up (softlight/include/softlight/SL_Geometry.hpp:314-333) */
+    int x1 = lowp(s0.x), y1 = lowp(s0.y), x2 = lowp(s1.x), y2 = lowp(s1.y);
+    const int minX = min(x1, x2), maxX = max(x1, x2), minY = min(y1, y2), maxY = max(y1, y2);
+    const bool steep = abs(x1 - x2) < abs(y1 - y2);
+    if (steep)
+    {
+        int t = x1; x1 = y1; y1 = t;
+        t = x2; x2 = y2; y2 = t;
+    }
+    if (x1 > x2)
+    {
+        int t = x1; x1 = x2; x2 = t;
+        t = y1; y1 = y2; y2 = t;
+    }
+    const int dxl = (int)(int16_t)(x2 - x1);
+    const int dErr = (int)(int16_t)(abs((int)(int16_t)(y2 - y1)) * 2);
+    const int yNeg = (y2 > y1) ? 0 : 1;
+    const bool wraps = maxX >= f.width;   /* pixels at x = W land on the next row */
+
+    Record rec;
+    const float ex = s1.x - s0.x, ey = s1.y - s0.y;
+    rec.r[0] = s0;
+    rec.r[1] = s1;
+    rec.r[2] = make_float4(1.f / sqrtf(ex * ex + ey * ey), 0.f, 0.f, 0.f);
+    rec.r[3] = make_float4(__int_as_float(x1), __int_as_float(x2), __int_as_float(y1), __int_as_float((steep ? 1 : 0) | (yNeg << 1)));
+    rec.r[4] = make_float4(__int_as_float(dxl), __int_as_float(dErr), __int_as_float(wraps ? 1 : 0), 0.f);
+    rec.r[5] = make_float4(0.f, 0.f, 0.f, 0.f);
+    rec.r[6] = wraps ? make_float4(__int_as_float(minY), __int_as_float(maxY + 2), __int_as_float(0), __int_as_float(f.width - 1))
+                     : make_float4(__int_as_float(minY), __int_as_float(maxY + 1), __int_as_float(minX), __int_as_float(maxX));
+    rec.r[7] = make_float4(__uint_as_float((uint32_t)di), __uint_as_float((uint32_t)primIndex), __uint_as_float((uint32_t)(primIndex >> 32)),
+                           __uint_as_float((uint32_t)d.depthTest | ((uint32_t)d.depthMask << 4) | kRecordLine));
+    store_record(f, slot, rec);
+    float4* dst = f.varyings + slot * kVaryingVec4;
+#pragma unroll
+    for (int vi = 0; vi < kMaxVaryings; ++vi)
+    {
+        if (vi < d.numVaryings)
+        {
+            dst[vi] = to_f4(va[vi]);
+            dst[4 + vi] = to_f4(vb[vi]);
+        }
+    }
+    tr = tile_range(rec.r[6], f);
+    counted = true;
+    return 1;
+}
+
+/* The Bresenham walk of a line record. */
+struct LineWalk
+{
+    int x1, x2, y1, dx, dErr, yErr;
+    bool steep, wraps;
+};
+
+__device__ __forceinline__ LineWalk line_walk(const float4* R)
+{
+    LineWalk w;
+    const float4 r3 = R[3], r4 = R[4];
+    w.x1 = __float_as_int(r3.x);
+    w.x2 = __float_as_int(r3.y);
+    w.y1 = __float_as_int(r3.z);
+    const int fl = __float_as_int(r3.w);
+    w.steep = (fl & 1) != 0;
+    w.yErr = (fl & 2) ? -1 : 1;
+    w.dx = __float_as_int(r4.x);
+    w.dErr = __float_as_int(r4.y);
+    w.wraps = __float_as_int(r4.z) != 0;
+    return w;
+}
+
+/* Pixel k (0..dx) of sl_draw_line_bresenham (SL_Geometry.hpp:335-363): the
+ * error term stays in (-dx, dx], so before pixel k the minor coordinate has
+ * moved ceil((k dErr - dx) / (2 dx)) steps. Returns the 16-bit (x, y) the
+ * callback receives. */
+__device__ __forceinline__ void line_pixel(const LineWalk& w, int k, uint32_t& X, uint32_t& Y)
+{
+    const int a = k * w.dErr - w.dx;
+    const int m = (a <= 0) ? 0 : (a + 2 * w.dx - 1) / (2 * w.dx);
+    const int p = (int)(int16_t)(w.x1 + k), q = (int)(int16_t)(w.y1 + w.yErr * m);
+    X = (uint32_t)(w.steep ? q : p) & 0xFFFFu;
+    Y = (uint32_t)(w.steep ? p : q) & 0xFFFFu;
+}
+
+/* Walk steps whose pixel can land in row y of the columns [x0, xLimit):
+ * [kLo, kHi] with callback row y, plus kWrap (or -1), the step whose pixel
+ * has x = W on row y - 1 and so is stored at (0, y). Inverting the closed
+ * form above: minor step m is taken by the steps k with
+ * 2 dx m - dx < k dErr <= 2 dx m + dx. */
+struct LineRow { int kLo, kHi, kWrap; };
+
+__device__ __forceinline__ LineRow line_row(const LineWalk& w, int y, int x0, int xLimit, int width)
+{
+    LineRow lr;
+    lr.kLo = 0;
+    lr.kHi = -1;
+    lr.kWrap = -1;
+    if (w.steep)
+    {
+        lr.kLo = lr.kHi = y - w.x1;
+        if (w.wraps && x0 == 0) lr.kWrap = y - 1 - w.x1;
+    }
+    else
+    {
+        const int m = (y - w.y1) * w.yErr;
+        if (m >= 0)
+        {
+            if (w.dErr == 0)
+            {
+                if (m == 0) lr.kHi = w.dx;
+            }
+            else
+            {
+                lr.kLo = (m == 0) ? 0 : (2 * w.dx * m - w.dx) / w.dErr + 1;
+                lr.kHi = (2 * w.dx * m + w.dx) / w.dErr;
+            }
+        }
+        lr.kLo = max(lr.kLo, x0 - w.x1);
+        lr.kHi = min(lr.kHi, min(xLimit, width) - 1 - w.x1);
+        if (w.wraps && x0 == 0) lr.kWrap = w.dx;
+    }
+    lr.kLo = max(lr.kLo, 0);
+    lr.kHi = min(lr.kHi, w.dx);
+    if (lr.kWrap > w.dx) lr.kWrap = -1;
+    return lr;
+}
+
+/* Stored pixel of walk step k: SoftLight addresses the buffers with
+ * x + W * y of the 16-bit callback coordinates, so x = W lands on the next
+ * row; steps past the end of the buffer are dropped (false). */
+__device__ __forceinline__ bool line_store_pixel(const LineWalk& w, int k, int width, int height, uint32_t& X, uint32_t& Y,
+                                                 int& px, int& py)
+{
+    line_pixel(w, k, X, Y);
+    const uint32_t lin = X + (uint32_t)width * Y;
+    if (lin >= (uint32_t)width * (uint32_t)height) return false;
+    py = (int)(lin / (uint32_t)width);
+    px = (int)(lin - (uint32_t)py * (uint32_t)width);
+    return true;
+}
+
+/* SL_LineRasterizer's fragment shading (SL_FragmentProcessor.cpp:346-402,
+ * interpolate_line_varyings :120-140): varyings mix(v0, v1, interp). */
+__device__ __forceinline__ bool shade_line(const Frame& f, const DrawDesc& dd, uint64_t rec, float interp, float4& out)
+{
+    slg_v4 vary[kMaxVaryings];
+    const float4* V = f.varyings + rec * kVaryingVec4;
+#pragma unroll
+    for (int vi = 0; vi < kMaxVaryings; ++vi)
+    {
+        if (vi < dd.numVaryings)
+        {
+            const float4 a = V[vi], b = V[4 + vi];
+            vary[vi] = slg_make_v4(mixf(a.x, b.x, interp), mixf(a.y, b.y, interp), mixf(a.z, b.z, interp), mixf(a.w, b.w, interp));
+        }
+        else
+        {
+            vary[vi] = slg_make_v4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+    slg_v4 outputs[4];
+    const DevEnv env = make_env(dd, f.tables);
+    const bool have = run_fragment_program(dd.fsProgram, env, vary, outputs);
+    out = to_f4(outputs[0]);
+    return have && dd.numOutputs > 0;
+}
+
+/* SL_LineRasterizer::render_line per pixel (SL_LineRasterizer.cpp:49-58):
+ * interp = |p - end0| / |end1 - end0|, z = mix(z0, z1, interp). */
+__device__ __forceinline__ float line_interp(const float4* R, uint32_t X, uint32_t Y)
+{
+    const float ex = (float)X - R[0].x, ey = (float)Y - R[0].y;
+    return sqrtf(((ex * ex + ey * ey) + 0.f) + 0.f) * R[2].x;
+}
+
+template <bool kLines>
 __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, TileRange& tr, bool& counted)
 {
     const int di = (f.numDraws > 1) ? find_draw(f, slot) : 0;
@@ -476,6 +767,10 @@ __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, Ti
     if (d.prim == kPrimPoint)
     {
         return setup_point(f, d, di, slot, local, tr, counted);
+    }
+    if (kLines && d.prim == kPrimLine)
+    {
+        return setup_line(f, d, di, slot, local, tr, counted);
     }
     const uint64_t inst = local / d.numTris;
     const uint64_t tri = local - inst * d.numTris;
@@ -581,6 +876,7 @@ __global__ void __launch_bounds__(128) clip_kernel(const Frame f)
     }
 }
 
+template <bool kLines>
 __global__ void __launch_bounds__(256) vs_setup_kernel(const Frame f)
 {
     const uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -589,7 +885,7 @@ __global__ void __launch_bounds__(256) vs_setup_kernel(const Frame f)
     bool counted = false;
     if (slot < f.numSlots)
     {
-        f.slotInfo[slot] = setup_slot(f, slot, tr, counted);
+        f.slotInfo[slot] = setup_slot<kLines>(f, slot, tr, counted);
     }
     /* per-tile counts of the unclipped records, one atomic per group of
      * lanes touching the same tile (clipped records count themselves) */
@@ -1116,6 +1412,47 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 return;
             }
             const uint32_t flags = __float_as_uint(R[7].w);
+            if (flags & kRecordLine)
+            {
+                /* the walk steps of this row whose pixels this thread owns:
+                 * one step on a steep line, every fourth on a flat one */
+                const LineWalk w = line_walk(R);
+                const LineRow lr = line_row(w, y, x0, xLimit, f.width);
+                const DrawDesc& dd = f.draws[__float_as_uint(R[7].x)];
+                const uint64_t rec = key_to_record(f, sRecKey[ri]);
+                const int step = w.steep ? 1 : 4;
+                const int kStart = w.steep ? lr.kLo : lr.kLo + ((myX0 - w.x1 - lr.kLo) & 3);
+                const int nRow = (lr.kHi >= kStart) ? (lr.kHi - kStart) / step + 1 : 0;
+                const int nAll = nRow + (lr.kWrap >= 0 ? 1 : 0);
+                for (int j = 0; j < nAll; ++j)
+                {
+                    const int k = (j < nRow) ? kStart + j * step : lr.kWrap;
+                    uint32_t X, Y;
+                    int px, py;
+                    if (!line_store_pixel(w, k, f.width, f.height, X, Y, px, py) || py != y || px < myX0 || px >= xLimit ||
+                        ((px - myX0) & 3) != 0)
+                    {
+                        continue;
+                    }
+                    const float interp = line_interp(R, X, Y);
+                    const float z = mixf(R[0].z, R[1].z, interp);
+                    const int idx = r * L::kStride + (px - x0);
+                    if (depth_cmp(flags & 0xF, z, sDepth[idx]))
+                    {
+                        float4 o;
+                        if (shade_line(f, dd, rec, interp, o) && f.color)
+                        {
+                            sColor[idx] = (dd.blend != SLG_BLEND_OFF) ? Color::store(blend_color(dd.blend, o, Color::load(sColor[idx])))
+                                                                      : Color::store(o);
+                        }
+                        if ((flags >> 4) & 1)
+                        {
+                            sDepth[idx] = z;
+                        }
+                    }
+                }
+                return;
+            }
             if (flags & kRecordPoint)
             {
                 const int px = __float_as_int(r6.z);
@@ -1258,7 +1595,8 @@ __device__ __forceinline__ unsigned long long free_pack(int func, bool mask, flo
  * sBest stores (b0, b1, b2, z). */
 template <int TW, int TH, bool kStore>
 __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sKey, const uint32_t* sPre, int cnt, int x0, int y0,
-                                          int xLimit, int func, bool mask, const float* sD0, unsigned long long* sBest, float4* sB)
+                                          int xLimit, int width, int height, int func, bool mask, const float* sD0,
+                                          unsigned long long* sBest, float4* sB)
 {
     const uint32_t total = sPre[cnt];
     for (uint32_t i = threadIdx.x; i < total; i += kFreeThreads)
@@ -1272,6 +1610,40 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
         }
         const float4* R = sRec + lo * kRecordVec4;
         const int y = max(__float_as_int(R[6].x), y0) + (int)(i - sPre[lo]);
+        if (__float_as_uint(R[7].w) & kRecordLine)
+        {
+            /* the walk steps of this row; sB keeps (interp, 0, 0, z) */
+            const LineWalk w = line_walk(R);
+            const LineRow lr = line_row(w, y, x0, xLimit, width);
+            const uint32_t key = sKey[lo];
+            for (int k = lr.kLo; k <= lr.kHi + 1; ++k)
+            {
+                const int kk = (k <= lr.kHi) ? k : lr.kWrap;
+                uint32_t X, Y;
+                int px, py;
+                if (kk < 0 || !line_store_pixel(w, kk, width, height, X, Y, px, py) || py != y || px < x0 || px >= xLimit)
+                {
+                    continue;
+                }
+                const float interp = line_interp(R, X, Y);
+                const float z = mixf(R[0].z, R[1].z, interp);
+                const int idx = (y - y0) * TW + (px - x0);
+                if (!depth_cmp(func, z, sD0[idx]))
+                {
+                    continue;
+                }
+                const unsigned long long p = free_pack(func, mask, z, key);
+                if (kStore)
+                {
+                    if (sBest[idx] == p) sB[idx] = make_float4(interp, 0.f, 0.f, z);
+                }
+                else
+                {
+                    atomicMin(sBest + idx, p);
+                }
+            }
+            continue;
+        }
         if (__float_as_uint(R[7].w) & kRecordPoint)
         {
             const int px = __float_as_int(R[6].z);
@@ -1394,9 +1766,9 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
         if (threadIdx.x == 0) sPre[0] = 0u;
         __syncthreads();
 
-        free_walk<TW, TH, false>(sRec, sKey, sPre, cnt, x0, y0, xLimit, depthFunc, mask, sD0, sBest, sB);
+        free_walk<TW, TH, false>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB);
         __syncthreads();
-        free_walk<TW, TH, true>(sRec, sKey, sPre, cnt, x0, y0, xLimit, depthFunc, mask, sD0, sBest, sB);
+        free_walk<TW, TH, true>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB);
     }
     __syncthreads();
 
@@ -1419,8 +1791,11 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
         if (f.color && dd.numOutputs > 0)
         {
             float4 o;
-            const bool point = (__float_as_uint(R[7].w) & kRecordPoint) != 0;
-            if (point ? shade_point(f, dd, rec, o) : shade(f, dd, rec, R[2].w, R[5], b.x, b.y, b.z, o))
+            const uint32_t kind = __float_as_uint(R[7].w);
+            const bool have = (kind & kRecordPoint) ? shade_point(f, dd, rec, o)
+                              : (kind & kRecordLine) ? shade_line(f, dd, rec, b.x, o)
+                                                     : shade(f, dd, rec, R[2].w, R[5], b.x, b.y, b.z, o);
+            if (have)
             {
                 Color::write(f.color, gi, Color::store(o));
             }
@@ -1519,7 +1894,8 @@ cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEven
     if (f.numSlots > 0)
     {
         const unsigned blocks = (unsigned)((f.numSlots + vsBlock - 1) / vsBlock);
-        vs_setup_kernel<<<blocks, vsBlock, 0, s>>>(f);
+        if (f.hasLines) vs_setup_kernel<true><<<blocks, vsBlock, 0, s>>>(f);
+        else vs_setup_kernel<false><<<blocks, vsBlock, 0, s>>>(f);
         clip_kernel<<<152 * 4, 128, 0, s>>>(f);
     }
     if (ev) cudaEventRecord(ev[1], s);

@@ -134,6 +134,130 @@ def random_points(ctx, num_points=3000, width=64, height=48, seed=41, blend=A.BL
     return s
 
 
+def random_lines(ctx, num_lines=400, width=64, height=48, seed=61, blend=A.BLEND_OFF,
+                 depth_test=A.DEPTH_TEST_LESS_THAN, depth_mask=A.DEPTH_MASK_ON, indexed=None,
+                 color_type=A.COLOR_RGBA_8U, clear_depth=1.0, num_instances=1, persp=False, odd_end=False):
+    """Line draw (SL_RENDER_MODE_LINES): seeded segments in and around the
+    view volume, so that many are clipped to the viewport (and, with
+    `persp`, some cross the camera plane and are culled); vertex colour x
+    RGBA8 texture program with vertex alpha, the uv interpolated along the
+    line. `odd_end` ends the element range on an odd count: the last line
+    reads the vertex after elementEnd, as the reference's loop does."""
+    rng = np.random.default_rng(seed)
+    s = S.Scene(ctx, f"lines_{seed}", width, height, color_type=color_type)
+    n = 2 * num_lines
+    if persp:
+        pos = np.stack([rng.uniform(-3.0, 3.0, n), rng.uniform(-2.0, 2.0, n), rng.uniform(-2.5, 3.5, n)], 1)
+        mvp = S.perspective(60.0, width / height, 0.1, 10.0) @ S.translate((0.0, 0.0, -3.0))
+    else:
+        pos = np.stack([rng.uniform(-1.6, 1.6, n), rng.uniform(-1.6, 1.6, n), rng.uniform(-1.2, 1.2, n)], 1)
+        mvp = np.eye(4)
+    col = np.concatenate([rng.uniform(0.0, 1.0, (n, 3)), rng.uniform(0.2, 1.0, (n, 1))], 1)
+    uv = rng.uniform(-0.5, 1.5, (n, 2))
+    verts = np.concatenate([pos, col, uv], 1).astype(np.float32)
+    tex = s.add_texture_rgba8(S.to_rgba8(S.value_noise(32, 32, seed=seed, octaves=2, alpha=1.0)))
+    if indexed is None:
+        mesh = s.add_mesh(verts, None, stride=36)
+        mesh.mode = A.RENDER_MODE_LINES
+    else:
+        order = rng.permutation(n)
+        mesh = s.add_mesh(verts, order.astype(indexed), stride=36)
+        mesh.mode = A.RENDER_MODE_INDEXED_LINES
+    if odd_end:
+        mesh.elementEnd -= 1
+    sh = s.add_shader(A.PROGRAM_VCOLOR_TEX_ALPHA, 2, S.vcolor_uniforms(mvp, tex), cull=A.CULL_OFF,
+                      depth_test=depth_test, depth_mask=depth_mask, blend=blend)
+    s.draws.append((mesh, num_instances, sh))
+    s.num_triangles = num_lines
+    s.clear_depth = clear_depth
+    return s
+
+
+def line_edges(ctx, width=40, height=30):
+    """Lines at the edges of the reference's line path, identity transform,
+    flat colour, depth LESS: a full-width line (its x = W end lands on the
+    next row), a vertical line at x = W (every pixel lands one row down), the
+    diagonal whose last pixel (W, H) falls past the buffer, lines clipped at
+    one or both ends, lines wholly outside, zero-length lines inside and
+    outside, a line whose z leaves the volume (clipped with nothing to cut),
+    steep and shallow lines in all octants."""
+    s = S.Scene(ctx, "line_edges", width, height)
+    segs = [
+        ((-1.0, -0.2, 0.1), (1.0, -0.2, 0.1)),
+        ((1.0, -0.9, 0.2), (1.0, 0.9, 0.2)),
+        ((-1.0, -1.0, 0.0), (1.0, 1.0, 0.3)),
+        ((-2.0, 0.3, -0.5), (2.0, -0.4, 0.5)),
+        ((0.2, -3.0, 0.0), (-0.1, 0.5, 0.4)),
+        ((1.5, 1.5, 0.0), (2.0, 2.0, 0.0)),
+        ((0.1, 0.1, 0.0), (0.1, 0.1, 0.0)),
+        ((1.4, 0.1, 0.0), (1.4, 0.1, 0.0)),
+        ((-0.5, 0.6, -2.0), (0.5, 0.7, 0.5)),
+        ((-0.9, 0.9, -0.1), (-0.8, -0.95, 0.6)),
+        ((0.95, 0.2, 0.0), (-0.95, 0.25, -0.2)),
+        ((0.3, -0.8, 0.7), (0.35, 0.85, -0.7)),
+        ((-0.7, 0.4, 0.9), (0.6, 0.45, 0.9)),
+        ((0.0, 0.0, 0.5), (1.0, 0.0, -0.5)),
+    ]
+    verts = np.zeros((2 * len(segs), 9), np.float32)
+    for i, (a, b) in enumerate(segs):
+        verts[2 * i, :3] = a
+        verts[2 * i + 1, :3] = b
+    mesh = s.add_mesh(verts, None, stride=36)
+    mesh.mode = A.RENDER_MODE_LINES
+    sh = s.add_shader(A.PROGRAM_FLAT_COLOR, 0, S.flat_uniforms(np.eye(4), (0.25, 1.0, 0.5, 1.0)),
+                      cull=A.CULL_OFF, depth_test=A.DEPTH_TEST_LESS_THAN, depth_mask=A.DEPTH_MASK_ON)
+    s.draws.append((mesh, 1, sh))
+    return s
+
+
+def mixed_prims(ctx, width=160, height=120, batched=False, blend_lines=False, seed=81):
+    """Triangles, lines and points into one frame, issued draw by draw or as
+    one batch (one launch holding all three record kinds); opaque with one
+    depth rule (order-free raster), or with blended lines (ordered raster)."""
+    rng = np.random.default_rng(seed)
+    s = S.Scene(ctx, "mixed", width, height)
+    tex = s.add_texture_rgba8(S.to_rgba8(S.value_noise(32, 32, seed=seed, octaves=2, alpha=1.0)))
+    soup, proj = S.soup_triangles(300, width, height, seed=seed)
+    tris = s.add_mesh(soup, None, stride=36)
+    s.draws.append((tris, 1, s.add_shader(A.PROGRAM_VCOLOR_TEX_ALPHA, 2, S.vcolor_uniforms(proj, tex), cull=A.CULL_OFF)))
+    n = 1200
+    pos = np.stack([rng.uniform(-1.4, 1.4, n), rng.uniform(-1.4, 1.4, n), rng.uniform(-1.0, 1.0, n)], 1)
+    col = np.concatenate([rng.uniform(0.0, 1.0, (n, 3)), rng.uniform(0.2, 1.0, (n, 1))], 1)
+    verts = np.concatenate([pos, col, rng.uniform(-0.5, 1.5, (n, 2))], 1).astype(np.float32)
+    lines = s.add_mesh(verts, None, stride=36)
+    lines.mode = A.RENDER_MODE_LINES
+    blend = A.BLEND_ALPHA if blend_lines else A.BLEND_OFF
+    s.draws.append((lines, 1, s.add_shader(A.PROGRAM_VCOLOR_TEX_ALPHA, 2, S.vcolor_uniforms(np.eye(4), tex),
+                                           cull=A.CULL_OFF, blend=blend)))
+    points = s.add_mesh(verts[::-1].copy(), None, stride=36)
+    points.mode = A.RENDER_MODE_POINTS
+    s.draws.append((points, 1, s.add_shader(A.PROGRAM_VCOLOR_TEX_ALPHA, 2, S.vcolor_uniforms(np.eye(4), tex),
+                                            cull=A.CULL_OFF)))
+    s.batched = batched
+    return s
+
+
+LINE_ALIAS_PIXEL = (10, 0)   # (row, column) that both ends of line_alias's line address
+
+
+def line_alias(ctx, width=40, height=30):
+    """A full-width line whose last pixel (x = W, row 9) is stored at the
+    address of its first pixel (x = 0, row 10). SoftLight tests both against
+    the depth before the line (its 600-fragment queue is written after the
+    test) and writes them in walk order, so the later, farther fragment wins
+    there; the GPU path applies them in order. Depth LESS, z from 0.2 to 0.5."""
+    s = S.Scene(ctx, "line_alias", width, height)
+    verts = np.zeros((2, 9), np.float32)
+    verts[0, :3] = (-1.0, -0.32, 0.2)
+    verts[1, :3] = (1.0, -0.38, 0.5)
+    mesh = s.add_mesh(verts, None, stride=36)
+    mesh.mode = A.RENDER_MODE_LINES
+    sh = s.add_shader(A.PROGRAM_FLAT_COLOR, 0, S.flat_uniforms(np.eye(4), (1.0, 1.0, 1.0, 1.0)),
+                      cull=A.CULL_OFF, depth_test=A.DEPTH_TEST_LESS_THAN, depth_mask=A.DEPTH_MASK_ON)
+    s.draws.append((mesh, 1, sh))
+    return s
+
+
 def point_edges(ctx, width=40, height=30):
     """Points placed at the edges of the reference's point addressing: x = W
     lands on the next row's first pixel (linear index x + W*y), x = W on the

@@ -34,6 +34,24 @@ SCENES = {
                                                   color_type=A.COLOR_RGBA_FLOAT, seed=44)),
     "points_not_equal": (E.random_points, dict(depth_test=A.DEPTH_TEST_NOT_EQUAL, clear_depth=0.5, seed=45)),
     "point_edges": (E.point_edges, dict()),
+    "lines_less": (E.random_lines, dict()),
+    "lines_persp_clip_cull": (E.random_lines, dict(persp=True, seed=62, num_lines=1500, width=120, height=80)),
+    "lines_blend_alpha": (E.random_lines, dict(blend=A.BLEND_ALPHA, depth_mask=A.DEPTH_MASK_OFF, seed=63)),
+    "lines_u16_gequal_float": (E.random_lines, dict(indexed=np.uint16, depth_test=A.DEPTH_TEST_GREATER_EQUAL,
+                                                    clear_depth=-1.0, color_type=A.COLOR_RGBA_FLOAT, seed=64)),
+    "lines_instanced_odd_end": (E.random_lines, dict(num_instances=3, seed=65, odd_end=True)),
+    "lines_not_equal_700x40": (E.random_lines, dict(depth_test=A.DEPTH_TEST_NOT_EQUAL, clear_depth=0.5, seed=66,
+                                                    num_lines=3000, width=700, height=40)),
+    "line_edges": (E.line_edges, dict()),
+    "line_alias": (E.line_alias, dict()),
+}
+
+
+# Pixels (row, column) where the GPU path is known to differ from SoftLight,
+# with the reason: line_alias's last pixel shares its first pixel's address
+# and SoftLight tests both against the depth before the line.
+GPU_KNOWN_DIFFERENCES = {
+    "line_alias": [E.LINE_ALIAS_PIXEL],
 }
 
 

@@ -80,7 +80,8 @@ def test_oracle_threads_match_one_thread(oracle_mod, threads):
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_TREE), reason="reference tree not present")
-@pytest.mark.parametrize("name", ["c1_sphere_160x120", "c3_soup_2000_160x96", "multi_draw", "soup_not_equal"])
+@pytest.mark.parametrize("name", ["c1_sphere_160x120", "c3_soup_2000_160x96", "multi_draw", "soup_not_equal",
+                                  "lines_persp_clip_cull", "line_alias"])
 def test_reference_build_matches_oracle_live(oracle_mod, name):
     """Builds the reference sources (oracle/ref_build.py) and renders live."""
     import sys

@@ -247,3 +247,76 @@ def test_points_all_tiles(ctxs, tile):
     g.set_tile_size(*tile)
     sg, so = render_both(E.random_points, g, o, num_points=30000, width=300, height=200, seed=55)
     compare_scenes(sg, so, f"points {tile}")
+
+
+@pytest.mark.parametrize("kw", [
+    dict(num_lines=4000, width=320, height=240),
+    dict(num_lines=3000, width=256, height=192, persp=True, seed=72),
+    dict(num_lines=2000, width=256, height=192, blend=A.BLEND_ALPHA, depth_mask=A.DEPTH_MASK_OFF, seed=73),
+    dict(num_lines=1500, width=200, height=150, num_instances=3, odd_end=True, seed=74),
+    dict(num_lines=2000, width=200, height=150, depth_test=A.DEPTH_TEST_LESS_EQUAL, indexed=np.uint32, seed=75),
+    dict(num_lines=3000, width=1000, height=60, depth_test=A.DEPTH_TEST_NOT_EQUAL, clear_depth=0.5, seed=76),
+    dict(num_lines=2000, width=240, height=160, depth_test=A.DEPTH_TEST_GREATER_EQUAL, clear_depth=-1.0,
+         color_type=A.COLOR_RGBA_FLOAT, seed=77),
+], ids=["less_4k", "persp_clip_cull", "blend_alpha", "instanced_odd_end", "lequal_indexed", "not_equal_1000x60",
+        "gequal_float"])
+def test_lines(ctxs, kw):
+    """SL_RENDER_MODE_LINES: clipping, Bresenham walk, per-pixel depth and
+    varyings along the line, order-free and ordered resolution."""
+    g, o = ctxs
+    sg, so = render_both(E.random_lines, g, o, **kw)
+    compare_scenes(sg, so, "lines")
+    assert (sg.read_depth() != sg.clear_depth).sum() > 1000 or kw.get("depth_mask") == A.DEPTH_MASK_OFF
+
+
+@pytest.mark.parametrize("tile", [(8, 8), (32, 16), (64, 64)])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_lines_all_tiles_and_modes(ctxs, tile, mode):
+    g, o = ctxs
+    g.set_tile_size(*tile)
+    g.set_raster_mode(mode)
+    sg, so = render_both(E.line_edges, g, o)
+    compare_scenes(sg, so, f"line edges {tile} mode {mode}")
+    sg, so = render_both(E.random_lines, g, o, num_lines=2500, width=300, height=200, persp=True, seed=78)
+    compare_scenes(sg, so, f"lines {tile} mode {mode}")
+
+
+def test_line_alias_known_difference(ctxs):
+    """The one case the GPU path does not reproduce: a line whose last pixel
+    (x = W) shares its first pixel's address. Everything else matches; at
+    that pixel the GPU applies the two fragments in order (the nearer first
+    one stays) where SoftLight keeps the later one."""
+    g, o = ctxs
+    sg, so = render_both(E.line_alias, g, o)
+    dg, do = sg.read_depth(), so.read_depth()
+    py, px = E.LINE_ALIAS_PIXEL
+    assert do[py, px] == np.float32(0.5) and dg[py, px] == np.float32(0.2)
+    dg[py, px] = do[py, px]
+    assert np.array_equal(dg.view(np.uint32), do.view(np.uint32))
+    assert np.array_equal(sg.read_color(), so.read_color())
+
+
+@pytest.mark.parametrize("batched", [False, True])
+@pytest.mark.parametrize("blend_lines", [False, True])
+def test_mixed_primitives(ctxs, batched, blend_lines):
+    """Triangles, lines and points into one frame; batched, one launch holds
+    all three record kinds."""
+    g, o = ctxs
+    sg, so = render_both(E.mixed_prims, g, o, batched=batched, blend_lines=blend_lines)
+    compare_scenes(sg, so, f"mixed batched={batched} blend={blend_lines}")
+
+
+def test_line_draw_rejections(gpu_lib):
+    """Line draws whose last line would read past the index buffer, and line
+    draws into framebuffers wider than the reference's int16 Bresenham error
+    term allows, are rejected before any launch."""
+    ctx = gpu_lib.Context()
+    s = E.random_lines(ctx, num_lines=10, indexed=np.uint16)
+    mesh = s.draws[0][0]
+    bad = A.Mesh(mesh.vaoId, 1, 20, A.RENDER_MODE_INDEXED_LINES, 0)   # last line reads element 20
+    with pytest.raises(A.SLError):
+        ctx.draw(bad, s.draws[0][2], s.fbo)
+    wide = E.random_lines(ctx, num_lines=10, width=11000, height=4)
+    with pytest.raises(A.SLError):
+        ctx.draw(wide.draws[0][0], wide.draws[0][2], wide.fbo)
+    ctx.close()
