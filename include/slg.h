@@ -222,13 +222,21 @@ size_t slg_create_shader(slg_context* ctx, const slg_vertex_shader* vs,
                          const slg_fragment_shader* fs, size_t uboId);
 
 /* SL_Context::clear_framebuffer / clear_color_buffer / clear_depth_buffer
- * (softlight/src/SL_Context.cpp:881-969) */
+ * (softlight/src/SL_Context.cpp:881-969). As in SL_ClearProcessor
+ * (softlight/src/SL_ClearProcessor.cpp:22-33) the clear reaches the texels
+ * its thread partition covers for the slg_num_threads count: with one thread
+ * and width * height % 3 == 2 the last texel keeps its value. */
 int slg_clear_framebuffer(slg_context* ctx, size_t fboId, unsigned attachment, const double rgba[4], double depth);
 int slg_clear_color_buffer(slg_context* ctx, size_t fboId, unsigned attachment, const double rgba[4]);
 int slg_clear_depth_buffer(slg_context* ctx, size_t fboId, double depth);
 
 /* SL_Context::draw / draw_instanced / draw_multiple
- * (softlight/include/softlight/SL_Context.hpp:215-225; softlight/src/SL_Context.cpp:714-740) */
+ * (softlight/include/softlight/SL_Context.hpp:215-225; softlight/src/SL_Context.cpp:714-740).
+ * Render modes: [INDEXED_]TRIANGLES, [INDEXED_]LINES and [INDEXED_]POINTS;
+ * TRI_WIRE is rejected (SLG_ERR_INVALID_ARG). A partial last primitive reads
+ * the elements after elementEnd as the reference does, and those reads are
+ * validated. Line draws need a framebuffer of at most 10922 x 10922 (the
+ * reference's int16 Bresenham error term) and no visibility map. */
 int slg_draw(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId);
 int slg_draw_instanced(slg_context* ctx, const slg_mesh* m, size_t numInstances, size_t shaderId, size_t fboId);
 int slg_draw_multiple(slg_context* ctx, const slg_mesh* meshes, size_t numMeshes, size_t shaderId, size_t fboId);

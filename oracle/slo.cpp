@@ -1388,9 +1388,28 @@ size_t slo_create_shader(slo_context* ctx, const slg_vertex_shader* vs, const sl
     return ctx->shaders.size() - 1;
 }
 
-static void clear_color(Texture& t, const double rgba[4])
+/* SL_ClearProcessor::clear_texture's reach (softlight/src/SL_ClearProcessor.cpp:22-33
+ * with sl_calc_indexed_parition2<1>, softlight/include/softlight/SL_ShaderUtil.hpp:222-231):
+ * thread t clears [t*range, min((t+1)*range, w*h)) with
+ * range = total + (1 - total % 3) in size_t, total = w*h / threads. */
+static size_t clear_reach(size_t count, unsigned threads)
 {
-    const size_t n = (size_t)t.w * t.h * t.d;
+    size_t reach = 0;
+    const size_t n = threads ? threads : 1u;
+    const size_t total = count / n;
+    const size_t range = total + (size_t(1) - (total % 3));
+    for (size_t id = 0; id < n; ++id)
+    {
+        const size_t begin = range * id, end = begin + range;
+        const size_t stop = end < count ? end : count;
+        if (stop > begin && stop > reach) reach = stop;
+    }
+    return reach;
+}
+
+static void clear_color(Texture& t, const double rgba[4], unsigned threads)
+{
+    const size_t n = clear_reach((size_t)t.w * t.h, threads);
     if (t.type == SLG_COLOR_RGBA_8U)
     {
         /* color_cast<uint8_t, double> (SL_Color.cpp:148; SL_Color.hpp:625) */
@@ -1417,7 +1436,7 @@ static void clear_color(Texture& t, const double rgba[4])
 int slo_clear_color_buffer(slo_context* ctx, size_t fbo, unsigned att, const double rgba[4])
 {
     if (fbo >= ctx->fbos.size() || att >= ctx->fbos[fbo].numColors) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo");
-    clear_color(*ctx->textures[ctx->fbos[fbo].colors[att]], rgba);
+    clear_color(*ctx->textures[ctx->fbos[fbo].colors[att]], rgba, ctx->numThreads);
     return SLG_OK;
 }
 
@@ -1425,7 +1444,7 @@ int slo_clear_depth_buffer(slo_context* ctx, size_t fbo, double depth)
 {
     if (fbo >= ctx->fbos.size() || ctx->fbos[fbo].depth == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo");
     const double d[4] = {depth, 0, 0, 0};
-    clear_color(*ctx->textures[ctx->fbos[fbo].depth], d);
+    clear_color(*ctx->textures[ctx->fbos[fbo].depth], d, ctx->numThreads);
     return SLG_OK;
 }
 

@@ -87,6 +87,7 @@ bool valid_program(uint32_t p) { return p >= SLG_PROGRAM_LAMBERT_TEX && p <= SLG
 constexpr size_t kDescRing = 4096;
 constexpr uint64_t kMaxSlots = (1ull << 29) - 1; /* keys are slot << 3 | sub in 32 bits */
 constexpr int kMaxLineExtent = 10922;            /* 3 * 10922 < 32768 */
+constexpr uint32_t kAliasCap = 4096;             /* line address aliases per launch */
 
 } // namespace
 
@@ -125,6 +126,7 @@ struct slg_context
 
     /* scratch */
     DevBuffer records, varyings, slotInfo, slotOvf, ovfCount, clipQueue, clipCount;
+    DevBuffer aliasEvents, aliasCount; /* line address aliases (slg::AliasEvent) */
     DevBuffer tileCount, tileOffset, tileCursor, entries, status;
     DevBuffer blitBuf;      /* destination of slg_blit_read */
     uint64_t slotCap = 0, ovfCap = 0, tileCap = 0, entryCap = 0;
@@ -242,6 +244,8 @@ int ensure_scratch(slg_context* ctx, uint64_t numSlots, uint64_t numTiles)
     {
         if ((r = dev_alloc(ctx, ctx->ovfCount, sizeof(uint32_t), true))) return r;
         if ((r = dev_alloc(ctx, ctx->clipCount, sizeof(uint32_t), true))) return r;
+        if ((r = dev_alloc(ctx, ctx->aliasEvents, kAliasCap * sizeof(slg::AliasEvent), false))) return r;
+        if ((r = dev_alloc(ctx, ctx->aliasCount, sizeof(uint32_t), true))) return r;
         if ((r = dev_alloc(ctx, ctx->status, 4 * sizeof(int32_t), true))) return r;
     }
     if (numTiles > ctx->tileCap)
@@ -285,6 +289,10 @@ int check_status(slg_context* ctx)
     {
         msg += " triangles per tile";
     }
+    if (bits & slg::kStatusAliasOverflow)
+    {
+        msg += " full-width line aliases (at most 4096 per launch, 4096 records per aliased pixel)";
+    }
     msg += " (the affected draws were skipped; buffers have been grown)";
     return ctx->fail(SLG_ERR_OVERFLOW, msg);
 }
@@ -323,12 +331,29 @@ int color_value(int type, const double rgba[4], uint32_t out[4])
     return 0;
 }
 
+/* Texels SL_ClearProcessor::clear_texture reaches (softlight/src/
+ * SL_ClearProcessor.cpp:22-33): the w*h texels are dealt to the threads by
+ * sl_calc_indexed_parition2<1> (softlight/include/softlight/SL_ShaderUtil.hpp:
+ * 222-231), whose per-thread range count/threads + (1 - (count/threads) % 3)
+ * is computed in size_t, so together the threads clear the prefix
+ * [0, min(threads * range, count)); with one thread and count % 3 == 2 the
+ * last texel keeps its value. */
+uint64_t clear_extent(uint64_t count, unsigned threads)
+{
+    const uint64_t n = threads ? threads : 1u;
+    const uint64_t total = count / n;
+    const uint64_t range = total + (uint64_t(1) - total % 3u);
+    const uint64_t reach = n * range;
+    return (range != 0 && reach / range == n && reach < count) ? reach : count;
+}
+
 int clear_texture(slg_context* ctx, size_t texId, const double rgba[4])
 {
     const Texture& t = ctx->textures[texId];
     uint32_t v[4];
     if (color_value(t.type, rgba, v)) return ctx->fail(SLG_ERR_INVALID_ARG, "unsupported clear format");
-    cudaError_t e = slg::launch_clear(static_cast<uint8_t*>(t.buf.ptr), (size_t)t.w * t.h * t.d, (int)t.bpt, v, ctx->stream);
+    const uint64_t texels = clear_extent((uint64_t)t.w * t.h, ctx->numThreads);
+    cudaError_t e = slg::launch_clear(static_cast<uint8_t*>(t.buf.ptr), (size_t)texels, (int)t.bpt, v, ctx->stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "clear launch");
     return SLG_OK;
 }
@@ -670,6 +695,12 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
             return ctx->fail(SLG_ERR_INVALID_ARG, "line draws need a framebuffer of at most 10922 x 10922");
         if (descs[i].prim == slg::kPrimLine) f.hasLines = 1;
     }
+    if (f.hasLines)
+    {
+        f.aliasEvents = static_cast<slg::AliasEvent*>(ctx->aliasEvents.ptr);
+        f.aliasCount = static_cast<uint32_t*>(ctx->aliasCount.ptr);
+        f.aliasCap = kAliasCap;
+    }
     f.tables.textures = static_cast<const TexView*>(ctx->texTable.ptr);
     f.tables.buffers = static_cast<const uint8_t* const*>(ctx->bufTable.ptr);
 
@@ -677,6 +708,8 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
 
     if (fbo.visEnabled)
     {
+        if (f.hasLines)
+            return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map takes triangle and point draws only");
         if (!f.orderFree)
             return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map takes opaque draws only (no blending, one depth rule)");
         if (fbo.vis.bytes < (size_t)f.width * f.height * sizeof(uint32_t))
@@ -743,7 +776,8 @@ void slg_context_destroy(slg_context* ctx)
     for (Ubo& u : ctx->ubos) dev_free(u.buf);
     for (Fbo& f : ctx->fbos) dev_free(f.vis);
     DevBuffer* scratch[] = {&ctx->texTable, &ctx->bufTable, &ctx->records, &ctx->varyings, &ctx->slotInfo, &ctx->slotOvf,
-                            &ctx->ovfCount, &ctx->clipQueue, &ctx->clipCount, &ctx->tileCount, &ctx->tileOffset,
+                            &ctx->ovfCount, &ctx->clipQueue, &ctx->clipCount, &ctx->aliasEvents, &ctx->aliasCount,
+                            &ctx->tileCount, &ctx->tileOffset,
                             &ctx->tileCursor, &ctx->entries, &ctx->blitBuf,
                             &ctx->status, &ctx->devDescs, &ctx->devStarts};
     for (DevBuffer* b : scratch) dev_free(*b);
@@ -1263,8 +1297,8 @@ constexpr size_t kNoAllocTextures = 256, kNoAllocBuffers = 256;
 constexpr size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
 
 /* layout of the static scratch; the first kNoAllocZeroBytes must be zero
- * when the pipeline starts: ovfCount (+0), clipCount (+4), the status words
- * (+16..+31) and the per-tile triangle counters (+256) */
+ * when the pipeline starts: ovfCount (+0), clipCount (+4), aliasCount (+8),
+ * the status words (+16..+31) and the per-tile triangle counters (+256) */
 constexpr size_t kOffCounters = 0;
 constexpr size_t kOffTileCount = 256;
 constexpr size_t kNoAllocZeroBytes = kOffTileCount + align256(kNoAllocTiles * sizeof(uint32_t));
@@ -1278,7 +1312,9 @@ constexpr size_t kOffBufTable = kOffTexTable + align256(kNoAllocTextures * sizeo
 constexpr size_t kOffRecords = kOffBufTable + align256(kNoAllocBuffers * sizeof(void*));
 constexpr size_t kOffVaryings = kOffRecords + align256(kNoAllocRecords * slg::kRecordVec4 * sizeof(float4));
 constexpr size_t kOffEntries = kOffVaryings + align256(kNoAllocRecords * slg::kVaryingVec4 * sizeof(float4));
-constexpr size_t kNoAllocBytes = kOffEntries + align256(kNoAllocEntries * sizeof(uint32_t));
+constexpr uint32_t kNoAllocAliases = 64;
+constexpr size_t kOffAliases = kOffEntries + align256(kNoAllocEntries * sizeof(uint32_t));
+constexpr size_t kNoAllocBytes = kOffAliases + align256(kNoAllocAliases * sizeof(slg::AliasEvent));
 static_assert(kNoAllocBytes < (8u << 20), "static draw scratch stays under 8 MiB");
 
 static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocBytes];
@@ -1359,6 +1395,9 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
         if (std::max(f.width, f.height) > kMaxLineExtent)
             return ctx->fail(SLG_ERR_INVALID_ARG, "line draws need a framebuffer of at most 10922 x 10922");
         f.hasLines = 1;
+        f.aliasEvents = reinterpret_cast<slg::AliasEvent*>(scratch + kOffAliases);
+        f.aliasCount = reinterpret_cast<uint32_t*>(scratch + kOffCounters + 8);
+        f.aliasCap = kNoAllocAliases;
     }
 
     /* resource tables: the context's when they are current, else a copy of

@@ -95,6 +95,22 @@ constexpr uint32_t kRecordPoint = 1u << 5;
 constexpr uint32_t kRecordLine = 1u << 6;
 
 /* Per-launch scratch and framebuffer description. */
+/* A line whose last walk step (x = W on row y - 1) is stored at the address
+ * of its first step (x = 0 on row y). SoftLight depth-tests line fragments
+ * when it queues them and writes them when its 600-fragment queue is
+ * flushed, so when fewer than 600 of the line's fragments were queued before
+ * the last step, both steps are tested against the depth before the line.
+ * The vertex stage logs such lines (depth mask on, depth test on); the
+ * ordered raster counts `queued`; alias_fixup_kernel replays the pixel. */
+struct AliasEvent
+{
+    uint32_t slot;      /* the line's record */
+    uint32_t pixel;     /* linear index of the shared pixel (column 0) */
+    uint32_t queued;    /* steps 0 < k < dx that passed the depth test */
+    float    depth0;    /* the pixel's depth before the launch */
+    uint4    color0;    /* the pixel's colour bits before the launch */
+};
+
 struct Frame
 {
     /* framebuffer */
@@ -141,6 +157,12 @@ struct Frame
      * the line set-up runs (kept apart from the triangle variant's registers) */
     int32_t hasLines;
 
+    /* line address aliases (AliasEvent); null without line draws. Order-free
+     * launches take the ordered raster when any alias was logged. */
+    AliasEvent* aliasEvents;
+    uint32_t*   aliasCount;
+    uint32_t    aliasCap;
+
     /* optional visibility map (order-free raster only): per pixel written,
      * 1 + the launch slot (triangle) of the winning fragment; null: off */
     uint32_t* ids;
@@ -150,7 +172,8 @@ enum StatusBits
 {
     kStatusEntryOverflow = 1,
     kStatusOvfOverflow = 2,
-    kStatusTileOverflow = 4
+    kStatusTileOverflow = 4,
+    kStatusAliasOverflow = 8
 };
 
 /*-----------------------------------------------------------------------------

@@ -474,7 +474,7 @@ __device__ __forceinline__ uint32_t setup_point(const Frame& f, const DrawDesc& 
  *   r0, r1 = screen positions of the two ends (x, y, z, w)
  *   r2     = (1 / |end1 - end0|, 0, 0, 0)
  *   r3     = Bresenham walk as int32 bits: (x1, x2, y1, steep | (yErr < 0) << 1)
- *   r4     = (dx, dErr, wraps, 0) as int32 bits
+ *   r4     = (dx, dErr, wraps, alias event + 1 or 0) as int32 bits
  *   r6     = pixel bounds, r7 = (draw, primIndex lo, hi, flags | kRecordLine)
 -----------------------------------------------------------------------------*/
 constexpr float kLineEpsilon = 1.0e-6f;   /* LS_EPSILON */
@@ -603,13 +603,44 @@ __device__ __forceinline__ uint32_t setup_line(const Frame& f, const DrawDesc& d
     const int yNeg = (y2 > y1) ? 0 : 1;
     const bool wraps = maxX >= f.width;   /* pixels at x = W land on the next row */
 
+    /* the last step (x = W, row y2) is stored at the first step's address
+     * (x = 0, row y1 = y2 + 1): logged for alias_fixup_kernel when the depth
+     * state can tell the queue's test order from the sequential one */
+    int aliasTag = 0;
+    if (!steep && x1 == 0 && x2 == f.width && y2 == y1 - 1 && y1 < f.height && d.depthMask && d.depthTest != SLG_DEPTH_TEST_OFF &&
+        f.aliasEvents)
+    {
+        const uint32_t e = atomicAdd(f.aliasCount, 1u);
+        if (e < f.aliasCap)
+        {
+            AliasEvent& ev = f.aliasEvents[e];
+            const uint32_t pix = (uint32_t)y1 * (uint32_t)f.width;
+            ev.slot = (uint32_t)slot;
+            ev.pixel = pix;
+            ev.queued = 0;
+            ev.depth0 = f.depth[pix];
+            uint4 c = make_uint4(0u, 0u, 0u, 0u);
+            if (f.color)
+            {
+                if (f.colorType == SLG_COLOR_RGBA_FLOAT) c = reinterpret_cast<const uint4*>(f.color)[pix];
+                else c.x = reinterpret_cast<const uint32_t*>(f.color)[pix];
+            }
+            ev.color0 = c;
+            aliasTag = (int)e + 1;
+        }
+        else
+        {
+            atomicOr(f.status, kStatusAliasOverflow);
+        }
+    }
+
     Record rec;
     const float ex = s1.x - s0.x, ey = s1.y - s0.y;
     rec.r[0] = s0;
     rec.r[1] = s1;
     rec.r[2] = make_float4(1.f / sqrtf(ex * ex + ey * ey), 0.f, 0.f, 0.f);
     rec.r[3] = make_float4(__int_as_float(x1), __int_as_float(x2), __int_as_float(y1), __int_as_float((steep ? 1 : 0) | (yNeg << 1)));
-    rec.r[4] = make_float4(__int_as_float(dxl), __int_as_float(dErr), __int_as_float(wraps ? 1 : 0), 0.f);
+    rec.r[4] = make_float4(__int_as_float(dxl), __int_as_float(dErr), __int_as_float(wraps ? 1 : 0), __int_as_float(aliasTag));
     rec.r[5] = make_float4(0.f, 0.f, 0.f, 0.f);
     rec.r[6] = wraps ? make_float4(__int_as_float(minY), __int_as_float(maxY + 2), __int_as_float(0), __int_as_float(f.width - 1))
                      : make_float4(__int_as_float(minY), __int_as_float(maxY + 1), __int_as_float(minX), __int_as_float(maxX));
@@ -1328,6 +1359,14 @@ __device__ __forceinline__ void for_band_records(const float4* sRec, int cnt, in
  * and every thread applies, for the pixels it owns, each fragment in
  * submission order: depth test, fragment program, blend, depth write.
 -----------------------------------------------------------------------------*/
+/* Whether the ordered raster renders this launch: always when it is not
+ * order-free, and for an order-free launch whose line draws logged address
+ * aliases (the order-free raster then stands aside). */
+__device__ __forceinline__ bool ordered_raster_runs(const Frame& f)
+{
+    return !f.orderFree || (f.aliasCount != nullptr && *f.aliasCount != 0u);
+}
+
 /* Sorts each tile's key list in place (ascending = submission order) for
  * the ordered raster; one CTA per tile, the list staged in shared memory. */
 __global__ void __launch_bounds__(1024) tile_sort_kernel(const Frame f, int sortCap)
@@ -1337,7 +1376,7 @@ __global__ void __launch_bounds__(1024) tile_sort_kernel(const Frame f, int sort
     const int tile = blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
     const uint32_t n = f.tileOffset[tile + 1] - begin;
-    if (n < 2 || (f.status[0] & kStatusEntryOverflow))
+    if (n < 2 || (f.status[0] & kStatusEntryOverflow) || !ordered_raster_runs(f))
     {
         return;
     }
@@ -1367,7 +1406,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
     const int tile = blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
     const uint32_t n = f.tileOffset[tile + 1] - begin;
-    if (n == 0 || (f.status[0] & (kStatusEntryOverflow | kStatusTileOverflow)))
+    if (n == 0 || (f.status[0] & (kStatusEntryOverflow | kStatusTileOverflow)) || !ordered_raster_runs(f))
     {
         return;
     }
@@ -1439,6 +1478,12 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                     const int idx = r * L::kStride + (px - x0);
                     if (depth_cmp(flags & 0xF, z, sDepth[idx]))
                     {
+                        const int aliasTag = __float_as_int(R[4].w);
+                        if (aliasTag && k > 0 && k < w.dx)
+                        {
+                            /* a fragment SoftLight queues ahead of the line's last step */
+                            atomicAdd(&f.aliasEvents[aliasTag - 1].queued, 1u);
+                        }
                         float4 o;
                         if (shade_line(f, dd, rec, interp, o) && f.color)
                         {
@@ -1616,12 +1661,14 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
             const LineWalk w = line_walk(R);
             const LineRow lr = line_row(w, y, x0, xLimit, width);
             const uint32_t key = sKey[lo];
-            for (int k = lr.kLo; k <= lr.kHi + 1; ++k)
+            const int nRow = max(lr.kHi - lr.kLo + 1, 0);
+            const int nAll = nRow + (lr.kWrap >= 0 ? 1 : 0);
+            for (int j = 0; j < nAll; ++j)
             {
-                const int kk = (k <= lr.kHi) ? k : lr.kWrap;
+                const int kk = (j < nRow) ? lr.kLo + j : lr.kWrap;
                 uint32_t X, Y;
                 int px, py;
-                if (kk < 0 || !line_store_pixel(w, kk, width, height, X, Y, px, py) || py != y || px < x0 || px >= xLimit)
+                if (!line_store_pixel(w, kk, width, height, X, Y, px, py) || py != y || px < x0 || px >= xLimit)
                 {
                     continue;
                 }
@@ -1718,7 +1765,7 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
     const int tile = blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
     const uint32_t n = f.tileOffset[tile + 1] - begin;
-    if (n == 0 || (f.status[0] & kStatusEntryOverflow))
+    if (n == 0 || (f.status[0] & kStatusEntryOverflow) || ordered_raster_runs(f))
     {
         return;
     }
@@ -1812,6 +1859,182 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
 }
 
 /*-----------------------------------------------------------------------------
+ * Line address aliases (AliasEvent). After the ordered raster, each logged
+ * pixel is replayed from its pre-launch state through every record that
+ * covers it, in submission order. The aliasing line's two fragments there
+ * follow SoftLight's queue (SL_LineRasterizer.cpp:49-85, flushed every
+ * SL_SHADER_MAX_QUEUED_FRAGS = 600 queued fragments): when fewer than 600 of
+ * the line's steps before the last one passed the depth test, the last step
+ * is tested against the depth before the line; both writes then follow in
+ * walk order.
+-----------------------------------------------------------------------------*/
+constexpr int kAliasThreads = 256;
+constexpr int kAliasKeys = 4096;          /* records covering one pixel (power of two) */
+constexpr uint32_t kLineQueue = 600;      /* SL_SHADER_MAX_QUEUED_FRAGS */
+
+template <class Color>
+__device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_t* keys, int m)
+{
+    typedef typename Color::stored Stored;
+    const uint32_t gi = ev.pixel;
+    const int py = (int)(gi / (uint32_t)f.width);
+    const float yf = (float)py;
+
+    /* the pixel's state before the launch */
+    float depth = ev.depth0;
+    Stored color{};
+    if (f.color)
+    {
+        if (f.colorType == SLG_COLOR_RGBA_FLOAT) reinterpret_cast<uint4*>(f.color)[gi] = ev.color0;
+        else reinterpret_cast<uint32_t*>(f.color)[gi] = ev.color0.x;
+        color = Color::read(f.color, gi);
+    }
+    auto put = [&](const DrawDesc& dd, bool have, const float4 o) {
+        if (have && f.color)
+        {
+            color = (dd.blend != SLG_BLEND_OFF) ? Color::store(blend_color(dd.blend, o, Color::load(color))) : Color::store(o);
+        }
+    };
+
+    for (int i = 0; i < m; ++i)
+    {
+        const uint64_t rec = key_to_record(f, keys[i]);
+        const float4* R = f.records + rec * kRecordVec4;
+        const uint32_t flags = __float_as_uint(R[7].w);
+        const int func = flags & 0xF;
+        const bool mask = ((flags >> 4) & 1) != 0;
+        const DrawDesc& dd = f.draws[__float_as_uint(R[7].x)];
+        float4 o;
+        if (flags & kRecordLine)
+        {
+            const LineWalk w = line_walk(R);
+            const LineRow lr = line_row(w, py, 0, 1, f.width);
+            int ks[2];
+            int nk = 0;
+            for (int k = lr.kLo; k <= lr.kHi && nk < 2; ++k) ks[nk++] = k;
+            if (lr.kWrap >= 0 && nk < 2) ks[nk++] = lr.kWrap;
+            int kh[2];
+            float zh[2], ih[2];
+            int nh = 0;
+            for (int j = 0; j < nk; ++j)
+            {
+                uint32_t X, Y;
+                int px, qy;
+                if (line_store_pixel(w, ks[j], f.width, f.height, X, Y, px, qy) && (uint32_t)qy * (uint32_t)f.width + (uint32_t)px == gi)
+                {
+                    ih[nh] = line_interp(R, X, Y);
+                    zh[nh] = mixf(R[0].z, R[1].z, ih[nh]);
+                    kh[nh] = ks[j];
+                    ++nh;
+                }
+            }
+            const int tag = __float_as_int(R[4].w);
+            const float before = depth;
+            for (int j = 0; j < nh; ++j)
+            {
+                float against = depth;
+                if (j == 1 && tag != 0 && kh[1] == w.dx)
+                {
+                    /* the last step: the first one is written before its test
+                     * only if the queue was flushed in between */
+                    const uint32_t queued = f.aliasEvents[tag - 1].queued + (depth_cmp(func, zh[0], before) ? 1u : 0u);
+                    if (queued < kLineQueue) against = before;
+                }
+                if (depth_cmp(func, zh[j], against))
+                {
+                    put(dd, shade_line(f, dd, rec, ih[j], o), o);
+                    if (mask) depth = zh[j];
+                }
+            }
+        }
+        else if (flags & kRecordPoint)
+        {
+            const float4 r6 = R[6];
+            if (__float_as_int(r6.z) == 0 && __float_as_int(r6.x) == py && depth_cmp(func, R[0].z, depth))
+            {
+                put(dd, shade_point(f, dd, rec, o), o);
+                if (mask) depth = R[0].z;
+            }
+        }
+        else
+        {
+            Chain ch;
+            if (chain_begin(R, yf, 0, 1, ch) && ch.x == 0)
+            {
+                const float z = chain_depth(R, ch);
+                if (depth_cmp(func, z, depth))
+                {
+                    put(dd, shade(f, dd, rec, R[2].w, R[5], ch.b0, ch.b1, ch.b2, o), o);
+                    if (mask) depth = z;
+                }
+            }
+        }
+    }
+    f.depth[gi] = depth;
+    if (f.color) Color::write(f.color, gi, color);
+}
+
+template <class Color>
+__global__ void __launch_bounds__(kAliasThreads) alias_fixup_kernel(const Frame f)
+{
+    __shared__ uint32_t sKeys[kAliasKeys];
+    __shared__ uint32_t sCount;
+    __shared__ int sSkip;
+    if (f.status[0] & (kStatusEntryOverflow | kStatusTileOverflow))
+    {
+        return;
+    }
+    const uint32_t count = min(*f.aliasCount, f.aliasCap);
+    for (uint32_t e = blockIdx.x; e < count; e += gridDim.x)
+    {
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            sCount = 0;
+            sSkip = 0;
+        }
+        __syncthreads();
+        const AliasEvent ev = f.aliasEvents[e];
+        /* one replay per pixel, by its first event */
+        for (uint32_t j = threadIdx.x; j < e; j += blockDim.x)
+        {
+            if (f.aliasEvents[j].pixel == ev.pixel) sSkip = 1;
+        }
+        __syncthreads();
+        const bool skip = sSkip != 0;
+        const int py = (int)(ev.pixel / (uint32_t)f.width);
+        const int tile = (py / f.tileH) * f.tilesX;
+        const uint32_t begin = f.tileOffset[tile];
+        const uint32_t n = f.tileOffset[tile + 1] - begin;
+        if (!skip)
+        {
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+            {
+                const uint32_t key = f.entries[begin + i];
+                const float4 r6 = f.records[key_to_record(f, key) * kRecordVec4 + 6];
+                if (__float_as_int(r6.x) <= py && py < __float_as_int(r6.y) && __float_as_int(r6.z) <= 0)
+                {
+                    const uint32_t q = atomicAdd(&sCount, 1u);
+                    if (q < (uint32_t)kAliasKeys) sKeys[q] = key;
+                }
+            }
+        }
+        __syncthreads();
+        const int m = skip ? 0 : (int)sCount;
+        if (m > kAliasKeys)
+        {
+            if (threadIdx.x == 0) atomicOr(f.status, kStatusAliasOverflow);
+            continue;
+        }
+        if (!skip)
+        {
+            sort_keys(sKeys, m);
+            if (threadIdx.x == 0) alias_replay<Color>(f, ev, sKeys, m);
+        }
+    }
+}
+
+/*-----------------------------------------------------------------------------
  * Clear (SL_ClearProcessor, softlight/src/SL_ClearProcessor.cpp)
 -----------------------------------------------------------------------------*/
 __global__ void clear_kernel(uint8_t* dst, size_t numTexels, int bytesPerTexel, uint4 value)
@@ -1835,11 +2058,17 @@ static cudaError_t launch_raster_t(const Frame& f, int numTiles, int keyCap, cud
     {
         raster_free_kernel<TW, TH, Color><<<numTiles, kFreeThreads, FreeLayout<TW, TH>::bytes(), s>>>(f, f.freeDepthFunc, f.freeDepthMask);
     }
-    else
+    if (!f.orderFree || f.aliasCount)
     {
-        /* keyCap keys of 4 bytes per tile for the sort (<= 227 KB) */
+        /* keyCap keys of 4 bytes per tile for the sort (<= 227 KB); for an
+         * order-free launch with line draws both rasters are queued and the
+         * device decides (ordered_raster_runs) */
         tile_sort_kernel<<<numTiles, 1024, sizeof(uint32_t) * (size_t)keyCap, s>>>(f, keyCap);
         raster_ordered_kernel<TW, TH, Color><<<numTiles, L::kThreads, L::ordered_bytes(), s>>>(f);
+    }
+    if (f.aliasCount)
+    {
+        alias_fixup_kernel<Color><<<64, kAliasThreads, 0, s>>>(f);
     }
     return cudaGetLastError();
 }
@@ -1891,6 +2120,10 @@ cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEven
     const int numTiles = f.tilesX * f.tilesY;
     const int vsBlock = (f.vsBlock == 64 || f.vsBlock == 256) ? f.vsBlock : 128;
     if (ev) cudaEventRecord(ev[0], s);
+    if (f.aliasCount)
+    {
+        cudaMemsetAsync(f.aliasCount, 0, sizeof(uint32_t), s);
+    }
     if (f.numSlots > 0)
     {
         const unsigned blocks = (unsigned)((f.numSlots + vsBlock - 1) / vsBlock);

@@ -243,9 +243,10 @@ LINE_ALIAS_PIXEL = (10, 0)   # (row, column) that both ends of line_alias's line
 def line_alias(ctx, width=40, height=30):
     """A full-width line whose last pixel (x = W, row 9) is stored at the
     address of its first pixel (x = 0, row 10). SoftLight tests both against
-    the depth before the line (its 600-fragment queue is written after the
-    test) and writes them in walk order, so the later, farther fragment wins
-    there; the GPU path applies them in order. Depth LESS, z from 0.2 to 0.5."""
+    the depth before the line (fewer than 600 fragments are queued before the
+    last one, so the queue is written after both tests) and writes them in
+    walk order: the later, farther fragment wins there. Depth LESS, z from
+    0.2 to 0.5."""
     s = S.Scene(ctx, "line_alias", width, height)
     verts = np.zeros((2, 9), np.float32)
     verts[0, :3] = (-1.0, -0.32, 0.2)
@@ -255,6 +256,34 @@ def line_alias(ctx, width=40, height=30):
     sh = s.add_shader(A.PROGRAM_FLAT_COLOR, 0, S.flat_uniforms(np.eye(4), (1.0, 1.0, 1.0, 1.0)),
                       cull=A.CULL_OFF, depth_test=A.DEPTH_TEST_LESS_THAN, depth_mask=A.DEPTH_MASK_ON)
     s.draws.append((mesh, 1, sh))
+    return s
+
+
+def line_alias_wide(ctx, occluded=True, batched=False, blend=A.BLEND_OFF, width=700, height=20):
+    """A 700-wide framebuffer and a line from (0, row 10) to (W, row 9), its
+    last pixel stored at its first. With `occluded`, a nearer quad hides
+    columns 50..690 of rows 7..12 first: fewer than 600 of the line's
+    fragments are queued before its last step, so SoftLight tests that step
+    against the depth before the line; unoccluded, the queue is flushed in
+    between and the test follows the first step's write."""
+    s = S.Scene(ctx, f"line_alias_wide_{int(occluded)}", width, height)
+    if occluded:
+        xa, xb = 50.0 / (width / 2) - 1.0, 690.0 / (width / 2) - 1.0
+        quad = np.zeros((6, 9), np.float32)
+        quad[:, :3] = [(xa, -0.3, 0.0), (xb, -0.3, 0.0), (xb, 0.3, 0.0), (xa, -0.3, 0.0), (xb, 0.3, 0.0), (xa, 0.3, 0.0)]
+        mesh = s.add_mesh(quad, None, stride=36)
+        sh = s.add_shader(A.PROGRAM_FLAT_COLOR, 0, S.flat_uniforms(np.eye(4), (0.2, 0.2, 0.9, 1.0)),
+                          cull=A.CULL_OFF, depth_test=A.DEPTH_TEST_LESS_THAN, depth_mask=A.DEPTH_MASK_ON)
+        s.draws.append((mesh, 1, sh))
+    verts = np.zeros((2, 9), np.float32)
+    verts[0, :3] = (-1.0, 0.05, 0.2)
+    verts[1, :3] = (1.0, -0.05, 0.5)
+    line = s.add_mesh(verts, None, stride=36)
+    line.mode = A.RENDER_MODE_LINES
+    sh = s.add_shader(A.PROGRAM_FLAT_COLOR, 0, S.flat_uniforms(np.eye(4), (1.0, 0.8, 0.1, 0.6)),
+                      cull=A.CULL_OFF, depth_test=A.DEPTH_TEST_LESS_THAN, depth_mask=A.DEPTH_MASK_ON, blend=blend)
+    s.draws.append((line, 1, sh))
+    s.batched = batched
     return s
 
 

@@ -44,15 +44,11 @@ SCENES = {
                                                     num_lines=3000, width=700, height=40)),
     "line_edges": (E.line_edges, dict()),
     "line_alias": (E.line_alias, dict()),
+    "line_alias_wide_occluded": (E.line_alias_wide, dict(occluded=True)),
+    "line_alias_wide_open": (E.line_alias_wide, dict(occluded=False)),
+    "line_alias_wide_occluded_blend": (E.line_alias_wide, dict(occluded=True, blend=A.BLEND_ALPHA)),
 }
 
-
-# Pixels (row, column) where the GPU path is known to differ from SoftLight,
-# with the reason: line_alias's last pixel shares its first pixel's address
-# and SoftLight tests both against the depth before the line.
-GPU_KNOWN_DIFFERENCES = {
-    "line_alias": [E.LINE_ALIAS_PIXEL],
-}
 
 
 # (name, source: "color" | "depth" | "colorf", destination type, width, height)

@@ -27,9 +27,6 @@ def test_gpu_matches_reference_golden(gpu_lib, name, mode, tile):
     d = np.load(os.path.join(GOLDEN, name + ".npz"))
     gc, gd = d["color"], d["depth"]
     c, dd = scene.read_color(), scene.read_depth()
-    for (py, px) in G.GPU_KNOWN_DIFFERENCES.get(name, []):
-        gd, gc = gd.copy(), gc.copy()
-        gd[py, px], gc[py, px] = dd[py, px], c[py, px]
     bad = (dd.view(np.uint32) != gd.view(np.uint32)) & ~(np.isnan(dd) & np.isnan(gd))
     assert not bad.any(), f"{name}: {int(bad.sum())} depth texels differ from the reference"
     if c.dtype == np.uint8:

@@ -281,19 +281,38 @@ def test_lines_all_tiles_and_modes(ctxs, tile, mode):
     compare_scenes(sg, so, f"lines {tile} mode {mode}")
 
 
-def test_line_alias_known_difference(ctxs):
-    """The one case the GPU path does not reproduce: a line whose last pixel
-    (x = W) shares its first pixel's address. Everything else matches; at
-    that pixel the GPU applies the two fragments in order (the nearer first
-    one stays) where SoftLight keeps the later one."""
+def test_line_alias(ctxs):
+    """A line whose last pixel (x = W) shares its first pixel's address: both
+    are tested against the depth before the line, the later one wins."""
     g, o = ctxs
     sg, so = render_both(E.line_alias, g, o)
-    dg, do = sg.read_depth(), so.read_depth()
-    py, px = E.LINE_ALIAS_PIXEL
-    assert do[py, px] == np.float32(0.5) and dg[py, px] == np.float32(0.2)
-    dg[py, px] = do[py, px]
-    assert np.array_equal(dg.view(np.uint32), do.view(np.uint32))
-    assert np.array_equal(sg.read_color(), so.read_color())
+    compare_scenes(sg, so, "line alias")
+    assert sg.read_depth()[E.LINE_ALIAS_PIXEL] == np.float32(0.5)
+
+
+@pytest.mark.parametrize("occluded", [True, False])
+@pytest.mark.parametrize("batched", [False, True])
+@pytest.mark.parametrize("blend", [A.BLEND_OFF, A.BLEND_ALPHA])
+def test_line_alias_queue_rule(ctxs, occluded, batched, blend):
+    """700 px wide: occluded, fewer than 600 of the line's fragments are
+    queued before its last step (tested against the depth before the line);
+    open, the queue is written in between (tested after the first write)."""
+    g, o = ctxs
+    sg, so = render_both(E.line_alias_wide, g, o, occluded=occluded, batched=batched, blend=blend)
+    compare_scenes(sg, so, f"wide alias occluded={occluded} batched={batched} blend={blend}")
+    assert sg.read_depth()[10, 0] == np.float32(0.5 if occluded else 0.2)
+
+
+@pytest.mark.parametrize("threads", [1, 3, 7])
+def test_clear_extent_and_carry_over(ctxs, threads):
+    """SoftLight's clear reaches only the prefix its thread partition covers
+    (53 x 37 = 1961 texels, 1961 % 3 == 2: one thread leaves the last texel);
+    what the previous frame drew there carries over into the next."""
+    g, o = ctxs
+    g.num_threads(threads)
+    o.num_threads(threads)
+    sg, so = render_both(E.random_soup, g, o, width=53, height=37, frames=3, num_tris=400)
+    compare_scenes(sg, so, f"clear extent, {threads} threads")
 
 
 @pytest.mark.parametrize("batched", [False, True])
