@@ -639,10 +639,16 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
 
     Frame f;
     std::memset(&f, 0, sizeof(f));
+    for (size_t i = 0; i < n; ++i)
+    {
+        if (descs[i].prim == slg::kPrimLine) f.hasLines = 1;
+    }
     f.width = depthTex.w;
     f.height = depthTex.h;
-    f.tileW = ctx->tileW;
-    f.tileH = ctx->tileH;
+    /* launches with line draws use the line-carrying raster, compiled for
+     * one tile size */
+    f.tileW = f.hasLines ? slg::kLineTile : ctx->tileW;
+    f.tileH = f.hasLines ? slg::kLineTile : ctx->tileH;
     f.tilesX = (f.width + f.tileW - 1) / f.tileW;
     f.tilesY = (f.height + f.tileH - 1) / f.tileH;
     const uint64_t numTiles = (uint64_t)f.tilesX * f.tilesY;
@@ -693,7 +699,6 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
          * 3 * dx fits, dx <= max(W, H) */
         if (descs[i].prim == slg::kPrimLine && std::max(f.width, f.height) > kMaxLineExtent)
             return ctx->fail(SLG_ERR_INVALID_ARG, "line draws need a framebuffer of at most 10922 x 10922");
-        if (descs[i].prim == slg::kPrimLine) f.hasLines = 1;
     }
     if (f.hasLines)
     {
@@ -1379,10 +1384,11 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
 
     Frame f;
     std::memset(&f, 0, sizeof(f));
+    f.hasLines = (desc->prim == slg::kPrimLine) ? 1 : 0;
     f.width = depthTex.w;
     f.height = depthTex.h;
-    f.tileW = ctx->tileW;
-    f.tileH = ctx->tileH;
+    f.tileW = f.hasLines ? slg::kLineTile : ctx->tileW;
+    f.tileH = f.hasLines ? slg::kLineTile : ctx->tileH;
     f.tilesX = (f.width + f.tileW - 1) / f.tileW;
     f.tilesY = (f.height + f.tileH - 1) / f.tileH;
     const uint64_t numTiles = (uint64_t)f.tilesX * f.tilesY;
@@ -1394,7 +1400,6 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
     {
         if (std::max(f.width, f.height) > kMaxLineExtent)
             return ctx->fail(SLG_ERR_INVALID_ARG, "line draws need a framebuffer of at most 10922 x 10922");
-        f.hasLines = 1;
         f.aliasEvents = reinterpret_cast<slg::AliasEvent*>(scratch + kOffAliases);
         f.aliasCount = reinterpret_cast<uint32_t*>(scratch + kOffCounters + 8);
         f.aliasCap = kNoAllocAliases;

@@ -95,6 +95,10 @@ constexpr uint32_t kRecordPoint = 1u << 5;
 constexpr uint32_t kRecordLine = 1u << 6;
 
 /* Per-launch scratch and framebuffer description. */
+/* Screen tile of launches that contain line draws: the raster kernels that
+ * carry line records are compiled for this tile size only. */
+constexpr int kLineTile = 32;
+
 /* A line whose last walk step (x = W on row y - 1) is stored at the address
  * of its first step (x = 0 on row y). SoftLight depth-tests line fragments
  * when it queues them and writes them when its 600-fragment queue is

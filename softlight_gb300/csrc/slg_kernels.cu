@@ -1392,7 +1392,9 @@ __global__ void __launch_bounds__(1024) tile_sort_kernel(const Frame f, int sort
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) f.entries[begin + i] = sKeys[i];
 }
 
-template <int TW, int TH, class Color>
+/* kLines: the instantiation that carries line records (launches with line
+ * draws, 32 x 32 tiles); the others keep the triangle loop's registers. */
+template <int TW, int TH, class Color, bool kLines>
 __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
 {
     typedef RasterLayout<TW, TH, Color> L;
@@ -1451,7 +1453,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 return;
             }
             const uint32_t flags = __float_as_uint(R[7].w);
-            if (flags & kRecordLine)
+            if (kLines && (flags & kRecordLine))
             {
                 /* the walk steps of this row whose pixels this thread owns:
                  * one step on a steep line, every fourth on a flat one */
@@ -1638,7 +1640,7 @@ __device__ __forceinline__ unsigned long long free_pack(int func, bool mask, flo
 /* Walks the scan-line tasks of the staged batch. kStore false: fold every
  * passing fragment into sBest; true: the fragment equal to its pixel's
  * sBest stores (b0, b1, b2, z). */
-template <int TW, int TH, bool kStore>
+template <int TW, int TH, bool kStore, bool kLines>
 __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sKey, const uint32_t* sPre, int cnt, int x0, int y0,
                                           int xLimit, int width, int height, int func, bool mask, const float* sD0,
                                           unsigned long long* sBest, float4* sB)
@@ -1655,7 +1657,7 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
         }
         const float4* R = sRec + lo * kRecordVec4;
         const int y = max(__float_as_int(R[6].x), y0) + (int)(i - sPre[lo]);
-        if (__float_as_uint(R[7].w) & kRecordLine)
+        if (kLines && (__float_as_uint(R[7].w) & kRecordLine))
         {
             /* the walk steps of this row; sB keeps (interp, 0, 0, z) */
             const LineWalk w = line_walk(R);
@@ -1749,7 +1751,7 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
     }
 }
 
-template <int TW, int TH, class Color>
+template <int TW, int TH, class Color, bool kLines>
 __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Frame f, int depthFunc, int depthMask)
 {
     typedef FreeLayout<TW, TH> L;
@@ -1813,9 +1815,9 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
         if (threadIdx.x == 0) sPre[0] = 0u;
         __syncthreads();
 
-        free_walk<TW, TH, false>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB);
+        free_walk<TW, TH, false, kLines>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB);
         __syncthreads();
-        free_walk<TW, TH, true>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB);
+        free_walk<TW, TH, true, kLines>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB);
     }
     __syncthreads();
 
@@ -1839,9 +1841,9 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
         {
             float4 o;
             const uint32_t kind = __float_as_uint(R[7].w);
-            const bool have = (kind & kRecordPoint) ? shade_point(f, dd, rec, o)
-                              : (kind & kRecordLine) ? shade_line(f, dd, rec, b.x, o)
-                                                     : shade(f, dd, rec, R[2].w, R[5], b.x, b.y, b.z, o);
+            const bool have = (kind & kRecordPoint)            ? shade_point(f, dd, rec, o)
+                              : (kLines && (kind & kRecordLine)) ? shade_line(f, dd, rec, b.x, o)
+                                                                 : shade(f, dd, rec, R[2].w, R[5], b.x, b.y, b.z, o);
             if (have)
             {
                 Color::write(f.color, gi, Color::store(o));
@@ -2050,13 +2052,13 @@ __global__ void clear_kernel(uint8_t* dst, size_t numTexels, int bytesPerTexel, 
 /*-----------------------------------------------------------------------------
  * Host-side launchers
 -----------------------------------------------------------------------------*/
-template <int TW, int TH, class Color>
+template <int TW, int TH, class Color, bool kLines>
 static cudaError_t launch_raster_t(const Frame& f, int numTiles, int keyCap, cudaStream_t s)
 {
     typedef RasterLayout<TW, TH, Color> L;
     if (f.orderFree)
     {
-        raster_free_kernel<TW, TH, Color><<<numTiles, kFreeThreads, FreeLayout<TW, TH>::bytes(), s>>>(f, f.freeDepthFunc, f.freeDepthMask);
+        raster_free_kernel<TW, TH, Color, kLines><<<numTiles, kFreeThreads, FreeLayout<TW, TH>::bytes(), s>>>(f, f.freeDepthFunc, f.freeDepthMask);
     }
     if (!f.orderFree || f.aliasCount)
     {
@@ -2064,7 +2066,7 @@ static cudaError_t launch_raster_t(const Frame& f, int numTiles, int keyCap, cud
          * order-free launch with line draws both rasters are queued and the
          * device decides (ordered_raster_runs) */
         tile_sort_kernel<<<numTiles, 1024, sizeof(uint32_t) * (size_t)keyCap, s>>>(f, keyCap);
-        raster_ordered_kernel<TW, TH, Color><<<numTiles, L::kThreads, L::ordered_bytes(), s>>>(f);
+        raster_ordered_kernel<TW, TH, Color, kLines><<<numTiles, L::kThreads, L::ordered_bytes(), s>>>(f);
     }
     if (f.aliasCount)
     {
@@ -2073,25 +2075,27 @@ static cudaError_t launch_raster_t(const Frame& f, int numTiles, int keyCap, cud
     return cudaGetLastError();
 }
 
-template <int TW, int TH, class Color>
+template <int TW, int TH, class Color, bool kLines>
 static cudaError_t attributes_t()
 {
     typedef RasterLayout<TW, TH, Color> L;
-    cudaError_t e = cudaFuncSetAttribute(raster_free_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FreeLayout<TW, TH>::bytes());
+    cudaError_t e = cudaFuncSetAttribute(raster_free_kernel<TW, TH, Color, kLines>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)FreeLayout<TW, TH>::bytes());
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(raster_ordered_kernel<TW, TH, Color>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::ordered_bytes());
+        e = cudaFuncSetAttribute(raster_ordered_kernel<TW, TH, Color, kLines>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::ordered_bytes());
     return e;
 }
 
 template <class Color>
 static cudaError_t attributes_c()
 {
-    cudaError_t e = attributes_t<8, 8, Color>();
-    if (e == cudaSuccess) e = attributes_t<16, 16, Color>();
-    if (e == cudaSuccess) e = attributes_t<32, 16, Color>();
-    if (e == cudaSuccess) e = attributes_t<32, 32, Color>();
-    if (e == cudaSuccess) e = attributes_t<64, 32, Color>();
-    if (e == cudaSuccess) e = attributes_t<64, 64, Color>();
+    cudaError_t e = attributes_t<8, 8, Color, false>();
+    if (e == cudaSuccess) e = attributes_t<16, 16, Color, false>();
+    if (e == cudaSuccess) e = attributes_t<32, 16, Color, false>();
+    if (e == cudaSuccess) e = attributes_t<32, 32, Color, false>();
+    if (e == cudaSuccess) e = attributes_t<64, 32, Color, false>();
+    if (e == cudaSuccess) e = attributes_t<64, 64, Color, false>();
+    if (e == cudaSuccess) e = attributes_t<kLineTile, kLineTile, Color, true>();
     return e;
 }
 
@@ -2107,12 +2111,18 @@ cudaError_t init_kernel_attributes(int keyCap)
 template <class Color>
 static cudaError_t launch_raster_c(const Frame& f, int numTiles, int keyCap, cudaStream_t s)
 {
-    if (f.tileW == 16 && f.tileH == 16) return launch_raster_t<16, 16, Color>(f, numTiles, keyCap, s);
-    if (f.tileW == 32 && f.tileH == 16) return launch_raster_t<32, 16, Color>(f, numTiles, keyCap, s);
-    if (f.tileW == 64 && f.tileH == 32) return launch_raster_t<64, 32, Color>(f, numTiles, keyCap, s);
-    if (f.tileW == 64 && f.tileH == 64) return launch_raster_t<64, 64, Color>(f, numTiles, keyCap, s);
-    if (f.tileW == 8 && f.tileH == 8) return launch_raster_t<8, 8, Color>(f, numTiles, keyCap, s);
-    return launch_raster_t<32, 32, Color>(f, numTiles, keyCap, s);
+    if (f.hasLines)
+    {
+        /* the host sets kLineTile x kLineTile tiles for launches with line draws */
+        if (f.tileW != kLineTile || f.tileH != kLineTile) return cudaErrorInvalidValue;
+        return launch_raster_t<kLineTile, kLineTile, Color, true>(f, numTiles, keyCap, s);
+    }
+    if (f.tileW == 16 && f.tileH == 16) return launch_raster_t<16, 16, Color, false>(f, numTiles, keyCap, s);
+    if (f.tileW == 32 && f.tileH == 16) return launch_raster_t<32, 16, Color, false>(f, numTiles, keyCap, s);
+    if (f.tileW == 64 && f.tileH == 32) return launch_raster_t<64, 32, Color, false>(f, numTiles, keyCap, s);
+    if (f.tileW == 64 && f.tileH == 64) return launch_raster_t<64, 64, Color, false>(f, numTiles, keyCap, s);
+    if (f.tileW == 8 && f.tileH == 8) return launch_raster_t<8, 8, Color, false>(f, numTiles, keyCap, s);
+    return launch_raster_t<32, 32, Color, false>(f, numTiles, keyCap, s);
 }
 
 cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEvent_t* ev)

@@ -272,6 +272,8 @@ def test_lines(ctxs, kw):
 @pytest.mark.parametrize("tile", [(8, 8), (32, 16), (64, 64)])
 @pytest.mark.parametrize("mode", [0, 1])
 def test_lines_all_tiles_and_modes(ctxs, tile, mode):
+    """Launches with line draws use 32 x 32 tiles whatever the context's tile
+    setting; both raster strategies."""
     g, o = ctxs
     g.set_tile_size(*tile)
     g.set_raster_mode(mode)
