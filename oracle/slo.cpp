@@ -1079,6 +1079,89 @@ static void process_lines(const RasterState& rs, const DrawState& ds, const Ibo*
     }
 }
 
+/* SL_TriRasterizer::render_wireframe (softlight/src/SL_TriRasterizer.cpp:116-204):
+ * per scan-line the left edge run of d0 pixels, then a jump to the right edge
+ * run; d0 / d1 are how far the span's ends moved since the row above (at
+ * least 1). Barycentrics are evaluated directly per pixel; each fragment is
+ * depth-tested when it is queued and written when the thread's queue of
+ * SL_SHADER_MAX_QUEUED_FRAGS (600) is flushed or the bin ends. */
+static void raster_wire_bin(const RasterState& rs, const Bin& bin, int rowStride, int rowPhase, uint64_t& frags)
+{
+    const Shader& sh = *rs.shaders[bin.drawIndex];
+    const V4* pts = bin.screen;
+    const int32_t bboxMinY = f2i(lm_min(lm_min(pts[0][1], pts[1][1]), pts[2][1]));
+    const int32_t bboxMaxY = f2i(lm_max(lm_max(pts[0][1], pts[1][1]), pts[2][1]));
+    int32_t y0 = bboxMinY;
+    if (rowStride > 1)
+    {
+        const int32_t n1 = rowStride - 1;
+        y0 += n1 - ((bboxMinY + (n1 - rowPhase)) % rowStride);
+    }
+
+    /* SL_ScanlineBounds::init / step (SL_ScanlineBounds.hpp:137-186,301-321) */
+    V4 p0 = pts[0], p1 = pts[1], p2 = pts[2];
+    if (p0[1] < p1[1]) std::swap(p0, p1);
+    if (p0[1] < p2[1]) std::swap(p0, p2);
+    if (p1[1] < p2[1]) std::swap(p1, p2);
+    const V4 p2p0 = sub(p2, p0), p2p1 = sub(p2, p1), p1p0 = sub(p1, p0);
+    const float v0y = p0[1], v1y = p1[1], v0x = p0[0], v1x = p1[0];
+    const float p20y = 1.f / p2p0[1];
+    const float p20x = p2p0[0];
+    const float p21xy = p2p1[0] * (1.f / p2p1[1]);
+    const float p10xy = p1p0[0] * (1.f / p1p0[1]);
+    const auto step = [&](float yf, int32_t& xMin, int32_t& xMax) {
+        const float d0 = yf - v0y, d1 = yf - v1y;
+        const float alpha = d0 * p20y;
+        const int32_t lo = f2i(p20x * alpha + v0x);
+        const int32_t sa = f2i(p21xy * d1 + v1x);
+        const int32_t sb = f2i(p10xy * d0 + v0x);
+        const int32_t hi = (d1 < 0.f) ? sa : sb;
+        xMin = (lo >= hi) ? hi : lo;
+        xMax = (lo >= hi) ? lo : hi;
+    };
+    /* int32 differences and abs as the reference computes them (wrapping) */
+    const auto absdiff = [](int32_t a, int32_t b) {
+        const uint32_t d = (uint32_t)a - (uint32_t)b;
+        return (int32_t)(((int32_t)d < 0) ? (0u - d) : d);
+    };
+
+    const V4* bcs = bin.bc;
+    const V4 depth = mk(pts[0][2], pts[1][2], pts[2][2], 0.f);
+    struct Frag { int32_t x, y; float z; V4 bc; };
+    std::vector<Frag> queue;
+    queue.reserve(600);
+    const auto flush = [&]() {
+        for (const Frag& q : queue) shade_fragment(rs, bin, q.x, q.y, q.z, q.bc, frags);
+        queue.clear();
+    };
+    for (int32_t y = y0; y < bboxMaxY; y += rowStride)
+    {
+        const float yf = (float)y;
+        const V4 bcY = mk(bcs[1][0] * yf + bcs[2][0], bcs[1][1] * yf + bcs[2][1], bcs[1][2] * yf + bcs[2][2], bcs[1][3] * 0.f + bcs[2][3]);
+        int32_t xMin0, xMax0, xMin1, xMax1;
+        step(yf, xMin0, xMax0);
+        step(yf - 1.f, xMin1, xMax1);
+        const int32_t d0 = std::max(absdiff(xMin0, xMin1), 1);
+        const int32_t d1 = std::max(absdiff(xMax0, xMax1), 1);
+        for (int32_t ix = 0, x = xMin0; (uint32_t)x < (uint32_t)xMax0; ++ix, ++x)
+        {
+            if (ix == d0)
+            {
+                x = std::max(xMin0, (int32_t)((uint32_t)xMax0 - (uint32_t)d1 - 1u));
+                continue;
+            }
+            const float xf = (float)x;
+            const V4 bc = mk(bcs[0][0] * xf + bcY[0], bcs[0][1] * xf + bcY[1], bcs[0][2] * xf + bcY[2], bcs[0][3] * 0.f + bcY[3]);
+            const float z = dot(depth, bc);
+            const float d = rs.depth[(size_t)x + (size_t)rs.width * y];
+            if (!depth_cmp(sh.depthTest, z, d)) continue;
+            queue.push_back({x, y, z, bc});
+            if (queue.size() == 600) flush();
+        }
+    }
+    flush();
+}
+
 static void order_bins(std::vector<Bin>& bins, bool blending)
 {
     if (!blending)
@@ -1627,7 +1710,7 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
         {
             const DrawItem& it = group[u.draw];
             const Vao& vao = ctx->vaos[it.mesh.vaoId];
-            const bool indexed = (it.mesh.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES);
+            const bool indexed = (it.mesh.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES || it.mesh.mode == SLG_RENDER_MODE_INDEXED_TRI_WIRE);
             const Ibo* ibo = (indexed && vao.ibo != SLG_INVALID_ID) ? &ctx->ibos[vao.ibo] : nullptr;
             if (indexed && !ibo) return ctx->fail(SLG_ERR_INVALID_ARG, "indexed draw without index buffer");
             const size_t begin = it.mesh.elementBegin, end = it.mesh.elementEnd;
@@ -1657,9 +1740,15 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
         ctx->lastBinList = bins;
         totalBins += bins.size();
 
+        const bool wire = !group.empty() && (group[0].mesh.mode == SLG_RENDER_MODE_TRI_WIRE ||
+                                             group[0].mesh.mode == SLG_RENDER_MODE_INDEXED_TRI_WIRE);
+        const auto raster = [&](const Bin& b, int stride, int phase, uint64_t& fr) {
+            if (wire) raster_wire_bin(rs, b, stride, phase, fr);
+            else raster_bin(rs, b, stride, phase, fr);
+        };
         if (nthreads == 1)
         {
-            for (const Bin& b : bins) raster_bin(rs, b, 1, 0, totalFrags);
+            for (const Bin& b : bins) raster(b, 1, 0, totalFrags);
         }
         else
         {
@@ -1668,7 +1757,7 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
             for (unsigned t = 0; t < nthreads; ++t)
             {
                 pool.emplace_back([&, t]() {
-                    for (const Bin& b : bins) raster_bin(rs, b, (int)nthreads, (int)t, frags[t]);
+                    for (const Bin& b : bins) raster(b, (int)nthreads, (int)t, frags[t]);
                 });
             }
             for (std::thread& th : pool) th.join();
@@ -1685,7 +1774,8 @@ static bool valid_tri_mesh(const slg_mesh* m)
 {
     return m && (m->mode == SLG_RENDER_MODE_TRIANGLES || m->mode == SLG_RENDER_MODE_INDEXED_TRIANGLES ||
                  m->mode == SLG_RENDER_MODE_POINTS || m->mode == SLG_RENDER_MODE_INDEXED_POINTS ||
-                 m->mode == SLG_RENDER_MODE_LINES || m->mode == SLG_RENDER_MODE_INDEXED_LINES);
+                 m->mode == SLG_RENDER_MODE_LINES || m->mode == SLG_RENDER_MODE_INDEXED_LINES ||
+                 m->mode == SLG_RENDER_MODE_TRI_WIRE || m->mode == SLG_RENDER_MODE_INDEXED_TRI_WIRE);
 }
 
 int slo_draw(slo_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId)
@@ -1695,7 +1785,7 @@ int slo_draw(slo_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId)
 
 int slo_draw_instanced(slo_context* ctx, const slg_mesh* m, size_t numInstances, size_t shaderId, size_t fboId)
 {
-    if (!valid_tri_mesh(m)) return ctx->fail(SLG_ERR_INVALID_ARG, "only point, line and triangle render modes are supported");
+    if (!valid_tri_mesh(m)) return ctx->fail(SLG_ERR_INVALID_ARG, "unsupported render mode");
     std::vector<std::vector<DrawItem>> groups(1);
     groups[0].push_back({*m, numInstances, shaderId, false});
     return run_draws(ctx, groups, fboId);
@@ -1707,7 +1797,7 @@ int slo_draw_multiple(slo_context* ctx, const slg_mesh* meshes, size_t numMeshes
     std::vector<std::vector<DrawItem>> groups(1);
     for (size_t i = 0; i < numMeshes; ++i)
     {
-        if (!valid_tri_mesh(&meshes[i])) return ctx->fail(SLG_ERR_INVALID_ARG, "only point, line and triangle render modes are supported");
+        if (!valid_tri_mesh(&meshes[i])) return ctx->fail(SLG_ERR_INVALID_ARG, "unsupported render mode");
         groups[0].push_back({meshes[i], 1, shaderId, true});
     }
     return run_draws(ctx, groups, fboId);
@@ -1718,7 +1808,7 @@ int slo_draw_batch(slo_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, s
     std::vector<std::vector<DrawItem>> groups;
     for (size_t i = 0; i < numCmds; ++i)
     {
-        if (!valid_tri_mesh(&cmds[i].mesh)) return ctx->fail(SLG_ERR_INVALID_ARG, "only point, line and triangle render modes are supported");
+        if (!valid_tri_mesh(&cmds[i].mesh)) return ctx->fail(SLG_ERR_INVALID_ARG, "unsupported render mode");
         groups.push_back({{cmds[i].mesh, cmds[i].numInstances, cmds[i].shaderId, false}});
     }
     return run_draws(ctx, groups, fboId);

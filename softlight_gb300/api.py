@@ -20,6 +20,7 @@ INVALID_ID = (1 << 64) - 1
 VERTEX_DATA_BYTE, VERTEX_DATA_SHORT, VERTEX_DATA_INT, VERTEX_DATA_LONG, VERTEX_DATA_FLOAT = 0, 1, 2, 3, 4
 RENDER_MODE_POINTS, RENDER_MODE_INDEXED_POINTS = 0x01, 0x03
 RENDER_MODE_LINES, RENDER_MODE_INDEXED_LINES = 0x04, 0x0C
+RENDER_MODE_TRI_WIRE, RENDER_MODE_INDEXED_TRI_WIRE = 0x50, 0x70
 RENDER_MODE_TRIANGLES, RENDER_MODE_INDEXED_TRIANGLES = 0x10, 0x30
 CULL_BACK_FACE, CULL_FRONT_FACE, CULL_OFF = 0, 1, 2
 DEPTH_TEST_OFF, DEPTH_TEST_LESS_THAN, DEPTH_TEST_LESS_EQUAL, DEPTH_TEST_GREATER_THAN = 0, 1, 2, 3

@@ -271,7 +271,7 @@ int check_status(slg_context* ctx)
 
     const int32_t zero[4] = {0, 0, 0, 0};
     cudaMemcpy(ctx->status.ptr, zero, sizeof(zero), cudaMemcpyHostToDevice);
-    std::string msg = "device-side overflow:";
+    std::string msg = "device-side status:";
     if (bits & slg::kStatusEntryOverflow)
     {
         const uint64_t want = (uint64_t)ctx->hostStatus[1] * 2;
@@ -292,6 +292,10 @@ int check_status(slg_context* ctx)
     if (bits & slg::kStatusAliasOverflow)
     {
         msg += " full-width line aliases (at most 4096 per launch, 4096 records per aliased pixel)";
+    }
+    if (bits & slg::kStatusWireQueue)
+    {
+        msg += " blended wireframe triangle of more than 600 edge fragments visiting a pixel twice (queue flush order not reproduced)";
     }
     msg += " (the affected draws were skipped; buffers have been grown)";
     return ctx->fail(SLG_ERR_OVERFLOW, msg);
@@ -415,14 +419,27 @@ uint64_t render_mode_vertices(int mode)
         case SLG_RENDER_MODE_LINES:
         case SLG_RENDER_MODE_INDEXED_LINES:     return 2;
         case SLG_RENDER_MODE_TRIANGLES:
-        case SLG_RENDER_MODE_INDEXED_TRIANGLES: return 3;
+        case SLG_RENDER_MODE_INDEXED_TRIANGLES:
+        case SLG_RENDER_MODE_TRI_WIRE:
+        case SLG_RENDER_MODE_INDEXED_TRI_WIRE:  return 3;
         default:                                return 0;
     }
 }
 
 bool render_mode_indexed(int mode)
 {
-    return mode == SLG_RENDER_MODE_INDEXED_POINTS || mode == SLG_RENDER_MODE_INDEXED_LINES || mode == SLG_RENDER_MODE_INDEXED_TRIANGLES;
+    return mode == SLG_RENDER_MODE_INDEXED_POINTS || mode == SLG_RENDER_MODE_INDEXED_LINES || mode == SLG_RENDER_MODE_INDEXED_TRIANGLES ||
+           mode == SLG_RENDER_MODE_INDEXED_TRI_WIRE;
+}
+
+uint8_t render_mode_prim(int mode)
+{
+    switch (render_mode_vertices(mode))
+    {
+        case 1:  return slg::kPrimPoint;
+        case 2:  return slg::kPrimLine;
+        default: return (mode == SLG_RENDER_MODE_TRI_WIRE || mode == SLG_RENDER_MODE_INDEXED_TRI_WIRE) ? slg::kPrimWire : slg::kPrimTriangle;
+    }
 }
 
 /* Host-side bounds checks of everything a draw's kernels will read: the
@@ -502,7 +519,7 @@ int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, Draw
     if (m.vaoId >= ctx->vaos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid vao id");
     const uint64_t perPrim = render_mode_vertices(m.mode);
     if (perPrim == 0)
-        return ctx->fail(SLG_ERR_INVALID_ARG, "only point, line and triangle render modes are supported");
+        return ctx->fail(SLG_ERR_INVALID_ARG, "unsupported render mode");
     const Shader& sh = ctx->shaders[req.shaderId];
     const Vao& vao = ctx->vaos[m.vaoId];
     if (vao.vbo == SLG_INVALID_ID || !ctx->vbos[vao.vbo].buf.ptr) return ctx->fail(SLG_ERR_INVALID_ARG, "vao has no vertex buffer");
@@ -526,7 +543,7 @@ int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, Draw
     d.elementBegin = m.elementBegin;
     d.numElements = (m.elementEnd > m.elementBegin) ? (m.elementEnd - m.elementBegin) : 0;
     d.numTris = (d.numElements + perPrim - 1) / perPrim;
-    d.prim = (perPrim == 1) ? slg::kPrimPoint : (perPrim == 2) ? slg::kPrimLine : slg::kPrimTriangle;
+    d.prim = render_mode_prim(m.mode);
     d.numInstances = std::max<size_t>(1, req.numInstances);
     d.slotBase = slotBase;
     d.primBase = req.primBase;
@@ -642,13 +659,15 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     for (size_t i = 0; i < n; ++i)
     {
         if (descs[i].prim == slg::kPrimLine) f.hasLines = 1;
+        if (descs[i].prim == slg::kPrimWire) f.hasWire = 1;
     }
     f.width = depthTex.w;
     f.height = depthTex.h;
-    /* launches with line draws use the line-carrying raster, compiled for
-     * one tile size */
-    f.tileW = f.hasLines ? slg::kLineTile : ctx->tileW;
-    f.tileH = f.hasLines ? slg::kLineTile : ctx->tileH;
+    /* launches with line or wireframe draws use the raster that carries
+     * those records, compiled for one tile size */
+    const bool edges = f.hasLines || f.hasWire;
+    f.tileW = edges ? slg::kLineTile : ctx->tileW;
+    f.tileH = edges ? slg::kLineTile : ctx->tileH;
     f.tilesX = (f.width + f.tileW - 1) / f.tileW;
     f.tilesY = (f.height + f.tileH - 1) / f.tileH;
     const uint64_t numTiles = (uint64_t)f.tilesX * f.tilesY;
@@ -713,8 +732,8 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
 
     if (fbo.visEnabled)
     {
-        if (f.hasLines)
-            return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map takes triangle and point draws only");
+        if (f.hasLines || f.hasWire)
+            return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map takes filled triangle and point draws only");
         if (!f.orderFree)
             return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map takes opaque draws only (no blending, one depth rule)");
         if (fbo.vis.bytes < (size_t)f.width * f.height * sizeof(uint32_t))
@@ -1385,10 +1404,11 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
     Frame f;
     std::memset(&f, 0, sizeof(f));
     f.hasLines = (desc->prim == slg::kPrimLine) ? 1 : 0;
+    f.hasWire = (desc->prim == slg::kPrimWire) ? 1 : 0;
     f.width = depthTex.w;
     f.height = depthTex.h;
-    f.tileW = f.hasLines ? slg::kLineTile : ctx->tileW;
-    f.tileH = f.hasLines ? slg::kLineTile : ctx->tileH;
+    f.tileW = (f.hasLines || f.hasWire) ? slg::kLineTile : ctx->tileW;
+    f.tileH = (f.hasLines || f.hasWire) ? slg::kLineTile : ctx->tileH;
     f.tilesX = (f.width + f.tileW - 1) / f.tileW;
     f.tilesY = (f.height + f.tileH - 1) / f.tileH;
     const uint64_t numTiles = (uint64_t)f.tilesX * f.tilesY;

@@ -86,17 +86,19 @@ enum PrimKind
 {
     kPrimTriangle = 0,
     kPrimPoint = 1,
-    kPrimLine = 2
+    kPrimLine = 2,
+    kPrimWire = 3     /* triangles drawn as wireframe */
 };
 
-/* record r7.w: depth test | depth mask << 4 | one of these bits for a point
- * or a line record (none for a triangle) */
+/* record r7.w: depth test | depth mask << 4 | one of these bits for a point,
+ * a line or a wireframe triangle record (none for a filled triangle) */
 constexpr uint32_t kRecordPoint = 1u << 5;
 constexpr uint32_t kRecordLine = 1u << 6;
+constexpr uint32_t kRecordWire = 1u << 7;
 
 /* Per-launch scratch and framebuffer description. */
-/* Screen tile of launches that contain line draws: the raster kernels that
- * carry line records are compiled for this tile size only. */
+/* Screen tile of launches that contain line or wireframe draws: the raster
+ * kernels that carry those records are compiled for this tile size only. */
 constexpr int kLineTile = 32;
 
 /* A line whose last walk step (x = W on row y - 1) is stored at the address
@@ -161,6 +163,9 @@ struct Frame
      * the line set-up runs (kept apart from the triangle variant's registers) */
     int32_t hasLines;
 
+    /* some draw of the launch is a wireframe draw (SL_RENDER_MODE_TRI_WIRE) */
+    int32_t hasWire;
+
     /* line address aliases (AliasEvent); null without line draws. Order-free
      * launches take the ordered raster when any alias was logged. */
     AliasEvent* aliasEvents;
@@ -177,7 +182,8 @@ enum StatusBits
     kStatusEntryOverflow = 1,
     kStatusOvfOverflow = 2,
     kStatusTileOverflow = 4,
-    kStatusAliasOverflow = 8
+    kStatusAliasOverflow = 8,
+    kStatusWireQueue = 16
 };
 
 /*-----------------------------------------------------------------------------

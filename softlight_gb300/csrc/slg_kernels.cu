@@ -159,6 +159,16 @@ __device__ __forceinline__ void make_record(const float4 p0, const float4 p1, co
                            __uint_as_float((uint32_t)(primIndex >> 32)), __uint_as_float(depthFlags));
 }
 
+/* r7.w of a triangle record: depth test, depth mask, wireframe bit */
+__device__ __forceinline__ uint32_t record_flags(const DrawDesc& d)
+{
+    return (uint32_t)d.depthTest | ((uint32_t)d.depthMask << 4) | (d.prim == kPrimWire ? kRecordWire : 0u);
+}
+
+/* Flags blended wireframe triangles whose queue flush points matter
+ * (defined with the wireframe raster below). */
+__device__ __noinline__ void wire_queue_check(const Frame& f, const float4* R);
+
 /* Inclusive tile range touched by a record; empty when tx1 < tx0 or ty1 < ty0. */
 struct TileRange { int tx0, tx1, ty0, ty1; };
 
@@ -385,7 +395,8 @@ __device__ __noinline__ uint32_t clip_and_emit(const Frame& f, const DrawDesc& d
             continue;
         }
         Record rec;
-        make_record(a, b, c, drawIndex, primIndex, (uint32_t)d.depthTest | ((uint32_t)d.depthMask << 4), rec);
+        make_record(a, b, c, drawIndex, primIndex, record_flags(d), rec);
+        if (d.prim == kPrimWire && d.blend != SLG_BLEND_OFF) wire_queue_check(f, rec.r);
         const uint64_t recIndex = f.numSlots + base + sub;
         store_record(f, recIndex, rec);
         store_varyings(f, recIndex, nv, newVarys, newVarys + (i + 1) * 4, newVarys + (i + 2) * 4);
@@ -847,7 +858,8 @@ __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, Ti
         if (bin_visible(s0, s1, s2))
         {
             Record rec;
-            make_record(s0, s1, s2, (uint32_t)di, primIndex, (uint32_t)d.depthTest | ((uint32_t)d.depthMask << 4), rec);
+            make_record(s0, s1, s2, (uint32_t)di, primIndex, record_flags(d), rec);
+            if (kLines && d.prim == kPrimWire && d.blend != SLG_BLEND_OFF) wire_queue_check(f, rec.r);
             store_record(f, slot, rec);
             tr = tile_range(rec.r[6], f);
             float4* dst = f.varyings + slot * kVaryingVec4;
@@ -1249,6 +1261,92 @@ __device__ __forceinline__ float chain_depth(const float4* R, const Chain& ch)
     return __fadd_rn((r3.w * ch.b0 + r4.w * ch.b1) + r5.x * ch.b2, 0.f * r2.w);
 }
 
+/*-----------------------------------------------------------------------------
+ * Wireframe (SL_TriRasterizer::render_wireframe, SL_TriRasterizer.cpp:116-204):
+ * the same triangle records; per scan-line the left run of d0 pixels from the
+ * span's start and, when the span is longer, the right run
+ * [max(xMin, xMax - d1 - 1) + 1, xMax), where d0 / d1 are how far the span's
+ * ends moved since the row above (at least 1). The runs overlap on narrow
+ * rows: those pixels are visited twice with the same fragment. Barycentrics
+ * are evaluated directly per pixel, bc = bc0 * x + (bc1 * y + bc2).
+-----------------------------------------------------------------------------*/
+constexpr uint32_t kFragQueue = 600;      /* SL_SHADER_MAX_QUEUED_FRAGS */
+
+struct WireRow { int a0, a1, b0, b1; };   /* runs [a0, a1) and [b0, b1) */
+
+__device__ __forceinline__ int abs_diff_wrap(int32_t a, int32_t b)
+{
+    const uint32_t d = (uint32_t)a - (uint32_t)b;
+    return (int)(((int32_t)d < 0) ? (0u - d) : d);
+}
+
+__device__ __forceinline__ WireRow wire_row(const float4* R, float yf)
+{
+    WireRow w;
+    w.a0 = w.a1 = w.b0 = w.b1 = 0;
+    const Span s0 = scanline_span(R[0], R[1], yf);
+    if (!((uint32_t)s0.xMin < (uint32_t)s0.xMax))
+    {
+        return w;
+    }
+    const Span s1 = scanline_span(R[0], R[1], yf - 1.f);
+    const int d0 = max(abs_diff_wrap(s0.xMin, s1.xMin), 1);
+    const int d1 = max(abs_diff_wrap(s0.xMax, s1.xMax), 1);
+    const long long reach = (long long)s0.xMin + d0;
+    w.a0 = s0.xMin;
+    if (reach < (long long)s0.xMax)
+    {
+        w.a1 = (int)reach;
+        w.b0 = max(s0.xMin, (int)((uint32_t)s0.xMax - (uint32_t)d1 - 1u)) + 1;
+        w.b1 = s0.xMax;
+    }
+    else
+    {
+        w.a1 = s0.xMax;
+    }
+    return w;
+}
+
+/* visits of pixel x on a wire row: 0, 1 or 2 */
+__device__ __forceinline__ int wire_visits(const WireRow& w, int x)
+{
+    return (x >= w.a0 && x < w.a1 ? 1 : 0) + (x >= w.b0 && x < w.b1 ? 1 : 0);
+}
+
+/* direct barycentrics and depth of pixel x on the row whose bcY is given */
+__device__ __forceinline__ float wire_fragment(const float4* R, float bcY0, float bcY1, float bcY2, int x, float& b0, float& b1, float& b2)
+{
+    const float4 r2 = R[2], r3 = R[3], r4 = R[4], r5 = R[5];
+    const float xf = (float)x;
+    b0 = r2.x * xf + bcY0;
+    b1 = r2.y * xf + bcY1;
+    b2 = r2.z * xf + bcY2;
+    return __fadd_rn((r3.w * b0 + r4.w * b1) + r5.x * b2, 0.f * r2.w);
+}
+
+/* A blended wireframe triangle that visits some pixel twice and queues more
+ * than 600 fragments can have a queue flush between the two visits, after
+ * which the second is tested against the first one's write; that order is
+ * not replayed (the two visits are applied as one unflushed queue), so the
+ * launch reports kStatusWireQueue. */
+__device__ __noinline__ void wire_queue_check(const Frame& f, const float4* R)
+{
+    const int minY = __float_as_int(R[6].x), maxY = __float_as_int(R[6].y);
+    long long visits = 0;
+    bool twice = false;
+    for (int y = minY; y < maxY; ++y)
+    {
+        const WireRow w = wire_row(R, (float)y);
+        visits += (long long)(w.a1 - w.a0) + (long long)(w.b1 - w.b0);
+        twice = twice || (w.b1 > w.b0 && w.b0 < w.a1);
+        if (twice && visits > (long long)kFragQueue)
+        {
+            atomicOr(f.status, kStatusWireQueue);
+            return;
+        }
+    }
+}
+
 /* Perspective correction, varying interpolation and the fragment program of
  * SL_FragmentProcessor::flush_tri_fragments (SL_FragmentProcessor.cpp:463-529,
  * interpolate_tri_varyings :308-330). Returns whether colour is written. */
@@ -1500,6 +1598,50 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 }
                 return;
             }
+            if (kLines && (flags & kRecordWire))
+            {
+                /* this thread's pixels of the row's runs; a pixel visited twice
+                 * takes its fragment twice (both visits are tested against the
+                 * depth before the triangle: one unflushed queue) */
+                const WireRow wr = wire_row(R, yf);
+                const float bcY0 = R[3].x * yf + R[4].x, bcY1 = R[3].y * yf + R[4].y, bcY2 = R[3].z * yf + R[4].z;
+                const DrawDesc& dd = f.draws[__float_as_uint(R[7].x)];
+                const uint64_t rec = key_to_record(f, sRecKey[ri]);
+                const int lo = max(wr.a0, myX0);
+                const int xFirst = lo + ((myX0 - lo) & 3);
+                const int xEnd = min(max(wr.a1, wr.b1), xLimit);
+                for (int x = xFirst; x < xEnd; x += 4)
+                {
+                    const int n = wire_visits(wr, x);
+                    if (n == 0)
+                    {
+                        continue;
+                    }
+                    float b0, b1, b2;
+                    const float z = wire_fragment(R, bcY0, bcY1, bcY2, x, b0, b1, b2);
+                    const int idx = r * L::kStride + (x - x0);
+                    if (depth_cmp(flags & 0xF, z, sDepth[idx]))
+                    {
+                        float4 o;
+                        if (shade(f, dd, rec, R[2].w, R[5], b0, b1, b2, o) && f.color)
+                        {
+                            if (dd.blend != SLG_BLEND_OFF)
+                            {
+                                for (int v = 0; v < n; ++v) sColor[idx] = Color::store(blend_color(dd.blend, o, Color::load(sColor[idx])));
+                            }
+                            else
+                            {
+                                sColor[idx] = Color::store(o);
+                            }
+                        }
+                        if ((flags >> 4) & 1)
+                        {
+                            sDepth[idx] = z;
+                        }
+                    }
+                }
+                return;
+            }
             if (flags & kRecordPoint)
             {
                 const int px = __float_as_int(r6.z);
@@ -1693,6 +1835,39 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
             }
             continue;
         }
+        if (kLines && (__float_as_uint(R[7].w) & kRecordWire))
+        {
+            /* each visited pixel once: the left run, then the right run past it */
+            const float yf = (float)y;
+            const WireRow wr = wire_row(R, yf);
+            const float bcY0 = R[3].x * yf + R[4].x, bcY1 = R[3].y * yf + R[4].y, bcY2 = R[3].z * yf + R[4].z;
+            const uint32_t key = sKey[lo];
+            for (int run = 0; run < 2; ++run)
+            {
+                const int xa = max(run ? max(wr.b0, wr.a1) : wr.a0, x0);
+                const int xb = min(run ? wr.b1 : wr.a1, xLimit);
+                for (int x = xa; x < xb; ++x)
+                {
+                    float b0, b1, b2;
+                    const float z = wire_fragment(R, bcY0, bcY1, bcY2, x, b0, b1, b2);
+                    const int idx = (y - y0) * TW + (x - x0);
+                    if (!depth_cmp(func, z, sD0[idx]))
+                    {
+                        continue;
+                    }
+                    const unsigned long long p = free_pack(func, mask, z, key);
+                    if (kStore)
+                    {
+                        if (sBest[idx] == p) sB[idx] = make_float4(b0, b1, b2, z);
+                    }
+                    else
+                    {
+                        atomicMin(sBest + idx, p);
+                    }
+                }
+            }
+            continue;
+        }
         if (__float_as_uint(R[7].w) & kRecordPoint)
         {
             const int px = __float_as_int(R[6].z);
@@ -1872,7 +2047,6 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
 -----------------------------------------------------------------------------*/
 constexpr int kAliasThreads = 256;
 constexpr int kAliasKeys = 4096;          /* records covering one pixel (power of two) */
-constexpr uint32_t kLineQueue = 600;      /* SL_SHADER_MAX_QUEUED_FRAGS */
 
 template <class Color>
 __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_t* keys, int m)
@@ -1940,12 +2114,28 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
                     /* the last step: the first one is written before its test
                      * only if the queue was flushed in between */
                     const uint32_t queued = f.aliasEvents[tag - 1].queued + (depth_cmp(func, zh[0], before) ? 1u : 0u);
-                    if (queued < kLineQueue) against = before;
+                    if (queued < kFragQueue) against = before;
                 }
                 if (depth_cmp(func, zh[j], against))
                 {
                     put(dd, shade_line(f, dd, rec, ih[j], o), o);
                     if (mask) depth = zh[j];
+                }
+            }
+        }
+        else if (flags & kRecordWire)
+        {
+            const WireRow wr = wire_row(R, yf);
+            const int n = wire_visits(wr, 0);
+            if (n > 0)
+            {
+                float b0, b1, b2;
+                const float z = wire_fragment(R, R[3].x * yf + R[4].x, R[3].y * yf + R[4].y, R[3].z * yf + R[4].z, 0, b0, b1, b2);
+                if (depth_cmp(func, z, depth))
+                {
+                    const bool have = shade(f, dd, rec, R[2].w, R[5], b0, b1, b2, o);
+                    for (int v = 0; v < ((dd.blend != SLG_BLEND_OFF) ? n : 1); ++v) put(dd, have, o);
+                    if (mask) depth = z;
                 }
             }
         }
@@ -2111,9 +2301,9 @@ cudaError_t init_kernel_attributes(int keyCap)
 template <class Color>
 static cudaError_t launch_raster_c(const Frame& f, int numTiles, int keyCap, cudaStream_t s)
 {
-    if (f.hasLines)
+    if (f.hasLines || f.hasWire)
     {
-        /* the host sets kLineTile x kLineTile tiles for launches with line draws */
+        /* the host sets kLineTile x kLineTile tiles for launches with line or wireframe draws */
         if (f.tileW != kLineTile || f.tileH != kLineTile) return cudaErrorInvalidValue;
         return launch_raster_t<kLineTile, kLineTile, Color, true>(f, numTiles, keyCap, s);
     }
@@ -2137,7 +2327,7 @@ cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEven
     if (f.numSlots > 0)
     {
         const unsigned blocks = (unsigned)((f.numSlots + vsBlock - 1) / vsBlock);
-        if (f.hasLines) vs_setup_kernel<true><<<blocks, vsBlock, 0, s>>>(f);
+        if (f.hasLines || f.hasWire) vs_setup_kernel<true><<<blocks, vsBlock, 0, s>>>(f);
         else vs_setup_kernel<false><<<blocks, vsBlock, 0, s>>>(f);
         clip_kernel<<<152 * 4, 128, 0, s>>>(f);
     }

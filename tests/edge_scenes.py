@@ -10,9 +10,10 @@ from softlight_gb300 import scenes as S
 def random_soup(ctx, num_tris=300, width=96, height=80, seed=11, blend=A.BLEND_OFF,
                 depth_test=A.DEPTH_TEST_LESS_THAN, depth_mask=A.DEPTH_MASK_ON, cull=A.CULL_BACK_FACE,
                 color_type=A.COLOR_RGBA_8U, program=A.PROGRAM_VCOLOR_TEX_ALPHA, indexed=None, clear_depth=1.0,
-                max_area=None):
+                max_area=None, wire=False, num_instances=1):
     """Triangle soup like the c3 workload at a small size, with the pipeline
-    state as parameters. indexed: None (non-indexed) or a numpy index dtype."""
+    state as parameters. indexed: None (non-indexed) or a numpy index dtype;
+    wire: draw the triangles as wireframe (SL_RENDER_MODE_[INDEXED_]TRI_WIRE)."""
     s = S.Scene(ctx, f"soup_{seed}", width, height, color_type=color_type)
     verts, proj = S.soup_triangles(num_tris, width, height, seed=seed)
     if max_area is not None:
@@ -33,17 +34,20 @@ def random_soup(ctx, num_tris=300, width=96, height=80, seed=11, blend=A.BLEND_O
         tex = s.add_texture_rgbaf(S.value_noise(64, 64, seed=seed, octaves=2).astype(np.float32))
     else:
         tex = s.add_texture_rgba8(S.to_rgba8(S.value_noise(64, 64, seed=seed, octaves=2, alpha=1.0)))
+    if wire:
+        mesh.mode = A.RENDER_MODE_TRI_WIRE if indexed is None else A.RENDER_MODE_INDEXED_TRI_WIRE
     ub = S.vcolor_uniforms(proj, tex)
     sh = s.add_shader(program, 2, ub, cull=cull, depth_test=depth_test, depth_mask=depth_mask, blend=blend)
-    s.draws.append((mesh, 1, sh))
+    s.draws.append((mesh, num_instances, sh))
     s.num_triangles = num_tris
     s.clear_depth = clear_depth
     return s
 
 
-def big_triangles(ctx, width=300, height=200, seed=5):
+def big_triangles(ctx, width=300, height=200, seed=5, wire=False, blend=A.BLEND_OFF):
     """A few triangles spanning many tiles (long catch-up chains), one of
-    them screen-filling, plus equal-depth overlaps (order ties)."""
+    them screen-filling, plus equal-depth overlaps (order ties); optionally
+    as wireframe."""
     s = S.Scene(ctx, "big", width, height)
     rng = np.random.default_rng(seed)
     tris = []
@@ -61,7 +65,9 @@ def big_triangles(ctx, width=300, height=200, seed=5):
     mesh = s.add_mesh(verts, None, stride=36)
     tex = s.add_texture_rgba8(S.checker(32, 32, 4))
     proj = S.perspective(60.0, width / height, 0.1, 100.0)
-    sh = s.add_shader(A.PROGRAM_VCOLOR_TEX_ALPHA, 2, S.vcolor_uniforms(proj, tex), cull=A.CULL_OFF)
+    if wire:
+        mesh.mode = A.RENDER_MODE_TRI_WIRE
+    sh = s.add_shader(A.PROGRAM_VCOLOR_TEX_ALPHA, 2, S.vcolor_uniforms(proj, tex), cull=A.CULL_OFF, blend=blend)
     s.draws.append((mesh, 1, sh))
     s.num_triangles = len(tris)
     return s

@@ -47,6 +47,20 @@ SCENES = {
     "line_alias_wide_occluded": (E.line_alias_wide, dict(occluded=True)),
     "line_alias_wide_open": (E.line_alias_wide, dict(occluded=False)),
     "line_alias_wide_occluded_blend": (E.line_alias_wide, dict(occluded=True, blend=A.BLEND_ALPHA)),
+    "wire_soup_less": (E.random_soup, dict(wire=True)),
+    "wire_soup_u16_cull_off": (E.random_soup, dict(wire=True, cull=A.CULL_OFF, indexed=np.uint16, num_tris=120, seed=12)),
+    "wire_soup_blend_alpha": (E.random_soup, dict(wire=True, blend=A.BLEND_ALPHA, seed=13)),
+    "wire_soup_not_equal": (E.random_soup, dict(wire=True, depth_test=A.DEPTH_TEST_NOT_EQUAL, clear_depth=0.5, seed=14)),
+    "wire_soup_instanced_float": (E.random_soup, dict(wire=True, num_instances=2, color_type=A.COLOR_RGBA_FLOAT, seed=15)),
+    "wire_big_triangles": (E.big_triangles, dict(wire=True)),
+    "wire_big_blend_additive": (E.big_triangles, dict(wire=True, blend=A.BLEND_ADDITIVE)),
+}
+
+# Scenes whose draws the GPU path reports as not reproduced (SLError at
+# finish), with the reason: blended wireframe triangles of more than 600 edge
+# fragments that visit a pixel twice (the reference's queue flush points).
+GPU_REPORTED = {
+    "wire_big_blend_additive": "queue flush order",
 }
 
 

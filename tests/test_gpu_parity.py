@@ -341,3 +341,33 @@ def test_line_draw_rejections(gpu_lib):
     with pytest.raises(A.SLError):
         ctx.draw(wide.draws[0][0], wide.draws[0][2], wide.fbo)
     ctx.close()
+
+
+@pytest.mark.parametrize("kw", [
+    dict(num_tris=2000, width=320, height=240),
+    dict(num_tris=1500, width=320, height=240, depth_test=A.DEPTH_TEST_NOT_EQUAL, clear_depth=0.5, seed=92),
+    dict(num_tris=800, width=160, height=120, blend=A.BLEND_ALPHA, seed=93),
+    dict(num_tris=800, width=160, height=120, blend=A.BLEND_ADDITIVE, depth_mask=A.DEPTH_MASK_OFF,
+         color_type=A.COLOR_RGBA_FLOAT, seed=94),
+    dict(num_tris=600, width=200, height=150, cull=A.CULL_OFF, indexed=np.uint32, num_instances=2, seed=95),
+], ids=["less_2k", "not_equal", "blend_alpha", "additive_float_mask_off", "indexed_instanced"])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_wireframe(ctxs, kw, mode):
+    """SL_RENDER_MODE_TRI_WIRE: the edge runs of every scan-line, direct
+    barycentrics, pixels visited twice on narrow rows (blended twice)."""
+    g, o = ctxs
+    g.set_raster_mode(mode)
+    sg, so = render_both(E.random_soup, g, o, wire=True, **kw)
+    compare_scenes(sg, so, f"wire mode {mode}")
+
+
+def test_wireframe_queue_order_reported(gpu_lib):
+    """A blended wireframe triangle of more than 600 edge fragments that
+    visits a pixel twice is reported (SLError at finish), not silently drawn
+    with a different queue flush order."""
+    ctx = gpu_lib.Context()
+    s = E.big_triangles(ctx, wire=True, blend=A.BLEND_ADDITIVE)
+    with pytest.raises(A.SLError, match="queue flush order"):
+        s.render()
+        ctx.finish()
+    ctx.close()
