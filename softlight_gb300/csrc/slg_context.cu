@@ -295,7 +295,7 @@ int check_status(slg_context* ctx)
     }
     if (bits & slg::kStatusWireQueue)
     {
-        msg += " blended wireframe triangle of more than 600 edge fragments visiting a pixel twice (queue flush order not reproduced)";
+        msg += " blended wireframe triangle revisiting a pixel after 600 queued fragments (queue flush order not reproduced)";
     }
     msg += " (the affected draws were skipped; buffers have been grown)";
     return ctx->fail(SLG_ERR_OVERFLOW, msg);

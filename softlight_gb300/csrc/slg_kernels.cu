@@ -1324,26 +1324,27 @@ __device__ __forceinline__ float wire_fragment(const float4* R, float bcY0, floa
     return __fadd_rn((r3.w * b0 + r4.w * b1) + r5.x * b2, 0.f * r2.w);
 }
 
-/* A blended wireframe triangle that visits some pixel twice and queues more
- * than 600 fragments can have a queue flush between the two visits, after
- * which the second is tested against the first one's write; that order is
- * not replayed (the two visits are applied as one unflushed queue), so the
- * launch reports kStatusWireQueue. */
+/* A blended wireframe triangle can have a queue flush between the two
+ * visits of a pixel, after which the second is tested against the first
+ * one's write. That needs 600 queued fragments before the second visit, which
+ * comes right after the row's left run; when some row with a revisited pixel
+ * has that many visits before it, the order is not replayed (the two visits
+ * are applied as one unflushed queue) and the launch reports
+ * kStatusWireQueue. */
 __device__ __noinline__ void wire_queue_check(const Frame& f, const float4* R)
 {
     const int minY = __float_as_int(R[6].x), maxY = __float_as_int(R[6].y);
     long long visits = 0;
-    bool twice = false;
     for (int y = minY; y < maxY; ++y)
     {
         const WireRow w = wire_row(R, (float)y);
-        visits += (long long)(w.a1 - w.a0) + (long long)(w.b1 - w.b0);
-        twice = twice || (w.b1 > w.b0 && w.b0 < w.a1);
-        if (twice && visits > (long long)kFragQueue)
+        const bool twice = w.b1 > w.b0 && w.b0 < w.a1;
+        if (twice && visits + (long long)(w.a1 - w.a0) >= (long long)kFragQueue)
         {
             atomicOr(f.status, kStatusWireQueue);
             return;
         }
+        visits += (long long)(w.a1 - w.a0) + (long long)(w.b1 - w.b0);
     }
 }
 

@@ -243,6 +243,24 @@ def mixed_prims(ctx, width=160, height=120, batched=False, blend_lines=False, se
     return s
 
 
+def wire_queue(ctx, blend=A.BLEND_ADDITIVE, width=700, height=80):
+    """One blended wireframe triangle with a long top edge and a sharp bottom
+    vertex: its scan-lines near the vertex are narrower than the edges' moves,
+    so their pixels are visited twice, after more than 600 queued fragments,
+    where SoftLight's queue may be flushed between the two visits."""
+    s = S.Scene(ctx, "wire_queue", width, height)
+    pts = [(20.0, 10.0), (680.0, 10.0), (350.0, 70.0)]
+    verts = np.zeros((3, 9), np.float32)
+    for i, (x, y) in enumerate(pts):
+        verts[i, :3] = (2.0 * x / width - 1.0, 2.0 * y / height - 1.0, 0.5)
+    mesh = s.add_mesh(verts, None, stride=36)
+    mesh.mode = A.RENDER_MODE_TRI_WIRE
+    sh = s.add_shader(A.PROGRAM_FLAT_COLOR, 0, S.flat_uniforms(np.eye(4), (0.3, 0.2, 0.1, 0.5)),
+                      cull=A.CULL_OFF, depth_test=A.DEPTH_TEST_LESS_THAN, depth_mask=A.DEPTH_MASK_ON, blend=blend)
+    s.draws.append((mesh, 1, sh))
+    return s
+
+
 LINE_ALIAS_PIXEL = (10, 0)   # (row, column) that both ends of line_alias's line address
 
 

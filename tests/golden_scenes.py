@@ -54,13 +54,14 @@ SCENES = {
     "wire_soup_instanced_float": (E.random_soup, dict(wire=True, num_instances=2, color_type=A.COLOR_RGBA_FLOAT, seed=15)),
     "wire_big_triangles": (E.big_triangles, dict(wire=True)),
     "wire_big_blend_additive": (E.big_triangles, dict(wire=True, blend=A.BLEND_ADDITIVE)),
+    "wire_queue_additive": (E.wire_queue, dict()),
 }
 
 # Scenes whose draws the GPU path reports as not reproduced (SLError at
-# finish), with the reason: blended wireframe triangles of more than 600 edge
-# fragments that visit a pixel twice (the reference's queue flush points).
+# finish), with the reason: a blended wireframe triangle revisits a pixel
+# after 600 queued fragments (the reference's queue flush points).
 GPU_REPORTED = {
-    "wire_big_blend_additive": "queue flush order",
+    "wire_queue_additive": "queue flush order",
 }
 
 

@@ -362,12 +362,18 @@ def test_wireframe(ctxs, kw, mode):
 
 
 def test_wireframe_queue_order_reported(gpu_lib):
-    """A blended wireframe triangle of more than 600 edge fragments that
-    visits a pixel twice is reported (SLError at finish), not silently drawn
-    with a different queue flush order."""
+    """A blended wireframe triangle that revisits a pixel after 600 queued
+    fragments is reported (SLError at finish), not silently drawn with
+    another queue flush order; opaque, the same triangle is exact."""
     ctx = gpu_lib.Context()
-    s = E.big_triangles(ctx, wire=True, blend=A.BLEND_ADDITIVE)
+    s = E.wire_queue(ctx)
     with pytest.raises(A.SLError, match="queue flush order"):
         s.render()
         ctx.finish()
     ctx.close()
+
+
+def test_wireframe_queue_scene_opaque_exact(ctxs):
+    g, o = ctxs
+    sg, so = render_both(E.wire_queue, g, o, blend=A.BLEND_OFF)
+    compare_scenes(sg, so, "wire queue opaque")
