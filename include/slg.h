@@ -232,8 +232,10 @@ int slg_clear_depth_buffer(slg_context* ctx, size_t fboId, double depth);
 
 /* SL_Context::draw / draw_instanced / draw_multiple
  * (softlight/include/softlight/SL_Context.hpp:215-225; softlight/src/SL_Context.cpp:714-740).
- * Render modes: [INDEXED_]TRIANGLES, [INDEXED_]LINES and [INDEXED_]POINTS;
- * TRI_WIRE is rejected (SLG_ERR_INVALID_ARG). A partial last primitive reads
+ * Render modes: [INDEXED_]TRIANGLES, [INDEXED_]TRI_WIRE, [INDEXED_]LINES and
+ * [INDEXED_]POINTS. A blended wireframe triangle that revisits a pixel after
+ * 600 queued fragments is reported at finish (SLG_ERR_OVERFLOW: the
+ * reference's queue flush order is not reproduced). A partial last primitive reads
  * the elements after elementEnd as the reference does, and those reads are
  * validated. Line draws need a framebuffer of at most 10922 x 10922 (the
  * reference's int16 Bresenham error term) and no visibility map. */
