@@ -103,7 +103,8 @@ enum slg_shader_program
     SLG_PROGRAM_BLINN_PHONG_INST   = 2, /* textured Blinn-Phong, 4 point lights, per-instance matrices */
     SLG_PROGRAM_VCOLOR_TEX_ALPHA   = 3, /* vertex colour x RGBA8 texture, vertex alpha */
     SLG_PROGRAM_VCOLOR_TEXF        = 4, /* vertex colour x RGBA float texture */
-    SLG_PROGRAM_FLAT_COLOR         = 5  /* uniform colour, no varyings */
+    SLG_PROGRAM_FLAT_COLOR         = 5, /* uniform colour, no varyings */
+    SLG_PROGRAM_GBUFFER            = 6  /* up to four outputs for multiple render targets (vertex-colour layout) */
 };
 
 /* SL_Mesh (softlight/include/softlight/SL_Mesh.hpp:30-39), same layout */

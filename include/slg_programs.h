@@ -66,8 +66,8 @@ typedef struct slg_blinn_uniforms
     uint32_t instanceBufferId; /* vertex buffer of column-major float 4x4 model matrices, one per instance */
 } slg_blinn_uniforms;
 
-/* SLG_PROGRAM_VCOLOR_TEX_ALPHA and SLG_PROGRAM_VCOLOR_TEXF. Vertex layout
- * (binding 0): float pos[3], rgba[4], uv[2]; 36-byte stride. */
+/* SLG_PROGRAM_VCOLOR_TEX_ALPHA, SLG_PROGRAM_VCOLOR_TEXF and SLG_PROGRAM_GBUFFER.
+ * Vertex layout (binding 0): float pos[3], rgba[4], uv[2]; 36-byte stride. */
 typedef struct slg_vcolor_uniforms
 {
     float    mvpMatrix[16];
@@ -231,6 +231,24 @@ SLG_HD bool slg_fs_vcolor_texf(const Env& env, const slg_v4* varyings, slg_v4* o
     const slg_vcolor_uniforms* u = (const slg_vcolor_uniforms*)env.uniforms();
     const slg_v4 t = env.sample_rgbaf(u->textureId, varyings[1].x, varyings[1].y);
     outputs[0] = slg_mul(varyings[0], t);
+    return true;
+}
+
+/* SLG_PROGRAM_GBUFFER: the outputs of a deferred G-buffer pass, one per
+ * render target (SL_FragmentParam::pOutputs[0..3]): vertex colour x texture
+ * (vertex alpha), the texture sample, the vertex colour, and the uv as
+ * (u, v, u*v, 1). The texture is RGBA8 (slg_vcolor_uniforms::textureId). */
+template <class Env>
+SLG_HD bool slg_fs_gbuffer(const Env& env, const slg_v4* varyings, slg_v4* outputs)
+{
+    const slg_vcolor_uniforms* u = (const slg_vcolor_uniforms*)env.uniforms();
+    const slg_v4 c = varyings[0];
+    const slg_v4 uv = varyings[1];
+    const slg_v4 t = env.sample_rgba8(u->textureId, uv.x, uv.y);
+    outputs[0] = slg_make_v4(c.x * t.x, c.y * t.y, c.z * t.z, c.w);
+    outputs[1] = t;
+    outputs[2] = c;
+    outputs[3] = slg_make_v4(uv.x, uv.y, uv.x * uv.y, 1.f);
     return true;
 }
 

@@ -101,7 +101,8 @@ math::vec4 vs_callback(SL_VertexParam& param)
         case SLG_PROGRAM_LAMBERT_TEX:      r = slg_vs_lambert(env, param.vertId, param.instanceId, vary); break;
         case SLG_PROGRAM_BLINN_PHONG_INST: r = slg_vs_blinn(env, param.vertId, param.instanceId, vary); break;
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
-        case SLG_PROGRAM_VCOLOR_TEXF:      r = slg_vs_vcolor(env, param.vertId, param.instanceId, vary); break;
+        case SLG_PROGRAM_VCOLOR_TEXF:
+        case SLG_PROGRAM_GBUFFER:          r = slg_vs_vcolor(env, param.vertId, param.instanceId, vary); break;
         default:                           r = slg_vs_flat(env, param.vertId, param.instanceId, vary); break;
     }
     const int n = (P == SLG_PROGRAM_BLINN_PHONG_INST) ? 3 : (P == SLG_PROGRAM_FLAT_COLOR ? 0 : 2);
@@ -129,6 +130,7 @@ bool fs_callback(SL_FragmentParam& param)
         case SLG_PROGRAM_BLINN_PHONG_INST: r = slg_fs_blinn(env, vary, outs); break;
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA: r = slg_fs_vcolor_tex_alpha(env, vary, outs); break;
         case SLG_PROGRAM_VCOLOR_TEXF:      r = slg_fs_vcolor_texf(env, vary, outs); break;
+        case SLG_PROGRAM_GBUFFER:          r = slg_fs_gbuffer(env, vary, outs); break;
         default:                           r = slg_fs_flat(env, vary, outs); break;
     }
     for (int i = 0; i < 4; ++i)
@@ -150,6 +152,7 @@ VsFn vs_for(uint32_t p)
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA: return vs_callback<SLG_PROGRAM_VCOLOR_TEX_ALPHA>;
         case SLG_PROGRAM_VCOLOR_TEXF:      return vs_callback<SLG_PROGRAM_VCOLOR_TEXF>;
         case SLG_PROGRAM_FLAT_COLOR:       return vs_callback<SLG_PROGRAM_FLAT_COLOR>;
+        case SLG_PROGRAM_GBUFFER:          return vs_callback<SLG_PROGRAM_GBUFFER>;
         default:                           return nullptr;
     }
 }
@@ -163,6 +166,7 @@ FsFn fs_for(uint32_t p)
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA: return fs_callback<SLG_PROGRAM_VCOLOR_TEX_ALPHA>;
         case SLG_PROGRAM_VCOLOR_TEXF:      return fs_callback<SLG_PROGRAM_VCOLOR_TEXF>;
         case SLG_PROGRAM_FLAT_COLOR:       return fs_callback<SLG_PROGRAM_FLAT_COLOR>;
+        case SLG_PROGRAM_GBUFFER:          return fs_callback<SLG_PROGRAM_GBUFFER>;
         default:                           return nullptr;
     }
 }

@@ -318,7 +318,8 @@ static V4 run_vs(uint32_t program, const Env& env, uint64_t vertId, uint64_t ins
         case SLG_PROGRAM_LAMBERT_TEX:      r = slg_vs_lambert(env, vertId, instId, vary); break;
         case SLG_PROGRAM_BLINN_PHONG_INST: r = slg_vs_blinn(env, vertId, instId, vary); break;
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
-        case SLG_PROGRAM_VCOLOR_TEXF:      r = slg_vs_vcolor(env, vertId, instId, vary); break;
+        case SLG_PROGRAM_VCOLOR_TEXF:
+        case SLG_PROGRAM_GBUFFER:          r = slg_vs_vcolor(env, vertId, instId, vary); break;
         default:                           r = slg_vs_flat(env, vertId, instId, vary); break;
     }
     for (int i = 0; i < 4; ++i) varyings[i] = from_slg(vary[i]);
@@ -336,6 +337,7 @@ static bool run_fs(uint32_t program, const Env& env, const V4* varyings, V4* out
         case SLG_PROGRAM_BLINN_PHONG_INST: r = slg_fs_blinn(env, vary, outs); break;
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA: r = slg_fs_vcolor_tex_alpha(env, vary, outs); break;
         case SLG_PROGRAM_VCOLOR_TEXF:      r = slg_fs_vcolor_texf(env, vary, outs); break;
+        case SLG_PROGRAM_GBUFFER:          r = slg_fs_gbuffer(env, vary, outs); break;
         default:                           r = slg_fs_flat(env, vary, outs); break;
     }
     for (int i = 0; i < 4; ++i) outputs[i] = from_slg(outs[i]);
@@ -1409,10 +1411,15 @@ int slo_blit_read(slo_context* ctx, size_t inId, int dstType, uint16_t dstW, uin
 
 size_t slo_create_framebuffer(slo_context* ctx) { ctx->fbos.emplace_back(); return ctx->fbos.size() - 1; }
 
+/* SL_Framebuffer::reserve_color_buffers (softlight/src/SL_Framebuffer.cpp:821-845) */
 int slo_fbo_reserve_color_buffers(slo_context* ctx, size_t fbo, unsigned n)
 {
-    if (fbo >= ctx->fbos.size() || n > 4) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo or count");
-    ctx->fbos[fbo].numColors = n;
+    if (fbo >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo");
+    Fbo& b = ctx->fbos[fbo];
+    if (n == b.numColors) return SLG_OK;
+    if (n < 1 || n > 4) return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer has 1 to 4 colour attachments");
+    for (size_t& c : b.colors) c = SLG_INVALID_ID;
+    b.numColors = n;
     return SLG_OK;
 }
 
@@ -1558,13 +1565,15 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
     rs.depth = reinterpret_cast<float*>(depthTex.bytes.data());
     rs.width = depthTex.w;
     rs.height = depthTex.h;
-    rs.numOutputs = fbo.numColors;
-    for (unsigned i = 0; i < fbo.numColors; ++i)
+    rs.numOutputs = 0;
+    for (unsigned i = 0; i < fbo.numColors && i < 4; ++i)
     {
+        if (fbo.colors[i] == SLG_INVALID_ID || fbo.colors[i] >= ctx->textures.size()) break;
         Texture& t = *ctx->textures[fbo.colors[i]];
         rs.colors[i].bytes = t.bytes.data();
         rs.colors[i].type = t.type;
         rs.colors[i].w = t.w;
+        rs.numOutputs = i + 1;
     }
 
     /* SL_TriProcessor::execute viewport set-up (SL_TriProcessor.cpp:672-675,

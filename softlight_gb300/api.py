@@ -29,7 +29,7 @@ DEPTH_MASK_OFF, DEPTH_MASK_ON = 0, 1
 BLEND_OFF, BLEND_ALPHA, BLEND_PREMULTIPLED_ALPHA, BLEND_ADDITIVE, BLEND_SCREEN = 0, 1, 2, 3, 4
 COLOR_R_FLOAT, COLOR_RGBA_8U, COLOR_RGBA_FLOAT = 5, 21, 26
 PROGRAM_LAMBERT_TEX, PROGRAM_BLINN_PHONG_INST, PROGRAM_VCOLOR_TEX_ALPHA = 1, 2, 3
-PROGRAM_VCOLOR_TEXF, PROGRAM_FLAT_COLOR = 4, 5
+PROGRAM_VCOLOR_TEXF, PROGRAM_FLAT_COLOR, PROGRAM_GBUFFER = 4, 5, 6
 
 BYTES_PER_COLOR = {COLOR_R_FLOAT: 4, COLOR_RGBA_8U: 4, COLOR_RGBA_FLOAT: 16}
 

@@ -82,7 +82,7 @@ size_t index_bytes(int type)
     }
 }
 
-bool valid_program(uint32_t p) { return p >= SLG_PROGRAM_LAMBERT_TEX && p <= SLG_PROGRAM_FLAT_COLOR; }
+bool valid_program(uint32_t p) { return p >= SLG_PROGRAM_LAMBERT_TEX && p <= SLG_PROGRAM_GBUFFER; }
 
 constexpr size_t kDescRing = 4096;
 constexpr uint64_t kMaxSlots = (1ull << 29) - 1; /* keys are slot << 3 | sub in 32 bits */
@@ -399,7 +399,8 @@ size_t program_vertex_bytes(uint32_t program)
         case SLG_PROGRAM_LAMBERT_TEX:
         case SLG_PROGRAM_BLINN_PHONG_INST: return 32;
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
-        case SLG_PROGRAM_VCOLOR_TEXF:      return 36;
+        case SLG_PROGRAM_VCOLOR_TEXF:
+        case SLG_PROGRAM_GBUFFER:          return 36;
         default:                           return 12;
     }
 }
@@ -483,6 +484,7 @@ int validate_draw(slg_context* ctx, const Shader& sh, const Vao& vao, const slg_
             if (!texture_ok(ctx, tex, SLG_COLOR_RGBA_8U)) return ctx->fail(SLG_ERR_INVALID_ARG, "uniform textureId is not an RGBA8 texture");
             break;
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
+        case SLG_PROGRAM_GBUFFER:
             std::memcpy(&tex, u + offsetof(slg_vcolor_uniforms, textureId), 4);
             if (!texture_ok(ctx, tex, SLG_COLOR_RGBA_8U)) return ctx->fail(SLG_ERR_INVALID_ARG, "uniform textureId is not an RGBA8 texture");
             break;
@@ -511,6 +513,34 @@ struct DrawRequest
     size_t shaderId;
     uint64_t primBase;
 };
+
+/* Colour attachments of the framebuffer into the frame (SL_Framebuffer::
+ * build_output_functions, softlight/src/SL_Framebuffer.cpp:1207-1231). A
+ * program writing more outputs than the framebuffer has attachments would
+ * call unset output functions in the reference; here it is rejected. */
+int bind_attachments(slg_context* ctx, const Fbo& fbo, const Texture& depthTex, const DrawDesc* descs, size_t n, Frame& f)
+{
+    f.numColors = 0;
+    for (unsigned k = 0; k < fbo.numColors && k < 4; ++k)
+    {
+        if (fbo.colors[k] == SLG_INVALID_ID || fbo.colors[k] >= ctx->textures.size()) break;
+        const Texture& t = ctx->textures[fbo.colors[k]];
+        if (!t.buf.ptr) break;
+        if (t.w != depthTex.w || t.h != depthTex.h) return ctx->fail(SLG_ERR_INVALID_ARG, "colour and depth attachments differ in size");
+        if (t.type != SLG_COLOR_RGBA_8U && t.type != SLG_COLOR_RGBA_FLOAT && t.type != SLG_COLOR_R_FLOAT)
+            return ctx->fail(SLG_ERR_INVALID_ARG, "unsupported colour attachment format");
+        f.colors[k] = static_cast<uint8_t*>(t.buf.ptr);
+        f.colorTypes[k] = t.type;
+        f.numColors = (int32_t)k + 1;
+    }
+    for (size_t i = 0; i < n; ++i)
+    {
+        if (f.numColors > 0 && descs[i].numOutputs > f.numColors)
+            return ctx->fail(SLG_ERR_INVALID_ARG, "the fragment program writes more outputs than the framebuffer has colour attachments");
+        if (f.numColors > 1 && descs[i].numOutputs > 1) f.hasMrt = 1;
+    }
+    return SLG_OK;
+}
 
 int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, DrawDesc& d, uint64_t& numSlots)
 {
@@ -663,9 +693,10 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     }
     f.width = depthTex.w;
     f.height = depthTex.h;
-    /* launches with line or wireframe draws use the raster that carries
-     * those records, compiled for one tile size */
-    const bool edges = f.hasLines || f.hasWire;
+    if ((r = bind_attachments(ctx, fbo, depthTex, descs, n, f))) return r;
+    /* launches with line or wireframe draws or several render targets use
+     * the raster that carries those, compiled for one tile size */
+    const bool edges = f.hasLines || f.hasWire || f.hasMrt;
     f.tileW = edges ? slg::kLineTile : ctx->tileW;
     f.tileH = edges ? slg::kLineTile : ctx->tileH;
     f.tilesX = (f.width + f.tileW - 1) / f.tileW;
@@ -1053,10 +1084,16 @@ int slg_blit_read(slg_context* ctx, size_t inId, int dstType, uint16_t dstW, uin
 
 size_t slg_create_framebuffer(slg_context* ctx) { ctx->fbos.emplace_back(); return ctx->fbos.size() - 1; }
 
+/* SL_Framebuffer::reserve_color_buffers (softlight/src/SL_Framebuffer.cpp:
+ * 821-845): 1..4 attachments; a new count detaches every colour attachment. */
 int slg_fbo_reserve_color_buffers(slg_context* ctx, size_t fbo, unsigned n)
 {
-    if (!id_ok(fbo, ctx->fbos.size()) || n > 4) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo or count");
-    ctx->fbos[fbo].numColors = n;
+    if (!id_ok(fbo, ctx->fbos.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo");
+    Fbo& b = ctx->fbos[fbo];
+    if (n == b.numColors) return SLG_OK;
+    if (n < 1 || n > 4) return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer has 1 to 4 colour attachments");
+    for (size_t& c : b.colors) c = SLG_INVALID_ID;
+    b.numColors = n;
     return SLG_OK;
 }
 
@@ -1407,8 +1444,9 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
     f.hasWire = (desc->prim == slg::kPrimWire) ? 1 : 0;
     f.width = depthTex.w;
     f.height = depthTex.h;
-    f.tileW = (f.hasLines || f.hasWire) ? slg::kLineTile : ctx->tileW;
-    f.tileH = (f.hasLines || f.hasWire) ? slg::kLineTile : ctx->tileH;
+    if ((r = bind_attachments(ctx, fbo, depthTex, desc, 1, f))) return r;
+    f.tileW = (f.hasLines || f.hasWire || f.hasMrt) ? slg::kLineTile : ctx->tileW;
+    f.tileH = (f.hasLines || f.hasWire || f.hasMrt) ? slg::kLineTile : ctx->tileH;
     f.tilesX = (f.width + f.tileW - 1) / f.tileW;
     f.tilesY = (f.height + f.tileH - 1) / f.tileH;
     const uint64_t numTiles = (uint64_t)f.tilesX * f.tilesY;

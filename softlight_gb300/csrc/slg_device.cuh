@@ -97,8 +97,9 @@ constexpr uint32_t kRecordLine = 1u << 6;
 constexpr uint32_t kRecordWire = 1u << 7;
 
 /* Per-launch scratch and framebuffer description. */
-/* Screen tile of launches that contain line or wireframe draws: the raster
- * kernels that carry those records are compiled for this tile size only. */
+/* Screen tile of launches that contain line or wireframe draws or write
+ * several render targets: the raster kernels that carry those are compiled
+ * for this tile size only. */
 constexpr int kLineTile = 32;
 
 /* A line whose last walk step (x = W on row y - 1) is stored at the address
@@ -114,7 +115,8 @@ struct AliasEvent
     uint32_t pixel;     /* linear index of the shared pixel (column 0) */
     uint32_t queued;    /* steps 0 < k < dx that passed the depth test */
     float    depth0;    /* the pixel's depth before the launch */
-    uint4    color0;    /* the pixel's colour bits before the launch */
+    uint4    color0;    /* the pixel's colour bits before the launch, attachment 0 */
+    uint4    colorN[3]; /* and attachments 1..3 */
 };
 
 struct Frame
@@ -165,6 +167,13 @@ struct Frame
 
     /* some draw of the launch is a wireframe draw (SL_RENDER_MODE_TRI_WIRE) */
     int32_t hasWire;
+
+    /* colour attachments 0..numColors-1 (colors[0] == color); hasMrt: some
+     * draw writes more than one of them (outputs k -> attachment k) */
+    uint8_t* colors[4];
+    int32_t  colorTypes[4];
+    int32_t  numColors;
+    int32_t  hasMrt;
 
     /* line address aliases (AliasEvent); null without line draws. Order-free
      * launches take the ordered raster when any alias was logged. */
@@ -312,7 +321,8 @@ __device__ __forceinline__ slg_v4 run_vertex_program(uint32_t program, const Dev
         case SLG_PROGRAM_LAMBERT_TEX:      return slg_vs_lambert(env, vertId, instanceId, varyings);
         case SLG_PROGRAM_BLINN_PHONG_INST: return slg_vs_blinn(env, vertId, instanceId, varyings);
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
-        case SLG_PROGRAM_VCOLOR_TEXF:      return slg_vs_vcolor(env, vertId, instanceId, varyings);
+        case SLG_PROGRAM_VCOLOR_TEXF:
+        case SLG_PROGRAM_GBUFFER:          return slg_vs_vcolor(env, vertId, instanceId, varyings);
         default:                           return slg_vs_flat(env, vertId, instanceId, varyings);
     }
 }
@@ -325,6 +335,7 @@ __device__ __forceinline__ bool run_fragment_program(uint32_t program, const Dev
         case SLG_PROGRAM_BLINN_PHONG_INST: return slg_fs_blinn(env, varyings, outputs);
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA: return slg_fs_vcolor_tex_alpha(env, varyings, outputs);
         case SLG_PROGRAM_VCOLOR_TEXF:      return slg_fs_vcolor_texf(env, varyings, outputs);
+        case SLG_PROGRAM_GBUFFER:          return slg_fs_gbuffer(env, varyings, outputs);
         default:                           return slg_fs_flat(env, varyings, outputs);
     }
 }

@@ -637,6 +637,16 @@ __device__ __forceinline__ uint32_t setup_line(const Frame& f, const DrawDesc& d
                 else c.x = reinterpret_cast<const uint32_t*>(f.color)[pix];
             }
             ev.color0 = c;
+            for (int k = 1; k < 4; ++k)
+            {
+                uint4 ck = make_uint4(0u, 0u, 0u, 0u);
+                if (k < f.numColors)
+                {
+                    if (f.colorTypes[k] == SLG_COLOR_RGBA_FLOAT) ck = reinterpret_cast<const uint4*>(f.colors[k])[pix];
+                    else ck.x = reinterpret_cast<const uint32_t*>(f.colors[k])[pix];
+                }
+                ev.colorN[k - 1] = ck;
+            }
             aliasTag = (int)e + 1;
         }
         else
@@ -764,32 +774,6 @@ __device__ __forceinline__ bool line_store_pixel(const LineWalk& w, int k, int w
     py = (int)(lin / (uint32_t)width);
     px = (int)(lin - (uint32_t)py * (uint32_t)width);
     return true;
-}
-
-/* SL_LineRasterizer's fragment shading (SL_FragmentProcessor.cpp:346-402,
- * interpolate_line_varyings :120-140): varyings mix(v0, v1, interp). */
-__device__ __forceinline__ bool shade_line(const Frame& f, const DrawDesc& dd, uint64_t rec, float interp, float4& out)
-{
-    slg_v4 vary[kMaxVaryings];
-    const float4* V = f.varyings + rec * kVaryingVec4;
-#pragma unroll
-    for (int vi = 0; vi < kMaxVaryings; ++vi)
-    {
-        if (vi < dd.numVaryings)
-        {
-            const float4 a = V[vi], b = V[4 + vi];
-            vary[vi] = slg_make_v4(mixf(a.x, b.x, interp), mixf(a.y, b.y, interp), mixf(a.z, b.z, interp), mixf(a.w, b.w, interp));
-        }
-        else
-        {
-            vary[vi] = slg_make_v4(0.f, 0.f, 0.f, 0.f);
-        }
-    }
-    slg_v4 outputs[4];
-    const DevEnv env = make_env(dd, f.tables);
-    const bool have = run_fragment_program(dd.fsProgram, env, vary, outputs);
-    out = to_f4(outputs[0]);
-    return have && dd.numOutputs > 0;
 }
 
 /* SL_LineRasterizer::render_line per pixel (SL_LineRasterizer.cpp:49-58):
@@ -1124,6 +1108,41 @@ __device__ __forceinline__ float4 blend_color(int mode, const float4 s, const fl
     return r;
 }
 
+/* A texel of an attachment of one of the supported colour formats, as the
+ * float4 the blend reads and from the float4 a fragment writes. */
+__device__ __forceinline__ float4 texel_load(int type, const uint8_t* p, size_t i)
+{
+    if (type == SLG_COLOR_RGBA_FLOAT) return ColorRGBAF::load(ColorRGBAF::read(p, i));
+    if (type == SLG_COLOR_R_FLOAT) return ColorRF::load(ColorRF::read(p, i));
+    return ColorRGBA8::load(ColorRGBA8::read(p, i));
+}
+
+__device__ __forceinline__ void texel_store(int type, uint8_t* p, size_t i, const float4 c)
+{
+    if (type == SLG_COLOR_RGBA_FLOAT) ColorRGBAF::write(p, i, ColorRGBAF::store(c));
+    else if (type == SLG_COLOR_R_FLOAT) ColorRF::write(p, i, ColorRF::store(c));
+    else ColorRGBA8::write(p, i, ColorRGBA8::store(c));
+}
+
+/* Outputs 1..3 of a fragment into colour attachments 1..3, blended per
+ * attachment: the reference's output mask writes pOutputs[k] to attachment k
+ * for every k below the program's output count (SL_FragmentProcessor.cpp:
+ * 376-395, SL_Framebuffer.cpp:1207-1231). reps: the fragment's visits. */
+__device__ __forceinline__ void emit_extra_outputs(const Frame& f, const DrawDesc& dd, size_t gi, const slg_v4* outputs, int reps)
+{
+    const int n = min((int)dd.numOutputs, f.numColors);
+    for (int k = 1; k < n; ++k)
+    {
+        uint8_t* p = f.colors[k];
+        const int t = f.colorTypes[k];
+        const float4 o = to_f4(outputs[k]);
+        for (int r = 0; r < reps; ++r)
+        {
+            texel_store(t, p, gi, (dd.blend != SLG_BLEND_OFF) ? blend_color(dd.blend, o, texel_load(t, p, gi)) : o);
+        }
+    }
+}
+
 __device__ __forceinline__ uint64_t key_to_record(const Frame& f, uint32_t key)
 {
     const uint64_t slot = key >> kSubShift;
@@ -1351,8 +1370,9 @@ __device__ __noinline__ void wire_queue_check(const Frame& f, const float4* R)
 /* Perspective correction, varying interpolation and the fragment program of
  * SL_FragmentProcessor::flush_tri_fragments (SL_FragmentProcessor.cpp:463-529,
  * interpolate_tri_varyings :308-330). Returns whether colour is written. */
+template <bool kExtra>
 __device__ __forceinline__ bool shade(const Frame& f, const DrawDesc& dd, uint64_t rec, float bcw, const float4 r5,
-                                      float b0, float b1, float b2, float4& out)
+                                      float b0, float b1, float b2, float4& out, size_t gi = 0, int reps = 1)
 {
     const float bp0 = b0 * r5.y, bp1 = b1 * r5.z, bp2 = b2 * r5.w;
     const float bp3 = bcw * 0.f;
@@ -1380,12 +1400,17 @@ __device__ __forceinline__ bool shade(const Frame& f, const DrawDesc& dd, uint64
     const DevEnv env = make_env(dd, f.tables);
     const bool have = run_fragment_program(dd.fsProgram, env, vary, outputs);
     out = to_f4(outputs[0]);
+    if (kExtra && have && f.numColors > 1)
+    {
+        emit_extra_outputs(f, dd, gi, outputs, reps);
+    }
     return have && dd.numOutputs > 0;
 }
 
 /* SL_PointRasterizer::render_point's shading (SL_PointRasterizer.cpp:59-90):
  * the point's varyings are handed to the fragment program unchanged. */
-__device__ __forceinline__ bool shade_point(const Frame& f, const DrawDesc& dd, uint64_t rec, float4& out)
+template <bool kExtra>
+__device__ __forceinline__ bool shade_point(const Frame& f, const DrawDesc& dd, uint64_t rec, float4& out, size_t gi = 0, int reps = 1)
 {
     slg_v4 vary[kMaxVaryings];
     const float4* V = f.varyings + rec * kVaryingVec4;
@@ -1399,6 +1424,42 @@ __device__ __forceinline__ bool shade_point(const Frame& f, const DrawDesc& dd, 
     const DevEnv env = make_env(dd, f.tables);
     const bool have = run_fragment_program(dd.fsProgram, env, vary, outputs);
     out = to_f4(outputs[0]);
+    if (kExtra && have && f.numColors > 1)
+    {
+        emit_extra_outputs(f, dd, gi, outputs, reps);
+    }
+    return have && dd.numOutputs > 0;
+}
+
+/* SL_LineRasterizer's fragment shading (SL_FragmentProcessor.cpp:346-402,
+ * interpolate_line_varyings :120-140): varyings mix(v0, v1, interp). */
+template <bool kExtra>
+__device__ __forceinline__ bool shade_line(const Frame& f, const DrawDesc& dd, uint64_t rec, float interp, float4& out, size_t gi = 0,
+                                           int reps = 1)
+{
+    slg_v4 vary[kMaxVaryings];
+    const float4* V = f.varyings + rec * kVaryingVec4;
+#pragma unroll
+    for (int vi = 0; vi < kMaxVaryings; ++vi)
+    {
+        if (vi < dd.numVaryings)
+        {
+            const float4 a = V[vi], b = V[4 + vi];
+            vary[vi] = slg_make_v4(mixf(a.x, b.x, interp), mixf(a.y, b.y, interp), mixf(a.z, b.z, interp), mixf(a.w, b.w, interp));
+        }
+        else
+        {
+            vary[vi] = slg_make_v4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+    slg_v4 outputs[4];
+    const DevEnv env = make_env(dd, f.tables);
+    const bool have = run_fragment_program(dd.fsProgram, env, vary, outputs);
+    out = to_f4(outputs[0]);
+    if (kExtra && have && f.numColors > 1)
+    {
+        emit_extra_outputs(f, dd, gi, outputs, reps);
+    }
     return have && dd.numOutputs > 0;
 }
 
@@ -1491,9 +1552,10 @@ __global__ void __launch_bounds__(1024) tile_sort_kernel(const Frame f, int sort
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) f.entries[begin + i] = sKeys[i];
 }
 
-/* kLines: the instantiation that carries line records (launches with line
- * draws, 32 x 32 tiles); the others keep the triangle loop's registers. */
-template <int TW, int TH, class Color, bool kLines>
+/* kGeneral: the instantiation that carries line and wireframe records and
+ * writes several render targets (such launches use kLineTile tiles); the
+ * others keep the triangle loop's registers. */
+template <int TW, int TH, class Color, bool kGeneral>
 __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
 {
     typedef RasterLayout<TW, TH, Color> L;
@@ -1552,7 +1614,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 return;
             }
             const uint32_t flags = __float_as_uint(R[7].w);
-            if (kLines && (flags & kRecordLine))
+            if (kGeneral && (flags & kRecordLine))
             {
                 /* the walk steps of this row whose pixels this thread owns:
                  * one step on a steep line, every fourth on a flat one */
@@ -1586,7 +1648,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                             atomicAdd(&f.aliasEvents[aliasTag - 1].queued, 1u);
                         }
                         float4 o;
-                        if (shade_line(f, dd, rec, interp, o) && f.color)
+                        if (shade_line<kGeneral>(f, dd, rec, interp, o, (size_t)px + (size_t)f.width * y) && f.color)
                         {
                             sColor[idx] = (dd.blend != SLG_BLEND_OFF) ? Color::store(blend_color(dd.blend, o, Color::load(sColor[idx])))
                                                                       : Color::store(o);
@@ -1599,7 +1661,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 }
                 return;
             }
-            if (kLines && (flags & kRecordWire))
+            if (kGeneral && (flags & kRecordWire))
             {
                 /* this thread's pixels of the row's runs; a pixel visited twice
                  * takes its fragment twice (both visits are tested against the
@@ -1624,7 +1686,8 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                     if (depth_cmp(flags & 0xF, z, sDepth[idx]))
                     {
                         float4 o;
-                        if (shade(f, dd, rec, R[2].w, R[5], b0, b1, b2, o) && f.color)
+                        if (shade<kGeneral>(f, dd, rec, R[2].w, R[5], b0, b1, b2, o, (size_t)x + (size_t)f.width * y,
+                                          (dd.blend != SLG_BLEND_OFF) ? n : 1) && f.color)
                         {
                             if (dd.blend != SLG_BLEND_OFF)
                             {
@@ -1656,7 +1719,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 {
                     const DrawDesc& dd = f.draws[__float_as_uint(R[7].x)];
                     float4 o;
-                    if (shade_point(f, dd, key_to_record(f, sRecKey[ri]), o) && f.color)
+                    if (shade_point<kGeneral>(f, dd, key_to_record(f, sRecKey[ri]), o, (size_t)px + (size_t)f.width * y) && f.color)
                     {
                         sColor[idx] = (dd.blend != SLG_BLEND_OFF) ? Color::store(blend_color(dd.blend, o, Color::load(sColor[idx])))
                                                                   : Color::store(o);
@@ -1684,7 +1747,8 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 {
                     const DrawDesc& dd = f.draws[drawIndex];
                     float4 o;
-                    if (shade(f, dd, key_to_record(f, sRecKey[ri]), R[2].w, R[5], ch.b0, ch.b1, ch.b2, o) && f.color)
+                    if (shade<kGeneral>(f, dd, key_to_record(f, sRecKey[ri]), R[2].w, R[5], ch.b0, ch.b1, ch.b2, o,
+                                      (size_t)ch.x + (size_t)f.width * y) && f.color)
                     {
                         sColor[idx] = (dd.blend != SLG_BLEND_OFF) ? Color::store(blend_color(dd.blend, o, Color::load(sColor[idx])))
                                                                   : Color::store(o);
@@ -1783,7 +1847,7 @@ __device__ __forceinline__ unsigned long long free_pack(int func, bool mask, flo
 /* Walks the scan-line tasks of the staged batch. kStore false: fold every
  * passing fragment into sBest; true: the fragment equal to its pixel's
  * sBest stores (b0, b1, b2, z). */
-template <int TW, int TH, bool kStore, bool kLines>
+template <int TW, int TH, bool kStore, bool kGeneral>
 __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sKey, const uint32_t* sPre, int cnt, int x0, int y0,
                                           int xLimit, int width, int height, int func, bool mask, const float* sD0,
                                           unsigned long long* sBest, float4* sB)
@@ -1800,7 +1864,7 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
         }
         const float4* R = sRec + lo * kRecordVec4;
         const int y = max(__float_as_int(R[6].x), y0) + (int)(i - sPre[lo]);
-        if (kLines && (__float_as_uint(R[7].w) & kRecordLine))
+        if (kGeneral && (__float_as_uint(R[7].w) & kRecordLine))
         {
             /* the walk steps of this row; sB keeps (interp, 0, 0, z) */
             const LineWalk w = line_walk(R);
@@ -1836,7 +1900,7 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
             }
             continue;
         }
-        if (kLines && (__float_as_uint(R[7].w) & kRecordWire))
+        if (kGeneral && (__float_as_uint(R[7].w) & kRecordWire))
         {
             /* each visited pixel once: the left run, then the right run past it */
             const float yf = (float)y;
@@ -1927,7 +1991,7 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
     }
 }
 
-template <int TW, int TH, class Color, bool kLines>
+template <int TW, int TH, class Color, bool kGeneral>
 __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Frame f, int depthFunc, int depthMask)
 {
     typedef FreeLayout<TW, TH> L;
@@ -1991,9 +2055,9 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
         if (threadIdx.x == 0) sPre[0] = 0u;
         __syncthreads();
 
-        free_walk<TW, TH, false, kLines>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB);
+        free_walk<TW, TH, false, kGeneral>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB);
         __syncthreads();
-        free_walk<TW, TH, true, kLines>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB);
+        free_walk<TW, TH, true, kGeneral>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB);
     }
     __syncthreads();
 
@@ -2017,9 +2081,9 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
         {
             float4 o;
             const uint32_t kind = __float_as_uint(R[7].w);
-            const bool have = (kind & kRecordPoint)            ? shade_point(f, dd, rec, o)
-                              : (kLines && (kind & kRecordLine)) ? shade_line(f, dd, rec, b.x, o)
-                                                                 : shade(f, dd, rec, R[2].w, R[5], b.x, b.y, b.z, o);
+            const bool have = (kind & kRecordPoint)            ? shade_point<kGeneral>(f, dd, rec, o, gi)
+                              : (kGeneral && (kind & kRecordLine)) ? shade_line<kGeneral>(f, dd, rec, b.x, o, gi)
+                                                                 : shade<kGeneral>(f, dd, rec, R[2].w, R[5], b.x, b.y, b.z, o, gi);
             if (have)
             {
                 Color::write(f.color, gi, Color::store(o));
@@ -2059,6 +2123,11 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
 
     /* the pixel's state before the launch */
     float depth = ev.depth0;
+    for (int k = 1; k < f.numColors; ++k)
+    {
+        if (f.colorTypes[k] == SLG_COLOR_RGBA_FLOAT) reinterpret_cast<uint4*>(f.colors[k])[gi] = ev.colorN[k - 1];
+        else reinterpret_cast<uint32_t*>(f.colors[k])[gi] = ev.colorN[k - 1].x;
+    }
     Stored color{};
     if (f.color)
     {
@@ -2119,7 +2188,7 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
                 }
                 if (depth_cmp(func, zh[j], against))
                 {
-                    put(dd, shade_line(f, dd, rec, ih[j], o), o);
+                    put(dd, shade_line<true>(f, dd, rec, ih[j], o, gi), o);
                     if (mask) depth = zh[j];
                 }
             }
@@ -2134,7 +2203,7 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
                 const float z = wire_fragment(R, R[3].x * yf + R[4].x, R[3].y * yf + R[4].y, R[3].z * yf + R[4].z, 0, b0, b1, b2);
                 if (depth_cmp(func, z, depth))
                 {
-                    const bool have = shade(f, dd, rec, R[2].w, R[5], b0, b1, b2, o);
+                    const bool have = shade<true>(f, dd, rec, R[2].w, R[5], b0, b1, b2, o, gi, (dd.blend != SLG_BLEND_OFF) ? n : 1);
                     for (int v = 0; v < ((dd.blend != SLG_BLEND_OFF) ? n : 1); ++v) put(dd, have, o);
                     if (mask) depth = z;
                 }
@@ -2145,7 +2214,7 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
             const float4 r6 = R[6];
             if (__float_as_int(r6.z) == 0 && __float_as_int(r6.x) == py && depth_cmp(func, R[0].z, depth))
             {
-                put(dd, shade_point(f, dd, rec, o), o);
+                put(dd, shade_point<true>(f, dd, rec, o, gi), o);
                 if (mask) depth = R[0].z;
             }
         }
@@ -2157,7 +2226,7 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
                 const float z = chain_depth(R, ch);
                 if (depth_cmp(func, z, depth))
                 {
-                    put(dd, shade(f, dd, rec, R[2].w, R[5], ch.b0, ch.b1, ch.b2, o), o);
+                    put(dd, shade<true>(f, dd, rec, R[2].w, R[5], ch.b0, ch.b1, ch.b2, o, gi), o);
                     if (mask) depth = z;
                 }
             }
@@ -2243,13 +2312,13 @@ __global__ void clear_kernel(uint8_t* dst, size_t numTexels, int bytesPerTexel, 
 /*-----------------------------------------------------------------------------
  * Host-side launchers
 -----------------------------------------------------------------------------*/
-template <int TW, int TH, class Color, bool kLines>
+template <int TW, int TH, class Color, bool kGeneral>
 static cudaError_t launch_raster_t(const Frame& f, int numTiles, int keyCap, cudaStream_t s)
 {
     typedef RasterLayout<TW, TH, Color> L;
     if (f.orderFree)
     {
-        raster_free_kernel<TW, TH, Color, kLines><<<numTiles, kFreeThreads, FreeLayout<TW, TH>::bytes(), s>>>(f, f.freeDepthFunc, f.freeDepthMask);
+        raster_free_kernel<TW, TH, Color, kGeneral><<<numTiles, kFreeThreads, FreeLayout<TW, TH>::bytes(), s>>>(f, f.freeDepthFunc, f.freeDepthMask);
     }
     if (!f.orderFree || f.aliasCount)
     {
@@ -2257,7 +2326,7 @@ static cudaError_t launch_raster_t(const Frame& f, int numTiles, int keyCap, cud
          * order-free launch with line draws both rasters are queued and the
          * device decides (ordered_raster_runs) */
         tile_sort_kernel<<<numTiles, 1024, sizeof(uint32_t) * (size_t)keyCap, s>>>(f, keyCap);
-        raster_ordered_kernel<TW, TH, Color, kLines><<<numTiles, L::kThreads, L::ordered_bytes(), s>>>(f);
+        raster_ordered_kernel<TW, TH, Color, kGeneral><<<numTiles, L::kThreads, L::ordered_bytes(), s>>>(f);
     }
     if (f.aliasCount)
     {
@@ -2266,14 +2335,14 @@ static cudaError_t launch_raster_t(const Frame& f, int numTiles, int keyCap, cud
     return cudaGetLastError();
 }
 
-template <int TW, int TH, class Color, bool kLines>
+template <int TW, int TH, class Color, bool kGeneral>
 static cudaError_t attributes_t()
 {
     typedef RasterLayout<TW, TH, Color> L;
-    cudaError_t e = cudaFuncSetAttribute(raster_free_kernel<TW, TH, Color, kLines>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(raster_free_kernel<TW, TH, Color, kGeneral>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)FreeLayout<TW, TH>::bytes());
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(raster_ordered_kernel<TW, TH, Color, kLines>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::ordered_bytes());
+        e = cudaFuncSetAttribute(raster_ordered_kernel<TW, TH, Color, kGeneral>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::ordered_bytes());
     return e;
 }
 
@@ -2302,9 +2371,9 @@ cudaError_t init_kernel_attributes(int keyCap)
 template <class Color>
 static cudaError_t launch_raster_c(const Frame& f, int numTiles, int keyCap, cudaStream_t s)
 {
-    if (f.hasLines || f.hasWire)
+    if (f.hasLines || f.hasWire || f.hasMrt)
     {
-        /* the host sets kLineTile x kLineTile tiles for launches with line or wireframe draws */
+        /* the host sets kLineTile x kLineTile tiles for these launches */
         if (f.tileW != kLineTile || f.tileH != kLineTile) return cudaErrorInvalidValue;
         return launch_raster_t<kLineTile, kLineTile, Color, true>(f, numTiles, keyCap, s);
     }

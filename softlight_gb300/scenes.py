@@ -257,6 +257,7 @@ class Scene:
         ctx.fbo_reserve_color_buffers(self.fbo, 1)
         ctx.fbo_attach_color_buffer(self.fbo, 0, self.color_tex)
         ctx.fbo_attach_depth_buffer(self.fbo, self.depth_tex)
+        self.attachments = [(self.color_tex, color_type)]
         self.clear_color = (0.0, 0.0, 0.0, 1.0)
         self.clear_depth = 1.0
         self.draws = []          # list of (kind, args)
@@ -266,6 +267,20 @@ class Scene:
         self.texture_bytes = 0
         self.geometry_bytes = 0
         self.blending = False
+
+    def set_color_attachments(self, types):
+        """Colour attachments 0..len(types)-1 of the given formats (multiple
+        render targets, SL_Framebuffer::reserve_color_buffers and
+        attach_color_buffer); attachment 0 replaces the default one."""
+        ctx = self.ctx
+        ctx.fbo_reserve_color_buffers(self.fbo, len(types))
+        self.attachments = []
+        for k, t in enumerate(types):
+            tex = ctx.create_texture()
+            ctx.texture_init(tex, t, self.width, self.height, 1)
+            ctx.fbo_attach_color_buffer(self.fbo, k, tex)
+            self.attachments.append((tex, t))
+        self.color_tex, self.color_type = self.attachments[0]
 
     def add_texture_rgba8(self, img):
         t = self.ctx.create_texture()
@@ -316,6 +331,8 @@ class Scene:
         ctx = self.ctx
         if clear:
             ctx.clear_framebuffer(self.fbo, 0, self.clear_color, self.clear_depth)
+            for k in range(1, len(self.attachments)):
+                ctx.clear_color_buffer(self.fbo, k, self.clear_color)
         if self.batched:
             cmds = [A.DrawCmd(m, n, s) for (m, n, s) in self.draws]
             ctx.draw_batch(cmds, self.fbo)
@@ -326,12 +343,16 @@ class Scene:
                 else:
                     ctx.draw_instanced(m, n, s, self.fbo)
 
-    def read_color(self):
-        if self.color_type == A.COLOR_RGBA_8U:
-            return self.ctx.texture_read(self.color_tex, (self.height, self.width, 4), np.uint8)
-        if self.color_type == A.COLOR_RGBA_FLOAT:
-            return self.ctx.texture_read(self.color_tex, (self.height, self.width, 4), np.float32)
-        return self.ctx.texture_read(self.color_tex, (self.height, self.width), np.float32)
+    def read_color(self, k=0):
+        tex, ctype = self.attachments[k]
+        if ctype == A.COLOR_RGBA_8U:
+            return self.ctx.texture_read(tex, (self.height, self.width, 4), np.uint8)
+        if ctype == A.COLOR_RGBA_FLOAT:
+            return self.ctx.texture_read(tex, (self.height, self.width, 4), np.float32)
+        return self.ctx.texture_read(tex, (self.height, self.width), np.float32)
+
+    def read_colors(self):
+        return [self.read_color(k) for k in range(len(self.attachments))]
 
     def read_depth(self):
         return self.ctx.texture_read(self.depth_tex, (self.height, self.width), np.float32)

@@ -261,6 +261,37 @@ def wire_queue(ctx, blend=A.BLEND_ADDITIVE, width=700, height=80):
     return s
 
 
+MRT_FORMATS = (A.COLOR_RGBA_8U, A.COLOR_RGBA_FLOAT, A.COLOR_R_FLOAT, A.COLOR_RGBA_8U)
+
+
+def mrt(ctx, types=MRT_FORMATS, num_outputs=4, prim="tri", blend=A.BLEND_OFF, depth_test=A.DEPTH_TEST_LESS_THAN,
+        num_tris=300, width=96, height=80, seed=101, single_after=False, batched=False):
+    """Multiple render targets: the G-buffer program writes num_outputs
+    outputs into colour attachments of the given formats (output k to
+    attachment k), as filled triangles, wireframe, lines or points of a
+    triangle soup. single_after adds a one-output draw into the same
+    framebuffer (it writes attachment 0 only)."""
+    s = S.Scene(ctx, f"mrt_{seed}", width, height)
+    s.set_color_attachments(list(types))
+    verts, proj = S.soup_triangles(num_tris, width, height, seed=seed)
+    mesh = s.add_mesh(verts, None, stride=36)
+    mesh.mode = {"tri": A.RENDER_MODE_TRIANGLES, "wire": A.RENDER_MODE_TRI_WIRE,
+                 "line": A.RENDER_MODE_LINES, "point": A.RENDER_MODE_POINTS}[prim]
+    tex = s.add_texture_rgba8(S.to_rgba8(S.value_noise(32, 32, seed=seed, octaves=2, alpha=1.0)))
+    sh = s.add_shader(A.PROGRAM_GBUFFER, 2, S.vcolor_uniforms(proj, tex), cull=A.CULL_OFF, depth_test=depth_test,
+                      blend=blend, num_outputs=num_outputs)
+    s.draws.append((mesh, 1, sh))
+    if single_after:
+        soup, proj2 = S.soup_triangles(num_tris // 2, width, height, seed=seed + 1)
+        mesh2 = s.add_mesh(soup, None, stride=36)
+        sh2 = s.add_shader(A.PROGRAM_VCOLOR_TEX_ALPHA, 2, S.vcolor_uniforms(proj2, tex), cull=A.CULL_OFF,
+                           depth_test=depth_test, blend=blend)
+        s.draws.append((mesh2, 1, sh2))
+    s.num_triangles = num_tris
+    s.batched = batched
+    return s
+
+
 LINE_ALIAS_PIXEL = (10, 0)   # (row, column) that both ends of line_alias's line address
 
 

@@ -48,7 +48,8 @@ def main():
         scene = builder(ctx, **kw)
         scene.render()
         color, depth = scene.read_color(), scene.read_depth()
-        np.savez_compressed(os.path.join(HERE, name + ".npz"), color=color, depth=depth)
+        extra = {f"color{k}": scene.read_color(k) for k in range(1, len(scene.attachments))}
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), color=color, depth=depth, **extra)
         index[name] = {"color_sha256": digest(color), "depth_sha256": digest(depth),
                        "shape": list(color.shape), "covered": int((depth < scene.clear_depth).sum())}
         ctx.close()

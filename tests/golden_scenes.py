@@ -55,6 +55,14 @@ SCENES = {
     "wire_big_triangles": (E.big_triangles, dict(wire=True)),
     "wire_big_blend_additive": (E.big_triangles, dict(wire=True, blend=A.BLEND_ADDITIVE)),
     "wire_queue_additive": (E.wire_queue, dict()),
+    "mrt_4_mixed_formats": (E.mrt, dict()),
+    "mrt_3_blend_alpha": (E.mrt, dict(types=(A.COLOR_RGBA_8U, A.COLOR_RGBA_8U, A.COLOR_RGBA_FLOAT), num_outputs=3,
+                                      blend=A.BLEND_ALPHA, seed=102)),
+    "mrt_2_of_3_then_single": (E.mrt, dict(types=(A.COLOR_RGBA_8U, A.COLOR_RGBA_FLOAT, A.COLOR_R_FLOAT), num_outputs=2,
+                                           seed=103, single_after=True)),
+    "mrt_wire_additive": (E.mrt, dict(prim="wire", blend=A.BLEND_ADDITIVE, seed=104)),
+    "mrt_lines": (E.mrt, dict(prim="line", types=(A.COLOR_RGBA_8U, A.COLOR_RGBA_FLOAT), num_outputs=2, seed=105)),
+    "mrt_points_premultiplied": (E.mrt, dict(prim="point", blend=A.BLEND_PREMULTIPLED_ALPHA, seed=106, num_tris=2000)),
 }
 
 # Scenes whose draws the GPU path reports as not reproduced (SLError at

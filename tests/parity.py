@@ -23,13 +23,21 @@ def render_both(builder, gpu_ctx, oracle_ctx, frames=1, **kw):
 
 
 def compare_scenes(sg, so, label=""):
-    cg, co = sg.read_color(), so.read_color()
+    """Depth bit-exact, then every colour attachment; returns the number of
+    colour values of attachment 0 that differ at all."""
     dg, do = sg.read_depth(), so.read_depth()
     # depth: bit-exact (covers coverage and depth-test outcomes). A NaN depth
     # (written by a zero-area triangle when the depth test is off) matches any
     # NaN: each ISA produces its own NaN payload (x86 sets the sign bit).
     bad = (dg.view(np.uint32) != do.view(np.uint32)) & ~(np.isnan(dg) & np.isnan(do))
     assert not bad.any(), f"{label}: {int(bad.sum())} depth texels differ, first at {np.argwhere(bad)[:3].tolist()}"
+    for k in range(1, len(sg.attachments)):
+        compare_colors(sg.read_color(k), so.read_color(k), f"{label} attachment {k}")
+    return compare_colors(sg.read_color(), so.read_color(), label)
+
+
+def compare_colors(cg, co, label=""):
+    """RGBA8 within 1 LSB, float within 1e-5 relative (NaN matches NaN)."""
     if cg.dtype == np.uint8:
         diff = np.abs(cg.astype(np.int16) - co.astype(np.int16))
         assert diff.max(initial=0) <= RGBA8_TOL, f"{label}: colour differs by {diff.max()} LSB at {np.argwhere(diff > RGBA8_TOL)[:3].tolist()}"

@@ -49,6 +49,9 @@ def test_oracle_matches_reference_golden(oracle_mod, name):
     c, d = scene.read_color(), scene.read_depth()
     assert same(d, gd), f"{name}: depth differs from the reference in {int((d != gd).sum())} texels"
     assert same(c, gc), f"{name}: colour differs from the reference"
+    fixture = np.load(os.path.join(GOLDEN, name + ".npz"))
+    for k in range(1, len(scene.attachments)):
+        assert same(scene.read_color(k), fixture[f"color{k}"]), f"{name}: colour attachment {k} differs from the reference"
     ctx.close()
 
 

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 import golden_scenes as G
+from parity import compare_colors
 
 pytestmark = pytest.mark.gpu
 
@@ -32,16 +33,12 @@ def test_gpu_matches_reference_golden(gpu_lib, name, mode, tile):
     scene.render()
     ctx.finish()
     d = np.load(os.path.join(GOLDEN, name + ".npz"))
-    gc, gd = d["color"], d["depth"]
-    c, dd = scene.read_color(), scene.read_depth()
+    gd = d["depth"]
+    dd = scene.read_depth()
     bad = (dd.view(np.uint32) != gd.view(np.uint32)) & ~(np.isnan(dd) & np.isnan(gd))
     assert not bad.any(), f"{name}: {int(bad.sum())} depth texels differ from the reference"
-    if c.dtype == np.uint8:
-        diff = np.abs(c.astype(np.int16) - gc.astype(np.int16)).max(initial=0)
-        assert diff <= 1, f"{name}: colour differs by {diff} LSB"
-    else:
-        ok = (np.abs(c - gc) <= 1e-5 * np.maximum(np.abs(gc), 1e-30)) | (c == gc) | (np.isnan(c) & np.isnan(gc))
-        assert ok.all(), f"{name}: float colour differs"
+    for k in range(len(scene.attachments)):
+        compare_colors(scene.read_color(k), d["color" if k == 0 else f"color{k}"], f"{name} attachment {k}")
     ctx.close()
 
 

@@ -377,3 +377,42 @@ def test_wireframe_queue_scene_opaque_exact(ctxs):
     g, o = ctxs
     sg, so = render_both(E.wire_queue, g, o, blend=A.BLEND_OFF)
     compare_scenes(sg, so, "wire queue opaque")
+
+
+@pytest.mark.parametrize("kw", [
+    dict(num_tris=2000, width=320, height=240),
+    dict(types=(A.COLOR_RGBA_8U, A.COLOR_RGBA_8U, A.COLOR_RGBA_FLOAT), num_outputs=3, blend=A.BLEND_ALPHA,
+         num_tris=1500, width=320, height=240, seed=112),
+    dict(types=(A.COLOR_RGBA_FLOAT, A.COLOR_R_FLOAT), num_outputs=2, depth_test=A.DEPTH_TEST_NOT_EQUAL,
+         num_tris=1000, width=200, height=150, seed=113),
+    dict(num_outputs=2, single_after=True, num_tris=1000, width=200, height=150, seed=114),
+    dict(num_outputs=4, single_after=True, batched=True, blend=A.BLEND_SCREEN, num_tris=800, width=200, height=150,
+         seed=115),
+    dict(prim="wire", blend=A.BLEND_ADDITIVE, num_tris=600, width=160, height=120, seed=116),
+    dict(prim="line", num_tris=2000, width=256, height=192, seed=117),
+    dict(prim="point", num_tris=4000, width=200, height=150, blend=A.BLEND_PREMULTIPLED_ALPHA, seed=118),
+], ids=["four_targets", "three_blend_alpha", "two_not_equal", "two_then_single", "batched_screen", "wire_additive",
+        "lines", "points_premultiplied"])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_multiple_render_targets(ctxs, kw, mode):
+    """Up to four colour attachments of mixed formats: output k of the
+    G-buffer program into attachment k, blended per attachment."""
+    g, o = ctxs
+    g.set_raster_mode(mode)
+    sg, so = render_both(E.mrt, g, o, **kw)
+    compare_scenes(sg, so, f"mrt mode {mode}")
+
+
+def test_mrt_rejections(gpu_lib):
+    """A program writing more outputs than the framebuffer has attachments is
+    rejected (the reference would call unset output functions); counts of
+    attachments outside 1..4 are rejected as in SL_Framebuffer."""
+    ctx = gpu_lib.Context()
+    s = E.mrt(ctx, types=(A.COLOR_RGBA_8U, A.COLOR_RGBA_8U), num_outputs=3)
+    with pytest.raises(A.SLError):
+        ctx.draw(s.draws[0][0], s.draws[0][2], s.fbo)
+    with pytest.raises(A.SLError):
+        ctx.fbo_reserve_color_buffers(s.fbo, 5)
+    with pytest.raises(A.SLError):
+        ctx.fbo_reserve_color_buffers(s.fbo, 0)
+    ctx.close()
