@@ -652,7 +652,6 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
     const Fbo& fbo = ctx->fbos[fboId];
     if (fbo.depth == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "framebuffer has no depth attachment");
-    if (fbo.numColors > 1) return ctx->fail(SLG_ERR_INVALID_ARG, "more than one colour attachment is not supported");
     if (reqs.empty()) return SLG_OK;
     if (reqs.size() + 1 > kDescRing) return ctx->fail(SLG_ERR_INVALID_ARG, "too many draws in one batch");
 
@@ -1412,7 +1411,6 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
     if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
     const Fbo& fbo = ctx->fbos[fboId];
     if (fbo.depth == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "framebuffer has no depth attachment");
-    if (fbo.numColors > 1) return ctx->fail(SLG_ERR_INVALID_ARG, "more than one colour attachment is not supported");
     const Texture& depthTex = ctx->textures[fbo.depth];
     const Texture* colorTex = (fbo.numColors > 0 && fbo.colors[0] != SLG_INVALID_ID) ? &ctx->textures[fbo.colors[0]] : nullptr;
     if (colorTex && (colorTex->w != depthTex.w || colorTex->h != depthTex.h))
