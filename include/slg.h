@@ -88,7 +88,9 @@ enum slg_blend_mode
  * (softlight/include/softlight/SL_Color.hpp:31). Values are the reference's. */
 enum slg_color_type
 {
+    SLG_COLOR_R_HALF     = 4,   /* depth attachments (IEEE binary16) */
     SLG_COLOR_R_FLOAT    = 5,
+    SLG_COLOR_R_DOUBLE   = 6,   /* depth attachments */
     SLG_COLOR_RGBA_8U    = 21,
     SLG_COLOR_RGBA_FLOAT = 26
 };

@@ -27,6 +27,8 @@
 
 #include "../setup/_shim_setup.h"
 
+#include "../../../../include/slg_half.h"
+
 namespace ls
 {
 namespace math
@@ -52,53 +54,10 @@ struct half
 
     operator float() const noexcept { return to_float(bits); }
 
-    static uint16_t from_float(float f) noexcept
-    {
-        uint32_t x;
-        std::memcpy(&x, &f, 4);
-        const uint32_t sign = (x >> 16) & 0x8000u;
-        const int32_t exp = (int32_t)((x >> 23) & 0xFF) - 127 + 15;
-        uint32_t mant = x & 0x7FFFFFu;
-        if (((x >> 23) & 0xFF) == 0xFF) return (uint16_t)(sign | 0x7C00u | (mant ? 0x200u : 0u));
-        if (exp >= 31) return (uint16_t)(sign | 0x7C00u);
-        if (exp <= 0)
-        {
-            if (exp < -10) return (uint16_t)sign;
-            mant |= 0x800000u;
-            const uint32_t shift = (uint32_t)(14 - exp);
-            uint32_t h = mant >> shift;
-            const uint32_t rem = mant & ((1u << shift) - 1u), halfway = 1u << (shift - 1);
-            if (rem > halfway || (rem == halfway && (h & 1u))) ++h;
-            return (uint16_t)(sign | h);
-        }
-        uint32_t h = ((uint32_t)exp << 10) | (mant >> 13);
-        const uint32_t rem = mant & 0x1FFFu;
-        if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) ++h;
-        return (uint16_t)(sign | h);
-    }
-
-    static float to_float(uint16_t h) noexcept
-    {
-        const uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
-        const uint32_t exp = (h >> 10) & 0x1F;
-        const uint32_t mant = h & 0x3FFu;
-        uint32_t x;
-        if (exp == 0)
-        {
-            if (!mant) x = sign;
-            else
-            {
-                float f = (float)mant * (1.f / 16777216.f);
-                std::memcpy(&x, &f, 4);
-                x |= sign;
-            }
-        }
-        else if (exp == 31) x = sign | 0x7F800000u | (mant << 13);
-        else x = sign | ((exp - 15 + 127) << 23) | (mant << 13);
-        float f;
-        std::memcpy(&f, &x, 4);
-        return f;
-    }
+    /* IEEE binary16, round to nearest even (include/slg_half.h, shared with
+     * the GPU kernels and the CPU checker) */
+    static uint16_t from_float(float f) noexcept { return slg_float_to_half(f); }
+    static float to_float(uint16_t h) noexcept { return slg_half_to_float(h); }
 };
 
 /*-----------------------------------------------------------------------------

@@ -23,6 +23,7 @@
  *   range -> INT32_MIN) so the result does not depend on the host ISA.
  */
 #include "slo.h"
+#include "../include/slg_half.h"
 #include "../include/slg_programs.h"
 
 #include <algorithm>
@@ -149,7 +150,9 @@ static size_t bytes_per_color(int type)
 {
     switch (type)
     {
+        case SLG_COLOR_R_HALF: return 2;
         case SLG_COLOR_R_FLOAT: return 4;
+        case SLG_COLOR_R_DOUBLE: return 8;
         case SLG_COLOR_RGBA_8U: return 4;
         case SLG_COLOR_RGBA_FLOAT: return 16;
         default: return 0;
@@ -739,7 +742,8 @@ static inline bool depth_cmp(uint8_t func, float z, float d)
 struct RasterState
 {
     const slo_context* ctx;
-    float* depth;
+    uint8_t* depth;     /* R_HALF, R_FLOAT or R_DOUBLE texels */
+    int depthType;
     uint16_t width;
     uint16_t height;
     Target colors[4];
@@ -747,6 +751,25 @@ struct RasterState
     std::vector<const Shader*> shaders; /* per draw index */
     std::vector<Env> envs;               /* per draw index */
 };
+
+/* The depth texel as the rasterizers compare it, (float)depth_type, and the
+ * write (depth_type)z (_sl_get_depth_texel, SL_TriRasterizer.cpp:95-101;
+ * SL_FragmentProcessor.cpp:398-401, 524-527). */
+static inline float dget(const RasterState& rs, size_t i)
+{
+    if (rs.depthType == SLG_COLOR_R_HALF) { uint16_t h; std::memcpy(&h, rs.depth + 2 * i, 2); return slg_half_to_float(h); }
+    if (rs.depthType == SLG_COLOR_R_DOUBLE) { double d; std::memcpy(&d, rs.depth + 8 * i, 8); return (float)d; }
+    float f;
+    std::memcpy(&f, rs.depth + 4 * i, 4);
+    return f;
+}
+
+static inline void dset(const RasterState& rs, size_t i, float z)
+{
+    if (rs.depthType == SLG_COLOR_R_HALF) { const uint16_t h = slg_float_to_half(z); std::memcpy(rs.depth + 2 * i, &h, 2); }
+    else if (rs.depthType == SLG_COLOR_R_DOUBLE) { const double d = (double)z; std::memcpy(rs.depth + 8 * i, &d, 8); }
+    else std::memcpy(rs.depth + 4 * i, &z, 4);
+}
 
 /* SL_FragmentProcessor::flush_tri_fragments for one fragment, portable
  * (SL_FragmentProcessor.cpp:417-531, interpolate_tri_varyings :308-330) */
@@ -779,7 +802,7 @@ static inline void shade_fragment(const RasterState& rs, const Bin& bin, int x, 
     }
     if (sh.depthMask == SLG_DEPTH_MASK_ON)
     {
-        rs.depth[(size_t)x + (size_t)rs.width * y] = z;
+        dset(rs, (size_t)x + (size_t)rs.width * y, z);
     }
     ++frags;
 }
@@ -864,7 +887,7 @@ static void raster_bin(const RasterState& rs, const Bin& bin, int rowStride, int
                     if (x4[k] < xMax)
                     {
                         const float z = dot(depth, bc[k]);
-                        const float d = rs.depth[(size_t)x4[k] + (size_t)rs.width * y];
+                        const float d = dget(rs, (size_t)x4[k] + (size_t)rs.width * y);
                         if (depth_cmp(sh.depthTest, z, d))
                         {
                             shade_fragment(rs, bin, x4[k], y, z, bc[k], frags);
@@ -964,7 +987,7 @@ static void render_line(const RasterState& rs, const DrawState& ds, const LineVe
                     write_color(rs.colors[t], (unsigned)(lin % W), (unsigned)(lin / W), outputs[t], sh.blend);
                 }
             }
-            if (sh.depthMask == SLG_DEPTH_MASK_ON) rs.depth[lin] = q.z;
+            if (sh.depthMask == SLG_DEPTH_MASK_ON) dset(rs, lin, q.z);
             ++frags;
         }
         queue.clear();
@@ -978,7 +1001,7 @@ static void render_line(const RasterState& rs, const DrawState& ds, const LineVe
                        const float z = (z1 - z0) * interp + z0;
                        const size_t lin = (size_t)x + W * y;
                        if (lin >= W * H) return; /* past the buffer: out of bounds in the reference */
-                       if (!depth_cmp(sh.depthTest, z, rs.depth[lin])) return;
+                       if (!depth_cmp(sh.depthTest, z, dget(rs, lin))) return;
                        queue.push_back({interp, z, x, y});
                        if (queue.size() == 600) flush();
                    });
@@ -1155,7 +1178,7 @@ static void raster_wire_bin(const RasterState& rs, const Bin& bin, int rowStride
             const float xf = (float)x;
             const V4 bc = mk(bcs[0][0] * xf + bcY[0], bcs[0][1] * xf + bcY[1], bcs[0][2] * xf + bcY[2], bcs[0][3] * 0.f + bcY[3]);
             const float z = dot(depth, bc);
-            const float d = rs.depth[(size_t)x + (size_t)rs.width * y];
+            const float d = dget(rs, (size_t)x + (size_t)rs.width * y);
             if (!depth_cmp(sh.depthTest, z, d)) continue;
             queue.push_back({x, y, z, bc});
             if (queue.size() == 600) flush();
@@ -1434,7 +1457,9 @@ int slo_fbo_attach_color_buffer(slo_context* ctx, size_t fbo, unsigned index, si
 int slo_fbo_attach_depth_buffer(slo_context* ctx, size_t fbo, size_t tex)
 {
     if (fbo >= ctx->fbos.size() || tex >= ctx->textures.size()) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo attachment");
-    if (ctx->textures[tex]->type != SLG_COLOR_R_FLOAT) return ctx->fail(SLG_ERR_INVALID_ARG, "depth must be R_FLOAT");
+    const int dt = ctx->textures[tex]->type;
+    if (dt != SLG_COLOR_R_HALF && dt != SLG_COLOR_R_FLOAT && dt != SLG_COLOR_R_DOUBLE)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "depth must be R_HALF, R_FLOAT or R_DOUBLE");
     ctx->fbos[fbo].depth = tex;
     return SLG_OK;
 }
@@ -1516,6 +1541,17 @@ static void clear_color(Texture& t, const double rgba[4], unsigned threads)
         const float c[4] = {(float)rgba[0], (float)rgba[1], (float)rgba[2], (float)rgba[3]};
         for (size_t i = 0; i < n; ++i) std::memcpy(t.bytes.data() + 16 * i, c, 16);
     }
+    else if (t.type == SLG_COLOR_R_HALF)
+    {
+        /* SL_Context::clear_depth_buffer: (half)(float)depth (SL_Context.cpp:897-913) */
+        const uint16_t c = slg_float_to_half((float)rgba[0]);
+        for (size_t i = 0; i < n; ++i) std::memcpy(t.bytes.data() + 2 * i, &c, 2);
+    }
+    else if (t.type == SLG_COLOR_R_DOUBLE)
+    {
+        const double c = rgba[0];
+        for (size_t i = 0; i < n; ++i) std::memcpy(t.bytes.data() + 8 * i, &c, 8);
+    }
     else
     {
         const float c = (float)rgba[0];
@@ -1562,7 +1598,8 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
 
     RasterState rs;
     rs.ctx = ctx;
-    rs.depth = reinterpret_cast<float*>(depthTex.bytes.data());
+    rs.depth = depthTex.bytes.data();
+    rs.depthType = depthTex.type;
     rs.width = depthTex.w;
     rs.height = depthTex.h;
     rs.numOutputs = 0;
@@ -1683,7 +1720,7 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
                     const size_t lin = x + W * y;
                     if (lin >= W * H) continue;
                     const float z = v[2];
-                    if (!depth_cmp(sh.depthTest, z, rs.depth[lin])) continue;
+                    if (!depth_cmp(sh.depthTest, z, dget(rs, lin))) continue;
                     V4 outputs[4];
                     if (run_fs(sh.fsProgram, ds.env, vary, outputs))
                     {
@@ -1692,7 +1729,7 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
                             write_color(rs.colors[t], (unsigned)(lin % W), (unsigned)(lin / W), outputs[t], sh.blend);
                         }
                     }
-                    if (sh.depthMask == SLG_DEPTH_MASK_ON) rs.depth[lin] = z;
+                    if (sh.depthMask == SLG_DEPTH_MASK_ON) dset(rs, lin, z);
                     ++totalFrags;
                 }
             }

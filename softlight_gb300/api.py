@@ -27,11 +27,11 @@ DEPTH_TEST_OFF, DEPTH_TEST_LESS_THAN, DEPTH_TEST_LESS_EQUAL, DEPTH_TEST_GREATER_
 DEPTH_TEST_GREATER_EQUAL, DEPTH_TEST_EQUAL, DEPTH_TEST_NOT_EQUAL = 4, 5, 6
 DEPTH_MASK_OFF, DEPTH_MASK_ON = 0, 1
 BLEND_OFF, BLEND_ALPHA, BLEND_PREMULTIPLED_ALPHA, BLEND_ADDITIVE, BLEND_SCREEN = 0, 1, 2, 3, 4
-COLOR_R_FLOAT, COLOR_RGBA_8U, COLOR_RGBA_FLOAT = 5, 21, 26
+COLOR_R_HALF, COLOR_R_FLOAT, COLOR_R_DOUBLE, COLOR_RGBA_8U, COLOR_RGBA_FLOAT = 4, 5, 6, 21, 26
 PROGRAM_LAMBERT_TEX, PROGRAM_BLINN_PHONG_INST, PROGRAM_VCOLOR_TEX_ALPHA = 1, 2, 3
 PROGRAM_VCOLOR_TEXF, PROGRAM_FLAT_COLOR, PROGRAM_GBUFFER = 4, 5, 6
 
-BYTES_PER_COLOR = {COLOR_R_FLOAT: 4, COLOR_RGBA_8U: 4, COLOR_RGBA_FLOAT: 16}
+BYTES_PER_COLOR = {COLOR_R_HALF: 2, COLOR_R_FLOAT: 4, COLOR_R_DOUBLE: 8, COLOR_RGBA_8U: 4, COLOR_RGBA_FLOAT: 16}
 
 
 class Mesh(C.Structure):

@@ -64,7 +64,9 @@ size_t bytes_per_color(int type)
 {
     switch (type)
     {
+        case SLG_COLOR_R_HALF: return 2;
         case SLG_COLOR_R_FLOAT: return 4;
+        case SLG_COLOR_R_DOUBLE: return 8;
         case SLG_COLOR_RGBA_8U: return 4;
         case SLG_COLOR_RGBA_FLOAT: return 16;
         default: return 0;
@@ -327,6 +329,16 @@ int color_value(int type, const double rgba[4], uint32_t out[4])
     {
         const float f = (float)rgba[0];
         std::memcpy(&out[0], &f, 4);
+    }
+    else if (type == SLG_COLOR_R_HALF)
+    {
+        /* SL_Context::clear_depth_buffer: (half)(float)depth (softlight/src/SL_Context.cpp:897-913) */
+        out[0] = slg_float_to_half((float)rgba[0]);
+    }
+    else if (type == SLG_COLOR_R_DOUBLE)
+    {
+        const double d = rgba[0];
+        std::memcpy(&out[0], &d, 8);
     }
     else
     {
@@ -710,6 +722,7 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     f.color = colorTex ? static_cast<uint8_t*>(colorTex->buf.ptr) : nullptr;
     f.colorType = colorTex ? colorTex->type : SLG_COLOR_RGBA_8U;
     f.depth = static_cast<float*>(depthTex.buf.ptr);
+    f.depthType = depthTex.type;
     viewport_setup((float)f.width, (float)f.height, f.scissor, f.viewport);
     f.records = static_cast<float4*>(ctx->records.ptr);
     f.varyings = static_cast<float4*>(ctx->varyings.ptr);
@@ -742,6 +755,9 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
             f.orderFree = 0;
         }
     }
+    /* a half depth is rounded on every write and re-read by later
+     * fragments: the outcome depends on the order, not the set */
+    if (f.depthType == SLG_COLOR_R_HALF) f.orderFree = 0;
     for (size_t i = 0; i < n; ++i)
     {
         /* the reference's Bresenham error term is int16: it stays exact while
@@ -762,6 +778,8 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
 
     if (fbo.visEnabled)
     {
+        if (f.depthType != SLG_COLOR_R_FLOAT)
+            return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map needs an R_FLOAT depth attachment");
         if (f.hasLines || f.hasWire)
             return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map takes filled triangle and point draws only");
         if (!f.orderFree)
@@ -1107,7 +1125,9 @@ int slg_fbo_attach_color_buffer(slg_context* ctx, size_t fbo, unsigned index, si
 int slg_fbo_attach_depth_buffer(slg_context* ctx, size_t fbo, size_t tex)
 {
     if (!id_ok(fbo, ctx->fbos.size()) || !id_ok(tex, ctx->textures.size())) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo attachment");
-    if (ctx->textures[tex].type != SLG_COLOR_R_FLOAT) return ctx->fail(SLG_ERR_INVALID_ARG, "depth must be R_FLOAT");
+    const int dt = ctx->textures[tex].type;
+    if (dt != SLG_COLOR_R_HALF && dt != SLG_COLOR_R_FLOAT && dt != SLG_COLOR_R_DOUBLE)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "depth must be R_HALF, R_FLOAT or R_DOUBLE");
     ctx->fbos[fbo].depth = tex;
     return SLG_OK;
 }
@@ -1507,6 +1527,7 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
     f.color = colorTex ? static_cast<uint8_t*>(colorTex->buf.ptr) : nullptr;
     f.colorType = colorTex ? colorTex->type : SLG_COLOR_RGBA_8U;
     f.depth = static_cast<float*>(depthTex.buf.ptr);
+    f.depthType = depthTex.type;
     viewport_setup((float)f.width, (float)f.height, f.scissor, f.viewport);
     f.records = reinterpret_cast<float4*>(scratch + kOffRecords);
     f.varyings = reinterpret_cast<float4*>(scratch + kOffVaryings);
@@ -1526,7 +1547,8 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
     f.draws = devDesc;
     f.drawSlotStart = devStarts;
     f.numDraws = 1;
-    f.orderFree = (desc->blend == SLG_BLEND_OFF && desc->depthTest != SLG_DEPTH_TEST_NOT_EQUAL && !ctx->forceOrdered) ? 1 : 0;
+    f.orderFree = (desc->blend == SLG_BLEND_OFF && desc->depthTest != SLG_DEPTH_TEST_NOT_EQUAL && !ctx->forceOrdered &&
+                   f.depthType != SLG_COLOR_R_HALF) ? 1 : 0;
     f.freeDepthFunc = desc->depthTest;
     f.freeDepthMask = desc->depthMask;
     f.vsBlock = ctx->vsBlock;

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/slg.h"
+#include "../../include/slg_half.h"
 #include "../../include/slg_programs.h"
 
 namespace slg
@@ -123,7 +124,8 @@ struct Frame
 {
     /* framebuffer */
     uint8_t* color;         /* attachment 0, or null */
-    float*   depth;
+    float*   depth;         /* texels of depthType: R_HALF, R_FLOAT or R_DOUBLE */
+    int32_t  depthType;
     int32_t  colorType;
     int32_t  width, height;
     int32_t  tileW, tileH, tilesX, tilesY;

@@ -159,6 +159,29 @@ __device__ __forceinline__ void make_record(const float4 p0, const float4 p1, co
                            __uint_as_float((uint32_t)(primIndex >> 32)), __uint_as_float(depthFlags));
 }
 
+/* The depth texel as the reference compares it, (float)depth_type, and its
+ * write, (depth_type)z (_sl_get_depth_texel, SL_TriRasterizer.cpp:95-101;
+ * SL_FragmentProcessor.cpp:398-401,524-527). A half depth is re-read after
+ * every write, so depth_quant rounds a written z the same way. */
+__device__ __forceinline__ float depth_load(const Frame& f, size_t i)
+{
+    if (f.depthType == SLG_COLOR_R_HALF) return slg_half_to_float(reinterpret_cast<const uint16_t*>(f.depth)[i]);
+    if (f.depthType == SLG_COLOR_R_DOUBLE) return (float)reinterpret_cast<const double*>(f.depth)[i];
+    return f.depth[i];
+}
+
+__device__ __forceinline__ void depth_store(const Frame& f, size_t i, float z)
+{
+    if (f.depthType == SLG_COLOR_R_HALF) reinterpret_cast<uint16_t*>(f.depth)[i] = slg_float_to_half(z);
+    else if (f.depthType == SLG_COLOR_R_DOUBLE) reinterpret_cast<double*>(f.depth)[i] = (double)z;
+    else f.depth[i] = z;
+}
+
+__device__ __forceinline__ float depth_quant(bool halfDepth, float z)
+{
+    return halfDepth ? slg_half_to_float(slg_float_to_half(z)) : z;
+}
+
 /* r7.w of a triangle record: depth test, depth mask, wireframe bit */
 __device__ __forceinline__ uint32_t record_flags(const DrawDesc& d)
 {
@@ -629,7 +652,7 @@ __device__ __forceinline__ uint32_t setup_line(const Frame& f, const DrawDesc& d
             ev.slot = (uint32_t)slot;
             ev.pixel = pix;
             ev.queued = 0;
-            ev.depth0 = f.depth[pix];
+            ev.depth0 = depth_load(f, pix);
             uint4 c = make_uint4(0u, 0u, 0u, 0u);
             if (f.color)
             {
@@ -1574,6 +1597,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
         return;
     }
     const uint32_t* sKeys = f.entries + begin; /* sorted by tile_sort_kernel */
+    const bool halfDepth = f.depthType == SLG_COLOR_R_HALF;
 
     const int tx = tile % f.tilesX, ty = tile / f.tilesX;
     const int x0 = tx * TW, y0 = ty * TH;
@@ -1585,7 +1609,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
         if (gx < f.width && gy < f.height)
         {
             const size_t gi = (size_t)gx + (size_t)f.width * gy;
-            sDepth[py * L::kStride + px] = f.depth[gi];
+            sDepth[py * L::kStride + px] = depth_load(f, gi);
             if (f.color) sColor[py * L::kStride + px] = Color::read(f.color, gi);
         }
     }
@@ -1655,7 +1679,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                         }
                         if ((flags >> 4) & 1)
                         {
-                            sDepth[idx] = z;
+                            sDepth[idx] = depth_quant(halfDepth, z);
                         }
                     }
                 }
@@ -1700,7 +1724,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                         }
                         if ((flags >> 4) & 1)
                         {
-                            sDepth[idx] = z;
+                            sDepth[idx] = depth_quant(halfDepth, z);
                         }
                     }
                 }
@@ -1726,7 +1750,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                     }
                     if ((flags >> 4) & 1)
                     {
-                        sDepth[idx] = z;
+                        sDepth[idx] = depth_quant(halfDepth, z);
                     }
                 }
                 return;
@@ -1755,7 +1779,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                     }
                     if (depthMask)
                     {
-                        sDepth[idx] = z;
+                        sDepth[idx] = depth_quant(halfDepth, z);
                     }
                 }
             }
@@ -1770,7 +1794,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
         if (gx < f.width && gy < f.height)
         {
             const size_t gi = (size_t)gx + (size_t)f.width * gy;
-            f.depth[gi] = sDepth[py * L::kStride + px];
+            depth_store(f, gi, sDepth[py * L::kStride + px]);
             if (f.color) Color::write(f.color, gi, sColor[py * L::kStride + px]);
         }
     }
@@ -2022,7 +2046,7 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
     {
         const int x = x0 + i % TW, y = y0 + i / TW;
         sBest[i] = ~0ull;
-        sD0[i] = (x < xLimit && y < yLimit) ? f.depth[(size_t)x + (size_t)f.width * y] : 0.f;
+        sD0[i] = (x < xLimit && y < yLimit) ? depth_load(f, (size_t)x + (size_t)f.width * y) : 0.f;
     }
 
     for (uint32_t b0 = 0; b0 < n; b0 += kFreeBatch)
@@ -2091,7 +2115,7 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
         }
         if (mask)
         {
-            f.depth[gi] = b.w;
+            depth_store(f, gi, b.w);
         }
         if (f.ids)
         {
@@ -2121,6 +2145,7 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
     const int py = (int)(gi / (uint32_t)f.width);
     const float yf = (float)py;
 
+    const bool halfDepth = f.depthType == SLG_COLOR_R_HALF;
     /* the pixel's state before the launch */
     float depth = ev.depth0;
     for (int k = 1; k < f.numColors; ++k)
@@ -2189,7 +2214,7 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
                 if (depth_cmp(func, zh[j], against))
                 {
                     put(dd, shade_line<true>(f, dd, rec, ih[j], o, gi), o);
-                    if (mask) depth = zh[j];
+                    if (mask) depth = depth_quant(halfDepth, zh[j]);
                 }
             }
         }
@@ -2205,7 +2230,7 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
                 {
                     const bool have = shade<true>(f, dd, rec, R[2].w, R[5], b0, b1, b2, o, gi, (dd.blend != SLG_BLEND_OFF) ? n : 1);
                     for (int v = 0; v < ((dd.blend != SLG_BLEND_OFF) ? n : 1); ++v) put(dd, have, o);
-                    if (mask) depth = z;
+                    if (mask) depth = depth_quant(halfDepth, z);
                 }
             }
         }
@@ -2215,7 +2240,7 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
             if (__float_as_int(r6.z) == 0 && __float_as_int(r6.x) == py && depth_cmp(func, R[0].z, depth))
             {
                 put(dd, shade_point<true>(f, dd, rec, o, gi), o);
-                if (mask) depth = R[0].z;
+                if (mask) depth = depth_quant(halfDepth, R[0].z);
             }
         }
         else
@@ -2227,12 +2252,12 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
                 if (depth_cmp(func, z, depth))
                 {
                     put(dd, shade<true>(f, dd, rec, R[2].w, R[5], ch.b0, ch.b1, ch.b2, o, gi), o);
-                    if (mask) depth = z;
+                    if (mask) depth = depth_quant(halfDepth, z);
                 }
             }
         }
     }
-    f.depth[gi] = depth;
+    depth_store(f, gi, depth);
     if (f.color) Color::write(f.color, gi, color);
 }
 
@@ -2305,6 +2330,8 @@ __global__ void clear_kernel(uint8_t* dst, size_t numTexels, int bytesPerTexel, 
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < numTexels; i += stride)
     {
         if (bytesPerTexel == 16) reinterpret_cast<uint4*>(dst)[i] = value;
+        else if (bytesPerTexel == 8) reinterpret_cast<uint2*>(dst)[i] = make_uint2(value.x, value.y);
+        else if (bytesPerTexel == 2) reinterpret_cast<uint16_t*>(dst)[i] = (uint16_t)value.x;
         else reinterpret_cast<uint32_t*>(dst)[i] = value.x;
     }
 }

@@ -246,13 +246,14 @@ def flat_uniforms(mvp, rgba):
 class Scene:
     """Resources of one workload in one context plus its frame sequence."""
 
-    def __init__(self, ctx, name, width, height, color_type=A.COLOR_RGBA_8U):
+    def __init__(self, ctx, name, width, height, color_type=A.COLOR_RGBA_8U, depth_type=A.COLOR_R_FLOAT):
         self.ctx, self.name, self.width, self.height = ctx, name, width, height
         self.color_type = color_type
+        self.depth_type = depth_type
         self.color_tex = ctx.create_texture()
         ctx.texture_init(self.color_tex, color_type, width, height, 1)
         self.depth_tex = ctx.create_texture()
-        ctx.texture_init(self.depth_tex, A.COLOR_R_FLOAT, width, height, 1)
+        ctx.texture_init(self.depth_tex, depth_type, width, height, 1)
         self.fbo = ctx.create_framebuffer()
         ctx.fbo_reserve_color_buffers(self.fbo, 1)
         ctx.fbo_attach_color_buffer(self.fbo, 0, self.color_tex)
@@ -355,7 +356,8 @@ class Scene:
         return [self.read_color(k) for k in range(len(self.attachments))]
 
     def read_depth(self):
-        return self.ctx.texture_read(self.depth_tex, (self.height, self.width), np.float32)
+        dtype = {A.COLOR_R_HALF: np.float16, A.COLOR_R_DOUBLE: np.float64}.get(self.depth_type, np.float32)
+        return self.ctx.texture_read(self.depth_tex, (self.height, self.width), dtype)
 
     def framebuffer_bytes(self):
         return self.width * self.height * (A.BYTES_PER_COLOR[self.color_type] + 4)

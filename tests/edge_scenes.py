@@ -10,11 +10,11 @@ from softlight_gb300 import scenes as S
 def random_soup(ctx, num_tris=300, width=96, height=80, seed=11, blend=A.BLEND_OFF,
                 depth_test=A.DEPTH_TEST_LESS_THAN, depth_mask=A.DEPTH_MASK_ON, cull=A.CULL_BACK_FACE,
                 color_type=A.COLOR_RGBA_8U, program=A.PROGRAM_VCOLOR_TEX_ALPHA, indexed=None, clear_depth=1.0,
-                max_area=None, wire=False, num_instances=1):
+                max_area=None, wire=False, num_instances=1, depth_type=A.COLOR_R_FLOAT):
     """Triangle soup like the c3 workload at a small size, with the pipeline
     state as parameters. indexed: None (non-indexed) or a numpy index dtype;
     wire: draw the triangles as wireframe (SL_RENDER_MODE_[INDEXED_]TRI_WIRE)."""
-    s = S.Scene(ctx, f"soup_{seed}", width, height, color_type=color_type)
+    s = S.Scene(ctx, f"soup_{seed}", width, height, color_type=color_type, depth_type=depth_type)
     verts, proj = S.soup_triangles(num_tris, width, height, seed=seed)
     if max_area is not None:
         pass
@@ -142,7 +142,8 @@ def random_points(ctx, num_points=3000, width=64, height=48, seed=41, blend=A.BL
 
 def random_lines(ctx, num_lines=400, width=64, height=48, seed=61, blend=A.BLEND_OFF,
                  depth_test=A.DEPTH_TEST_LESS_THAN, depth_mask=A.DEPTH_MASK_ON, indexed=None,
-                 color_type=A.COLOR_RGBA_8U, clear_depth=1.0, num_instances=1, persp=False, odd_end=False):
+                 color_type=A.COLOR_RGBA_8U, clear_depth=1.0, num_instances=1, persp=False, odd_end=False,
+                 depth_type=A.COLOR_R_FLOAT):
     """Line draw (SL_RENDER_MODE_LINES): seeded segments in and around the
     view volume, so that many are clipped to the viewport (and, with
     `persp`, some cross the camera plane and are culled); vertex colour x
@@ -150,7 +151,7 @@ def random_lines(ctx, num_lines=400, width=64, height=48, seed=61, blend=A.BLEND
     line. `odd_end` ends the element range on an odd count: the last line
     reads the vertex after elementEnd, as the reference's loop does."""
     rng = np.random.default_rng(seed)
-    s = S.Scene(ctx, f"lines_{seed}", width, height, color_type=color_type)
+    s = S.Scene(ctx, f"lines_{seed}", width, height, color_type=color_type, depth_type=depth_type)
     n = 2 * num_lines
     if persp:
         pos = np.stack([rng.uniform(-3.0, 3.0, n), rng.uniform(-2.0, 2.0, n), rng.uniform(-2.5, 3.5, n)], 1)

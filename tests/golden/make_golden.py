@@ -26,8 +26,8 @@ sys.path.insert(0, os.path.dirname(HERE))
 
 def canonical(a):
     a = np.ascontiguousarray(a).copy()
-    if a.dtype == np.float32:
-        a[np.isnan(a)] = np.float32("nan")
+    if a.dtype.kind == "f":
+        a[np.isnan(a)] = a.dtype.type("nan")
     return a
 
 

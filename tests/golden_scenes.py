@@ -63,6 +63,14 @@ SCENES = {
     "mrt_wire_additive": (E.mrt, dict(prim="wire", blend=A.BLEND_ADDITIVE, seed=104)),
     "mrt_lines": (E.mrt, dict(prim="line", types=(A.COLOR_RGBA_8U, A.COLOR_RGBA_FLOAT), num_outputs=2, seed=105)),
     "mrt_points_premultiplied": (E.mrt, dict(prim="point", blend=A.BLEND_PREMULTIPLED_ALPHA, seed=106, num_tris=2000)),
+    "soup_half_depth_less": (E.random_soup, dict(depth_type=A.COLOR_R_HALF)),
+    "soup_half_depth_lequal": (E.random_soup, dict(depth_type=A.COLOR_R_HALF, depth_test=A.DEPTH_TEST_LESS_EQUAL, seed=21)),
+    "soup_half_depth_not_equal_blend": (E.random_soup, dict(depth_type=A.COLOR_R_HALF, depth_test=A.DEPTH_TEST_NOT_EQUAL,
+                                                            clear_depth=0.5, blend=A.BLEND_ALPHA, seed=22)),
+    "soup_double_depth_greater": (E.random_soup, dict(depth_type=A.COLOR_R_DOUBLE, depth_test=A.DEPTH_TEST_GREATER_THAN,
+                                                      clear_depth=0.1, seed=23)),
+    "wire_double_depth": (E.random_soup, dict(depth_type=A.COLOR_R_DOUBLE, wire=True, seed=24)),
+    "lines_half_depth": (E.random_lines, dict(depth_type=A.COLOR_R_HALF, seed=25)),
 }
 
 # Scenes whose draws the GPU path reports as not reproduced (SLError at

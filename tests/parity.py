@@ -29,7 +29,8 @@ def compare_scenes(sg, so, label=""):
     # depth: bit-exact (covers coverage and depth-test outcomes). A NaN depth
     # (written by a zero-area triangle when the depth test is off) matches any
     # NaN: each ISA produces its own NaN payload (x86 sets the sign bit).
-    bad = (dg.view(np.uint32) != do.view(np.uint32)) & ~(np.isnan(dg) & np.isnan(do))
+    bits = {2: np.uint16, 4: np.uint32, 8: np.uint64}[dg.dtype.itemsize]
+    bad = (dg.view(bits) != do.view(bits)) & ~(np.isnan(dg) & np.isnan(do))
     assert not bad.any(), f"{label}: {int(bad.sum())} depth texels differ, first at {np.argwhere(bad)[:3].tolist()}"
     for k in range(1, len(sg.attachments)):
         compare_colors(sg.read_color(k), so.read_color(k), f"{label} attachment {k}")

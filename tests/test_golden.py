@@ -22,10 +22,11 @@ def load(name):
 
 
 def same(a, b):
-    if a.dtype == np.float32:
-        return np.array_equal(a.view(np.uint32), b.view(np.uint32)) or \
-            (np.array_equal(np.isnan(a), np.isnan(b)) and
-             np.array_equal(np.where(np.isnan(a), 0, a).view(np.uint32), np.where(np.isnan(b), 0, b).view(np.uint32)))
+    if a.dtype.kind == "f":
+        bits = {2: np.uint16, 4: np.uint32, 8: np.uint64}[a.dtype.itemsize]
+        return a.dtype == b.dtype and (np.array_equal(a.view(bits), b.view(bits)) or
+                                       (np.array_equal(np.isnan(a), np.isnan(b)) and
+                                        np.array_equal(np.where(np.isnan(a), 0, a).view(bits), np.where(np.isnan(b), 0, b).view(bits))))
     return np.array_equal(a, b)
 
 

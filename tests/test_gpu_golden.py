@@ -35,7 +35,8 @@ def test_gpu_matches_reference_golden(gpu_lib, name, mode, tile):
     d = np.load(os.path.join(GOLDEN, name + ".npz"))
     gd = d["depth"]
     dd = scene.read_depth()
-    bad = (dd.view(np.uint32) != gd.view(np.uint32)) & ~(np.isnan(dd) & np.isnan(gd))
+    bits = {2: np.uint16, 4: np.uint32, 8: np.uint64}[dd.dtype.itemsize]
+    bad = (dd.view(bits) != gd.view(bits)) & ~(np.isnan(dd) & np.isnan(gd))
     assert not bad.any(), f"{name}: {int(bad.sum())} depth texels differ from the reference"
     for k in range(len(scene.attachments)):
         compare_colors(scene.read_color(k), d["color" if k == 0 else f"color{k}"], f"{name} attachment {k}")

@@ -416,3 +416,27 @@ def test_mrt_rejections(gpu_lib):
     with pytest.raises(A.SLError):
         ctx.fbo_reserve_color_buffers(s.fbo, 0)
     ctx.close()
+
+
+@pytest.mark.parametrize("depth_type", [A.COLOR_R_HALF, A.COLOR_R_DOUBLE])
+@pytest.mark.parametrize("depth_test", [A.DEPTH_TEST_LESS_THAN, A.DEPTH_TEST_LESS_EQUAL, A.DEPTH_TEST_GREATER_EQUAL,
+                                        A.DEPTH_TEST_EQUAL, A.DEPTH_TEST_NOT_EQUAL])
+def test_half_and_double_depth(ctxs, depth_type, depth_test):
+    """R_HALF and R_DOUBLE depth attachments: compared as (float)depth,
+    written as (depth_type)z; a half depth is re-read rounded after each
+    write (ordered raster), a double depth keeps z exactly."""
+    g, o = ctxs
+    clear = 0.5 if depth_test in (A.DEPTH_TEST_GREATER_EQUAL, A.DEPTH_TEST_EQUAL, A.DEPTH_TEST_NOT_EQUAL) else 1.0
+    sg, so = render_both(E.random_soup, g, o, depth_type=depth_type, depth_test=depth_test, clear_depth=clear,
+                         num_tris=1500, width=320, height=240, frames=2)
+    compare_scenes(sg, so, f"depth type {depth_type} test {depth_test}")
+
+
+@pytest.mark.parametrize("depth_type", [A.COLOR_R_HALF, A.COLOR_R_DOUBLE])
+def test_half_and_double_depth_other_primitives(ctxs, depth_type):
+    g, o = ctxs
+    for builder, kw in [(E.random_lines, dict(num_lines=2000, width=256, height=192, persp=True, seed=131)),
+                        (E.random_soup, dict(wire=True, num_tris=800, width=200, height=150, seed=132)),
+                        (E.random_soup, dict(blend=A.BLEND_ADDITIVE, num_tris=800, width=200, height=150, seed=133))]:
+        sg, so = render_both(builder, g, o, depth_type=depth_type, **kw)
+        compare_scenes(sg, so, f"{builder.__name__} depth type {depth_type}")
