@@ -90,6 +90,8 @@ constexpr size_t kDescRing = 4096;
 constexpr uint64_t kMaxSlots = (1ull << 29) - 1; /* keys are slot << 3 | sub in 32 bits */
 constexpr int kMaxLineExtent = 10922;            /* 3 * 10922 < 32768 */
 constexpr uint32_t kAliasCap = 4096;             /* line address aliases per launch */
+constexpr uint64_t kMaxCacheEntries = 1ull << 25; /* vertex-cache entries per launch (80 B each) */
+constexpr uint64_t kMinCachedSlots = 1ull << 16;  /* smaller launches run the programs per corner */
 
 } // namespace
 
@@ -129,6 +131,9 @@ struct slg_context
     /* scratch */
     DevBuffer records, varyings, slotInfo, slotOvf, ovfCount, clipQueue, clipCount;
     DevBuffer aliasEvents, aliasCount; /* line address aliases (slg::AliasEvent) */
+    DevBuffer cachePos, cacheVary;     /* post-transform vertex cache */
+    DevBuffer recVerts;                /* per slot: cache entries of a cached record */
+    uint64_t cacheCap = 0;
     DevBuffer tileCount, tileOffset, tileCursor, entries, status;
     DevBuffer blitBuf;      /* destination of slg_blit_read */
     uint64_t slotCap = 0, ovfCap = 0, tileCap = 0, entryCap = 0;
@@ -233,6 +238,7 @@ int ensure_scratch(slg_context* ctx, uint64_t numSlots, uint64_t numTiles)
         if ((r = dev_alloc(ctx, ctx->slotInfo, cap * sizeof(uint32_t), false))) return r;
         if ((r = dev_alloc(ctx, ctx->slotOvf, cap * sizeof(uint32_t), false))) return r;
         if ((r = dev_alloc(ctx, ctx->clipQueue, cap * sizeof(uint32_t), false))) return r;
+        if ((r = dev_alloc(ctx, ctx->recVerts, cap * sizeof(uint4), false))) return r;
         ctx->slotCap = cap;
         ctx->ovfCap = ovf;
         const uint64_t wantEntries = std::max<uint64_t>(8 * cap, 32u << 20);
@@ -589,6 +595,16 @@ int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, Draw
     d.numInstances = std::max<size_t>(1, req.numInstances);
     d.slotBase = slotBase;
     d.primBase = req.primBase;
+    /* post-transform vertex cache for indexed triangles whose vertices are
+     * shared by enough corners: the program then runs once per vertex and
+     * instance instead of once per corner (run_launch assigns the entries) */
+    d.cacheBase = 0;
+    d.cacheVerts = 0;
+    if (indexed && (d.prim == slg::kPrimTriangle || d.prim == slg::kPrimWire))
+    {
+        const uint64_t verts = (uint64_t)ctx->ibos[vao.ibo].maxIndex + 1;
+        if (2 * d.numTris >= verts) d.cacheVerts = verts;
+    }
     d.indexType = indexed ? ctx->ibos[vao.ibo].type : -1;
     d.vsProgram = sh.vsProgram;
     d.fsProgram = sh.fsProgram;
@@ -694,6 +710,22 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     }
     starts[n] = numSlots;
     if (numSlots > kMaxSlots) return ctx->fail(SLG_ERR_INVALID_ARG, "too many triangles in one launch (max 2^29-1)");
+    /* the vertex cache costs a launch: used from kMinCachedSlots triangles on */
+    uint64_t cacheEntries = 0;
+    for (size_t i = 0; i < n; ++i)
+    {
+        descs[i].cacheBase = cacheEntries;
+        const uint64_t add = descs[i].cacheVerts * descs[i].numInstances;
+        if (descs[i].cacheVerts && numSlots >= kMinCachedSlots && starts[i + 1] > starts[i] && cacheEntries + add <= kMaxCacheEntries)
+            cacheEntries += add;
+        else descs[i].cacheVerts = 0;
+    }
+    if (cacheEntries > ctx->cacheCap)
+    {
+        if ((r = dev_alloc(ctx, ctx->cachePos, cacheEntries * sizeof(float4), false))) return r;
+        if ((r = dev_alloc(ctx, ctx->cacheVary, cacheEntries * slg::kMaxVaryings * sizeof(float4), false))) return r;
+        ctx->cacheCap = cacheEntries;
+    }
 
     Frame f;
     std::memset(&f, 0, sizeof(f));
@@ -725,6 +757,15 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     f.depthType = depthTex.type;
     viewport_setup((float)f.width, (float)f.height, f.scissor, f.viewport);
     f.records = static_cast<float4*>(ctx->records.ptr);
+    f.cachePos = static_cast<float4*>(ctx->cachePos.ptr);
+    f.cacheVary = static_cast<float4*>(ctx->cacheVary.ptr);
+    f.cacheEntries = cacheEntries;
+    f.recVerts = static_cast<uint4*>(ctx->recVerts.ptr);
+    f.allCached = cacheEntries > 0 ? 1 : 0;
+    for (size_t i = 0; i < n; ++i)
+    {
+        if (starts[i + 1] > starts[i] && (descs[i].cacheVerts == 0 || descs[i].prim != slg::kPrimTriangle)) f.allCached = 0;
+    }
     f.varyings = static_cast<float4*>(ctx->varyings.ptr);
     f.slotInfo = static_cast<uint32_t*>(ctx->slotInfo.ptr);
     f.slotOvf = static_cast<uint32_t*>(ctx->slotOvf.ptr);
@@ -849,6 +890,7 @@ void slg_context_destroy(slg_context* ctx)
     for (Fbo& f : ctx->fbos) dev_free(f.vis);
     DevBuffer* scratch[] = {&ctx->texTable, &ctx->bufTable, &ctx->records, &ctx->varyings, &ctx->slotInfo, &ctx->slotOvf,
                             &ctx->ovfCount, &ctx->clipQueue, &ctx->clipCount, &ctx->aliasEvents, &ctx->aliasCount,
+                            &ctx->cachePos, &ctx->cacheVary, &ctx->recVerts,
                             &ctx->tileCount, &ctx->tileOffset,
                             &ctx->tileCursor, &ctx->entries, &ctx->blitBuf,
                             &ctx->status, &ctx->devDescs, &ctx->devStarts};
@@ -1451,6 +1493,7 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
     uint64_t numSlots = 0;
     const DrawRequest req = {*m, 1, shaderId, 0};
     if ((r = build_desc(ctx, req, 0, *desc, numSlots))) return r;
+    desc->cacheVerts = 0; /* the static scratch has no vertex cache */
     if (numSlots == 0) return SLG_OK;
     if (numSlots > kNoAllocTris)
         return ctx->fail(SLG_ERR_INVALID_ARG, "slg_draw_noalloc: " + std::to_string(numSlots) + " triangles exceed the static limit of " +

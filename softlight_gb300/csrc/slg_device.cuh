@@ -76,6 +76,8 @@ struct DrawDesc
     uint64_t numInstances;
     uint64_t slotBase;      /* first slot of this draw in the launch */
     uint64_t primBase;      /* primIndex offset (draw_multiple keeps per-mesh primIndex) */
+    uint64_t cacheBase;     /* first vertex-cache entry of the draw (non-decreasing over the launch's draws) */
+    uint64_t cacheVerts;    /* cached vertices per instance (the index buffer's max index + 1); 0: not cached */
     int32_t  indexType;     /* -1: non-indexed */
     uint32_t vsProgram;
     uint32_t fsProgram;
@@ -96,6 +98,9 @@ enum PrimKind
 constexpr uint32_t kRecordPoint = 1u << 5;
 constexpr uint32_t kRecordLine = 1u << 6;
 constexpr uint32_t kRecordWire = 1u << 7;
+/* the record's varyings are the vertex cache's: Frame::recVerts holds the
+ * slot's three cache entries (x, y, z) instead of copies */
+constexpr uint32_t kRecordCached = 1u << 8;
 
 /* Per-launch scratch and framebuffer description. */
 /* Screen tile of launches that contain line or wireframe draws or write
@@ -169,6 +174,15 @@ struct Frame
 
     /* some draw of the launch is a wireframe draw (SL_RENDER_MODE_TRI_WIRE) */
     int32_t hasWire;
+
+    /* post-transform vertex cache of indexed draws that reuse vertices: per
+     * entry (cacheBase + instance * cacheVerts + vertex) the program's
+     * position and kMaxVaryings varyings; cacheEntries 0: unused */
+    float4*  cachePos;
+    float4*  cacheVary;
+    uint64_t cacheEntries;
+    uint4*   recVerts;      /* per slot: the cache entries of a kRecordCached record */
+    int32_t  allCached;     /* every draw with slots is a cached triangle draw */
 
     /* colour attachments 0..numColors-1 (colors[0] == color); hasMrt: some
      * draw writes more than one of them (outputs k -> attachment k) */

@@ -807,17 +807,20 @@ __device__ __forceinline__ float line_interp(const float4* R, uint32_t X, uint32
     return sqrtf(((ex * ex + ey * ey) + 0.f) + 0.f) * R[2].x;
 }
 
-template <bool kLines>
+/* kCached: every draw of the launch is an indexed triangle draw served by
+ * the vertex cache, so the vertex programs are compiled out of this
+ * instantiation (fewer registers, more resident warps). */
+template <bool kLines, bool kCached>
 __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, TileRange& tr, bool& counted)
 {
     const int di = (f.numDraws > 1) ? find_draw(f, slot) : 0;
     const DrawDesc& d = f.draws[di];
     const uint64_t local = slot - d.slotBase;
-    if (d.prim == kPrimPoint)
+    if (!kCached && d.prim == kPrimPoint)
     {
         return setup_point(f, d, di, slot, local, tr, counted);
     }
-    if (kLines && d.prim == kPrimLine)
+    if (!kCached && kLines && d.prim == kPrimLine)
     {
         return setup_line(f, d, di, slot, local, tr, counted);
     }
@@ -831,12 +834,21 @@ __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, Ti
      * registers while culling and set-up run) */
     float4 clip[3];
     uint64_t vids[3];
+    const bool cached = kCached || d.cacheVerts != 0;
 #pragma unroll
     for (int k = 0; k < 3; ++k)
     {
-        slg_v4 unused[kMaxVaryings];
         vids[k] = (d.indexType >= 0) ? read_index(d, i + k) : (i + k);
-        clip[k] = to_f4(run_vertex_program(d.vsProgram, env, vids[k], inst, unused));
+        if (cached)
+        {
+            vids[k] += d.cacheBase + inst * d.cacheVerts;
+            clip[k] = f.cachePos[vids[k]];
+        }
+        else if (!kCached)
+        {
+            slg_v4 unused[kMaxVaryings];
+            clip[k] = to_f4(run_vertex_program(d.vsProgram, env, vids[k], inst, unused));
+        }
     }
 
     if (d.cull != SLG_CULL_OFF)
@@ -865,10 +877,20 @@ __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, Ti
         if (bin_visible(s0, s1, s2))
         {
             Record rec;
-            make_record(s0, s1, s2, (uint32_t)di, primIndex, record_flags(d), rec);
+            make_record(s0, s1, s2, (uint32_t)di, primIndex, record_flags(d) | (cached ? kRecordCached : 0u), rec);
             if (kLines && d.prim == kPrimWire && d.blend != SLG_BLEND_OFF) wire_queue_check(f, rec.r);
             store_record(f, slot, rec);
             tr = tile_range(rec.r[6], f);
+            if (cached)
+            {
+                f.recVerts[slot] = make_uint4((uint32_t)vids[0], (uint32_t)vids[1], (uint32_t)vids[2], 0u);
+                counted = true;
+                return 1;
+            }
+            if (kCached)
+            {
+                return 0;
+            }
             float4* dst = f.varyings + slot * kVaryingVec4;
             const int nv = d.numVaryings;
 #pragma unroll
@@ -926,7 +948,43 @@ __global__ void __launch_bounds__(128) clip_kernel(const Frame f)
     }
 }
 
-template <bool kLines>
+/* Kernel 0: the post-transform vertex cache. One thread per entry runs the
+ * vertex program once for its (draw, instance, vertex); SoftLight runs it for
+ * every triangle corner (SL_TriProcessor.cpp:125-234), which gives the same
+ * values, so the triangle stage reads positions here and the raster reads
+ * varyings here. */
+__global__ void __launch_bounds__(256) vertex_cache_kernel(const Frame f)
+{
+    const uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= f.cacheEntries)
+    {
+        return;
+    }
+    /* the owner is the last draw whose first entry is <= e (uncached draws
+     * own no entries, so one with the same base is never the last) */
+    int lo = 0, hi = f.numDraws - 1;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi + 1) >> 1;
+        if (f.draws[mid].cacheBase <= e) lo = mid;
+        else hi = mid - 1;
+    }
+    const DrawDesc& d = f.draws[lo];
+    const uint64_t local = e - d.cacheBase;
+    const uint64_t inst = local / d.cacheVerts;
+    const uint64_t vid = local - inst * d.cacheVerts;
+    slg_v4 vary[kMaxVaryings];
+    const DevEnv env = make_env(d, f.tables);
+    f.cachePos[e] = to_f4(run_vertex_program(d.vsProgram, env, vid, inst, vary));
+    float4* dst = f.cacheVary + e * kMaxVaryings;
+#pragma unroll
+    for (int vi = 0; vi < kMaxVaryings; ++vi)
+    {
+        if (vi < d.numVaryings) dst[vi] = to_f4(vary[vi]);
+    }
+}
+
+template <bool kLines, bool kCached>
 __global__ void __launch_bounds__(256) vs_setup_kernel(const Frame f)
 {
     const uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -935,7 +993,7 @@ __global__ void __launch_bounds__(256) vs_setup_kernel(const Frame f)
     bool counted = false;
     if (slot < f.numSlots)
     {
-        f.slotInfo[slot] = setup_slot<kLines>(f, slot, tr, counted);
+        f.slotInfo[slot] = setup_slot<kLines, kCached>(f, slot, tr, counted);
     }
     /* per-tile counts of the unclipped records, one atomic per group of
      * lanes touching the same tile (clipped records count themselves) */
@@ -1394,7 +1452,7 @@ __device__ __noinline__ void wire_queue_check(const Frame& f, const float4* R)
  * SL_FragmentProcessor::flush_tri_fragments (SL_FragmentProcessor.cpp:463-529,
  * interpolate_tri_varyings :308-330). Returns whether colour is written. */
 template <bool kExtra>
-__device__ __forceinline__ bool shade(const Frame& f, const DrawDesc& dd, uint64_t rec, float bcw, const float4 r5,
+__device__ __forceinline__ bool shade(const Frame& f, const DrawDesc& dd, uint64_t rec, uint32_t recFlags, float bcw, const float4 r5,
                                       float b0, float b1, float b2, float4& out, size_t gi = 0, int reps = 1)
 {
     const float bp0 = b0 * r5.y, bp1 = b1 * r5.z, bp2 = b2 * r5.w;
@@ -1403,14 +1461,27 @@ __device__ __forceinline__ bool shade(const Frame& f, const DrawDesc& dd, uint64
     const float q0 = bp0 * persp, q1 = bp1 * persp, q2 = bp2 * persp;
 
     slg_v4 vary[4];
-    const float4* V = f.varyings + rec * kVaryingVec4;
+    const float4 *V0, *V1, *V2;
+    if (recFlags & kRecordCached)
+    {
+        const uint4 e = f.recVerts[rec];
+        V0 = f.cacheVary + (size_t)e.x * kMaxVaryings;
+        V1 = f.cacheVary + (size_t)e.y * kMaxVaryings;
+        V2 = f.cacheVary + (size_t)e.z * kMaxVaryings;
+    }
+    else
+    {
+        V0 = f.varyings + rec * kVaryingVec4;
+        V1 = V0 + 4;
+        V2 = V0 + 8;
+    }
     const int nv = dd.numVaryings;
 #pragma unroll
     for (int vi = 0; vi < kMaxVaryings; ++vi)
     {
         if (vi < nv)
         {
-            const float4 a = V[vi], b = V[4 + vi], c = V[8 + vi];
+            const float4 a = V0[vi], b = V1[vi], c = V2[vi];
             vary[vi] = slg_make_v4((a.x * q0 + b.x * q1) + c.x * q2, (a.y * q0 + b.y * q1) + c.y * q2,
                                    (a.z * q0 + b.z * q1) + c.z * q2, (a.w * q0 + b.w * q1) + c.w * q2);
         }
@@ -1710,7 +1781,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                     if (depth_cmp(flags & 0xF, z, sDepth[idx]))
                     {
                         float4 o;
-                        if (shade<kGeneral>(f, dd, rec, R[2].w, R[5], b0, b1, b2, o, (size_t)x + (size_t)f.width * y,
+                        if (shade<kGeneral>(f, dd, rec, flags, R[2].w, R[5], b0, b1, b2, o, (size_t)x + (size_t)f.width * y,
                                           (dd.blend != SLG_BLEND_OFF) ? n : 1) && f.color)
                         {
                             if (dd.blend != SLG_BLEND_OFF)
@@ -1771,7 +1842,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 {
                     const DrawDesc& dd = f.draws[drawIndex];
                     float4 o;
-                    if (shade<kGeneral>(f, dd, key_to_record(f, sRecKey[ri]), R[2].w, R[5], ch.b0, ch.b1, ch.b2, o,
+                    if (shade<kGeneral>(f, dd, key_to_record(f, sRecKey[ri]), flags, R[2].w, R[5], ch.b0, ch.b1, ch.b2, o,
                                       (size_t)ch.x + (size_t)f.width * y) && f.color)
                     {
                         sColor[idx] = (dd.blend != SLG_BLEND_OFF) ? Color::store(blend_color(dd.blend, o, Color::load(sColor[idx])))
@@ -2107,7 +2178,7 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
             const uint32_t kind = __float_as_uint(R[7].w);
             const bool have = (kind & kRecordPoint)            ? shade_point<kGeneral>(f, dd, rec, o, gi)
                               : (kGeneral && (kind & kRecordLine)) ? shade_line<kGeneral>(f, dd, rec, b.x, o, gi)
-                                                                 : shade<kGeneral>(f, dd, rec, R[2].w, R[5], b.x, b.y, b.z, o, gi);
+                                                                 : shade<kGeneral>(f, dd, rec, kind, R[2].w, R[5], b.x, b.y, b.z, o, gi);
             if (have)
             {
                 Color::write(f.color, gi, Color::store(o));
@@ -2228,7 +2299,7 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
                 const float z = wire_fragment(R, R[3].x * yf + R[4].x, R[3].y * yf + R[4].y, R[3].z * yf + R[4].z, 0, b0, b1, b2);
                 if (depth_cmp(func, z, depth))
                 {
-                    const bool have = shade<true>(f, dd, rec, R[2].w, R[5], b0, b1, b2, o, gi, (dd.blend != SLG_BLEND_OFF) ? n : 1);
+                    const bool have = shade<true>(f, dd, rec, flags, R[2].w, R[5], b0, b1, b2, o, gi, (dd.blend != SLG_BLEND_OFF) ? n : 1);
                     for (int v = 0; v < ((dd.blend != SLG_BLEND_OFF) ? n : 1); ++v) put(dd, have, o);
                     if (mask) depth = depth_quant(halfDepth, z);
                 }
@@ -2251,7 +2322,7 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
                 const float z = chain_depth(R, ch);
                 if (depth_cmp(func, z, depth))
                 {
-                    put(dd, shade<true>(f, dd, rec, R[2].w, R[5], ch.b0, ch.b1, ch.b2, o, gi), o);
+                    put(dd, shade<true>(f, dd, rec, flags, R[2].w, R[5], ch.b0, ch.b1, ch.b2, o, gi), o);
                     if (mask) depth = depth_quant(halfDepth, z);
                 }
             }
@@ -2421,11 +2492,16 @@ cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEven
     {
         cudaMemsetAsync(f.aliasCount, 0, sizeof(uint32_t), s);
     }
+    if (f.cacheEntries > 0)
+    {
+        vertex_cache_kernel<<<(unsigned)((f.cacheEntries + 255) / 256), 256, 0, s>>>(f);
+    }
     if (f.numSlots > 0)
     {
         const unsigned blocks = (unsigned)((f.numSlots + vsBlock - 1) / vsBlock);
-        if (f.hasLines || f.hasWire) vs_setup_kernel<true><<<blocks, vsBlock, 0, s>>>(f);
-        else vs_setup_kernel<false><<<blocks, vsBlock, 0, s>>>(f);
+        if (f.hasLines || f.hasWire) vs_setup_kernel<true, false><<<blocks, vsBlock, 0, s>>>(f);
+        else if (f.allCached) vs_setup_kernel<false, true><<<blocks, vsBlock, 0, s>>>(f);
+        else vs_setup_kernel<false, false><<<blocks, vsBlock, 0, s>>>(f);
         clip_kernel<<<152 * 4, 128, 0, s>>>(f);
     }
     if (ev) cudaEventRecord(ev[1], s);
