@@ -73,11 +73,11 @@ def big_triangles(ctx, width=300, height=200, seed=5, wire=False, blend=A.BLEND_
     return s
 
 
-def multi_draw(ctx, width=128, height=96, batched=False, seed=21):
+def multi_draw(ctx, width=128, height=96, batched=False, seed=21, lon=16, lat=8):
     """Several draws with different programs and depth states into one frame,
-    issued one by one or as one batch."""
+    issued one by one or as one batch (lon x lat sphere segments)."""
     s = S.Scene(ctx, "multi", width, height)
-    verts, idx = S.uv_sphere(16, 8)
+    verts, idx = S.uv_sphere(lon, lat)
     sphere = s.add_mesh(verts, idx)
     tex = s.add_texture_rgba8(S.checker(64, 64, 8))
     vp = S.perspective(60.0, width / height, 0.1, 100.0) @ S.look_at((0, 0, 6), (0, 0, 0), (0, 1, 0))

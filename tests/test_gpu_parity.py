@@ -440,3 +440,14 @@ def test_half_and_double_depth_other_primitives(ctxs, depth_type):
                         (E.random_soup, dict(blend=A.BLEND_ADDITIVE, num_tris=800, width=200, height=150, seed=133))]:
         sg, so = render_both(builder, g, o, depth_type=depth_type, **kw)
         compare_scenes(sg, so, f"{builder.__name__} depth type {depth_type}")
+
+
+@pytest.mark.parametrize("batched", [False, True])
+def test_vertex_cache_mixed_launch(ctxs, batched):
+    """Batched, the five 16K-triangle sphere draws are served by the vertex
+    cache in the same launch as the blended, non-indexed soup (which is not);
+    one by one, each draw is below the cache's size threshold."""
+    g, o = ctxs
+    sg, so = render_both(E.multi_draw, g, o, batched=batched, lon=128, lat=64, width=320, height=240)
+    compare_scenes(sg, so, f"cache mix batched={batched}")
+    assert (sg.read_depth() < 1.0).sum() > 10000
