@@ -176,8 +176,9 @@ struct Frame
     int32_t hasWire;
 
     /* post-transform vertex cache of indexed draws that reuse vertices: per
-     * entry (cacheBase + instance * cacheVerts + vertex) the program's
-     * position and kMaxVaryings varyings; cacheEntries 0: unused */
+     * entry e = cacheBase + instance * cacheVerts + vertex the program's
+     * position cachePos[e] and varying vi at cacheVary[vi * cacheEntries + e]
+     * (one plane per varying); cacheEntries 0: unused */
     float4*  cachePos;
     float4*  cacheVary;
     uint64_t cacheEntries;

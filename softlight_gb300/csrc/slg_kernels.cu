@@ -296,11 +296,11 @@ __device__ __forceinline__ float4 mix4(const float4 a, const float4 b, float t)
 
 /* SL_TriProcessor::clip_and_process_tris (SL_TriProcessor.cpp:370-519).
  * Returns the slotInfo value for the slot. */
-struct ClipTri { float4 p[3]; uint64_t vid[3]; };
+struct ClipTri { float4 p[3]; uint64_t vid[3]; };   /* vid: vertex id, or vertex-cache entry of a cached draw */
 
-/* The varyings of a clipped triangle's vertices are recomputed here (the
- * vertex program is a pure function of vertex and instance id), so the
- * common unclipped path keeps them in registers. */
+/* The varyings of a clipped triangle's vertices are read from the vertex
+ * cache or recomputed here (the vertex program is a pure function of vertex
+ * and instance id), so the common unclipped path keeps them in registers. */
 __device__ __noinline__ uint32_t clip_and_emit(const Frame& f, const DrawDesc& d, uint32_t drawIndex, uint64_t slot,
                                                uint64_t primIndex, uint64_t inst, const ClipTri tri)
 {
@@ -315,9 +315,20 @@ __device__ __noinline__ uint32_t clip_and_emit(const Frame& f, const DrawDesc& d
     for (int k = 0; k < 3; ++k)
     {
         newVerts[k] = tri.p[k];
-        slg_v4 vary[4];
-        (void)run_vertex_program(d.vsProgram, env, tri.vid[k], inst, vary);
-        for (int i = 0; i < nv; ++i) newVarys[k * 4 + i] = vary[i];
+        if (d.cacheVerts)
+        {
+            for (int i = 0; i < nv; ++i)
+            {
+                const float4 cv = f.cacheVary[(uint64_t)i * f.cacheEntries + tri.vid[k]];
+                newVarys[k * 4 + i] = slg_make_v4(cv.x, cv.y, cv.z, cv.w);
+            }
+        }
+        else
+        {
+            slg_v4 vary[4];
+            (void)run_vertex_program(d.vsProgram, env, tri.vid[k], inst, vary);
+            for (int i = 0; i < nv; ++i) newVarys[k * 4 + i] = vary[i];
+        }
     }
 
     for (int e = 0; e < 6; ++e)
@@ -940,8 +951,16 @@ __global__ void __launch_bounds__(128) clip_kernel(const Frame f)
         for (int k = 0; k < 3; ++k)
         {
             ct.vid[k] = (d.indexType >= 0) ? read_index(d, i + k) : (i + k);
-            slg_v4 vary[4];
-            ct.p[k] = mat_mul(f.scissor, to_f4(run_vertex_program(d.vsProgram, env, ct.vid[k], inst, vary)));
+            if (d.cacheVerts)
+            {
+                ct.vid[k] += d.cacheBase + inst * d.cacheVerts;
+                ct.p[k] = mat_mul(f.scissor, f.cachePos[ct.vid[k]]);
+            }
+            else
+            {
+                slg_v4 vary[4];
+                ct.p[k] = mat_mul(f.scissor, to_f4(run_vertex_program(d.vsProgram, env, ct.vid[k], inst, vary)));
+            }
         }
         const uint64_t primIndex = d.primBase + d.numElements * inst + i;
         f.slotInfo[slot] = clip_and_emit(f, d, (uint32_t)di, slot, primIndex, inst, ct);
@@ -976,11 +995,10 @@ __global__ void __launch_bounds__(256) vertex_cache_kernel(const Frame f)
     slg_v4 vary[kMaxVaryings];
     const DevEnv env = make_env(d, f.tables);
     f.cachePos[e] = to_f4(run_vertex_program(d.vsProgram, env, vid, inst, vary));
-    float4* dst = f.cacheVary + e * kMaxVaryings;
 #pragma unroll
     for (int vi = 0; vi < kMaxVaryings; ++vi)
     {
-        if (vi < d.numVaryings) dst[vi] = to_f4(vary[vi]);
+        if (vi < d.numVaryings) f.cacheVary[(uint64_t)vi * f.cacheEntries + e] = to_f4(vary[vi]);
     }
 }
 
@@ -1461,19 +1479,24 @@ __device__ __forceinline__ bool shade(const Frame& f, const DrawDesc& dd, uint64
     const float q0 = bp0 * persp, q1 = bp1 * persp, q2 = bp2 * persp;
 
     slg_v4 vary[4];
+    /* varying vi of corner k is V_k[vi * stride]: planes of the vertex
+     * cache, or the record's own copies */
     const float4 *V0, *V1, *V2;
+    size_t stride;
     if (recFlags & kRecordCached)
     {
         const uint4 e = f.recVerts[rec];
-        V0 = f.cacheVary + (size_t)e.x * kMaxVaryings;
-        V1 = f.cacheVary + (size_t)e.y * kMaxVaryings;
-        V2 = f.cacheVary + (size_t)e.z * kMaxVaryings;
+        V0 = f.cacheVary + e.x;
+        V1 = f.cacheVary + e.y;
+        V2 = f.cacheVary + e.z;
+        stride = (size_t)f.cacheEntries;
     }
     else
     {
         V0 = f.varyings + rec * kVaryingVec4;
         V1 = V0 + 4;
         V2 = V0 + 8;
+        stride = 1;
     }
     const int nv = dd.numVaryings;
 #pragma unroll
@@ -1481,7 +1504,7 @@ __device__ __forceinline__ bool shade(const Frame& f, const DrawDesc& dd, uint64
     {
         if (vi < nv)
         {
-            const float4 a = V0[vi], b = V1[vi], c = V2[vi];
+            const float4 a = V0[vi * stride], b = V1[vi * stride], c = V2[vi * stride];
             vary[vi] = slg_make_v4((a.x * q0 + b.x * q1) + c.x * q2, (a.y * q0 + b.y * q1) + c.y * q2,
                                    (a.z * q0 + b.z * q1) + c.z * q2, (a.w * q0 + b.w * q1) + c.w * q2);
         }
