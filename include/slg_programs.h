@@ -236,8 +236,9 @@ SLG_HD bool slg_fs_vcolor_texf(const Env& env, const slg_v4* varyings, slg_v4* o
 
 /* SLG_PROGRAM_GBUFFER: the outputs of a deferred G-buffer pass, one per
  * render target (SL_FragmentParam::pOutputs[0..3]): vertex colour x texture
- * (vertex alpha), the texture sample, the vertex colour, and the uv as
- * (u, v, u*v, 1). The texture is RGBA8 (slg_vcolor_uniforms::textureId). */
+ * (vertex alpha), the texture sample, the vertex colour, and channel products
+ * (r*g, g*b, b*r, texture alpha). Every output stays in [0, 1] for colours
+ * and textures in [0, 1]. The texture is RGBA8 (slg_vcolor_uniforms::textureId). */
 template <class Env>
 SLG_HD bool slg_fs_gbuffer(const Env& env, const slg_v4* varyings, slg_v4* outputs)
 {
@@ -248,7 +249,7 @@ SLG_HD bool slg_fs_gbuffer(const Env& env, const slg_v4* varyings, slg_v4* outpu
     outputs[0] = slg_make_v4(c.x * t.x, c.y * t.y, c.z * t.z, c.w);
     outputs[1] = t;
     outputs[2] = c;
-    outputs[3] = slg_make_v4(uv.x, uv.y, uv.x * uv.y, 1.f);
+    outputs[3] = slg_make_v4(c.x * c.y, c.y * c.z, c.z * c.x, t.w);
     return true;
 }
 

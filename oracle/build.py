@@ -19,7 +19,8 @@ CXXFLAGS = ["-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
 def build_oracle(force=False):
     src = os.path.join(HERE, "slo.cpp")
     deps = [src, os.path.join(HERE, "slo.h"), os.path.join(HERE, "..", "include", "slg.h"),
-            os.path.join(HERE, "..", "include", "slg_programs.h"), __file__]
+            os.path.join(HERE, "..", "include", "slg_programs.h"),
+            os.path.join(HERE, "..", "include", "slg_half.h"), __file__]
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in deps):
         return LIB
     os.makedirs(BUILD, exist_ok=True)

@@ -146,17 +146,13 @@ struct Bin
     uint32_t drawIndex;
 };
 
+/* bytes of a texel of SL_ColorDataType 0..27 (components type / 7 + 1 of
+ * u8, u16, u32, u64, half, float, double by type % 7) */
 static size_t bytes_per_color(int type)
 {
-    switch (type)
-    {
-        case SLG_COLOR_R_HALF: return 2;
-        case SLG_COLOR_R_FLOAT: return 4;
-        case SLG_COLOR_R_DOUBLE: return 8;
-        case SLG_COLOR_RGBA_8U: return 4;
-        case SLG_COLOR_RGBA_FLOAT: return 16;
-        default: return 0;
-    }
+    if (type < 0 || type > 27) return 0;
+    static const size_t kind[7] = {1, 2, 4, 8, 2, 4, 8};
+    return (size_t)(type / 7 + 1) * kind[type % 7];
 }
 
 static size_t index_bytes(int type)
@@ -650,30 +646,115 @@ struct Target
 };
 
 /* assign_pixel / assign_alpha_pixel, portable (SL_Framebuffer.cpp:45-80,271-368) */
+/* float -> unsigned as the reference build does it on x86-64: cvttss2si,
+ * 32-bit values from its 64-bit form, 64-bit values from gcc's two-range
+ * sequence (so 1.0 * (float)UINT32_MAX stores 0) */
+static inline uint64_t cvt_f32_i64(float x)
+{
+    return (x >= -9223372036854775808.f && x < 9223372036854775808.f) ? (uint64_t)(int64_t)x : 0x8000000000000000ull;
+}
+
+static inline uint64_t f2u_x86(float x, int kind)
+{
+    if (kind <= 1) return (uint64_t)(uint32_t)f2i(x);
+    if (kind == 2) return cvt_f32_i64(x) & 0xFFFFFFFFull;
+    if (!(x >= 9223372036854775808.f)) return cvt_f32_i64(x);
+    return cvt_f32_i64(x - 9223372036854775808.f) ^ 0x8000000000000000ull;
+}
+
+/* RGBA u32 texels: converting an out-of-range or NaN float to unsigned is
+ * undefined in C++, and for four-lane u32 vectors the reference build
+ * (x86-64 SSE2) emits the vectorised form: x >= 2^31 ? cvttps2dq(x - 2^31)
+ * ^ 2^31 : cvttps2dq(x), where cvttps2dq gives 0x80000000 out of int32
+ * range. In-range values convert identically either way. */
+static inline uint32_t f2u32_vec(float x)
+{
+    const bool big = x >= 2147483648.f;
+    const float y = big ? x - 2147483648.f : x;
+    const uint32_t i = (y >= -2147483648.f && y < 2147483648.f) ? (uint32_t)(int32_t)y : 0x80000000u;
+    return big ? (i ^ 0x80000000u) : i;
+}
+
+static inline uint32_t d2u32_vec(double x)
+{
+    const bool big = x >= 2147483648.0;
+    const double y = big ? x - 2147483648.0 : x;
+    const uint32_t i = (y >= -2147483648.0 && y < 2147483648.0) ? (uint32_t)(int32_t)y : 0x80000000u;
+    return big ? (i ^ 0x80000000u) : i;
+}
+
+/* component j of texel idx as float: color_cast<float, T> (SL_Color.hpp:640-670) */
+static inline float component_get(const Target& t, size_t idx, int j)
+{
+    const int nc = t.type / 7 + 1, kind = t.type % 7;
+    const size_t cb = bytes_per_color(t.type) / nc;
+    const uint8_t* c = t.bytes + (idx * nc + j) * cb;
+    switch (kind)
+    {
+        case 0: return (float)c[0] * 0.00392156862745f;
+        case 1: { uint16_t v; std::memcpy(&v, c, 2); return (float)v * (1.f / 65535.f); }
+        case 2: { uint32_t v; std::memcpy(&v, c, 4); return (float)v * (1.f / 4294967295.f); }
+        case 3: { uint64_t v; std::memcpy(&v, c, 8); return (float)v * (1.f / 18446744073709551615.f); }
+        case 4: { uint16_t v; std::memcpy(&v, c, 2); return slg_half_to_float(v); }
+        case 5: { float v; std::memcpy(&v, c, 4); return v; }
+        default: { double v; std::memcpy(&v, c, 8); return (float)v; }
+    }
+}
+
+/* the format's maximum as float: the alpha a texel without one is read with */
+static inline float kind_one(int kind)
+{
+    switch (kind)
+    {
+        case 0: return 255.f * 0.00392156862745f;
+        case 1: return 65535.f * (1.f / 65535.f);
+        case 2: return 4294967295.f * (1.f / 4294967295.f);
+        case 3: return 18446744073709551615.f * (1.f / 18446744073709551615.f);
+        default: return 1.f;
+    }
+}
+
+/* color_cast<T, float> of one component (SL_Color.hpp:618-637) */
+static inline void component_set(const Target& t, size_t idx, int j, float x)
+{
+    const int nc = t.type / 7 + 1, kind = t.type % 7;
+    const size_t cb = bytes_per_color(t.type) / nc;
+    uint8_t* c = t.bytes + (idx * nc + j) * cb;
+    static const float kMax[4] = {255.f, 65535.f, 4294967295.f, 18446744073709551615.f};
+    if (kind == 2 && nc == 4)
+    {
+        const uint32_t u = f2u32_vec(x * kMax[kind]);
+        std::memcpy(c, &u, 4);
+    }
+    else if (kind <= 3)
+    {
+        const uint64_t u = f2u_x86(x * kMax[kind], kind);
+        std::memcpy(c, &u, cb);   /* little-endian low bytes */
+    }
+    else if (kind == 4) { const uint16_t h = slg_float_to_half(x); std::memcpy(c, &h, 2); }
+    else if (kind == 5) std::memcpy(c, &x, 4);
+    else { const double d = (double)x; std::memcpy(c, &d, 8); }
+}
+
+/* assign_pixel / assign_alpha_pixel (softlight/src/SL_Framebuffer.cpp:45-80,
+ * 266-366): the blend reads the texel padded with the format's min (green,
+ * blue) and max (alpha), a three-component texel as (r, r, r, max); the
+ * blended value is clamped to [0, 1]; components beyond the format's are
+ * dropped. */
 static inline void write_color(const Target& t, unsigned x, unsigned y, const V4& rgba, uint8_t blend)
 {
     const size_t idx = (size_t)x + (size_t)t.w * y;
+    const int nc = t.type / 7 + 1, kind = t.type % 7;
     V4 src = rgba;
 
     if (blend != SLG_BLEND_OFF)
     {
         V4 d;
-        if (t.type == SLG_COLOR_RGBA_8U)
-        {
-            const uint8_t* q = t.bytes + 4 * idx;
-            d = mk((float)q[0] * 0.00392156862745f, (float)q[1] * 0.00392156862745f,
-                   (float)q[2] * 0.00392156862745f, (float)q[3] * 0.00392156862745f);
-        }
-        else if (t.type == SLG_COLOR_RGBA_FLOAT)
-        {
-            const float* q = reinterpret_cast<const float*>(t.bytes) + 4 * idx;
-            d = mk(q[0], q[1], q[2], q[3]);
-        }
-        else
-        {
-            const float* q = reinterpret_cast<const float*>(t.bytes) + idx;
-            d = mk(q[0], 0.f, 0.f, 1.f);
-        }
+        const float r = component_get(t, idx, 0);
+        if (nc == 1) d = mk(r, 0.f, 0.f, kind_one(kind));
+        else if (nc == 2) d = mk(r, component_get(t, idx, 1), 0.f, kind_one(kind));
+        else if (nc == 3) d = mk(r, r, r, kind_one(kind));
+        else d = mk(r, component_get(t, idx, 1), component_get(t, idx, 2), component_get(t, idx, 3));
 
         const float sa = rgba[3];
         const float modulation = 1.f - sa;
@@ -681,9 +762,9 @@ static inline void write_color(const Target& t, unsigned x, unsigned y, const V4
         {
             const float dstMod = modulation * d[3];
             const float dstAlpha = dstMod + sa;
-            const float r = 1.f / dstAlpha;
-            d = mk((rgba[0] * sa + d[0] * dstMod) * r, (rgba[1] * sa + d[1] * dstMod) * r,
-                   (rgba[2] * sa + d[2] * dstMod) * r, dstAlpha);
+            const float rc = 1.f / dstAlpha;
+            d = mk((rgba[0] * sa + d[0] * dstMod) * rc, (rgba[1] * sa + d[1] * dstMod) * rc,
+                   (rgba[2] * sa + d[2] * dstMod) * rc, dstAlpha);
         }
         else if (blend == SLG_BLEND_PREMULTIPLED_ALPHA)
         {
@@ -705,24 +786,7 @@ static inline void write_color(const Target& t, unsigned x, unsigned y, const V4
         src = d;
     }
 
-    if (t.type == SLG_COLOR_RGBA_8U)
-    {
-        uint8_t* q = t.bytes + 4 * idx;
-        for (int k = 0; k < 4; ++k)
-        {
-            q[k] = f2u8(src[k] * 255.f);
-        }
-    }
-    else if (t.type == SLG_COLOR_RGBA_FLOAT)
-    {
-        float* q = reinterpret_cast<float*>(t.bytes) + 4 * idx;
-        for (int k = 0; k < 4; ++k) q[k] = src[k];
-    }
-    else
-    {
-        float* q = reinterpret_cast<float*>(t.bytes) + idx;
-        q[0] = src[0];
-    }
+    for (int j = 0; j < nc; ++j) component_set(t, idx, j, src[j]);
 }
 
 static inline bool depth_cmp(uint8_t func, float z, float d)
@@ -1522,41 +1586,37 @@ static size_t clear_reach(size_t count, unsigned threads)
     return reach;
 }
 
+/* double -> unsigned as x86-64 code does it (cvttsd2si, as f2u_x86) */
+static inline uint64_t d2u_x86(double v, int kind)
+{
+    const auto i64 = [](double w) { return (w >= -9223372036854775808.0 && w < 9223372036854775808.0) ? (uint64_t)(int64_t)w : 0x8000000000000000ull; };
+    if (kind <= 1) return (uint64_t)(uint32_t)((v >= -2147483648.0 && v < 2147483648.0) ? (int32_t)v : INT32_MIN);
+    if (kind == 2) return i64(v) & 0xFFFFFFFFull;
+    if (!(v >= 9223372036854775808.0)) return i64(v);
+    return i64(v - 9223372036854775808.0) ^ 0x8000000000000000ull;
+}
+
+/* SL_Context::clear_color_buffer / clear_depth_buffer: per component
+ * color_cast<T, double> (sl_match_color_for_type, SL_Color.cpp:137-192;
+ * SL_Context.cpp:897-913 for depth), over the texels the clear reaches */
 static void clear_color(Texture& t, const double rgba[4], unsigned threads)
 {
     const size_t n = clear_reach((size_t)t.w * t.h, threads);
-    if (t.type == SLG_COLOR_RGBA_8U)
+    const size_t bpt = bytes_per_color(t.type);
+    const int nc = t.type / 7 + 1, kind = t.type % 7;
+    const size_t cb = bpt / nc;
+    static const double kMax[4] = {255.0, 65535.0, 4294967295.0, 18446744073709551615.0};
+    uint8_t texel[32] = {0};
+    for (int j = 0; j < nc; ++j)
     {
-        /* color_cast<uint8_t, double> (SL_Color.cpp:148; SL_Color.hpp:625) */
-        uint8_t c[4];
-        for (int k = 0; k < 4; ++k)
-        {
-            const double v = rgba[k] * 255.0;
-            c[k] = (uint8_t)(uint32_t)((v != v || v >= 2147483648.0 || v < -2147483648.0) ? INT32_MIN : (int32_t)v);
-        }
-        for (size_t i = 0; i < n; ++i) std::memcpy(t.bytes.data() + 4 * i, c, 4);
+        uint8_t* c = texel + j * cb;
+        if (kind == 2 && nc == 4) { const uint32_t u = d2u32_vec(rgba[j] * kMax[kind]); std::memcpy(c, &u, 4); }
+        else if (kind <= 3) { const uint64_t u = d2u_x86(rgba[j] * kMax[kind], kind); std::memcpy(c, &u, cb); }
+        else if (kind == 4) { const uint16_t h = slg_float_to_half((float)rgba[j]); std::memcpy(c, &h, 2); }
+        else if (kind == 5) { const float f = (float)rgba[j]; std::memcpy(c, &f, 4); }
+        else std::memcpy(c, &rgba[j], 8);
     }
-    else if (t.type == SLG_COLOR_RGBA_FLOAT)
-    {
-        const float c[4] = {(float)rgba[0], (float)rgba[1], (float)rgba[2], (float)rgba[3]};
-        for (size_t i = 0; i < n; ++i) std::memcpy(t.bytes.data() + 16 * i, c, 16);
-    }
-    else if (t.type == SLG_COLOR_R_HALF)
-    {
-        /* SL_Context::clear_depth_buffer: (half)(float)depth (SL_Context.cpp:897-913) */
-        const uint16_t c = slg_float_to_half((float)rgba[0]);
-        for (size_t i = 0; i < n; ++i) std::memcpy(t.bytes.data() + 2 * i, &c, 2);
-    }
-    else if (t.type == SLG_COLOR_R_DOUBLE)
-    {
-        const double c = rgba[0];
-        for (size_t i = 0; i < n; ++i) std::memcpy(t.bytes.data() + 8 * i, &c, 8);
-    }
-    else
-    {
-        const float c = (float)rgba[0];
-        for (size_t i = 0; i < n; ++i) std::memcpy(t.bytes.data() + 4 * i, &c, 4);
-    }
+    for (size_t i = 0; i < n; ++i) std::memcpy(t.bytes.data() + bpt * i, texel, bpt);
 }
 
 int slo_clear_color_buffer(slo_context* ctx, size_t fbo, unsigned att, const double rgba[4])

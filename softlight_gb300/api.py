@@ -27,11 +27,21 @@ DEPTH_TEST_OFF, DEPTH_TEST_LESS_THAN, DEPTH_TEST_LESS_EQUAL, DEPTH_TEST_GREATER_
 DEPTH_TEST_GREATER_EQUAL, DEPTH_TEST_EQUAL, DEPTH_TEST_NOT_EQUAL = 4, 5, 6
 DEPTH_MASK_OFF, DEPTH_MASK_ON = 0, 1
 BLEND_OFF, BLEND_ALPHA, BLEND_PREMULTIPLED_ALPHA, BLEND_ADDITIVE, BLEND_SCREEN = 0, 1, 2, 3, 4
-COLOR_R_HALF, COLOR_R_FLOAT, COLOR_R_DOUBLE, COLOR_RGBA_8U, COLOR_RGBA_FLOAT = 4, 5, 6, 21, 26
+# SL_ColorDataType 0..27: (R, RG, RGB, RGBA) x (8U, 16U, 32U, 64U, HALF, FLOAT, DOUBLE)
+COLOR_COMPONENT_DTYPES = ("uint8", "uint16", "uint32", "uint64", "float16", "float32", "float64")
+for _n, _prefix in enumerate(("R", "RG", "RGB", "RGBA")):
+    for _k, _suffix in enumerate(("8U", "16U", "32U", "64U", "HALF", "FLOAT", "DOUBLE")):
+        globals()[f"COLOR_{_prefix}_{_suffix}"] = 7 * _n + _k
+COLOR_TYPES = tuple(range(28))
 PROGRAM_LAMBERT_TEX, PROGRAM_BLINN_PHONG_INST, PROGRAM_VCOLOR_TEX_ALPHA = 1, 2, 3
 PROGRAM_VCOLOR_TEXF, PROGRAM_FLAT_COLOR, PROGRAM_GBUFFER = 4, 5, 6
 
-BYTES_PER_COLOR = {COLOR_R_HALF: 2, COLOR_R_FLOAT: 4, COLOR_R_DOUBLE: 8, COLOR_RGBA_8U: 4, COLOR_RGBA_FLOAT: 16}
+BYTES_PER_COLOR = {t: (t // 7 + 1) * (1, 2, 4, 8, 2, 4, 8)[t % 7] for t in COLOR_TYPES}
+
+
+def color_layout(t):
+    """(components, numpy dtype name) of a colour format."""
+    return t // 7 + 1, COLOR_COMPONENT_DTYPES[t % 7]
 
 
 class Mesh(C.Structure):

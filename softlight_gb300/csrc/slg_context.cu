@@ -60,17 +60,46 @@ struct Shader
     size_t ubo;
 };
 
+/* Bytes of a texel of SL_ColorDataType 0..27: components (type / 7 + 1) x
+ * the size of u8, u16, u32, u64, half, float or double (type % 7). */
 size_t bytes_per_color(int type)
 {
-    switch (type)
-    {
-        case SLG_COLOR_R_HALF: return 2;
-        case SLG_COLOR_R_FLOAT: return 4;
-        case SLG_COLOR_R_DOUBLE: return 8;
-        case SLG_COLOR_RGBA_8U: return 4;
-        case SLG_COLOR_RGBA_FLOAT: return 16;
-        default: return 0;
-    }
+    if (type < 0 || type > 27) return 0;
+    static const size_t kind[7] = {1, 2, 4, 8, 2, 4, 8};
+    return (size_t)(type / 7 + 1) * kind[type % 7];
+}
+
+bool core_color_type(int type)
+{
+    return type == SLG_COLOR_RGBA_8U || type == SLG_COLOR_RGBA_FLOAT || type == SLG_COLOR_R_FLOAT;
+}
+
+/* double -> unsigned as x86-64 code does it (cvttsd2si; 32-bit values from
+ * the 64-bit form, 64-bit values from gcc's two-range sequence): the clear
+ * colour conversion color_cast<T, double> of the reference build */
+int64_t cvt_f64_i64(double v)
+{
+    return (v >= -9223372036854775808.0 && v < 9223372036854775808.0) ? (int64_t)v : INT64_MIN;
+}
+
+/* RGBA u32 clear values: the reference build converts four-lane u32
+ * vectors with the vectorised SSE2 form (cvttpd2dq of x or of x - 2^31,
+ * 0x80000000 out of int32 range); the conversion is undefined in C++ out of
+ * range, identical within it. */
+uint32_t d2u32_vec(double x)
+{
+    const bool big = x >= 2147483648.0;
+    const double y = big ? x - 2147483648.0 : x;
+    const uint32_t i = (y >= -2147483648.0 && y < 2147483648.0) ? (uint32_t)(int32_t)y : 0x80000000u;
+    return big ? (i ^ 0x80000000u) : i;
+}
+
+uint64_t d2u_x86(double v, int kind)
+{
+    if (kind <= 1) return (uint64_t)(uint32_t)((v >= -2147483648.0 && v < 2147483648.0) ? (int32_t)v : INT32_MIN);
+    if (kind == 2) return (uint64_t)cvt_f64_i64(v) & 0xFFFFFFFFull;
+    if (!(v >= 9223372036854775808.0)) return (uint64_t)cvt_f64_i64(v);
+    return (uint64_t)cvt_f64_i64(v - 9223372036854775808.0) ^ 0x8000000000000000ull;
 }
 
 size_t index_bytes(int type)
@@ -309,46 +338,45 @@ int check_status(slg_context* ctx)
     return ctx->fail(SLG_ERR_OVERFLOW, msg);
 }
 
-int color_value(int type, const double rgba[4], uint32_t out[4])
+/* The clear value of a texel of `type` (SL_Context::clear_color_buffer ->
+ * sl_match_color_for_type, softlight/src/SL_Color.cpp:137-192): per component
+ * color_cast<T, double>, i.e. (T)(c * (double)max) for unsigned T, a half from
+ * (float)c, (float)c or c. out: the texel's bytes (up to 32). */
+int color_value(int type, const double rgba[4], uint32_t out[8])
 {
-    std::memset(out, 0, 4 * sizeof(uint32_t));
-    if (type == SLG_COLOR_RGBA_8U)
+    std::memset(out, 0, 8 * sizeof(uint32_t));
+    const size_t bpt = bytes_per_color(type);
+    if (!bpt) return -1;
+    const int nc = type / 7 + 1, kind = type % 7;
+    static const double kMax[4] = {255.0, 65535.0, 4294967295.0, 18446744073709551615.0};
+    uint8_t* bytes = reinterpret_cast<uint8_t*>(out);
+    for (int j = 0; j < nc; ++j)
     {
-        uint32_t packed = 0;
-        for (int k = 0; k < 4; ++k)
+        uint8_t* c = bytes + (size_t)j * (bpt / nc);
+        if (kind == 2 && nc == 4)
         {
-            const double v = rgba[k] * 255.0;
-            const int32_t iv = (v != v || v >= 2147483648.0 || v < -2147483648.0) ? INT32_MIN : (int32_t)v;
-            packed |= ((uint32_t)iv & 0xFFu) << (8 * k);
+            const uint32_t u = d2u32_vec(rgba[j] * kMax[kind]);
+            std::memcpy(c, &u, 4);
         }
-        out[0] = packed;
-    }
-    else if (type == SLG_COLOR_RGBA_FLOAT)
-    {
-        for (int k = 0; k < 4; ++k)
+        else if (kind <= 3)
         {
-            const float f = (float)rgba[k];
-            std::memcpy(&out[k], &f, 4);
+            const uint64_t u = d2u_x86(rgba[j] * kMax[kind], kind);
+            std::memcpy(c, &u, bpt / nc);   /* little-endian low bytes */
         }
-    }
-    else if (type == SLG_COLOR_R_FLOAT)
-    {
-        const float f = (float)rgba[0];
-        std::memcpy(&out[0], &f, 4);
-    }
-    else if (type == SLG_COLOR_R_HALF)
-    {
-        /* SL_Context::clear_depth_buffer: (half)(float)depth (softlight/src/SL_Context.cpp:897-913) */
-        out[0] = slg_float_to_half((float)rgba[0]);
-    }
-    else if (type == SLG_COLOR_R_DOUBLE)
-    {
-        const double d = rgba[0];
-        std::memcpy(&out[0], &d, 8);
-    }
-    else
-    {
-        return -1;
+        else if (kind == 4)
+        {
+            const uint16_t h = slg_float_to_half((float)rgba[j]);
+            std::memcpy(c, &h, 2);
+        }
+        else if (kind == 5)
+        {
+            const float f = (float)rgba[j];
+            std::memcpy(c, &f, 4);
+        }
+        else
+        {
+            std::memcpy(c, &rgba[j], 8);
+        }
     }
     return 0;
 }
@@ -372,7 +400,7 @@ uint64_t clear_extent(uint64_t count, unsigned threads)
 int clear_texture(slg_context* ctx, size_t texId, const double rgba[4])
 {
     const Texture& t = ctx->textures[texId];
-    uint32_t v[4];
+    uint32_t v[8];
     if (color_value(t.type, rgba, v)) return ctx->fail(SLG_ERR_INVALID_ARG, "unsupported clear format");
     const uint64_t texels = clear_extent((uint64_t)t.w * t.h, ctx->numThreads);
     cudaError_t e = slg::launch_clear(static_cast<uint8_t*>(t.buf.ptr), (size_t)texels, (int)t.bpt, v, ctx->stream);
@@ -545,12 +573,14 @@ int bind_attachments(slg_context* ctx, const Fbo& fbo, const Texture& depthTex, 
         const Texture& t = ctx->textures[fbo.colors[k]];
         if (!t.buf.ptr) break;
         if (t.w != depthTex.w || t.h != depthTex.h) return ctx->fail(SLG_ERR_INVALID_ARG, "colour and depth attachments differ in size");
-        if (t.type != SLG_COLOR_RGBA_8U && t.type != SLG_COLOR_RGBA_FLOAT && t.type != SLG_COLOR_R_FLOAT)
-            return ctx->fail(SLG_ERR_INVALID_ARG, "unsupported colour attachment format");
+        if (!bytes_per_color(t.type)) return ctx->fail(SLG_ERR_INVALID_ARG, "unsupported colour attachment format");
         f.colors[k] = static_cast<uint8_t*>(t.buf.ptr);
         f.colorTypes[k] = t.type;
         f.numColors = (int32_t)k + 1;
     }
+    /* attachment 0 of another format is written like attachments 1..3 */
+    f.generic0 = (f.numColors > 0 && !core_color_type(f.colorTypes[0])) ? 1 : 0;
+    if (f.generic0) f.hasMrt = 1;
     for (size_t i = 0; i < n; ++i)
     {
         if (f.numColors > 0 && descs[i].numOutputs > f.numColors)
@@ -753,6 +783,7 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
 
     f.color = colorTex ? static_cast<uint8_t*>(colorTex->buf.ptr) : nullptr;
     f.colorType = colorTex ? colorTex->type : SLG_COLOR_RGBA_8U;
+    if (f.generic0) f.color = nullptr;
     f.depth = static_cast<float*>(depthTex.buf.ptr);
     f.depthType = depthTex.type;
     viewport_setup((float)f.width, (float)f.height, f.scissor, f.viewport);
@@ -1569,6 +1600,7 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
 
     f.color = colorTex ? static_cast<uint8_t*>(colorTex->buf.ptr) : nullptr;
     f.colorType = colorTex ? colorTex->type : SLG_COLOR_RGBA_8U;
+    if (f.generic0) f.color = nullptr;
     f.depth = static_cast<float*>(depthTex.buf.ptr);
     f.depthType = depthTex.type;
     viewport_setup((float)f.width, (float)f.height, f.scissor, f.viewport);

@@ -121,8 +121,7 @@ struct AliasEvent
     uint32_t pixel;     /* linear index of the shared pixel (column 0) */
     uint32_t queued;    /* steps 0 < k < dx that passed the depth test */
     float    depth0;    /* the pixel's depth before the launch */
-    uint4    color0;    /* the pixel's colour bits before the launch, attachment 0 */
-    uint4    colorN[3]; /* and attachments 1..3 */
+    uint8_t  colors[4][32]; /* the pixel's texel bytes before the launch, attachments 0..3 */
 };
 
 struct Frame
@@ -191,6 +190,10 @@ struct Frame
     int32_t  colorTypes[4];
     int32_t  numColors;
     int32_t  hasMrt;
+    /* attachment 0 has a format other than RGBA8, RGBA float or R float: it
+     * is written like attachments 1..3 (general raster, global memory) and
+     * `color` is null */
+    int32_t  generic0;
 
     /* line address aliases (AliasEvent); null without line draws. Order-free
      * launches take the ordered raster when any alias was logged. */

@@ -182,6 +182,13 @@ __device__ __forceinline__ float depth_quant(bool halfDepth, float z)
     return halfDepth ? slg_half_to_float(slg_float_to_half(z)) : z;
 }
 
+/* bytes of a texel of colour format `type` (SL_ColorDataType 0..27) */
+__device__ __forceinline__ int texel_bytes(int type)
+{
+    const int kind = type % 7;
+    return (type / 7 + 1) * ((kind == 0) ? 1 : (kind == 1 || kind == 4) ? 2 : (kind == 2 || kind == 5) ? 4 : 8);
+}
+
 /* r7.w of a triangle record: depth test, depth mask, wireframe bit */
 __device__ __forceinline__ uint32_t record_flags(const DrawDesc& d)
 {
@@ -664,22 +671,10 @@ __device__ __forceinline__ uint32_t setup_line(const Frame& f, const DrawDesc& d
             ev.pixel = pix;
             ev.queued = 0;
             ev.depth0 = depth_load(f, pix);
-            uint4 c = make_uint4(0u, 0u, 0u, 0u);
-            if (f.color)
+            for (int k = 0; k < f.numColors; ++k)
             {
-                if (f.colorType == SLG_COLOR_RGBA_FLOAT) c = reinterpret_cast<const uint4*>(f.color)[pix];
-                else c.x = reinterpret_cast<const uint32_t*>(f.color)[pix];
-            }
-            ev.color0 = c;
-            for (int k = 1; k < 4; ++k)
-            {
-                uint4 ck = make_uint4(0u, 0u, 0u, 0u);
-                if (k < f.numColors)
-                {
-                    if (f.colorTypes[k] == SLG_COLOR_RGBA_FLOAT) ck = reinterpret_cast<const uint4*>(f.colors[k])[pix];
-                    else ck.x = reinterpret_cast<const uint32_t*>(f.colors[k])[pix];
-                }
-                ev.colorN[k - 1] = ck;
+                const int bpt = texel_bytes(f.colorTypes[k]);
+                for (int b = 0; b < bpt; ++b) ev.colors[k][b] = f.colors[k][(size_t)pix * bpt + b];
             }
             aliasTag = (int)e + 1;
         }
@@ -1207,20 +1202,126 @@ __device__ __forceinline__ float4 blend_color(int mode, const float4 s, const fl
     return r;
 }
 
-/* A texel of an attachment of one of the supported colour formats, as the
- * float4 the blend reads and from the float4 a fragment writes. */
+/*-----------------------------------------------------------------------------
+ * Colour formats (SL_ColorDataType 0..27: R / RG / RGB / RGBA of u8, u16,
+ * u32, u64, half, float, double). A fragment output is written as
+ * color_cast<T, float> (SL_Color.hpp:606-660): integers (T)(x * (float)max),
+ * half and double by conversion; the blend reads color_cast<float, T> of the
+ * texel padded by assign_alpha_pixel (SL_Framebuffer.cpp:268-312): missing
+ * green / blue are the format's minimum and alpha its maximum, and a
+ * three-component texel is read as (r, r, r, max). Float -> unsigned
+ * conversions follow the reference as compiled for x86-64 (cvttss2si, with
+ * 32-bit values taken from its 64-bit form and 64-bit ones from gcc's
+ * two-range sequence), so e.g. 1.0 stores 0 in a u32 or u64 channel, as the
+ * reference does.
+-----------------------------------------------------------------------------*/
+__device__ __forceinline__ int format_components(int type) { return type / 7 + 1; }
+__device__ __forceinline__ int format_kind(int type) { return type % 7; }   /* 0 u8 1 u16 2 u32 3 u64 4 half 5 float 6 double */
+__device__ __forceinline__ int kind_bytes(int kind) { return (kind == 0) ? 1 : (kind == 1 || kind == 4) ? 2 : (kind == 2 || kind == 5) ? 4 : 8; }
+
+/* cvttss2si with a 64-bit destination: NaN and out of range give INT64_MIN */
+__device__ __forceinline__ uint64_t cvt_f32_i64(float x)
+{
+    return (x >= -9223372036854775808.f && x < 9223372036854775808.f) ? (uint64_t)__float2ll_rz(x) : 0x8000000000000000ull;
+}
+
+__device__ __forceinline__ uint64_t f2u_x86(float x, int kind)
+{
+    if (kind <= 1) return (uint64_t)(uint32_t)f2i(x);            /* u8 / u16: 32-bit cvttss2si */
+    if (kind == 2) return cvt_f32_i64(x) & 0xFFFFFFFFull;        /* u32: low half of the 64-bit form */
+    if (!(x >= 9223372036854775808.f)) return cvt_f32_i64(x);     /* u64 below 2^63 (and NaN) */
+    return cvt_f32_i64(x - 9223372036854775808.f) ^ 0x8000000000000000ull;
+}
+
+/* RGBA u32 texels: converting an out-of-range or NaN float to unsigned is
+ * undefined in C++, and for four-lane u32 vectors the reference build
+ * (x86-64 SSE2) emits the vectorised form: x >= 2^31 ? cvttps2dq(x - 2^31)
+ * ^ 2^31 : cvttps2dq(x), where cvttps2dq gives 0x80000000 out of int32
+ * range. In-range values convert identically either way. */
+__device__ __forceinline__ uint32_t f2u32_vec(float x)
+{
+    const bool big = x >= 2147483648.f;
+    const float y = big ? x - 2147483648.f : x;
+    const uint32_t i = (y >= -2147483648.f && y < 2147483648.f) ? (uint32_t)__float2int_rz(y) : 0x80000000u;
+    return big ? (i ^ 0x80000000u) : i;
+}
+
+__device__ __forceinline__ float kind_max(int kind)
+{
+    return (kind == 0) ? 255.f : (kind == 1) ? 65535.f : (kind == 2) ? 4294967295.f : 18446744073709551615.f;
+}
+
+/* component j of texel i as float (color_cast<float, T>) */
+__device__ __forceinline__ float component_load(int kind, int nc, const uint8_t* p, size_t i, int j)
+{
+    const uint8_t* c = p + (i * (size_t)nc + (size_t)j) * (size_t)kind_bytes(kind);
+    switch (kind)
+    {
+        case 0: return (float)c[0] * 0.00392156862745f;
+        case 1: return (float)*reinterpret_cast<const uint16_t*>(c) * (1.f / 65535.f);
+        case 2: return (float)*reinterpret_cast<const uint32_t*>(c) * (1.f / 4294967295.f);
+        case 3: return (float)*reinterpret_cast<const unsigned long long*>(c) * (1.f / 18446744073709551615.f);
+        case 4: return slg_half_to_float(*reinterpret_cast<const uint16_t*>(c));
+        case 5: return *reinterpret_cast<const float*>(c);
+        default: return (float)*reinterpret_cast<const double*>(c);
+    }
+}
+
+/* the format's maximum as float (the padding of a missing alpha) */
+__device__ __forceinline__ float kind_one(int kind)
+{
+    switch (kind)
+    {
+        case 0: return 255.f * 0.00392156862745f;
+        case 1: return 65535.f * (1.f / 65535.f);
+        case 2: return 4294967295.f * (1.f / 4294967295.f);
+        case 3: return 18446744073709551615.f * (1.f / 18446744073709551615.f);
+        default: return 1.f;
+    }
+}
+
+__device__ __forceinline__ void component_store(int kind, int nc, uint8_t* p, size_t i, int j, float x)
+{
+    uint8_t* c = p + (i * (size_t)nc + (size_t)j) * (size_t)kind_bytes(kind);
+    switch (kind)
+    {
+        case 0: c[0] = (uint8_t)f2u_x86(x * 255.f, 0); break;
+        case 1: *reinterpret_cast<uint16_t*>(c) = (uint16_t)f2u_x86(x * 65535.f, 1); break;
+        case 2: *reinterpret_cast<uint32_t*>(c) = (nc == 4) ? f2u32_vec(x * 4294967295.f) : (uint32_t)f2u_x86(x * 4294967295.f, 2); break;
+        case 3: *reinterpret_cast<unsigned long long*>(c) = f2u_x86(x * 18446744073709551615.f, 3); break;
+        case 4: *reinterpret_cast<uint16_t*>(c) = slg_float_to_half(x); break;
+        case 5: *reinterpret_cast<float*>(c) = x; break;
+        default: *reinterpret_cast<double*>(c) = (double)x; break;
+    }
+}
+
+/* A texel of an attachment, as the float4 the blend reads and from the
+ * float4 a fragment writes (the three core formats keep their fast forms). */
 __device__ __forceinline__ float4 texel_load(int type, const uint8_t* p, size_t i)
 {
     if (type == SLG_COLOR_RGBA_FLOAT) return ColorRGBAF::load(ColorRGBAF::read(p, i));
     if (type == SLG_COLOR_R_FLOAT) return ColorRF::load(ColorRF::read(p, i));
-    return ColorRGBA8::load(ColorRGBA8::read(p, i));
+    if (type == SLG_COLOR_RGBA_8U) return ColorRGBA8::load(ColorRGBA8::read(p, i));
+    const int nc = format_components(type), kind = format_kind(type);
+    const float r = component_load(kind, nc, p, i, 0);
+    if (nc == 1) return make_float4(r, 0.f, 0.f, kind_one(kind));
+    if (nc == 3) return make_float4(r, r, r, kind_one(kind));
+    const float g = component_load(kind, nc, p, i, 1);
+    if (nc == 2) return make_float4(r, g, 0.f, kind_one(kind));
+    return make_float4(r, g, component_load(kind, nc, p, i, 2), component_load(kind, nc, p, i, 3));
 }
 
 __device__ __forceinline__ void texel_store(int type, uint8_t* p, size_t i, const float4 c)
 {
     if (type == SLG_COLOR_RGBA_FLOAT) ColorRGBAF::write(p, i, ColorRGBAF::store(c));
     else if (type == SLG_COLOR_R_FLOAT) ColorRF::write(p, i, ColorRF::store(c));
-    else ColorRGBA8::write(p, i, ColorRGBA8::store(c));
+    else if (type == SLG_COLOR_RGBA_8U) ColorRGBA8::write(p, i, ColorRGBA8::store(c));
+    else
+    {
+        const int nc = format_components(type), kind = format_kind(type);
+        const float v[4] = {c.x, c.y, c.z, c.w};
+        for (int j = 0; j < nc; ++j) component_store(kind, nc, p, i, j, v[j]);
+    }
 }
 
 /* Outputs 1..3 of a fragment into colour attachments 1..3, blended per
@@ -1230,7 +1331,7 @@ __device__ __forceinline__ void texel_store(int type, uint8_t* p, size_t i, cons
 __device__ __forceinline__ void emit_extra_outputs(const Frame& f, const DrawDesc& dd, size_t gi, const slg_v4* outputs, int reps)
 {
     const int n = min((int)dd.numOutputs, f.numColors);
-    for (int k = 1; k < n; ++k)
+    for (int k = f.generic0 ? 0 : 1; k < n; ++k)
     {
         uint8_t* p = f.colors[k];
         const int t = f.colorTypes[k];
@@ -1517,7 +1618,7 @@ __device__ __forceinline__ bool shade(const Frame& f, const DrawDesc& dd, uint64
     const DevEnv env = make_env(dd, f.tables);
     const bool have = run_fragment_program(dd.fsProgram, env, vary, outputs);
     out = to_f4(outputs[0]);
-    if (kExtra && have && f.numColors > 1)
+    if (kExtra && have && (f.numColors > 1 || f.generic0))
     {
         emit_extra_outputs(f, dd, gi, outputs, reps);
     }
@@ -1541,7 +1642,7 @@ __device__ __forceinline__ bool shade_point(const Frame& f, const DrawDesc& dd, 
     const DevEnv env = make_env(dd, f.tables);
     const bool have = run_fragment_program(dd.fsProgram, env, vary, outputs);
     out = to_f4(outputs[0]);
-    if (kExtra && have && f.numColors > 1)
+    if (kExtra && have && (f.numColors > 1 || f.generic0))
     {
         emit_extra_outputs(f, dd, gi, outputs, reps);
     }
@@ -1573,7 +1674,7 @@ __device__ __forceinline__ bool shade_line(const Frame& f, const DrawDesc& dd, u
     const DevEnv env = make_env(dd, f.tables);
     const bool have = run_fragment_program(dd.fsProgram, env, vary, outputs);
     out = to_f4(outputs[0]);
-    if (kExtra && have && f.numColors > 1)
+    if (kExtra && have && (f.numColors > 1 || f.generic0))
     {
         emit_extra_outputs(f, dd, gi, outputs, reps);
     }
@@ -2195,7 +2296,7 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
         const float4* R = f.records + rec * kRecordVec4;
         const DrawDesc& dd = f.draws[__float_as_uint(R[7].x)];
         const float4 b = sB[i];
-        if (f.color && dd.numOutputs > 0)
+        if ((f.color || f.generic0) && dd.numOutputs > 0)
         {
             float4 o;
             const uint32_t kind = __float_as_uint(R[7].w);
@@ -2242,16 +2343,14 @@ __device__ void alias_replay(const Frame& f, const AliasEvent& ev, const uint32_
     const bool halfDepth = f.depthType == SLG_COLOR_R_HALF;
     /* the pixel's state before the launch */
     float depth = ev.depth0;
-    for (int k = 1; k < f.numColors; ++k)
+    for (int k = 0; k < f.numColors; ++k)
     {
-        if (f.colorTypes[k] == SLG_COLOR_RGBA_FLOAT) reinterpret_cast<uint4*>(f.colors[k])[gi] = ev.colorN[k - 1];
-        else reinterpret_cast<uint32_t*>(f.colors[k])[gi] = ev.colorN[k - 1].x;
+        const int bpt = texel_bytes(f.colorTypes[k]);
+        for (int b = 0; b < bpt; ++b) f.colors[k][(size_t)gi * bpt + b] = ev.colors[k][b];
     }
     Stored color{};
     if (f.color)
     {
-        if (f.colorType == SLG_COLOR_RGBA_FLOAT) reinterpret_cast<uint4*>(f.color)[gi] = ev.color0;
-        else reinterpret_cast<uint32_t*>(f.color)[gi] = ev.color0.x;
         color = Color::read(f.color, gi);
     }
     auto put = [&](const DrawDesc& dd, bool have, const float4 o) {
@@ -2418,15 +2517,23 @@ __global__ void __launch_bounds__(kAliasThreads) alias_fixup_kernel(const Frame 
 /*-----------------------------------------------------------------------------
  * Clear (SL_ClearProcessor, softlight/src/SL_ClearProcessor.cpp)
 -----------------------------------------------------------------------------*/
-__global__ void clear_kernel(uint8_t* dst, size_t numTexels, int bytesPerTexel, uint4 value)
+struct TexelValue { uint32_t w[8]; };   /* up to 32 bytes of one texel */
+
+__global__ void clear_kernel(uint8_t* dst, size_t numTexels, int bytesPerTexel, TexelValue value)
 {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < numTexels; i += stride)
     {
-        if (bytesPerTexel == 16) reinterpret_cast<uint4*>(dst)[i] = value;
-        else if (bytesPerTexel == 8) reinterpret_cast<uint2*>(dst)[i] = make_uint2(value.x, value.y);
-        else if (bytesPerTexel == 2) reinterpret_cast<uint16_t*>(dst)[i] = (uint16_t)value.x;
-        else reinterpret_cast<uint32_t*>(dst)[i] = value.x;
+        if (bytesPerTexel == 16) reinterpret_cast<uint4*>(dst)[i] = make_uint4(value.w[0], value.w[1], value.w[2], value.w[3]);
+        else if (bytesPerTexel == 8) reinterpret_cast<uint2*>(dst)[i] = make_uint2(value.w[0], value.w[1]);
+        else if (bytesPerTexel == 4) reinterpret_cast<uint32_t*>(dst)[i] = value.w[0];
+        else if (bytesPerTexel == 2) reinterpret_cast<uint16_t*>(dst)[i] = (uint16_t)value.w[0];
+        else
+        {
+            /* 1, 3, 6, 12, 24 or 32 bytes: byte by byte */
+            const uint8_t* v = reinterpret_cast<const uint8_t*>(value.w);
+            for (int b = 0; b < bytesPerTexel; ++b) dst[i * (size_t)bytesPerTexel + b] = v[b];
+        }
     }
 }
 
@@ -2621,9 +2728,10 @@ cudaError_t launch_blit(const BlitArgs& a, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[4], cudaStream_t s)
+cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[8], cudaStream_t s)
 {
-    const uint4 v = make_uint4(value[0], value[1], value[2], value[3]);
+    TexelValue v;
+    for (int k = 0; k < 8; ++k) v.w[k] = value[k];
     const unsigned blocks = (unsigned)std::min<size_t>((numTexels + 255) / 256, 152u * 16u);
     clear_kernel<<<blocks ? blocks : 1, 256, 0, s>>>(dst, numTexels, bytesPerTexel, v);
     return cudaGetLastError();

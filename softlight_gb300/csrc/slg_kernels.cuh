@@ -20,7 +20,7 @@ cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEven
 cudaError_t init_kernel_attributes(int keyCap);
 
 /* Fill numTexels texels of 4 or 16 bytes with value. */
-cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[4], cudaStream_t s);
+cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[8], cudaStream_t s);
 
 /* Nearest-neighbour blit of SL_BlitProcessor::blit_nearest over destination
  * pixels [x0, x0 + nx) x [y0, y0 + ny); all reads were checked in bounds. */

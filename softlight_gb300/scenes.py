@@ -346,11 +346,9 @@ class Scene:
 
     def read_color(self, k=0):
         tex, ctype = self.attachments[k]
-        if ctype == A.COLOR_RGBA_8U:
-            return self.ctx.texture_read(tex, (self.height, self.width, 4), np.uint8)
-        if ctype == A.COLOR_RGBA_FLOAT:
-            return self.ctx.texture_read(tex, (self.height, self.width, 4), np.float32)
-        return self.ctx.texture_read(tex, (self.height, self.width), np.float32)
+        nc, dtype = A.color_layout(ctype)
+        shape = (self.height, self.width) if nc == 1 else (self.height, self.width, nc)
+        return self.ctx.texture_read(tex, shape, np.dtype(dtype))
 
     def read_colors(self):
         return [self.read_color(k) for k in range(len(self.attachments))]

@@ -266,7 +266,7 @@ MRT_FORMATS = (A.COLOR_RGBA_8U, A.COLOR_RGBA_FLOAT, A.COLOR_R_FLOAT, A.COLOR_RGB
 
 
 def mrt(ctx, types=MRT_FORMATS, num_outputs=4, prim="tri", blend=A.BLEND_OFF, depth_test=A.DEPTH_TEST_LESS_THAN,
-        num_tris=300, width=96, height=80, seed=101, single_after=False, batched=False):
+        num_tris=300, width=96, height=80, seed=101, single_after=False, batched=False, clear_color=None):
     """Multiple render targets: the G-buffer program writes num_outputs
     outputs into colour attachments of the given formats (output k to
     attachment k), as filled triangles, wireframe, lines or points of a
@@ -274,6 +274,8 @@ def mrt(ctx, types=MRT_FORMATS, num_outputs=4, prim="tri", blend=A.BLEND_OFF, de
     framebuffer (it writes attachment 0 only)."""
     s = S.Scene(ctx, f"mrt_{seed}", width, height)
     s.set_color_attachments(list(types))
+    if clear_color is not None:
+        s.clear_color = clear_color
     verts, proj = S.soup_triangles(num_tris, width, height, seed=seed)
     mesh = s.add_mesh(verts, None, stride=36)
     mesh.mode = {"tri": A.RENDER_MODE_TRIANGLES, "wire": A.RENDER_MODE_TRI_WIRE,
@@ -290,6 +292,27 @@ def mrt(ctx, types=MRT_FORMATS, num_outputs=4, prim="tri", blend=A.BLEND_OFF, de
         s.draws.append((mesh2, 1, sh2))
     s.num_triangles = num_tris
     s.batched = batched
+    return s
+
+
+FORMAT_GROUPS = tuple(tuple(range(4 * g, 4 * g + 4)) for g in range(7))   # the 28 SL_ColorDataType formats
+
+
+def format_edges(ctx, color_type, width=8, height=6):
+    """One colour attachment of the given format: the left half gets an
+    unblended flat colour outside [0, 1] (-0.25, 1.5, 3.0, 0.5), the right
+    half an alpha-blended colour of alpha 0 over a cleared alpha 0 (0 / 0:
+    NaN components), the conversions where formats differ most."""
+    s = S.Scene(ctx, f"format_edges_{color_type}", width, height)
+    s.set_color_attachments([color_type])
+    s.clear_color = (0.1, 0.2, 0.3, 0.0)
+    for x0, x1, col, blend in [(-1.0, 0.0, (-0.25, 1.5, 3.0, 0.5), A.BLEND_OFF), (0.0, 1.0, (0.3, 0.6, 0.9, 0.0), A.BLEND_ALPHA)]:
+        verts = np.zeros((6, 9), np.float32)
+        verts[:, :3] = [(x0, -1, 0), (x1, -1, 0), (x1, 1, 0), (x0, -1, 0), (x1, 1, 0), (x0, 1, 0)]
+        mesh = s.add_mesh(verts, None, stride=36)
+        sh = s.add_shader(A.PROGRAM_FLAT_COLOR, 0, S.flat_uniforms(np.eye(4), col), cull=A.CULL_OFF,
+                          depth_test=A.DEPTH_TEST_OFF, depth_mask=A.DEPTH_MASK_OFF, blend=blend)
+        s.draws.append((mesh, 1, sh))
     return s
 
 

@@ -73,6 +73,16 @@ SCENES = {
     "lines_half_depth": (E.random_lines, dict(depth_type=A.COLOR_R_HALF, seed=25)),
 }
 
+# every colour format: four per scene through the G-buffer program, unblended
+# and alpha-blended over a clear colour, and the out-of-range / NaN writes
+for _g, _types in enumerate(E.FORMAT_GROUPS):
+    for _blend, _bname in [(A.BLEND_OFF, "opaque"), (A.BLEND_ALPHA, "alpha")]:
+        SCENES[f"formats_{_types[0]}_{_types[-1]}_{_bname}"] = (
+            E.mrt, dict(types=_types, num_outputs=4, blend=_blend, seed=140 + _types[0], width=48, height=40,
+                        num_tris=120, clear_color=(0.2, 0.4, 0.6, 0.8)))
+for _t in range(28):
+    SCENES[f"format_edges_{_t}"] = (E.format_edges, dict(color_type=_t))
+
 # Scenes whose draws the GPU path reports as not reproduced (SLError at
 # finish), with the reason: a blended wireframe triangle revisits a pixel
 # after 600 queued fragments (the reference's queue flush points).

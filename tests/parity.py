@@ -38,13 +38,21 @@ def compare_scenes(sg, so, label=""):
 
 
 def compare_colors(cg, co, label=""):
-    """RGBA8 within 1 LSB, float within 1e-5 relative (NaN matches NaN)."""
+    """8-bit channels within 1 LSB, wider integer channels exact, float
+    channels within 1e-5 relative (NaN matches NaN)."""
+    assert cg.dtype == co.dtype and cg.shape == co.shape, f"{label}: {cg.dtype}{cg.shape} vs {co.dtype}{co.shape}"
     if cg.dtype == np.uint8:
         diff = np.abs(cg.astype(np.int16) - co.astype(np.int16))
         assert diff.max(initial=0) <= RGBA8_TOL, f"{label}: colour differs by {diff.max()} LSB at {np.argwhere(diff > RGBA8_TOL)[:3].tolist()}"
         return int((diff > 0).sum())
-    scale = np.maximum(np.abs(co), 1e-30)
-    rel = np.abs(cg - co) / scale
-    ok = (np.abs(cg - co) <= FLOAT_RTOL * scale) | (cg == co) | (np.isnan(cg) & np.isnan(co))
+    if cg.dtype.kind == "u":
+        bad = cg != co
+        assert not bad.any(), f"{label}: {int(bad.sum())} integer colour values differ, first at {np.argwhere(bad)[:3].tolist()}"
+        return 0
+    a, b = cg.astype(np.float64), co.astype(np.float64)
+    scale = np.maximum(np.abs(b), 1e-30)
+    rel = np.abs(a - b) / scale
+    ok = (np.abs(a - b) <= FLOAT_RTOL * scale) | (a == b) | (np.isnan(a) & np.isnan(b))
     assert ok.all(), f"{label}: float colour rel err {np.nanmax(rel)}"
-    return int((cg.view(np.uint32) != co.view(np.uint32)).sum())
+    bits = {2: np.uint16, 4: np.uint32, 8: np.uint64}[cg.dtype.itemsize]
+    return int((cg.view(bits) != co.view(bits)).sum())
