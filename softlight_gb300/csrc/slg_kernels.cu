@@ -2303,7 +2303,7 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
             const bool have = (kind & kRecordPoint)            ? shade_point<kGeneral>(f, dd, rec, o, gi)
                               : (kGeneral && (kind & kRecordLine)) ? shade_line<kGeneral>(f, dd, rec, b.x, o, gi)
                                                                  : shade<kGeneral>(f, dd, rec, kind, R[2].w, R[5], b.x, b.y, b.z, o, gi);
-            if (have)
+            if (have && f.color)
             {
                 Color::write(f.color, gi, Color::store(o));
             }
