@@ -84,15 +84,42 @@ enum slg_blend_mode
     SLG_BLEND_SCREEN
 };
 
-/* SL_ColorDataType subset used by framebuffers and textures
- * (softlight/include/softlight/SL_Color.hpp:31). Values are the reference's. */
+/* SL_ColorDataType (softlight/include/softlight/SL_Color.hpp:31), values the
+ * reference's: R / RG / RGB / RGBA (type / 7 + 1 components) of u8, u16,
+ * u32, u64, half, float, double (type % 7), densely packed. Colour
+ * attachments and clears accept all 28; depth attachments R_HALF, R_FLOAT,
+ * R_DOUBLE; sampled textures RGBA_8U or RGBA_FLOAT; blits R_FLOAT, RGBA_8U,
+ * RGBA_FLOAT. */
 enum slg_color_type
 {
-    SLG_COLOR_R_HALF     = 4,   /* depth attachments (IEEE binary16) */
-    SLG_COLOR_R_FLOAT    = 5,
-    SLG_COLOR_R_DOUBLE   = 6,   /* depth attachments */
-    SLG_COLOR_RGBA_8U    = 21,
-    SLG_COLOR_RGBA_FLOAT = 26
+    SLG_COLOR_R_8U        = 0,
+    SLG_COLOR_R_16U       = 1,
+    SLG_COLOR_R_32U       = 2,
+    SLG_COLOR_R_64U       = 3,
+    SLG_COLOR_R_HALF      = 4,
+    SLG_COLOR_R_FLOAT     = 5,
+    SLG_COLOR_R_DOUBLE    = 6,
+    SLG_COLOR_RG_8U       = 7,
+    SLG_COLOR_RG_16U      = 8,
+    SLG_COLOR_RG_32U      = 9,
+    SLG_COLOR_RG_64U      = 10,
+    SLG_COLOR_RG_HALF     = 11,
+    SLG_COLOR_RG_FLOAT    = 12,
+    SLG_COLOR_RG_DOUBLE   = 13,
+    SLG_COLOR_RGB_8U      = 14,
+    SLG_COLOR_RGB_16U     = 15,
+    SLG_COLOR_RGB_32U     = 16,
+    SLG_COLOR_RGB_64U     = 17,
+    SLG_COLOR_RGB_HALF    = 18,
+    SLG_COLOR_RGB_FLOAT   = 19,
+    SLG_COLOR_RGB_DOUBLE  = 20,
+    SLG_COLOR_RGBA_8U     = 21,
+    SLG_COLOR_RGBA_16U    = 22,
+    SLG_COLOR_RGBA_32U    = 23,
+    SLG_COLOR_RGBA_64U    = 24,
+    SLG_COLOR_RGBA_HALF   = 25,
+    SLG_COLOR_RGBA_FLOAT  = 26,
+    SLG_COLOR_RGBA_DOUBLE = 27
 };
 
 /* Built-in device shader programs. In SoftLight a shader is a host function
