@@ -86,8 +86,8 @@ enum slg_blend_mode
 
 /* SL_ColorDataType (softlight/include/softlight/SL_Color.hpp:31), values the
  * reference's: R / RG / RGB / RGBA (type / 7 + 1 components) of u8, u16,
- * u32, u64, half, float, double (type % 7), densely packed. Colour
- * attachments and clears accept all 28; depth attachments R_HALF, R_FLOAT,
+ * u32, u64, half, float, double (type % 7), densely packed, then five
+ * packed formats. Colour attachments and clears accept all 33; depth attachments R_HALF, R_FLOAT,
  * R_DOUBLE; sampled textures RGBA_8U or RGBA_FLOAT; blits R_FLOAT, RGBA_8U,
  * RGBA_FLOAT. */
 enum slg_color_type
@@ -119,7 +119,14 @@ enum slg_color_type
     SLG_COLOR_RGBA_64U    = 24,
     SLG_COLOR_RGBA_HALF   = 25,
     SLG_COLOR_RGBA_FLOAT  = 26,
-    SLG_COLOR_RGBA_DOUBLE = 27
+    SLG_COLOR_RGBA_DOUBLE = 27,
+    /* packed, one integer per texel, fields from bit 0 up
+     * (softlight/include/softlight/SL_ColorCompressed.hpp) */
+    SLG_COLOR_RGB_332      = 28,   /* u8:  r 3, g 3, b 2 */
+    SLG_COLOR_RGB_565      = 29,   /* u16: r 5, g 6, b 5 */
+    SLG_COLOR_RGBA_5551    = 30,   /* u16: r 5, g 5, b 5, a 1 */
+    SLG_COLOR_RGBA_4444    = 31,   /* u16: r 4, g 4, b 4, a 4 */
+    SLG_COLOR_RGBA_1010102 = 32    /* u32: r 10, g 10, b 10, a 2 */
 };
 
 /* Built-in device shader programs. In SoftLight a shader is a host function

@@ -146,10 +146,29 @@ struct Bin
     uint32_t drawIndex;
 };
 
-/* bytes of a texel of SL_ColorDataType 0..27 (components type / 7 + 1 of
- * u8, u16, u32, u64, half, float, double by type % 7) */
+/* The packed formats SL_COLOR_RGB_332 .. SL_COLOR_RGBA_1010102 (28..32,
+ * softlight/include/softlight/SL_ColorCompressed.hpp): unsigned bitfields
+ * allocated from bit 0 up, as gcc lays them out on little-endian targets. */
+struct PackedFormat
+{
+    int nc, bytes;
+    int bits[4], shift[4];
+};
+
+static const PackedFormat kPacked[5] = {
+    {3, 1, {3, 3, 2, 0}, {0, 3, 6, 0}},          /* RGB 332 */
+    {3, 2, {5, 6, 5, 0}, {0, 5, 11, 0}},         /* RGB 565 */
+    {4, 2, {5, 5, 5, 1}, {0, 5, 10, 15}},        /* RGBA 5551 */
+    {4, 2, {4, 4, 4, 4}, {0, 4, 8, 12}},         /* RGBA 4444 */
+    {4, 4, {10, 10, 10, 2}, {0, 10, 20, 30}},    /* RGBA 1010102 */
+};
+
+/* bytes of a texel of SL_ColorDataType 0..32: components type / 7 + 1 of
+ * u8, u16, u32, u64, half, float, double by type % 7, then the packed
+ * formats (sl_bytes_per_color, softlight/src/SL_Color.cpp:12-56) */
 static size_t bytes_per_color(int type)
 {
+    if (type >= 28 && type <= 32) return (size_t)kPacked[type - 28].bytes;
     if (type < 0 || type > 27) return 0;
     static const size_t kind[7] = {1, 2, 4, 8, 2, 4, 8};
     return (size_t)(type / 7 + 1) * kind[type % 7];
@@ -736,25 +755,69 @@ static inline void component_set(const Target& t, size_t idx, int j, float x)
     else { const double d = (double)x; std::memcpy(c, &d, 8); }
 }
 
+/* Packed texels. Read (rgba_cast<float, T>, SL_ColorCompressed.hpp:165-184
+ * and the like): each field as (float)c / (float)max, alpha 1 for the RGB
+ * formats. Write (rgba_cast<T, float>, :112-132 and the like): each field
+ * (uint8_t or uint16_t)(x * (float)max), i.e. cvttss2si's 32-bit result,
+ * keeping the field's low bits. */
+static inline uint32_t packed_bits(const Target& t, size_t idx)
+{
+    const PackedFormat& pf = kPacked[t.type - 28];
+    uint32_t bits = 0;
+    std::memcpy(&bits, t.bytes + idx * pf.bytes, pf.bytes);   /* little-endian */
+    return bits;
+}
+
+static inline V4 packed_get(const Target& t, size_t idx)
+{
+    const PackedFormat& pf = kPacked[t.type - 28];
+    const uint32_t bits = packed_bits(t, idx);
+    V4 d = mk(0.f, 0.f, 0.f, 1.f);
+    for (int j = 0; j < pf.nc; ++j)
+    {
+        const uint32_t mask = (1u << pf.bits[j]) - 1u;
+        d[j] = (float)((bits >> pf.shift[j]) & mask) / (float)mask;
+    }
+    return d;
+}
+
+static inline void packed_set(const Target& t, size_t idx, const V4& c)
+{
+    const PackedFormat& pf = kPacked[t.type - 28];
+    uint32_t bits = 0;
+    for (int j = 0; j < pf.nc; ++j)
+    {
+        const uint32_t mask = (1u << pf.bits[j]) - 1u;
+        bits |= ((uint32_t)f2i(c[j] * (float)mask) & mask) << pf.shift[j];
+    }
+    std::memcpy(t.bytes + idx * pf.bytes, &bits, pf.bytes);
+}
+
 /* assign_pixel / assign_alpha_pixel (softlight/src/SL_Framebuffer.cpp:45-80,
  * 266-366): the blend reads the texel padded with the format's min (green,
  * blue) and max (alpha), a three-component texel as (r, r, r, max); the
  * blended value is clamped to [0, 1]; components beyond the format's are
- * dropped. */
+ * dropped. Packed formats read and write whole texels (SL_Framebuffer.cpp:
+ * 85-145, 371-587, with the same blend and clamp). */
 static inline void write_color(const Target& t, unsigned x, unsigned y, const V4& rgba, uint8_t blend)
 {
     const size_t idx = (size_t)x + (size_t)t.w * y;
-    const int nc = t.type / 7 + 1, kind = t.type % 7;
+    const bool packed = t.type >= 28;
+    const int nc = packed ? 0 : t.type / 7 + 1, kind = packed ? 0 : t.type % 7;
     V4 src = rgba;
 
     if (blend != SLG_BLEND_OFF)
     {
         V4 d;
-        const float r = component_get(t, idx, 0);
-        if (nc == 1) d = mk(r, 0.f, 0.f, kind_one(kind));
-        else if (nc == 2) d = mk(r, component_get(t, idx, 1), 0.f, kind_one(kind));
-        else if (nc == 3) d = mk(r, r, r, kind_one(kind));
-        else d = mk(r, component_get(t, idx, 1), component_get(t, idx, 2), component_get(t, idx, 3));
+        if (packed) d = packed_get(t, idx);
+        else
+        {
+            const float r = component_get(t, idx, 0);
+            if (nc == 1) d = mk(r, 0.f, 0.f, kind_one(kind));
+            else if (nc == 2) d = mk(r, component_get(t, idx, 1), 0.f, kind_one(kind));
+            else if (nc == 3) d = mk(r, r, r, kind_one(kind));
+            else d = mk(r, component_get(t, idx, 1), component_get(t, idx, 2), component_get(t, idx, 3));
+        }
 
         const float sa = rgba[3];
         const float modulation = 1.f - sa;
@@ -786,7 +849,8 @@ static inline void write_color(const Target& t, unsigned x, unsigned y, const V4
         src = d;
     }
 
-    for (int j = 0; j < nc; ++j) component_set(t, idx, j, src[j]);
+    if (packed) packed_set(t, idx, src);
+    else for (int j = 0; j < nc; ++j) component_set(t, idx, j, src[j]);
 }
 
 static inline bool depth_cmp(uint8_t func, float z, float d)
@@ -1603,10 +1667,24 @@ static void clear_color(Texture& t, const double rgba[4], unsigned threads)
 {
     const size_t n = clear_reach((size_t)t.w * t.h, threads);
     const size_t bpt = bytes_per_color(t.type);
-    const int nc = t.type / 7 + 1, kind = t.type % 7;
-    const size_t cb = bpt / nc;
+    const bool packed = t.type >= 28;
+    const int nc = packed ? 0 : t.type / 7 + 1, kind = packed ? 0 : t.type % 7;
+    const size_t cb = packed ? 0 : bpt / nc;
     static const double kMax[4] = {255.0, 65535.0, 4294967295.0, 18446744073709551615.0};
     uint8_t texel[32] = {0};
+    if (packed)
+    {
+        /* rgba_cast<T, double> (SL_Color.cpp:180-184): (uint8_t or
+         * uint16_t)(c * (double)max) per field, low bits kept */
+        const PackedFormat& pf = kPacked[t.type - 28];
+        uint32_t bits = 0;
+        for (int j = 0; j < pf.nc; ++j)
+        {
+            const uint32_t mask = (1u << pf.bits[j]) - 1u;
+            bits |= ((uint32_t)d2u_x86(rgba[j] * (double)mask, 0) & mask) << pf.shift[j];
+        }
+        std::memcpy(texel, &bits, pf.bytes);
+    }
     for (int j = 0; j < nc; ++j)
     {
         uint8_t* c = texel + j * cb;

@@ -32,15 +32,23 @@ COLOR_COMPONENT_DTYPES = ("uint8", "uint16", "uint32", "uint64", "float16", "flo
 for _n, _prefix in enumerate(("R", "RG", "RGB", "RGBA")):
     for _k, _suffix in enumerate(("8U", "16U", "32U", "64U", "HALF", "FLOAT", "DOUBLE")):
         globals()[f"COLOR_{_prefix}_{_suffix}"] = 7 * _n + _k
-COLOR_TYPES = tuple(range(28))
+# packed formats (SL_ColorCompressed.hpp): one integer per texel
+COLOR_RGB_332, COLOR_RGB_565, COLOR_RGBA_5551, COLOR_RGBA_4444, COLOR_RGBA_1010102 = 28, 29, 30, 31, 32
+PACKED_FORMATS = {28: ("uint8", (3, 3, 2)), 29: ("uint16", (5, 6, 5)), 30: ("uint16", (5, 5, 5, 1)),
+                  31: ("uint16", (4, 4, 4, 4)), 32: ("uint32", (10, 10, 10, 2))}
+COLOR_TYPES = tuple(range(33))
 PROGRAM_LAMBERT_TEX, PROGRAM_BLINN_PHONG_INST, PROGRAM_VCOLOR_TEX_ALPHA = 1, 2, 3
 PROGRAM_VCOLOR_TEXF, PROGRAM_FLAT_COLOR, PROGRAM_GBUFFER = 4, 5, 6
 
-BYTES_PER_COLOR = {t: (t // 7 + 1) * (1, 2, 4, 8, 2, 4, 8)[t % 7] for t in COLOR_TYPES}
+BYTES_PER_COLOR = {t: (t // 7 + 1) * (1, 2, 4, 8, 2, 4, 8)[t % 7] for t in range(28)}
+BYTES_PER_COLOR.update({28: 1, 29: 2, 30: 2, 31: 2, 32: 4})
 
 
 def color_layout(t):
-    """(components, numpy dtype name) of a colour format."""
+    """(components, numpy dtype name) of a colour format; a packed format is
+    one integer per texel."""
+    if t in PACKED_FORMATS:
+        return 1, PACKED_FORMATS[t][0]
     return t // 7 + 1, COLOR_COMPONENT_DTYPES[t % 7]
 
 

@@ -60,10 +60,18 @@ struct Shader
     size_t ubo;
 };
 
-/* Bytes of a texel of SL_ColorDataType 0..27: components (type / 7 + 1) x
- * the size of u8, u16, u32, u64, half, float or double (type % 7). */
+/* Field widths of the packed formats 28..32 (RGB 332, RGB 565, RGBA 5551,
+ * RGBA 4444, RGBA 1010102; softlight/include/softlight/SL_ColorCompressed.hpp),
+ * from bit 0 up, and their texel bytes. */
+const int kPackedWidths[5][4] = {{3, 3, 2, 0}, {5, 6, 5, 0}, {5, 5, 5, 1}, {4, 4, 4, 4}, {10, 10, 10, 2}};
+const size_t kPackedBytes[5] = {1, 2, 2, 2, 4};
+
+/* Bytes of a texel of SL_ColorDataType 0..32: components (type / 7 + 1) x
+ * the size of u8, u16, u32, u64, half, float or double (type % 7), then the
+ * packed formats (sl_bytes_per_color, softlight/src/SL_Color.cpp:12-56). */
 size_t bytes_per_color(int type)
 {
+    if (type >= 28 && type <= 32) return kPackedBytes[type - 28];
     if (type < 0 || type > 27) return 0;
     static const size_t kind[7] = {1, 2, 4, 8, 2, 4, 8};
     return (size_t)(type / 7 + 1) * kind[type % 7];
@@ -347,6 +355,23 @@ int color_value(int type, const double rgba[4], uint32_t out[8])
     std::memset(out, 0, 8 * sizeof(uint32_t));
     const size_t bpt = bytes_per_color(type);
     if (!bpt) return -1;
+    if (type >= 28)
+    {
+        /* rgba_cast<T, double> (SL_Color.cpp:180-184): (uint8_t or
+         * uint16_t)(c * (double)max) per field, the field keeping its low bits */
+        uint32_t bits = 0;
+        int shift = 0;
+        for (int j = 0; j < 4; ++j)
+        {
+            const int b = kPackedWidths[type - 28][j];
+            if (!b) break;
+            const uint32_t mask = (1u << b) - 1u;
+            bits |= ((uint32_t)d2u_x86(rgba[j] * (double)mask, 0) & mask) << shift;
+            shift += b;
+        }
+        out[0] = bits;
+        return 0;
+    }
     const int nc = type / 7 + 1, kind = type % 7;
     static const double kMax[4] = {255.0, 65535.0, 4294967295.0, 18446744073709551615.0};
     uint8_t* bytes = reinterpret_cast<uint8_t*>(out);

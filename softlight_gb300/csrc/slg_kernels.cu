@@ -182,9 +182,29 @@ __device__ __forceinline__ float depth_quant(bool halfDepth, float z)
     return halfDepth ? slg_half_to_float(slg_float_to_half(z)) : z;
 }
 
-/* bytes of a texel of colour format `type` (SL_ColorDataType 0..27) */
+/* The packed formats 28..32 (RGB 332, RGB 565, RGBA 5551, RGBA 4444,
+ * RGBA 1010102; softlight/include/softlight/SL_ColorCompressed.hpp):
+ * unsigned bitfields from bit 0 up, the field widths one nibble each. */
+constexpr int kFirstPacked = 28;
+
+__device__ __forceinline__ uint32_t packed_widths(int type)
+{
+    switch (type)
+    {
+        case 28: return 0x0233u;
+        case 29: return 0x0565u;
+        case 30: return 0x1555u;
+        case 31: return 0x4444u;
+        default: return 0x2AAAu;
+    }
+}
+
+__device__ __forceinline__ int packed_bytes(int type) { return (type == 28) ? 1 : (type == 32) ? 4 : 2; }
+
+/* bytes of a texel of colour format `type` (SL_ColorDataType 0..32) */
 __device__ __forceinline__ int texel_bytes(int type)
 {
+    if (type >= kFirstPacked) return packed_bytes(type);
     const int kind = type % 7;
     return (type / 7 + 1) * ((kind == 0) ? 1 : (kind == 1 || kind == 4) ? 2 : (kind == 2 || kind == 5) ? 4 : 8);
 }
@@ -1295,6 +1315,59 @@ __device__ __forceinline__ void component_store(int kind, int nc, uint8_t* p, si
     }
 }
 
+/* Packed texels. Read (rgba_cast<float, T>, SL_ColorCompressed.hpp:165-184
+ * and its siblings): each field (float)c / (float)max, alpha 1 for RGB 332
+ * and RGB 565. Write (rgba_cast<T, float>, :112-132 and siblings): each
+ * field (uint8_t or uint16_t)(x * (float)max) - cvttss2si's 32-bit result,
+ * the field keeping its low bits. */
+__device__ __noinline__ float4 packed_load(int type, const uint8_t* p, size_t i)
+{
+    const int nb = packed_bytes(type);
+    const uint32_t bits = (nb == 1) ? (uint32_t)p[i]
+                        : (nb == 2) ? (uint32_t)reinterpret_cast<const uint16_t*>(p)[i]
+                                    : reinterpret_cast<const uint32_t*>(p)[i];
+    const uint32_t w = packed_widths(type);
+    const int nc = (type <= 29) ? 3 : 4;
+    float v[4] = {0.f, 0.f, 0.f, 1.f};
+    int shift = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+    {
+        if (j < nc)
+        {
+            const int b = (int)((w >> (4 * j)) & 15u);
+            const uint32_t mask = (1u << b) - 1u;
+            v[j] = (float)((bits >> shift) & mask) / (float)mask;
+            shift += b;
+        }
+    }
+    return make_float4(v[0], v[1], v[2], v[3]);
+}
+
+__device__ __noinline__ void packed_store(int type, uint8_t* p, size_t i, const float4 c)
+{
+    const uint32_t w = packed_widths(type);
+    const int nc = (type <= 29) ? 3 : 4;
+    const float v[4] = {c.x, c.y, c.z, c.w};
+    uint32_t bits = 0;
+    int shift = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+    {
+        if (j < nc)
+        {
+            const int b = (int)((w >> (4 * j)) & 15u);
+            const uint32_t mask = (1u << b) - 1u;
+            bits |= ((uint32_t)f2i(v[j] * (float)mask) & mask) << shift;
+            shift += b;
+        }
+    }
+    const int nb = packed_bytes(type);
+    if (nb == 1) p[i] = (uint8_t)bits;
+    else if (nb == 2) reinterpret_cast<uint16_t*>(p)[i] = (uint16_t)bits;
+    else reinterpret_cast<uint32_t*>(p)[i] = bits;
+}
+
 /* A texel of an attachment, as the float4 the blend reads and from the
  * float4 a fragment writes (the three core formats keep their fast forms). */
 __device__ __forceinline__ float4 texel_load(int type, const uint8_t* p, size_t i)
@@ -1302,6 +1375,7 @@ __device__ __forceinline__ float4 texel_load(int type, const uint8_t* p, size_t 
     if (type == SLG_COLOR_RGBA_FLOAT) return ColorRGBAF::load(ColorRGBAF::read(p, i));
     if (type == SLG_COLOR_R_FLOAT) return ColorRF::load(ColorRF::read(p, i));
     if (type == SLG_COLOR_RGBA_8U) return ColorRGBA8::load(ColorRGBA8::read(p, i));
+    if (type >= kFirstPacked) return packed_load(type, p, i);
     const int nc = format_components(type), kind = format_kind(type);
     const float r = component_load(kind, nc, p, i, 0);
     if (nc == 1) return make_float4(r, 0.f, 0.f, kind_one(kind));
@@ -1316,6 +1390,7 @@ __device__ __forceinline__ void texel_store(int type, uint8_t* p, size_t i, cons
     if (type == SLG_COLOR_RGBA_FLOAT) ColorRGBAF::write(p, i, ColorRGBAF::store(c));
     else if (type == SLG_COLOR_R_FLOAT) ColorRF::write(p, i, ColorRF::store(c));
     else if (type == SLG_COLOR_RGBA_8U) ColorRGBA8::write(p, i, ColorRGBA8::store(c));
+    else if (type >= kFirstPacked) packed_store(type, p, i, c);
     else
     {
         const int nc = format_components(type), kind = format_kind(type);

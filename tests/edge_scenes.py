@@ -295,7 +295,8 @@ def mrt(ctx, types=MRT_FORMATS, num_outputs=4, prim="tri", blend=A.BLEND_OFF, de
     return s
 
 
-FORMAT_GROUPS = tuple(tuple(range(4 * g, 4 * g + 4)) for g in range(7))   # the 28 SL_ColorDataType formats
+# the 28 component formats in groups of four, then the five packed ones
+FORMAT_GROUPS = tuple(tuple(range(4 * g, 4 * g + 4)) for g in range(7)) + ((28, 29, 30, 31), (32, 28, 21, 5))
 
 
 def format_edges(ctx, color_type, width=8, height=6):

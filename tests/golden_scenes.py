@@ -80,7 +80,7 @@ for _g, _types in enumerate(E.FORMAT_GROUPS):
         SCENES[f"formats_{_types[0]}_{_types[-1]}_{_bname}"] = (
             E.mrt, dict(types=_types, num_outputs=4, blend=_blend, seed=140 + _types[0], width=48, height=40,
                         num_tris=120, clear_color=(0.2, 0.4, 0.6, 0.8)))
-for _t in range(28):
+for _t in range(33):
     SCENES[f"format_edges_{_t}"] = (E.format_edges, dict(color_type=_t))
 
 # Scenes whose draws the GPU path reports as not reproduced (SLError at

@@ -456,16 +456,17 @@ def test_vertex_cache_mixed_launch(ctxs, batched):
 @pytest.mark.parametrize("types", E.FORMAT_GROUPS, ids=[f"formats_{t[0]}_{t[-1]}" for t in E.FORMAT_GROUPS])
 @pytest.mark.parametrize("blend", [A.BLEND_OFF, A.BLEND_ALPHA, A.BLEND_ADDITIVE])
 def test_colour_formats(ctxs, types, blend):
-    """All 28 colour formats (R / RG / RGB / RGBA of u8, u16, u32, u64, half,
-    float, double), four attachments per launch, attachment 0 included:
-    written as color_cast<T, float>, blended through the padded read-back."""
+    """All 33 colour formats (R / RG / RGB / RGBA of u8, u16, u32, u64, half,
+    float, double; the five packed ones), four attachments per launch,
+    attachment 0 included: written as color_cast<T, float> (rgba_cast for
+    packed texels), blended through the format's read-back."""
     g, o = ctxs
     sg, so = render_both(E.mrt, g, o, types=types, blend=blend, num_tris=1200, width=200, height=150,
                          seed=150 + types[0], clear_color=(0.2, 0.4, 0.6, 0.8))
     compare_scenes(sg, so, f"formats {types} blend {blend}")
 
 
-@pytest.mark.parametrize("color_type", range(28))
+@pytest.mark.parametrize("color_type", range(33))
 def test_format_edges(ctxs, color_type):
     """Out-of-range and NaN components (their conversions to unsigned follow
     the reference build), per format."""
