@@ -74,6 +74,12 @@ struct long_medp_t
     constexpr long_medp_t operator*(const long_medp_t& o) const noexcept { return long_medp_t{(int64_t)(((__int128)v * o.v) >> 32)}; }
 };
 
+/* 16.16 fixed point: named by SL_Plane's SL_Planex typedef only */
+struct medp_t
+{
+    int32_t v;
+};
+
 template <typename fixed_t, typename T>
 constexpr fixed_t fixed_cast(T n) noexcept { return fixed_t{(int64_t)((double)n * 4294967296.0)}; }
 
@@ -305,12 +311,15 @@ struct mat2_t
     constexpr const vec2_t<T>& operator[](std::size_t i) const noexcept { return m[i]; }
 };
 
+template <typename T> struct mat4_t;
+
 template <typename T>
 struct mat3_t
 {
     vec3_t<T> m[3];
     mat3_t() noexcept = default;
     constexpr mat3_t(const vec3_t<T>& a, const vec3_t<T>& b, const vec3_t<T>& c) noexcept : m{a, b, c} {}
+    explicit mat3_t(const mat4_t<T>& a) noexcept;   /* the upper-left 3x3 */
     vec3_t<T>& operator[](std::size_t i) noexcept { return m[i]; }
     constexpr const vec3_t<T>& operator[](std::size_t i) const noexcept { return m[i]; }
 };
@@ -340,6 +349,12 @@ struct mat4_t
     mat4_t& operator+=(const vec4_t<T>& v) noexcept { for (int i = 0; i < 4; ++i) m[i] += v; return *this; }
     mat4_t& operator+=(const mat4_t& o) noexcept { for (int i = 0; i < 4; ++i) m[i] += o.m[i]; return *this; }
 };
+
+template <typename T> inline mat3_t<T>::mat3_t(const mat4_t<T>& a) noexcept
+    : m{vec3_t<T>{a.m[0].v[0], a.m[0].v[1], a.m[0].v[2]}, vec3_t<T>{a.m[1].v[0], a.m[1].v[1], a.m[1].v[2]},
+        vec3_t<T>{a.m[2].v[0], a.m[2].v[1], a.m[2].v[2]}}
+{
+}
 
 typedef mat2_t<float> mat2;
 typedef mat3_t<float> mat3;

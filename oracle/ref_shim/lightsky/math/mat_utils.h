@@ -1,1 +1,2 @@
 #include "_shim_math.h"
+#include "_shim_quat.h"

@@ -23,7 +23,7 @@
 #define LS_UNLIKELY(x) __builtin_expect(!!(x), 0)
 #define LS_UNREACHABLE() __builtin_unreachable()
 #define LS_ARRAY_SIZE(a) (sizeof(a) / sizeof((a)[0]))
-#define LS_ENUM_VAL(e) (e)
+#define LS_ENUM_VAL(e) (static_cast<typename std::underlying_type<decltype(e)>::type>(e))
 #define LS_PREFETCH(addr, rw, locality) __builtin_prefetch((addr), 0, 0)
 #define LS_PREFETCH_ACCESS_R 0
 #define LS_PREFETCH_ACCESS_RW 1

@@ -32,6 +32,16 @@ namespace ls
 namespace utils
 {
 
+/* string hash for SL_Animation's ids: FNV-1a, 64 bits */
+typedef uint64_t hash_t;
+inline hash_t string_hash(const char* str) noexcept
+{
+    hash_t h = 14695981039346656037ull;
+    for (; *str; ++str) h = (h ^ (uint8_t)*str) * 1099511628211ull;
+    return h;
+}
+
+
 inline void* aligned_malloc(std::size_t n) noexcept
 {
     void* p = nullptr;
@@ -114,6 +124,7 @@ inline UniqueAlignedPointer<T> make_unique_aligned_pointer(Args&&... args) noexc
 
 inline void fast_memset(void* dst, int v, std::size_t numBytes) noexcept { std::memset(dst, v, numBytes); }
 inline void fast_memcpy(void* dst, const void* src, std::size_t numBytes) noexcept { std::memcpy(dst, src, numBytes); }
+template <typename T> inline void fast_copy(T* dst, const T* src, std::size_t count) noexcept { for (std::size_t i = 0; i < count; ++i) dst[i] = src[i]; }
 
 template <typename T> inline void fill_pattern(void* dst, T v, std::size_t numBytes) noexcept
 {
