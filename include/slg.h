@@ -314,6 +314,73 @@ int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_
  * a caller loop over SL_Context::draw (softlight/tests/sl_instancing_test.cpp:236-279). */
 int slg_draw_batch(slg_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, size_t fboId);
 
+/*-----------------------------------------------------------------------------
+ * Scene graph (SL_SceneGraph, softlight/include/softlight/SL_SceneGraph.hpp:215)
+ * and the draw list of its mesh nodes. Nodes keep their insertion order
+ * (a parent precedes its children); update follows SL_SceneGraph::update
+ * (softlight/src/SL_SceneGraph.cpp:259-299) on the device; draw traverses
+ * the mesh nodes as SoftLight's scene demos do
+ * (softlight/tests/sl_large_scene_test.cpp:678-740) and draws the result as
+ * one batched launch whose uniform blocks and culling are written on the
+ * device.
+-----------------------------------------------------------------------------*/
+/* SL_Transform's parameters (softlight/include/softlight/SL_Transform.hpp:60-75) */
+typedef struct slg_transform
+{
+    float    position[3];
+    float    scaling[3];
+    float    orientation[4];  /* quaternion x, y, z, w */
+    uint32_t type;            /* SL_TransformType: 0 model, 1 view FPS, 2 view arc,
+                                 3 view FPS locked y, 4 view arc locked y */
+} slg_transform;
+
+#define SLG_SCENE_ROOT ((size_t)-1)   /* SCENE_NODE_ROOT_ID */
+
+size_t slg_create_scene(slg_context* ctx);
+
+/* SL_SceneGraph::insert_mesh (SL_SceneGraph.cpp:1212-1223): a mesh and its
+ * bounding box (points with w = 1). Mesh nodes also append a default box
+ * (max 1, min -1) to the same list, as the reference does, and culling reads
+ * the box at the submesh's mesh index. */
+int slg_scene_insert_mesh(slg_context* ctx, size_t sceneId, const slg_mesh* mesh, const float maxPoint[3],
+                          const float minPoint[3], size_t* outMeshId);
+
+/* A material (SL_Material) reduced to its ambient texture, the one the
+ * demos' traversal binds; slg_mesh.materialId indexes these. */
+int slg_scene_insert_material(slg_context* ctx, size_t sceneId, size_t ambientTextureId, size_t* outMaterialId);
+
+/* SL_SceneGraph::insert_empty_node (numSubMeshes == 0) or insert_mesh_node
+ * (SL_SceneGraph.cpp:1180-1258): the node is appended (the reference's
+ * reparent call leaves it in place) with a dirty transform and an identity
+ * model matrix until the next update. Paths from a root hold at most 64
+ * nodes. */
+int slg_scene_insert_node(slg_context* ctx, size_t sceneId, size_t parentId, size_t numSubMeshes, const size_t* subMeshIds,
+                          const slg_transform* transform, size_t* outNodeId);
+
+/* SL_Transform::position / scaling / orientation / type of a node's
+ * current transform: marks it dirty. */
+int slg_scene_set_transform(slg_context* ctx, size_t sceneId, size_t nodeId, const slg_transform* transform);
+
+/* SL_SceneGraph::update: recomputes the model matrices of the nodes the
+ * reference's loop recomputes (each dirty node and the nodes after it up to
+ * the first whose parent precedes it). */
+int slg_scene_update(slg_context* ctx, size_t sceneId);
+
+/* The model matrices (mModelMatrices, 16 floats per node, column-major). */
+int slg_scene_read_models(slg_context* ctx, size_t sceneId, float* out, size_t numNodes);
+
+/* Draws every triangle-mode submesh of every mesh node in node order with
+ * shaderId's state and a copy of its uniform block: program
+ * SLG_PROGRAM_LAMBERT_TEX, vpMatrix = projection * view, modelMatrix = the
+ * node's model matrix, textureId = the material's ambient texture. With a
+ * cullProjection (the demos pass a fixed perspective), a submesh whose
+ * bounding box fails sl_is_visible(box, view * model, frustum planes of
+ * cullProjection) (softlight/src/SL_Camera.cpp:25-85) is skipped; NULL
+ * draws them all. Shader and uniform-block ids for the draws are created on
+ * first use and kept by the scene. */
+int slg_scene_draw(slg_context* ctx, size_t sceneId, size_t fboId, size_t shaderId, const float projection[16],
+                   const float view[16], const float cullProjection[16]);
+
 /* Wait for all queued work (SL_Context::draw is synchronous in the reference;
  * here results are synchronous at slg_finish / slg_texture_read). */
 int slg_finish(slg_context* ctx);

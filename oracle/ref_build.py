@@ -27,6 +27,9 @@ SOURCES = [
     "SL_ShaderProcessor.cpp", "SL_Texture.cpp", "SL_TriProcessor.cpp", "SL_TriRasterizer.cpp",
     "SL_UniformBuffer.cpp", "SL_VertexArray.cpp", "SL_VertexBuffer.cpp", "SL_VertexProcessor.cpp",
     "SL_ViewportState.cpp",
+    # scene graph (the caller of the batched draw path)
+    "SL_Animation.cpp", "SL_AnimationChannel.cpp", "SL_AnimationKeyList.cpp", "SL_BoundingBox.cpp", "SL_Camera.cpp", "SL_Material.cpp",
+    "SL_SceneGraph.cpp", "SL_Transform.cpp",
 ]
 
 CXXFLAGS = ["-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-pthread", "-w",

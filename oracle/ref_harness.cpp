@@ -12,6 +12,7 @@
  * uniform blocks are resolved against the current context.
  */
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -27,6 +28,11 @@
 #include "softlight/SL_UniformBuffer.hpp"
 #include "softlight/SL_VertexArray.hpp"
 #include "softlight/SL_VertexBuffer.hpp"
+#include "softlight/SL_BoundingBox.hpp"
+#include "softlight/SL_Camera.hpp"
+#include "softlight/SL_SceneGraph.hpp"
+#include "softlight/SL_SceneNode.hpp"
+#include "softlight/SL_Transform.hpp"
 
 #include "../include/slg.h"
 #include "../include/slg_programs.h"
@@ -37,11 +43,20 @@ namespace math = ls::math;
  * definition needs FreeImage; image files are not used here. */
 const void* SL_ImgFile::data() const { return nullptr; }
 
+/* A reference scene graph with the materials the demos bind (the ambient
+ * texture id per material). */
+struct slr_scene
+{
+    SL_SceneGraph graph;
+    std::vector<size_t> materials;
+};
+
 struct slr_context
 {
     SL_Context ctx;
     std::string err;
     std::vector<size_t> shaderUbo; /* uniform block id of each shader */
+    std::vector<std::unique_ptr<slr_scene>> scenes;
 
     /* SL_Context::create_shader stores &mUniforms[uboId]
      * (softlight/src/SL_Context.cpp:601), a pointer into a vector that a later
@@ -361,5 +376,127 @@ int slr_draw_batch(slr_context* c, const slg_draw_cmd* cmds, size_t n, size_t fb
     return SLG_OK;
 }
 int slr_finish(slr_context*) { return SLG_OK; }
+
+/*-----------------------------------------------------------------------------
+ * Scene graph: the reference's SL_SceneGraph, SL_Transform, SL_BoundingBox and
+ * sl_extract_frustum_planes / sl_is_visible drive the demos' traversal
+ * (softlight/tests/sl_large_scene_test.cpp:678-740), which is caller code and
+ * restated here: per mesh node the model and view-projection matrices, per
+ * submesh the frustum test, the triangle-mode test, the material's texture
+ * and SL_Context::draw.
+-----------------------------------------------------------------------------*/
+static SL_Transform make_transform(const slg_transform* t)
+{
+    SL_Transform r{(SL_TransformType)t->type};
+    r.position(math::vec3{t->position[0], t->position[1], t->position[2]});
+    r.scaling(math::vec3{t->scaling[0], t->scaling[1], t->scaling[2]});
+    r.orientation(math::quat{t->orientation[0], t->orientation[1], t->orientation[2], t->orientation[3]});
+    return r;
+}
+
+size_t slr_create_scene(slr_context* c)
+{
+    c->scenes.emplace_back(new slr_scene());
+    return c->scenes.size() - 1;
+}
+
+int slr_scene_insert_mesh(slr_context* c, size_t sid, const slg_mesh* m, const float maxPoint[3], const float minPoint[3], size_t* out)
+{
+    SL_BoundingBox bb;
+    bb.max_point(math::vec3{maxPoint[0], maxPoint[1], maxPoint[2]});
+    bb.min_point(math::vec3{minPoint[0], minPoint[1], minPoint[2]});
+    *out = c->scenes[sid]->graph.insert_mesh(to_mesh(m), bb);
+    return SLG_OK;
+}
+
+int slr_scene_insert_material(slr_context* c, size_t sid, size_t tex, size_t* out)
+{
+    c->scenes[sid]->materials.push_back(tex);
+    *out = c->scenes[sid]->materials.size() - 1;
+    return SLG_OK;
+}
+
+int slr_scene_insert_node(slr_context* c, size_t sid, size_t parent, size_t n, const size_t* ids, const slg_transform* t, size_t* out)
+{
+    SL_SceneGraph& g = c->scenes[sid]->graph;
+    const SL_Transform tr = make_transform(t);
+    *out = n ? g.insert_mesh_node(parent, "node", n, ids, tr) : g.insert_empty_node(parent, "node", tr);
+    return SLG_OK;
+}
+
+int slr_scene_set_transform(slr_context* c, size_t sid, size_t node, const slg_transform* t)
+{
+    SL_Transform& tr = c->scenes[sid]->graph.mCurrentTransforms[node];
+    tr.type((SL_TransformType)t->type);
+    tr.position(math::vec3{t->position[0], t->position[1], t->position[2]});
+    tr.scaling(math::vec3{t->scaling[0], t->scaling[1], t->scaling[2]});
+    tr.orientation(math::quat{t->orientation[0], t->orientation[1], t->orientation[2], t->orientation[3]});
+    return SLG_OK;
+}
+
+int slr_scene_update(slr_context* c, size_t sid)
+{
+    c->scenes[sid]->graph.update();
+    return SLG_OK;
+}
+
+int slr_scene_read_models(slr_context* c, size_t sid, float* out, size_t n)
+{
+    SL_SceneGraph& g = c->scenes[sid]->graph;
+    if (n != g.mModelMatrices.size()) return SLG_ERR_INVALID_ARG;
+    for (size_t i = 0; i < n; ++i) std::memcpy(out + 16 * i, &g.mModelMatrices[i], 64);
+    return SLG_OK;
+}
+
+int slr_scene_draw(slr_context* c, size_t sid, size_t fbo, size_t shader, const float projection[16], const float view[16],
+                   const float cullProjection[16])
+{
+    slr_scene& sc = *c->scenes[sid];
+    SL_SceneGraph& g = sc.graph;
+    math::mat4 p, v;
+    std::memcpy(&p, projection, 64);
+    std::memcpy(&v, view, 64);
+    const bool cull = cullProjection != nullptr;
+    math::vec4 planes[6];
+    if (cull)
+    {
+        math::mat4 cp;
+        std::memcpy(&cp, cullProjection, 64);
+        sl_extract_frustum_planes(cp, planes);
+    }
+    const math::mat4 vp = p * v;
+    const size_t ubo = c->shaderUbo[shader];
+    slg_lambert_uniforms* u = reinterpret_cast<slg_lambert_uniforms*>(c->ctx.ubo(ubo).buffer());
+    slg_lambert_uniforms saved;
+    std::memcpy(&saved, u, sizeof(saved));
+    for (size_t nodeId = 0; nodeId < g.mNodes.size(); ++nodeId)
+    {
+        const SL_SceneNode& n = g.mNodes[nodeId];
+        if (n.type != NODE_TYPE_MESH) continue;
+        const math::mat4& modelMat = g.mModelMatrices[nodeId];
+        const math::mat4 mv = v * modelMat;
+        std::memcpy(u->vpMatrix, &vp, 64);
+        std::memcpy(u->modelMatrix, &modelMat, 64);
+        const size_t numNodeMeshes = g.mNumNodeMeshes[n.dataId];
+        const size_t* meshIds = g.mNodeMeshes[n.dataId].get();
+        for (size_t k = 0; k < numNodeMeshes; ++k)
+        {
+            const size_t meshId = meshIds[k];
+            const SL_Mesh& m = g.mMeshes[meshId];
+            if (cull && !sl_is_visible(g.mMeshBounds[meshId], mv, planes)) continue;
+            if (!(m.mode & SL_RenderMode::RENDER_MODE_TRIANGLES)) continue;
+            u->textureId = (uint32_t)sc.materials[m.materialId];
+            slg_mesh gm;
+            gm.vaoId = m.vaoId;
+            gm.elementBegin = m.elementBegin;
+            gm.elementEnd = m.elementEnd;
+            gm.mode = (uint32_t)m.mode;
+            gm.materialId = m.materialId;
+            slr_draw(c, &gm, shader, fbo);
+        }
+    }
+    std::memcpy(u, &saved, sizeof(saved));
+    return SLG_OK;
+}
 
 } // extern "C"

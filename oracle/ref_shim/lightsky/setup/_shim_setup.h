@@ -32,6 +32,7 @@
 #define LS_PREFETCH_LEVEL_L2 2
 #define LS_PREFETCH_LEVEL_L3 1
 #define LS_DECLARE_CLASS_TYPE(name, base, ...) typedef base<__VA_ARGS__> name
+#define LS_DEFINE_CLASS_TYPE(base, ...) template class base<__VA_ARGS__>
 #define LS_OS_LINUX 1
 #define LS_OS_UNIX 1
 #define LS_COMPILER_GNU 1

@@ -34,6 +34,7 @@
 #include <new>
 #include <string>
 #include <thread>
+#include <array>
 #include <vector>
 
 namespace
@@ -187,6 +188,21 @@ static size_t index_bytes(int type)
 
 } // namespace
 
+/* A scene graph (SL_SceneGraph's node arrays, softlight/include/softlight/
+ * SL_SceneGraph.hpp:224-300): nodes in insertion order, a parent before its
+ * children. */
+struct SloScene
+{
+    std::vector<uint64_t> parents;             /* SLG_SCENE_ROOT or an earlier node */
+    std::vector<slg_transform> transforms;
+    std::vector<uint8_t> dirty;
+    std::vector<std::array<float, 16>> models;
+    std::vector<std::vector<uint64_t>> nodeMeshes;   /* empty for an empty node */
+    std::vector<slg_mesh> meshes;
+    std::vector<std::array<float, 8>> bounds;  /* mMeshBounds: max xyzw, min xyzw */
+    std::vector<size_t> materials;             /* ambient texture per material */
+};
+
 struct slo_context
 {
     std::string err;
@@ -198,6 +214,7 @@ struct slo_context
     std::vector<Fbo> fbos;
     std::vector<Ubo*> ubos;
     std::vector<Shader> shaders;
+    std::vector<SloScene> scenes;
     uint64_t lastBins = 0, lastFrags = 0;
     std::vector<Bin> lastBinList; /* bins of the last draw group, kept for debugging */
 
@@ -2020,6 +2037,243 @@ void slo_last_stats(const slo_context* ctx, uint64_t* numBins, uint64_t* numFrag
 {
     if (numBins) *numBins = ctx->lastBins;
     if (numFragments) *numFragments = ctx->lastFrags;
+}
+
+/*-----------------------------------------------------------------------------
+ * Scene graph: SL_SceneGraph (softlight/src/SL_SceneGraph.cpp) with
+ * SL_Transform (softlight/src/SL_Transform.cpp) and the mesh-node traversal
+ * of SoftLight's scene demos (softlight/tests/sl_large_scene_test.cpp:678-740).
+ * Matrix arithmetic in the order of the LightMath layer the reference is
+ * built against: column-major, mat * vec sums the scaled columns left to
+ * right.
+-----------------------------------------------------------------------------*/
+static void sg_mat_vec(const float* m, const float v[4], float out[4])
+{
+    for (int r = 0; r < 4; ++r) out[r] = ((m[r] * v[0] + m[4 + r] * v[1]) + m[8 + r] * v[2]) + m[12 + r] * v[3];
+}
+
+static std::array<float, 16> sg_mat_mul(const float* a, const float* b)
+{
+    std::array<float, 16> r;
+    for (int c = 0; c < 4; ++c) sg_mat_vec(a, b + 4 * c, r.data() + 4 * c);
+    return r;
+}
+
+/* get_rst_matrix / get_str_matrix (SL_Transform.cpp:408-432) with the
+ * quaternion's rotation matrix; apply_transform swaps them for the FPS view
+ * types (SL_Transform.cpp:319-328) */
+static std::array<float, 16> sg_local(const slg_transform& t)
+{
+    const float x = t.orientation[0], y = t.orientation[1], z = t.orientation[2], w = t.orientation[3];
+    const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z, wx = w * x, wy = w * y, wz = w * z;
+    const float rot[16] = {1.f - 2.f * (yy + zz), 2.f * (xy + wz), 2.f * (xz - wy), 0.f,
+                           2.f * (xy - wz), 1.f - 2.f * (xx + zz), 2.f * (yz + wx), 0.f,
+                           2.f * (xz + wy), 2.f * (yz - wx), 1.f - 2.f * (xx + yy), 0.f,
+                           0.f, 0.f, 0.f, 1.f};
+    const float ts[16] = {t.scaling[0], 0.f, 0.f, 0.f, 0.f, t.scaling[1], 0.f, 0.f, 0.f, 0.f, t.scaling[2], 0.f,
+                          t.position[0], t.position[1], t.position[2], 1.f};
+    const bool fps = t.type == 1 || t.type == 3;
+    return fps ? sg_mat_mul(rot, ts) : sg_mat_mul(ts, rot);
+}
+
+/* sl_is_visible(const SL_BoundingBox&, mv, planes) (SL_Camera.cpp:63-85) */
+static bool sg_visible(const std::array<float, 8>& b, const float* mv, const float planes[24])
+{
+    float hi[4], lo[4];
+    sg_mat_vec(mv, b.data(), hi);
+    sg_mat_vec(mv, b.data() + 4, lo);
+    float c[3], h[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        c[k] = (hi[k] + lo[k]) * 0.5f;
+        h[k] = (hi[k] - lo[k]) * 0.5f;
+    }
+    const float radius = std::sqrt((h[0] * h[0] + h[1] * h[1]) + h[2] * h[2]);
+    for (int i = 0; i < 6; ++i)
+    {
+        const float* p = planes + 4 * i;
+        if ((((c[0] * p[0] + c[1] * p[1]) + c[2] * p[2]) + p[3]) + radius <= 0.f) return false;
+    }
+    return true;
+}
+
+static SloScene* sg_scene(slo_context* ctx, size_t id)
+{
+    return (id < ctx->scenes.size()) ? &ctx->scenes[id] : nullptr;
+}
+
+size_t slo_create_scene(slo_context* ctx)
+{
+    ctx->scenes.emplace_back();
+    return ctx->scenes.size() - 1;
+}
+
+int slo_scene_insert_mesh(slo_context* ctx, size_t sceneId, const slg_mesh* mesh, const float maxPoint[3],
+                          const float minPoint[3], size_t* outMeshId)
+{
+    SloScene* sc = sg_scene(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    if (!mesh || !maxPoint || !minPoint || !outMeshId) return ctx->fail(SLG_ERR_INVALID_ARG, "null argument");
+    if (mesh->vaoId >= ctx->vaos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid vao id");
+    sc->meshes.push_back(*mesh);
+    sc->bounds.push_back({maxPoint[0], maxPoint[1], maxPoint[2], 1.f, minPoint[0], minPoint[1], minPoint[2], 1.f});
+    *outMeshId = sc->meshes.size() - 1;
+    return SLG_OK;
+}
+
+int slo_scene_insert_material(slo_context* ctx, size_t sceneId, size_t ambientTextureId, size_t* outMaterialId)
+{
+    SloScene* sc = sg_scene(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    if (!outMaterialId) return ctx->fail(SLG_ERR_INVALID_ARG, "null argument");
+    sc->materials.push_back(ambientTextureId);
+    *outMaterialId = sc->materials.size() - 1;
+    return SLG_OK;
+}
+
+/* insert_empty_node / insert_mesh_node (SL_SceneGraph.cpp:1180-1258): the
+ * node is appended with the transform as given (dirty; its model matrix
+ * the identity of a transform never applied), a mesh node's default
+ * bounding box appended to mMeshBounds */
+int slo_scene_insert_node(slo_context* ctx, size_t sceneId, size_t parentId, size_t numSubMeshes, const size_t* subMeshIds,
+                          const slg_transform* transform, size_t* outNodeId)
+{
+    SloScene* sc = sg_scene(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    if (!outNodeId || !transform || (numSubMeshes && !subMeshIds)) return ctx->fail(SLG_ERR_INVALID_ARG, "null argument");
+    if (transform->type > 4) return ctx->fail(SLG_ERR_INVALID_ARG, "unknown transform type");
+    if (parentId != SLG_SCENE_ROOT && parentId >= sc->parents.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid parent node");
+    size_t depth = 1;
+    for (uint64_t p = parentId; p != SLG_SCENE_ROOT; p = sc->parents[p]) ++depth;
+    if (depth > 64) return ctx->fail(SLG_ERR_INVALID_ARG, "scene paths hold at most 64 nodes");
+    for (size_t k = 0; k < numSubMeshes; ++k)
+        if (subMeshIds[k] >= sc->meshes.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid submesh id");
+    sc->parents.push_back(parentId);
+    sc->transforms.push_back(*transform);
+    sc->dirty.push_back(1);
+    std::array<float, 16> ident{};
+    ident[0] = ident[5] = ident[10] = ident[15] = 1.f;
+    sc->models.push_back(ident);
+    sc->nodeMeshes.emplace_back(subMeshIds, subMeshIds + numSubMeshes);
+    if (numSubMeshes) sc->bounds.push_back({1.f, 1.f, 1.f, 1.f, -1.f, -1.f, -1.f, 1.f});
+    *outNodeId = sc->parents.size() - 1;
+    return SLG_OK;
+}
+
+int slo_scene_set_transform(slo_context* ctx, size_t sceneId, size_t nodeId, const slg_transform* transform)
+{
+    SloScene* sc = sg_scene(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    if (nodeId >= sc->parents.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid node id");
+    if (!transform || transform->type > 4) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid transform");
+    sc->transforms[nodeId] = *transform;
+    sc->dirty[nodeId] = 1;
+    return SLG_OK;
+}
+
+/* SL_SceneGraph::update (SL_SceneGraph.cpp:223-299) */
+int slo_scene_update(slo_context* ctx, size_t sceneId)
+{
+    SloScene* sc = sg_scene(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    const size_t n = sc->parents.size();
+    auto update_node = [&](size_t j) {
+        const std::array<float, 16> local = sg_local(sc->transforms[j]);
+        sc->models[j] = (sc->parents[j] == SLG_SCENE_ROOT) ? local : sg_mat_mul(sc->models[sc->parents[j]].data(), local.data());
+        sc->dirty[j] = 0;
+    };
+    for (size_t i = 0; i < n; ++i)
+    {
+        if (!sc->dirty[i]) continue;
+        update_node(i);
+        for (size_t j = i + 1; j < n; ++j)
+        {
+            if (sc->parents[j] < i)
+            {
+                i = j - 1;
+                break;
+            }
+            update_node(j);
+        }
+    }
+    return SLG_OK;
+}
+
+int slo_scene_read_models(slo_context* ctx, size_t sceneId, float* out, size_t numNodes)
+{
+    SloScene* sc = sg_scene(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    if (!out || numNodes != sc->parents.size()) return ctx->fail(SLG_ERR_INVALID_ARG, "node count");
+    for (size_t i = 0; i < numNodes; ++i) std::memcpy(out + 16 * i, sc->models[i].data(), 64);
+    return SLG_OK;
+}
+
+/* The demos' traversal: per mesh node, model and vp * ... into the uniform
+ * block; per submesh, the frustum test, the triangle-mode test, the
+ * material's texture, then SL_Context::draw. The template block is written
+ * for each draw and restored at the end. */
+int slo_scene_draw(slo_context* ctx, size_t sceneId, size_t fboId, size_t shaderId, const float projection[16],
+                   const float view[16], const float cullProjection[16])
+{
+    SloScene* sc = sg_scene(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    if (!projection || !view) return ctx->fail(SLG_ERR_INVALID_ARG, "null matrix");
+    if (shaderId >= ctx->shaders.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid shader id");
+    const Shader& sh = ctx->shaders[shaderId];
+    if (sh.vsProgram != SLG_PROGRAM_LAMBERT_TEX || sh.fsProgram != SLG_PROGRAM_LAMBERT_TEX || sh.ubo == SLG_INVALID_ID)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "scene draws take a SLG_PROGRAM_LAMBERT_TEX shader with a uniform block");
+    if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
+
+    /* sl_extract_frustum_planes (SL_Camera.cpp:25-49) */
+    const bool cull = cullProjection != nullptr;
+    float planes[24] = {};
+    for (int i = 0; i < 4 && cull; ++i)
+    {
+        const float* col = cullProjection + 4 * i;
+        planes[0 + i] = col[3] + col[0];
+        planes[4 + i] = col[3] - col[0];
+        planes[8 + i] = col[3] + col[1];
+        planes[12 + i] = col[3] - col[1];
+        planes[16 + i] = col[3] + col[2];
+        planes[20 + i] = col[3] - col[2];
+    }
+    for (int k = 0; k < 6 && cull; ++k)
+    {
+        float* q = planes + 4 * k;
+        const float lenInv = 1.f / std::sqrt((q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]);
+        for (int i = 0; i < 4; ++i) q[i] = q[i] * lenInv;
+    }
+    const std::array<float, 16> vp = sg_mat_mul(projection, view);
+
+    Ubo& ubo = *ctx->ubos[sh.ubo];
+    slg_lambert_uniforms saved;
+    std::memcpy(&saved, ubo.bytes, sizeof(saved));
+    int status = SLG_OK;
+    for (size_t node = 0; node < sc->parents.size() && status == SLG_OK; ++node)
+    {
+        if (sc->nodeMeshes[node].empty()) continue;
+        const std::array<float, 16>& model = sc->models[node];
+        const std::array<float, 16> mv = sg_mat_mul(view, model.data());
+        for (const uint64_t meshId : sc->nodeMeshes[node])
+        {
+            const slg_mesh& m = sc->meshes[meshId];
+            if (cull && !sg_visible(sc->bounds[meshId], mv.data(), planes)) continue;
+            if (!(m.mode & SLG_RENDER_MODE_TRIANGLES)) continue;
+            if (m.materialId >= sc->materials.size())
+            {
+                status = ctx->fail(SLG_ERR_INVALID_ARG, "scene mesh has no material");
+                break;
+            }
+            slg_lambert_uniforms u = saved;
+            std::memcpy(u.vpMatrix, vp.data(), 64);
+            std::memcpy(u.modelMatrix, model.data(), 64);
+            u.textureId = (uint32_t)sc->materials[m.materialId];
+            std::memcpy(ubo.bytes, &u, sizeof(u));
+            status = slo_draw(ctx, &m, shaderId, fboId);
+        }
+    }
+    std::memcpy(ubo.bytes, &saved, sizeof(saved));
+    return status;
 }
 
 } // extern "C"

@@ -58,6 +58,25 @@ class Mesh(C.Structure):
                 ("mode", C.c_uint32), ("materialId", C.c_uint32)]
 
 
+class Transform(C.Structure):
+    """SL_Transform's parameters (softlight/include/softlight/SL_Transform.hpp:60-75):
+    orientation is a quaternion (x, y, z, w); type an SL_TransformType."""
+    _fields_ = [("position", C.c_float * 3), ("scaling", C.c_float * 3), ("orientation", C.c_float * 4),
+                ("type", C.c_uint32)]
+
+
+SCENE_ROOT = 2 ** (8 * C.sizeof(C.c_size_t)) - 1   # SCENE_NODE_ROOT_ID
+
+
+def make_transform(position=(0.0, 0.0, 0.0), scaling=(1.0, 1.0, 1.0), orientation=(0.0, 0.0, 0.0, 1.0), type=0):
+    t = Transform()
+    t.position[:] = [float(v) for v in position]
+    t.scaling[:] = [float(v) for v in scaling]
+    t.orientation[:] = [float(v) for v in orientation]
+    t.type = type
+    return t
+
+
 class VertexShader(C.Structure):
     """SL_VertexShader (softlight/include/softlight/SL_Shader.hpp:58)."""
     _fields_ = [("numVaryings", C.c_uint8), ("cullMode", C.c_uint8), ("program", C.c_uint32)]
@@ -114,6 +133,17 @@ _SIGNATURES = [
     ("blit_rect", C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t] + [C.c_uint16] * 8),
     ("blit_read", C.c_int, [C.c_void_p, C.c_size_t, C.c_int, C.c_uint16, C.c_uint16, C.c_void_p, C.c_size_t]),
     ("finish", C.c_int, [C.c_void_p]),
+    ("create_scene", C.c_size_t, [C.c_void_p]),
+    ("scene_insert_mesh", C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(Mesh), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                    C.POINTER(C.c_size_t)]),
+    ("scene_insert_material", C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t, C.POINTER(C.c_size_t)]),
+    ("scene_insert_node", C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t, C.c_size_t, C.POINTER(C.c_size_t),
+                                    C.POINTER(Transform), C.POINTER(C.c_size_t)]),
+    ("scene_set_transform", C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t, C.POINTER(Transform)]),
+    ("scene_update", C.c_int, [C.c_void_p, C.c_size_t]),
+    ("scene_read_models", C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t]),
+    ("scene_draw", C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t, C.c_size_t, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                             C.POINTER(C.c_float)]),
 ]
 
 # GPU-only entry points (include/slg.h, "GPU-only controls")
@@ -314,6 +344,50 @@ class SLContext:
     def draw_batch(self, cmds, fbo):
         arr = (DrawCmd * len(cmds))(*cmds)
         self._call("draw_batch", arr, len(cmds), fbo)
+
+    # scene graph (SL_SceneGraph)
+    def create_scene(self):
+        return self._id("create_scene")
+
+    def scene_insert_mesh(self, scene, mesh, max_point, min_point):
+        out = C.c_size_t()
+        hi = (C.c_float * 3)(*[float(v) for v in max_point])
+        lo = (C.c_float * 3)(*[float(v) for v in min_point])
+        self._call("scene_insert_mesh", scene, C.byref(mesh), hi, lo, C.byref(out))
+        return out.value
+
+    def scene_insert_material(self, scene, texture):
+        out = C.c_size_t()
+        self._call("scene_insert_material", scene, texture, C.byref(out))
+        return out.value
+
+    def scene_insert_node(self, scene, parent, sub_meshes, transform):
+        out = C.c_size_t()
+        ids = (C.c_size_t * max(1, len(sub_meshes)))(*sub_meshes)
+        self._call("scene_insert_node", scene, parent, len(sub_meshes), ids, C.byref(transform), C.byref(out))
+        return out.value
+
+    def scene_set_transform(self, scene, node, transform):
+        self._call("scene_set_transform", scene, node, C.byref(transform))
+
+    def scene_update(self, scene):
+        self._call("scene_update", scene)
+
+    def scene_read_models(self, scene, num_nodes):
+        out = np.zeros((num_nodes, 16), np.float32)
+        self._call("scene_read_models", scene, out.ctypes.data_as(C.c_void_p), num_nodes)
+        return out
+
+    def scene_draw(self, scene, fbo, shader, projection, view, cull_projection=None):
+        """projection, view, cull_projection: 4x4 row-major numpy matrices
+        (passed column-major); no culling when cull_projection is None."""
+        def cm(m):
+            return np.ascontiguousarray(np.asarray(m, np.float32).T).ravel()
+        p, v = cm(projection), cm(view)
+        cp = cm(cull_projection) if cull_projection is not None else None
+        self._call("scene_draw", scene, fbo, shader, p.ctypes.data_as(C.POINTER(C.c_float)),
+                   v.ctypes.data_as(C.POINTER(C.c_float)),
+                   cp.ctypes.data_as(C.POINTER(C.c_float)) if cp is not None else None)
 
     def draw_noalloc(self, mesh, shader, fbo):
         """slg_draw with its scratch in a fixed device array (no allocation)."""

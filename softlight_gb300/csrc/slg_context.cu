@@ -132,6 +132,36 @@ constexpr uint64_t kMinCachedSlots = 1ull << 16;  /* smaller launches run the pr
 
 } // namespace
 
+/* A scene graph: SL_SceneGraph's node arrays (softlight/include/softlight/
+ * SL_SceneGraph.hpp:224-300) on the host, the nodes' transforms and model
+ * matrices and the draw list on the device. */
+struct Scene
+{
+    std::vector<uint64_t> parents;              /* SLG_SCENE_ROOT or an earlier node */
+    std::vector<uint32_t> depth;                /* nodes on the path from a root */
+    std::vector<slg_transform> transforms;
+    std::vector<uint8_t> dirty;
+    std::vector<uint64_t> meshFirst, meshCount; /* per node, into nodeMeshes (count 0: empty node) */
+    std::vector<uint64_t> nodeMeshes;
+    std::vector<slg_mesh> meshes;
+    std::vector<float> bounds;                  /* mMeshBounds: max xyzw, min xyzw per entry */
+    std::vector<size_t> materials;              /* ambient texture per material */
+    uint64_t modelsReady = 0;                   /* nodes whose device model matrix exists */
+    DevBuffer dNodes, dList, dModel, dBounds, dEntries;
+
+    /* the draw list: one entry per triangle-mode submesh of a mesh node */
+    struct Entry
+    {
+        uint64_t node, mesh;
+        size_t texture, ubo, shader;
+    };
+    std::vector<Entry> entries;
+    std::vector<size_t> pool;                   /* ubo, shader pairs made for entries */
+    bool listDirty = true;
+    size_t listShader = SLG_INVALID_ID;
+    size_t boundsUploaded = 0;
+};
+
 struct slg_context
 {
     std::string err;
@@ -160,6 +190,7 @@ struct slg_context
     std::vector<Fbo> fbos;
     std::vector<Ubo> ubos;
     std::vector<Shader> shaders;
+    std::vector<Scene> scenes;
 
     /* resource tables visible to device programs */
     DevBuffer texTable, bufTable;
@@ -730,7 +761,16 @@ int launch_batch_graph(slg_context* ctx, const Frame& frame, const DrawDesc* des
 
 /* One launch of the pipeline over a sequence of draws that share a
  * framebuffer. The result equals issuing the draws one after another. */
-int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fboId, bool batch = false)
+/* Work enqueued between the descriptor upload and the pipeline (the scene
+ * graph's draw-list kernel writes uniform blocks and hidden flags there). */
+struct LaunchHook
+{
+    cudaError_t (*fn)(void* user, DrawDesc* devDescs, cudaStream_t s);
+    void* user;
+};
+
+int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fboId, bool batch = false,
+               const LaunchHook* hook = nullptr)
 {
     if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
     const Fbo& fbo = ctx->fbos[fboId];
@@ -886,7 +926,7 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
         f.ids = static_cast<uint32_t*>(fbo.vis.ptr);
     }
 
-    if (batch && ctx->batchGraphs && !ctx->profileStages)
+    if (batch && ctx->batchGraphs && !ctx->profileStages && !hook)
     {
         return launch_batch_graph(ctx, f, descs, starts, n);
     }
@@ -895,6 +935,11 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     if (e == cudaSuccess) e = cudaMemcpyAsync(devStarts, starts, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "descriptor upload");
     ctx->descHead += n + 1;
+    if (hook)
+    {
+        e = hook->fn(hook->user, devDescs, ctx->stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "scene draw list");
+    }
 
     e = slg::launch_pipeline(f, ctx->keyCap, ctx->stream, ctx->profileStages ? ctx->stageEvents : nullptr);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "draw launch");
@@ -902,6 +947,158 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
 }
 
 bool id_ok(size_t id, size_t n) { return id < n; }
+
+/*-----------------------------------------------------------------------------
+ * Scene graph helpers
+-----------------------------------------------------------------------------*/
+/* mat4 * mat4 in the LightMath layer's order (column i = sum of a's columns
+ * scaled by b's column i, left to right); host code is built without
+ * contraction, like the kernels. */
+void mat4_mul(const float* a, const float* b, float* out)
+{
+    float r[16];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            r[4 * i + j] = ((a[j] * b[4 * i] + a[4 + j] * b[4 * i + 1]) + a[8 + j] * b[4 * i + 2]) + a[12 + j] * b[4 * i + 3];
+    std::memcpy(out, r, sizeof(r));
+}
+
+/* sl_extract_frustum_planes (softlight/src/SL_Camera.cpp:25-49): left, right,
+ * bottom, top, near, far from the projection's rows, each scaled by
+ * 1 / |xyz|. */
+void frustum_planes(const float* p, float planes[24])
+{
+    for (int i = 0; i < 4; ++i)
+    {
+        const float w = p[4 * i + 3];
+        planes[0 + i] = w + p[4 * i + 0];
+        planes[4 + i] = w - p[4 * i + 0];
+        planes[8 + i] = w + p[4 * i + 1];
+        planes[12 + i] = w - p[4 * i + 1];
+        planes[16 + i] = w + p[4 * i + 2];
+        planes[20 + i] = w - p[4 * i + 2];
+    }
+    for (int k = 0; k < 6; ++k)
+    {
+        float* q = planes + 4 * k;
+        const float lenInv = 1.f / std::sqrt((q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]);
+        for (int i = 0; i < 4; ++i) q[i] = q[i] * lenInv;
+    }
+}
+
+Scene* scene_of(slg_context* ctx, size_t id)
+{
+    if (!id_ok(id, ctx->scenes.size())) return nullptr;
+    return &ctx->scenes[id];
+}
+
+/* device model matrices for every node (identity for nodes never updated) */
+int scene_models(slg_context* ctx, Scene& sc)
+{
+    const uint64_t n = sc.parents.size();
+    if (sc.modelsReady == n) return SLG_OK;
+    if (sc.dModel.bytes < n * 64)
+    {
+        DevBuffer grown;
+        int r = dev_alloc(ctx, grown, std::max<size_t>(n * 64, sc.dModel.bytes * 2), false);
+        if (r) return r;
+        if (sc.modelsReady)
+        {
+            cudaError_t e = cudaMemcpyAsync(grown.ptr, sc.dModel.ptr, sc.modelsReady * 64, cudaMemcpyDeviceToDevice, ctx->stream);
+            if (e != cudaSuccess) return ctx->cuda_fail(e, "scene models");
+        }
+        cudaStreamSynchronize(ctx->stream);
+        dev_free(sc.dModel);
+        sc.dModel = grown;
+    }
+    std::vector<float> ident((n - sc.modelsReady) * 16, 0.f);
+    for (size_t k = 0; k < n - sc.modelsReady; ++k)
+        for (int d = 0; d < 4; ++d) ident[16 * k + 5 * d] = 1.f;
+    cudaError_t e = cudaMemcpyAsync(static_cast<float*>(sc.dModel.ptr) + 16 * sc.modelsReady, ident.data(), ident.size() * sizeof(float),
+                                    cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "scene models");
+    sc.modelsReady = n;
+    return SLG_OK;
+}
+
+int check_transform(slg_context* ctx, const slg_transform* t)
+{
+    if (!t) return ctx->fail(SLG_ERR_INVALID_ARG, "null transform");
+    if (t->type > 4) return ctx->fail(SLG_ERR_INVALID_ARG, "unknown transform type");
+    return SLG_OK;
+}
+
+/* The draw list of the scene's mesh nodes for shaderId: entries reuse the
+ * scene's shader / uniform-block pairs, made on first use. */
+int scene_build_list(slg_context* ctx, Scene& sc, size_t shaderId)
+{
+    const Shader tmpl = ctx->shaders[shaderId];
+    sc.entries.clear();
+    size_t used = 0;
+    for (size_t node = 0; node < sc.parents.size(); ++node)
+    {
+        for (uint64_t k = 0; k < sc.meshCount[node]; ++k)
+        {
+            const uint64_t meshId = sc.nodeMeshes[sc.meshFirst[node] + k];
+            const slg_mesh& m = sc.meshes[meshId];
+            if (!(m.mode & SLG_RENDER_MODE_TRIANGLES)) continue;
+            if (m.materialId >= sc.materials.size()) return ctx->fail(SLG_ERR_INVALID_ARG, "scene mesh has no material");
+            const size_t tex = sc.materials[m.materialId];
+            if (!texture_ok(ctx, (uint32_t)tex, SLG_COLOR_RGBA_8U)) return ctx->fail(SLG_ERR_INVALID_ARG, "scene material texture is not an RGBA8 texture");
+            if (used == sc.pool.size() / 2)
+            {
+                const size_t ubo = slg_create_ubo(ctx);
+                if (ubo == SLG_INVALID_ID) return ctx->fail(SLG_ERR_NO_MEMORY, "scene uniform block");
+                ctx->shaders.push_back(tmpl);
+                sc.pool.push_back(ubo);
+                sc.pool.push_back(ctx->shaders.size() - 1);
+            }
+            Scene::Entry en;
+            en.node = node;
+            en.mesh = meshId;
+            en.texture = tex;
+            en.ubo = sc.pool[2 * used];
+            en.shader = sc.pool[2 * used + 1];
+            ++used;
+            Shader& sh = ctx->shaders[en.shader];
+            sh = tmpl;
+            sh.ubo = en.ubo;
+            /* the host copy carries the texture the draw validates */
+            std::memcpy(ctx->ubos[en.ubo].shadow, ctx->ubos[tmpl.ubo].shadow, sizeof(slg_lambert_uniforms));
+            const uint32_t tex32 = (uint32_t)tex;
+            std::memcpy(ctx->ubos[en.ubo].shadow + offsetof(slg_lambert_uniforms, textureId), &tex32, 4);
+            sc.entries.push_back(en);
+        }
+    }
+    if (sc.entries.size() + 1 > kDescRing) return ctx->fail(SLG_ERR_INVALID_ARG, "too many scene draws in one launch");
+    std::vector<slg::SceneEntryGpu> dev(sc.entries.size());
+    for (size_t i = 0; i < sc.entries.size(); ++i)
+    {
+        dev[i].node = sc.entries[i].node;
+        dev[i].bounds = (uint32_t)sc.entries[i].mesh;
+        dev[i].textureId = (uint32_t)sc.entries[i].texture;
+        dev[i].ubo = static_cast<uint8_t*>(ctx->ubos[sc.entries[i].ubo].buf.ptr);
+    }
+    if (!dev.empty())
+    {
+        int r = dev_alloc(ctx, sc.dEntries, dev.size() * sizeof(slg::SceneEntryGpu), false);
+        if (r) return r;
+        cudaError_t e = cudaMemcpyAsync(sc.dEntries.ptr, dev.data(), dev.size() * sizeof(slg::SceneEntryGpu), cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "scene draw list upload");
+    }
+    sc.listDirty = false;
+    sc.listShader = shaderId;
+    return SLG_OK;
+}
+
+cudaError_t scene_draw_hook(void* user, DrawDesc* devDescs, cudaStream_t s)
+{
+    slg::SceneDrawArgs* a = static_cast<slg::SceneDrawArgs*>(user);
+    a->descs = devDescs;
+    return slg::launch_scene_draw(*a, s);
+}
 
 } // namespace
 
@@ -944,6 +1141,14 @@ void slg_context_destroy(slg_context* ctx)
     for (Texture& t : ctx->textures) dev_free(t.buf);
     for (Ubo& u : ctx->ubos) dev_free(u.buf);
     for (Fbo& f : ctx->fbos) dev_free(f.vis);
+    for (Scene& sc : ctx->scenes)
+    {
+        dev_free(sc.dNodes);
+        dev_free(sc.dList);
+        dev_free(sc.dModel);
+        dev_free(sc.dBounds);
+        dev_free(sc.dEntries);
+    }
     DevBuffer* scratch[] = {&ctx->texTable, &ctx->bufTable, &ctx->records, &ctx->varyings, &ctx->slotInfo, &ctx->slotOvf,
                             &ctx->ovfCount, &ctx->clipQueue, &ctx->clipCount, &ctx->aliasEvents, &ctx->aliasCount,
                             &ctx->cachePos, &ctx->cacheVary, &ctx->recVerts,
@@ -1401,6 +1606,210 @@ int slg_autotune(slg_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, siz
     ctx->profileStages = prof;
     if (out) { out[0] = bw; out[1] = bh; out[2] = bb; }
     return status;
+}
+
+/*-----------------------------------------------------------------------------
+ * Scene graph (SL_SceneGraph, softlight/include/softlight/SL_SceneGraph.hpp:215)
+-----------------------------------------------------------------------------*/
+size_t slg_create_scene(slg_context* ctx)
+{
+    ctx->scenes.emplace_back();
+    return ctx->scenes.size() - 1;
+}
+
+int slg_scene_insert_mesh(slg_context* ctx, size_t sceneId, const slg_mesh* mesh, const float maxPoint[3],
+                          const float minPoint[3], size_t* outMeshId)
+{
+    Scene* sc = scene_of(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    if (!mesh || !maxPoint || !minPoint || !outMeshId) return ctx->fail(SLG_ERR_INVALID_ARG, "null argument");
+    if (mesh->vaoId >= ctx->vaos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid vao id");
+    sc->meshes.push_back(*mesh);
+    const float b[8] = {maxPoint[0], maxPoint[1], maxPoint[2], 1.f, minPoint[0], minPoint[1], minPoint[2], 1.f};
+    sc->bounds.insert(sc->bounds.end(), b, b + 8);
+    sc->listDirty = true;
+    *outMeshId = sc->meshes.size() - 1;
+    return SLG_OK;
+}
+
+int slg_scene_insert_material(slg_context* ctx, size_t sceneId, size_t ambientTextureId, size_t* outMaterialId)
+{
+    Scene* sc = scene_of(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    if (!outMaterialId) return ctx->fail(SLG_ERR_INVALID_ARG, "null argument");
+    sc->materials.push_back(ambientTextureId);
+    sc->listDirty = true;
+    *outMaterialId = sc->materials.size() - 1;
+    return SLG_OK;
+}
+
+int slg_scene_insert_node(slg_context* ctx, size_t sceneId, size_t parentId, size_t numSubMeshes, const size_t* subMeshIds,
+                          const slg_transform* transform, size_t* outNodeId)
+{
+    Scene* sc = scene_of(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    if (!outNodeId || (numSubMeshes && !subMeshIds)) return ctx->fail(SLG_ERR_INVALID_ARG, "null argument");
+    int r = check_transform(ctx, transform);
+    if (r) return r;
+    if (parentId != SLG_SCENE_ROOT && parentId >= sc->parents.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid parent node");
+    const uint32_t depth = (parentId == SLG_SCENE_ROOT) ? 1u : sc->depth[parentId] + 1u;
+    if (depth > (uint32_t)slg::kSceneMaxDepth) return ctx->fail(SLG_ERR_INVALID_ARG, "scene paths hold at most 64 nodes");
+    if (sc->parents.size() >= 0xFFFFFFFFull) return ctx->fail(SLG_ERR_INVALID_ARG, "too many scene nodes");
+    for (size_t k = 0; k < numSubMeshes; ++k)
+        if (subMeshIds[k] >= sc->meshes.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid submesh id");
+    sc->parents.push_back(parentId == SLG_SCENE_ROOT ? slg::kSceneRoot : (uint64_t)parentId);
+    sc->depth.push_back(depth);
+    sc->transforms.push_back(*transform);
+    sc->dirty.push_back(1);
+    sc->meshFirst.push_back(sc->nodeMeshes.size());
+    sc->meshCount.push_back(numSubMeshes);
+    sc->nodeMeshes.insert(sc->nodeMeshes.end(), subMeshIds, subMeshIds + numSubMeshes);
+    if (numSubMeshes)
+    {
+        /* insert_mesh_node appends a default box to mMeshBounds (max 1, min -1) */
+        const float b[8] = {1.f, 1.f, 1.f, 1.f, -1.f, -1.f, -1.f, 1.f};
+        sc->bounds.insert(sc->bounds.end(), b, b + 8);
+    }
+    sc->listDirty = true;
+    *outNodeId = sc->parents.size() - 1;
+    return SLG_OK;
+}
+
+int slg_scene_set_transform(slg_context* ctx, size_t sceneId, size_t nodeId, const slg_transform* transform)
+{
+    Scene* sc = scene_of(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    if (nodeId >= sc->parents.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid node id");
+    int r = check_transform(ctx, transform);
+    if (r) return r;
+    sc->transforms[nodeId] = *transform;
+    sc->dirty[nodeId] = 1;
+    return SLG_OK;
+}
+
+int slg_scene_update(slg_context* ctx, size_t sceneId)
+{
+    Scene* sc = scene_of(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    int r = scene_models(ctx, *sc);
+    if (r) return r;
+    const size_t n = sc->parents.size();
+    /* SL_SceneGraph::update's loop (SL_SceneGraph.cpp:269-290): a dirty node
+     * and every following node until one whose parent precedes it; a node
+     * updated this way is clean when the loop reaches it */
+    std::vector<slg::SceneNodeGpu> nodes(n);
+    std::vector<uint32_t> list;
+    auto mark = [&](size_t j) {
+        if (!nodes[j].update) list.push_back((uint32_t)j);
+        nodes[j].update = 1;
+        sc->dirty[j] = 0;
+    };
+    for (size_t i = 0; i < n; ++i)
+    {
+        if (!sc->dirty[i]) continue;
+        mark(i);
+        for (size_t j = i + 1; j < n; ++j)
+        {
+            if (sc->parents[j] < i)
+            {
+                i = j - 1;
+                break;
+            }
+            mark(j);
+        }
+    }
+    if (list.empty()) return SLG_OK;
+    for (size_t i = 0; i < n; ++i)
+    {
+        const slg_transform& t = sc->transforms[i];
+        slg::SceneNodeGpu& g = nodes[i];
+        g.parent = sc->parents[i];
+        std::memcpy(g.position, t.position, sizeof(g.position));
+        std::memcpy(g.scaling, t.scaling, sizeof(g.scaling));
+        std::memcpy(g.orientation, t.orientation, sizeof(g.orientation));
+        /* apply_transform flips the order for the FPS view types (SL_Transform.cpp:319-328) */
+        g.viewFps = (t.type == 1 || t.type == 3) ? 1u : 0u;
+    }
+    if ((r = dev_alloc(ctx, sc->dNodes, n * sizeof(slg::SceneNodeGpu), false))) return r;
+    if ((r = dev_alloc(ctx, sc->dList, list.size() * sizeof(uint32_t), false))) return r;
+    cudaError_t e = cudaMemcpyAsync(sc->dNodes.ptr, nodes.data(), n * sizeof(slg::SceneNodeGpu), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sc->dList.ptr, list.data(), list.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = slg::launch_scene_update(static_cast<const slg::SceneNodeGpu*>(sc->dNodes.ptr), static_cast<const uint32_t*>(sc->dList.ptr),
+                                     (uint32_t)list.size(), static_cast<float*>(sc->dModel.ptr), ctx->stream);
+    /* the host vectors are released on return: the copies must have read them */
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "scene update");
+    return SLG_OK;
+}
+
+int slg_scene_read_models(slg_context* ctx, size_t sceneId, float* out, size_t numNodes)
+{
+    Scene* sc = scene_of(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    if (!out || numNodes != sc->parents.size()) return ctx->fail(SLG_ERR_INVALID_ARG, "node count");
+    int r = scene_models(ctx, *sc);
+    if (r) return r;
+    if (!numNodes) return SLG_OK;
+    cudaError_t e = cudaMemcpyAsync(out, sc->dModel.ptr, numNodes * 64, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "scene model read");
+    return SLG_OK;
+}
+
+int slg_scene_draw(slg_context* ctx, size_t sceneId, size_t fboId, size_t shaderId, const float projection[16],
+                   const float view[16], const float cullProjection[16])
+{
+    Scene* sc = scene_of(ctx, sceneId);
+    if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
+    if (!projection || !view) return ctx->fail(SLG_ERR_INVALID_ARG, "null matrix");
+    if (!id_ok(shaderId, ctx->shaders.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid shader id");
+    /* a copy: building the draw list appends to ctx->shaders */
+    const Shader sh = ctx->shaders[shaderId];
+    if (sh.vsProgram != SLG_PROGRAM_LAMBERT_TEX || sh.fsProgram != SLG_PROGRAM_LAMBERT_TEX || sh.ubo == SLG_INVALID_ID)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "scene draws take a SLG_PROGRAM_LAMBERT_TEX shader with a uniform block");
+    if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
+    int r = scene_models(ctx, *sc);
+    if (r) return r;
+    if (sc->listDirty || sc->listShader != shaderId)
+    {
+        if ((r = scene_build_list(ctx, *sc, shaderId))) return r;
+    }
+    if (sc->entries.empty()) return SLG_OK;
+    if (sc->boundsUploaded != sc->bounds.size())
+    {
+        if ((r = dev_alloc(ctx, sc->dBounds, sc->bounds.size() * sizeof(float), false))) return r;
+        cudaError_t e = cudaMemcpyAsync(sc->dBounds.ptr, sc->bounds.data(), sc->bounds.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "scene bounds upload");
+        sc->boundsUploaded = sc->bounds.size();
+    }
+    slg::SceneDrawArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.entries = static_cast<const slg::SceneEntryGpu*>(sc->dEntries.ptr);
+    a.numEntries = (uint32_t)sc->entries.size();
+    a.cull = cullProjection ? 1 : 0;
+    a.model = static_cast<const float*>(sc->dModel.ptr);
+    a.bounds = static_cast<const float*>(sc->dBounds.ptr);
+    mat4_mul(projection, view, a.vp);
+    std::memcpy(a.view, view, sizeof(a.view));
+    if (cullProjection) frustum_planes(cullProjection, a.planes);
+    static_assert(sizeof(slg_lambert_uniforms) <= sizeof(a.templ), "template block");
+    std::memcpy(a.templ, ctx->ubos[sh.ubo].shadow, sizeof(slg_lambert_uniforms));
+    a.templWords = sizeof(slg_lambert_uniforms) / 4;
+    std::vector<DrawRequest> reqs;
+    reqs.reserve(sc->entries.size());
+    for (const Scene::Entry& en : sc->entries)
+    {
+        DrawRequest q;
+        q.mesh = sc->meshes[en.mesh];
+        q.numInstances = 1;
+        q.shaderId = en.shader;
+        q.primBase = 0;
+        reqs.push_back(q);
+    }
+    const LaunchHook hook = {scene_draw_hook, &a};
+    return run_launch(ctx, reqs, fboId, false, &hook);
 }
 
 int slg_finish(slg_context* ctx)

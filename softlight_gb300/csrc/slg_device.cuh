@@ -81,7 +81,8 @@ struct DrawDesc
     int32_t  indexType;     /* -1: non-indexed */
     uint32_t vsProgram;
     uint32_t fsProgram;
-    uint8_t  cull, numVaryings, depthTest, depthMask, blend, numOutputs, prim, pad1;
+    uint8_t  cull, numVaryings, depthTest, depthMask, blend, numOutputs, prim;
+    uint8_t  hidden;        /* 1: culled as a whole by the scene-graph producer (set on the device) */
 };
 
 /* DrawDesc::prim */

@@ -841,6 +841,10 @@ __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, Ti
 {
     const int di = (f.numDraws > 1) ? find_draw(f, slot) : 0;
     const DrawDesc& d = f.draws[di];
+    if (d.hidden)
+    {
+        return 0;
+    }
     const uint64_t local = slot - d.slotBase;
     if (!kCached && d.prim == kPrimPoint)
     {
@@ -1004,6 +1008,10 @@ __global__ void __launch_bounds__(256) vertex_cache_kernel(const Frame f)
         else hi = mid - 1;
     }
     const DrawDesc& d = f.draws[lo];
+    if (d.hidden)
+    {
+        return;
+    }
     const uint64_t local = e - d.cacheBase;
     const uint64_t inst = local / d.cacheVerts;
     const uint64_t vid = local - inst * d.cacheVerts;
@@ -2610,6 +2618,171 @@ __global__ void clear_kernel(uint8_t* dst, size_t numTexels, int bytesPerTexel, 
             for (int b = 0; b < bytesPerTexel; ++b) dst[i * (size_t)bytesPerTexel + b] = v[b];
         }
     }
+}
+
+/*-----------------------------------------------------------------------------
+ * Scene graph: SL_SceneGraph::update (softlight/src/SL_SceneGraph.cpp:223-299)
+ * and the draw list of a mesh-node traversal, in the arithmetic of the
+ * LightMath layer the reference sources are built against (mat4 * vec4 sums
+ * the scaled columns left to right; mat4 * mat4 applies that per column).
+-----------------------------------------------------------------------------*/
+struct M4
+{
+    float4 c[4];
+};
+
+__device__ __forceinline__ float4 m4_apply(const M4& a, const float4 v)
+{
+    return make_float4(((a.c[0].x * v.x + a.c[1].x * v.y) + a.c[2].x * v.z) + a.c[3].x * v.w,
+                       ((a.c[0].y * v.x + a.c[1].y * v.y) + a.c[2].y * v.z) + a.c[3].y * v.w,
+                       ((a.c[0].z * v.x + a.c[1].z * v.y) + a.c[2].z * v.z) + a.c[3].z * v.w,
+                       ((a.c[0].w * v.x + a.c[1].w * v.y) + a.c[2].w * v.z) + a.c[3].w * v.w);
+}
+
+__device__ __forceinline__ M4 m4_mul(const M4& a, const M4& b)
+{
+    M4 r;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r.c[i] = m4_apply(a, b.c[i]);
+    return r;
+}
+
+__device__ __forceinline__ M4 m4_load(const float* p)
+{
+    M4 r;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r.c[i] = make_float4(p[4 * i], p[4 * i + 1], p[4 * i + 2], p[4 * i + 3]);
+    return r;
+}
+
+__device__ __forceinline__ void m4_store(float* p, const M4& m)
+{
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+    {
+        p[4 * i] = m.c[i].x;
+        p[4 * i + 1] = m.c[i].y;
+        p[4 * i + 2] = m.c[i].z;
+        p[4 * i + 3] = m.c[i].w;
+    }
+}
+
+/* SL_Transform::get_rst_matrix / get_str_matrix (softlight/src/SL_Transform.cpp:
+ * 408-432): (translation x scale) * R or R * (translation x scale), R the
+ * rotation of the orientation quaternion (columns (1-2(yy+zz), 2(xy+wz),
+ * 2(xz-wy)), (2(xy-wz), 1-2(xx+zz), 2(yz+wx)), (2(xz+wy), 2(yz-wx),
+ * 1-2(xx+yy))). */
+__device__ M4 scene_local(const SceneNodeGpu& n)
+{
+    const float x = n.orientation[0], y = n.orientation[1], z = n.orientation[2], w = n.orientation[3];
+    const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z, wx = w * x, wy = w * y, wz = w * z;
+    M4 r;
+    r.c[0] = make_float4(1.f - 2.f * (yy + zz), 2.f * (xy + wz), 2.f * (xz - wy), 0.f);
+    r.c[1] = make_float4(2.f * (xy - wz), 1.f - 2.f * (xx + zz), 2.f * (yz + wx), 0.f);
+    r.c[2] = make_float4(2.f * (xz + wy), 2.f * (yz - wx), 1.f - 2.f * (xx + yy), 0.f);
+    r.c[3] = make_float4(0.f, 0.f, 0.f, 1.f);
+    M4 ts;
+    ts.c[0] = make_float4(n.scaling[0], 0.f, 0.f, 0.f);
+    ts.c[1] = make_float4(0.f, n.scaling[1], 0.f, 0.f);
+    ts.c[2] = make_float4(0.f, 0.f, n.scaling[2], 0.f);
+    ts.c[3] = make_float4(n.position[0], n.position[1], n.position[2], 1.f);
+    return n.viewFps ? m4_mul(r, ts) : m4_mul(ts, r);
+}
+
+/* One thread per recomputed node: update_node_transform sets
+ * model = parent's model * local (apply_pre_transform), or local for a node
+ * of the root. The parent's model is the one this update computes when the
+ * parent is recomputed too (it precedes the node in the reference's loop),
+ * so the thread walks up through recomputed ancestors and multiplies down;
+ * every thread writes only its own node. */
+__global__ void __launch_bounds__(128) scene_update_kernel(const SceneNodeGpu* nodes, const uint32_t* list, uint32_t n, float* model)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+    {
+        return;
+    }
+    uint32_t chain[kSceneMaxDepth];
+    int len = 0;
+    uint64_t c = list[i];
+    for (;;)
+    {
+        chain[len++] = (uint32_t)c;
+        const uint64_t p = nodes[c].parent;
+        if (p == kSceneRoot || !nodes[p].update || len == kSceneMaxDepth)
+        {
+            break;
+        }
+        c = p;
+    }
+    const uint64_t top = chain[len - 1];
+    const uint64_t topParent = nodes[top].parent;
+    M4 m = scene_local(nodes[top]);
+    if (topParent != kSceneRoot)
+    {
+        m = m4_mul(m4_load(model + 16 * topParent), m);
+    }
+    for (int k = len - 2; k >= 0; --k)
+    {
+        m = m4_mul(m, scene_local(nodes[chain[k]]));
+    }
+    m4_store(model + 16 * (uint64_t)list[i], m);
+}
+
+/* One thread per draw of the list: the traversal of SoftLight's scene demos
+ * (softlight/tests/sl_large_scene_test.cpp:689-740): mv = view * model,
+ * sl_is_visible(bounds, mv, frustum planes) (softlight/src/SL_Camera.cpp:
+ * 63-85), then the draw's uniform block. */
+__global__ void __launch_bounds__(128) scene_draw_kernel(const SceneDrawArgs a)
+{
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= a.numEntries)
+    {
+        return;
+    }
+    const SceneEntryGpu en = a.entries[e];
+    const float* mp = a.model + 16 * en.node;
+    bool visible = true;
+    if (a.cull)
+    {
+        const M4 mv = m4_mul(m4_load(a.view), m4_load(mp));
+        const float* b = a.bounds + 8 * (uint64_t)en.bounds;
+        const float4 bmax = m4_apply(mv, make_float4(b[0], b[1], b[2], b[3]));
+        const float4 bmin = m4_apply(mv, make_float4(b[4], b[5], b[6], b[7]));
+        const float cx = (bmax.x + bmin.x) * 0.5f, cy = (bmax.y + bmin.y) * 0.5f, cz = (bmax.z + bmin.z) * 0.5f;
+        const float hx = (bmax.x - bmin.x) * 0.5f, hy = (bmax.y - bmin.y) * 0.5f, hz = (bmax.z - bmin.z) * 0.5f;
+        const float radius = sqrtf((hx * hx + hy * hy) + hz * hz);
+        for (int i = 0; i < 6; ++i)
+        {
+            const float* pl = a.planes + 4 * i;
+            if (((((cx * pl[0] + cy * pl[1]) + cz * pl[2]) + pl[3]) + radius) <= 0.f)
+            {
+                visible = false;
+                break;
+            }
+        }
+    }
+    uint32_t* dst = reinterpret_cast<uint32_t*>(en.ubo);
+    for (uint32_t k = 0; k < a.templWords; ++k) dst[k] = a.templ[k];
+    float* u = reinterpret_cast<float*>(en.ubo);
+    for (int k = 0; k < 16; ++k) u[offsetof(slg_lambert_uniforms, vpMatrix) / 4 + k] = a.vp[k];
+    for (int k = 0; k < 16; ++k) u[offsetof(slg_lambert_uniforms, modelMatrix) / 4 + k] = mp[k];
+    dst[offsetof(slg_lambert_uniforms, textureId) / 4] = en.textureId;
+    a.descs[e].hidden = visible ? 0 : 1;
+}
+
+cudaError_t launch_scene_update(const SceneNodeGpu* nodes, const uint32_t* list, uint32_t n, float* model, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    scene_update_kernel<<<(n + 127) / 128, 128, 0, s>>>(nodes, list, n, model);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scene_draw(const SceneDrawArgs& a, cudaStream_t s)
+{
+    if (a.numEntries == 0) return cudaSuccess;
+    scene_draw_kernel<<<(a.numEntries + 127) / 128, 128, 0, s>>>(a);
+    return cudaGetLastError();
 }
 
 /*-----------------------------------------------------------------------------

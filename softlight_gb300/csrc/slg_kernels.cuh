@@ -36,6 +36,50 @@ struct BlitArgs
 };
 cudaError_t launch_blit(const BlitArgs& a, cudaStream_t s);
 
+/* Scene graph: the device copy of a node (SL_SceneGraph's mNodeParentIds
+ * and mCurrentTransforms, softlight/include/softlight/SL_SceneGraph.hpp:230-260). */
+constexpr int kSceneMaxDepth = 64;    /* nodes on a path from a root, inclusive */
+constexpr uint64_t kSceneRoot = ~0ull; /* SCENE_NODE_ROOT_ID */
+struct SceneNodeGpu
+{
+    uint64_t parent;          /* kSceneRoot: attached to the root */
+    float position[3];
+    float scaling[3];
+    float orientation[4];     /* quaternion x, y, z, w */
+    uint32_t viewFps;         /* SL_TRANSFORM_TYPE_VIEW_FPS(_LOCKED_Y): R * TS instead of TS * R */
+    uint32_t update;          /* recomputed by this update */
+};
+
+/* Recomputes the model matrices (16 floats per node, column-major) of the
+ * n nodes in list (SL_SceneGraph::update's set for this call). */
+cudaError_t launch_scene_update(const SceneNodeGpu* nodes, const uint32_t* list, uint32_t n, float* model, cudaStream_t s);
+
+/* One draw of the scene's draw list: a submesh of a mesh node. */
+struct SceneEntryGpu
+{
+    uint64_t node;
+    uint32_t bounds;          /* bounding box index (8 floats: max xyzw, min xyzw) */
+    uint32_t textureId;       /* the material's ambient texture */
+    uint8_t* ubo;             /* the draw's slg_lambert_uniforms */
+};
+
+struct SceneDrawArgs
+{
+    const SceneEntryGpu* entries;
+    uint32_t numEntries;
+    int32_t cull;             /* frustum-cull by bounding box (sl_is_visible) */
+    const float* model;       /* 16 floats per node */
+    const float* bounds;
+    DrawDesc* descs;          /* entry e's descriptor of the launch */
+    float vp[16], view[16], planes[24];
+    uint32_t templ[64];       /* the template uniform block, copied first */
+    uint32_t templWords;
+};
+
+/* Writes each entry's uniform block (template, vpMatrix, modelMatrix,
+ * textureId) and its descriptor's hidden flag. */
+cudaError_t launch_scene_draw(const SceneDrawArgs& a, cudaStream_t s);
+
 } // namespace slg
 
 #endif /* SLG_KERNELS_CUH */

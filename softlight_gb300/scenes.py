@@ -524,6 +524,131 @@ def build_c4(ctx, num_draws=256, width=3840, height=2160, tex_size=512, batched=
     return s
 
 
+def quat_axis_angle(axis, angle):
+    """Unit quaternion (x, y, z, w) of a rotation by angle about axis."""
+    a = np.asarray(axis, np.float64)
+    a = a / np.linalg.norm(a)
+    h = math.sin(0.5 * angle)
+    return (float(a[0] * h), float(a[1] * h), float(a[2] * h), float(math.cos(0.5 * angle)))
+
+
+class GraphScene(Scene):
+    """A scene graph (SL_SceneGraph) drawn through the library's scene entry
+    points: per frame, clear, the frame's transform changes, update, then
+    the mesh-node traversal as one draw list."""
+
+    def __init__(self, ctx, name, width, height):
+        super().__init__(ctx, name, width, height)
+        self.scene = ctx.create_scene()
+        self.num_nodes = 0
+        self.shader = None
+        self.projection = np.eye(4)
+        self.view = np.eye(4)
+        self.cull_projection = None   # frustum of the culling test (None: no culling)
+        self.frame = 0
+        self.animate = None      # callable(scene, frame) setting transforms
+
+    def node(self, parent, sub_meshes, transform):
+        n = self.ctx.scene_insert_node(self.scene, parent, list(sub_meshes), transform)
+        self.num_nodes += 1
+        return n
+
+    def render(self, clear=True):
+        ctx = self.ctx
+        if clear:
+            ctx.clear_framebuffer(self.fbo, 0, self.clear_color, self.clear_depth)
+        if self.animate is not None:
+            self.animate(self, self.frame)
+        ctx.scene_update(self.scene)
+        ctx.scene_draw(self.scene, self.fbo, self.shader, self.projection, self.view, self.cull_projection)
+        self.frame += 1
+
+    def read_models(self):
+        return self.ctx.scene_read_models(self.scene, self.num_nodes)
+
+
+def build_scene_graph(ctx, width=320, height=240, groups=6, per_group=5, seed=21, tex_size=64, lon=24, lat=12, cull_fov=40.0):
+    """A scene graph of `groups` group nodes in a ring, each with `per_group`
+    mesh-node children (some with two submeshes, one with a lines-mode
+    submesh the traversal skips, one with a grandchild), an FPS-view
+    transform on one child, a group far outside the frustum, and two
+    children inserted after all groups (so their subtrees are not
+    contiguous: the reference's update leaves the second one stale when its
+    group changes). Frames 1, 2, ... rotate group 3, move one child and one
+    grandchild. Lambert with one texture per mesh, cull on back faces; submeshes
+    culled against a cull_fov-degree frustum (None: no culling), narrower than
+    the drawn 55 degrees."""
+    rng = np.random.default_rng(seed)
+    s = GraphScene(ctx, f"scene_graph_{groups}x{per_group}", width, height)
+    shapes = [uv_sphere(lon, lat), torus(lon, max(6, lat // 2)), grid(8, 8)]
+    meshes = []
+    tris = []
+    for k, (verts, idx) in enumerate(shapes):
+        mesh = s.add_mesh(verts, idx)
+        tex = s.add_texture_rgba8(to_rgba8(value_noise(tex_size, tex_size, seed=seed + k, octaves=2, alpha=1.0)))
+        mesh.materialId = ctx.scene_insert_material(s.scene, tex)
+        meshes.append(ctx.scene_insert_mesh(s.scene, mesh, verts[:, :3].max(0), verts[:, :3].min(0)))
+        tris.append(idx.size // 3)
+    lines = A.Mesh(mesh.vaoId, 0, (shapes[2][1].size // 2) * 2, A.RENDER_MODE_INDEXED_LINES, mesh.materialId)
+    lines_id = ctx.scene_insert_mesh(s.scene, lines, (1, 1, 1), (-1, -1, -1))
+    light = np.asarray([0.4, 0.8, 0.45])
+    light = light / np.linalg.norm(light)
+    s.projection = perspective(55.0, width / height, 0.5, 60.0)
+    s.view = look_at((0.0, 6.0, 17.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0))
+    # a narrower culling frustum than the drawn one, so culling shows in the image
+    s.cull_projection = perspective(cull_fov, width / height, 0.5, 60.0) if cull_fov else None
+    s.shader = s.add_shader(A.PROGRAM_LAMBERT_TEX, 2, lambert_uniforms(np.eye(4), np.eye(4), [*light, 0.0],
+                                                                       [0.12, 0.12, 0.12, 0.0], 0))
+    T = A.make_transform
+    group_ids, children = [], []
+    num_tris = 0
+    for g in range(groups):
+        ang = 2.0 * math.pi * g / groups
+        gpos = (9.0 * math.cos(ang), float(rng.uniform(-2.0, 2.0)), 9.0 * math.sin(ang) - 3.0)
+        gn = s.node(A.SCENE_ROOT, [], T(gpos, (1.0, 1.0, 1.0), quat_axis_angle(rng.normal(size=3), rng.uniform(0, math.pi))))
+        group_ids.append(gn)
+        for c in range(per_group):
+            subs = [meshes[(g + c) % 3]]
+            if c % 3 == 0:
+                subs.append(meshes[(g + c + 1) % 3])
+            if c == 1:
+                subs.append(lines_id)
+            pos = rng.uniform(-3.0, 3.0, 3)
+            sc = rng.uniform(0.4, 1.2, 3)
+            cn = s.node(gn, subs, T(pos, sc, quat_axis_angle(rng.normal(size=3), rng.uniform(0, math.pi)),
+                                    type=1 if (g == 2 and c == 0) else 0))
+            num_tris += sum(tris[m] for m in subs if m < len(tris))
+            children.append(cn)
+            if c == 2:
+                gc = s.node(cn, [meshes[0]], T((0.0, 1.6, 0.0), (0.5, 0.5, 0.5), (0.0, 0.0, 0.0, 1.0)))
+                num_tris += tris[0]
+                children.append(gc)
+    far = s.node(A.SCENE_ROOT, [], T((0.0, 0.0, 200.0)))
+    s.node(far, [meshes[1]], T())
+    num_tris += tris[1]
+    late0 = s.node(group_ids[0], [meshes[1]], T((0.0, -2.5, 0.0), (0.7, 0.7, 0.7)))
+    late3 = s.node(group_ids[min(3, groups - 1)], [meshes[0]], T((0.0, 2.5, 0.0), (0.8, 0.8, 0.8)))
+    num_tris += tris[1] + tris[0]
+    s.num_triangles = num_tris
+    s.late_children = (late0, late3)
+    g3 = group_ids[min(3, groups - 1)]
+    g3_pos = (9.0 * math.cos(2.0 * math.pi * min(3, groups - 1) / groups), 0.5, 9.0 * math.sin(2.0 * math.pi * min(3, groups - 1) / groups) - 3.0)
+    mover = children[1]
+    grand = children[3] if len(children) > 3 else children[-1]
+
+    def animate(scene, frame):
+        if frame == 0:
+            return
+        scene.ctx.scene_set_transform(scene.scene, g3, T(g3_pos, (1.0, 1.0, 1.0), quat_axis_angle((0.2, 1.0, 0.1), 0.4 * frame)))
+        scene.ctx.scene_set_transform(scene.scene, mover, T((0.5 * frame - 1.0, 0.3, 0.2), (0.9, 0.9, 0.9),
+                                                            quat_axis_angle((1.0, 0.0, 0.3), 0.3 * frame)))
+        if frame % 2 == 0:
+            scene.ctx.scene_set_transform(scene.scene, grand, T((0.0, 1.6 + 0.1 * frame, 0.0), (0.5, 0.6, 0.5)))
+
+    s.animate = animate
+    return s
+
+
 def displaced_sphere(lon=100, lat=50, seed=5, amplitude=0.1, waves=6):
     """UV sphere (lon*lat*2 triangles) with radius 1 + amplitude * noise(n),
     noise a seeded sum of sinusoids of the direction: positions (V x 3),

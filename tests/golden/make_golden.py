@@ -64,6 +64,11 @@ def main():
     np.savez_compressed(os.path.join(HERE, "blits.npz"), **blits)
     print("blits", sorted(blits))
 
+    # the scene graph: update + mesh-node traversal over three frames
+    graph = G.scene_graph_cases(lambda: SLContext(lib, "slr_", gpu=False))
+    np.savez_compressed(os.path.join(HERE, "scene_graph.npz"), **graph)
+    print("scene_graph", sorted(graph))
+
 
 if __name__ == "__main__":
     main()

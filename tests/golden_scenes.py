@@ -131,3 +131,26 @@ def blit_cases(ctx):
     ctx.blit(dstf, s.depth_tex)
     out["whole_rf_to_rgbaf_64x48"] = ctx.texture_read(dstf, (48, 64, 4), np.float32)
     return out
+
+
+# The scene graph (SL_SceneGraph): three frames of build_scene_graph, culled
+# against a 40-degree frustum and unculled; per frame the model matrices,
+# colour and depth.
+SCENE_GRAPH_VARIANTS = {"cull40": 40.0, "nocull": None}
+SCENE_GRAPH_FRAMES = 3
+
+
+def scene_graph_cases(make_ctx):
+    """{variant}_{models,color,depth}_f{k} arrays, one new context per variant."""
+    from softlight_gb300 import scenes as S
+    out = {}
+    for variant, fov in SCENE_GRAPH_VARIANTS.items():
+        ctx = make_ctx()
+        scene = S.build_scene_graph(ctx, cull_fov=fov)
+        for k in range(SCENE_GRAPH_FRAMES):
+            scene.render()
+            out[f"{variant}_models_f{k}"] = scene.read_models()
+            out[f"{variant}_color_f{k}"] = scene.read_color()
+            out[f"{variant}_depth_f{k}"] = scene.read_depth()
+        ctx.close()
+    return out

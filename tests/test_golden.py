@@ -68,6 +68,67 @@ def test_oracle_blits_match_reference_golden(oracle_mod):
         assert same(got[name], want[name]), f"blit {name} differs from the reference"
 
 
+def test_oracle_scene_graph_matches_reference_golden(oracle_mod):
+    """SL_SceneGraph::update and the mesh-node traversal over three frames
+    (dirty propagation including a child the reference's update leaves
+    stale, an FPS-view transform, a lines-mode submesh skipped, frustum
+    culling): model matrices, colour and depth bit for bit against the
+    reference's (tests/golden/scene_graph.npz)."""
+    want = np.load(os.path.join(GOLDEN, "scene_graph.npz"))
+    got = G.scene_graph_cases(oracle_mod.Context)
+    assert set(got) == set(want.files)
+    for name in want.files:
+        assert same(got[name], want[name]), f"scene graph {name} differs from the reference"
+
+
+def test_oracle_scene_graph_rejections(oracle_mod):
+    """Bad ids, a non-Lambert shader and paths deeper than 64 nodes fail."""
+    from softlight_gb300 import api as A
+    from softlight_gb300 import scenes as S
+    ctx = oracle_mod.Context()
+    s = S.build_scene_graph(ctx, groups=2, per_group=2)
+    T = A.make_transform
+    with pytest.raises(A.SLError, match="invalid parent"):
+        ctx.scene_insert_node(s.scene, 10 ** 6, [], T())
+    with pytest.raises(A.SLError, match="invalid submesh"):
+        ctx.scene_insert_node(s.scene, A.SCENE_ROOT, [99], T())
+    with pytest.raises(A.SLError, match="invalid scene"):
+        ctx.scene_update(77)
+    with pytest.raises(A.SLError, match="unknown transform type"):
+        ctx.scene_insert_node(s.scene, A.SCENE_ROOT, [], T(type=9))
+    parent = A.SCENE_ROOT
+    for _ in range(64):
+        parent = ctx.scene_insert_node(s.scene, parent, [], T())
+    with pytest.raises(A.SLError, match="at most 64"):
+        ctx.scene_insert_node(s.scene, parent, [], T())
+    flat = s.add_shader(A.PROGRAM_FLAT_COLOR, 0, S.flat_uniforms(np.eye(4), (1, 1, 1, 1)))
+    with pytest.raises(A.SLError, match="LAMBERT_TEX"):
+        ctx.scene_draw(s.scene, s.fbo, flat, np.eye(4), np.eye(4))
+    ctx.close()
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_TREE), reason="reference tree not present")
+def test_reference_scene_graph_matches_oracle_live(oracle_mod):
+    """The reference's SL_SceneGraph, SL_Transform and sl_is_visible, built
+    from its sources, against the oracle on a larger graph over four frames."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(HERE), "oracle"))
+    import ref_build
+    from softlight_gb300.api import SLContext, open_library
+    from softlight_gb300 import scenes as S
+    lib = open_library(ref_build.build_ref(), "slr_", gpu=False)
+    r = SLContext(lib, "slr_", gpu=False)
+    o = oracle_mod.Context()
+    sr = S.build_scene_graph(r, groups=9, per_group=7, seed=33, cull_fov=30.0)
+    so = S.build_scene_graph(o, groups=9, per_group=7, seed=33, cull_fov=30.0)
+    for _ in range(4):
+        sr.render()
+        so.render()
+        assert same(sr.read_models(), so.read_models())
+        assert same(sr.read_depth(), so.read_depth())
+        assert same(sr.read_color(), so.read_color())
+
+
 @pytest.mark.parametrize("threads", [2, 5])
 def test_oracle_threads_match_one_thread(oracle_mod, threads):
     """The oracle's multi-threaded mode (used for the CPU baseline timing)

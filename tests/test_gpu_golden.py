@@ -60,6 +60,19 @@ def test_gpu_blits_match_reference_golden(gpu_lib):
         assert same, f"blit {name} differs from the reference"
 
 
+def test_gpu_scene_graph_matches_reference_golden(gpu_lib):
+    """SL_SceneGraph::update and the mesh-node traversal on the GPU (update
+    kernel, draw-list kernel, one batched launch per frame): model matrices,
+    colour and depth bit for bit against the reference's three frames
+    (tests/golden/scene_graph.npz)."""
+    want = np.load(os.path.join(GOLDEN, "scene_graph.npz"))
+    got = G.scene_graph_cases(gpu_lib.Context)
+    assert set(got) == set(want.files)
+    for name in want.files:
+        a, b = got[name], want[name]
+        assert a.dtype == b.dtype and np.array_equal(a.view(np.uint8), b.view(np.uint8)), f"scene graph {name} differs from the reference"
+
+
 def test_gpu_blit_rejects_out_of_bounds_rectangles(gpu_lib):
     from softlight_gb300 import api as A
     ctx = gpu_lib.Context()

@@ -473,3 +473,59 @@ def test_format_edges(ctxs, color_type):
     g, o = ctxs
     sg, so = render_both(E.format_edges, g, o, color_type=color_type, width=40, height=24)
     compare_scenes(sg, so, f"format edges {color_type}")
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("cull_fov", [None, 30.0])
+def test_scene_graph(ctxs, mode, cull_fov):
+    """A larger scene graph over five frames in both raster modes: model
+    matrices bit for bit, images against the oracle."""
+    g, o = ctxs
+    g.set_raster_mode(mode)
+    sg = S.build_scene_graph(g, width=640, height=480, groups=14, per_group=9, seed=44, cull_fov=cull_fov)
+    so = S.build_scene_graph(o, width=640, height=480, groups=14, per_group=9, seed=44, cull_fov=cull_fov)
+    for f in range(5):
+        sg.render()
+        so.render()
+        mg, mo = sg.read_models(), so.read_models()
+        assert np.array_equal(mg.view(np.uint32), mo.view(np.uint32)), f"frame {f}: model matrices differ"
+        compare_scenes(sg, so, f"scene graph frame {f} cull {cull_fov} mode {mode}")
+
+
+def test_scene_graph_grown_and_redrawn(ctxs):
+    """Grows the graph between frames (the draw list is rebuilt), then draws
+    over the previous frame without clearing, with the first and then a
+    second template shader."""
+    g, o = ctxs
+    out = []
+    for c in (g, o):
+        s = S.build_scene_graph(c, groups=4, per_group=4, seed=9)
+        s.render()
+        c.scene_insert_node(s.scene, A.SCENE_ROOT, [0, 1], A.make_transform((0.0, -1.0, 2.0), (2.0, 2.0, 2.0)))
+        s.num_nodes += 1
+        s.render(clear=False)
+        s.shader = s.add_shader(A.PROGRAM_LAMBERT_TEX, 2, S.lambert_uniforms(np.eye(4), np.eye(4), [0.0, 1.0, 0.0, 0.0],
+                                                                           [0.3, 0.2, 0.1, 0.0], 0), cull=A.CULL_OFF)
+        s.render(clear=False)
+        out.append(s)
+    assert np.array_equal(out[0].read_models().view(np.uint32), out[1].read_models().view(np.uint32))
+    compare_scenes(out[0], out[1], "scene graph grown and redrawn")
+
+
+def test_scene_graph_rejections(gpu_lib):
+    ctx = gpu_lib.Context()
+    s = S.build_scene_graph(ctx, groups=2, per_group=2)
+    T = A.make_transform
+    with pytest.raises(A.SLError, match="invalid parent"):
+        ctx.scene_insert_node(s.scene, 10 ** 6, [], T())
+    with pytest.raises(A.SLError, match="invalid submesh"):
+        ctx.scene_insert_node(s.scene, A.SCENE_ROOT, [99], T())
+    parent = A.SCENE_ROOT
+    for _ in range(64):
+        parent = ctx.scene_insert_node(s.scene, parent, [], T())
+    with pytest.raises(A.SLError, match="at most 64"):
+        ctx.scene_insert_node(s.scene, parent, [], T())
+    flat = s.add_shader(A.PROGRAM_FLAT_COLOR, 0, S.flat_uniforms(np.eye(4), (1, 1, 1, 1)))
+    with pytest.raises(A.SLError, match="LAMBERT_TEX"):
+        ctx.scene_draw(s.scene, s.fbo, flat, np.eye(4), np.eye(4))
+    ctx.close()
