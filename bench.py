@@ -201,6 +201,64 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def scene_graph_timing(sg, torch, flush, steps, warmup, cpu_seconds):
+    """Scene graph at 2160p: 32 groups x 8 mesh nodes (+ grandchildren and
+    late children; 64x32 spheres, tori, grids; 512^2 textures), three
+    transforms changed per frame, culled against a 40-degree frustum. A frame
+    is clear + transform changes + update + draw list. Device time with CUDA
+    events after an L2 flush; host wall time per frame (the host side of the
+    producer, its per-draw validation included); the oracle port on all host
+    cores for the same frames."""
+    from softlight_gb300 import scenes as S
+    kw = dict(width=3840, height=2160, groups=32, per_group=8, seed=21, tex_size=512, lon=64, lat=32)
+    ctx = sg.Context()
+    s = S.build_scene_graph(ctx, **kw)
+    ctx.set_tile_size(16, 16)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+    for _ in range(max(3, warmup)):
+        s.render()
+    ctx.finish()
+    dev = []
+    for i in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xFF)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        s.render()
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        dev.append(e0.elapsed_time(e1))
+    ctx.finish()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.render()
+    ctx.finish()
+    host_ms = (time.perf_counter() - t0) * 1000.0 / steps
+    draws = len(s.read_models())
+    ctx.close()
+    out = {"workload": "scene graph 32x8 mesh nodes, 3840x2160, 512^2 textures, 64x32 meshes, 40-degree cull frustum",
+           "nodes": draws, "triangles_submitted": s.num_triangles,
+           "device_ms": statistics.median(dev), "frames_per_s": 1000.0 / statistics.median(dev),
+           "wall_ms": host_ms, "wall_frames_per_s": 1000.0 / host_ms, "launches_per_frame": 10}
+    if cpu_seconds > 0:
+        import oracle
+        octx = oracle.Context(num_threads=os.cpu_count() or 1)
+        so = S.build_scene_graph(octx, **kw)
+        so.render()
+        times = []
+        t_end = time.perf_counter() + cpu_seconds
+        while (time.perf_counter() < t_end or len(times) < 2) and len(times) < 20:
+            t1 = time.perf_counter()
+            so.render()
+            times.append(time.perf_counter() - t1)
+        octx.close()
+        out["cpu_baseline"] = {"value": 1.0 / statistics.median(times), "unit": "frames/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": f"{len(times)} full frames"}
+    return out
+
+
 def adjoint_timing(sg, torch, flush, steps, warmup):
     """Differentiable render (512x512, 10k-triangle displaced sphere, vertex
     colours x 256^2 float texture): device time of the forward (clear + exact
@@ -431,6 +489,8 @@ def run_gpu(args):
             line["per_draw"] = per_draw
         if not args.no_adjoint and world == 1:
             line["adjoint"] = adjoint_timing(sg, torch, flush, max(args.steps, 5), args.warmup)
+            line["scene_graph"] = scene_graph_timing(sg, torch, flush, max(args.steps, 5), args.warmup,
+                                                     0 if args.no_cpu_baseline else min(10.0, args.cpu_sample_seconds))
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:
