@@ -52,7 +52,7 @@ struct Fbo
     DevBuffer vis;          /* visibility map, when enabled */
     bool visEnabled = false;
 };
-struct Ubo { DevBuffer buf; uint8_t shadow[1024] = {}; };
+struct Ubo { DevBuffer buf; uint8_t shadow[1024] = {}; uint32_t pending = 0; /* bytes queued for upload */ };
 struct Shader
 {
     uint8_t cull, depthTest, depthMask, blend, numVaryings, numOutputs;
@@ -191,6 +191,18 @@ struct slg_context
     std::vector<Ubo> ubos;
     std::vector<Shader> shaders;
     std::vector<Scene> scenes;
+
+    /* uniform blocks assigned since the last launch, uploaded together
+     * through a ring of pinned staging slots */
+    std::vector<size_t> uboPending;
+    struct UboStage
+    {
+        uint8_t* host = nullptr;
+        size_t cap = 0;
+        cudaEvent_t done = nullptr;
+    } uboStage[4];
+    int uboStageNext = 0;
+    DevBuffer uboStageDev;
 
     /* resource tables visible to device programs */
     DevBuffer texTable, bufTable;
@@ -646,6 +658,63 @@ int bind_attachments(slg_context* ctx, const Fbo& fbo, const Texture& depthTex, 
     return SLG_OK;
 }
 
+/* Uploads the queued uniform blocks: with allocation allowed, one copy of a
+ * packed staging slot and one scatter kernel; otherwise (the no-allocation
+ * draw) one copy per block from its host copy. */
+int flush_ubos(slg_context* ctx, bool allowAlloc)
+{
+    if (ctx->uboPending.empty()) return SLG_OK;
+    cudaError_t e = cudaSuccess;
+    if (!allowAlloc)
+    {
+        for (size_t id : ctx->uboPending)
+        {
+            Ubo& u = ctx->ubos[id];
+            if (e == cudaSuccess) e = cudaMemcpyAsync(u.buf.ptr, u.shadow, u.pending, cudaMemcpyHostToDevice, ctx->stream);
+            u.pending = 0;
+        }
+        ctx->uboPending.clear();
+        return (e == cudaSuccess) ? SLG_OK : ctx->cuda_fail(e, "uniform block upload");
+    }
+    const size_t n = ctx->uboPending.size();
+    const size_t header = (n * sizeof(slg::UboCopy) + 15) & ~(size_t)15;
+    size_t bytes = header;
+    for (size_t id : ctx->uboPending) bytes += (ctx->ubos[id].pending + 15) & ~15u;
+    slg_context::UboStage& st = ctx->uboStage[ctx->uboStageNext];
+    ctx->uboStageNext = (ctx->uboStageNext + 1) % 4;
+    if (st.done) cudaEventSynchronize(st.done);   /* the slot's last copy has read it */
+    else if ((e = cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming)) != cudaSuccess) return ctx->cuda_fail(e, "ubo staging event");
+    if (st.cap < bytes)
+    {
+        if (st.host) cudaFreeHost(st.host);
+        st.host = nullptr;
+        st.cap = 0;
+        const size_t cap = std::max<size_t>(bytes, 64 << 10);
+        if ((e = cudaMallocHost(&st.host, cap)) != cudaSuccess) return ctx->cuda_fail(e, "ubo staging");
+        st.cap = cap;
+    }
+    int r = dev_alloc(ctx, ctx->uboStageDev, std::max<size_t>(bytes, 64 << 10), false);
+    if (r) return r;
+    slg::UboCopy* rec = reinterpret_cast<slg::UboCopy*>(st.host);
+    size_t off = header;
+    for (size_t k = 0; k < n; ++k)
+    {
+        Ubo& u = ctx->ubos[ctx->uboPending[k]];
+        const uint32_t words = (u.pending + 3) / 4;   /* whole words of the 1024-byte block */
+        rec[k].dst = static_cast<uint8_t*>(u.buf.ptr);
+        rec[k].src = (uint32_t)off;
+        rec[k].words = words;
+        std::memcpy(st.host + off, u.shadow, (size_t)words * 4);
+        off += ((size_t)words * 4 + 15) & ~(size_t)15;
+        u.pending = 0;
+    }
+    ctx->uboPending.clear();
+    e = cudaMemcpyAsync(ctx->uboStageDev.ptr, st.host, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(st.done, ctx->stream);
+    if (e == cudaSuccess) e = slg::launch_ubo_scatter(static_cast<const uint8_t*>(ctx->uboStageDev.ptr), (uint32_t)n, ctx->stream);
+    return (e == cudaSuccess) ? SLG_OK : ctx->cuda_fail(e, "uniform block upload");
+}
+
 int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, DrawDesc& d, uint64_t& numSlots)
 {
     const slg_mesh& m = req.mesh;
@@ -780,6 +849,7 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
 
     int r = upload_tables(ctx);
     if (r) return r;
+    if ((r = flush_ubos(ctx, true))) return r;
 
     const Texture& depthTex = ctx->textures[fbo.depth];
     const Texture* colorTex = (fbo.numColors > 0 && fbo.colors[0] != SLG_INVALID_ID) ? &ctx->textures[fbo.colors[0]] : nullptr;
@@ -1141,6 +1211,12 @@ void slg_context_destroy(slg_context* ctx)
     for (Texture& t : ctx->textures) dev_free(t.buf);
     for (Ubo& u : ctx->ubos) dev_free(u.buf);
     for (Fbo& f : ctx->fbos) dev_free(f.vis);
+    for (auto& st : ctx->uboStage)
+    {
+        if (st.host) cudaFreeHost(st.host);
+        if (st.done) cudaEventDestroy(st.done);
+    }
+    dev_free(ctx->uboStageDev);
     for (Scene& sc : ctx->scenes)
     {
         dev_free(sc.dNodes);
@@ -1446,12 +1522,16 @@ size_t slg_create_ubo(slg_context* ctx)
     return ctx->ubos.size() - 1;
 }
 
+/* SL_UniformBuffer contents: the host copy is written now; the device copy
+ * before the next launch that reads uniform blocks (flush_ubos). */
 int slg_ubo_assign(slg_context* ctx, size_t id, const void* data, size_t numBytes)
 {
     if (!id_ok(id, ctx->ubos.size()) || numBytes > 1024 || (!data && numBytes)) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid ubo");
-    std::memcpy(ctx->ubos[id].shadow, data, numBytes);
-    cudaError_t e = cudaMemcpyAsync(ctx->ubos[id].buf.ptr, data, numBytes, cudaMemcpyHostToDevice, ctx->stream);
-    if (e != cudaSuccess) return ctx->cuda_fail(e, "ubo assign");
+    if (!numBytes) return SLG_OK;
+    Ubo& u = ctx->ubos[id];
+    std::memcpy(u.shadow, data, numBytes);
+    if (!u.pending) ctx->uboPending.push_back(id);
+    u.pending = std::max<uint32_t>(u.pending, (uint32_t)numBytes);
     return SLG_OK;
 }
 
@@ -2062,6 +2142,7 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
     f.freeDepthMask = desc->depthMask;
     f.vsBlock = ctx->vsBlock;
 
+    if (flush_ubos(ctx, false)) return SLG_ERR_CUDA;
     e = slg::launch_pipeline(f, ctx->keyCap, ctx->stream, nullptr);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "slg_draw_noalloc: launch");
     return SLG_OK;
@@ -2184,6 +2265,7 @@ int slg_diff_shade(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_t 
     if (!image || ((uintptr_t)image & 15) || count < (size_t)a.width * a.height * 4 || !device_visible(image))
         return ctx->fail(SLG_ERR_INVALID_ARG, "image must be a 16-byte aligned device buffer of width*height*4 floats");
     a.image = reinterpret_cast<float4*>(image);
+    if ((r = flush_ubos(ctx, true))) return r;
     cudaError_t e = slg::launch_diff_shade(a, ctx->stream);
     return (e == cudaSuccess) ? SLG_OK : ctx->cuda_fail(e, "diff shade launch");
 }
@@ -2204,6 +2286,7 @@ int slg_draw_adjoint(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_
     a.dImage = reinterpret_cast<const float4*>(dImage);
     a.dVertices = dVertices;
     a.dTexels = reinterpret_cast<float4*>(dTexels);
+    if ((r = flush_ubos(ctx, true))) return r;
     cudaError_t e = slg::launch_diff_adjoint(a, ctx->stream);
     return (e == cudaSuccess) ? SLG_OK : ctx->cuda_fail(e, "adjoint launch");
 }

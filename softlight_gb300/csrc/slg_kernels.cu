@@ -2771,6 +2771,21 @@ __global__ void __launch_bounds__(128) scene_draw_kernel(const SceneDrawArgs a)
     a.descs[e].hidden = visible ? 0 : 1;
 }
 
+__global__ void __launch_bounds__(64) ubo_scatter_kernel(const uint8_t* stage)
+{
+    const UboCopy c = reinterpret_cast<const UboCopy*>(stage)[blockIdx.x];
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(stage + c.src);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(c.dst);
+    for (uint32_t w = threadIdx.x; w < c.words; w += blockDim.x) dst[w] = src[w];
+}
+
+cudaError_t launch_ubo_scatter(const uint8_t* stage, uint32_t n, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    ubo_scatter_kernel<<<n, 64, 0, s>>>(stage);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_scene_update(const SceneNodeGpu* nodes, const uint32_t* list, uint32_t n, float* model, cudaStream_t s)
 {
     if (n == 0) return cudaSuccess;

@@ -36,6 +36,16 @@ struct BlitArgs
 };
 cudaError_t launch_blit(const BlitArgs& a, cudaStream_t s);
 
+/* Queued uniform-block uploads: a staging area of UboCopy records, then the
+ * blocks' bytes (16-byte aligned); one CTA copies one block. */
+struct UboCopy
+{
+    uint8_t* dst;
+    uint32_t src;      /* byte offset of the block in the staging area */
+    uint32_t words;    /* 4-byte words */
+};
+cudaError_t launch_ubo_scatter(const uint8_t* stage, uint32_t n, cudaStream_t s);
+
 /* Scene graph: the device copy of a node (SL_SceneGraph's mNodeParentIds
  * and mCurrentTransforms, softlight/include/softlight/SL_SceneGraph.hpp:230-260). */
 constexpr int kSceneMaxDepth = 64;    /* nodes on a path from a root, inclusive */

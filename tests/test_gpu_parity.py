@@ -529,3 +529,26 @@ def test_scene_graph_rejections(gpu_lib):
     with pytest.raises(A.SLError, match="LAMBERT_TEX"):
         ctx.scene_draw(s.scene, s.fbo, flat, np.eye(4), np.eye(4))
     ctx.close()
+
+
+def test_uniform_block_reassigned_between_draws(ctxs):
+    """Uniform blocks are uploaded in batches before the next launch: a block
+    assigned twice (the second time partially) before a draw, and between
+    draws of one frame, must draw what the last assignment holds."""
+    g, o = ctxs
+    out = []
+    for c in (g, o):
+        s = S.build_c1(c, width=160, height=120)
+        ubo, ub = s.frame_ubos[0]
+        s.render()
+        moved = bytearray(ub)
+        model = np.eye(4, dtype=np.float32)
+        model[0, 3] = 0.35
+        moved[64:128] = S.col_major(model).tobytes()
+        c.ubo_assign(ubo, bytes(moved))
+        c.ubo_assign(ubo, bytes(ub[:64]))             # vpMatrix only: the moved model matrix stays
+        s.render(clear=False)
+        c.ubo_assign(ubo, bytes(ub))
+        s.render(clear=False)
+        out.append(s)
+    compare_scenes(out[0], out[1], "uniform blocks reassigned")
