@@ -177,11 +177,6 @@ def run_reference(args):
     ctx = oracle.Context(num_threads=threads)
     scene = builder(ctx, **kwargs)
     scale = 1.0
-    if args.workload == "c2":
-        m, n, s = scene.draws[0]
-        k = 128
-        scene.draws = [(m, k, s)]
-        scale = n / k
     for _ in range(args.warmup):
         scene.render()
     t0 = time.perf_counter()
@@ -189,8 +184,7 @@ def run_reference(args):
         scene.render()
     dt = (time.perf_counter() - t0) * scale
     fps = args.steps / dt
-    sample = (f"each step renders {scene.draws[0][1]} of {int(scene.draws[0][1] * scale)} instances; time scaled to the full frame"
-              if scale != 1.0 else "full frames")
+    sample = "full frames, mean over the timed steps"
     line = {"impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / fps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
@@ -467,10 +461,9 @@ def run_gpu(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        frac = (64 / 1024) if args.workload == "c2" else None
-        v, frames, sc = cpu_port_time(builder, kwargs, frac, threads, args.cpu_sample_seconds)
+        v, frames, sc = cpu_port_time(builder, kwargs, None, threads, args.cpu_sample_seconds)
         cpu = {"value": v, "unit": "frames/s", "cores": threads, "kind": "port",
-               "sample": (f"{frames} frames of 64 of 1024 instances, time scaled x{sc:g}" if frac else f"{frames} full frames")}
+               "sample": f"{frames} full frames (median)"}
 
     if rank == 0:
         cfg = dict(cfg)
