@@ -35,10 +35,12 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "sg"])
     p.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-render timing")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    p.add_argument("--ref-seconds", type=float, default=0.0,
+                   help="reference arm: time full frames for about this long (median) instead of --steps")
     p.add_argument("--tile", default="auto", help="screen tile WxH (8x8 .. 64x64) or auto (autotuner)")
     return p.parse_args()
 
@@ -48,6 +50,30 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+SCENE_GRAPH_KW = dict(width=3840, height=2160, groups=32, per_group=8, seed=21, tex_size=512, lon=64, lat=32)
+
+
+def usable_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline_subprocess(workload, seconds):
+    """The oracle port timed in a fresh process (no CUDA context; the GPU
+    process's CPU affinity can be narrower than the host's), through the
+    reference arm bounded to about `seconds` of full frames."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--workload", workload,
+           "--steps", "1", "--warmup", "1", "--ref-seconds", str(seconds)]
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    res = subprocess.run(cmd, capture_output=True, text=True, timeout=600 + 20 * seconds, env=env)
+    if res.returncode != 0:
+        raise RuntimeError(f"cpu baseline failed: {res.stderr[-2000:]}")
+    line = json.loads(res.stdout.strip().splitlines()[-1])
+    return line["cpu_baseline"]
 
 
 def workload_config(name):
@@ -60,6 +86,9 @@ def workload_config(name):
     if name == "c3":
         return S.build_c3, {}, {"workload": "2M-triangle soup, 30% back-facing, 10% near-plane clipped, alpha blend, 2048^2 texture",
                                  "resolution": "1920x1080"}
+    if name == "sg":
+        return S.build_scene_graph, dict(SCENE_GRAPH_KW), {"workload": "scene graph 32x8 mesh nodes, 3840x2160, 512^2 textures, "
+                                                                  "64x32 meshes, 40-degree cull frustum", "resolution": "3840x2160"}
     if name == "c5":
         return S.build_c5, {}, {"workload": "10k-triangle noise-displaced sphere, float32 vertex colours x 256^2 float32 texture, "
                                              "visibility map recorded", "resolution": "512x512"}
@@ -139,33 +168,6 @@ def profiled_traffic(workload, kernel):
     return d.get(workload, {}).get(kernel)
 
 
-def cpu_port_time(builder, kwargs, sample_frac_instances, threads, seconds):
-    """Times the CPU restatement (oracle port) on a bounded sample of the
-    workload; returns (frames/s scaled to the full workload, description)."""
-    import oracle
-    ctx = oracle.Context(num_threads=threads)
-    scene = builder(ctx, **kwargs)
-    full_draws = list(scene.draws)
-    scale = 1.0
-    if sample_frac_instances is not None:
-        m, n, s = full_draws[0]
-        k = max(1, int(n * sample_frac_instances))
-        scene.draws = [(m, k, s)]
-        scale = n / k
-    scene.render()
-    times = []
-    t_end = time.perf_counter() + seconds
-    while time.perf_counter() < t_end or len(times) < 2:
-        t0 = time.perf_counter()
-        scene.render()
-        times.append(time.perf_counter() - t0)
-        if len(times) >= 50:
-            break
-    t = statistics.median(times) * scale
-    ctx.close()
-    return 1.0 / t, len(times), scale
-
-
 def run_reference(args):
     """--impl reference: the reference path's CPU restatement on all host cores."""
     rank, world, _ = dist_env()
@@ -173,18 +175,26 @@ def run_reference(args):
         return
     builder, kwargs, cfg = workload_config(args.workload)
     import oracle
-    threads = os.cpu_count() or 1
+    threads = usable_cores()
     ctx = oracle.Context(num_threads=threads)
     scene = builder(ctx, **kwargs)
-    scale = 1.0
     for _ in range(args.warmup):
         scene.render()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        scene.render()
-    dt = (time.perf_counter() - t0) * scale
-    fps = args.steps / dt
-    sample = "full frames, mean over the timed steps"
+    if args.ref_seconds > 0:
+        times = []
+        t_end = time.perf_counter() + args.ref_seconds
+        while (time.perf_counter() < t_end or len(times) < 2) and len(times) < 50:
+            t0 = time.perf_counter()
+            scene.render()
+            times.append(time.perf_counter() - t0)
+        fps = 1.0 / statistics.median(times)
+        sample = f"{len(times)} full frames, median"
+    else:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            scene.render()
+        fps = args.steps / (time.perf_counter() - t0)
+        sample = "full frames, mean over the timed steps"
     line = {"impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / fps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
@@ -204,7 +214,7 @@ def scene_graph_timing(sg, torch, flush, steps, warmup, cpu_seconds):
     producer, its per-draw validation included); the oracle port on all host
     cores for the same frames."""
     from softlight_gb300 import scenes as S
-    kw = dict(width=3840, height=2160, groups=32, per_group=8, seed=21, tex_size=512, lon=64, lat=32)
+    kw = dict(SCENE_GRAPH_KW)
     ctx = sg.Context()
     s = S.build_scene_graph(ctx, **kw)
     ctx.set_tile_size(16, 16)
@@ -237,19 +247,7 @@ def scene_graph_timing(sg, torch, flush, steps, warmup, cpu_seconds):
            "device_ms": statistics.median(dev), "frames_per_s": 1000.0 / statistics.median(dev),
            "wall_ms": host_ms, "wall_frames_per_s": 1000.0 / host_ms, "launches_per_frame": 10}
     if cpu_seconds > 0:
-        import oracle
-        octx = oracle.Context(num_threads=os.cpu_count() or 1)
-        so = S.build_scene_graph(octx, **kw)
-        so.render()
-        times = []
-        t_end = time.perf_counter() + cpu_seconds
-        while (time.perf_counter() < t_end or len(times) < 2) and len(times) < 20:
-            t1 = time.perf_counter()
-            so.render()
-            times.append(time.perf_counter() - t1)
-        octx.close()
-        out["cpu_baseline"] = {"value": 1.0 / statistics.median(times), "unit": "frames/s", "cores": os.cpu_count() or 1,
-                               "kind": "port", "sample": f"{len(times)} full frames"}
+        out["cpu_baseline"] = cpu_baseline_subprocess("sg", cpu_seconds)
     return out
 
 
@@ -334,6 +332,9 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
+    if args.workload == "sg":
+        raise SystemExit("the scene-graph workload is timed inside the default run (its \"scene_graph\" key); "
+                         "--workload sg is for --impl reference")
     sg.build()
     builder, kwargs, cfg = workload_config(args.workload)
     ctx = sg.Context()
@@ -460,10 +461,7 @@ def run_gpu(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        v, frames, sc = cpu_port_time(builder, kwargs, None, threads, args.cpu_sample_seconds)
-        cpu = {"value": v, "unit": "frames/s", "cores": threads, "kind": "port",
-               "sample": f"{frames} full frames (median)"}
+        cpu = cpu_baseline_subprocess(args.workload, args.cpu_sample_seconds)
 
     if rank == 0:
         cfg = dict(cfg)

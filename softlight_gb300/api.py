@@ -312,9 +312,13 @@ class SLContext:
         return self._id("create_ubo")
 
     def ubo_assign(self, ubo, data):
-        b = bytes(data) if not isinstance(data, np.ndarray) else np.ascontiguousarray(data).tobytes()
-        buf = C.create_string_buffer(b, len(b))
-        self._call("ubo_assign", ubo, C.cast(buf, C.c_void_p), len(b))
+        """data: bytes or a numpy array, passed to the C ABI without a copy."""
+        if isinstance(data, np.ndarray):
+            a = np.ascontiguousarray(data)
+            self._call("ubo_assign", ubo, a.ctypes.data_as(C.c_void_p), a.nbytes)
+        else:
+            b = bytes(data)
+            self._call("ubo_assign", ubo, C.cast(C.c_char_p(b), C.c_void_p), len(b))
 
     def create_shader(self, vs, fs, ubo=INVALID_ID):
         return self._id("create_shader", C.byref(vs), C.byref(fs), ubo)
