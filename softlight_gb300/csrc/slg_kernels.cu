@@ -1053,12 +1053,27 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const Frame f, int numT
     if (tid == 0) sCarry = 0;
     __syncthreads();
 
-    /* 1024 tiles per step: coalesced load, warp-shuffle scan, warp sums */
-    for (int base = 0; base < numTiles; base += 1024)
+    /* 4096 tiles per step: four consecutive tiles per thread (one 16-byte
+     * load where the arrays allow it), warp-shuffle scan of the thread sums,
+     * warp sums scanned by warp 0 */
+    const bool vec = ((reinterpret_cast<uintptr_t>(f.tileCount) | reinterpret_cast<uintptr_t>(f.tileOffset) |
+                       reinterpret_cast<uintptr_t>(f.tileCursor)) & 15u) == 0;
+    for (int base = 0; base < numTiles; base += 4096)
     {
-        const int t = base + tid;
-        const uint32_t c = (t < numTiles) ? f.tileCount[t] : 0u;
-        uint32_t v = c;
+        const int t0 = base + 4 * tid;
+        uint32_t c[4];
+        if (vec && t0 + 3 < numTiles)
+        {
+            const uint4 q = *reinterpret_cast<const uint4*>(f.tileCount + t0);
+            c[0] = q.x; c[1] = q.y; c[2] = q.z; c[3] = q.w;
+        }
+        else
+        {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) c[k] = (t0 + k < numTiles) ? f.tileCount[t0 + k] : 0u;
+        }
+        const uint32_t p1 = c[0], p2 = p1 + c[1], p3 = p2 + c[2], sum = p3 + c[3];
+        uint32_t v = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1)
         {
@@ -1080,12 +1095,27 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const Frame f, int numT
         }
         __syncthreads();
         const uint32_t carry = sCarry;
-        const uint32_t excl = carry + (warp ? sWarp[warp - 1] : 0u) + v - c;
-        if (t < numTiles)
+        const uint32_t excl = carry + (warp ? sWarp[warp - 1] : 0u) + v - sum;
+        const uint32_t off[4] = {excl, excl + p1, excl + p2, excl + p3};
+        if (vec && t0 + 3 < numTiles)
         {
-            f.tileOffset[t] = excl;
-            f.tileCursor[t] = excl;
-            f.tileCount[t] = 0;
+            const uint4 o4 = make_uint4(off[0], off[1], off[2], off[3]);
+            *reinterpret_cast<uint4*>(f.tileOffset + t0) = o4;
+            *reinterpret_cast<uint4*>(f.tileCursor + t0) = o4;
+            *reinterpret_cast<uint4*>(f.tileCount + t0) = make_uint4(0u, 0u, 0u, 0u);
+        }
+        else
+        {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+            {
+                if (t0 + k < numTiles)
+                {
+                    f.tileOffset[t0 + k] = off[k];
+                    f.tileCursor[t0 + k] = off[k];
+                    f.tileCount[t0 + k] = 0;
+                }
+            }
         }
         __syncthreads();
         if (tid == 1023) sCarry = carry + sWarp[31];
