@@ -2925,7 +2925,7 @@ cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEven
         if (f.hasLines || f.hasWire) vs_setup_kernel<true, false><<<blocks, vsBlock, 0, s>>>(f);
         else if (f.allCached) vs_setup_kernel<false, true><<<blocks, vsBlock, 0, s>>>(f);
         else vs_setup_kernel<false, false><<<blocks, vsBlock, 0, s>>>(f);
-        clip_kernel<<<152 * 4, 128, 0, s>>>(f);
+        clip_kernel<<<152 * 6, 128, 0, s>>>(f);   /* 80 registers: six CTAs per SM */
     }
     if (ev) cudaEventRecord(ev[1], s);
     tile_scan_kernel<<<1, 1024, 0, s>>>(f, numTiles);
