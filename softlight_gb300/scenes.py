@@ -7,7 +7,7 @@ inputs are synthetic: procedural meshes (UV spheres, tori, grids, triangle
 soup), procedural textures (checker, value noise) and matrices computed in
 float64 and stored as float32.
 
-Configurations (BASELINE workloads):
+Configurations (the benchmark workloads C1-C5):
   c1  one 64x32 UV sphere (4096 tris), 256^2 RGBA8 checker, Lambert, 640x480
   c2  the sphere x1024 instances, 1024^2 noise texture, Blinn-Phong 4 lights, 1920x1080
   c3  2M-triangle soup, 30% back-facing, 10% crossing the near plane, alpha blend, 1920x1080

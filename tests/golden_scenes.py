@@ -1,5 +1,5 @@
 """Workloads with golden fixtures (tests/golden/*.npz): reduced-size versions
-of the BASELINE configurations plus the edge-case scenes, small enough that
+of the benchmark configurations plus the edge-case scenes, small enough that
 the fixtures stay a few hundred KB and the CPU oracle renders each in well
 under a second."""
 import numpy as np
