@@ -316,10 +316,18 @@ def adjoint_timing(sg, torch, flush, steps, warmup):
 
 def launches_per_frame(scene):
     """Kernels one frame launches: two clears, then vs_setup, clip, tile_scan,
-    bin_fill and raster per launch, plus tile_sort on the ordered path."""
+    bin_fill and raster per launch, plus tile_sort on the ordered path and
+    the vertex cache for launches of 64K or more indexed triangles."""
+    from softlight_gb300 import api as A
     per_launch = 5 + (1 if scene.blending else 0)
-    launches = 1 if scene.batched else len(scene.draws)
-    return 2 + per_launch * launches
+    indexed = any(m.mode == A.RENDER_MODE_INDEXED_TRIANGLES for (m, _, _) in scene.draws)
+    if scene.batched:
+        return 2 + per_launch + (1 if indexed and scene.num_triangles >= 65536 else 0)
+    total = 2
+    for (m, n, _) in scene.draws:
+        tris = n * (m.elementEnd - m.elementBegin) // 3
+        total += per_launch + (1 if m.mode == A.RENDER_MODE_INDEXED_TRIANGLES and tris >= 65536 else 0)
+    return total
 
 
 def run_gpu(args):
