@@ -60,13 +60,20 @@ def test_gpu_blits_match_reference_golden(gpu_lib):
         assert same, f"blit {name} differs from the reference"
 
 
-def test_gpu_scene_graph_matches_reference_golden(gpu_lib):
+@pytest.mark.parametrize("mode,tile", [(0, (16, 16)), (1, (32, 32)), (0, (8, 8))])
+def test_gpu_scene_graph_matches_reference_golden(gpu_lib, mode, tile):
     """SL_SceneGraph::update and the mesh-node traversal on the GPU (update
     kernel, draw-list kernel, one batched launch per frame): model matrices,
     colour and depth bit for bit against the reference's three frames
-    (tests/golden/scene_graph.npz)."""
+    (tests/golden/scene_graph.npz), in three raster configurations."""
     want = np.load(os.path.join(GOLDEN, "scene_graph.npz"))
-    got = G.scene_graph_cases(gpu_lib.Context)
+
+    def make_ctx():
+        c = gpu_lib.Context()
+        c.set_raster_mode(mode)
+        c.set_tile_size(*tile)
+        return c
+    got = G.scene_graph_cases(make_ctx)
     assert set(got) == set(want.files)
     for name in want.files:
         a, b = got[name], want[name]
