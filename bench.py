@@ -55,6 +55,24 @@ def dist_env():
 SCENE_GRAPH_KW = dict(width=3840, height=2160, groups=32, per_group=8, seed=21, tex_size=512, lon=64, lat=32)
 
 
+def max_over_ranks(value, world, device="cuda"):
+    """The largest of a per-rank float over the process group (the slowest
+    replica's time); the value itself on one rank."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, steps, seconds):
+    """Whole-job frames/s of `world` replicas that each drew `steps` frames,
+    timed by the slowest one."""
+    return world * steps / seconds
+
+
 def usable_cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -392,12 +410,8 @@ def run_gpu(args):
         step_ms, _ = timed_frames(args.steps, False)
         _, stage_ms = timed_frames(max(3, min(args.steps, 10)), True)
     torch.cuda.synchronize()
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    fps = world * args.steps / (total_ms / 1000.0)
+    total_ms = max_over_ranks(sum(step_ms), world)
+    fps = replica_throughput(world, args.steps, total_ms / 1000.0)
 
     per_draw = None
     if scene.batched:
@@ -442,12 +456,8 @@ def run_gpu(args):
             ctx.vbo_assign(inst[0], inst_host)
         scene.render()
         read_color()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_fps = world * args.steps / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_fps = replica_throughput(world, args.steps, e2e_s)
 
     # roofline of the dominant kernel
     stages = np.asarray(stage_ms)
