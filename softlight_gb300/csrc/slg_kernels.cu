@@ -2144,13 +2144,18 @@ template <int TW, int TH>
 struct FreeLayout
 {
     static constexpr int kPix = TW * TH;
+    /* records staged per step: 64 for tiles of at most 64 pixels (half the
+     * shared memory, so more CTAs fit an SM), else kFreeBatch */
+    static constexpr int kBatch = (TW * TH <= 64) ? 64 : kFreeBatch;
+    /* resident CTAs the launch bounds ask for */
+    static constexpr int kMinBlocks = (TW * TH <= 64) ? 12 : 4;
     static constexpr size_t kRecOff = 0;                                                   /* float4 [batch][8] */
-    static constexpr size_t kBOff = kRecOff + sizeof(float4) * kFreeBatch * kRecordVec4;    /* float4 (b0, b1, b2, z) per pixel */
+    static constexpr size_t kBOff = kRecOff + sizeof(float4) * kBatch * kRecordVec4;        /* float4 (b0, b1, b2, z) per pixel */
     static constexpr size_t kBestOff = kBOff + sizeof(float4) * kPix;                      /* u64 per pixel */
     static constexpr size_t kD0Off = kBestOff + sizeof(unsigned long long) * kPix;         /* pre-launch depth per pixel */
     static constexpr size_t kKeyOff = kD0Off + sizeof(float) * kPix;                       /* u32 per staged record */
-    static constexpr size_t kPreOff = kKeyOff + sizeof(uint32_t) * kFreeBatch;             /* u32 [batch + 1] row prefix */
-    static constexpr size_t kWarpOff = kPreOff + sizeof(uint32_t) * (kFreeBatch + 4);      /* u32 per warp */
+    static constexpr size_t kPreOff = kKeyOff + sizeof(uint32_t) * kBatch;                 /* u32 [threads + 1] row prefix */
+    static constexpr size_t kWarpOff = kPreOff + sizeof(uint32_t) * (kFreeThreads + 4);    /* u32 per warp */
     static constexpr size_t bytes() { return kWarpOff + sizeof(uint32_t) * (kFreeThreads / 32); }
 };
 
@@ -2324,7 +2329,7 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
 }
 
 template <int TW, int TH, class Color, bool kGeneral>
-__global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Frame f, int depthFunc, int depthMask)
+__global__ void __launch_bounds__(kFreeThreads, kGeneral ? 4 : FreeLayout<TW, TH>::kMinBlocks) raster_free_kernel(const Frame f, int depthFunc, int depthMask)
 {
     typedef FreeLayout<TW, TH> L;
     extern __shared__ __align__(16) uint8_t smem[];
@@ -2357,11 +2362,11 @@ __global__ void __launch_bounds__(kFreeThreads, 4) raster_free_kernel(const Fram
         sD0[i] = (x < xLimit && y < yLimit) ? depth_load(f, (size_t)x + (size_t)f.width * y) : 0.f;
     }
 
-    for (uint32_t b0 = 0; b0 < n; b0 += kFreeBatch)
+    for (uint32_t b0 = 0; b0 < n; b0 += L::kBatch)
     {
-        const int cnt = (int)min((uint32_t)kFreeBatch, n - b0);
+        const int cnt = (int)min((uint32_t)L::kBatch, n - b0);
         __syncthreads();
-        stage_records<kFreeBatch>(f, f.entries + begin + b0, cnt, sRec, sKey);
+        stage_records<L::kBatch>(f, f.entries + begin + b0, cnt, sRec, sKey);
         __syncthreads();
 
         /* rows of each staged record inside the tile, prefix-summed */
