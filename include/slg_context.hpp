@@ -106,6 +106,48 @@ class UniformBufferRef
     size_t mId;
 };
 
+/* SL_SceneGraph (softlight/include/softlight/SL_SceneGraph.hpp:215):
+ * insert_mesh / insert_empty_node / insert_mesh_node, a node's current
+ * transform, update(), mModelMatrices, and the draw list of the mesh nodes
+ * (the traversal SoftLight's demos write by hand). Insertion calls return
+ * SLG_INVALID_ID on error. */
+class SceneGraphRef
+{
+  public:
+    SceneGraphRef(slg_context* c, size_t id) noexcept : mCtx(c), mId(id) {}
+    size_t insert_mesh(const slg_mesh& m, const float maxPoint[3], const float minPoint[3]) noexcept
+    {
+        size_t out = SLG_INVALID_ID;
+        return slg_scene_insert_mesh(mCtx, mId, &m, maxPoint, minPoint, &out) ? SLG_INVALID_ID : out;
+    }
+    size_t insert_material(size_t ambientTextureId) noexcept
+    {
+        size_t out = SLG_INVALID_ID;
+        return slg_scene_insert_material(mCtx, mId, ambientTextureId, &out) ? SLG_INVALID_ID : out;
+    }
+    size_t insert_empty_node(size_t parentId, const slg_transform& t) noexcept
+    {
+        size_t out = SLG_INVALID_ID;
+        return slg_scene_insert_node(mCtx, mId, parentId, 0, nullptr, &t, &out) ? SLG_INVALID_ID : out;
+    }
+    size_t insert_mesh_node(size_t parentId, size_t numSubMeshes, const size_t* subMeshIds, const slg_transform& t) noexcept
+    {
+        size_t out = SLG_INVALID_ID;
+        return slg_scene_insert_node(mCtx, mId, parentId, numSubMeshes, subMeshIds, &t, &out) ? SLG_INVALID_ID : out;
+    }
+    int transform(size_t nodeId, const slg_transform& t) noexcept { return slg_scene_set_transform(mCtx, mId, nodeId, &t); }
+    int update() noexcept { return slg_scene_update(mCtx, mId); }
+    int model_matrices(float* out, size_t numNodes) noexcept { return slg_scene_read_models(mCtx, mId, out, numNodes); }
+    int draw(size_t fboId, size_t shaderId, const float projection[16], const float view[16],
+             const float cullProjection[16] = nullptr) noexcept
+    {
+        return slg_scene_draw(mCtx, mId, fboId, shaderId, projection, view, cullProjection);
+    }
+  private:
+    slg_context* mCtx;
+    size_t mId;
+};
+
 class Context
 {
   public:
@@ -135,6 +177,8 @@ class Context
     TextureRef texture(size_t id) noexcept { return TextureRef(mCtx, id); }
     FramebufferRef framebuffer(size_t id) noexcept { return FramebufferRef(mCtx, id); }
     UniformBufferRef ubo(size_t id) noexcept { return UniformBufferRef(mCtx, id); }
+    size_t create_scene() noexcept { return slg_create_scene(mCtx); }
+    SceneGraphRef scene(size_t id) noexcept { return SceneGraphRef(mCtx, id); }
 
     /* SL_Context::draw / draw_multiple / draw_instanced: void and noexcept as
      * in the reference; a failure is recorded for finish() / last_error(). */

@@ -10,12 +10,12 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def build_cpp(tmp_path):
+def build_cpp(tmp_path, name="draw_test"):
     import softlight_gb300 as sg
     lib = sg.build()
-    exe = str(tmp_path / "draw_test")
+    exe = str(tmp_path / name)
     cmd = ["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"),
-           os.path.join(ROOT, "tests", "cpp", "draw_test.cpp"), "-o", exe,
+           os.path.join(ROOT, "tests", "cpp", name + ".cpp"), "-o", exe,
            "-L", os.path.dirname(lib), "-lslg", f"-Wl,-rpath,{os.path.dirname(lib)}"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
@@ -24,6 +24,16 @@ def build_cpp(tmp_path):
 
 def test_cpp_facade_compiles_and_links(tmp_path):
     assert os.path.exists(build_cpp(tmp_path))
+    assert os.path.exists(build_cpp(tmp_path, "scene_test"))
+
+
+@pytest.mark.gpu
+def test_cpp_scene_graph_facade(tmp_path):
+    """SL_SceneGraph-shaped calls from C++: exact model matrices of a
+    two-level graph and a drawn draw list."""
+    exe = build_cpp(tmp_path, "scene_test")
+    res = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0, (res.returncode, res.stdout, res.stderr)
 
 
 @pytest.mark.gpu
