@@ -2144,9 +2144,9 @@ template <int TW, int TH>
 struct FreeLayout
 {
     static constexpr int kPix = TW * TH;
-    /* records staged per step: 64 for tiles of at most 64 pixels (half the
-     * shared memory, so more CTAs fit an SM), else kFreeBatch */
-    static constexpr int kBatch = (TW * TH <= 64) ? 64 : kFreeBatch;
+    /* records staged per step: 96 for tiles of at most 64 pixels (less
+     * shared memory, so 12 CTAs fit an SM), else kFreeBatch */
+    static constexpr int kBatch = (TW * TH <= 64) ? 96 : kFreeBatch;
     /* resident CTAs the launch bounds ask for */
     static constexpr int kMinBlocks = (TW * TH <= 64) ? 12 : 4;
     static constexpr size_t kRecOff = 0;                                                   /* float4 [batch][8] */
