@@ -2156,7 +2156,9 @@ struct FreeLayout
     static constexpr size_t kKeyOff = kD0Off + sizeof(float) * kPix;                       /* u32 per staged record */
     static constexpr size_t kPreOff = kKeyOff + sizeof(uint32_t) * kBatch;                 /* u32 [threads + 1] row prefix */
     static constexpr size_t kWarpOff = kPreOff + sizeof(uint32_t) * (kFreeThreads + 4);    /* u32 per warp */
-    static constexpr size_t bytes() { return kWarpOff + sizeof(uint32_t) * (kFreeThreads / 32); }
+    static constexpr size_t kWonOff = kWarpOff + sizeof(uint32_t) * (kFreeThreads / 32);           /* u32 bit per scan-line task */
+    static constexpr int kWonWords = (kBatch * TH + 31) / 32; /* a staged record has at most TH rows in the tile */
+    static constexpr size_t bytes() { return kWonOff + sizeof(uint32_t) * kWonWords; }
 };
 
 /* Total order of depths as unsigned words (-0 and +0 equal, as they compare). */
@@ -2187,11 +2189,31 @@ __device__ __forceinline__ unsigned long long free_pack(int func, bool mask, flo
 template <int TW, int TH, bool kStore, bool kGeneral>
 __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sKey, const uint32_t* sPre, int cnt, int x0, int y0,
                                           int xLimit, int width, int height, int func, bool mask, const float* sD0,
-                                          unsigned long long* sBest, float4* sB)
+                                          unsigned long long* sBest, float4* sB, uint32_t* sWon)
 {
     const uint32_t total = sPre[cnt];
     for (uint32_t i = threadIdx.x; i < total; i += kFreeThreads)
     {
+        if (kStore && !((sWon[i >> 5] >> (i & 31)) & 1u))
+        {
+            continue;
+        }
+        /* sBest only decreases and packed values are unique per pixel, so a
+         * fragment not below the value read here can never be its pixel's
+         * final best: it is dropped, and only tasks with a fragment that
+         * passed are walked again by the store pass */
+        bool marked = false;
+        auto fold = [&](int idx, unsigned long long p) {
+            if (p < *reinterpret_cast<volatile unsigned long long*>(sBest + idx))
+            {
+                atomicMin(sBest + idx, p);
+                if (!marked)
+                {
+                    marked = true;
+                    atomicOr(sWon + (i >> 5), 1u << (i & 31));
+                }
+            }
+        };
         int lo = 0, hi = cnt;
         while (hi - lo > 1)
         {
@@ -2232,7 +2254,7 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
                 }
                 else
                 {
-                    atomicMin(sBest + idx, p);
+                    fold(idx, p);
                 }
             }
             continue;
@@ -2264,7 +2286,7 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
                     }
                     else
                     {
-                        atomicMin(sBest + idx, p);
+                        fold(idx, p);
                     }
                 }
             }
@@ -2286,7 +2308,7 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
             }
             else
             {
-                atomicMin(sBest + idx, p);
+                fold(idx, p);
             }
             continue;
         }
@@ -2321,7 +2343,7 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
                 }
                 else
                 {
-                    atomicMin(sBest + idx, p);
+                    fold(idx, p);
                 }
             }
         }
@@ -2340,6 +2362,7 @@ __global__ void __launch_bounds__(kFreeThreads, kGeneral ? 4 : FreeLayout<TW, TH
     uint32_t* sKey = reinterpret_cast<uint32_t*>(smem + L::kKeyOff);
     uint32_t* sPre = reinterpret_cast<uint32_t*>(smem + L::kPreOff);
     uint32_t* sWarp = reinterpret_cast<uint32_t*>(smem + L::kWarpOff);
+    uint32_t* sWon = reinterpret_cast<uint32_t*>(smem + L::kWonOff);
 
     const int tile = blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
@@ -2390,11 +2413,12 @@ __global__ void __launch_bounds__(kFreeThreads, kGeneral ? 4 : FreeLayout<TW, TH
         for (int w = 0; w < warp; ++w) incl += sWarp[w];
         sPre[threadIdx.x + 1] = incl;
         if (threadIdx.x == 0) sPre[0] = 0u;
+        for (int w = threadIdx.x; w < L::kWonWords; w += kFreeThreads) sWon[w] = 0u;
         __syncthreads();
 
-        free_walk<TW, TH, false, kGeneral>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB);
+        free_walk<TW, TH, false, kGeneral>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB, sWon);
         __syncthreads();
-        free_walk<TW, TH, true, kGeneral>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB);
+        free_walk<TW, TH, true, kGeneral>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB, sWon);
     }
     __syncthreads();
 
