@@ -287,9 +287,12 @@ int slg_draw_multiple(slg_context* ctx, const slg_mesh* meshes, size_t numMeshes
  * callers that must not allocate mid-frame (a fixed device-memory budget, a
  * thread that must not meet cudaMalloc's implicit device synchronisation, an
  * allocator hook that forbids new allocations) use this variant, whose
- * scratch is one file-scope device array of about 4.3 MiB sized for the
+ * scratch is one file-scope device array of about 4.8 MiB sized for the
  * worst case of the limits below. Same arguments, results and errors as
- * slg_draw, plus:
+ * slg_draw (device-side conditions such as a blended wireframe revisit after
+ * 600 queued fragments are reported at slg_finish through the context's own
+ * status words; a framebuffer with a visibility map gets the same checks and
+ * the map is written), plus:
  *  - limits: at most SLG_NOALLOC_MAX_TRIANGLES triangles per call and a
  *    framebuffer of at most SLG_NOALLOC_MAX_TILES tiles of the context's tile
  *    size (256x256 pixels at the default 32x32); larger draws are rejected

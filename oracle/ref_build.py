@@ -19,6 +19,12 @@ OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libslref.so")
 REF = os.environ.get("SOFTLIGHT_REF", "/root/reference/softlight")
 
+
+def available():
+    """Whether the reference tree this recipe compiles is present (it is not
+    on machines that only run the tests and the benchmark)."""
+    return os.path.isdir(REF)
+
 SOURCES = [
     "SL_BlitCompressedProcessor.cpp", "SL_BlitProcessor.cpp", "SL_ClearProcessor.cpp", "SL_Color.cpp",
     "SL_Context.cpp", "SL_FragmentProcessor.cpp", "SL_Framebuffer.cpp", "SL_Geometry.cpp",

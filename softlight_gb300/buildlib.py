@@ -49,7 +49,8 @@ def build(verbose=False, force=False):
     """Compile the CUDA sources and link libslg.so; returns its path."""
     os.makedirs(BUILD, exist_ok=True)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    deps += [os.path.join(HERE, "..", "include", f) for f in ("slg.h", "slg_programs.h")]
+    inc = os.path.join(HERE, "..", "include")
+    deps += [os.path.join(inc, f) for f in os.listdir(inc)]
     if not force and os.path.exists(LIB):
         newest = max(os.path.getmtime(d) for d in deps if os.path.exists(d))
         if os.path.getmtime(LIB) >= newest and os.path.getmtime(LIB) >= os.path.getmtime(__file__):

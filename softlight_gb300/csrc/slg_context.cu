@@ -334,7 +334,6 @@ int ensure_scratch(slg_context* ctx, uint64_t numSlots, uint64_t numTiles)
         if ((r = dev_alloc(ctx, ctx->clipCount, sizeof(uint32_t), true))) return r;
         if ((r = dev_alloc(ctx, ctx->aliasEvents, kAliasCap * sizeof(slg::AliasEvent), false))) return r;
         if ((r = dev_alloc(ctx, ctx->aliasCount, sizeof(uint32_t), true))) return r;
-        if ((r = dev_alloc(ctx, ctx->status, 4 * sizeof(int32_t), true))) return r;
     }
     if (numTiles > ctx->tileCap)
     {
@@ -655,6 +654,25 @@ int bind_attachments(slg_context* ctx, const Fbo& fbo, const Texture& depthTex, 
             return ctx->fail(SLG_ERR_INVALID_ARG, "the fragment program writes more outputs than the framebuffer has colour attachments");
         if (f.numColors > 1 && descs[i].numOutputs > 1) f.hasMrt = 1;
     }
+    return SLG_OK;
+}
+
+/* The framebuffer's visibility map (slg_fbo_enable_visibility) into the
+ * frame, after the checks that keep it exact: the order-free raster writes
+ * it, so the launch must be order-free, of filled triangles or points, into
+ * an R_FLOAT depth attachment. */
+int bind_visibility(slg_context* ctx, const Fbo& fbo, Frame& f)
+{
+    if (!fbo.visEnabled) return SLG_OK;
+    if (f.depthType != SLG_COLOR_R_FLOAT)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map needs an R_FLOAT depth attachment");
+    if (f.hasLines || f.hasWire)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map takes filled triangle and point draws only");
+    if (!f.orderFree)
+        return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map takes opaque draws only (no blending, one depth rule)");
+    if (fbo.vis.bytes < (size_t)f.width * f.height * sizeof(uint32_t))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "visibility map is smaller than the framebuffer (enable it again after resizing)");
+    f.ids = static_cast<uint32_t*>(fbo.vis.ptr);
     return SLG_OK;
 }
 
@@ -983,18 +1001,7 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
 
     f.vsBlock = ctx->vsBlock;
 
-    if (fbo.visEnabled)
-    {
-        if (f.depthType != SLG_COLOR_R_FLOAT)
-            return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map needs an R_FLOAT depth attachment");
-        if (f.hasLines || f.hasWire)
-            return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map takes filled triangle and point draws only");
-        if (!f.orderFree)
-            return ctx->fail(SLG_ERR_INVALID_ARG, "a framebuffer with a visibility map takes opaque draws only (no blending, one depth rule)");
-        if (fbo.vis.bytes < (size_t)f.width * f.height * sizeof(uint32_t))
-            return ctx->fail(SLG_ERR_INVALID_ARG, "visibility map is smaller than the framebuffer (enable it again after resizing)");
-        f.ids = static_cast<uint32_t*>(fbo.vis.ptr);
-    }
+    if ((r = bind_visibility(ctx, fbo, f))) return r;
 
     if (batch && ctx->batchGraphs && !ctx->profileStages && !hook)
     {
@@ -1189,6 +1196,11 @@ int slg_context_create(slg_context** outCtx)
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->hostStatus, 4 * sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->devDescs.ptr, kDescRing * sizeof(DrawDesc));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->devStarts.ptr, kDescRing * sizeof(uint64_t));
+    /* the device status words (overflow bits and sizes), read and cleared by
+     * check_status; every launch of the context reports into them, the
+     * no-allocation draw included */
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->status.ptr, 4 * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMemset(ctx->status.ptr, 0, 4 * sizeof(int32_t));
     for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->stageEvents[i]);
     if (e == cudaSuccess) e = slg::init_kernel_attributes(ctx->keyCap);
     if (e != cudaSuccess)
@@ -1198,6 +1210,7 @@ int slg_context_create(slg_context** outCtx)
     }
     ctx->devDescs.bytes = kDescRing * sizeof(DrawDesc);
     ctx->devStarts.bytes = kDescRing * sizeof(uint64_t);
+    ctx->status.bytes = 4 * sizeof(int32_t);
     *outCtx = ctx;
     return SLG_OK;
 }
@@ -1964,8 +1977,10 @@ constexpr size_t kNoAllocTextures = 256, kNoAllocBuffers = 256;
 constexpr size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
 
 /* layout of the static scratch; the first kNoAllocZeroBytes must be zero
- * when the pipeline starts: ovfCount (+0), clipCount (+4), aliasCount (+8),
- * the status words (+16..+31) and the per-tile triangle counters (+256) */
+ * when the pipeline starts: ovfCount (+0), clipCount (+4), aliasCount (+8)
+ * and the per-tile triangle counters (+256). The status words are the
+ * context's own (allocated when the context is created), so errors of a
+ * no-allocation draw are reported at slg_finish like those of slg_draw. */
 constexpr size_t kOffCounters = 0;
 constexpr size_t kOffTileCount = 256;
 constexpr size_t kNoAllocZeroBytes = kOffTileCount + align256(kNoAllocTiles * sizeof(uint32_t));
@@ -1979,10 +1994,11 @@ constexpr size_t kOffBufTable = kOffTexTable + align256(kNoAllocTextures * sizeo
 constexpr size_t kOffRecords = kOffBufTable + align256(kNoAllocBuffers * sizeof(void*));
 constexpr size_t kOffVaryings = kOffRecords + align256(kNoAllocRecords * slg::kRecordVec4 * sizeof(float4));
 constexpr size_t kOffEntries = kOffVaryings + align256(kNoAllocRecords * slg::kVaryingVec4 * sizeof(float4));
-constexpr uint32_t kNoAllocAliases = 64;
+constexpr uint32_t kNoAllocAliases = kAliasCap;   /* as slg_draw: 4096 full-width line aliases */
 constexpr size_t kOffAliases = kOffEntries + align256(kNoAllocEntries * sizeof(uint32_t));
 constexpr size_t kNoAllocBytes = kOffAliases + align256(kNoAllocAliases * sizeof(slg::AliasEvent));
 static_assert(kNoAllocBytes < (8u << 20), "static draw scratch stays under 8 MiB");
+static_assert(kNoAllocZeroBytes % 4 == 0, "counters are cleared in whole words");
 
 static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocBytes];
 
@@ -2060,6 +2076,12 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
         return ctx->fail(SLG_ERR_INVALID_ARG, "slg_draw_noalloc: a " + std::to_string(f.width) + "x" + std::to_string(f.height) +
                                                   " framebuffer is " + std::to_string(numTiles) + " tiles of " + std::to_string(f.tileW) + "x" +
                                                   std::to_string(f.tileH) + ", over the static limit of " + std::to_string(kNoAllocTiles));
+    f.depthType = depthTex.type;
+    f.orderFree = (desc->blend == SLG_BLEND_OFF && desc->depthTest != SLG_DEPTH_TEST_NOT_EQUAL && !ctx->forceOrdered &&
+                   f.depthType != SLG_COLOR_R_HALF) ? 1 : 0;
+    f.freeDepthFunc = desc->depthTest;
+    f.freeDepthMask = desc->depthMask;
+    if ((r = bind_visibility(ctx, fbo, f))) return r;
     if (desc->prim == slg::kPrimLine)
     {
         if (std::max(f.width, f.height) > kMaxLineExtent)
@@ -2124,7 +2146,7 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
     f.slotOvf = reinterpret_cast<uint32_t*>(scratch + kOffSlotOvf);
     f.ovfCount = reinterpret_cast<uint32_t*>(scratch + kOffCounters);
     f.clipCount = reinterpret_cast<uint32_t*>(scratch + kOffCounters + 4);
-    f.status = reinterpret_cast<int32_t*>(scratch + kOffCounters + 16);
+    f.status = static_cast<int32_t*>(ctx->status.ptr);
     f.clipQueue = reinterpret_cast<uint32_t*>(scratch + kOffClipQueue);
     f.ovfCap = (uint32_t)kNoAllocOvf;
     f.numSlots = numSlots;
@@ -2136,10 +2158,6 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
     f.draws = devDesc;
     f.drawSlotStart = devStarts;
     f.numDraws = 1;
-    f.orderFree = (desc->blend == SLG_BLEND_OFF && desc->depthTest != SLG_DEPTH_TEST_NOT_EQUAL && !ctx->forceOrdered &&
-                   f.depthType != SLG_COLOR_R_HALF) ? 1 : 0;
-    f.freeDepthFunc = desc->depthTest;
-    f.freeDepthMask = desc->depthMask;
     f.vsBlock = ctx->vsBlock;
 
     if (flush_ubos(ctx, false)) return SLG_ERR_CUDA;

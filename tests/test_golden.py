@@ -13,7 +13,17 @@ from golden.make_golden import digest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
-REF_TREE = "/root/reference/softlight"
+
+
+def _reference_available():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("ref_build", os.path.join(os.path.dirname(HERE), "oracle", "ref_build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.available()
+
+
+REFERENCE_PRESENT = _reference_available()
 
 
 def load(name):
@@ -107,7 +117,7 @@ def test_oracle_scene_graph_rejections(oracle_mod):
     ctx.close()
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_TREE), reason="reference tree not present")
+@pytest.mark.skipif(not REFERENCE_PRESENT, reason="reference tree not present")
 def test_reference_scene_graph_matches_oracle_live(oracle_mod):
     """The reference's SL_SceneGraph, SL_Transform and sl_is_visible, built
     from its sources, against the oracle on a larger graph over four frames."""
@@ -144,7 +154,7 @@ def test_oracle_threads_match_one_thread(oracle_mod, threads):
     assert same(a.read_depth(), b.read_depth())
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_TREE), reason="reference tree not present")
+@pytest.mark.skipif(not REFERENCE_PRESENT, reason="reference tree not present")
 @pytest.mark.parametrize("name", ["c1_sphere_160x120", "c3_soup_2000_160x96", "multi_draw", "soup_not_equal",
                                   "lines_persp_clip_cull", "line_alias"])
 def test_reference_build_matches_oracle_live(oracle_mod, name):
