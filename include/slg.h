@@ -140,7 +140,10 @@ enum slg_shader_program
     SLG_PROGRAM_VCOLOR_TEX_ALPHA   = 3, /* vertex colour x RGBA8 texture, vertex alpha */
     SLG_PROGRAM_VCOLOR_TEXF        = 4, /* vertex colour x RGBA float texture */
     SLG_PROGRAM_FLAT_COLOR         = 5, /* uniform colour, no varyings */
-    SLG_PROGRAM_GBUFFER            = 6  /* up to four outputs for multiple render targets (vertex-colour layout) */
+    SLG_PROGRAM_GBUFFER            = 6, /* up to four outputs for multiple render targets (vertex-colour layout) */
+    SLG_PROGRAM_VCOLOR_TEX_CUTOUT  = 7, /* vertex colour x RGBA8 texture with an alpha test: discards below alphaRef */
+    SLG_PROGRAM_FRAG_COORD         = 8, /* fragment position and depth as colour; screen-door discard; writes depth */
+    SLG_PROGRAM_USER_FIRST         = 256 /* ids from here on name programs registered with slg_register_programs */
 };
 
 /* SL_Mesh (softlight/include/softlight/SL_Mesh.hpp:30-39), same layout */
@@ -257,6 +260,50 @@ int    slg_ubo_assign(slg_context* ctx, size_t uboId, const void* data, size_t n
  * validation, SLG_INVALID_ID where the reference returns (size_t)-1. */
 size_t slg_create_shader(slg_context* ctx, const slg_vertex_shader* vs,
                          const slg_fragment_shader* fs, size_t uboId);
+
+/*-----------------------------------------------------------------------------
+ * Caller-defined shader programs. SoftLight takes shaders as host function
+ * pointers over SL_VertexParam / SL_FragmentParam
+ * (softlight/include/softlight/SL_Shader.hpp:41-119) handed to
+ * SL_Context::create_shader (softlight/src/SL_Context.cpp:488-606). Here a
+ * caller writes its programs as __device__ functions over parameter structs
+ * of the same shape (slg::VertexParam / slg::FragmentParam in
+ * include/slg_shader.cuh), compiles the draw-path kernels for them in its
+ * own CUDA translation unit (SLG_DEFINE_PROGRAMS) and registers the result
+ * here; slg_create_shader then takes their ids like the built-in ones. The
+ * vertex and fragment program of one shader come from the same set.
+-----------------------------------------------------------------------------*/
+#define SLG_PIPELINE_ABI_VERSION 1u
+
+/* The kernels of one program set, behind plain function pointers (the frame
+ * and stream are the library's launch description and cudaStream_t). */
+typedef struct slg_pipeline_ops
+{
+    uint32_t abiVersion;   /* SLG_PIPELINE_ABI_VERSION the set was compiled against */
+    uint32_t frameBytes;   /* size of the launch description it was compiled against */
+    int (*set_attributes)(void);
+    int (*launch_vertex)(const void* frame, void* stream);
+    int (*launch_raster)(const void* frame, void* stream);
+} slg_pipeline_ops;
+
+/* What the host needs to know about a program to launch it correctly. */
+#define SLG_PROGRAM_DISCARDS     1u  /* the fragment program may return false (SL_FragmentShader semantics) */
+#define SLG_PROGRAM_WRITES_DEPTH 2u  /* the fragment program may change coord.depth */
+
+typedef struct slg_program_info
+{
+    uint32_t id;           /* >= SLG_PROGRAM_USER_FIRST, not yet registered in the context */
+    uint32_t vertexBytes;  /* bytes the vertex program reads per vertex at binding 0's offset (checked against the buffer) */
+    uint32_t flags;        /* SLG_PROGRAM_DISCARDS | SLG_PROGRAM_WRITES_DEPTH */
+} slg_program_info;
+
+/* Registers the programs of one compiled set. Launches whose fragment
+ * programs discard or write depth take the ordered raster; a program that
+ * returns false without SLG_PROGRAM_DISCARDS is reported at slg_finish
+ * (SLG_ERR_INVALID_ARG). Vertex programs must be pure functions of the
+ * vertex, the instance and the resources they read: the vertex stage may
+ * run them once per vertex instead of once per triangle corner. */
+int slg_register_programs(slg_context* ctx, const slg_pipeline_ops* ops, const slg_program_info* programs, size_t numPrograms);
 
 /* SL_Context::clear_framebuffer / clear_color_buffer / clear_depth_buffer
  * (softlight/src/SL_Context.cpp:881-969). As in SL_ClearProcessor

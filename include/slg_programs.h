@@ -75,6 +75,32 @@ typedef struct slg_vcolor_uniforms
     uint32_t pad[3];
 } slg_vcolor_uniforms;
 
+/* SLG_PROGRAM_VCOLOR_TEX_CUTOUT. Same vertex layout and block prefix as
+ * slg_vcolor_uniforms; fragments whose alpha (vertex alpha x texel alpha)
+ * is below alphaRef are discarded. */
+typedef struct slg_cutout_uniforms
+{
+    float    mvpMatrix[16];
+    uint32_t textureId;        /* RGBA8 texture, bilinear, REPEAT */
+    float    alphaRef;
+    uint32_t pad[2];
+} slg_cutout_uniforms;
+
+/* SLG_PROGRAM_FRAG_COORD. Same vertex layout and block prefix as
+ * slg_vcolor_uniforms. The fragment stage reads the fragment coordinate:
+ * output (x * invSize[0], y * invSize[1], depth, vertex alpha); where
+ * screenDoor != 0, fragments with ((x ^ y) & screenDoor) == 0 are
+ * discarded; the depth written is depth * depthScale + depthBias. */
+typedef struct slg_fragcoord_uniforms
+{
+    float    mvpMatrix[16];
+    float    invSize[2];
+    float    depthScale;
+    float    depthBias;
+    uint32_t screenDoor;
+    uint32_t pad[3];
+} slg_fragcoord_uniforms;
+
 /* SLG_PROGRAM_FLAT_COLOR. Vertex layout: float pos[3] at binding 0. */
 typedef struct slg_flat_uniforms
 {
@@ -86,6 +112,17 @@ typedef struct slg_flat_uniforms
  * Minimal vector helpers with a fixed evaluation order
 -----------------------------------------------------------------------------*/
 typedef struct slg_v4 { float x, y, z, w; } slg_v4;
+
+/* SL_FragCoordXYZ (softlight/include/softlight/SL_ShaderUtil.hpp:668-673),
+ * same layout: the fragment's 16-bit screen coordinates and its depth. A
+ * fragment program may change depth; that value is what is written to the
+ * depth buffer (softlight/src/SL_FragmentProcessor.cpp:524-527). */
+typedef struct slg_frag_coord
+{
+    uint16_t x;
+    uint16_t y;
+    float    depth;
+} slg_frag_coord;
 
 SLG_HD slg_v4 slg_make_v4(float x, float y, float z, float w) { slg_v4 r; r.x = x; r.y = y; r.z = z; r.w = w; return r; }
 SLG_HD slg_v4 slg_v4_load(const float* p) { return slg_make_v4(p[0], p[1], p[2], p[3]); }
@@ -250,6 +287,40 @@ SLG_HD bool slg_fs_gbuffer(const Env& env, const slg_v4* varyings, slg_v4* outpu
     outputs[1] = t;
     outputs[2] = c;
     outputs[3] = slg_make_v4(c.x * c.y, c.y * c.z, c.z * c.x, t.w);
+    return true;
+}
+
+/* SLG_PROGRAM_VCOLOR_TEX_CUTOUT: an alpha test. Returns false (the fragment
+ * is discarded: no colour is written, depth still is) where the combined
+ * alpha is below alphaRef. */
+template <class Env>
+SLG_HD bool slg_fs_cutout(const Env& env, const slg_v4* varyings, slg_v4* outputs)
+{
+    const slg_cutout_uniforms* u = (const slg_cutout_uniforms*)env.uniforms();
+    const slg_v4 c = varyings[0];
+    const slg_v4 t = env.sample_rgba8(u->textureId, varyings[1].x, varyings[1].y);
+    const float a = c.w * t.w;
+    if (a < u->alphaRef)
+    {
+        return false;
+    }
+    outputs[0] = slg_make_v4(c.x * t.x, c.y * t.y, c.z * t.z, a);
+    return true;
+}
+
+/* SLG_PROGRAM_FRAG_COORD: reads and writes the fragment coordinate. */
+template <class Env>
+SLG_HD bool slg_fs_frag_coord(const Env& env, slg_frag_coord* coord, const slg_v4* varyings, slg_v4* outputs)
+{
+    const slg_fragcoord_uniforms* u = (const slg_fragcoord_uniforms*)env.uniforms();
+    const uint32_t x = coord->x, y = coord->y;
+    if (u->screenDoor != 0u && ((x ^ y) & u->screenDoor) == 0u)
+    {
+        return false;
+    }
+    const float depth = coord->depth;
+    outputs[0] = slg_make_v4((float)x * u->invSize[0], (float)y * u->invSize[1], depth, varyings[0].w);
+    coord->depth = depth * u->depthScale + u->depthBias;
     return true;
 }
 

@@ -117,7 +117,9 @@ math::vec4 vs_callback(SL_VertexParam& param)
         case SLG_PROGRAM_BLINN_PHONG_INST: r = slg_vs_blinn(env, param.vertId, param.instanceId, vary); break;
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
         case SLG_PROGRAM_VCOLOR_TEXF:
-        case SLG_PROGRAM_GBUFFER:          r = slg_vs_vcolor(env, param.vertId, param.instanceId, vary); break;
+        case SLG_PROGRAM_GBUFFER:
+        case SLG_PROGRAM_VCOLOR_TEX_CUTOUT:
+        case SLG_PROGRAM_FRAG_COORD:       r = slg_vs_vcolor(env, param.vertId, param.instanceId, vary); break;
         default:                           r = slg_vs_flat(env, param.vertId, param.instanceId, vary); break;
     }
     const int n = (P == SLG_PROGRAM_BLINN_PHONG_INST) ? 3 : (P == SLG_PROGRAM_FLAT_COLOR ? 0 : 2);
@@ -146,6 +148,19 @@ bool fs_callback(SL_FragmentParam& param)
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA: r = slg_fs_vcolor_tex_alpha(env, vary, outs); break;
         case SLG_PROGRAM_VCOLOR_TEXF:      r = slg_fs_vcolor_texf(env, vary, outs); break;
         case SLG_PROGRAM_GBUFFER:          r = slg_fs_gbuffer(env, vary, outs); break;
+        case SLG_PROGRAM_VCOLOR_TEX_CUTOUT: r = slg_fs_cutout(env, vary, outs); break;
+        case SLG_PROGRAM_FRAG_COORD:
+        {
+            /* SL_FragmentParam::coord in and out: the reference writes the
+             * depth the program leaves there */
+            slg_frag_coord c;
+            c.x = param.coord.x;
+            c.y = param.coord.y;
+            c.depth = param.coord.depth;
+            r = slg_fs_frag_coord(env, &c, vary, outs);
+            param.coord.depth = c.depth;
+            break;
+        }
         default:                           r = slg_fs_flat(env, vary, outs); break;
     }
     for (int i = 0; i < 4; ++i)
@@ -168,6 +183,8 @@ VsFn vs_for(uint32_t p)
         case SLG_PROGRAM_VCOLOR_TEXF:      return vs_callback<SLG_PROGRAM_VCOLOR_TEXF>;
         case SLG_PROGRAM_FLAT_COLOR:       return vs_callback<SLG_PROGRAM_FLAT_COLOR>;
         case SLG_PROGRAM_GBUFFER:          return vs_callback<SLG_PROGRAM_GBUFFER>;
+        case SLG_PROGRAM_VCOLOR_TEX_CUTOUT: return vs_callback<SLG_PROGRAM_VCOLOR_TEX_CUTOUT>;
+        case SLG_PROGRAM_FRAG_COORD:       return vs_callback<SLG_PROGRAM_FRAG_COORD>;
         default:                           return nullptr;
     }
 }
@@ -182,6 +199,8 @@ FsFn fs_for(uint32_t p)
         case SLG_PROGRAM_VCOLOR_TEXF:      return fs_callback<SLG_PROGRAM_VCOLOR_TEXF>;
         case SLG_PROGRAM_FLAT_COLOR:       return fs_callback<SLG_PROGRAM_FLAT_COLOR>;
         case SLG_PROGRAM_GBUFFER:          return fs_callback<SLG_PROGRAM_GBUFFER>;
+        case SLG_PROGRAM_VCOLOR_TEX_CUTOUT: return fs_callback<SLG_PROGRAM_VCOLOR_TEX_CUTOUT>;
+        case SLG_PROGRAM_FRAG_COORD:       return fs_callback<SLG_PROGRAM_FRAG_COORD>;
         default:                           return nullptr;
     }
 }

@@ -354,14 +354,19 @@ static V4 run_vs(uint32_t program, const Env& env, uint64_t vertId, uint64_t ins
         case SLG_PROGRAM_BLINN_PHONG_INST: r = slg_vs_blinn(env, vertId, instId, vary); break;
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
         case SLG_PROGRAM_VCOLOR_TEXF:
-        case SLG_PROGRAM_GBUFFER:          r = slg_vs_vcolor(env, vertId, instId, vary); break;
+        case SLG_PROGRAM_GBUFFER:
+        case SLG_PROGRAM_VCOLOR_TEX_CUTOUT:
+        case SLG_PROGRAM_FRAG_COORD:       r = slg_vs_vcolor(env, vertId, instId, vary); break;
         default:                           r = slg_vs_flat(env, vertId, instId, vary); break;
     }
     for (int i = 0; i < 4; ++i) varyings[i] = from_slg(vary[i]);
     return from_slg(r);
 }
 
-static bool run_fs(uint32_t program, const Env& env, const V4* varyings, V4* outputs)
+/* The fragment program with SL_FragmentParam's coord (x, y, depth) in and
+ * out: the depth buffer receives coord.depth after the program
+ * (SL_FragmentProcessor.cpp:501-529). */
+static bool run_fs(uint32_t program, const Env& env, slg_frag_coord& coord, const V4* varyings, V4* outputs)
 {
     slg_v4 vary[4], outs[4];
     for (int i = 0; i < 4; ++i) { vary[i] = to_slg(varyings[i]); outs[i] = slg_make_v4(0.f, 0.f, 0.f, 0.f); }
@@ -373,10 +378,21 @@ static bool run_fs(uint32_t program, const Env& env, const V4* varyings, V4* out
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA: r = slg_fs_vcolor_tex_alpha(env, vary, outs); break;
         case SLG_PROGRAM_VCOLOR_TEXF:      r = slg_fs_vcolor_texf(env, vary, outs); break;
         case SLG_PROGRAM_GBUFFER:          r = slg_fs_gbuffer(env, vary, outs); break;
+        case SLG_PROGRAM_VCOLOR_TEX_CUTOUT: r = slg_fs_cutout(env, vary, outs); break;
+        case SLG_PROGRAM_FRAG_COORD:       r = slg_fs_frag_coord(env, &coord, vary, outs); break;
         default:                           r = slg_fs_flat(env, vary, outs); break;
     }
     for (int i = 0; i < 4; ++i) outputs[i] = from_slg(outs[i]);
     return r;
+}
+
+static inline slg_frag_coord frag_coord(uint32_t x, uint32_t y, float depth)
+{
+    slg_frag_coord c;
+    c.x = (uint16_t)x;
+    c.y = (uint16_t)y;
+    c.depth = depth;
+    return c;
 }
 
 /*-----------------------------------------------------------------------------
@@ -937,7 +953,8 @@ static inline void shade_fragment(const RasterState& rs, const Bin& bin, int x, 
     }
 
     V4 outputs[4];
-    const bool haveOutputs = run_fs(sh.fsProgram, rs.envs[bin.drawIndex], varyings, outputs);
+    slg_frag_coord coord = frag_coord((uint32_t)x, (uint32_t)y, z);
+    const bool haveOutputs = run_fs(sh.fsProgram, rs.envs[bin.drawIndex], coord, varyings, outputs);
     if (haveOutputs)
     {
         for (unsigned t = 0; t < sh.numOutputs && t < rs.numOutputs; ++t)
@@ -947,7 +964,7 @@ static inline void shade_fragment(const RasterState& rs, const Bin& bin, int x, 
     }
     if (sh.depthMask == SLG_DEPTH_MASK_ON)
     {
-        dset(rs, (size_t)x + (size_t)rs.width * y, z);
+        dset(rs, (size_t)x + (size_t)rs.width * y, coord.depth);
     }
     ++frags;
 }
@@ -1125,14 +1142,15 @@ static void render_line(const RasterState& rs, const DrawState& ds, const LineVe
             for (unsigned i = 0; i < ds.numVaryings; ++i) vary[i] = mix(a.varyings[i], b.varyings[i], q.interp);
             V4 outputs[4];
             const size_t lin = (size_t)q.x + W * q.y;
-            if (run_fs(sh.fsProgram, ds.env, vary, outputs))
+            slg_frag_coord coord = frag_coord(q.x, q.y, q.z);
+            if (run_fs(sh.fsProgram, ds.env, coord, vary, outputs))
             {
                 for (unsigned t = 0; t < sh.numOutputs && t < rs.numOutputs; ++t)
                 {
                     write_color(rs.colors[t], (unsigned)(lin % W), (unsigned)(lin / W), outputs[t], sh.blend);
                 }
             }
-            if (sh.depthMask == SLG_DEPTH_MASK_ON) dset(rs, lin, q.z);
+            if (sh.depthMask == SLG_DEPTH_MASK_ON) dset(rs, lin, coord.depth);
             ++frags;
         }
         queue.clear();
@@ -1877,14 +1895,15 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
                     const float z = v[2];
                     if (!depth_cmp(sh.depthTest, z, dget(rs, lin))) continue;
                     V4 outputs[4];
-                    if (run_fs(sh.fsProgram, ds.env, vary, outputs))
+                    slg_frag_coord coord = frag_coord((uint32_t)x, (uint32_t)y, z);
+                    if (run_fs(sh.fsProgram, ds.env, coord, vary, outputs))
                     {
                         for (unsigned t = 0; t < sh.numOutputs && t < rs.numOutputs; ++t)
                         {
                             write_color(rs.colors[t], (unsigned)(lin % W), (unsigned)(lin / W), outputs[t], sh.blend);
                         }
                     }
-                    if (sh.depthMask == SLG_DEPTH_MASK_ON) dset(rs, lin, z);
+                    if (sh.depthMask == SLG_DEPTH_MASK_ON) dset(rs, lin, coord.depth);
                     ++totalFrags;
                 }
             }

@@ -39,6 +39,9 @@ PACKED_FORMATS = {28: ("uint8", (3, 3, 2)), 29: ("uint16", (5, 6, 5)), 30: ("uin
 COLOR_TYPES = tuple(range(33))
 PROGRAM_LAMBERT_TEX, PROGRAM_BLINN_PHONG_INST, PROGRAM_VCOLOR_TEX_ALPHA = 1, 2, 3
 PROGRAM_VCOLOR_TEXF, PROGRAM_FLAT_COLOR, PROGRAM_GBUFFER = 4, 5, 6
+PROGRAM_VCOLOR_TEX_CUTOUT, PROGRAM_FRAG_COORD = 7, 8
+PROGRAM_USER_FIRST = 256
+PROGRAM_DISCARDS, PROGRAM_WRITES_DEPTH = 1, 2
 
 BYTES_PER_COLOR = {t: (t // 7 + 1) * (1, 2, 4, 8, 2, 4, 8)[t % 7] for t in range(28)}
 BYTES_PER_COLOR.update({28: 1, 29: 2, 30: 2, 31: 2, 32: 4})
@@ -94,6 +97,11 @@ class DrawCmd(C.Structure):
 
 class SLError(RuntimeError):
     pass
+
+
+class ProgramInfo(C.Structure):
+    """slg_program_info (include/slg.h): one registered program."""
+    _fields_ = [("id", C.c_uint32), ("vertexBytes", C.c_uint32), ("flags", C.c_uint32)]
 
 
 # (name, restype, argtypes) for every entry point of include/slg.h
@@ -158,6 +166,7 @@ _GPU_SIGNATURES = [
     ("autotune", C.c_int, [C.c_void_p, C.POINTER(DrawCmd), C.c_size_t, C.c_size_t, C.POINTER(C.c_double),
                            C.c_double, C.POINTER(C.c_int)]),
     ("draw_noalloc", C.c_int, [C.c_void_p, C.POINTER(Mesh), C.c_size_t, C.c_size_t]),
+    ("register_programs", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(ProgramInfo), C.c_size_t]),
     ("fbo_enable_visibility", C.c_int, [C.c_void_p, C.c_size_t, C.c_int]),
     ("fbo_read_visibility", C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t]),
     ("diff_shade", C.c_int, [C.c_void_p, C.POINTER(Mesh), C.c_size_t, C.c_size_t, C.c_void_p, C.c_size_t]),
@@ -392,6 +401,13 @@ class SLContext:
         self._call("scene_draw", scene, fbo, shader, p.ctypes.data_as(C.POINTER(C.c_float)),
                    v.ctypes.data_as(C.POINTER(C.c_float)),
                    cp.ctypes.data_as(C.POINTER(C.c_float)) if cp is not None else None)
+
+    def register_programs(self, ops_ptr, programs):
+        """slg_register_programs: ops_ptr is the address of an
+        slg_pipeline_ops table (a caller's compiled program set); programs
+        is a list of (id, vertex bytes, flags)."""
+        arr = (ProgramInfo * len(programs))(*[ProgramInfo(*p) for p in programs])
+        self._call("register_programs", C.c_void_p(ops_ptr), arr, len(programs))
 
     def draw_noalloc(self, mesh, shader, fbo):
         """slg_draw with its scratch in a fixed device array (no allocation)."""

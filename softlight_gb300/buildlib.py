@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libslg.so")
 
-SOURCES = ["slg_kernels.cu", "slg_context.cu", "slg_adjoint.cu"]
+SOURCES = ["slg_builtin_raster_rgba8.cu", "slg_builtin_raster_rgbaf.cu", "slg_builtin_raster_rf.cu",
+           "slg_builtin_vertex.cu", "slg_kernels.cu", "slg_context.cu", "slg_adjoint.cu"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

@@ -1,0 +1,8 @@
+/*
+ * slg_builtin_raster_rf.cu - the built-in programs' raster stage for
+ * colour attachment 0 in R float (order-free and ordered rasters at every tile
+ * size, line-address fix-up).
+ */
+#include "slg_pipeline.cuh"
+
+SLG_PIPELINE_RASTER(slg::BuiltinPrograms, ColorRF)

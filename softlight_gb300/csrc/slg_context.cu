@@ -58,6 +58,17 @@ struct Shader
     uint8_t cull, depthTest, depthMask, blend, numVaryings, numOutputs;
     uint32_t vsProgram, fsProgram;
     size_t ubo;
+    uint32_t programSet;     /* 0: built-in programs, else 1 + the registration */
+    uint32_t fsFlags;        /* SLG_PROGRAM_DISCARDS | SLG_PROGRAM_WRITES_DEPTH of the fragment program */
+    uint32_t vertexBytes;    /* bytes the vertex program reads per vertex at binding 0 */
+};
+
+/* A registered program set (slg_register_programs): its kernels' entry
+ * table and its programs. */
+struct ProgramSet
+{
+    slg_pipeline_ops ops;
+    std::vector<slg_program_info> programs;
 };
 
 /* Field widths of the packed formats 28..32 (RGB 332, RGB 565, RGBA 5551,
@@ -121,7 +132,15 @@ size_t index_bytes(int type)
     }
 }
 
-bool valid_program(uint32_t p) { return p >= SLG_PROGRAM_LAMBERT_TEX && p <= SLG_PROGRAM_GBUFFER; }
+bool valid_program(uint32_t p) { return p >= SLG_PROGRAM_LAMBERT_TEX && p <= SLG_PROGRAM_FRAG_COORD; }
+
+/* SLG_PROGRAM_DISCARDS / SLG_PROGRAM_WRITES_DEPTH of a built-in fragment program. */
+uint32_t builtin_program_flags(uint32_t p)
+{
+    if (p == SLG_PROGRAM_VCOLOR_TEX_CUTOUT) return SLG_PROGRAM_DISCARDS;
+    if (p == SLG_PROGRAM_FRAG_COORD) return SLG_PROGRAM_DISCARDS | SLG_PROGRAM_WRITES_DEPTH;
+    return 0;
+}
 
 constexpr size_t kDescRing = 4096;
 constexpr uint64_t kMaxSlots = (1ull << 29) - 1; /* keys are slot << 3 | sub in 32 bits */
@@ -191,6 +210,7 @@ struct slg_context
     std::vector<Ubo> ubos;
     std::vector<Shader> shaders;
     std::vector<Scene> scenes;
+    std::vector<ProgramSet> programSets;   /* registered caller program sets */
 
     /* uniform blocks assigned since the last launch, uploaded together
      * through a ring of pinned staging slots */
@@ -205,7 +225,7 @@ struct slg_context
     DevBuffer uboStageDev;
 
     /* resource tables visible to device programs */
-    DevBuffer texTable, bufTable;
+    DevBuffer texTable, bufTable, vaoTable;
     bool tablesDirty = true;
 
     /* scratch */
@@ -277,6 +297,30 @@ void dev_free(DevBuffer& b)
     b.bytes = 0;
 }
 
+void fill_vao_views(const slg_context* ctx, slg::VaoView* out)
+{
+    for (size_t i = 0; i < ctx->vaos.size(); ++i)
+    {
+        for (int k = 0; k < 8; ++k)
+        {
+            out[i].offset[k] = ctx->vaos[i].bindings[k].offset;
+            out[i].stride[k] = ctx->vaos[i].bindings[k].stride;
+        }
+    }
+}
+
+/* The resource tables of a frame: textures, vertex buffers and vertex
+ * arrays by id (device pointers to the uploaded tables). */
+void set_tables(const slg_context* ctx, slg::Tables& t, const void* tex, const void* bufs, const void* vaos)
+{
+    t.textures = static_cast<const TexView*>(tex);
+    t.buffers = static_cast<const uint8_t* const*>(bufs);
+    t.vaos = static_cast<const slg::VaoView*>(vaos);
+    t.numTextures = (uint32_t)ctx->textures.size();
+    t.numBuffers = (uint32_t)ctx->vbos.size();
+    t.numVaos = (uint32_t)ctx->vaos.size();
+}
+
 int upload_tables(slg_context* ctx)
 {
     if (!ctx->tablesDirty) return SLG_OK;
@@ -292,14 +336,19 @@ int upload_tables(slg_context* ctx)
     }
     std::vector<const uint8_t*> bufs(std::max<size_t>(1, ctx->vbos.size()), nullptr);
     for (size_t i = 0; i < ctx->vbos.size(); ++i) bufs[i] = static_cast<const uint8_t*>(ctx->vbos[i].buf.ptr);
+    std::vector<slg::VaoView> vaos(std::max<size_t>(1, ctx->vaos.size()));
+    fill_vao_views(ctx, vaos.data());
 
     int r = dev_alloc(ctx, ctx->texTable, tex.size() * sizeof(TexView), false);
     if (r) return r;
     r = dev_alloc(ctx, ctx->bufTable, bufs.size() * sizeof(void*), false);
     if (r) return r;
+    r = dev_alloc(ctx, ctx->vaoTable, vaos.size() * sizeof(slg::VaoView), false);
+    if (r) return r;
     cudaStreamSynchronize(ctx->stream);
     cudaError_t e = cudaMemcpy(ctx->texTable.ptr, tex.data(), tex.size() * sizeof(TexView), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(ctx->bufTable.ptr, bufs.data(), bufs.size() * sizeof(void*), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(ctx->vaoTable.ptr, vaos.data(), vaos.size() * sizeof(slg::VaoView), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "table upload");
     ctx->tablesDirty = false;
     return SLG_OK;
@@ -383,6 +432,12 @@ int check_status(slg_context* ctx)
     if (bits & slg::kStatusWireQueue)
     {
         msg += " blended wireframe triangle revisiting a pixel after 600 queued fragments (queue flush order not reproduced)";
+    }
+    if (bits & slg::kStatusUndeclaredDiscard)
+    {
+        return ctx->fail(SLG_ERR_INVALID_ARG, "device-side status: a fragment program discarded a fragment in a launch that took the "
+                                              "order-free raster; register programs that return false with SLG_PROGRAM_DISCARDS "
+                                              "(the affected pixels keep the wrong colour)");
     }
     msg += " (the affected draws were skipped; buffers have been grown)";
     return ctx->fail(SLG_ERR_OVERFLOW, msg);
@@ -513,8 +568,25 @@ size_t program_vertex_bytes(uint32_t program)
         case SLG_PROGRAM_BLINN_PHONG_INST: return 32;
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
         case SLG_PROGRAM_VCOLOR_TEXF:
-        case SLG_PROGRAM_GBUFFER:          return 36;
+        case SLG_PROGRAM_GBUFFER:
+        case SLG_PROGRAM_VCOLOR_TEX_CUTOUT:
+        case SLG_PROGRAM_FRAG_COORD:       return 36;
         default:                           return 12;
+    }
+}
+
+/* Bytes of one component of SL_DataType (softlight/include/softlight/SL_Geometry.hpp:30). */
+uint64_t vertex_type_bytes(int type)
+{
+    switch (type)
+    {
+        case SLG_VERTEX_DATA_BYTE:   return 1;
+        case SLG_VERTEX_DATA_SHORT:  return 2;
+        case SLG_VERTEX_DATA_INT:    return 4;
+        case SLG_VERTEX_DATA_LONG:   return 8;
+        case SLG_VERTEX_DATA_FLOAT:  return 4;
+        case SLG_VERTEX_DATA_DOUBLE: return 8;
+        default:                     return 0;
     }
 }
 
@@ -580,9 +652,24 @@ int validate_draw(slg_context* ctx, const Shader& sh, const Vao& vao, const slg_
     {
         maxVertex = lastElement;
     }
-    const uint64_t need = (uint64_t)b0.offset + (uint64_t)b0.stride * maxVertex + program_vertex_bytes(sh.vsProgram);
+    const uint64_t need = (uint64_t)b0.offset + (uint64_t)b0.stride * maxVertex + sh.vertexBytes;
     if (need > vbo.size + 64) return ctx->fail(SLG_ERR_INVALID_ARG, "vertex range exceeds the vertex buffer");
 
+    /* a caller's programs may read any configured binding (SL_VertexArray::
+     * offset(bindId, vertId)); each must stay inside the buffer for every
+     * vertex the draw reaches. Uniform blocks are theirs to interpret. */
+    if (sh.programSet != 0)
+    {
+        for (int k = 1; k < 8; ++k)
+        {
+            const Binding& b = vao.bindings[k];
+            if (b.stride == 0 && b.comps == 0) continue;
+            const uint64_t elem = (uint64_t)b.comps * vertex_type_bytes(b.type);
+            if (b.offset < 0 || b.stride < 0 || (uint64_t)b.offset + (uint64_t)b.stride * maxVertex + elem > vbo.size + 64)
+                return ctx->fail(SLG_ERR_INVALID_ARG, "vertex binding " + std::to_string(k) + " reaches past the vertex buffer");
+        }
+        return SLG_OK;
+    }
     if (sh.ubo == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "built-in programs need a uniform block");
     const uint8_t* u = ctx->ubos[sh.ubo].shadow;
     uint32_t tex = 0, buf = 0;
@@ -598,6 +685,7 @@ int validate_draw(slg_context* ctx, const Shader& sh, const Vao& vao, const slg_
             break;
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
         case SLG_PROGRAM_GBUFFER:
+        case SLG_PROGRAM_VCOLOR_TEX_CUTOUT:
             std::memcpy(&tex, u + offsetof(slg_vcolor_uniforms, textureId), 4);
             if (!texture_ok(ctx, tex, SLG_COLOR_RGBA_8U)) return ctx->fail(SLG_ERR_INVALID_ARG, "uniform textureId is not an RGBA8 texture");
             break;
@@ -781,6 +869,7 @@ int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, Draw
     d.indexType = indexed ? ctx->ibos[vao.ibo].type : -1;
     d.vsProgram = sh.vsProgram;
     d.fsProgram = sh.fsProgram;
+    d.vaoId = (uint32_t)m.vaoId;
     d.cull = sh.cull;
     d.numVaryings = sh.numVaryings;
     d.depthTest = sh.depthTest;
@@ -792,11 +881,18 @@ int build_desc(slg_context* ctx, const DrawRequest& req, uint64_t slotBase, Draw
     return SLG_OK;
 }
 
+/* The kernels of program set `set` (0: built-in). */
+const slg_pipeline_ops& pipeline_ops(const slg_context* ctx, uint32_t set)
+{
+    return set == 0 ? slg::builtin_pipeline() : ctx->programSets[set - 1].ops;
+}
+
 /* Replays the cached CUDA graph of a batch launch when the descriptors and
  * the launch parameters are unchanged (uniform-block contents may change:
  * they are read from device memory and were validated again on the host),
  * otherwise captures the pipeline of this launch into a new graph. */
-int launch_batch_graph(slg_context* ctx, const Frame& frame, const DrawDesc* descs, const uint64_t* starts, size_t n)
+int launch_batch_graph(slg_context* ctx, const Frame& frame, const DrawDesc* descs, const uint64_t* starts, size_t n,
+                       const slg_pipeline_ops& ops)
 {
     slg_context::GraphCache& g = ctx->graph;
     int r;
@@ -827,7 +923,7 @@ int launch_batch_graph(slg_context* ctx, const Frame& frame, const DrawDesc* des
         cudaGraph_t graph = nullptr;
         e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return ctx->cuda_fail(e, "cudaStreamBeginCapture");
-        const cudaError_t le = slg::launch_pipeline(f, ctx->keyCap, ctx->stream, nullptr);
+        const cudaError_t le = slg::launch_pipeline(f, ops, ctx->keyCap, ctx->stream, nullptr);
         e = cudaStreamEndCapture(ctx->stream, &graph);
         if (le != cudaSuccess) e = le;
         if (e == cudaSuccess) e = cudaGraphInstantiate(&g.exec, graph, 0);
@@ -864,6 +960,28 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     if (fbo.depth == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "framebuffer has no depth attachment");
     if (reqs.empty()) return SLG_OK;
     if (reqs.size() + 1 > kDescRing) return ctx->fail(SLG_ERR_INVALID_ARG, "too many draws in one batch");
+
+    /* a launch runs the kernels of one program set: draws whose shaders come
+     * from different sets go out as consecutive launches, which gives the
+     * same result as one */
+    uint32_t programSet = 0;
+    for (size_t i = 0; i < reqs.size(); ++i)
+    {
+        if (reqs[i].shaderId >= ctx->shaders.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid shader id");
+        const uint32_t set = ctx->shaders[reqs[i].shaderId].programSet;
+        if (i == 0)
+        {
+            programSet = set;
+        }
+        else if (set != programSet)
+        {
+            if (hook) return ctx->fail(SLG_ERR_INVALID_ARG, "a draw list mixes program sets");
+            const std::vector<DrawRequest> head(reqs.begin(), reqs.begin() + i), tail(reqs.begin() + i, reqs.end());
+            int r = run_launch(ctx, head, fboId, false, nullptr);
+            return r ? r : run_launch(ctx, tail, fboId, false, nullptr);
+        }
+    }
+    const slg_pipeline_ops& ops = pipeline_ops(ctx, programSet);
 
     int r = upload_tables(ctx);
     if (r) return r;
@@ -974,8 +1092,12 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     f.freeDepthMask = descs[0].depthMask;
     for (size_t i = 0; i < n; ++i)
     {
+        /* a discarded fragment leaves an earlier one's colour and a written
+         * coord.depth changes later tests: both need the order */
+        const uint32_t flags = ctx->shaders[reqs[i].shaderId].fsFlags;
         if (descs[i].blend != SLG_BLEND_OFF || descs[i].depthTest == SLG_DEPTH_TEST_NOT_EQUAL ||
-            descs[i].depthTest != f.freeDepthFunc || descs[i].depthMask != f.freeDepthMask || ctx->forceOrdered)
+            descs[i].depthTest != f.freeDepthFunc || descs[i].depthMask != f.freeDepthMask || ctx->forceOrdered ||
+            (flags & (SLG_PROGRAM_DISCARDS | SLG_PROGRAM_WRITES_DEPTH)))
         {
             f.orderFree = 0;
         }
@@ -996,8 +1118,7 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
         f.aliasCount = static_cast<uint32_t*>(ctx->aliasCount.ptr);
         f.aliasCap = kAliasCap;
     }
-    f.tables.textures = static_cast<const TexView*>(ctx->texTable.ptr);
-    f.tables.buffers = static_cast<const uint8_t* const*>(ctx->bufTable.ptr);
+    set_tables(ctx, f.tables, ctx->texTable.ptr, ctx->bufTable.ptr, ctx->vaoTable.ptr);
 
     f.vsBlock = ctx->vsBlock;
 
@@ -1005,7 +1126,7 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
 
     if (batch && ctx->batchGraphs && !ctx->profileStages && !hook)
     {
-        return launch_batch_graph(ctx, f, descs, starts, n);
+        return launch_batch_graph(ctx, f, descs, starts, n, ops);
     }
 
     e = cudaMemcpyAsync(devDescs, descs, n * sizeof(DrawDesc), cudaMemcpyHostToDevice, ctx->stream);
@@ -1018,7 +1139,7 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
         if (e != cudaSuccess) return ctx->cuda_fail(e, "scene draw list");
     }
 
-    e = slg::launch_pipeline(f, ctx->keyCap, ctx->stream, ctx->profileStages ? ctx->stageEvents : nullptr);
+    e = slg::launch_pipeline(f, ops, ctx->keyCap, ctx->stream, ctx->profileStages ? ctx->stageEvents : nullptr);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "draw launch");
     return SLG_OK;
 }
@@ -1202,7 +1323,8 @@ int slg_context_create(slg_context** outCtx)
     if (e == cudaSuccess) e = cudaMalloc(&ctx->status.ptr, 4 * sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMemset(ctx->status.ptr, 0, 4 * sizeof(int32_t));
     for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->stageEvents[i]);
-    if (e == cudaSuccess) e = slg::init_kernel_attributes(ctx->keyCap);
+    if (e == cudaSuccess) e = slg::init_library_attributes(ctx->keyCap);
+    if (e == cudaSuccess) e = (cudaError_t)slg::builtin_pipeline().set_attributes();
     if (e != cudaSuccess)
     {
         slg_context_destroy(ctx);
@@ -1238,7 +1360,7 @@ void slg_context_destroy(slg_context* ctx)
         dev_free(sc.dBounds);
         dev_free(sc.dEntries);
     }
-    DevBuffer* scratch[] = {&ctx->texTable, &ctx->bufTable, &ctx->records, &ctx->varyings, &ctx->slotInfo, &ctx->slotOvf,
+    DevBuffer* scratch[] = {&ctx->texTable, &ctx->bufTable, &ctx->vaoTable, &ctx->records, &ctx->varyings, &ctx->slotInfo, &ctx->slotOvf,
                             &ctx->ovfCount, &ctx->clipQueue, &ctx->clipCount, &ctx->aliasEvents, &ctx->aliasCount,
                             &ctx->cachePos, &ctx->cacheVary, &ctx->recVerts,
                             &ctx->tileCount, &ctx->tileOffset,
@@ -1324,7 +1446,7 @@ int slg_ibo_init(slg_context* ctx, size_t id, size_t numElements, int indexType,
     return SLG_OK;
 }
 
-size_t slg_create_vao(slg_context* ctx) { ctx->vaos.emplace_back(); return ctx->vaos.size() - 1; }
+size_t slg_create_vao(slg_context* ctx) { ctx->vaos.emplace_back(); ctx->tablesDirty = true; return ctx->vaos.size() - 1; }
 
 int slg_vao_set_vertex_buffer(slg_context* ctx, size_t vao, size_t vbo)
 {
@@ -1349,6 +1471,7 @@ int slg_vao_set_binding(slg_context* ctx, size_t vao, unsigned bindId, ptrdiff_t
     b.stride = stride;
     b.comps = numComponents;
     b.type = dataType;
+    ctx->tablesDirty = true;
     return SLG_OK;
 }
 
@@ -1554,7 +1677,30 @@ size_t slg_create_shader(slg_context* ctx, const slg_vertex_shader* vs, const sl
     /* SL_Context::create_shader (softlight/src/SL_Context.cpp:492-505) */
     if (vs->numVaryings < fs->numVaryings || vs->numVaryings > 4 || fs->numVaryings > 4 || fs->numOutputs > 4)
         return ctx->fail_id("invalid varying or output count");
-    if (!valid_program(vs->program) || !valid_program(fs->program)) return ctx->fail_id("unknown shader program");
+    /* the vertex and fragment program run in one set's kernels */
+    /* program -> its set (0: built-in) and registration; both programs of a
+     * shader must come from one set */
+    const auto find = [&](uint32_t id, uint32_t& set, const slg_program_info*& info) {
+        set = 0;
+        info = nullptr;
+        if (valid_program(id)) return true;
+        for (size_t k = 0; k < ctx->programSets.size(); ++k)
+            for (const slg_program_info& p : ctx->programSets[k].programs)
+                if (p.id == id)
+                {
+                    set = (uint32_t)k + 1;
+                    info = &p;
+                    return true;
+                }
+        return false;
+    };
+    uint32_t set = 0, fSet = 0;
+    const slg_program_info* vi = nullptr;
+    const slg_program_info* fi = nullptr;
+    if (!find(vs->program, set, vi) || !find(fs->program, fSet, fi)) return ctx->fail_id("unknown shader program");
+    if (set != fSet) return ctx->fail_id("the vertex and fragment programs come from different program sets");
+    const uint32_t fsFlags = fi ? fi->flags : builtin_program_flags(fs->program);
+    const uint32_t vertexBytes = vi ? vi->vertexBytes : (uint32_t)program_vertex_bytes(vs->program);
     if (vs->cullMode > SLG_CULL_OFF || fs->depthTest > SLG_DEPTH_TEST_NOT_EQUAL || fs->blend > SLG_BLEND_SCREEN || fs->depthMask > 1)
         return ctx->fail_id("invalid pipeline state");
     if (ubo != SLG_INVALID_ID && !id_ok(ubo, ctx->ubos.size())) return ctx->fail_id("invalid ubo id");
@@ -1568,8 +1714,37 @@ size_t slg_create_shader(slg_context* ctx, const slg_vertex_shader* vs, const sl
     s.vsProgram = vs->program;
     s.fsProgram = fs->program;
     s.ubo = ubo;
+    s.programSet = set;
+    s.fsFlags = fsFlags;
+    s.vertexBytes = vertexBytes;
     ctx->shaders.push_back(s);
     return ctx->shaders.size() - 1;
+}
+
+int slg_register_programs(slg_context* ctx, const slg_pipeline_ops* ops, const slg_program_info* programs, size_t numPrograms)
+{
+    if (!ops || !programs || !numPrograms) return ctx->fail(SLG_ERR_INVALID_ARG, "null program set");
+    if (ops->abiVersion != SLG_PIPELINE_ABI_VERSION || ops->frameBytes != sizeof(Frame))
+        return ctx->fail(SLG_ERR_INVALID_ARG, "program set compiled against another version of the draw-path headers");
+    if (!ops->set_attributes || !ops->launch_vertex || !ops->launch_raster) return ctx->fail(SLG_ERR_INVALID_ARG, "incomplete program set");
+    for (size_t i = 0; i < numPrograms; ++i)
+    {
+        const slg_program_info& p = programs[i];
+        if (p.id < SLG_PROGRAM_USER_FIRST) return ctx->fail(SLG_ERR_INVALID_ARG, "registered program ids start at SLG_PROGRAM_USER_FIRST");
+        if (p.flags & ~(SLG_PROGRAM_DISCARDS | SLG_PROGRAM_WRITES_DEPTH)) return ctx->fail(SLG_ERR_INVALID_ARG, "unknown program flags");
+        for (size_t j = 0; j < i; ++j)
+            if (programs[j].id == p.id) return ctx->fail(SLG_ERR_INVALID_ARG, "program id listed twice");
+        for (const ProgramSet& set : ctx->programSets)
+            for (const slg_program_info& q : set.programs)
+                if (q.id == p.id) return ctx->fail(SLG_ERR_INVALID_ARG, "program id already registered");
+    }
+    const cudaError_t e = (cudaError_t)ops->set_attributes();
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "program set kernel attributes");
+    ProgramSet set;
+    set.ops = *ops;
+    set.programs.assign(programs, programs + numPrograms);
+    ctx->programSets.push_back(std::move(set));
+    return SLG_OK;
 }
 
 int slg_clear_color_buffer(slg_context* ctx, size_t fbo, unsigned att, const double rgba[4])
@@ -1991,13 +2166,15 @@ constexpr size_t kOffSlotOvf = kOffSlotInfo + align256(kNoAllocTris * sizeof(uin
 constexpr size_t kOffClipQueue = kOffSlotOvf + align256(kNoAllocTris * sizeof(uint32_t));
 constexpr size_t kOffTexTable = kOffClipQueue + align256(kNoAllocTris * sizeof(uint32_t));
 constexpr size_t kOffBufTable = kOffTexTable + align256(kNoAllocTextures * sizeof(TexView));
-constexpr size_t kOffRecords = kOffBufTable + align256(kNoAllocBuffers * sizeof(void*));
+constexpr size_t kOffVaoTable = kOffBufTable + align256(kNoAllocBuffers * sizeof(void*));
+constexpr size_t kOffRecords = kOffVaoTable + align256(kNoAllocBuffers * sizeof(slg::VaoView));
 constexpr size_t kOffVaryings = kOffRecords + align256(kNoAllocRecords * slg::kRecordVec4 * sizeof(float4));
 constexpr size_t kOffEntries = kOffVaryings + align256(kNoAllocRecords * slg::kVaryingVec4 * sizeof(float4));
 constexpr uint32_t kNoAllocAliases = kAliasCap;   /* as slg_draw: 4096 full-width line aliases */
 constexpr size_t kOffAliases = kOffEntries + align256(kNoAllocEntries * sizeof(uint32_t));
 constexpr size_t kNoAllocBytes = kOffAliases + align256(kNoAllocAliases * sizeof(slg::AliasEvent));
 static_assert(kNoAllocBytes < (8u << 20), "static draw scratch stays under 8 MiB");
+static_assert(offsetof(slg_cutout_uniforms, textureId) == offsetof(slg_vcolor_uniforms, textureId), "cutout block extends the vertex-colour block");
 static_assert(kNoAllocZeroBytes % 4 == 0, "counters are cleared in whole words");
 
 static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocBytes];
@@ -2077,8 +2254,9 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
                                                   " framebuffer is " + std::to_string(numTiles) + " tiles of " + std::to_string(f.tileW) + "x" +
                                                   std::to_string(f.tileH) + ", over the static limit of " + std::to_string(kNoAllocTiles));
     f.depthType = depthTex.type;
+    const Shader& shader = ctx->shaders[shaderId];
     f.orderFree = (desc->blend == SLG_BLEND_OFF && desc->depthTest != SLG_DEPTH_TEST_NOT_EQUAL && !ctx->forceOrdered &&
-                   f.depthType != SLG_COLOR_R_HALF) ? 1 : 0;
+                   f.depthType != SLG_COLOR_R_HALF && !(shader.fsFlags & (SLG_PROGRAM_DISCARDS | SLG_PROGRAM_WRITES_DEPTH))) ? 1 : 0;
     f.freeDepthFunc = desc->depthTest;
     f.freeDepthMask = desc->depthMask;
     if ((r = bind_visibility(ctx, fbo, f))) return r;
@@ -2095,17 +2273,19 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
      * them into the static scratch */
     const size_t numTex = ctx->textures.size(), numBuf = ctx->vbos.size();
     cudaError_t e = cudaSuccess;
-    if (!ctx->tablesDirty && ctx->texTable.ptr && ctx->bufTable.ptr)
+    const size_t numVao = ctx->vaos.size();
+    if (!ctx->tablesDirty && ctx->texTable.ptr && ctx->bufTable.ptr && ctx->vaoTable.ptr)
     {
-        f.tables.textures = static_cast<const TexView*>(ctx->texTable.ptr);
-        f.tables.buffers = static_cast<const uint8_t* const*>(ctx->bufTable.ptr);
+        set_tables(ctx, f.tables, ctx->texTable.ptr, ctx->bufTable.ptr, ctx->vaoTable.ptr);
     }
     else
     {
-        if (numTex > kNoAllocTextures || numBuf > kNoAllocBuffers)
-            return ctx->fail(SLG_ERR_INVALID_ARG, "slg_draw_noalloc: more than 256 textures or vertex buffers since the last slg_draw");
+        if (numTex > kNoAllocTextures || numBuf > kNoAllocBuffers || numVao > kNoAllocBuffers)
+            return ctx->fail(SLG_ERR_INVALID_ARG,
+                             "slg_draw_noalloc: more than 256 textures, vertex buffers or vertex arrays since the last slg_draw");
         TexView tex[kNoAllocTextures];
         const uint8_t* bufs[kNoAllocBuffers];
+        static thread_local slg::VaoView vaoViews[kNoAllocBuffers];   /* 32 KB: off the stack */
         for (size_t i = 0; i < numTex; ++i)
         {
             const Texture& t = ctx->textures[i];
@@ -2119,9 +2299,13 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
         if (numTex) e = cudaMemcpyAsync(scratch + kOffTexTable, tex, numTex * sizeof(TexView), cudaMemcpyHostToDevice, ctx->stream);
         if (e == cudaSuccess && numBuf)
             e = cudaMemcpyAsync(scratch + kOffBufTable, bufs, numBuf * sizeof(void*), cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess && numVao)
+        {
+            fill_vao_views(ctx, vaoViews);
+            e = cudaMemcpyAsync(scratch + kOffVaoTable, vaoViews, numVao * sizeof(slg::VaoView), cudaMemcpyHostToDevice, ctx->stream);
+        }
         if (e != cudaSuccess) return ctx->cuda_fail(e, "slg_draw_noalloc: table upload");
-        f.tables.textures = reinterpret_cast<const TexView*>(scratch + kOffTexTable);
-        f.tables.buffers = reinterpret_cast<const uint8_t* const*>(scratch + kOffBufTable);
+        set_tables(ctx, f.tables, scratch + kOffTexTable, scratch + kOffBufTable, scratch + kOffVaoTable);
     }
 
     starts[0] = 0;
@@ -2161,7 +2345,7 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
     f.vsBlock = ctx->vsBlock;
 
     if (flush_ubos(ctx, false)) return SLG_ERR_CUDA;
-    e = slg::launch_pipeline(f, ctx->keyCap, ctx->stream, nullptr);
+    e = slg::launch_pipeline(f, pipeline_ops(ctx, shader.programSet), ctx->keyCap, ctx->stream, nullptr);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "slg_draw_noalloc: launch");
     return SLG_OK;
 }

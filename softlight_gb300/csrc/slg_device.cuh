@@ -55,10 +55,20 @@ struct TexView
     int32_t type;          /* slg_color_type */
 };
 
+/* SL_VertexArray's bindings (softlight/include/softlight/SL_VertexArray.hpp:
+ * 20-34, 109-126): per binding the byte offset of vertex 0 and the stride. */
+struct VaoView
+{
+    int64_t offset[8];
+    int64_t stride[8];
+};
+
 struct Tables
 {
     const TexView* textures;
     const uint8_t* const* buffers; /* vertex buffer base pointers by id */
+    const VaoView* vaos;           /* vertex array bindings by id */
+    uint32_t numTextures, numBuffers, numVaos;
 };
 
 /* One draw: what SL_ProcessorPool::run_shader_processors hands to
@@ -81,6 +91,7 @@ struct DrawDesc
     int32_t  indexType;     /* -1: non-indexed */
     uint32_t vsProgram;
     uint32_t fsProgram;
+    uint32_t vaoId;         /* the mesh's vertex array (Tables::vaos) */
     uint8_t  cull, numVaryings, depthTest, depthMask, blend, numOutputs, prim;
     uint8_t  hidden;        /* 1: culled as a whole by the scene-graph producer (set on the device) */
 };
@@ -213,7 +224,8 @@ enum StatusBits
     kStatusOvfOverflow = 2,
     kStatusTileOverflow = 4,
     kStatusAliasOverflow = 8,
-    kStatusWireQueue = 16
+    kStatusWireQueue = 16,
+    kStatusUndeclaredDiscard = 32   /* a program discarded in an order-free launch */
 };
 
 /*-----------------------------------------------------------------------------
@@ -343,23 +355,44 @@ __device__ __forceinline__ slg_v4 run_vertex_program(uint32_t program, const Dev
         case SLG_PROGRAM_BLINN_PHONG_INST: return slg_vs_blinn(env, vertId, instanceId, varyings);
         case SLG_PROGRAM_VCOLOR_TEX_ALPHA:
         case SLG_PROGRAM_VCOLOR_TEXF:
-        case SLG_PROGRAM_GBUFFER:          return slg_vs_vcolor(env, vertId, instanceId, varyings);
+        case SLG_PROGRAM_GBUFFER:
+        case SLG_PROGRAM_VCOLOR_TEX_CUTOUT:
+        case SLG_PROGRAM_FRAG_COORD:       return slg_vs_vcolor(env, vertId, instanceId, varyings);
         default:                           return slg_vs_flat(env, vertId, instanceId, varyings);
     }
 }
 
-__device__ __forceinline__ bool run_fragment_program(uint32_t program, const DevEnv& env, const slg_v4* varyings, slg_v4* outputs)
+__device__ __forceinline__ bool run_fragment_program(uint32_t program, const DevEnv& env, slg_frag_coord& coord, const slg_v4* varyings,
+                                                     slg_v4* outputs)
 {
     switch (program)
     {
-        case SLG_PROGRAM_LAMBERT_TEX:      return slg_fs_lambert(env, varyings, outputs);
-        case SLG_PROGRAM_BLINN_PHONG_INST: return slg_fs_blinn(env, varyings, outputs);
-        case SLG_PROGRAM_VCOLOR_TEX_ALPHA: return slg_fs_vcolor_tex_alpha(env, varyings, outputs);
-        case SLG_PROGRAM_VCOLOR_TEXF:      return slg_fs_vcolor_texf(env, varyings, outputs);
-        case SLG_PROGRAM_GBUFFER:          return slg_fs_gbuffer(env, varyings, outputs);
-        default:                           return slg_fs_flat(env, varyings, outputs);
+        case SLG_PROGRAM_LAMBERT_TEX:       return slg_fs_lambert(env, varyings, outputs);
+        case SLG_PROGRAM_BLINN_PHONG_INST:  return slg_fs_blinn(env, varyings, outputs);
+        case SLG_PROGRAM_VCOLOR_TEX_ALPHA:  return slg_fs_vcolor_tex_alpha(env, varyings, outputs);
+        case SLG_PROGRAM_VCOLOR_TEXF:       return slg_fs_vcolor_texf(env, varyings, outputs);
+        case SLG_PROGRAM_GBUFFER:           return slg_fs_gbuffer(env, varyings, outputs);
+        case SLG_PROGRAM_VCOLOR_TEX_CUTOUT: return slg_fs_cutout(env, varyings, outputs);
+        case SLG_PROGRAM_FRAG_COORD:        return slg_fs_frag_coord(env, &coord, varyings, outputs);
+        default:                            return slg_fs_flat(env, varyings, outputs);
     }
 }
+
+/* The library's own program set (include/slg_programs.h), in the form the
+ * draw-path kernel templates take (slg_pipeline.cuh). */
+struct BuiltinPrograms
+{
+    static __device__ __forceinline__ slg_v4 vertex(const DrawDesc& d, const Tables& t, uint64_t vertId, uint64_t instanceId,
+                                                    slg_v4* varyings)
+    {
+        return run_vertex_program(d.vsProgram, make_env(d, t), vertId, instanceId, varyings);
+    }
+    static __device__ __forceinline__ bool fragment(const DrawDesc& d, const Tables& t, slg_frag_coord& coord, const slg_v4* varyings,
+                                                    slg_v4* outputs)
+    {
+        return run_fragment_program(d.fsProgram, make_env(d, t), coord, varyings, outputs);
+    }
+};
 
 } // namespace slg
 

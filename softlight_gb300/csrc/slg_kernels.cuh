@@ -10,14 +10,18 @@
 namespace slg
 {
 
-/* Enqueue vs_setup, tile_scan, bin_fill and raster for one launch on s.
- * When ev is not null, ev[0..4] are recorded before vs_setup, after
- * vs_setup, after tile_scan, after bin_fill and after raster. */
-cudaError_t launch_pipeline(const Frame& f, int keyCap, cudaStream_t s, cudaEvent_t* ev);
+/* Enqueue one launch on s: ops' vertex stage, tile_scan, bin_fill, the tile
+ * sort when the ordered raster may run, ops' raster stage. When ev is not
+ * null, ev[0..4] are recorded before the vertex stage, after it, after
+ * tile_scan, after bin_fill and after the raster. */
+cudaError_t launch_pipeline(const Frame& f, const slg_pipeline_ops& ops, int keyCap, cudaStream_t s, cudaEvent_t* ev);
 
-/* Raises the dynamic shared-memory limits of the raster and sort kernels
- * once, so launches (and stream captures) need no attribute calls. */
-cudaError_t init_kernel_attributes(int keyCap);
+/* Raises the dynamic shared-memory limit of the tile sort once, so
+ * launches (and stream captures) need no attribute calls. */
+cudaError_t init_library_attributes(int keyCap);
+
+/* The entry table of the built-in programs (slg_builtin_vertex.cu). */
+const slg_pipeline_ops& builtin_pipeline();
 
 /* Fill numTexels texels of 4 or 16 bytes with value. */
 cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[8], cudaStream_t s);

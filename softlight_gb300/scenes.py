@@ -234,6 +234,16 @@ def vcolor_uniforms(mvp, tex_id):
     return col_major(mvp).tobytes() + struct.pack("<4I", tex_id, 0, 0, 0)
 
 
+def cutout_uniforms(mvp, tex_id, alpha_ref):
+    """slg_cutout_uniforms: the vertex-colour block plus the alpha test's reference."""
+    return col_major(mvp).tobytes() + struct.pack("<If2I", tex_id, alpha_ref, 0, 0)
+
+
+def fragcoord_uniforms(mvp, inv_w, inv_h, depth_scale=1.0, depth_bias=0.0, screen_door=0):
+    """slg_fragcoord_uniforms of SLG_PROGRAM_FRAG_COORD."""
+    return col_major(mvp).tobytes() + struct.pack("<4fI3I", inv_w, inv_h, depth_scale, depth_bias, screen_door, 0, 0, 0)
+
+
 def flat_uniforms(mvp, rgba):
     return col_major(mvp).tobytes() + np.asarray(rgba, np.float32).tobytes()
 

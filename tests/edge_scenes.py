@@ -383,3 +383,30 @@ def point_edges(ctx, width=40, height=30):
                       cull=A.CULL_OFF, depth_test=A.DEPTH_TEST_OFF, depth_mask=A.DEPTH_MASK_OFF)
     s.draws.append((mesh, 1, sh))
     return s
+
+
+def program_soup(ctx, program, num_tris=300, width=96, height=80, seed=51, prim="tri", blend=A.BLEND_OFF,
+                 depth_test=A.DEPTH_TEST_LESS_THAN, depth_mask=A.DEPTH_MASK_ON, color_type=A.COLOR_RGBA_8U,
+                 depth_type=A.COLOR_R_FLOAT, alpha_ref=0.3, depth_scale=0.5, depth_bias=0.25, screen_door=3,
+                 clear_depth=1.0, num_instances=1):
+    """A triangle soup drawn as filled triangles, wireframe, lines or points
+    with one of the programs that need the ordered raster: the alpha-cutout
+    program (SLG_PROGRAM_VCOLOR_TEX_CUTOUT: discards where vertex alpha x
+    texel alpha < alpha_ref, over a texture with varying alpha) or the
+    fragment-coordinate program (SLG_PROGRAM_FRAG_COORD: colour from x, y and
+    depth, screen-door discard, depth written as depth * scale + bias)."""
+    s = S.Scene(ctx, f"prog_{program}_{seed}", width, height, color_type=color_type, depth_type=depth_type)
+    verts, proj = S.soup_triangles(num_tris, width, height, seed=seed)
+    mesh = s.add_mesh(verts, None, stride=36)
+    mesh.mode = {"tri": A.RENDER_MODE_TRIANGLES, "wire": A.RENDER_MODE_TRI_WIRE,
+                 "line": A.RENDER_MODE_LINES, "point": A.RENDER_MODE_POINTS}[prim]
+    if program == A.PROGRAM_VCOLOR_TEX_CUTOUT:
+        tex = s.add_texture_rgba8(S.to_rgba8(S.value_noise(32, 32, seed=seed, octaves=2)))
+        ub = S.cutout_uniforms(proj, tex, alpha_ref)
+    else:
+        ub = S.fragcoord_uniforms(proj, 1.0 / width, 1.0 / height, depth_scale, depth_bias, screen_door)
+    sh = s.add_shader(program, 2, ub, cull=A.CULL_OFF, depth_test=depth_test, depth_mask=depth_mask, blend=blend)
+    s.draws.append((mesh, num_instances, sh))
+    s.num_triangles = num_tris
+    s.clear_depth = clear_depth
+    return s

@@ -71,6 +71,26 @@ SCENES = {
                                                       clear_depth=0.1, seed=23)),
     "wire_double_depth": (E.random_soup, dict(depth_type=A.COLOR_R_DOUBLE, wire=True, seed=24)),
     "lines_half_depth": (E.random_lines, dict(depth_type=A.COLOR_R_HALF, seed=25)),
+    # fragment programs that discard (SL_FragmentShader returning false: no
+    # colour, depth still written) and that read / write SL_FragCoordXYZ
+    "cutout_soup": (E.program_soup, dict(program=A.PROGRAM_VCOLOR_TEX_CUTOUT)),
+    "cutout_soup_blend_alpha": (E.program_soup, dict(program=A.PROGRAM_VCOLOR_TEX_CUTOUT, blend=A.BLEND_ALPHA, seed=52)),
+    "cutout_soup_depth_off": (E.program_soup, dict(program=A.PROGRAM_VCOLOR_TEX_CUTOUT, depth_test=A.DEPTH_TEST_OFF,
+                                                   alpha_ref=0.2, seed=53)),
+    "cutout_wire": (E.program_soup, dict(program=A.PROGRAM_VCOLOR_TEX_CUTOUT, prim="wire", seed=54)),
+    "cutout_lines_instanced": (E.program_soup, dict(program=A.PROGRAM_VCOLOR_TEX_CUTOUT, prim="line", seed=55,
+                                                    num_instances=2)),
+    "cutout_points": (E.program_soup, dict(program=A.PROGRAM_VCOLOR_TEX_CUTOUT, prim="point", seed=56, num_tris=1000)),
+    "fragcoord_soup_float": (E.program_soup, dict(program=A.PROGRAM_FRAG_COORD, color_type=A.COLOR_RGBA_FLOAT, seed=57)),
+    "fragcoord_soup_greater_nodoor": (E.program_soup, dict(program=A.PROGRAM_FRAG_COORD, depth_test=A.DEPTH_TEST_GREATER_THAN,
+                                                           clear_depth=-1.0, screen_door=0, depth_scale=-1.0,
+                                                           depth_bias=0.0, seed=58)),
+    "fragcoord_wire_half_depth": (E.program_soup, dict(program=A.PROGRAM_FRAG_COORD, prim="wire", depth_type=A.COLOR_R_HALF,
+                                                       seed=59)),
+    "fragcoord_lines_float": (E.program_soup, dict(program=A.PROGRAM_FRAG_COORD, prim="line", color_type=A.COLOR_RGBA_FLOAT,
+                                                   seed=60)),
+    "fragcoord_points_float": (E.program_soup, dict(program=A.PROGRAM_FRAG_COORD, prim="point", color_type=A.COLOR_RGBA_FLOAT,
+                                                    seed=61, num_tris=1000)),
 }
 
 # every colour format: four per scene through the G-buffer program, unblended

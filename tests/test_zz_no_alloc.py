@@ -167,11 +167,12 @@ def test_device_status_reported_at_finish(ctx):
     """A blended wireframe triangle whose pixels are revisited after 600
     queued fragments is reported at slg_finish (SLG_ERR_OVERFLOW), through
     draw_noalloc as through draw."""
-    s = S.Scene(ctx, "wire_queue_small", 700, 40)
-    pts = [(20.0, 4.0), (680.0, 4.0), (350.0, 36.0)]
+    # 1024 x 64 pixels: 32 x 2 tiles of 32 x 32, the most the static scratch takes
+    s = S.Scene(ctx, "wire_queue_small", 1024, 64)
+    pts = [(30.0, 1.0), (994.0, 1.0), (515.0, 63.0)]
     verts = np.zeros((3, 9), np.float32)
     for i, (x, y) in enumerate(pts):
-        verts[i, :3] = (2.0 * x / 700 - 1.0, 2.0 * y / 40 - 1.0, 0.5)
+        verts[i, :3] = (2.0 * x / 1024 - 1.0, 2.0 * y / 64 - 1.0, 0.5)
     mesh = s.add_mesh(verts, None, stride=36)
     mesh.mode = A.RENDER_MODE_TRI_WIRE
     sh = s.add_shader(A.PROGRAM_FLAT_COLOR, 0, S.flat_uniforms(np.eye(4), (0.3, 0.2, 0.1, 0.5)),
