@@ -236,6 +236,8 @@ struct slg_context
     uint64_t cacheCap = 0;
     DevBuffer tileCount, tileOffset, tileCursor, entries, status;
     DevBuffer blitBuf;      /* destination of slg_blit_read */
+    DevBuffer rankOf, recOfRank, seqRec, seqKey, binBlocks;   /* blend order of a multi-mesh draw */
+    uint64_t rankCap = 0;
     uint64_t slotCap = 0, ovfCap = 0, tileCap = 0, entryCap = 0;
 
     /* draw descriptors: pinned host ring mirrored to a device ring */
@@ -953,7 +955,7 @@ struct LaunchHook
 };
 
 int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fboId, bool batch = false,
-               const LaunchHook* hook = nullptr)
+               const LaunchHook* hook = nullptr, bool multiple = false)
 {
     if (fboId >= ctx->fbos.size()) return ctx->fail(SLG_ERR_INVALID_ID, "invalid fbo id");
     const Fbo& fbo = ctx->fbos[fboId];
@@ -1124,6 +1126,34 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
 
     if ((r = bind_visibility(ctx, fbo, f))) return r;
 
+    /* one draw_multiple call over several meshes with blending: the
+     * reference's flush groups interleave the meshes by primIndex */
+    bool flushSort = multiple && n >= 2 && descs[0].blend != SLG_BLEND_OFF;
+    for (size_t i = 0; i < n; ++i)
+    {
+        if (descs[i].prim != slg::kPrimTriangle && descs[i].prim != slg::kPrimWire) flushSort = false;
+    }
+    if (flushSort && numSlots > 0)
+    {
+        const uint64_t recs = ctx->slotCap + ctx->ovfCap;
+        const uint64_t blocks = (numSlots + 1023) / 1024;
+        if (recs > ctx->rankCap)
+        {
+            if ((r = dev_alloc(ctx, ctx->rankOf, recs * sizeof(uint32_t), false))) return r;
+            if ((r = dev_alloc(ctx, ctx->recOfRank, recs * sizeof(uint32_t), false))) return r;
+            if ((r = dev_alloc(ctx, ctx->seqRec, recs * sizeof(uint32_t), false))) return r;
+            if ((r = dev_alloc(ctx, ctx->seqKey, recs * sizeof(unsigned long long), false))) return r;
+            ctx->rankCap = recs;
+        }
+        if ((r = dev_alloc(ctx, ctx->binBlocks, (blocks + 1) * sizeof(uint32_t), false))) return r;
+        f.rankOf = static_cast<uint32_t*>(ctx->rankOf.ptr);
+        f.recOfRank = static_cast<uint32_t*>(ctx->recOfRank.ptr);
+        f.seqRec = static_cast<uint32_t*>(ctx->seqRec.ptr);
+        f.seqKey = static_cast<unsigned long long*>(ctx->seqKey.ptr);
+        f.binBlocks = static_cast<uint32_t*>(ctx->binBlocks.ptr);
+        f.rankGrid = (uint32_t)std::min<uint64_t>((recs + 1023) / 1024, 152 * 4);
+    }
+
     if (batch && ctx->batchGraphs && !ctx->profileStages && !hook)
     {
         return launch_batch_graph(ctx, f, descs, starts, n, ops);
@@ -1145,6 +1175,35 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
 }
 
 bool id_ok(size_t id, size_t n) { return id < n; }
+
+/* The mode a mesh of draw_multiple is drawn with: the processor and raster
+ * mode of the first mesh, the index use of its own mode. */
+uint32_t multiple_mesh_mode(uint32_t first, uint32_t own)
+{
+    switch (first)
+    {
+        case SLG_RENDER_MODE_TRIANGLES:
+        case SLG_RENDER_MODE_INDEXED_TRIANGLES:
+        {
+            const bool indexed = own == SLG_RENDER_MODE_INDEXED_TRIANGLES || own == SLG_RENDER_MODE_INDEXED_TRI_WIRE;
+            return indexed ? SLG_RENDER_MODE_INDEXED_TRIANGLES : SLG_RENDER_MODE_TRIANGLES;
+        }
+        case SLG_RENDER_MODE_TRI_WIRE:
+        case SLG_RENDER_MODE_INDEXED_TRI_WIRE:
+        {
+            const bool indexed = own == SLG_RENDER_MODE_INDEXED_TRIANGLES || own == SLG_RENDER_MODE_INDEXED_TRI_WIRE;
+            return indexed ? SLG_RENDER_MODE_INDEXED_TRI_WIRE : SLG_RENDER_MODE_TRI_WIRE;
+        }
+        case SLG_RENDER_MODE_LINES:
+        case SLG_RENDER_MODE_INDEXED_LINES:
+            return own == SLG_RENDER_MODE_INDEXED_LINES ? SLG_RENDER_MODE_INDEXED_LINES : SLG_RENDER_MODE_LINES;
+        case SLG_RENDER_MODE_POINTS:
+        case SLG_RENDER_MODE_INDEXED_POINTS:
+            return own == SLG_RENDER_MODE_INDEXED_POINTS ? SLG_RENDER_MODE_INDEXED_POINTS : SLG_RENDER_MODE_POINTS;
+        default:
+            return own;
+    }
+}
 
 /*-----------------------------------------------------------------------------
  * Scene graph helpers
@@ -1365,6 +1424,7 @@ void slg_context_destroy(slg_context* ctx)
                             &ctx->cachePos, &ctx->cacheVary, &ctx->recVerts,
                             &ctx->tileCount, &ctx->tileOffset,
                             &ctx->tileCursor, &ctx->entries, &ctx->blitBuf,
+                            &ctx->rankOf, &ctx->recOfRank, &ctx->seqRec, &ctx->seqKey, &ctx->binBlocks,
                             &ctx->status, &ctx->devDescs, &ctx->devStarts};
     for (DevBuffer* b : scratch) dev_free(*b);
     if (ctx->graph.exec) cudaGraphExecDestroy(ctx->graph.exec);
@@ -1789,8 +1849,18 @@ int slg_draw_multiple(slg_context* ctx, const slg_mesh* meshes, size_t numMeshes
 {
     if (!meshes || !numMeshes) return SLG_OK;
     std::vector<DrawRequest> reqs(numMeshes);
-    for (size_t i = 0; i < numMeshes; ++i) reqs[i] = {meshes[i], 1, shaderId, 0};
-    return run_launch(ctx, reqs, fboId);
+    for (size_t i = 0; i < numMeshes; ++i)
+    {
+        /* SL_ProcessorPool::run_shader_processors picks the processor and
+         * the raster mode from the first mesh (softlight/src/
+         * SL_ProcessorPool.cpp:333-357); each mesh only decides whether
+         * its elements are indices (SL_TriProcessor.cpp:686-712,
+         * SL_LineProcessor.cpp:207, SL_PointProcessor.cpp:77) */
+        slg_mesh m = meshes[i];
+        m.mode = multiple_mesh_mode(meshes[0].mode, meshes[i].mode);
+        reqs[i] = {m, 1, shaderId, 0};
+    }
+    return run_launch(ctx, reqs, fboId, false, nullptr, true);
 }
 
 int slg_draw_batch(slg_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, size_t fboId)

@@ -216,6 +216,16 @@ struct Frame
     /* optional visibility map (order-free raster only): per pixel written,
      * 1 + the launch slot (triangle) of the winning fragment; null: off */
     uint32_t* ids;
+
+    /* blend order of a multi-mesh draw (flush_sort_kernel): when recOfRank
+     * is set, tile-list keys are ranks in the reference's rasterisation
+     * order and recOfRank maps a rank to its record; null otherwise */
+    uint32_t* rankOf;             /* per record: its rank */
+    uint32_t* recOfRank;          /* per rank: the record */
+    uint32_t* seqRec;             /* per bin in push order: the record */
+    unsigned long long* seqKey;   /* per bin in push order: primIndex */
+    uint32_t* binBlocks;          /* per 1024 slots: bins, then their exclusive scan; [numBlocks] = all bins */
+    uint32_t  rankGrid;           /* CTAs of flush_sort_kernel */
 };
 
 enum StatusBits

@@ -135,7 +135,9 @@ __global__ void __launch_bounds__(256) bin_fill_kernel(const Frame f)
     {
         tr = tile_range(f.records[slot * kRecordVec4 + 6], f);
     }
-    const uint32_t key = (uint32_t)(slot << kSubShift);
+    /* the ordering key: slot << 3 | sub, or the record's rank in a launch
+     * whose order flush_sort_kernel computed */
+    const uint32_t key = f.rankOf ? ((info == 1) ? f.rankOf[slot] : 0u) : (uint32_t)(slot << kSubShift);
     warp_tile_walk(f, tr, info == 1, f.tileCursor, [&](uint32_t, uint32_t pos) {
         if (pos < f.entryCap) f.entries[pos] = key;
     });
@@ -144,8 +146,161 @@ __global__ void __launch_bounds__(256) bin_fill_kernel(const Frame f)
         const uint32_t base = f.slotOvf[slot];
         for (uint32_t s = 0; s < info - 2; ++s)
         {
-            fill_record(f, f.numSlots + base + s, key | (s + 1));
+            const uint64_t rec = f.numSlots + base + s;
+            fill_record(f, rec, f.rankOf ? f.rankOf[rec] : (key | (s + 1)));
         }
+    }
+}
+
+/*-----------------------------------------------------------------------------
+ * Blend order of a multi-mesh draw. With blending, SL_VertexProcessor::
+ * flush_rasterizer (softlight/src/SL_VertexProcessor.cpp:84-181) stable-sorts
+ * each group of SL_SHADER_MAX_BINNED_PRIMS (1024) consecutive bins by
+ * primIndex before rasterising it. primIndex is a triangle's element index
+ * within its mesh (softlight/src/SL_TriProcessor.cpp:546-547,626-630), so
+ * in a draw_multiple over several meshes the sort interleaves the meshes.
+ * Here the bins are numbered in push order (a scan of the per-slot bin
+ * counts), each group is sorted by (primIndex, position in the group), and
+ * the tile lists hold each record's rank in that order.
+-----------------------------------------------------------------------------*/
+constexpr int kFlushGroup = 1024;   /* SL_SHADER_MAX_BINNED_PRIMS */
+constexpr int kBinBlock = 1024;     /* slots per block of the bin numbering */
+
+__device__ __forceinline__ uint32_t slot_bins(uint32_t info) { return (info == 1) ? 1u : (info >= 2 ? info - 2u : 0u); }
+
+/* Block-wide exclusive scan of one value per thread (1024 threads); returns
+ * the thread's exclusive prefix and sets total. */
+__device__ __forceinline__ uint32_t block_scan_1024(uint32_t v, uint32_t* sWarp, uint32_t& total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += n;
+    }
+    if (lane == 31) sWarp[warp] = incl;
+    __syncthreads();
+    if (warp == 0)
+    {
+        uint32_t w = sWarp[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= o) w += n;
+        }
+        sWarp[lane] = w;
+    }
+    __syncthreads();
+    total = sWarp[31];
+    const uint32_t excl = (warp ? sWarp[warp - 1] : 0u) + incl - v;
+    __syncthreads();
+    return excl;
+}
+
+/* bins per block of 1024 slots */
+__global__ void __launch_bounds__(kBinBlock) bin_block_sums_kernel(const Frame f)
+{
+    __shared__ uint32_t sWarp[32];
+    const uint64_t slot = (uint64_t)blockIdx.x * kBinBlock + threadIdx.x;
+    const uint32_t b = (slot < f.numSlots) ? slot_bins(f.slotInfo[slot]) : 0u;
+    uint32_t total;
+    (void)block_scan_1024(b, sWarp, total);
+    if (threadIdx.x == 0) f.binBlocks[blockIdx.x] = total;
+}
+
+/* exclusive scan of the block sums in place (one CTA); [numBlocks] = total */
+__global__ void __launch_bounds__(1024) bin_block_scan_kernel(const Frame f, uint32_t numBlocks)
+{
+    __shared__ uint32_t sWarp[32];
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < numBlocks; base += 1024)
+    {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t v = (i < numBlocks) ? f.binBlocks[i] : 0u;
+        uint32_t total;
+        const uint32_t excl = block_scan_1024(v, sWarp, total);
+        if (i < numBlocks) f.binBlocks[i] = carry + excl;
+        carry += total;
+    }
+    if (threadIdx.x == 0) f.binBlocks[numBlocks] = carry;
+}
+
+__device__ __forceinline__ unsigned long long record_prim_index(const Frame& f, uint64_t rec)
+{
+    const float4 r7 = f.records[rec * kRecordVec4 + 7];
+    return ((unsigned long long)__float_as_uint(r7.z) << 32) | __float_as_uint(r7.y);
+}
+
+/* every bin's record and primIndex at its push-order number */
+__global__ void __launch_bounds__(kBinBlock) bin_seq_kernel(const Frame f)
+{
+    __shared__ uint32_t sWarp[32];
+    const uint64_t slot = (uint64_t)blockIdx.x * kBinBlock + threadIdx.x;
+    const uint32_t info = (slot < f.numSlots) ? f.slotInfo[slot] : 0u;
+    uint32_t total;
+    const uint32_t seq = f.binBlocks[blockIdx.x] + block_scan_1024(slot_bins(info), sWarp, total);
+    if (info == 1)
+    {
+        f.seqRec[seq] = (uint32_t)slot;
+        f.seqKey[seq] = record_prim_index(f, slot);
+    }
+    else if (info >= 2)
+    {
+        /* the clipped fan's records, in the reference's push order */
+        const uint32_t base = f.slotOvf[slot];
+        for (uint32_t s = 0; s < info - 2; ++s)
+        {
+            const uint64_t rec = f.numSlots + base + s;
+            f.seqRec[seq + s] = (uint32_t)rec;
+            f.seqKey[seq + s] = record_prim_index(f, rec);
+        }
+    }
+}
+
+/* One CTA per group of 1024 bins (grid-stride over the groups): stable sort
+ * by primIndex, i.e. by (primIndex, position), then each record's rank. */
+__global__ void __launch_bounds__(1024) flush_sort_kernel(const Frame f, uint32_t numBlocks)
+{
+    __shared__ unsigned long long sKey[kFlushGroup];
+    const uint32_t total = f.binBlocks[numBlocks];
+    for (uint32_t g0 = blockIdx.x * kFlushGroup; g0 < total; g0 += gridDim.x * kFlushGroup)
+    {
+        const uint32_t n = min((uint32_t)kFlushGroup, total - g0);
+        for (uint32_t i = threadIdx.x; i < kFlushGroup; i += blockDim.x)
+        {
+            sKey[i] = (i < n) ? ((f.seqKey[g0 + i] << 10) | i) : ~0ull;
+        }
+        __syncthreads();
+        for (int k = 2; k <= kFlushGroup; k <<= 1)
+        {
+            for (int j = k >> 1; j > 0; j >>= 1)
+            {
+                for (int i = threadIdx.x; i < kFlushGroup; i += blockDim.x)
+                {
+                    const int ixj = i ^ j;
+                    if (ixj > i)
+                    {
+                        const unsigned long long a = sKey[i], b = sKey[ixj];
+                        if ((a > b) == ((i & k) == 0))
+                        {
+                            sKey[i] = b;
+                            sKey[ixj] = a;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (uint32_t p = threadIdx.x; p < n; p += blockDim.x)
+        {
+            const uint32_t rec = f.seqRec[g0 + (uint32_t)(sKey[p] & (kFlushGroup - 1))];
+            f.rankOf[rec] = g0 + p;
+            f.recOfRank[g0 + p] = rec;
+        }
+        __syncthreads();
     }
 }
 
@@ -401,6 +556,14 @@ cudaError_t launch_pipeline(const Frame& f, const slg_pipeline_ops& ops, int key
     }
     cudaError_t e = (cudaError_t)ops.launch_vertex(&f, s);
     if (e != cudaSuccess) return e;
+    if (f.rankOf && f.numSlots > 0)
+    {
+        const uint32_t numBlocks = (uint32_t)((f.numSlots + kBinBlock - 1) / kBinBlock);
+        bin_block_sums_kernel<<<numBlocks, kBinBlock, 0, s>>>(f);
+        bin_block_scan_kernel<<<1, 1024, 0, s>>>(f, numBlocks);
+        bin_seq_kernel<<<numBlocks, kBinBlock, 0, s>>>(f);
+        flush_sort_kernel<<<f.rankGrid, 1024, 0, s>>>(f, numBlocks);
+    }
     if (ev) cudaEventRecord(ev[1], s);
     tile_scan_kernel<<<1, 1024, 0, s>>>(f, numTiles);
     if (ev) cudaEventRecord(ev[2], s);

@@ -1342,6 +1342,10 @@ __device__ __forceinline__ void emit_extra_outputs(const Frame& f, const DrawDes
 
 __device__ __forceinline__ uint64_t key_to_record(const Frame& f, uint32_t key)
 {
+    if (f.recOfRank)
+    {
+        return f.recOfRank[key];
+    }
     const uint64_t slot = key >> kSubShift;
     const uint32_t sub = key & ((1u << kSubShift) - 1u);
     return (sub == 0) ? slot : (f.numSlots + f.slotOvf[slot] + (sub - 1));

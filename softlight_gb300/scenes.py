@@ -344,7 +344,10 @@ class Scene:
             ctx.clear_framebuffer(self.fbo, 0, self.clear_color, self.clear_depth)
             for k in range(1, len(self.attachments)):
                 ctx.clear_color_buffer(self.fbo, k, self.clear_color)
-        if self.batched:
+        if getattr(self, "multiple", False):
+            # one SL_Context::draw_multiple call over every mesh, with the first draw's shader
+            ctx.draw_multiple([m for (m, _, _) in self.draws], self.draws[0][2], self.fbo)
+        elif self.batched:
             cmds = [A.DrawCmd(m, n, s) for (m, n, s) in self.draws]
             ctx.draw_batch(cmds, self.fbo)
         else:

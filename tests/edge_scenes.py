@@ -410,3 +410,34 @@ def program_soup(ctx, program, num_tris=300, width=96, height=80, seed=51, prim=
     s.num_triangles = num_tris
     s.clear_depth = clear_depth
     return s
+
+
+def multi_mesh(ctx, num_tris=700, num_meshes=3, width=128, height=96, seed=91, blend=A.BLEND_ALPHA,
+               modes=None, depth_test=A.DEPTH_TEST_LESS_THAN):
+    """One SL_Context::draw_multiple call over several triangle soups of the
+    same size, so their primIndex ranges (element indices within each mesh)
+    overlap: with blending, the reference's flush groups of 1024 bins are
+    sorted by primIndex and interleave the meshes. `modes` gives each mesh's
+    render mode (the first mesh's decides the processor and raster mode;
+    indexed modes get an identity-permuted index buffer)."""
+    s = S.Scene(ctx, f"multi_mesh_{seed}", width, height)
+    tex = s.add_texture_rgba8(S.to_rgba8(S.value_noise(32, 32, seed=seed, octaves=2, alpha=1.0)))
+    proj = None
+    for k in range(num_meshes):
+        verts, proj = S.soup_triangles(num_tris, width, height, seed=seed + k)
+        mode = modes[k] if modes else A.RENDER_MODE_TRIANGLES
+        indexed = mode in (A.RENDER_MODE_INDEXED_TRIANGLES, A.RENDER_MODE_INDEXED_TRI_WIRE)
+        idx = np.random.default_rng(seed + 10 + k).permutation(verts.shape[0]).astype(np.uint32) if indexed else None
+        if idx is not None:
+            inv = np.empty_like(idx)
+            inv[idx] = np.arange(idx.size, dtype=np.uint32)
+            verts, idx = verts[idx], inv
+        mesh = s.add_mesh(verts, idx, stride=36)
+        mesh.mode = mode
+        s.draws.append((mesh, 1, None))
+    sh = s.add_shader(A.PROGRAM_VCOLOR_TEX_ALPHA, 2, S.vcolor_uniforms(proj, tex), cull=A.CULL_OFF, blend=blend,
+                      depth_test=depth_test)
+    s.draws = [(m, 1, sh) for (m, _, _) in s.draws]
+    s.multiple = True
+    s.num_triangles = num_tris * num_meshes
+    return s

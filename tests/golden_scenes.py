@@ -91,6 +91,16 @@ SCENES = {
                                                    seed=60)),
     "fragcoord_points_float": (E.program_soup, dict(program=A.PROGRAM_FRAG_COORD, prim="point", color_type=A.COLOR_RGBA_FLOAT,
                                                     seed=61, num_tris=1000)),
+    # draw_multiple over meshes with overlapping primIndex ranges: blended,
+    # the reference's 1024-bin flush groups are sorted by primIndex
+    "multi_mesh_blend_alpha": (E.multi_mesh, dict()),
+    "multi_mesh_blend_additive_le": (E.multi_mesh, dict(blend=A.BLEND_ADDITIVE, depth_test=A.DEPTH_TEST_LESS_EQUAL, seed=92,
+                                                        num_meshes=4, num_tris=500)),
+    "multi_mesh_wire_blend": (E.multi_mesh, dict(modes=(A.RENDER_MODE_TRI_WIRE, A.RENDER_MODE_TRI_WIRE, A.RENDER_MODE_TRI_WIRE),
+                                                 seed=93)),
+    "multi_mesh_mixed_modes_blend": (E.multi_mesh, dict(modes=(A.RENDER_MODE_TRIANGLES, A.RENDER_MODE_INDEXED_TRI_WIRE,
+                                                               A.RENDER_MODE_INDEXED_TRIANGLES), seed=94)),
+    "multi_mesh_opaque": (E.multi_mesh, dict(blend=A.BLEND_OFF, seed=95)),
 }
 
 # every colour format: four per scene through the G-buffer program, unblended
