@@ -27,6 +27,10 @@
 #include "../include/slg_programs.h"
 
 #include <algorithm>
+#include <condition_variable>
+#include <functional>
+#include <memory>
+#include <mutex>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
@@ -203,6 +207,69 @@ struct SloScene
     std::vector<size_t> materials;             /* ambient texture per material */
 };
 
+/* A fixed set of host threads, kept by the context, that run one phase
+ * function at a time: run(fn) calls fn(t) on thread t for every t (the
+ * calling thread takes t = 0) and returns when all have finished, like the
+ * reference's persistent processor pool (SL_ProcessorPool.cpp:280-380). */
+class WorkerPool
+{
+  public:
+    explicit WorkerPool(unsigned n) : mN(n)
+    {
+        for (unsigned t = 1; t < n; ++t) mThreads.emplace_back([this, t]() { loop(t); });
+    }
+    ~WorkerPool()
+    {
+        {
+            std::lock_guard<std::mutex> lk(mMutex);
+            mStop = true;
+            ++mGen;
+        }
+        mCv.notify_all();
+        for (std::thread& th : mThreads) th.join();
+    }
+    unsigned size() const { return mN; }
+    void run(const std::function<void(unsigned)>& fn)
+    {
+        {
+            std::lock_guard<std::mutex> lk(mMutex);
+            mFn = fn;
+            mPending = mN - 1;
+            ++mGen;
+        }
+        mCv.notify_all();
+        mFn(0u);
+        std::unique_lock<std::mutex> lk(mMutex);
+        mDone.wait(lk, [this]() { return mPending == 0; });
+    }
+
+  private:
+    void loop(unsigned t)
+    {
+        uint64_t seen = 0;
+        for (;;)
+        {
+            {
+                std::unique_lock<std::mutex> lk(mMutex);
+                mCv.wait(lk, [&]() { return mGen != seen; });
+                seen = mGen;
+                if (mStop) return;
+            }
+            mFn(t);
+            std::lock_guard<std::mutex> lk(mMutex);
+            if (--mPending == 0) mDone.notify_one();
+        }
+    }
+    std::function<void(unsigned)> mFn;
+    unsigned mN;
+    std::vector<std::thread> mThreads;
+    std::mutex mMutex;
+    std::condition_variable mCv, mDone;
+    uint64_t mGen = 0;
+    unsigned mPending = 0;
+    bool mStop = false;
+};
+
 struct slo_context
 {
     std::string err;
@@ -216,7 +283,7 @@ struct slo_context
     std::vector<Shader> shaders;
     std::vector<SloScene> scenes;
     uint64_t lastBins = 0, lastFrags = 0;
-    std::vector<Bin> lastBinList; /* bins of the last draw group, kept for debugging */
+    std::unique_ptr<WorkerPool> pool;   /* host threads of the multi-threaded mode */
 
     ~slo_context()
     {
@@ -237,7 +304,10 @@ namespace
  * (softlight/include/softlight/SL_Sampler.hpp:97-115,187-218) */
 static inline float wrap_repeat(float uvw)
 {
-    return (uvw < 0.f ? 1.f : 0.f) + std::fmod(uvw, 1.f);
+    /* fmod(uvw, 1) as uvw - trunc(uvw): exact for every binary32 input
+     * (Sterbenz for |uvw| >= 1, trunc = 0 below), so the same value as
+     * the reference's fmod at a fraction of its cost */
+    return (uvw < 0.f ? 1.f : 0.f) + (uvw - std::trunc(uvw));
 }
 
 struct BilinearCoords
@@ -974,9 +1044,28 @@ static inline void shade_fragment(const RasterState& rs, const Bin& bin, int x, 
  * branches (SL_ScanlineBounds.hpp:137-186,301-321). Only rows with
  * y % rowStride == rowPhase are drawn (the reference's scan-line
  * interleave across threads, SL_ScanlineBounds.hpp:32-50). */
-static void raster_bin(const RasterState& rs, const Bin& bin, int rowStride, int rowPhase, uint64_t& frags)
+/* The depth texel as the reference reads it, (float)depth_type
+ * (_sl_get_depth_texel, SL_TriRasterizer.cpp:95-101), for a depth type
+ * known at compile time. */
+template <int DepthType>
+static inline float depth_texel(const uint8_t* depth, size_t i)
 {
-    const Shader& sh = *rs.shaders[bin.drawIndex];
+    if (DepthType == SLG_COLOR_R_HALF) { uint16_t h; std::memcpy(&h, depth + 2 * i, 2); return slg_half_to_float(h); }
+    if (DepthType == SLG_COLOR_R_DOUBLE) { double d; std::memcpy(&d, depth + 8 * i, 8); return (float)d; }
+    float f;
+    std::memcpy(&f, depth + 4 * i, 4);
+    return f;
+}
+
+/* One bin with the depth type and depth test fixed at compile time, as the
+ * reference instantiates render_triangle_simd per depth functor and type
+ * (SL_TriRasterizer.cpp:965-1068). Four pixels are tested at once into a
+ * mask and the passing ones queued (SL_SHADER_MAX_QUEUED_FRAGS, 600) and
+ * shaded when the queue fills or the bin ends; a bin's pixels are
+ * distinct, so the queue gives the same result as shading at once. */
+template <int DepthType, int Func>
+static void raster_bin_t(const RasterState& rs, const Bin& bin, int rowStride, int rowPhase, uint64_t& frags)
+{
     const V4* pts = bin.screen;
     const int32_t bboxMinY = f2i(lm_min(lm_min(pts[0][1], pts[1][1]), pts[2][1]));
     const int32_t bboxMaxY = f2i(lm_max(lm_max(pts[0][1], pts[1][1]), pts[2][1]));
@@ -1011,6 +1100,10 @@ static void raster_bin(const RasterState& rs, const Bin& bin, int rowStride, int
 
     const V4* bcs = bin.bc;
     const V4 bcX = mulf(bcs[0], 4.f);
+    struct Frag { int32_t x, y; float z; V4 bc; };
+    constexpr unsigned kQueue = 600;   /* SL_SHADER_MAX_QUEUED_FRAGS (SL_Config.hpp:46) */
+    Frag queue[kQueue];
+    unsigned numQueued = 0;
 
     do
     {
@@ -1042,18 +1135,31 @@ static void raster_bin(const RasterState& rs, const Bin& bin, int rowStride, int
                            bcs[0][2] * xf + bcY[2], bcs[0][3] * xf + bcY[3]);
             }
 
+            const size_t rowBase = (size_t)rs.width * (size_t)y;
             do
             {
+                bool pass[4];
+                float z[4];
                 for (int k = 0; k < 4; ++k)
                 {
-                    if (x4[k] < xMax)
+                    z[k] = dot(depth, bc[k]);
+                    const bool in = x4[k] < xMax;
+                    const float d = in ? depth_texel<DepthType>(rs.depth, rowBase + (size_t)x4[k]) : 0.f;
+                    pass[k] = in & depth_cmp(Func, z[k], d);
+                }
+                if (pass[0] | pass[1] | pass[2] | pass[3])
+                {
+                    for (int k = 0; k < 4; ++k)
                     {
-                        const float z = dot(depth, bc[k]);
-                        const float d = dget(rs, (size_t)x4[k] + (size_t)rs.width * y);
-                        if (depth_cmp(sh.depthTest, z, d))
+                        if (pass[k])
                         {
-                            shade_fragment(rs, bin, x4[k], y, z, bc[k], frags);
+                            queue[numQueued++] = {x4[k], y, z[k], bc[k]};
                         }
+                    }
+                    if (numQueued > kQueue - 4)
+                    {
+                        for (unsigned q = 0; q < numQueued; ++q) shade_fragment(rs, bin, queue[q].x, queue[q].y, queue[q].z, queue[q].bc, frags);
+                        numQueued = 0;
                     }
                 }
                 for (int k = 0; k < 4; ++k)
@@ -1068,6 +1174,27 @@ static void raster_bin(const RasterState& rs, const Bin& bin, int rowStride, int
         y += rowStride;
     }
     while (y < bboxMaxY);
+    for (unsigned q = 0; q < numQueued; ++q) shade_fragment(rs, bin, queue[q].x, queue[q].y, queue[q].z, queue[q].bc, frags);
+}
+
+static void raster_bin(const RasterState& rs, const Bin& bin, int rowStride, int rowPhase, uint64_t& frags)
+{
+    const uint8_t func = rs.shaders[bin.drawIndex]->depthTest;
+#define SLO_RASTER_FUNCS(DT)                                                                                     \
+    switch (func)                                                                                                \
+    {                                                                                                            \
+        case SLG_DEPTH_TEST_LESS_THAN:     return raster_bin_t<DT, SLG_DEPTH_TEST_LESS_THAN>(rs, bin, rowStride, rowPhase, frags);     \
+        case SLG_DEPTH_TEST_LESS_EQUAL:    return raster_bin_t<DT, SLG_DEPTH_TEST_LESS_EQUAL>(rs, bin, rowStride, rowPhase, frags);    \
+        case SLG_DEPTH_TEST_GREATER_THAN:  return raster_bin_t<DT, SLG_DEPTH_TEST_GREATER_THAN>(rs, bin, rowStride, rowPhase, frags);  \
+        case SLG_DEPTH_TEST_GREATER_EQUAL: return raster_bin_t<DT, SLG_DEPTH_TEST_GREATER_EQUAL>(rs, bin, rowStride, rowPhase, frags); \
+        case SLG_DEPTH_TEST_EQUAL:         return raster_bin_t<DT, SLG_DEPTH_TEST_EQUAL>(rs, bin, rowStride, rowPhase, frags);         \
+        case SLG_DEPTH_TEST_NOT_EQUAL:     return raster_bin_t<DT, SLG_DEPTH_TEST_NOT_EQUAL>(rs, bin, rowStride, rowPhase, frags);     \
+        default:                           return raster_bin_t<DT, SLG_DEPTH_TEST_OFF>(rs, bin, rowStride, rowPhase, frags);           \
+    }
+    if (rs.depthType == SLG_COLOR_R_HALF) { SLO_RASTER_FUNCS(SLG_COLOR_R_HALF) }
+    if (rs.depthType == SLG_COLOR_R_DOUBLE) { SLO_RASTER_FUNCS(SLG_COLOR_R_DOUBLE) }
+    SLO_RASTER_FUNCS(SLG_COLOR_R_FLOAT)
+#undef SLO_RASTER_FUNCS
 }
 
 /* radix-sort of a flush group by primIndex when blending
@@ -1348,21 +1475,6 @@ static void raster_wire_bin(const RasterState& rs, const Bin& bin, int rowStride
         }
     }
     flush();
-}
-
-static void order_bins(std::vector<Bin>& bins, bool blending)
-{
-    if (!blending)
-    {
-        return;
-    }
-    const size_t group = 1024; /* SL_SHADER_MAX_BINNED_PRIMS (SL_Config.hpp:53) */
-    for (size_t b = 0; b < bins.size(); b += group)
-    {
-        const size_t e = std::min(bins.size(), b + group);
-        std::stable_sort(bins.begin() + b, bins.begin() + e,
-                         [](const Bin& l, const Bin& r) { return l.primIndex < r.primIndex; });
-    }
 }
 
 struct DrawItem
@@ -1729,7 +1841,17 @@ static void clear_color(Texture& t, const double rgba[4], unsigned threads)
         else if (kind == 5) { const float f = (float)rgba[j]; std::memcpy(c, &f, 4); }
         else std::memcpy(c, &rgba[j], 8);
     }
-    for (size_t i = 0; i < n; ++i) std::memcpy(t.bytes.data() + bpt * i, texel, bpt);
+    /* one texel, then the filled prefix doubled: the texel pattern repeats */
+    uint8_t* dst = t.bytes.data();
+    const size_t total = bpt * n;
+    if (total == 0) return;
+    std::memcpy(dst, texel, bpt);
+    for (size_t done = bpt; done < total;)
+    {
+        const size_t c = std::min(done, total - done);
+        std::memcpy(dst + done, dst, c);
+        done += c;
+    }
 }
 
 int slo_clear_color_buffer(slo_context* ctx, size_t fbo, unsigned att, const double rgba[4])
@@ -1924,65 +2046,119 @@ static int run_draws(slo_context* ctx, const std::vector<std::vector<DrawItem>>&
             continue;
         }
 
-        std::vector<Bin> bins;
-
-        for (const Unit& u : units)
-        {
-            const DrawItem& it = group[u.draw];
-            const Vao& vao = ctx->vaos[it.mesh.vaoId];
-            const bool indexed = (it.mesh.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES || it.mesh.mode == SLG_RENDER_MODE_INDEXED_TRI_WIRE);
-            const Ibo* ibo = (indexed && vao.ibo != SLG_INVALID_ID) ? &ctx->ibos[vao.ibo] : nullptr;
-            if (indexed && !ibo) return ctx->fail(SLG_ERR_INVALID_ARG, "indexed draw without index buffer");
-            const size_t begin = it.mesh.elementBegin, end = it.mesh.elementEnd;
-            const size_t numTris = (end > begin) ? (end - begin + 2) / 3 : 0;
-
-            if (nthreads == 1 || numTris < 4096)
-            {
-                process_verts(states[u.draw], ibo, it.mesh, u.instance, begin, end, bins);
-            }
-            else
-            {
-                std::vector<std::vector<Bin>> parts(nthreads);
-                std::vector<std::thread> pool;
-                const size_t per = (numTris + nthreads - 1) / nthreads;
-                for (unsigned t = 0; t < nthreads; ++t)
-                {
-                    const size_t f = begin + std::min(numTris, per * t) * 3;
-                    const size_t l = std::min(end, begin + std::min(numTris, per * (t + 1)) * 3);
-                    pool.emplace_back([&, t, f, l]() { process_verts(states[u.draw], ibo, it.mesh, u.instance, f, l, parts[t]); });
-                }
-                for (std::thread& th : pool) th.join();
-                for (auto& p : parts) bins.insert(bins.end(), p.begin(), p.end());
-            }
-        }
-
-        order_bins(bins, blending);
-        ctx->lastBinList = bins;
-        totalBins += bins.size();
-
+        /* Bins are produced in chunks of whole triangles, each chunk split
+         * into contiguous per-thread slices (concatenated in order), and
+         * rasterised in whole 1024-bin flush groups as they complete
+         * (SL_VertexProcessor::flush_rasterizer, SL_VertexProcessor.cpp:
+         * 84-181): the groups are sorted by primIndex when blending, and
+         * thread t draws rows y % N == t of every bin in order, so each
+         * pixel sees its fragments in the one-thread order. */
         const bool wire = !group.empty() && (group[0].mesh.mode == SLG_RENDER_MODE_TRI_WIRE ||
                                              group[0].mesh.mode == SLG_RENDER_MODE_INDEXED_TRI_WIRE);
-        const auto raster = [&](const Bin& b, int stride, int phase, uint64_t& fr) {
-            if (wire) raster_wire_bin(rs, b, stride, phase, fr);
-            else raster_bin(rs, b, stride, phase, fr);
-        };
-        if (nthreads == 1)
+        struct Slice { size_t unit, first, last; };   /* elements [first, last) of one unit */
+        std::vector<const Ibo*> unitIbo(units.size(), nullptr);
+        std::vector<size_t> unitStart(units.size() + 1, 0);
+        for (size_t k = 0; k < units.size(); ++k)
         {
-            for (const Bin& b : bins) raster(b, 1, 0, totalFrags);
+            const DrawItem& it = group[units[k].draw];
+            const Vao& vao = ctx->vaos[it.mesh.vaoId];
+            const bool indexed = (it.mesh.mode == SLG_RENDER_MODE_INDEXED_TRIANGLES || it.mesh.mode == SLG_RENDER_MODE_INDEXED_TRI_WIRE);
+            unitIbo[k] = (indexed && vao.ibo != SLG_INVALID_ID) ? &ctx->ibos[vao.ibo] : nullptr;
+            if (indexed && !unitIbo[k]) return ctx->fail(SLG_ERR_INVALID_ARG, "indexed draw without index buffer");
+            const size_t begin = it.mesh.elementBegin, end = it.mesh.elementEnd;
+            unitStart[k + 1] = unitStart[k] + ((end > begin) ? (end - begin + 2) / 3 : 0);
         }
-        else
-        {
-            std::vector<uint64_t> frags(nthreads, 0);
-            std::vector<std::thread> pool;
-            for (unsigned t = 0; t < nthreads; ++t)
+        const size_t totalTris = unitStart[units.size()];
+        /* the elements of global triangles [t0, t1), unit by unit */
+        const auto slices_of = [&](size_t t0, size_t t1, std::vector<Slice>& out) {
+            out.clear();
+            size_t k = (size_t)(std::upper_bound(unitStart.begin(), unitStart.end(), t0) - unitStart.begin()) - 1;
+            for (; k < units.size() && unitStart[k] < t1; ++k)
             {
-                pool.emplace_back([&, t]() {
-                    for (const Bin& b : bins) raster(b, (int)nthreads, (int)t, frags[t]);
-                });
+                const size_t a = std::max(t0, unitStart[k]) - unitStart[k];
+                const size_t b = std::min(t1, unitStart[k + 1]) - unitStart[k];
+                if (a >= b) continue;
+                const slg_mesh& m = group[units[k].draw].mesh;
+                out.push_back({k, m.elementBegin + 3 * a, std::min(m.elementEnd, m.elementBegin + 3 * b)});
             }
-            for (std::thread& th : pool) th.join();
-            for (uint64_t f : frags) totalFrags += f;
+        };
+        const size_t chunkTris = std::max<size_t>(4096, 2048 * (size_t)nthreads);
+        /* bins of a chunk stay in the producing thread's vector; `stream`
+         * points at them in stream order. Bins left over past the last whole
+         * flush group are copied to `carry` (fewer than 1024) before the
+         * vectors are reused. */
+        std::vector<std::vector<Bin>> parts(nthreads);
+        std::vector<std::vector<Slice>> partSlices(nthreads);
+        std::vector<Bin> carry, carryNext;
+        std::vector<const Bin*> stream;
+        std::vector<uint64_t> frags(nthreads, 0);
+        size_t chunk0 = 0;
+        bool vertexPhase = true;
+        size_t rasterCount = 0;
+        const auto work = [&](unsigned t) {
+            if (vertexPhase)
+            {
+                parts[t].clear();
+                for (const Slice& sl : partSlices[t])
+                {
+                    const Unit& u = units[sl.unit];
+                    process_verts(states[u.draw], unitIbo[sl.unit], group[u.draw].mesh, u.instance, sl.first, sl.last, parts[t]);
+                }
+                return;
+            }
+            /* a local count: per-thread slots of one vector share cache lines */
+            uint64_t count = 0;
+            for (size_t i = 0; i < rasterCount; ++i)
+            {
+                if (wire) raster_wire_bin(rs, *stream[i], (int)nthreads, (int)t, count);
+                else raster_bin(rs, *stream[i], (int)nthreads, (int)t, count);
+            }
+            frags[t] += count;
+        };
+        if (!ctx->pool || ctx->pool->size() != nthreads) ctx->pool.reset(new WorkerPool(nthreads));
+        WorkerPool& pool = *ctx->pool;
+        while (chunk0 < totalTris || !carry.empty())
+        {
+            stream.clear();
+            for (const Bin& b : carry) stream.push_back(&b);
+            const size_t chunk1 = std::min(totalTris, chunk0 + chunkTris);
+            if (chunk0 < chunk1)
+            {
+                const size_t per = (chunk1 - chunk0 + nthreads - 1) / nthreads;
+                for (unsigned t = 0; t < nthreads; ++t)
+                {
+                    const size_t a = std::min(chunk1, chunk0 + per * t), b = std::min(chunk1, chunk0 + per * (t + 1));
+                    slices_of(a, b, partSlices[t]);
+                }
+                vertexPhase = true;
+                pool.run(work);
+                for (const std::vector<Bin>& p : parts)
+                    for (const Bin& b : p) stream.push_back(&b);
+            }
+            chunk0 = chunk1;
+            /* whole flush groups, or everything at the end of the stream */
+            const size_t flushGroup = 1024; /* SL_SHADER_MAX_BINNED_PRIMS (SL_Config.hpp:53) */
+            rasterCount = (chunk0 < totalTris) ? (stream.size() / flushGroup) * flushGroup : stream.size();
+            if (blending)
+            {
+                /* the stable sort of bin ids (utils::sort_radix) */
+                for (size_t b = 0; b < rasterCount; b += flushGroup)
+                {
+                    std::stable_sort(stream.begin() + b, stream.begin() + std::min(rasterCount, b + flushGroup),
+                                     [](const Bin* l, const Bin* r) { return l->primIndex < r->primIndex; });
+                }
+            }
+            if (rasterCount > 0)
+            {
+                vertexPhase = false;
+                pool.run(work);
+                totalBins += rasterCount;
+            }
+            carryNext.clear();
+            for (size_t i = rasterCount; i < stream.size(); ++i) carryNext.push_back(*stream[i]);
+            carry.swap(carryNext);
         }
+        for (uint64_t f : frags) totalFrags += f;
     }
 
     ctx->lastBins = totalBins;
@@ -2035,22 +2211,6 @@ int slo_draw_batch(slo_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, s
 }
 
 int slo_finish(slo_context*) { return SLG_OK; }
-
-/* Copies the last draw group's bins: per bin 12 floats of screen
- * coordinates (x, y, z, w for the three vertices) and the primIndex as a
- * float. Returns the number of bins available. */
-size_t slo_debug_bins(const slo_context* ctx, float* out, size_t maxBins)
-{
-    const size_t n = ctx->lastBinList.size();
-    for (size_t i = 0; i < n && i < maxBins; ++i)
-    {
-        const Bin& b = ctx->lastBinList[i];
-        for (int v = 0; v < 3; ++v)
-            for (int c = 0; c < 4; ++c) out[i * 13 + v * 4 + c] = b.screen[v][c];
-        out[i * 13 + 12] = (float)b.primIndex;
-    }
-    return n;
-}
 
 void slo_last_stats(const slo_context* ctx, uint64_t* numBins, uint64_t* numFragments)
 {

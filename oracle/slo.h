@@ -62,7 +62,6 @@ int slo_finish(slo_context* ctx);
 /* Statistics of the last draw call: triangles pushed to bins and fragments
  * that passed the depth test. */
 void slo_last_stats(const slo_context* ctx, uint64_t* numBins, uint64_t* numFragments);
-size_t slo_debug_bins(const slo_context* ctx, float* out, size_t maxBins);
 
 #ifdef __cplusplus
 }
