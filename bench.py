@@ -37,6 +37,7 @@ def parse():
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     p.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "sg"])
     p.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-render timing")
+    p.add_argument("--no-extra", action="store_true", help="default workload only: skip the c3 and c4 sub-objects")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     p.add_argument("--ref-seconds", type=float, default=0.0,
@@ -177,13 +178,51 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(workload, kernel):
-    path = os.path.join(ROOT, "profiles", "traffic.json")
+def cpu_calibration(workload):
+    """The port's speed relative to the reference's own sources built here
+    (portable branches, same thread count), from profiles/cpu_calibration.json."""
+    path = os.path.join(ROOT, "profiles", "cpu_calibration.json")
     if not os.path.exists(path):
         return None
     with open(path) as fh:
         d = json.load(fh)
-    return d.get(workload, {}).get(kernel)
+    r = d.get("port_over_reference", {}).get(workload)
+    if r is None:
+        return None
+    return {"port_over_reference_speed": r, "threads": d.get("threads"), "host": d.get("host"),
+            "reference_build": d.get("reference_build"), "source": "profiles/cpu_calibration.json"}
+
+
+def kernel_sources_digest():
+    """SHA-256 (16 hex digits) of the sources the draw-path kernels are built
+    from (softlight_gb300/csrc and include), to tell whether a recorded ncu
+    figure still describes the kernels that run."""
+    import hashlib
+    h = hashlib.sha256()
+    for d in (os.path.join(ROOT, "softlight_gb300", "csrc"), os.path.join(ROOT, "include")):
+        for f in sorted(os.listdir(d)):
+            with open(os.path.join(d, f), "rb") as fh:
+                h.update(f.encode() + b"\0" + fh.read())
+    return h.hexdigest()[:16]
+
+
+def profiled_traffic(workload, kernel):
+    """DRAM bytes per launch of `kernel` at `workload` from an ncu capture
+    (profiles/traffic.json), with where it came from; None when no capture
+    exists or the kernel sources changed since the capture."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None, "no ncu capture recorded"
+    with open(path) as fh:
+        d = json.load(fh)
+    entry = d.get(workload, {}).get(kernel)
+    if entry is None:
+        return None, f"no ncu capture of {kernel} at this workload"
+    if isinstance(entry, dict):
+        if entry.get("sources") != kernel_sources_digest():
+            return None, f"ncu capture {entry.get('capture')} is of other kernel sources ({entry.get('sources')})"
+        return entry["bytes"], f"ncu capture {entry.get('capture')} (dram__bytes_read.sum + dram__bytes_write.sum), kernel sources {entry['sources']}"
+    return None, "ncu capture without a kernel-source digest"
 
 
 def run_reference(args):
@@ -213,12 +252,15 @@ def run_reference(args):
             scene.render()
         fps = args.steps / (time.perf_counter() - t0)
         sample = "full frames, mean over the timed steps"
+    _, frags = oracle.last_stats(ctx)
     line = {"impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / fps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
             "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
                              "sample": sample + "; reference sources cannot be shipped to this host, so the oracle port "
-                                                "(CPU restatement of the reference's portable path) is timed"},
+                                                "(CPU restatement of the reference's portable path) is timed",
+                             "fragments_per_frame": frags, "mfragments_per_s": fps * frags / 1e6,
+                             "calibration": cpu_calibration(args.workload)},
             "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -348,25 +390,17 @@ def launches_per_frame(scene):
     return total
 
 
-def run_gpu(args):
+def time_workload(name, args, sg, torch, flush, world, local, rank, clocks=None, cpu_seconds=0.0):
+    """Times one workload: `args.steps` frames with CUDA events on the
+    context's stream after an L2 flush each, per-stage times, the same
+    frames issued one draw per launch for batched scenes, and the frames end
+    to end through the C ABI from pinned host buffers. Returns a dict of the
+    figures; clocks, when given, samples nvidia-smi during the timed frames."""
     import numpy as np
-    import torch
-    import softlight_gb300 as sg
-
-    rank, world, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    torch.cuda.set_device(local)
-    if args.workload == "sg":
-        raise SystemExit("the scene-graph workload is timed inside the default run (its \"scene_graph\" key); "
-                         "--workload sg is for --impl reference")
-    sg.build()
-    builder, kwargs, cfg = workload_config(args.workload)
+    builder, kwargs, cfg = workload_config(name)
     ctx = sg.Context()
     scene = builder(ctx, **kwargs)
     stream = torch.cuda.ExternalStream(ctx.stream_handle())
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     cmds = [sg.api.DrawCmd(m, n, sh) for (m, n, sh) in scene.draws]
     if args.tile == "auto":
         tw, th, vb = ctx.autotune(cmds, scene.fbo, scene.clear_color, scene.clear_depth)
@@ -406,14 +440,19 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clocks:
+    if clocks is not None:
+        with clocks:
+            step_ms, _ = timed_frames(args.steps, False)
+    else:
         step_ms, _ = timed_frames(args.steps, False)
-        _, stage_ms = timed_frames(max(3, min(args.steps, 10)), True)
+    _, stage_ms = timed_frames(max(3, min(args.steps, 10)), True)
     torch.cuda.synchronize()
     total_ms = max_over_ranks(sum(step_ms), world)
     fps = replica_throughput(world, args.steps, total_ms / 1000.0)
+    out = {"workload": cfg["workload"], "config": cfg, "value": fps, "unit": "frames/s", "ms_per_step": total_ms / args.steps,
+           "tile": f"{tw}x{th}", "vertex_block": vb, "batched_graph": bool(scene.batched),
+           "triangles_per_frame": scene.num_triangles, "launches_per_frame": launches_per_frame(scene)}
 
-    per_draw = None
     if scene.batched:
         # the same frames issued as one slg_draw call per mesh
         scene.batched = False
@@ -421,18 +460,20 @@ def run_gpu(args):
             scene.render()
         pd_ms, _ = timed_frames(args.steps, False)
         scene.batched = True
-        per_draw = {"value": args.steps / (sum(pd_ms) / 1000.0), "unit": "frames/s",
-                    "launches_per_frame": 2 + 6 * len(scene.draws),
-                    "batched_speedup": (sum(pd_ms) / max(total_ms, 1e-9))}
+        out["per_draw"] = {"value": args.steps / (sum(pd_ms) / 1000.0), "unit": "frames/s",
+                           "launches_per_frame": 2 + 6 * len(scene.draws),
+                           "batched_speedup": (sum(pd_ms) / max(total_ms, 1e-9))}
 
-    # end to end through the C ABI with pinned host buffers
-    ubos = []
+    # end to end through the C ABI with pinned host buffers: every uniform
+    # block of the frame (one slg_ubo_assign_many call), the instance
+    # matrices, the frame, and the colour attachment read back
     h2d = 0
-    for ubo_id, ubo_bytes in scene.frame_ubos:
-        ubo_host = torch.empty(len(ubo_bytes), dtype=torch.uint8, pin_memory=True).numpy()
-        ubo_host[:] = np.frombuffer(ubo_bytes, dtype=np.uint8)
-        ubos.append((ubo_id, ubo_host))
-        h2d += len(ubo_bytes)
+    ubo_ids = [u for u, _ in scene.frame_ubos]
+    nbytes = max(len(b) for _, b in scene.frame_ubos)
+    ubo_host = torch.zeros(len(ubo_ids), nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+    for k, (_, b) in enumerate(scene.frame_ubos):
+        ubo_host[k, :len(b)] = np.frombuffer(b, dtype=np.uint8)
+    h2d += ubo_host.nbytes
     inst = getattr(scene, "instance_matrices", None)
     if inst is not None:
         inst_host = torch.empty(inst[1].nbytes, dtype=torch.uint8, pin_memory=True).numpy()
@@ -450,16 +491,16 @@ def run_gpu(args):
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for ubo_id, ubo_host in ubos:
-            ctx.ubo_assign(ubo_id, ubo_host)
+        ctx.ubo_assign_many(ubo_ids, ubo_host)
         if inst is not None:
             ctx.vbo_assign(inst[0], inst_host)
         scene.render()
         read_color()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
-    e2e_fps = replica_throughput(world, args.steps, e2e_s)
+    out["e2e"] = {"value": replica_throughput(world, args.steps, e2e_s), "unit": "frames/s", "h2d_bytes_per_step": h2d,
+                  "d2h_bytes_per_step": color_bytes}
 
-    # roofline of the dominant kernel
+    # roofline of the dominant stage
     stages = np.asarray(stage_ms)
     mean_stage = stages.mean(0)
     names = ["vs_setup", "tile_scan", "bin_fill", "raster"]
@@ -469,39 +510,76 @@ def run_gpu(args):
     frame_bytes = geo + scene.texture_bytes + scene.framebuffer_bytes()
     peak, peak_kind = measured_peaks()
     achieved = algo[names[dom]] / (mean_stage[dom] / 1000.0) / 1e9
-    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": profiled_traffic(args.workload, names[dom]),
-                "algorithmic_bytes": algo[names[dom]], "kernel_ms": float(mean_stage[dom]),
-                "stage_ms": {n: float(v) for n, v in zip(names, mean_stage)},
-                "frame_algorithmic_bytes": frame_bytes,
-                "frame_frac": frame_bytes / (total_ms / args.steps / 1000.0) / 1e9 / peak}
+    traffic, traffic_note = profiled_traffic(name, names[dom])
+    out["roofline"] = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                       "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic, "traffic_source": traffic_note,
+                       "algorithmic_bytes": algo[names[dom]], "kernel_ms": float(mean_stage[dom]),
+                       "stage_ms": {n: float(v) for n, v in zip(names, mean_stage)},
+                       "frame_algorithmic_bytes": frame_bytes,
+                       "frame_frac": frame_bytes / (total_ms / args.steps / 1000.0) / 1e9 / peak}
+    ctx.close()
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_subprocess(args.workload, args.cpu_sample_seconds)
+    if rank == 0 and world == 1 and cpu_seconds > 0:
+        cpu = cpu_baseline_subprocess(name, cpu_seconds)
+        out["cpu_baseline"] = cpu
+        frags = cpu.get("fragments_per_frame")
+        if frags:
+            out["fragments_per_frame"] = frags
+            out["mfragments_per_s"] = fps * frags / 1e6
+            out["mfragments_source"] = ("fragments passing the depth test per frame in the reference's sequential "
+                                        "model (oracle count of the same frame; the GPU frame is bit-exact to it)")
+    return out
+
+
+def run_gpu(args):
+    import torch
+    import softlight_gb300 as sg
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    if args.workload == "sg":
+        raise SystemExit("the scene-graph workload is timed inside the default run (its \"scene_graph\" key); "
+                         "--workload sg is for --impl reference")
+    sg.build()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    cpu_s = 0.0 if args.no_cpu_baseline else args.cpu_sample_seconds
+    clocks = ClockSampler(local)
+    head = time_workload(args.workload, args, sg, torch, flush, world, local, rank, clocks=clocks,
+                         cpu_seconds=cpu_s if rank == 0 and world == 1 else 0.0)
+    extra = {}
+    if args.workload == "c2" and not args.no_extra:
+        # the hard 1080p configuration (2M blended soup) and the batched 2160p
+        # scene, each with its own CPU baseline
+        for name in ("c3", "c4"):
+            extra[name] = time_workload(name, args, sg, torch, flush, world, local, rank,
+                                        cpu_seconds=min(cpu_s, 10.0) if rank == 0 and world == 1 else 0.0)
 
     if rank == 0:
-        cfg = dict(cfg)
-        cfg.update({"l2": "flushed between timed frames (256 MiB write)", "tile": f"{tw}x{th}",
-                    "vertex_block": vb, "tuned": args.tile == "auto", "batched_graph": bool(scene.batched),
-                    "triangles_per_frame": scene.num_triangles})
-        line = {"metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        cfg = dict(head["config"])
+        cfg.update({"l2": "flushed between timed frames (256 MiB write)", "tile": head["tile"],
+                    "vertex_block": head["vertex_block"], "tuned": args.tile == "auto", "batched_graph": head["batched_graph"],
+                    "triangles_per_frame": head["triangles_per_frame"]})
+        line = {"metric": METRIC, "value": head["value"], "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": cfg,
-                "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d,
-                        "d2h_bytes_per_step": color_bytes},
-                "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks.summary(),
-                "gpu_launches": args.steps * (launches_per_frame(scene))}
-        if per_draw is not None:
-            line["per_draw"] = per_draw
+                "config": cfg, "e2e": head["e2e"], "roofline": head["roofline"],
+                "cpu_baseline": head.get("cpu_baseline"), "clocks": clocks.summary(),
+                "gpu_launches": args.steps * head["launches_per_frame"]}
+        for k in ("fragments_per_frame", "mfragments_per_s", "mfragments_source", "per_draw"):
+            if k in head:
+                line[k] = head[k]
+        for name, d in extra.items():
+            d = dict(d)
+            d.pop("config", None)
+            line[name] = d
         if not args.no_adjoint and world == 1:
             line["adjoint"] = adjoint_timing(sg, torch, flush, max(args.steps, 5), args.warmup)
             line["scene_graph"] = scene_graph_timing(sg, torch, flush, max(args.steps, 5), args.warmup,
                                                      0 if args.no_cpu_baseline else min(10.0, args.cpu_sample_seconds))
         print(json.dumps(line), flush=True)
-    ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 

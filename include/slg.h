@@ -256,6 +256,14 @@ int    slg_fbo_attach_depth_buffer(slg_context* ctx, size_t fboId, size_t texId)
 size_t slg_create_ubo(slg_context* ctx);
 int    slg_ubo_assign(slg_context* ctx, size_t uboId, const void* data, size_t numBytes);
 
+/* slg_ubo_assign for many blocks in one call: block k (numBytes bytes at
+ * blocks + k * blockStride) into uboIds[k]. No single reference
+ * counterpart: it replaces a caller loop of SL_UniformBuffer writes (one
+ * per draw of a frame, softlight/tests/sl_large_scene_test.cpp:690-720).
+ * All ids are checked before any block is written. */
+int    slg_ubo_assign_many(slg_context* ctx, const size_t* uboIds, size_t count, const void* blocks, size_t blockStride,
+                           size_t numBytes);
+
 /* SL_Context::create_shader (softlight/src/SL_Context.cpp:488-606): same
  * validation, SLG_INVALID_ID where the reference returns (size_t)-1. */
 size_t slg_create_shader(slg_context* ctx, const slg_vertex_shader* vs,

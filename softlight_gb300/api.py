@@ -166,6 +166,7 @@ _GPU_SIGNATURES = [
     ("autotune", C.c_int, [C.c_void_p, C.POINTER(DrawCmd), C.c_size_t, C.c_size_t, C.POINTER(C.c_double),
                            C.c_double, C.POINTER(C.c_int)]),
     ("draw_noalloc", C.c_int, [C.c_void_p, C.POINTER(Mesh), C.c_size_t, C.c_size_t]),
+    ("ubo_assign_many", C.c_int, [C.c_void_p, C.POINTER(C.c_size_t), C.c_size_t, C.c_void_p, C.c_size_t, C.c_size_t]),
     ("register_programs", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(ProgramInfo), C.c_size_t]),
     ("fbo_enable_visibility", C.c_int, [C.c_void_p, C.c_size_t, C.c_int]),
     ("fbo_read_visibility", C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t]),
@@ -401,6 +402,12 @@ class SLContext:
         self._call("scene_draw", scene, fbo, shader, p.ctypes.data_as(C.POINTER(C.c_float)),
                    v.ctypes.data_as(C.POINTER(C.c_float)),
                    cp.ctypes.data_as(C.POINTER(C.c_float)) if cp is not None else None)
+
+    def ubo_assign_many(self, ids, blocks):
+        """slg_ubo_assign_many: blocks is a C-contiguous uint8 array of shape
+        (len(ids), numBytes); row k goes to uniform block ids[k]."""
+        arr = (C.c_size_t * len(ids))(*ids)
+        self._call("ubo_assign_many", arr, len(ids), blocks.ctypes.data_as(C.c_void_p), blocks.strides[0], blocks.shape[1])
 
     def register_programs(self, ops_ptr, programs):
         """slg_register_programs: ops_ptr is the address of an

@@ -1731,6 +1731,24 @@ int slg_ubo_assign(slg_context* ctx, size_t id, const void* data, size_t numByte
     return SLG_OK;
 }
 
+int slg_ubo_assign_many(slg_context* ctx, const size_t* ids, size_t count, const void* blocks, size_t blockStride, size_t numBytes)
+{
+    if (!count) return SLG_OK;
+    if (!ids || !blocks || numBytes > 1024 || blockStride < numBytes) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid ubo blocks");
+    for (size_t k = 0; k < count; ++k)
+        if (!id_ok(ids[k], ctx->ubos.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid ubo id");
+    if (!numBytes) return SLG_OK;
+    const uint8_t* src = static_cast<const uint8_t*>(blocks);
+    for (size_t k = 0; k < count; ++k)
+    {
+        Ubo& u = ctx->ubos[ids[k]];
+        std::memcpy(u.shadow, src + k * blockStride, numBytes);
+        if (!u.pending) ctx->uboPending.push_back(ids[k]);
+        u.pending = std::max<uint32_t>(u.pending, (uint32_t)numBytes);
+    }
+    return SLG_OK;
+}
+
 size_t slg_create_shader(slg_context* ctx, const slg_vertex_shader* vs, const slg_fragment_shader* fs, size_t ubo)
 {
     if (!vs || !fs) return ctx->fail_id("null shader");
