@@ -460,6 +460,18 @@ int slg_set_tile_size(slg_context* ctx, int tileW, int tileH);
 int slg_profile_stages(slg_context* ctx, int enable);
 int slg_stage_times(slg_context* ctx, float ms[4]);
 
+/* Capacities of the scratch buffers for the next launches: tile-list
+ * entries, clipped-triangle records and keys of the shared-memory tile sort
+ * (0 keeps a value). A launch that needs more sets a capacity bit, writes
+ * nothing, and the work queued after it is skipped; at the next
+ * synchronisation point (slg_finish, slg_texture_read, ...) the buffer is
+ * grown and the recorded operations are replayed from that launch, so the
+ * frame comes out complete. Normal use never needs this call: buffers start
+ * large and grow on their own. It starts a context small so that the
+ * recovery path can be exercised; a launch with more triangle slots than
+ * any before resets the sizes. */
+int slg_set_scratch_caps(slg_context* ctx, size_t maxEntries, size_t maxClipRecords, unsigned maxSortKeys);
+
 /* Raster strategy: 0 (default) picks the order-free resolve for launches
  * without blending and with one order-independent depth rule, else the
  * ordered per-pixel replay; 1 forces the ordered replay. Both give the same

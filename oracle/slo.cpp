@@ -2394,6 +2394,7 @@ int slo_scene_read_models(slo_context* ctx, size_t sceneId, float* out, size_t n
 int slo_scene_draw(slo_context* ctx, size_t sceneId, size_t fboId, size_t shaderId, const float projection[16],
                    const float view[16], const float cullProjection[16])
 {
+    uint64_t bins = 0, frags = 0;
     SloScene* sc = sg_scene(ctx, sceneId);
     if (!sc) return ctx->fail(SLG_ERR_INVALID_ID, "invalid scene id");
     if (!projection || !view) return ctx->fail(SLG_ERR_INVALID_ARG, "null matrix");
@@ -2449,9 +2450,14 @@ int slo_scene_draw(slo_context* ctx, size_t sceneId, size_t fboId, size_t shader
             u.textureId = (uint32_t)sc->materials[m.materialId];
             std::memcpy(ubo.bytes, &u, sizeof(u));
             status = slo_draw(ctx, &m, shaderId, fboId);
+            bins += ctx->lastBins;
+            frags += ctx->lastFrags;
         }
     }
     std::memcpy(ubo.bytes, &saved, sizeof(saved));
+    /* the statistics of the whole draw list */
+    ctx->lastBins = bins;
+    ctx->lastFrags = frags;
     return status;
 }
 

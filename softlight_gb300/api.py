@@ -166,6 +166,7 @@ _GPU_SIGNATURES = [
     ("autotune", C.c_int, [C.c_void_p, C.POINTER(DrawCmd), C.c_size_t, C.c_size_t, C.POINTER(C.c_double),
                            C.c_double, C.POINTER(C.c_int)]),
     ("draw_noalloc", C.c_int, [C.c_void_p, C.POINTER(Mesh), C.c_size_t, C.c_size_t]),
+    ("set_scratch_caps", C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t, C.c_uint]),
     ("ubo_assign_many", C.c_int, [C.c_void_p, C.POINTER(C.c_size_t), C.c_size_t, C.c_void_p, C.c_size_t, C.c_size_t]),
     ("register_programs", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(ProgramInfo), C.c_size_t]),
     ("fbo_enable_visibility", C.c_int, [C.c_void_p, C.c_size_t, C.c_int]),
@@ -402,6 +403,11 @@ class SLContext:
         self._call("scene_draw", scene, fbo, shader, p.ctypes.data_as(C.POINTER(C.c_float)),
                    v.ctypes.data_as(C.POINTER(C.c_float)),
                    cp.ctypes.data_as(C.POINTER(C.c_float)) if cp is not None else None)
+
+    def set_scratch_caps(self, entries=0, clip_records=0, sort_keys=0):
+        """slg_set_scratch_caps: start the scratch buffers small (overflow
+        recovery tests)."""
+        self._call("set_scratch_caps", entries, clip_records, sort_keys)
 
     def ubo_assign_many(self, ids, blocks):
         """slg_ubo_assign_many: blocks is a C-contiguous uint8 array of shape

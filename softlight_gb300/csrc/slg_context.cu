@@ -63,6 +63,33 @@ struct Shader
     uint32_t vertexBytes;    /* bytes the vertex program reads per vertex at binding 0 */
 };
 
+struct DrawRequest
+{
+    slg_mesh mesh;
+    size_t numInstances;
+    size_t shaderId;
+    uint64_t primBase;
+};
+
+/* An operation that writes a framebuffer or what a later draw reads,
+ * recorded from the last synchronisation point on so that it can be
+ * replayed when a launch overflowed a buffer (settle). */
+struct LogOp
+{
+    enum Kind { kLaunch, kNoalloc, kOpaque, kClearColor, kClearDepth, kBlit, kUbo } kind;
+    std::vector<DrawRequest> reqs;     /* kLaunch */
+    size_t fbo = 0;                    /* kLaunch, kNoalloc, clears */
+    bool batch = false, multiple = false;
+    slg_mesh mesh{};                   /* kNoalloc */
+    size_t shader = 0;
+    unsigned attachment = 0;           /* kClearColor */
+    double value[4] = {0, 0, 0, 0};    /* clear colour, or depth in value[0] */
+    size_t out = 0, in = 0;            /* kBlit */
+    uint16_t rect[8] = {};
+    size_t ubo = 0;                    /* kUbo: the block's bytes before and after */
+    std::vector<uint8_t> before, after;
+};
+
 /* A registered program set (slg_register_programs): its kernels' entry
  * table and its programs. */
 struct ProgramSet
@@ -146,6 +173,7 @@ constexpr size_t kDescRing = 4096;
 constexpr uint64_t kMaxSlots = (1ull << 29) - 1; /* keys are slot << 3 | sub in 32 bits */
 constexpr int kMaxLineExtent = 10922;            /* 3 * 10922 < 32768 */
 constexpr uint32_t kAliasCap = 4096;             /* line address aliases per launch */
+constexpr size_t kLogCap = 4096;                 /* recorded operations before a launch settles them */
 constexpr uint64_t kMaxCacheEntries = 1ull << 25; /* vertex-cache entries per launch (80 B each) */
 constexpr uint64_t kMinCachedSlots = 1ull << 16;  /* smaller launches run the programs per corner */
 
@@ -211,6 +239,14 @@ struct slg_context
     std::vector<Shader> shaders;
     std::vector<Scene> scenes;
     std::vector<ProgramSet> programSets;   /* registered caller program sets */
+
+    /* operations since the last synchronisation point (settle) */
+    std::vector<LogOp> log;
+    bool replaying = false;
+    uint32_t aliasCap = kAliasCap;     /* line-alias events per launch */
+    uint64_t ovfWant = 0;              /* clipped-triangle records the last overflow needed */
+    bool sortFallback = false;         /* a tile list outgrew the shared-memory sort: keep sortScratch */
+    DevBuffer sortScratch;
 
     /* uniform blocks assigned since the last launch, uploaded together
      * through a ring of pinned staging slots */
@@ -359,10 +395,10 @@ int upload_tables(slg_context* ctx)
 int ensure_scratch(slg_context* ctx, uint64_t numSlots, uint64_t numTiles)
 {
     int r;
-    if (numSlots > ctx->slotCap)
+    if (numSlots > ctx->slotCap || ctx->ovfWant > ctx->ovfCap)
     {
-        const uint64_t cap = std::max<uint64_t>(numSlots, 1u << 16);
-        const uint64_t ovf = std::max<uint64_t>(std::min<uint64_t>(7 * cap, 1u << 22), cap / 2);
+        const uint64_t cap = std::max<uint64_t>(std::max<uint64_t>(numSlots, ctx->slotCap), 1u << 16);
+        const uint64_t ovf = std::max<uint64_t>(std::max<uint64_t>(std::min<uint64_t>(7 * cap, 1u << 22), cap / 2), ctx->ovfWant);
         const uint64_t recs = cap + ovf;
         if ((r = dev_alloc(ctx, ctx->records, recs * slg::kRecordVec4 * sizeof(float4), false))) return r;
         if ((r = dev_alloc(ctx, ctx->varyings, recs * slg::kVaryingVec4 * sizeof(float4), false))) return r;
@@ -383,8 +419,15 @@ int ensure_scratch(slg_context* ctx, uint64_t numSlots, uint64_t numTiles)
     {
         if ((r = dev_alloc(ctx, ctx->ovfCount, sizeof(uint32_t), true))) return r;
         if ((r = dev_alloc(ctx, ctx->clipCount, sizeof(uint32_t), true))) return r;
-        if ((r = dev_alloc(ctx, ctx->aliasEvents, kAliasCap * sizeof(slg::AliasEvent), false))) return r;
         if ((r = dev_alloc(ctx, ctx->aliasCount, sizeof(uint32_t), true))) return r;
+    }
+    if (ctx->aliasEvents.bytes < ctx->aliasCap * sizeof(slg::AliasEvent))
+    {
+        if ((r = dev_alloc(ctx, ctx->aliasEvents, ctx->aliasCap * sizeof(slg::AliasEvent), false))) return r;
+    }
+    if (ctx->sortFallback && ctx->sortScratch.bytes < 2 * ctx->entryCap * sizeof(uint32_t))
+    {
+        if ((r = dev_alloc(ctx, ctx->sortScratch, 2 * ctx->entryCap * sizeof(uint32_t), false))) return r;
     }
     if (numTiles > ctx->tileCap)
     {
@@ -397,53 +440,12 @@ int ensure_scratch(slg_context* ctx, uint64_t numSlots, uint64_t numTiles)
     return SLG_OK;
 }
 
-/* Reads and clears the device status word; grows buffers that overflowed. */
-int check_status(slg_context* ctx)
-{
-    if (!ctx->status.ptr) return SLG_OK;
-    cudaError_t e = cudaMemcpyAsync(ctx->hostStatus, ctx->status.ptr, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) return ctx->cuda_fail(e, "device status read");
-    const int32_t bits = ctx->hostStatus[0];
-    if (!bits) return SLG_OK;
+/* Waits for the queued work and completes it: replays launches that
+ * overflowed a buffer and reports device-side conditions (defined below). */
+int settle(slg_context* ctx);
 
-    const int32_t zero[4] = {0, 0, 0, 0};
-    cudaMemcpy(ctx->status.ptr, zero, sizeof(zero), cudaMemcpyHostToDevice);
-    std::string msg = "device-side status:";
-    if (bits & slg::kStatusEntryOverflow)
-    {
-        const uint64_t want = (uint64_t)ctx->hostStatus[1] * 2;
-        if (want > ctx->entryCap && dev_alloc(ctx, ctx->entries, want * sizeof(uint32_t), false) == SLG_OK) ctx->entryCap = want;
-        msg += " tile entries";
-    }
-    if (bits & slg::kStatusOvfOverflow)
-    {
-        msg += " clipped-triangle records";
-        ctx->slotCap = 0; /* reallocate with a larger overflow region on the next draw */
-        const uint64_t want = (uint64_t)ctx->hostStatus[2];
-        (void)want;
-    }
-    if (bits & slg::kStatusTileOverflow)
-    {
-        msg += " triangles per tile";
-    }
-    if (bits & slg::kStatusAliasOverflow)
-    {
-        msg += " full-width line aliases (at most 4096 per launch, 4096 records per aliased pixel)";
-    }
-    if (bits & slg::kStatusWireQueue)
-    {
-        msg += " blended wireframe triangle revisiting a pixel after 600 queued fragments (queue flush order not reproduced)";
-    }
-    if (bits & slg::kStatusUndeclaredDiscard)
-    {
-        return ctx->fail(SLG_ERR_INVALID_ARG, "device-side status: a fragment program discarded a fragment in a launch that took the "
-                                              "order-free raster; register programs that return false with SLG_PROGRAM_DISCARDS "
-                                              "(the affected pixels keep the wrong colour)");
-    }
-    msg += " (the affected draws were skipped; buffers have been grown)";
-    return ctx->fail(SLG_ERR_OVERFLOW, msg);
-}
+/* Records an operation while launches may still have to be replayed. */
+void log_op(slg_context* ctx, LogOp&& op) { ctx->log.push_back(std::move(op)); }
 
 /* The clear value of a texel of `type` (SL_Context::clear_color_buffer ->
  * sl_match_color_for_type, softlight/src/SL_Color.cpp:137-192): per component
@@ -527,7 +529,8 @@ int clear_texture(slg_context* ctx, size_t texId, const double rgba[4])
     uint32_t v[8];
     if (color_value(t.type, rgba, v)) return ctx->fail(SLG_ERR_INVALID_ARG, "unsupported clear format");
     const uint64_t texels = clear_extent((uint64_t)t.w * t.h, ctx->numThreads);
-    cudaError_t e = slg::launch_clear(static_cast<uint8_t*>(t.buf.ptr), (size_t)texels, (int)t.bpt, v, ctx->stream);
+    cudaError_t e = slg::launch_clear(static_cast<uint8_t*>(t.buf.ptr), (size_t)texels, (int)t.bpt, v,
+                                      static_cast<const int32_t*>(ctx->status.ptr), ctx->stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "clear launch");
     return SLG_OK;
 }
@@ -708,14 +711,6 @@ int validate_draw(slg_context* ctx, const Shader& sh, const Vao& vao, const slg_
         return ctx->fail(SLG_ERR_INVALID_ARG, "program pair not supported");
     return SLG_OK;
 }
-
-struct DrawRequest
-{
-    slg_mesh mesh;
-    size_t numInstances;
-    size_t shaderId;
-    uint64_t primBase;
-};
 
 /* Colour attachments of the framebuffer into the frame (SL_Framebuffer::
  * build_output_functions, softlight/src/SL_Framebuffer.cpp:1207-1231). A
@@ -961,6 +956,12 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     const Fbo& fbo = ctx->fbos[fboId];
     if (fbo.depth == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "framebuffer has no depth attachment");
     if (reqs.empty()) return SLG_OK;
+    if (ctx->log.size() >= kLogCap && !ctx->replaying)
+    {
+        /* a caller that never synchronises: complete the recorded work */
+        const int settled = settle(ctx);
+        if (settled) return settled;
+    }
     if (reqs.size() + 1 > kDescRing) return ctx->fail(SLG_ERR_INVALID_ARG, "too many draws in one batch");
 
     /* a launch runs the kernels of one program set: draws whose shaders come
@@ -1118,8 +1119,9 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     {
         f.aliasEvents = static_cast<slg::AliasEvent*>(ctx->aliasEvents.ptr);
         f.aliasCount = static_cast<uint32_t*>(ctx->aliasCount.ptr);
-        f.aliasCap = kAliasCap;
+        f.aliasCap = ctx->aliasCap;
     }
+    f.sortScratch = ctx->sortFallback ? static_cast<uint32_t*>(ctx->sortScratch.ptr) : nullptr;
     set_tables(ctx, f.tables, ctx->texTable.ptr, ctx->bufTable.ptr, ctx->vaoTable.ptr);
 
     f.vsBlock = ctx->vsBlock;
@@ -1154,6 +1156,17 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
         f.rankGrid = (uint32_t)std::min<uint64_t>((recs + 1023) / 1024, 152 * 4);
     }
 
+    /* from here on the launch is queued: a launch with a device-written
+     * draw list (the scene graph's) cannot be replayed */
+    {
+        LogOp op;
+        op.kind = hook ? LogOp::kOpaque : LogOp::kLaunch;
+        if (!hook) op.reqs = reqs;
+        op.fbo = fboId;
+        op.batch = batch;
+        op.multiple = multiple;
+        log_op(ctx, std::move(op));
+    }
     if (batch && ctx->batchGraphs && !ctx->profileStages && !hook)
     {
         return launch_batch_graph(ctx, f, descs, starts, n, ops);
@@ -1377,7 +1390,7 @@ int slg_context_create(slg_context** outCtx)
     if (e == cudaSuccess) e = cudaMalloc(&ctx->devDescs.ptr, kDescRing * sizeof(DrawDesc));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->devStarts.ptr, kDescRing * sizeof(uint64_t));
     /* the device status words (overflow bits and sizes), read and cleared by
-     * check_status; every launch of the context reports into them, the
+     * settle; every launch of the context reports into them, the
      * no-allocation draw included */
     if (e == cudaSuccess) e = cudaMalloc(&ctx->status.ptr, 4 * sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMemset(ctx->status.ptr, 0, 4 * sizeof(int32_t));
@@ -1425,6 +1438,7 @@ void slg_context_destroy(slg_context* ctx)
                             &ctx->tileCount, &ctx->tileOffset,
                             &ctx->tileCursor, &ctx->entries, &ctx->blitBuf,
                             &ctx->rankOf, &ctx->recOfRank, &ctx->seqRec, &ctx->seqKey, &ctx->binBlocks,
+                            &ctx->sortScratch,
                             &ctx->status, &ctx->devDescs, &ctx->devStarts};
     for (DevBuffer* b : scratch) dev_free(*b);
     if (ctx->graph.exec) cudaGraphExecDestroy(ctx->graph.exec);
@@ -1450,6 +1464,12 @@ size_t slg_create_vbo(slg_context* ctx) { ctx->vbos.emplace_back(); ctx->tablesD
 
 int slg_vbo_init(slg_context* ctx, size_t id, size_t numBytes, const void* data)
 {
+    /* queued draws read the old contents: complete them first */
+    if (!ctx->log.empty())
+    {
+        const int settled = settle(ctx);
+        if (settled) return settled;
+    }
     if (!id_ok(id, ctx->vbos.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid vbo id");
     Vbo& v = ctx->vbos[id];
     int r = dev_alloc(ctx, v.buf, numBytes + 64, true);
@@ -1467,6 +1487,12 @@ int slg_vbo_init(slg_context* ctx, size_t id, size_t numBytes, const void* data)
 
 int slg_vbo_assign(slg_context* ctx, size_t id, const void* data, size_t offset, size_t numBytes)
 {
+    /* queued draws read the old contents: complete them first */
+    if (!ctx->log.empty())
+    {
+        const int settled = settle(ctx);
+        if (settled) return settled;
+    }
     if (!id_ok(id, ctx->vbos.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid vbo id");
     Vbo& v = ctx->vbos[id];
     if (offset + numBytes > v.size) return ctx->fail(SLG_ERR_INVALID_ARG, "vbo range");
@@ -1479,6 +1505,12 @@ size_t slg_create_ibo(slg_context* ctx) { ctx->ibos.emplace_back(); return ctx->
 
 int slg_ibo_init(slg_context* ctx, size_t id, size_t numElements, int indexType, const void* data)
 {
+    /* queued draws read the old contents: complete them first */
+    if (!ctx->log.empty())
+    {
+        const int settled = settle(ctx);
+        if (settled) return settled;
+    }
     if (!id_ok(id, ctx->ibos.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid ibo id");
     const size_t ib = index_bytes(indexType);
     if (!ib) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid index type");
@@ -1539,6 +1571,12 @@ size_t slg_create_texture(slg_context* ctx) { ctx->textures.emplace_back(); ctx-
 
 int slg_texture_init(slg_context* ctx, size_t id, int colorType, uint16_t w, uint16_t h, uint16_t d)
 {
+    /* queued draws read the old contents: complete them first */
+    if (!ctx->log.empty())
+    {
+        const int settled = settle(ctx);
+        if (settled) return settled;
+    }
     if (!id_ok(id, ctx->textures.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
     const size_t bpt = bytes_per_color(colorType);
     if (!bpt || !w || !h || !d) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid texture format or size");
@@ -1559,6 +1597,12 @@ int slg_texture_init(slg_context* ctx, size_t id, int colorType, uint16_t w, uin
 
 int slg_texture_set_texels(slg_context* ctx, size_t id, const void* data, size_t numBytes)
 {
+    /* queued draws read the old contents: complete them first */
+    if (!ctx->log.empty())
+    {
+        const int settled = settle(ctx);
+        if (settled) return settled;
+    }
     if (!id_ok(id, ctx->textures.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
     Texture& t = ctx->textures[id];
     if (!t.buf.ptr || numBytes != (size_t)t.w * t.h * t.d * t.bpt) return ctx->fail(SLG_ERR_INVALID_ARG, "texel byte count");
@@ -1573,10 +1617,12 @@ int slg_texture_read(slg_context* ctx, size_t id, void* dst, size_t numBytes)
     if (!id_ok(id, ctx->textures.size())) return ctx->fail(SLG_ERR_INVALID_ID, "invalid texture id");
     Texture& t = ctx->textures[id];
     if (!t.buf.ptr || numBytes != (size_t)t.w * t.h * t.d * t.bpt) return ctx->fail(SLG_ERR_INVALID_ARG, "texel byte count");
+    /* the texels as the queued draws leave them, then the copy */
+    const int r = settle(ctx);
     cudaError_t e = cudaMemcpyAsync(dst, t.buf.ptr, numBytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "texture read");
-    return check_status(ctx);
+    return r;
 }
 
 } // extern "C"
@@ -1639,6 +1685,16 @@ int slg_blit_rect(slg_context* ctx, size_t outId, size_t inId, uint16_t srcX0, u
     a.dst = static_cast<uint8_t*>(dst.buf.ptr);
     a.srcType = src.type;
     a.dstType = dst.type;
+    a.status = static_cast<const int32_t*>(ctx->status.ptr);
+    {
+        LogOp op;
+        op.kind = LogOp::kBlit;
+        op.out = outId;
+        op.in = inId;
+        const uint16_t rect[8] = {srcX0, srcY0, srcX1, srcY1, dstX0, dstY0, dstX1, dstY1};
+        std::memcpy(op.rect, rect, sizeof(rect));
+        log_op(ctx, std::move(op));
+    }
     cudaError_t e = slg::launch_blit(a, ctx->stream);
     return (e == cudaSuccess) ? SLG_OK : ctx->cuda_fail(e, "blit launch");
 }
@@ -1662,6 +1718,8 @@ int slg_blit_read(slg_context* ctx, size_t inId, int dstType, uint16_t dstW, uin
     slg::BlitArgs a;
     int r = blit_geometry(ctx, src, dstW, dstH, 0, 0, src.w, src.h, 0, 0, dstW, dstH, a);
     if (r) return r;
+    if ((r = settle(ctx))) return r;   /* the source as the queued draws leave it */
+    a.status = nullptr;
     if ((r = dev_alloc(ctx, ctx->blitBuf, bytes, false))) return r;
     a.src = static_cast<const uint8_t*>(src.buf.ptr);
     a.dst = static_cast<uint8_t*>(ctx->blitBuf.ptr);
@@ -1671,7 +1729,7 @@ int slg_blit_read(slg_context* ctx, size_t inId, int dstType, uint16_t dstW, uin
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, ctx->blitBuf.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "blit read");
-    return check_status(ctx);
+    return SLG_OK;
 }
 
 size_t slg_create_framebuffer(slg_context* ctx) { ctx->fbos.emplace_back(); return ctx->fbos.size() - 1; }
@@ -1691,6 +1749,12 @@ int slg_fbo_reserve_color_buffers(slg_context* ctx, size_t fbo, unsigned n)
 
 int slg_fbo_attach_color_buffer(slg_context* ctx, size_t fbo, unsigned index, size_t tex)
 {
+    /* queued draws read the old contents: complete them first */
+    if (!ctx->log.empty())
+    {
+        const int settled = settle(ctx);
+        if (settled) return settled;
+    }
     if (!id_ok(fbo, ctx->fbos.size()) || !id_ok(tex, ctx->textures.size()) || index >= ctx->fbos[fbo].numColors)
         return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo attachment");
     ctx->fbos[fbo].colors[index] = tex;
@@ -1699,6 +1763,12 @@ int slg_fbo_attach_color_buffer(slg_context* ctx, size_t fbo, unsigned index, si
 
 int slg_fbo_attach_depth_buffer(slg_context* ctx, size_t fbo, size_t tex)
 {
+    /* queued draws read the old contents: complete them first */
+    if (!ctx->log.empty())
+    {
+        const int settled = settle(ctx);
+        if (settled) return settled;
+    }
     if (!id_ok(fbo, ctx->fbos.size()) || !id_ok(tex, ctx->textures.size())) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo attachment");
     const int dt = ctx->textures[tex].type;
     if (dt != SLG_COLOR_R_HALF && dt != SLG_COLOR_R_FLOAT && dt != SLG_COLOR_R_DOUBLE)
@@ -1725,6 +1795,15 @@ int slg_ubo_assign(slg_context* ctx, size_t id, const void* data, size_t numByte
     if (!id_ok(id, ctx->ubos.size()) || numBytes > 1024 || (!data && numBytes)) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid ubo");
     if (!numBytes) return SLG_OK;
     Ubo& u = ctx->ubos[id];
+    if (!ctx->log.empty())
+    {
+        LogOp op;
+        op.kind = LogOp::kUbo;
+        op.ubo = id;
+        op.before.assign(u.shadow, u.shadow + numBytes);
+        op.after.assign(static_cast<const uint8_t*>(data), static_cast<const uint8_t*>(data) + numBytes);
+        log_op(ctx, std::move(op));
+    }
     std::memcpy(u.shadow, data, numBytes);
     if (!u.pending) ctx->uboPending.push_back(id);
     u.pending = std::max<uint32_t>(u.pending, (uint32_t)numBytes);
@@ -1742,6 +1821,15 @@ int slg_ubo_assign_many(slg_context* ctx, const size_t* ids, size_t count, const
     for (size_t k = 0; k < count; ++k)
     {
         Ubo& u = ctx->ubos[ids[k]];
+        if (!ctx->log.empty())
+        {
+            LogOp op;
+            op.kind = LogOp::kUbo;
+            op.ubo = ids[k];
+            op.before.assign(u.shadow, u.shadow + numBytes);
+            op.after.assign(src + k * blockStride, src + k * blockStride + numBytes);
+            log_op(ctx, std::move(op));
+        }
         std::memcpy(u.shadow, src + k * blockStride, numBytes);
         if (!u.pending) ctx->uboPending.push_back(ids[k]);
         u.pending = std::max<uint32_t>(u.pending, (uint32_t)numBytes);
@@ -1829,12 +1917,27 @@ int slg_clear_color_buffer(slg_context* ctx, size_t fbo, unsigned att, const dou
 {
     if (!id_ok(fbo, ctx->fbos.size()) || att >= ctx->fbos[fbo].numColors || ctx->fbos[fbo].colors[att] == SLG_INVALID_ID)
         return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo attachment");
+    {
+        LogOp op;
+        op.kind = LogOp::kClearColor;
+        op.fbo = fbo;
+        op.attachment = att;
+        for (int k = 0; k < 4; ++k) op.value[k] = rgba[k];
+        log_op(ctx, std::move(op));
+    }
     return clear_texture(ctx, ctx->fbos[fbo].colors[att], rgba);
 }
 
 int slg_clear_depth_buffer(slg_context* ctx, size_t fbo, double depth)
 {
     if (!id_ok(fbo, ctx->fbos.size()) || ctx->fbos[fbo].depth == SLG_INVALID_ID) return ctx->fail(SLG_ERR_INVALID_ARG, "invalid fbo");
+    {
+        LogOp op;
+        op.kind = LogOp::kClearDepth;
+        op.fbo = fbo;
+        op.value[0] = depth;
+        log_op(ctx, std::move(op));
+    }
     const double d[4] = {depth, 0, 0, 0};
     int r = clear_texture(ctx, ctx->fbos[fbo].depth, d);
     if (r || !ctx->fbos[fbo].visEnabled) return r;
@@ -2170,9 +2273,7 @@ int slg_scene_draw(slg_context* ctx, size_t sceneId, size_t fboId, size_t shader
 
 int slg_finish(slg_context* ctx)
 {
-    cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) return ctx->cuda_fail(e, "stream synchronize");
-    return check_status(ctx);
+    return settle(ctx);
 }
 
 void* slg_context_stream(slg_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
@@ -2433,7 +2534,17 @@ extern "C" int slg_draw_noalloc(slg_context* ctx, const slg_mesh* m, size_t shad
     f.vsBlock = ctx->vsBlock;
 
     if (flush_ubos(ctx, false)) return SLG_ERR_CUDA;
-    e = slg::launch_pipeline(f, pipeline_ops(ctx, shader.programSet), ctx->keyCap, ctx->stream, nullptr);
+    {
+        LogOp op;
+        op.kind = LogOp::kNoalloc;
+        op.mesh = *m;
+        op.shader = shaderId;
+        op.fbo = fboId;
+        log_op(ctx, std::move(op));
+    }
+    /* the static scratch bounds a tile list by kNoAllocEntries / tiles; the
+     * shared-memory sort holds that many whatever the context's cap */
+    e = slg::launch_pipeline(f, pipeline_ops(ctx, shader.programSet), std::max(ctx->keyCap, (int)kNoAllocRecords), ctx->stream, nullptr);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "slg_draw_noalloc: launch");
     return SLG_OK;
 }
@@ -2540,10 +2651,11 @@ int slg_fbo_read_visibility(slg_context* ctx, size_t fboId, uint32_t* dst, size_
     const Fbo& fbo = ctx->fbos[fboId];
     if (!fbo.visEnabled) return ctx->fail(SLG_ERR_INVALID_ARG, "framebuffer has no visibility map");
     if (!dst || count * sizeof(uint32_t) > fbo.vis.bytes) return ctx->fail(SLG_ERR_INVALID_ARG, "bad destination size");
+    const int r = settle(ctx);
     cudaError_t e = cudaMemcpyAsync(dst, fbo.vis.ptr, count * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "visibility read");
-    return check_status(ctx);
+    return r;
 }
 
 int slg_diff_shade(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_t fboId, float* image, size_t count)
@@ -2582,3 +2694,170 @@ int slg_draw_adjoint(slg_context* ctx, const slg_mesh* m, size_t shaderId, size_
 }
 
 } // extern "C"
+
+/*-----------------------------------------------------------------------------
+ * Completion and overflow recovery. Scratch buffers are sized from what
+ * earlier launches needed; a launch that needs more than a buffer holds
+ * sets a capacity bit in the status words, writes nothing, and every later
+ * framebuffer write on the stream is skipped while the bit is set. At the
+ * next synchronisation point the host grows the buffer and replays the
+ * recorded operations from the launch that overflowed: the draws come out
+ * as if the buffer had been large enough from the start.
+-----------------------------------------------------------------------------*/
+namespace
+{
+
+/* Grows the buffers whose capacity bits are set in `bits`. */
+int grow_for(slg_context* ctx, int32_t bits, const int32_t* status)
+{
+    int r;
+    if (bits & slg::kStatusEntryOverflow)
+    {
+        const uint64_t want = std::max<uint64_t>((uint64_t)(uint32_t)status[1] + ((uint64_t)(uint32_t)status[1] >> 1), ctx->entryCap + 1);
+        if ((r = dev_alloc(ctx, ctx->entries, want * sizeof(uint32_t), false))) return r;
+        ctx->entryCap = want;
+    }
+    if (bits & slg::kStatusOvfOverflow)
+    {
+        ctx->ovfWant = std::max<uint64_t>((uint64_t)(uint32_t)status[2] + ((uint64_t)(uint32_t)status[2] >> 1), ctx->ovfCap + 1);
+    }
+    if (bits & slg::kStatusTileOverflow)
+    {
+        ctx->sortFallback = true;
+    }
+    if (bits & slg::kStatusAliasOverflow)
+    {
+        ctx->aliasCap *= 4;
+    }
+    if (ctx->sortFallback && ctx->sortScratch.bytes < 2 * ctx->entryCap * sizeof(uint32_t))
+    {
+        if ((r = dev_alloc(ctx, ctx->sortScratch, 2 * ctx->entryCap * sizeof(uint32_t), false))) return r;
+    }
+    if (ctx->aliasEvents.ptr && ctx->aliasEvents.bytes < ctx->aliasCap * sizeof(slg::AliasEvent))
+    {
+        if ((r = dev_alloc(ctx, ctx->aliasEvents, ctx->aliasCap * sizeof(slg::AliasEvent), false))) return r;
+    }
+    return SLG_OK;
+}
+
+int replay(slg_context* ctx, const LogOp& op)
+{
+    switch (op.kind)
+    {
+        case LogOp::kLaunch:     return run_launch(ctx, op.reqs, op.fbo, op.batch, nullptr, op.multiple);
+        case LogOp::kNoalloc:    return slg_draw_noalloc(ctx, &op.mesh, op.shader, op.fbo);
+        case LogOp::kClearColor: return slg_clear_color_buffer(ctx, op.fbo, op.attachment, op.value);
+        case LogOp::kClearDepth: return slg_clear_depth_buffer(ctx, op.fbo, op.value[0]);
+        case LogOp::kBlit:
+            return slg_blit_rect(ctx, op.out, op.in, op.rect[0], op.rect[1], op.rect[2], op.rect[3], op.rect[4], op.rect[5], op.rect[6],
+                                 op.rect[7]);
+        case LogOp::kUbo:        return slg_ubo_assign(ctx, op.ubo, op.after.data(), op.after.size());
+        default:                 return ctx->fail(SLG_ERR_INVALID_ARG, "operation cannot be replayed");
+    }
+}
+
+} // namespace
+
+namespace
+{
+
+int settle(slg_context* ctx)
+{
+    int32_t* hs = ctx->hostStatus;
+    for (int attempt = 0;; ++attempt)
+    {
+        cudaError_t e = cudaMemcpyAsync(hs, ctx->status.ptr, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "device status read");
+        const int32_t bits = hs[0];
+        if (!(bits & slg::kStatusSticky)) break;
+
+        /* the launch that overflowed: the first not counted as done */
+        const uint32_t done = (uint32_t)hs[3];
+        size_t pos = ctx->log.size(), launches = 0;
+        bool opaque = false;
+        for (size_t i = 0; i < ctx->log.size(); ++i)
+        {
+            const LogOp::Kind k = ctx->log[i].kind;
+            if (k == LogOp::kLaunch || k == LogOp::kNoalloc || k == LogOp::kOpaque)
+            {
+                if (launches == done && pos == ctx->log.size()) pos = i;
+                ++launches;
+            }
+            if (pos != ctx->log.size() && k == LogOp::kOpaque) opaque = true;
+        }
+        int r = grow_for(ctx, bits, hs);
+        std::vector<LogOp> ops;
+        if (pos < ctx->log.size()) ops.assign(std::make_move_iterator(ctx->log.begin() + pos), std::make_move_iterator(ctx->log.end()));
+        ctx->log.clear();
+        e = cudaMemsetAsync(ctx->status.ptr, 0, 4 * sizeof(int32_t), ctx->stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "device status reset");
+        if (r) return r;
+        if (opaque || ops.empty() || attempt == 3 || ctx->replaying)
+        {
+            std::string msg = "device-side status:";
+            if (bits & slg::kStatusEntryOverflow) msg += " tile entries";
+            if (bits & slg::kStatusOvfOverflow) msg += " clipped-triangle records";
+            if (bits & slg::kStatusTileOverflow) msg += " triangles per tile";
+            if (bits & slg::kStatusAliasOverflow) msg += " full-width line aliases";
+            msg += opaque ? " (a scene-graph draw list cannot be replayed: the draws from the overflow on were skipped; buffers have been grown)"
+                          : " (the draws from the overflow on were skipped; buffers have been grown)";
+            return ctx->fail(SLG_ERR_OVERFLOW, msg);
+        }
+        /* undo the uniform blocks written after the overflow, then replay */
+        for (size_t i = ops.size(); i--;)
+        {
+            if (ops[i].kind != LogOp::kUbo) continue;
+            Ubo& u = ctx->ubos[ops[i].ubo];
+            std::memcpy(u.shadow, ops[i].before.data(), ops[i].before.size());
+            if (!u.pending) ctx->uboPending.push_back(ops[i].ubo);
+            u.pending = std::max<uint32_t>(u.pending, (uint32_t)ops[i].before.size());
+        }
+        ctx->replaying = true;
+        for (const LogOp& op : ops)
+        {
+            if ((r = replay(ctx, op))) break;
+        }
+        ctx->replaying = false;
+        if (r) return r;
+    }
+    const int32_t bits = hs[0];
+    ctx->log.clear();
+    if (bits || hs[3])
+    {
+        cudaError_t e = cudaMemsetAsync(ctx->status.ptr, 0, 4 * sizeof(int32_t), ctx->stream);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "device status reset");
+    }
+    if (bits & slg::kStatusUndeclaredDiscard)
+    {
+        return ctx->fail(SLG_ERR_INVALID_ARG, "device-side status: a fragment program discarded a fragment in a launch that took the "
+                                              "order-free raster; register programs that return false with SLG_PROGRAM_DISCARDS "
+                                              "(the affected pixels keep the wrong colour)");
+    }
+    if (bits & (slg::kStatusWireQueue | slg::kStatusAliasKeys))
+    {
+        std::string msg = "device-side status:";
+        if (bits & slg::kStatusWireQueue)
+            msg += " blended wireframe triangle revisiting a pixel after 600 queued fragments (queue flush order not reproduced)";
+        if (bits & slg::kStatusAliasKeys) msg += " more than 4096 records cover a full-width line's shared pixel (not replayed)";
+        return ctx->fail(SLG_ERR_OVERFLOW, msg);
+    }
+    return SLG_OK;
+}
+
+} // namespace
+
+extern "C" int slg_set_scratch_caps(slg_context* ctx, size_t maxEntries, size_t maxClipRecords, unsigned maxSortKeys)
+{
+    const int settled = settle(ctx);
+    if (settled) return settled;
+    if (maxEntries)
+    {
+        const int r = dev_alloc(ctx, ctx->entries, maxEntries * sizeof(uint32_t), false);
+        if (r) return r;
+        ctx->entryCap = maxEntries;
+    }
+    if (maxClipRecords) ctx->ovfCap = std::min<uint64_t>(ctx->ovfCap, maxClipRecords);
+    if (maxSortKeys) ctx->keyCap = (int)std::max(2u, std::min(maxSortKeys, 32768u));
+    return SLG_OK;
+}

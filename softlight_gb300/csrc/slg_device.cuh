@@ -226,6 +226,11 @@ struct Frame
     unsigned long long* seqKey;   /* per bin in push order: primIndex */
     uint32_t* binBlocks;          /* per 1024 slots: bins, then their exclusive scan; [numBlocks] = all bins */
     uint32_t  rankGrid;           /* CTAs of flush_sort_kernel */
+
+    /* global-memory sort of tile lists longer than the shared-memory sort
+     * holds: two words per tile entry (the list padded to a power of two at
+     * twice its offset); null until a launch needed it */
+    uint32_t* sortScratch;
 };
 
 enum StatusBits
@@ -235,8 +240,16 @@ enum StatusBits
     kStatusTileOverflow = 4,
     kStatusAliasOverflow = 8,
     kStatusWireQueue = 16,
-    kStatusUndeclaredDiscard = 32   /* a program discarded in an order-free launch */
+    kStatusUndeclaredDiscard = 32,  /* a program discarded in an order-free launch */
+    kStatusAliasKeys = 64           /* more records than the line-alias replay holds cover one pixel */
 };
+
+/* Capacity overflows. Once one is set, every later kernel that writes a
+ * framebuffer skips its work until the host has read the status (at a
+ * synchronisation point), grown the buffer and replayed the launches from
+ * the first that overflowed. status[3] counts the launches that finished
+ * before the first overflow. */
+constexpr int32_t kStatusSticky = kStatusEntryOverflow | kStatusOvfOverflow | kStatusTileOverflow | kStatusAliasOverflow;
 
 /*-----------------------------------------------------------------------------
  * Texture sampling: sl_sample_bilinear<color, SL_WrapMode::REPEAT, ORDERED>

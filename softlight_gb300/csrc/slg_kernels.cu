@@ -316,13 +316,45 @@ __global__ void __launch_bounds__(1024) tile_sort_kernel(const Frame f, int sort
     const int tile = blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
     const uint32_t n = f.tileOffset[tile + 1] - begin;
-    if (n < 2 || (f.status[0] & kStatusEntryOverflow) || !ordered_raster_runs(f))
+    if (n < 2 || (f.status[0] & kStatusSticky) || !ordered_raster_runs(f))
     {
         return;
     }
     if ((int)n > sortCap)
     {
-        if (threadIdx.x == 0) atomicOr(f.status, kStatusTileOverflow);
+        if (!f.sortScratch)
+        {
+            if (threadIdx.x == 0) atomicOr(f.status, kStatusTileOverflow);
+            return;
+        }
+        /* bitonic sort in global memory: the list padded to p <= 2n keys at
+         * twice its offset, so the tiles' regions never overlap */
+        uint32_t* g = f.sortScratch + 2ull * begin;
+        uint32_t p = 2;
+        while (p < n) p <<= 1;
+        for (uint32_t i = threadIdx.x; i < p; i += blockDim.x) g[i] = (i < n) ? f.entries[begin + i] : 0xFFFFFFFFu;
+        __syncthreads();
+        for (uint32_t k = 2; k <= p; k <<= 1)
+        {
+            for (uint32_t j = k >> 1; j > 0; j >>= 1)
+            {
+                for (uint32_t i = threadIdx.x; i < p; i += blockDim.x)
+                {
+                    const uint32_t ixj = i ^ j;
+                    if (ixj > i)
+                    {
+                        const uint32_t a = g[i], b = g[ixj];
+                        if ((a > b) == ((i & k) == 0))
+                        {
+                            g[i] = b;
+                            g[ixj] = a;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) f.entries[begin + i] = g[i];
         return;
     }
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) sKeys[i] = f.entries[begin + i];
@@ -339,8 +371,12 @@ __global__ void __launch_bounds__(1024) tile_sort_kernel(const Frame f, int sort
 -----------------------------------------------------------------------------*/
 struct TexelValue { uint32_t w[8]; };   /* up to 32 bytes of one texel */
 
-__global__ void clear_kernel(uint8_t* dst, size_t numTexels, int bytesPerTexel, TexelValue value)
+__global__ void clear_kernel(uint8_t* dst, size_t numTexels, int bytesPerTexel, TexelValue value, const int32_t* status)
 {
+    if (status && (*status & kStatusSticky))
+    {
+        return;   /* replayed once the launch that overflowed has been */
+    }
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < numTexels; i += stride)
     {
@@ -541,6 +577,14 @@ cudaError_t launch_scene_draw(const SceneDrawArgs& a, cudaStream_t s)
  * One launch: the program set's vertex stage, the library's tile scan, tile
  * lists and tile sort, the program set's raster stage.
 -----------------------------------------------------------------------------*/
+/* After the last kernel that can overflow a buffer: counts the launch as
+ * done when no overflow has happened yet (status[3]), which tells the host
+ * the first launch to replay. */
+__global__ void launch_mark_kernel(int32_t* status)
+{
+    if (!(status[0] & kStatusSticky)) status[3] += 1;
+}
+
 cudaError_t init_library_attributes(int keyCap)
 {
     return cudaFuncSetAttribute(tile_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(uint32_t) * keyCap));
@@ -580,6 +624,7 @@ cudaError_t launch_pipeline(const Frame& f, const slg_pipeline_ops& ops, int key
          * ordered raster runs (ordered_raster_runs) */
         tile_sort_kernel<<<numTiles, 1024, sizeof(uint32_t) * (size_t)keyCap, s>>>(f, keyCap);
     }
+    launch_mark_kernel<<<1, 1, 0, s>>>(f.status);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     e = (cudaError_t)ops.launch_raster(&f, s);
@@ -607,6 +652,10 @@ __device__ __forceinline__ float4 blit_src_rgbaf(const BlitArgs& a, uint64_t i)
 
 __global__ void blit_kernel(const BlitArgs a)
 {
+    if (a.status && (*a.status & kStatusSticky))
+    {
+        return;   /* replayed once the launch that overflowed has been */
+    }
     const uint64_t n = a.nx * a.ny;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride)
@@ -660,12 +709,13 @@ cudaError_t launch_blit(const BlitArgs& a, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[8], cudaStream_t s)
+cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[8], const int32_t* status,
+                         cudaStream_t s)
 {
     TexelValue v;
     for (int k = 0; k < 8; ++k) v.w[k] = value[k];
     const unsigned blocks = (unsigned)std::min<size_t>((numTexels + 255) / 256, 152u * 16u);
-    clear_kernel<<<blocks ? blocks : 1, 256, 0, s>>>(dst, numTexels, bytesPerTexel, v);
+    clear_kernel<<<blocks ? blocks : 1, 256, 0, s>>>(dst, numTexels, bytesPerTexel, v, status);
     return cudaGetLastError();
 }
 

@@ -23,8 +23,10 @@ cudaError_t init_library_attributes(int keyCap);
 /* The entry table of the built-in programs (slg_builtin_vertex.cu). */
 const slg_pipeline_ops& builtin_pipeline();
 
-/* Fill numTexels texels of 4 or 16 bytes with value. */
-cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[8], cudaStream_t s);
+/* Fill numTexels texels of bytesPerTexel bytes with value; skipped while
+ * status (when not null) holds a capacity overflow. */
+cudaError_t launch_clear(uint8_t* dst, size_t numTexels, int bytesPerTexel, const uint32_t value[8], const int32_t* status,
+                         cudaStream_t s);
 
 /* Nearest-neighbour blit of SL_BlitProcessor::blit_nearest over destination
  * pixels [x0, x0 + nx) x [y0, y0 + ny); all reads were checked in bounds. */
@@ -37,6 +39,7 @@ struct BlitArgs
     uint64_t x0, y0, nx, ny;
     uint64_t foutW, foutH;             /* 16.16 source steps per destination pixel */
     uint64_t srcY0, srcY1;
+    const int32_t* status;             /* skipped while it holds a capacity overflow; may be null */
 };
 cudaError_t launch_blit(const BlitArgs& a, cudaStream_t s);
 

@@ -1790,7 +1790,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
     const int tile = blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
     const uint32_t n = f.tileOffset[tile + 1] - begin;
-    if (n == 0 || (f.status[0] & (kStatusEntryOverflow | kStatusTileOverflow)) || !ordered_raster_runs(f))
+    if (n == 0 || (f.status[0] & kStatusSticky) || !ordered_raster_runs(f))
     {
         return;
     }
@@ -2265,7 +2265,7 @@ __global__ void __launch_bounds__(kFreeThreads, kGeneral ? 4 : FreeLayout<TW, TH
     const int tile = blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
     const uint32_t n = f.tileOffset[tile + 1] - begin;
-    if (n == 0 || (f.status[0] & kStatusEntryOverflow) || ordered_raster_runs(f))
+    if (n == 0 || (f.status[0] & kStatusSticky) || ordered_raster_runs(f))
     {
         return;
     }
@@ -2532,7 +2532,7 @@ __global__ void __launch_bounds__(kAliasThreads) alias_fixup_kernel(const Frame 
     __shared__ uint32_t sKeys[kAliasKeys];
     __shared__ uint32_t sCount;
     __shared__ int sSkip;
-    if (f.status[0] & (kStatusEntryOverflow | kStatusTileOverflow))
+    if (f.status[0] & kStatusSticky)
     {
         return;
     }
@@ -2575,7 +2575,7 @@ __global__ void __launch_bounds__(kAliasThreads) alias_fixup_kernel(const Frame 
         const int m = skip ? 0 : (int)sCount;
         if (m > kAliasKeys)
         {
-            if (threadIdx.x == 0) atomicOr(f.status, kStatusAliasOverflow);
+            if (threadIdx.x == 0) atomicOr(f.status, kStatusAliasKeys);
             continue;
         }
         if (!skip)
