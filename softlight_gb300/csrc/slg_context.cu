@@ -1108,6 +1108,21 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     /* a half depth is rounded on every write and re-read by later
      * fragments: the outcome depends on the order, not the set */
     if (f.depthType == SLG_COLOR_R_HALF) f.orderFree = 0;
+    /* the ordered raster's depth bound holds while every pixel's depth moves
+     * one way: one family of depth test, no program writing depth */
+    f.depthBound = 0;
+    {
+        const auto family = [](uint8_t t) {
+            return (t == SLG_DEPTH_TEST_LESS_THAN || t == SLG_DEPTH_TEST_LESS_EQUAL) ? 1
+                 : (t == SLG_DEPTH_TEST_GREATER_THAN || t == SLG_DEPTH_TEST_GREATER_EQUAL) ? 2 : 0;
+        };
+        int32_t fam = family(descs[0].depthTest);
+        for (size_t i = 0; i < n && fam; ++i)
+        {
+            if (family(descs[i].depthTest) != fam || (ctx->shaders[reqs[i].shaderId].fsFlags & SLG_PROGRAM_WRITES_DEPTH)) fam = 0;
+        }
+        f.depthBound = fam;
+    }
     for (size_t i = 0; i < n; ++i)
     {
         /* the reference's Bresenham error term is int16: it stays exact while

@@ -227,6 +227,12 @@ struct Frame
     uint32_t* binBlocks;          /* per 1024 slots: bins, then their exclusive scan; [numBlocks] = all bins */
     uint32_t  rankGrid;           /* CTAs of flush_sort_kernel */
 
+    /* the ordered raster's depth bound (depth_bound_rejects): 1 when every
+     * draw uses LESS / LESS_EQUAL, 2 when every draw uses GREATER /
+     * GREATER_EQUAL, and no fragment program writes depth (the depth of a
+     * pixel then only moves one way); 0 otherwise */
+    int32_t depthBound;
+
     /* global-memory sort of tile lists longer than the shared-memory sort
      * holds: two words per tile entry (the list padded to a power of two at
      * twice its offset); null until a launch needed it */

@@ -1773,6 +1773,53 @@ __device__ __forceinline__ bool ordered_raster_runs(const Frame& f)
     return !f.orderFree || (f.aliasCount != nullptr && *f.aliasCount != 0u);
 }
 
+/* Whether no pixel of one thread's part of a scan-line can pass the depth
+ * test: the pixels xFirst, xFirst + 4, .. <= xLast of row yf, whose stored
+ * depth is at most dMax (dMin for the greater tests). Their depth, as the
+ * walk computes it (chain_begin_span / chain_step / chain_depth), is the
+ * plane z = A x + Cy of the record's barycentric gradients plus rounding;
+ * the plane's extreme over the pixels is at xFirst or xLast, and the
+ * rounding is bounded by the magnitudes the walk meets: the start value
+ * bc0 * xs + (bc1 * y + bc2) (terms of size Binit, a few roundings), then k
+ * additions of 4 * bc0 to values of size at most Bchain (one rounding each,
+ * |error| <= 2^-24 * |value|), then the depth dot product (three roundings
+ * on terms |z_i b_i|). The margin counts each rounding at 2^-21, eight
+ * times the unit roundoff. NaNs make every comparison false: nothing is
+ * rejected. */
+__device__ __forceinline__ bool depth_bound_rejects(const float4* R, float yf, int xs, int xFirst, int xLast, int func, float dMin,
+                                                    float dMax)
+{
+    const float4 r2 = R[2], r3 = R[3], r4 = R[4];
+    const float z0 = r3.w, z1 = r4.w, z2 = R[5].x;
+    const float bx[3] = {r2.x, r2.y, r2.z};
+    const float by[3] = {r3.x * yf + r4.x, r3.y * yf + r4.y, r3.z * yf + r4.z};
+    const float xsf = (float)xs, xaf = (float)xFirst, xbf = (float)xLast;
+    float binit = 0.f, bchain = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+    {
+        const float ri = (i == 0) ? r3.x : (i == 1) ? r3.y : r3.z;
+        const float ci = (i == 0) ? r4.x : (i == 1) ? r4.y : r4.z;
+        binit = fmaxf(binit, fabsf(bx[i] * xsf) + fabsf(ri * yf) + fabsf(ci));
+        bchain = fmaxf(bchain, fmaxf(fabsf(bx[i] * xsf + by[i]), fabsf(bx[i] * xbf + by[i])));
+    }
+    const float A = (z0 * bx[0] + z1 * bx[1]) + z2 * bx[2];
+    const float C = (z0 * by[0] + z1 * by[1]) + z2 * by[2];
+    const float za = A * xaf + C, zb = A * xbf + C;
+    const float k = (float)((xLast - xs) / 4 + 1);
+    const float zs = (fabsf(z0) + fabsf(z1)) + fabsf(z2);
+    const float margin = 4.76837158203125e-07f * zs * (4.f * binit + (k + 8.f) * bchain);   /* 2^-21 */
+    const float lo = fminf(za, zb) - margin, hi = fmaxf(za, zb) + margin;
+    switch (func)
+    {
+        case SLG_DEPTH_TEST_LESS_THAN:     return lo >= dMax;
+        case SLG_DEPTH_TEST_LESS_EQUAL:    return lo > dMax;
+        case SLG_DEPTH_TEST_GREATER_THAN:  return hi <= dMin;
+        case SLG_DEPTH_TEST_GREATER_EQUAL: return hi < dMin;
+        default:                           return false;
+    }
+}
+
 /* kGeneral: the instantiation that carries line and wireframe records and
  * writes several render targets (such launches use kLineTile tiles); the
  * others keep the triangle loop's registers. */
@@ -1826,6 +1873,21 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
     {
         const int cnt = (int)min((uint32_t)L::kBatch, n - b0);
         stage_records<L::kBatch>(f, sKeys + b0, cnt, sRec, sRecKey);
+        /* the depth range of this thread's pixels at the start of the batch:
+         * a bound for the whole batch, since depth only moves one way
+         * (Frame::depthBound) */
+        float dMin = 0.f, dMax = 0.f;
+        if (f.depthBound && rowActive)
+        {
+            dMin = __int_as_float(0x7F800000);
+            dMax = -dMin;
+            for (int x = myX0; x < xLimit; x += 4)
+            {
+                const float d = sDepth[r * L::kStride + (x - x0)];
+                dMin = fminf(dMin, d);
+                dMax = fmaxf(dMax, d);
+            }
+        }
         __syncthreads();
 
         for_band_records(sRec, cnt, bandY0, [&](int ri) {
@@ -1959,12 +2021,28 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 }
                 return;
             }
-            Chain ch;
-            if (!chain_begin(R, yf, myX0, xLimit, ch))
+            const Span sp = scanline_span(R[0], R[1], yf);
+            if (!((uint32_t)sp.xMin < (uint32_t)sp.xMax))
             {
                 return;
             }
             const int depthFunc = flags & 0xF;
+            if (f.depthBound)
+            {
+                const int xEnd = min(sp.xMax, xLimit);
+                const int xs = sp.xMin + ((myX0 - sp.xMin) & 3);
+                const int xFirst = max(xs, myX0);
+                if (xFirst >= xEnd ||
+                    depth_bound_rejects(R, yf, xs, xFirst, xFirst + ((xEnd - 1 - xFirst) & ~3), depthFunc, dMin, dMax))
+                {
+                    return;
+                }
+            }
+            Chain ch;
+            if (!chain_begin_span(R, yf, sp, myX0, xLimit, ch))
+            {
+                return;
+            }
             const bool depthMask = (flags >> 4) & 1;
             const uint32_t drawIndex = __float_as_uint(R[7].x);
             for (; ch.x < ch.xEnd; chain_step(ch))

@@ -441,3 +441,36 @@ def multi_mesh(ctx, num_tris=700, num_meshes=3, width=128, height=96, seed=91, b
     s.multiple = True
     s.num_triangles = num_tris * num_meshes
     return s
+
+
+def sliver_soup(ctx, num_tris=1500, width=320, height=200, seed=121, depth_test=A.DEPTH_TEST_LESS_THAN,
+                blend=A.BLEND_ALPHA, clear_depth=1.0, z_base=0.5, z_spread=1e-4):
+    """Near-degenerate triangles for the ordered raster's depth bound: long
+    slivers (up to the screen's width, 0.01..3 px thick) and small ones,
+    placed directly in clip space (identity transform) with depths packed
+    within z_spread of each other, so the rounding of the walk's
+    barycentrics decides many depth tests."""
+    rng = np.random.default_rng(seed)
+    s = S.Scene(ctx, f"slivers_{seed}", width, height)
+    verts = np.zeros((3 * num_tris, 9), np.float32)
+    for t in range(num_tris):
+        p0 = rng.uniform([-1.1, -1.1], [1.1, 1.1])
+        ang = rng.uniform(0, 2 * math.pi)
+        length = rng.choice([rng.uniform(0.01, 0.2), rng.uniform(0.5, 2.5)])
+        d = length * np.array([math.cos(ang), math.sin(ang)])
+        thick = rng.uniform(0.01, 3.0) * 2.0 / height
+        n = np.array([-d[1], d[0]]) / max(np.linalg.norm(d), 1e-9)
+        p1 = p0 + d
+        p2 = p0 + d * rng.uniform(0.0, 1.0) + n * thick
+        z = z_base + rng.uniform(-z_spread, z_spread, 3)
+        for k, p in enumerate((p0, p1, p2)):
+            verts[3 * t + k, :3] = (p[0], p[1], z[k])
+            verts[3 * t + k, 3:7] = (*rng.uniform(0.0, 1.0, 3), rng.uniform(0.3, 1.0))
+            verts[3 * t + k, 7:9] = rng.uniform(0.0, 1.0, 2)
+    mesh = s.add_mesh(verts, None, stride=36)
+    tex = s.add_texture_rgba8(S.to_rgba8(S.value_noise(32, 32, seed=seed, octaves=2, alpha=1.0)))
+    sh = s.add_shader(A.PROGRAM_VCOLOR_TEX_ALPHA, 2, S.vcolor_uniforms(np.eye(4), tex), cull=A.CULL_OFF,
+                      depth_test=depth_test, blend=blend)
+    s.draws.append((mesh, 1, sh))
+    s.clear_depth = clear_depth
+    return s

@@ -552,3 +552,18 @@ def test_uniform_block_reassigned_between_draws(ctxs):
         s.render(clear=False)
         out.append(s)
     compare_scenes(out[0], out[1], "uniform blocks reassigned")
+
+
+@pytest.mark.parametrize("depth_test,clear_depth", [(A.DEPTH_TEST_LESS_THAN, 1.0), (A.DEPTH_TEST_LESS_EQUAL, 1.0),
+                                                    (A.DEPTH_TEST_GREATER_THAN, 0.0), (A.DEPTH_TEST_GREATER_EQUAL, 0.0)])
+@pytest.mark.parametrize("spread", [1e-4, 1e-6])
+def test_depth_bound_on_slivers(ctxs, depth_test, clear_depth, spread):
+    """The ordered raster skips scan-lines whose depth bound cannot pass;
+    near-degenerate slivers with depths packed within `spread` put the
+    rounding of the walk's barycentrics at the test's edge. Two frames, so
+    the second starts from a depth buffer the first wrote."""
+    g, o = ctxs
+    for seed in (121, 122):
+        sg, so = render_both(E.sliver_soup, g, o, frames=2, seed=seed, depth_test=depth_test, clear_depth=clear_depth,
+                             z_spread=spread)
+        compare_scenes(sg, so, f"slivers {depth_test} spread {spread} seed {seed}")

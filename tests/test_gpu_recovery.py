@@ -102,20 +102,26 @@ def test_batch_graph_overflow_is_replayed(ctxs):
     compare_scenes(sg, so, "batched graph after recovery")
 
 
-def test_scene_graph_overflow_is_reported(gpu_lib):
+def test_scene_graph_overflow_is_reported(gpu_lib, oracle_mod):
     """The scene graph's draw list is written on the device, so its launch
     is not replayed: the overflow is reported at finish with the buffers
-    grown, and the next frame renders in full."""
+    grown, and the next frame renders in full (the scene animates: frame 3
+    is compared with the oracle's frame 3)."""
     g = gpu_lib.Context()
+    o = oracle_mod.Context()
     s = S.build_scene_graph(g, width=160, height=120, groups=3, per_group=3)
+    so = S.build_scene_graph(o, width=160, height=120, groups=3, per_group=3)
     s.render()
     g.finish()
-    want = s.read_color()
     g.set_scratch_caps(entries=64)
     s.render()
     with pytest.raises(A.SLError, match="scene-graph"):
         g.finish()
     s.render()
     g.finish()
-    assert np.array_equal(s.read_color(), want)
+    for _ in range(3):
+        so.render()
+    compare_scenes(s, so, "scene graph after a reported overflow")
+    assert np.array_equal(s.read_models().view(np.uint32), so.read_models().view(np.uint32))
     g.close()
+    o.close()
