@@ -1717,8 +1717,10 @@ struct RasterLayout
     static constexpr int kBatch = 64;            /* records staged per step */
     static constexpr int kPix = TH * kStride;
     static constexpr size_t kRecBytes = sizeof(float4) * kBatch * kRecordVec4;
-    /* ordered path: colour + depth tile, records, record ids, then keys */
-    static constexpr size_t ordered_bytes() { return sizeof(typename Color::stored) * kPix + sizeof(float) * kPix + kRecBytes + 2 * sizeof(uint32_t) * kBatch; }
+    /* ordered path: colour + depth tile, records, record ids, then keys,
+     * then each tile row's depth range (lo, hi) at the start of a batch */
+    static constexpr size_t kRowDOff = sizeof(typename Color::stored) * kPix + sizeof(float) * kPix + kRecBytes + 2 * sizeof(uint32_t) * kBatch;
+    static constexpr size_t ordered_bytes() { return kRowDOff + 2 * sizeof(float) * TH; }
 };
 
 /* Stages records [b0, b0+cnt) of the tile list into shared memory. */
@@ -1736,9 +1738,10 @@ __device__ __forceinline__ void stage_records(const Frame& f, const uint32_t* ke
 
 /* The warp owns rows [bandY0, bandY0 + 8): the 32 lanes test 32 staged
  * records at once against that band and the warp walks only the hits, in
- * order (ballot + find-first-set compaction). */
-template <class Fn>
-__device__ __forceinline__ void for_band_records(const float4* sRec, int cnt, int bandY0, Fn&& fn)
+ * order (ballot + find-first-set compaction). keep(ri, r6) may drop a hit
+ * whose walk can change nothing. */
+template <class Keep, class Fn>
+__device__ __forceinline__ void for_band_records(const float4* sRec, int cnt, int bandY0, Keep&& keep, Fn&& fn)
 {
     const int lane = threadIdx.x & 31;
     for (int base = 0; base < cnt; base += 32)
@@ -1748,7 +1751,7 @@ __device__ __forceinline__ void for_band_records(const float4* sRec, int cnt, in
         if (ri < cnt)
         {
             const float4 r6 = sRec[ri * kRecordVec4 + 6];
-            hit = __float_as_int(r6.x) < bandY0 + 8 && __float_as_int(r6.y) > bandY0;
+            hit = __float_as_int(r6.x) < bandY0 + 8 && __float_as_int(r6.y) > bandY0 && keep(ri, r6);
         }
         unsigned mask = __ballot_sync(0xFFFFFFFFu, hit);
         while (mask)
@@ -1820,6 +1823,60 @@ __device__ __forceinline__ bool depth_bound_rejects(const float4* R, float yf, i
     }
 }
 
+/* Largest screen coordinate for which depth_bound_rect holds: below it the
+ * scan-line span arithmetic errs by far less than a pixel, so every span
+ * lies in the record's [minX - 1, maxX + 1] (screen vertices are whole
+ * pixels: to_screen floors them), as the tile binning also relies on. */
+constexpr int kRectBoundMaxX = 1 << 20;
+
+/* depth_bound_rejects for every thread of a warp at once: whether no pixel
+ * of a triangle record on rows [ya, yb] of columns [xa, xb] can pass, given
+ * the range [dMin, dMax] of the stored depths there. Each walked chain
+ * starts at some xs in [xsMin, xb] (xsMin <= the span's start, >= 0) and
+ * ends by xb; the plane z = A x + B y + C takes its extremes over the
+ * rectangle at its corners, and the rounding terms take the largest start
+ * (|bc0| xb + |bc1| yb + |bc2|) and chain values (the corners of
+ * [xsMin, xb] x [ya, yb], the barycentrics being affine) and the longest
+ * chain, so the margin bounds the one of every thread's walk. */
+__device__ __forceinline__ bool depth_bound_rect(const float4* R, int ya, int yb, int xa, int xb, int xsMin, int func, float dMin,
+                                                 float dMax)
+{
+    const float4 r2 = R[2], r3 = R[3], r4 = R[4];
+    const float z0 = r3.w, z1 = r4.w, z2 = R[5].x;
+    const float bx[3] = {r2.x, r2.y, r2.z};
+    const float ry[3] = {r3.x, r3.y, r3.z};
+    const float rc[3] = {r4.x, r4.y, r4.z};
+    const float yaf = (float)ya, ybf = (float)yb, xaf = (float)xa, xbf = (float)xb, xsf = (float)xsMin;
+    float byA[3], byB[3];
+    float binit = 0.f, bchain = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+    {
+        byA[i] = ry[i] * yaf + rc[i];
+        byB[i] = ry[i] * ybf + rc[i];
+        binit = fmaxf(binit, fabsf(bx[i] * xbf) + fabsf(ry[i] * ybf) + fabsf(rc[i]));
+        bchain = fmaxf(bchain, fmaxf(fmaxf(fabsf(bx[i] * xsf + byA[i]), fabsf(bx[i] * xbf + byA[i])),
+                                     fmaxf(fabsf(bx[i] * xsf + byB[i]), fabsf(bx[i] * xbf + byB[i]))));
+    }
+    const float A = (z0 * bx[0] + z1 * bx[1]) + z2 * bx[2];
+    const float CA = (z0 * byA[0] + z1 * byA[1]) + z2 * byA[2];
+    const float CB = (z0 * byB[0] + z1 * byB[1]) + z2 * byB[2];
+    const float zaa = A * xaf + CA, zba = A * xbf + CA, zab = A * xaf + CB, zbb = A * xbf + CB;
+    const float k = (float)((xb - xsMin) / 4 + 1);
+    const float zs = (fabsf(z0) + fabsf(z1)) + fabsf(z2);
+    const float margin = 4.76837158203125e-07f * zs * (4.f * binit + (k + 8.f) * bchain);   /* 2^-21 */
+    const float lo = fminf(fminf(zaa, zba), fminf(zab, zbb)) - margin;
+    const float hi = fmaxf(fmaxf(zaa, zba), fmaxf(zab, zbb)) + margin;
+    switch (func)
+    {
+        case SLG_DEPTH_TEST_LESS_THAN:     return lo >= dMax;
+        case SLG_DEPTH_TEST_LESS_EQUAL:    return lo > dMax;
+        case SLG_DEPTH_TEST_GREATER_THAN:  return hi <= dMin;
+        case SLG_DEPTH_TEST_GREATER_EQUAL: return hi < dMin;
+        default:                           return false;
+    }
+}
+
 /* kGeneral: the instantiation that carries line and wireframe records and
  * writes several render targets (such launches use kLineTile tiles); the
  * others keep the triangle loop's registers. */
@@ -1833,6 +1890,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
     float*    sDepth = reinterpret_cast<float*>(smem + sizeof(Stored) * L::kPix);
     float4*   sRec   = reinterpret_cast<float4*>(smem + sizeof(Stored) * L::kPix + sizeof(float) * L::kPix);
     uint32_t* sRecKey = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(sRec) + L::kRecBytes);
+    float*    sRowD  = reinterpret_cast<float*>(smem + L::kRowDOff);
 
     const int tile = blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
@@ -1888,9 +1946,56 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 dMax = fmaxf(dMax, d);
             }
         }
+        if (f.depthBound)
+        {
+            /* each tile row's range, for the warp-wide record test */
+            float rowLo = rowActive ? dMin : __int_as_float(0x7F800000);
+            float rowHi = rowActive ? dMax : __int_as_float(0xFF800000);
+            rowLo = fminf(rowLo, __shfl_xor_sync(0xFFFFFFFFu, rowLo, 1));
+            rowHi = fmaxf(rowHi, __shfl_xor_sync(0xFFFFFFFFu, rowHi, 1));
+            rowLo = fminf(rowLo, __shfl_xor_sync(0xFFFFFFFFu, rowLo, 2));
+            rowHi = fmaxf(rowHi, __shfl_xor_sync(0xFFFFFFFFu, rowHi, 2));
+            if (c == 0)
+            {
+                sRowD[2 * r] = rowLo;
+                sRowD[2 * r + 1] = rowHi;
+            }
+        }
         __syncthreads();
 
-        for_band_records(sRec, cnt, bandY0, [&](int ri) {
+        /* a triangle record none of whose pixels in the band can pass the
+         * depth test is dropped for the whole warp (depth_bound_rect over
+         * its rows in the band and its columns in the tile) */
+        const auto keep = [&](int ri, const float4 r6) {
+            if (!f.depthBound)
+            {
+                return true;
+            }
+            const float4* R = sRec + ri * kRecordVec4;
+            const uint32_t flags = __float_as_uint(R[7].w);
+            const int minX = __float_as_int(r6.z), maxX = __float_as_int(r6.w);
+            if ((flags & (kRecordLine | kRecordWire | kRecordPoint)) || maxX >= kRectBoundMaxX || maxX < minX)
+            {
+                return true;
+            }
+            const int ya = max(__float_as_int(r6.x), bandY0);
+            const int yb = min(min(__float_as_int(r6.y), bandY0 + 8), f.height) - 1;
+            const int xsMin = max(minX - 2, 0);
+            const int xa = max(x0, xsMin), xb = min(xLimit - 1, maxX);
+            if (yb < ya || xb < xa)
+            {
+                return false;
+            }
+            float lo = __int_as_float(0x7F800000), hi = __int_as_float(0xFF800000);
+            for (int yy = ya; yy <= yb; ++yy)
+            {
+                lo = fminf(lo, sRowD[2 * (yy - y0)]);
+                hi = fmaxf(hi, sRowD[2 * (yy - y0) + 1]);
+            }
+            return !depth_bound_rect(R, ya, yb, xa, xb, xsMin, flags & 0xF, lo, hi);
+        };
+
+        for_band_records(sRec, cnt, bandY0, keep, [&](int ri) {
             const float4* R = sRec + ri * kRecordVec4;
             const float4 r6 = R[6];
             if (!rowActive || y < __float_as_int(r6.x) || y >= __float_as_int(r6.y))
