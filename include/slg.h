@@ -469,7 +469,9 @@ int slg_stage_times(slg_context* ctx, float ms[4]);
  * frame comes out complete. Normal use never needs this call: buffers start
  * large and grow on their own. It starts a context small so that the
  * recovery path can be exercised; a launch with more triangle slots than
- * any before resets the sizes. */
+ * any before resets the sizes. A sort-key cap also makes blended launches
+ * fill their tile lists by atomics and sort them per tile (otherwise they
+ * are filled in key order and need no sort). */
 int slg_set_scratch_caps(slg_context* ctx, size_t maxEntries, size_t maxClipRecords, unsigned maxSortKeys);
 
 /* Raster strategy: 0 (default) picks the order-free resolve for launches

@@ -176,6 +176,8 @@ constexpr uint32_t kAliasCap = 4096;             /* line address aliases per lau
 constexpr size_t kLogCap = 4096;                 /* recorded operations before a launch settles them */
 constexpr uint64_t kMaxCacheEntries = 1ull << 25; /* vertex-cache entries per launch (80 B each) */
 constexpr uint64_t kMinCachedSlots = 1ull << 16;  /* smaller launches run the programs per corner */
+constexpr uint64_t kMaxBinChunks = 4096;          /* chunks of the key-order tile list fill */
+constexpr uint64_t kMaxChunkCounts = 1ull << 24;  /* tiles x chunks it counts in (64 MB) */
 
 } // namespace
 
@@ -274,6 +276,8 @@ struct slg_context
     DevBuffer blitBuf;      /* destination of slg_blit_read */
     DevBuffer rankOf, recOfRank, seqRec, seqKey, binBlocks;   /* blend order of a multi-mesh draw */
     uint64_t rankCap = 0;
+    DevBuffer chunkCounts, itemKey;    /* tile lists in key order (Frame::chunkCounts) */
+    bool sortKeysCapped = false;       /* slg_set_scratch_caps set a sort-key cap */
     uint64_t slotCap = 0, ovfCap = 0, tileCap = 0, entryCap = 0;
 
     /* draw descriptors: pinned host ring mirrored to a device ring */
@@ -1171,6 +1175,30 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
         f.rankGrid = (uint32_t)std::min<uint64_t>((recs + 1023) / 1024, 152 * 4);
     }
 
+    /* ordered raster: the tile lists are filled in key order (no tile sort)
+     * when the per-chunk tile counts fit kMaxChunkCounts words; a sort-key
+     * cap set for testing keeps the atomic fill and the tile sort */
+    if (!f.orderFree && numSlots > 0 && !ctx->sortKeysCapped)
+    {
+        const uint64_t numTiles = (uint64_t)f.tilesX * f.tilesY;
+        uint64_t chunks = std::min<uint64_t>(kMaxBinChunks, ((numSlots + 255) / 256 + 7) & ~7ull);
+        chunks = std::min<uint64_t>(chunks, (kMaxChunkCounts / numTiles) & ~7ull);
+        if (chunks >= 8)
+        {
+            const uint64_t recs = ctx->slotCap + ctx->ovfCap;
+            const uint64_t blocks = (numSlots + 1023) / 1024;
+            if ((r = dev_alloc(ctx, ctx->seqRec, recs * sizeof(uint32_t), false))) return r;
+            if (!f.rankOf && (r = dev_alloc(ctx, ctx->itemKey, recs * sizeof(uint32_t), false))) return r;
+            if ((r = dev_alloc(ctx, ctx->binBlocks, (blocks + 1) * sizeof(uint32_t), false))) return r;
+            if ((r = dev_alloc(ctx, ctx->chunkCounts, numTiles * chunks * sizeof(uint32_t), false))) return r;
+            f.seqRec = static_cast<uint32_t*>(ctx->seqRec.ptr);
+            f.itemKey = f.rankOf ? nullptr : static_cast<uint32_t*>(ctx->itemKey.ptr);
+            f.binBlocks = static_cast<uint32_t*>(ctx->binBlocks.ptr);
+            f.chunkCounts = static_cast<uint32_t*>(ctx->chunkCounts.ptr);
+            f.binChunks = (uint32_t)chunks;
+        }
+    }
+
     /* from here on the launch is queued: a launch with a device-written
      * draw list (the scene graph's) cannot be replayed */
     {
@@ -1453,7 +1481,7 @@ void slg_context_destroy(slg_context* ctx)
                             &ctx->tileCount, &ctx->tileOffset,
                             &ctx->tileCursor, &ctx->entries, &ctx->blitBuf,
                             &ctx->rankOf, &ctx->recOfRank, &ctx->seqRec, &ctx->seqKey, &ctx->binBlocks,
-                            &ctx->sortScratch,
+                            &ctx->chunkCounts, &ctx->itemKey, &ctx->sortScratch,
                             &ctx->status, &ctx->devDescs, &ctx->devStarts};
     for (DevBuffer* b : scratch) dev_free(*b);
     if (ctx->graph.exec) cudaGraphExecDestroy(ctx->graph.exec);
@@ -2873,6 +2901,10 @@ extern "C" int slg_set_scratch_caps(slg_context* ctx, size_t maxEntries, size_t 
         ctx->entryCap = maxEntries;
     }
     if (maxClipRecords) ctx->ovfCap = std::min<uint64_t>(ctx->ovfCap, maxClipRecords);
-    if (maxSortKeys) ctx->keyCap = (int)std::max(2u, std::min(maxSortKeys, 32768u));
+    if (maxSortKeys)
+    {
+        ctx->keyCap = (int)std::max(2u, std::min(maxSortKeys, 32768u));
+        ctx->sortKeysCapped = true;
+    }
     return SLG_OK;
 }

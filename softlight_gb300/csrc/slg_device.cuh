@@ -227,6 +227,16 @@ struct Frame
     uint32_t* binBlocks;          /* per 1024 slots: bins, then their exclusive scan; [numBlocks] = all bins */
     uint32_t  rankGrid;           /* CTAs of flush_sort_kernel */
 
+    /* tile lists filled in key order (bin_count_ordered_kernel ..
+     * bin_fill_ordered_kernel): the bins in key order are cut into binChunks
+     * chunks, one warp each; chunkCounts (tile-major, numTiles x binChunks)
+     * holds each chunk's entries per tile, then their exclusive scan over the
+     * chunks, then the chunk's running cursor. null: the lists are filled by
+     * atomics and sorted per tile when the ordered raster needs them. */
+    uint32_t* chunkCounts;
+    uint32_t  binChunks;
+    uint32_t* itemKey;            /* per bin in push order: its tile-list key (launches without recOfRank) */
+
     /* the ordered raster's depth bound (depth_bound_rejects): 1 when every
      * draw uses LESS / LESS_EQUAL, 2 when every draw uses GREATER /
      * GREATER_EQUAL, and no fragment program writes depth (the depth of a

@@ -242,10 +242,12 @@ __global__ void __launch_bounds__(kBinBlock) bin_seq_kernel(const Frame f)
     const uint32_t info = (slot < f.numSlots) ? f.slotInfo[slot] : 0u;
     uint32_t total;
     const uint32_t seq = f.binBlocks[blockIdx.x] + block_scan_1024(slot_bins(info), sWarp, total);
+    const uint32_t key = (uint32_t)(slot << kSubShift);
     if (info == 1)
     {
         f.seqRec[seq] = (uint32_t)slot;
-        f.seqKey[seq] = record_prim_index(f, slot);
+        if (f.rankOf) f.seqKey[seq] = record_prim_index(f, slot);
+        if (f.itemKey) f.itemKey[seq] = key;
     }
     else if (info >= 2)
     {
@@ -255,7 +257,8 @@ __global__ void __launch_bounds__(kBinBlock) bin_seq_kernel(const Frame f)
         {
             const uint64_t rec = f.numSlots + base + s;
             f.seqRec[seq + s] = (uint32_t)rec;
-            f.seqKey[seq + s] = record_prim_index(f, rec);
+            if (f.rankOf) f.seqKey[seq + s] = record_prim_index(f, rec);
+            if (f.itemKey) f.itemKey[seq + s] = key | (s + 1);
         }
     }
 }
@@ -302,6 +305,196 @@ __global__ void __launch_bounds__(1024) flush_sort_kernel(const Frame f, uint32_
         }
         __syncthreads();
     }
+}
+
+/*-----------------------------------------------------------------------------
+ * Tile lists in key order for the ordered raster. The bins, taken in key
+ * order (push order, or rank order when flush_sort_kernel ranked them), are
+ * cut into binChunks equal runs, one warp each. A counting pass gives every
+ * (tile, chunk) its entries, a scan over the chunks of each tile gives the
+ * chunk's first position in the tile's list, and the fill pass writes each
+ * chunk's entries there in key order. Both passes expand 32 consecutive bins
+ * at a time into their (bin, tile) entries, in bin order, and deal the
+ * entries to the lanes 32 at a time; lanes holding the same tile are grouped
+ * with __match_any_sync, so a tile's entries of one step take consecutive
+ * positions in lane (= key) order and one lane advances the chunk's cursor.
+ * The lists come out sorted, with no atomics on shared tile cursors and no
+ * tile sort.
+-----------------------------------------------------------------------------*/
+constexpr int kOrderedWarps = 8;   /* chunks (warps) per CTA of the count and fill passes */
+
+__device__ __forceinline__ void bin_item(const Frame& f, uint32_t i, uint32_t& rec, uint32_t& key)
+{
+    if (f.recOfRank)
+    {
+        rec = f.recOfRank[i];
+        key = i;
+    }
+    else
+    {
+        rec = f.seqRec[i];
+        key = f.itemKey[i];
+    }
+}
+
+/* bins [begin, end) of a chunk: equal runs, a multiple of 32 long */
+__device__ __forceinline__ void chunk_bins(const Frame& f, uint32_t numBlocks, uint32_t chunk, uint32_t& begin, uint32_t& end)
+{
+    const uint32_t total = f.binBlocks[numBlocks];
+    const uint32_t per = (((total + f.binChunks - 1) / f.binChunks) + 31u) & ~31u;
+    begin = min(chunk * per, total);
+    end = min(begin + per, total);
+}
+
+struct GroupBins
+{
+    uint32_t start[32];     /* first entry of each bin of the group (exclusive scan) */
+    int4 range[32];         /* (tx0, width, ty0, unused) */
+    uint32_t key[32];
+};
+
+/* Walks the (bin, tile) entries of the chunk's bins in order, 32 per step;
+ * fn(tile, key, peers, valid) runs on every lane of every step (peers: the
+ * lanes of the step holding the same tile). Every lane of the warp calls it. */
+template <class Fn>
+__device__ __forceinline__ void for_chunk_entries(const Frame& f, uint32_t begin, uint32_t end, GroupBins& g, Fn&& fn)
+{
+    const int lane = threadIdx.x & 31;
+    for (uint32_t g0 = begin; g0 < end; g0 += 32)
+    {
+        const uint32_t i = g0 + lane;
+        uint32_t n = 0;
+        int4 rg = make_int4(0, 1, 0, 0);
+        uint32_t key = 0;
+        if (i < end)
+        {
+            uint32_t rec;
+            bin_item(f, i, rec, key);
+            const TileRange t = tile_range(f.records[(size_t)rec * kRecordVec4 + 6], f);
+            if (t.tx1 >= t.tx0 && t.ty1 >= t.ty0)
+            {
+                rg = make_int4(t.tx0, t.tx1 - t.tx0 + 1, t.ty0, 0);
+                n = (uint32_t)rg.y * (uint32_t)(t.ty1 - t.ty0 + 1);
+            }
+        }
+        uint32_t incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        __syncwarp();
+        g.start[lane] = incl - n;
+        g.range[lane] = rg;
+        g.key[lane] = key;
+        __syncwarp();
+        for (uint32_t e0 = 0; e0 < total; e0 += 32)
+        {
+            const uint32_t e = e0 + lane;
+            const bool valid = e < total;
+            uint32_t tile = 0xFFFFFFFFu, k = 0;
+            if (valid)
+            {
+                /* the bin holding entry e: the last one starting at or before e
+                 * (empty bins share their start with the next one) */
+                int lo = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                {
+                    if (lo + step < 32 && g.start[lo + step] <= e) lo += step;
+                }
+                const int4 r = g.range[lo];
+                const uint32_t local = e - g.start[lo];
+                const uint32_t w = (uint32_t)r.y;
+                tile = (uint32_t)((r.z + (int)(local / w)) * f.tilesX + r.x + (int)(local % w));
+                k = g.key[lo];
+            }
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, tile);
+            fn(tile, k, peers, valid);
+            __syncwarp();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kOrderedWarps * 32) bin_count_ordered_kernel(const Frame f, uint32_t numBlocks)
+{
+    __shared__ GroupBins sGroup[kOrderedWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t chunk = blockIdx.x * kOrderedWarps + warp;
+    if (chunk >= f.binChunks || (f.status[0] & kStatusSticky))
+    {
+        return;
+    }
+    uint32_t begin, end;
+    chunk_bins(f, numBlocks, chunk, begin, end);
+    for_chunk_entries(f, begin, end, sGroup[warp], [&](uint32_t tile, uint32_t, uint32_t peers, bool valid) {
+        if (valid && lane == __ffs(peers) - 1)
+        {
+            atomicAdd(f.chunkCounts + (size_t)tile * f.binChunks + chunk, (uint32_t)__popc(peers));
+        }
+    });
+}
+
+/* One CTA per tile: exclusive scan of its chunk counts, in place. */
+__global__ void __launch_bounds__(1024) bin_chunk_scan_kernel(const Frame f)
+{
+    __shared__ uint32_t sWarp[32];
+    if (f.status[0] & kStatusSticky)
+    {
+        return;
+    }
+    uint32_t* row = f.chunkCounts + (size_t)blockIdx.x * f.binChunks;
+    const uint32_t n = f.binChunks;
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < n; base += 4096)
+    {
+        const uint32_t i0 = base + 4 * threadIdx.x;
+        uint32_t c[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) c[k] = (i0 + k < n) ? row[i0 + k] : 0u;
+        const uint32_t p1 = c[0], p2 = p1 + c[1], p3 = p2 + c[2], sum = p3 + c[3];
+        uint32_t total;
+        const uint32_t excl = carry + block_scan_1024(sum, sWarp, total);
+        const uint32_t off[4] = {excl, excl + p1, excl + p2, excl + p3};
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            if (i0 + k < n) row[i0 + k] = off[k];
+        }
+        carry += total;
+    }
+}
+
+__global__ void __launch_bounds__(kOrderedWarps * 32) bin_fill_ordered_kernel(const Frame f, uint32_t numBlocks)
+{
+    __shared__ GroupBins sGroup[kOrderedWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t chunk = blockIdx.x * kOrderedWarps + warp;
+    if (chunk >= f.binChunks || (f.status[0] & kStatusSticky))
+    {
+        return;
+    }
+    uint32_t begin, end;
+    chunk_bins(f, numBlocks, chunk, begin, end);
+    for_chunk_entries(f, begin, end, sGroup[warp], [&](uint32_t tile, uint32_t key, uint32_t peers, bool valid) {
+        const int leader = __ffs(peers) - 1;
+        uint32_t* cursor = f.chunkCounts + (size_t)(valid ? tile : 0u) * f.binChunks + chunk;
+        uint32_t base = 0;
+        if (valid && lane == leader)
+        {
+            base = f.tileOffset[tile] + *cursor;
+        }
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (valid)
+        {
+            const uint32_t pos = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+            if (pos < f.entryCap) f.entries[pos] = key;
+            /* the step's entries of this tile advance the chunk's cursor */
+            if (lane == leader) *cursor += (uint32_t)__popc(peers);
+        }
+    });
 }
 
 /*-----------------------------------------------------------------------------
@@ -600,24 +793,33 @@ cudaError_t launch_pipeline(const Frame& f, const slg_pipeline_ops& ops, int key
     }
     cudaError_t e = (cudaError_t)ops.launch_vertex(&f, s);
     if (e != cudaSuccess) return e;
-    if (f.rankOf && f.numSlots > 0)
+    const uint32_t numBlocks = (uint32_t)((f.numSlots + kBinBlock - 1) / kBinBlock);
+    const bool ordered = f.chunkCounts != nullptr && f.numSlots > 0;
+    if ((f.rankOf || ordered) && f.numSlots > 0)
     {
-        const uint32_t numBlocks = (uint32_t)((f.numSlots + kBinBlock - 1) / kBinBlock);
         bin_block_sums_kernel<<<numBlocks, kBinBlock, 0, s>>>(f);
         bin_block_scan_kernel<<<1, 1024, 0, s>>>(f, numBlocks);
         bin_seq_kernel<<<numBlocks, kBinBlock, 0, s>>>(f);
-        flush_sort_kernel<<<f.rankGrid, 1024, 0, s>>>(f, numBlocks);
+        if (f.rankOf) flush_sort_kernel<<<f.rankGrid, 1024, 0, s>>>(f, numBlocks);
     }
     if (ev) cudaEventRecord(ev[1], s);
     tile_scan_kernel<<<1, 1024, 0, s>>>(f, numTiles);
     if (ev) cudaEventRecord(ev[2], s);
-    if (f.numSlots > 0)
+    if (ordered)
+    {
+        const unsigned blocks = (f.binChunks + kOrderedWarps - 1) / kOrderedWarps;
+        cudaMemsetAsync(f.chunkCounts, 0, sizeof(uint32_t) * (size_t)numTiles * f.binChunks, s);
+        bin_count_ordered_kernel<<<blocks, kOrderedWarps * 32, 0, s>>>(f, numBlocks);
+        bin_chunk_scan_kernel<<<numTiles, 1024, 0, s>>>(f);
+        bin_fill_ordered_kernel<<<blocks, kOrderedWarps * 32, 0, s>>>(f, numBlocks);
+    }
+    else if (f.numSlots > 0)
     {
         const unsigned blocks = (unsigned)((f.numSlots + 255) / 256);
         bin_fill_kernel<<<blocks, 256, 0, s>>>(f);
     }
     if (ev) cudaEventRecord(ev[3], s);
-    if (!f.orderFree || f.aliasCount)
+    if ((!f.orderFree || f.aliasCount) && !ordered)
     {
         /* keyCap keys of 4 bytes per tile (<= 227 KB of shared memory); for an
          * order-free launch with line draws the device decides whether the
