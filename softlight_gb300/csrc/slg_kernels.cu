@@ -437,7 +437,8 @@ __global__ void __launch_bounds__(kOrderedWarps * 32) bin_count_ordered_kernel(c
     });
 }
 
-/* One CTA per tile: exclusive scan of its chunk counts, in place. */
+/* One CTA per tile: exclusive scan of its chunk counts, in place, and the
+ * tile's total for tile_scan_kernel. */
 __global__ void __launch_bounds__(1024) bin_chunk_scan_kernel(const Frame f)
 {
     __shared__ uint32_t sWarp[32];
@@ -465,6 +466,7 @@ __global__ void __launch_bounds__(1024) bin_chunk_scan_kernel(const Frame f)
         }
         carry += total;
     }
+    if (threadIdx.x == 0) f.tileCount[blockIdx.x] = carry;
 }
 
 __global__ void __launch_bounds__(kOrderedWarps * 32) bin_fill_ordered_kernel(const Frame f, uint32_t numBlocks)
@@ -803,15 +805,19 @@ cudaError_t launch_pipeline(const Frame& f, const slg_pipeline_ops& ops, int key
         if (f.rankOf) flush_sort_kernel<<<f.rankGrid, 1024, 0, s>>>(f, numBlocks);
     }
     if (ev) cudaEventRecord(ev[1], s);
+    const unsigned chunkBlocks = (f.binChunks + kOrderedWarps - 1) / kOrderedWarps;
+    if (ordered)
+    {
+        /* per-chunk counts; their scan also gives each tile's total */
+        cudaMemsetAsync(f.chunkCounts, 0, sizeof(uint32_t) * (size_t)numTiles * f.binChunks, s);
+        bin_count_ordered_kernel<<<chunkBlocks, kOrderedWarps * 32, 0, s>>>(f, numBlocks);
+        bin_chunk_scan_kernel<<<numTiles, 1024, 0, s>>>(f);
+    }
     tile_scan_kernel<<<1, 1024, 0, s>>>(f, numTiles);
     if (ev) cudaEventRecord(ev[2], s);
     if (ordered)
     {
-        const unsigned blocks = (f.binChunks + kOrderedWarps - 1) / kOrderedWarps;
-        cudaMemsetAsync(f.chunkCounts, 0, sizeof(uint32_t) * (size_t)numTiles * f.binChunks, s);
-        bin_count_ordered_kernel<<<blocks, kOrderedWarps * 32, 0, s>>>(f, numBlocks);
-        bin_chunk_scan_kernel<<<numTiles, 1024, 0, s>>>(f);
-        bin_fill_ordered_kernel<<<blocks, kOrderedWarps * 32, 0, s>>>(f, numBlocks);
+        bin_fill_ordered_kernel<<<chunkBlocks, kOrderedWarps * 32, 0, s>>>(f, numBlocks);
     }
     else if (f.numSlots > 0)
     {

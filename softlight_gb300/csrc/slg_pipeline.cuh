@@ -344,148 +344,223 @@ __device__ __forceinline__ float4 mix4(const float4 a, const float4 b, float t)
     return make_float4((b.x - a.x) * t + a.x, (b.y - a.y) * t + a.y, (b.z - a.z) * t + a.z, (b.w - a.w) * t + a.w);
 }
 
-/* SL_TriProcessor::clip_and_process_tris (SL_TriProcessor.cpp:370-519).
- * Returns the slotInfo value for the slot. */
-struct ClipTri { float4 p[3]; uint64_t vid[3]; };   /* vid: vertex id, or vertex-cache entry of a cached draw */
-
-/* The varyings of a clipped triangle's vertices are read from the vertex
- * cache or recomputed here (the vertex program is a pure function of vertex
- * and instance id), so the common unclipped path keeps them in registers. */
-template <class P>
-__device__ __noinline__ uint32_t clip_and_emit(const Frame& f, const DrawDesc& d, uint32_t drawIndex, uint64_t slot,
-                                               uint64_t primIndex, uint64_t inst, const ClipTri tri)
+/* SL_TriProcessor::clip_and_process_tris (SL_TriProcessor.cpp:370-519),
+ * one warp per triangle. Lane v holds polygon vertex v (v < 9): its clip
+ * position and its four varying slots, as newVerts[v] and newVarys[v * 4 ..
+ * v * 4 + 3], plus its tempVerts / tempVarys entries. Per clip plane every
+ * lane tests its vertex, a warp scan places each vertex's outputs (the
+ * crossing point with the previous vertex, then the vertex if inside), and
+ * each output lane fetches its one or two source vertices by shuffle, so
+ * every interpolation is the reference's expression on the same operands.
+ * The reference's copy-back of the varyings moves numNew vectors from each
+ * output vertex's first slot (:471-475); slot 4 v + m is refreshed from
+ * tempVarys when v * 4 + m lies in some range [4 i, 4 i + numNew), i <
+ * numNew, which copied_slot evaluates per lane. Returns the slot's
+ * slotInfo value (valid in every lane). */
+__device__ __forceinline__ bool copied_slot(int v, int m, int numNew)
 {
-    const int nv = d.numVaryings;
-    float4 newVerts[9], tempVerts[9];
-    slg_v4 newVarys[36], tempVarys[36];
-    for (int i = 0; i < 9; ++i) { newVerts[i] = make_float4(0.f, 0.f, 0.f, 0.f); tempVerts[i] = newVerts[i]; }
-    for (int i = 0; i < 36; ++i) { newVarys[i] = slg_make_v4(0.f, 0.f, 0.f, 0.f); tempVarys[i] = newVarys[i]; }
+    return (v < numNew && m < numNew) || (v >= 1 && v - 1 < numNew && m + 4 < numNew) || (v >= 2 && v - 2 < numNew && m + 8 < numNew);
+}
 
-    unsigned numTotal = 3;
-    for (int k = 0; k < 3; ++k)
+__device__ __forceinline__ float4 shfl4(const float4 v, int src)
+{
+    return make_float4(__shfl_sync(0xFFFFFFFFu, v.x, src), __shfl_sync(0xFFFFFFFFu, v.y, src), __shfl_sync(0xFFFFFFFFu, v.z, src),
+                       __shfl_sync(0xFFFFFFFFu, v.w, src));
+}
+
+__device__ __forceinline__ slg_v4 shfl4(const slg_v4 v, int src)
+{
+    return slg_make_v4(__shfl_sync(0xFFFFFFFFu, v.x, src), __shfl_sync(0xFFFFFFFFu, v.y, src), __shfl_sync(0xFFFFFFFFu, v.z, src),
+                       __shfl_sync(0xFFFFFFFFu, v.w, src));
+}
+
+constexpr int kClipVerts = 9;   /* 3 + one per clip plane: the reference's array sizes */
+
+template <class P>
+__device__ __forceinline__ uint32_t clip_warp(const Frame& f, const DrawDesc& d, uint32_t drawIndex, uint64_t slot, uint64_t primIndex,
+                                              uint64_t inst, uint64_t vid, float4 pos)
+{
+    const int lane = threadIdx.x & 31;
+    const int nv = d.numVaryings;
+    const slg_v4 zero4 = slg_make_v4(0.f, 0.f, 0.f, 0.f);
+    slg_v4 cur[kMaxVaryings], tmp[kMaxVaryings];
+#pragma unroll
+    for (int i = 0; i < kMaxVaryings; ++i)
     {
-        newVerts[k] = tri.p[k];
+        cur[i] = zero4;
+        tmp[i] = zero4;
+    }
+    if (lane < 3)
+    {
         if (d.cacheVerts)
         {
-            for (int i = 0; i < nv; ++i)
+#pragma unroll
+            for (int i = 0; i < kMaxVaryings; ++i)
             {
-                const float4 cv = f.cacheVary[(uint64_t)i * f.cacheEntries + tri.vid[k]];
-                newVarys[k * 4 + i] = slg_make_v4(cv.x, cv.y, cv.z, cv.w);
+                if (i < nv)
+                {
+                    const float4 cv = f.cacheVary[(uint64_t)i * f.cacheEntries + vid];
+                    cur[i] = slg_make_v4(cv.x, cv.y, cv.z, cv.w);
+                }
             }
         }
         else
         {
-            slg_v4 vary[4];
-            (void)P::vertex(d, f.tables, tri.vid[k], inst, vary);
-            for (int i = 0; i < nv; ++i) newVarys[k * 4 + i] = vary[i];
+            slg_v4 vary[kMaxVaryings];
+            (void)P::vertex(d, f.tables, vid, inst, vary);
+#pragma unroll
+            for (int i = 0; i < kMaxVaryings; ++i)
+            {
+                if (i < nv) cur[i] = vary[i];
+            }
         }
     }
+    else
+    {
+        pos = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
 
+    int numTotal = 3;
     for (int e = 0; e < 6; ++e)
     {
         /* clipEdges: +x, -x, +y, -y, +z, -z against w (SL_TriProcessor.cpp:384-393) */
         const float ex = (e == 0) ? 1.f : (e == 1) ? -1.f : 0.f;
         const float ey = (e == 2) ? 1.f : (e == 3) ? -1.f : 0.f;
         const float ez = (e == 4) ? 1.f : (e == 5) ? -1.f : 0.f;
-        auto dotEdge = [&](const float4 p) { return ((p.x * ex + p.y * ey) + p.z * ez) + p.w * 1.f; };
-
-        unsigned numNew = 0;
-        unsigned j = numTotal - 1;
-        float4 q0 = newVerts[numTotal - 1];
-        float t0 = dotEdge(q0);
-        int vis0 = !sign_mask(t0);
-
-        for (unsigned k = 0; k < numTotal; ++k)
+        const bool mine = lane < numTotal;
+        const float t = mine ? ((pos.x * ex + pos.y * ey) + pos.z * ez) + pos.w * 1.f : 0.f;
+        const int vis = mine ? !sign_mask(t) : 0;
+        const int prev = (lane == 0) ? numTotal - 1 : lane - 1;
+        const int visPrev = __shfl_sync(0xFFFFFFFFu, vis, prev);
+        const int cross = (mine && (visPrev ^ vis)) ? 1 : 0;
+        const int cnt = cross + vis;
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
         {
-            const float4 q1 = newVerts[k];
-            const float t1 = dotEdge(q1);
-            const int vis1 = !sign_mask(t1);
-            if (vis0 ^ vis1)
-            {
-                const float t = t0 * (1.f / (t0 - t1));
-                tempVerts[numNew] = mix4(q0, q1, t);
-                for (int i = 0; i < nv; ++i)
-                {
-                    tempVarys[numNew * 4 + i] = mix4(newVarys[j * 4 + i], newVarys[k * 4 + i], t);
-                }
-                ++numNew;
-            }
-            if (vis1)
-            {
-                tempVerts[numNew] = q1;
-                for (int i = 0; i < nv; ++i) tempVarys[numNew * 4 + i] = newVarys[k * 4 + i];
-                ++numNew;
-            }
-            j = k;
-            q0 = q1;
-            t0 = t1;
-            vis0 = vis1;
+            const int n = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += n;
         }
-
-        if (!numNew)
+        const int numNew = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        if (numNew == 0 || numNew > kClipVerts)
         {
+            /* nothing left; more than 9 vertices would overrun the
+             * reference's arrays and is not rendered */
             return 0;
         }
-        numTotal = numNew;
-        for (unsigned i = 0; i < numNew; ++i) newVerts[i] = tempVerts[i];
-        /* copies numNew vectors from each vertex's first varying slot
-         * (SL_TriProcessor.cpp:471-475), bounded to the 36 slots */
-        for (unsigned i = numNew; i--;)
+        const int out0 = incl - cnt;
+        /* the vertex k whose outputs hold output slot `lane` */
+        int k = 0;
+        for (int q = 1; q < numTotal; ++q)
         {
-            for (unsigned m = 0; m < numNew; ++m)
+            if (__shfl_sync(0xFFFFFFFFu, out0, q) <= lane) k = q;
+        }
+        const int kOut0 = __shfl_sync(0xFFFFFFFFu, out0, k);
+        const int kCross = __shfl_sync(0xFFFFFFFFu, cross, k);
+        const bool isMix = kCross && lane == kOut0;
+        const int srcA = isMix ? ((k == 0) ? numTotal - 1 : k - 1) : k;
+        const float4 pa = shfl4(pos, srcA), pb = shfl4(pos, k);
+        const float ta = __shfl_sync(0xFFFFFFFFu, t, srcA), tb = __shfl_sync(0xFFFFFFFFu, t, k);
+        slg_v4 va[kMaxVaryings], vb[kMaxVaryings];
+#pragma unroll
+        for (int i = 0; i < kMaxVaryings; ++i)
+        {
+            va[i] = zero4;
+            vb[i] = zero4;
+            if (i < nv)
             {
-                const unsigned s = i * 4 + m;
-                if (s < 36) newVarys[s] = tempVarys[s];
+                va[i] = shfl4(cur[i], srcA);
+                vb[i] = shfl4(cur[i], k);
             }
         }
+        if (lane < numNew)
+        {
+            if (isMix)
+            {
+                const float tt = ta * (1.f / (ta - tb));
+                pos = mix4(pa, pb, tt);
+#pragma unroll
+                for (int i = 0; i < kMaxVaryings; ++i)
+                {
+                    if (i < nv) tmp[i] = mix4(va[i], vb[i], tt);
+                }
+            }
+            else
+            {
+                pos = pb;
+#pragma unroll
+                for (int i = 0; i < kMaxVaryings; ++i)
+                {
+                    if (i < nv) tmp[i] = vb[i];
+                }
+            }
+        }
+        if (lane < kClipVerts)
+        {
+#pragma unroll
+            for (int m = 0; m < kMaxVaryings; ++m)
+            {
+                if (copied_slot(lane, m, numNew)) cur[m] = tmp[m];
+            }
+        }
+        numTotal = numNew;
     }
 
     if (numTotal < 3)
     {
         return 0;
     }
+    const float4 sp = (lane < numTotal) ? to_screen(pos, f.viewport) : make_float4(0.f, 0.f, 0.f, 0.f);
 
-    for (unsigned i = 0; i < numTotal; ++i)
-    {
-        newVerts[i] = to_screen(newVerts[i], f.viewport);
-    }
-
-    /* fan (0, i+1, i+2) for i = numTotal-3 .. 0, in that order */
-    uint32_t survivors = 0;
-    for (unsigned i = numTotal - 2; i--;)
-    {
-        survivors += bin_visible(newVerts[0], newVerts[i + 1], newVerts[i + 2]) ? 1u : 0u;
-    }
-    if (!survivors)
+    /* fan (0, i+1, i+2) for i = numTotal-3 .. 0, in that order: lane i */
+    const int i1 = min(lane + 1, 31), i2 = min(lane + 2, 31);
+    const float4 a = shfl4(sp, 0), b = shfl4(sp, i1), c = shfl4(sp, i2);
+    const bool visible = lane < numTotal - 2 && bin_visible(a, b, c);
+    const uint32_t vmask = __ballot_sync(0xFFFFFFFFu, visible);
+    if (!vmask)
     {
         return 0;
     }
-
-    const uint32_t base = atomicAdd(f.ovfCount, survivors);
+    const uint32_t survivors = (uint32_t)__popc(vmask);
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(f.ovfCount, survivors);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
     if (base + survivors > f.ovfCap)
     {
-        atomicOr(f.status, kStatusOvfOverflow);
-        atomicMax(f.status + 2, (int)(base + survivors));
+        if (lane == 0)
+        {
+            atomicOr(f.status, kStatusOvfOverflow);
+            atomicMax(f.status + 2, (int)(base + survivors));
+        }
         return 0;
     }
-    f.slotOvf[slot] = base;
+    if (lane == 0) f.slotOvf[slot] = base;
 
-    uint32_t sub = 0;
-    for (unsigned i = numTotal - 2; i--;)
+    slg_v4 v0[kMaxVaryings], v1[kMaxVaryings], v2[kMaxVaryings];
+#pragma unroll
+    for (int i = 0; i < kMaxVaryings; ++i)
     {
-        const float4 a = newVerts[0], b = newVerts[i + 1], c = newVerts[i + 2];
-        if (!bin_visible(a, b, c))
+        v0[i] = zero4;
+        v1[i] = zero4;
+        v2[i] = zero4;
+        if (i < nv)
         {
-            continue;
+            v0[i] = shfl4(cur[i], 0);
+            v1[i] = shfl4(cur[i], i1);
+            v2[i] = shfl4(cur[i], i2);
         }
+    }
+    if (visible)
+    {
+        /* records in fan order: those of higher i come first */
+        const uint32_t sub = (uint32_t)__popc(vmask & ~((2u << lane) - 1u));
         Record rec;
         make_record(a, b, c, drawIndex, primIndex, record_flags(d), rec);
         if (d.prim == kPrimWire && d.blend != SLG_BLEND_OFF) wire_queue_check(f, rec.r);
         const uint64_t recIndex = f.numSlots + base + sub;
         store_record(f, recIndex, rec);
-        store_varyings(f, recIndex, nv, newVarys, newVarys + (i + 1) * 4, newVarys + (i + 2) * 4);
-        count_tiles(rec.r[6], f);
-        ++sub;
+        store_varyings(f, recIndex, nv, v0, v1, v2);
+        if (f.chunkCounts == nullptr) count_tiles(rec.r[6], f);
     }
     return 2u + survivors;
 }
@@ -979,7 +1054,9 @@ template <class P>
 __global__ void __launch_bounds__(128) clip_kernel(const Frame f)
 {
     const uint32_t count = *f.clipCount;
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x)
+    const int lane = threadIdx.x & 31;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < count; q += warps)
     {
         const uint64_t slot = f.clipQueue[q];
         const int di = (f.numDraws > 1) ? find_draw(f, slot) : 0;
@@ -988,23 +1065,26 @@ __global__ void __launch_bounds__(128) clip_kernel(const Frame f)
         const uint64_t inst = local / d.numTris;
         const uint64_t tri = local - inst * d.numTris;
         const uint64_t i = d.elementBegin + 3u * tri;
-        ClipTri ct;
-        for (int k = 0; k < 3; ++k)
+        /* lanes 0..2: the triangle's vertices */
+        uint64_t vid = 0;
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (lane < 3)
         {
-            ct.vid[k] = (d.indexType >= 0) ? read_index(d, i + k) : (i + k);
+            vid = (d.indexType >= 0) ? read_index(d, i + lane) : (i + lane);
             if (d.cacheVerts)
             {
-                ct.vid[k] += d.cacheBase + inst * d.cacheVerts;
-                ct.p[k] = mat_mul(f.scissor, f.cachePos[ct.vid[k]]);
+                vid += d.cacheBase + inst * d.cacheVerts;
+                p = mat_mul(f.scissor, f.cachePos[vid]);
             }
             else
             {
                 slg_v4 vary[4];
-                ct.p[k] = mat_mul(f.scissor, to_f4(P::vertex(d, f.tables, ct.vid[k], inst, vary)));
+                p = mat_mul(f.scissor, to_f4(P::vertex(d, f.tables, vid, inst, vary)));
             }
         }
         const uint64_t primIndex = d.primBase + d.numElements * inst + i;
-        f.slotInfo[slot] = clip_and_emit<P>(f, d, (uint32_t)di, slot, primIndex, inst, ct);
+        const uint32_t info = clip_warp<P>(f, d, (uint32_t)di, slot, primIndex, inst, vid, p);
+        if (lane == 0) f.slotInfo[slot] = info;
     }
 }
 
@@ -1059,8 +1139,9 @@ __global__ void __launch_bounds__(256) vs_setup_kernel(const Frame f)
         f.slotInfo[slot] = setup_slot<P, kLines, kCached>(f, slot, tr, counted);
     }
     /* per-tile counts of the unclipped records, one atomic per group of
-     * lanes touching the same tile (clipped records count themselves) */
-    warp_tile_walk(f, tr, counted, f.tileCount, [](uint32_t, uint32_t) {});
+     * lanes touching the same tile (clipped records count themselves);
+     * launches filling their lists in key order count per chunk instead */
+    warp_tile_walk(f, tr, counted && f.chunkCounts == nullptr, f.tileCount, [](uint32_t, uint32_t) {});
 }
 
 /*-----------------------------------------------------------------------------
