@@ -1176,9 +1176,10 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
     }
 
     /* ordered raster: the tile lists are filled in key order (no tile sort)
-     * when the per-chunk tile counts fit kMaxChunkCounts words; a sort-key
-     * cap set for testing keeps the atomic fill and the tile sort */
-    if (!f.orderFree && numSlots > 0 && !ctx->sortKeysCapped)
+     * for tile grids of at most kMaxOrderedTiles tiles whose per-chunk
+     * counts fit kMaxChunkCounts words; a sort-key cap set for testing keeps
+     * the atomic fill and the tile sort */
+    if (!f.orderFree && numSlots > 0 && !ctx->sortKeysCapped && (uint64_t)f.tilesX * f.tilesY <= (uint64_t)slg::kMaxOrderedTiles)
     {
         const uint64_t numTiles = (uint64_t)f.tilesX * f.tilesY;
         uint64_t chunks = std::min<uint64_t>(kMaxBinChunks, ((numSlots + 255) / 256 + 7) & ~7ull);

@@ -229,10 +229,11 @@ struct Frame
 
     /* tile lists filled in key order (bin_count_ordered_kernel ..
      * bin_fill_ordered_kernel): the bins in key order are cut into binChunks
-     * chunks, one warp each; chunkCounts (tile-major, numTiles x binChunks)
-     * holds each chunk's entries per tile, then their exclusive scan over the
-     * chunks, then the chunk's running cursor. null: the lists are filled by
-     * atomics and sorted per tile when the ordered raster needs them. */
+     * chunks, one warp each; chunkCounts (chunk-major, binChunks x
+     * numTiles) holds each chunk's entries per tile, then their exclusive
+     * scan over the chunks (the chunk's first position in each tile's list).
+     * null: the lists are filled by atomics and sorted per tile when the
+     * ordered raster needs them. */
     uint32_t* chunkCounts;
     uint32_t  binChunks;
     uint32_t* itemKey;            /* per bin in push order: its tile-list key (launches without recOfRank) */

@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(1024) flush_sort_kernel(const Frame f, uint32_
  * The lists come out sorted, with no atomics on shared tile cursors and no
  * tile sort.
 -----------------------------------------------------------------------------*/
-constexpr int kOrderedWarps = 8;   /* chunks (warps) per CTA of the count and fill passes */
+constexpr int kOrderedWarps = 4;   /* chunks (warps) per CTA of the count and fill passes */
 
 __device__ __forceinline__ void bin_item(const Frame& f, uint32_t i, uint32_t& rec, uint32_t& key)
 {
@@ -418,83 +418,102 @@ __device__ __forceinline__ void for_chunk_entries(const Frame& f, uint32_t begin
     }
 }
 
+/* Per chunk, its entries per tile: a histogram in the warp's shared memory,
+ * then one coalesced row of the chunk-major count matrix. */
 __global__ void __launch_bounds__(kOrderedWarps * 32) bin_count_ordered_kernel(const Frame f, uint32_t numBlocks)
 {
     __shared__ GroupBins sGroup[kOrderedWarps];
+    extern __shared__ uint32_t sHist[];   /* [kOrderedWarps][numTiles] */
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t chunk = blockIdx.x * kOrderedWarps + warp;
     if (chunk >= f.binChunks || (f.status[0] & kStatusSticky))
     {
         return;
     }
+    const uint32_t numTiles = (uint32_t)(f.tilesX * f.tilesY);
+    uint32_t* h = sHist + (size_t)warp * numTiles;
+    for (uint32_t t = lane; t < numTiles; t += 32) h[t] = 0u;
+    __syncwarp();
     uint32_t begin, end;
     chunk_bins(f, numBlocks, chunk, begin, end);
     for_chunk_entries(f, begin, end, sGroup[warp], [&](uint32_t tile, uint32_t, uint32_t peers, bool valid) {
-        if (valid && lane == __ffs(peers) - 1)
-        {
-            atomicAdd(f.chunkCounts + (size_t)tile * f.binChunks + chunk, (uint32_t)__popc(peers));
-        }
+        /* one lane per tile of the step; steps are separated by __syncwarp */
+        if (valid && lane == __ffs(peers) - 1) h[tile] += (uint32_t)__popc(peers);
     });
+    __syncwarp();
+    uint32_t* row = f.chunkCounts + (size_t)chunk * numTiles;
+    for (uint32_t t = lane; t < numTiles; t += 32) row[t] = h[t];
 }
 
-/* One CTA per tile: exclusive scan of its chunk counts, in place, and the
- * tile's total for tile_scan_kernel. */
+/* 32 tiles per CTA, one per lane; warp w scans chunks [w * per, (w+1) * per)
+ * of the chunk-major matrix (coalesced rows), the warps' sums are scanned in
+ * shared memory, and every count becomes the chunk's first position in the
+ * tile's list (relative); each tile's total goes to tileCount. */
 __global__ void __launch_bounds__(1024) bin_chunk_scan_kernel(const Frame f)
 {
-    __shared__ uint32_t sWarp[32];
+    __shared__ uint32_t sSum[32][33];
     if (f.status[0] & kStatusSticky)
     {
         return;
     }
-    uint32_t* row = f.chunkCounts + (size_t)blockIdx.x * f.binChunks;
-    const uint32_t n = f.binChunks;
-    uint32_t carry = 0;
-    for (uint32_t base = 0; base < n; base += 4096)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t numTiles = (uint32_t)(f.tilesX * f.tilesY);
+    const uint32_t t = blockIdx.x * 32 + lane;
+    const uint32_t W = f.binChunks;
+    const uint32_t per = (W + 31) / 32;
+    const uint32_t c0 = min(warp * per, W), c1 = min(c0 + per, W);
+    uint32_t sum = 0;
+    if (t < numTiles)
     {
-        const uint32_t i0 = base + 4 * threadIdx.x;
-        uint32_t c[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) c[k] = (i0 + k < n) ? row[i0 + k] : 0u;
-        const uint32_t p1 = c[0], p2 = p1 + c[1], p3 = p2 + c[2], sum = p3 + c[3];
-        uint32_t total;
-        const uint32_t excl = carry + block_scan_1024(sum, sWarp, total);
-        const uint32_t off[4] = {excl, excl + p1, excl + p2, excl + p3};
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-        {
-            if (i0 + k < n) row[i0 + k] = off[k];
-        }
-        carry += total;
+        for (uint32_t c = c0; c < c1; ++c) sum += f.chunkCounts[(size_t)c * numTiles + t];
     }
-    if (threadIdx.x == 0) f.tileCount[blockIdx.x] = carry;
+    sSum[warp][lane] = sum;
+    __syncthreads();
+    uint32_t base = 0;
+    for (int w = 0; w < warp; ++w) base += sSum[w][lane];
+    if (t < numTiles)
+    {
+        for (uint32_t c = c0; c < c1; ++c)
+        {
+            uint32_t* p = f.chunkCounts + (size_t)c * numTiles + t;
+            const uint32_t v = *p;
+            *p = base;
+            base += v;
+        }
+        if (warp == 31) f.tileCount[t] = base;
+    }
 }
 
+/* Each chunk's entries at its cursors: the warp's cursors (tile list offset
+ * + the chunk's first position) live in its shared memory. */
 __global__ void __launch_bounds__(kOrderedWarps * 32) bin_fill_ordered_kernel(const Frame f, uint32_t numBlocks)
 {
     __shared__ GroupBins sGroup[kOrderedWarps];
+    extern __shared__ uint32_t sCursor[];   /* [kOrderedWarps][numTiles] */
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t chunk = blockIdx.x * kOrderedWarps + warp;
     if (chunk >= f.binChunks || (f.status[0] & kStatusSticky))
     {
         return;
     }
+    const uint32_t numTiles = (uint32_t)(f.tilesX * f.tilesY);
+    uint32_t* cur = sCursor + (size_t)warp * numTiles;
+    const uint32_t* row = f.chunkCounts + (size_t)chunk * numTiles;
+    for (uint32_t t = lane; t < numTiles; t += 32) cur[t] = f.tileOffset[t] + row[t];
+    __syncwarp();
     uint32_t begin, end;
     chunk_bins(f, numBlocks, chunk, begin, end);
     for_chunk_entries(f, begin, end, sGroup[warp], [&](uint32_t tile, uint32_t key, uint32_t peers, bool valid) {
         const int leader = __ffs(peers) - 1;
-        uint32_t* cursor = f.chunkCounts + (size_t)(valid ? tile : 0u) * f.binChunks + chunk;
         uint32_t base = 0;
-        if (valid && lane == leader)
-        {
-            base = f.tileOffset[tile] + *cursor;
-        }
+        if (valid && lane == leader) base = cur[tile];
         base = __shfl_sync(0xFFFFFFFFu, base, leader);
         if (valid)
         {
             const uint32_t pos = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
             if (pos < f.entryCap) f.entries[pos] = key;
             /* the step's entries of this tile advance the chunk's cursor */
-            if (lane == leader) *cursor += (uint32_t)__popc(peers);
+            if (lane == leader) cur[tile] = base + (uint32_t)__popc(peers);
         }
     });
 }
@@ -782,7 +801,11 @@ __global__ void launch_mark_kernel(int32_t* status)
 
 cudaError_t init_library_attributes(int keyCap)
 {
-    return cudaFuncSetAttribute(tile_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(uint32_t) * keyCap));
+    const int chunkSmem = (int)(sizeof(uint32_t) * kOrderedWarps * kMaxOrderedTiles);
+    cudaError_t e = cudaFuncSetAttribute(tile_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(uint32_t) * keyCap));
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(bin_count_ordered_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, chunkSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(bin_fill_ordered_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, chunkSmem);
+    return e;
 }
 
 cudaError_t launch_pipeline(const Frame& f, const slg_pipeline_ops& ops, int keyCap, cudaStream_t s, cudaEvent_t* ev)
@@ -806,18 +829,18 @@ cudaError_t launch_pipeline(const Frame& f, const slg_pipeline_ops& ops, int key
     }
     if (ev) cudaEventRecord(ev[1], s);
     const unsigned chunkBlocks = (f.binChunks + kOrderedWarps - 1) / kOrderedWarps;
+    const size_t chunkSmem = sizeof(uint32_t) * kOrderedWarps * (size_t)numTiles;
     if (ordered)
     {
         /* per-chunk counts; their scan also gives each tile's total */
-        cudaMemsetAsync(f.chunkCounts, 0, sizeof(uint32_t) * (size_t)numTiles * f.binChunks, s);
-        bin_count_ordered_kernel<<<chunkBlocks, kOrderedWarps * 32, 0, s>>>(f, numBlocks);
-        bin_chunk_scan_kernel<<<numTiles, 1024, 0, s>>>(f);
+        bin_count_ordered_kernel<<<chunkBlocks, kOrderedWarps * 32, chunkSmem, s>>>(f, numBlocks);
+        bin_chunk_scan_kernel<<<(numTiles + 31) / 32, 1024, 0, s>>>(f);
     }
     tile_scan_kernel<<<1, 1024, 0, s>>>(f, numTiles);
     if (ev) cudaEventRecord(ev[2], s);
     if (ordered)
     {
-        bin_fill_ordered_kernel<<<chunkBlocks, kOrderedWarps * 32, 0, s>>>(f, numBlocks);
+        bin_fill_ordered_kernel<<<chunkBlocks, kOrderedWarps * 32, chunkSmem, s>>>(f, numBlocks);
     }
     else if (f.numSlots > 0)
     {

@@ -16,8 +16,14 @@ namespace slg
  * tile_scan, after bin_fill and after the raster. */
 cudaError_t launch_pipeline(const Frame& f, const slg_pipeline_ops& ops, int keyCap, cudaStream_t s, cudaEvent_t* ev);
 
-/* Raises the dynamic shared-memory limit of the tile sort once, so
- * launches (and stream captures) need no attribute calls. */
+/* Largest tile grid whose lists a blended launch fills in key order (the
+ * count and fill passes keep one word per tile and chunk in shared memory);
+ * larger grids fill by atomics and sort per tile. */
+constexpr int kMaxOrderedTiles = 4096;
+
+/* Raises the dynamic shared-memory limits of the tile sort and of the
+ * key-order fill once, so launches (and stream captures) need no attribute
+ * calls. */
 cudaError_t init_library_attributes(int keyCap);
 
 /* The entry table of the built-in programs (slg_builtin_vertex.cu). */

@@ -344,44 +344,74 @@ __device__ __forceinline__ float4 mix4(const float4 a, const float4 b, float t)
     return make_float4((b.x - a.x) * t + a.x, (b.y - a.y) * t + a.y, (b.z - a.z) * t + a.z, (b.w - a.w) * t + a.w);
 }
 
+/* Whether SoftLight's clipper leaves nothing of a triangle in its first
+ * pass that changes it: at the first plane (clipEdges order) with a vertex
+ * outside, all three are outside. The passes before it copy the triangle
+ * unchanged, so the clipper returns at that pass with no vertex; such a
+ * triangle is not queued. */
+__device__ __forceinline__ bool clip_trivially_empty(const float4* c)
+{
+#pragma unroll
+    for (int e = 0; e < 6; ++e)
+    {
+        const float ex = (e == 0) ? 1.f : (e == 1) ? -1.f : 0.f;
+        const float ey = (e == 2) ? 1.f : (e == 3) ? -1.f : 0.f;
+        const float ez = (e == 4) ? 1.f : (e == 5) ? -1.f : 0.f;
+        int out = 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            out += sign_mask(((c[k].x * ex + c[k].y * ey) + c[k].z * ez) + c[k].w * 1.f);
+        }
+        if (out == 3) return true;
+        if (out > 0) return false;
+    }
+    return false;
+}
+
 /* SL_TriProcessor::clip_and_process_tris (SL_TriProcessor.cpp:370-519),
- * one warp per triangle. Lane v holds polygon vertex v (v < 9): its clip
- * position and its four varying slots, as newVerts[v] and newVarys[v * 4 ..
- * v * 4 + 3], plus its tempVerts / tempVarys entries. Per clip plane every
- * lane tests its vertex, a warp scan places each vertex's outputs (the
- * crossing point with the previous vertex, then the vertex if inside), and
- * each output lane fetches its one or two source vertices by shuffle, so
- * every interpolation is the reference's expression on the same operands.
- * The reference's copy-back of the varyings moves numNew vectors from each
- * output vertex's first slot (:471-475); slot 4 v + m is refreshed from
- * tempVarys when v * 4 + m lies in some range [4 i, 4 i + numNew), i <
- * numNew, which copied_slot evaluates per lane. Returns the slot's
- * slotInfo value (valid in every lane). */
+ * two triangles per warp, one per 16-lane half. Lane v of a half holds
+ * polygon vertex v (v < 9): its clip position and its four varying slots,
+ * as newVerts[v] and newVarys[v * 4 .. v * 4 + 3], plus its tempVerts /
+ * tempVarys entries. Per clip plane every lane tests its vertex, a scan over
+ * the half places each vertex's outputs (the crossing point with the
+ * previous vertex, then the vertex if inside), and each output lane fetches
+ * its one or two source vertices by shuffle, so every interpolation is the
+ * reference's expression on the same operands. The reference's copy-back of
+ * the varyings moves numNew vectors from each output vertex's first slot
+ * (:471-475); slot 4 v + m is refreshed from tempVarys when v * 4 + m lies
+ * in some range [4 i, 4 i + numNew), i < numNew, which copied_slot
+ * evaluates per lane. Every lane of the warp calls it (no early exit: the
+ * halves shuffle together); returns the half's slotInfo value. */
 __device__ __forceinline__ bool copied_slot(int v, int m, int numNew)
 {
     return (v < numNew && m < numNew) || (v >= 1 && v - 1 < numNew && m + 4 < numNew) || (v >= 2 && v - 2 < numNew && m + 8 < numNew);
 }
 
+constexpr int kClipLanes = 16;  /* lanes per clipped triangle */
+
 __device__ __forceinline__ float4 shfl4(const float4 v, int src)
 {
-    return make_float4(__shfl_sync(0xFFFFFFFFu, v.x, src), __shfl_sync(0xFFFFFFFFu, v.y, src), __shfl_sync(0xFFFFFFFFu, v.z, src),
-                       __shfl_sync(0xFFFFFFFFu, v.w, src));
+    return make_float4(__shfl_sync(0xFFFFFFFFu, v.x, src, kClipLanes), __shfl_sync(0xFFFFFFFFu, v.y, src, kClipLanes),
+                       __shfl_sync(0xFFFFFFFFu, v.z, src, kClipLanes), __shfl_sync(0xFFFFFFFFu, v.w, src, kClipLanes));
 }
 
 __device__ __forceinline__ slg_v4 shfl4(const slg_v4 v, int src)
 {
-    return slg_make_v4(__shfl_sync(0xFFFFFFFFu, v.x, src), __shfl_sync(0xFFFFFFFFu, v.y, src), __shfl_sync(0xFFFFFFFFu, v.z, src),
-                       __shfl_sync(0xFFFFFFFFu, v.w, src));
+    return slg_make_v4(__shfl_sync(0xFFFFFFFFu, v.x, src, kClipLanes), __shfl_sync(0xFFFFFFFFu, v.y, src, kClipLanes),
+                       __shfl_sync(0xFFFFFFFFu, v.z, src, kClipLanes), __shfl_sync(0xFFFFFFFFu, v.w, src, kClipLanes));
 }
 
 constexpr int kClipVerts = 9;   /* 3 + one per clip plane: the reference's array sizes */
 
 template <class P>
-__device__ __forceinline__ uint32_t clip_warp(const Frame& f, const DrawDesc& d, uint32_t drawIndex, uint64_t slot, uint64_t primIndex,
-                                              uint64_t inst, uint64_t vid, float4 pos)
+__device__ __forceinline__ uint32_t clip_pair(const Frame& f, bool active, const DrawDesc& d, uint32_t drawIndex, uint64_t slot,
+                                              uint64_t primIndex, uint64_t inst, uint64_t vid, float4 pos)
 {
     const int lane = threadIdx.x & 31;
-    const int nv = d.numVaryings;
+    const int sl = lane & (kClipLanes - 1);
+    const int half = lane >> 4;
+    const int nv = active ? d.numVaryings : 0;
     const slg_v4 zero4 = slg_make_v4(0.f, 0.f, 0.f, 0.f);
     slg_v4 cur[kMaxVaryings], tmp[kMaxVaryings];
 #pragma unroll
@@ -390,7 +420,7 @@ __device__ __forceinline__ uint32_t clip_warp(const Frame& f, const DrawDesc& d,
         cur[i] = zero4;
         tmp[i] = zero4;
     }
-    if (lane < 3)
+    if (active && sl < 3)
     {
         if (d.cacheVerts)
         {
@@ -420,60 +450,82 @@ __device__ __forceinline__ uint32_t clip_warp(const Frame& f, const DrawDesc& d,
         pos = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 
-    int numTotal = 3;
+    /* numTotal 0: no triangle in this half, or nothing left of it */
+    int numTotal = active ? 3 : 0;
     for (int e = 0; e < 6; ++e)
     {
         /* clipEdges: +x, -x, +y, -y, +z, -z against w (SL_TriProcessor.cpp:384-393) */
         const float ex = (e == 0) ? 1.f : (e == 1) ? -1.f : 0.f;
         const float ey = (e == 2) ? 1.f : (e == 3) ? -1.f : 0.f;
         const float ez = (e == 4) ? 1.f : (e == 5) ? -1.f : 0.f;
-        const bool mine = lane < numTotal;
+        const bool mine = sl < numTotal;
         const float t = mine ? ((pos.x * ex + pos.y * ey) + pos.z * ez) + pos.w * 1.f : 0.f;
         const int vis = mine ? !sign_mask(t) : 0;
-        const int prev = (lane == 0) ? numTotal - 1 : lane - 1;
-        const int visPrev = __shfl_sync(0xFFFFFFFFu, vis, prev);
+        if (__ballot_sync(0xFFFFFFFFu, mine && !vis) == 0u)
+        {
+            /* every vertex inside, in both halves: the outputs are the
+             * inputs in order, so tempVerts / tempVarys take the current
+             * values and the copy-back runs as for any pass */
+            if (mine)
+            {
+#pragma unroll
+                for (int i = 0; i < kMaxVaryings; ++i)
+                {
+                    if (i < nv) tmp[i] = cur[i];
+                }
+            }
+            if (sl < kClipVerts && numTotal > 0)
+            {
+#pragma unroll
+                for (int m = 0; m < kMaxVaryings; ++m)
+                {
+                    if (copied_slot(sl, m, numTotal)) cur[m] = tmp[m];
+                }
+            }
+            continue;
+        }
+        const int prev = (sl == 0) ? max(numTotal - 1, 0) : sl - 1;
+        const int visPrev = __shfl_sync(0xFFFFFFFFu, vis, prev, kClipLanes);
         const int cross = (mine && (visPrev ^ vis)) ? 1 : 0;
         const int cnt = cross + vis;
         int incl = cnt;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
+        for (int o = 1; o < kClipLanes; o <<= 1)
         {
-            const int n = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= o) incl += n;
+            const int n = __shfl_up_sync(0xFFFFFFFFu, incl, o, kClipLanes);
+            if (sl >= o) incl += n;
         }
-        const int numNew = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        if (numNew == 0 || numNew > kClipVerts)
-        {
-            /* nothing left; more than 9 vertices would overrun the
-             * reference's arrays and is not rendered */
-            return 0;
-        }
+        int numNew = __shfl_sync(0xFFFFFFFFu, incl, kClipLanes - 1, kClipLanes);
+        /* more than 9 vertices would overrun the reference's arrays: such a
+         * polygon is not rendered */
+        if (numNew > kClipVerts) numNew = 0;
         const int out0 = incl - cnt;
-        /* the vertex k whose outputs hold output slot `lane` */
+        /* the vertex k whose outputs hold output slot sl */
         int k = 0;
-        for (int q = 1; q < numTotal; ++q)
+#pragma unroll
+        for (int q = 1; q < kClipVerts; ++q)
         {
-            if (__shfl_sync(0xFFFFFFFFu, out0, q) <= lane) k = q;
+            if (__shfl_sync(0xFFFFFFFFu, out0, q, kClipLanes) <= sl && q < numTotal) k = q;
         }
-        const int kOut0 = __shfl_sync(0xFFFFFFFFu, out0, k);
-        const int kCross = __shfl_sync(0xFFFFFFFFu, cross, k);
-        const bool isMix = kCross && lane == kOut0;
+        const int kOut0 = __shfl_sync(0xFFFFFFFFu, out0, k, kClipLanes);
+        const int kCross = __shfl_sync(0xFFFFFFFFu, cross, k, kClipLanes);
+        const bool isMix = kCross && sl == kOut0;
         const int srcA = isMix ? ((k == 0) ? numTotal - 1 : k - 1) : k;
         const float4 pa = shfl4(pos, srcA), pb = shfl4(pos, k);
-        const float ta = __shfl_sync(0xFFFFFFFFu, t, srcA), tb = __shfl_sync(0xFFFFFFFFu, t, k);
+        const float ta = __shfl_sync(0xFFFFFFFFu, t, srcA, kClipLanes), tb = __shfl_sync(0xFFFFFFFFu, t, k, kClipLanes);
         slg_v4 va[kMaxVaryings], vb[kMaxVaryings];
 #pragma unroll
         for (int i = 0; i < kMaxVaryings; ++i)
         {
             va[i] = zero4;
             vb[i] = zero4;
-            if (i < nv)
+            if (__any_sync(0xFFFFFFFFu, i < nv))
             {
                 va[i] = shfl4(cur[i], srcA);
                 vb[i] = shfl4(cur[i], k);
             }
         }
-        if (lane < numNew)
+        if (sl < numNew)
         {
             if (isMix)
             {
@@ -495,46 +547,41 @@ __device__ __forceinline__ uint32_t clip_warp(const Frame& f, const DrawDesc& d,
                 }
             }
         }
-        if (lane < kClipVerts)
+        if (sl < kClipVerts && numNew > 0)
         {
 #pragma unroll
             for (int m = 0; m < kMaxVaryings; ++m)
             {
-                if (copied_slot(lane, m, numNew)) cur[m] = tmp[m];
+                if (copied_slot(sl, m, numNew)) cur[m] = tmp[m];
             }
         }
         numTotal = numNew;
     }
 
-    if (numTotal < 3)
-    {
-        return 0;
-    }
-    const float4 sp = (lane < numTotal) ? to_screen(pos, f.viewport) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 sp = (sl < numTotal) ? to_screen(pos, f.viewport) : make_float4(0.f, 0.f, 0.f, 0.f);
 
     /* fan (0, i+1, i+2) for i = numTotal-3 .. 0, in that order: lane i */
-    const int i1 = min(lane + 1, 31), i2 = min(lane + 2, 31);
+    const int i1 = min(sl + 1, kClipLanes - 1), i2 = min(sl + 2, kClipLanes - 1);
     const float4 a = shfl4(sp, 0), b = shfl4(sp, i1), c = shfl4(sp, i2);
-    const bool visible = lane < numTotal - 2 && bin_visible(a, b, c);
-    const uint32_t vmask = __ballot_sync(0xFFFFFFFFu, visible);
-    if (!vmask)
-    {
-        return 0;
-    }
+    const bool fan = sl < numTotal - 2 && bin_visible(a, b, c);
+    const uint32_t vmask = (__ballot_sync(0xFFFFFFFFu, fan) >> (half * kClipLanes)) & 0xFFFFu;
     const uint32_t survivors = (uint32_t)__popc(vmask);
     uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(f.ovfCount, survivors);
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (base + survivors > f.ovfCap)
+    if (sl == 0 && survivors) base = atomicAdd(f.ovfCount, survivors);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0, kClipLanes);
+    const bool fits = survivors && base + survivors <= f.ovfCap;
+    if (sl == 0 && survivors)
     {
-        if (lane == 0)
+        if (fits)
+        {
+            f.slotOvf[slot] = base;
+        }
+        else
         {
             atomicOr(f.status, kStatusOvfOverflow);
             atomicMax(f.status + 2, (int)(base + survivors));
         }
-        return 0;
     }
-    if (lane == 0) f.slotOvf[slot] = base;
 
     slg_v4 v0[kMaxVaryings], v1[kMaxVaryings], v2[kMaxVaryings];
 #pragma unroll
@@ -543,17 +590,17 @@ __device__ __forceinline__ uint32_t clip_warp(const Frame& f, const DrawDesc& d,
         v0[i] = zero4;
         v1[i] = zero4;
         v2[i] = zero4;
-        if (i < nv)
+        if (__any_sync(0xFFFFFFFFu, i < nv))
         {
             v0[i] = shfl4(cur[i], 0);
             v1[i] = shfl4(cur[i], i1);
             v2[i] = shfl4(cur[i], i2);
         }
     }
-    if (visible)
+    if (fan && fits)
     {
         /* records in fan order: those of higher i come first */
-        const uint32_t sub = (uint32_t)__popc(vmask & ~((2u << lane) - 1u));
+        const uint32_t sub = (uint32_t)__popc(vmask & ~((2u << sl) - 1u));
         Record rec;
         make_record(a, b, c, drawIndex, primIndex, record_flags(d), rec);
         if (d.prim == kPrimWire && d.blend != SLG_BLEND_OFF) wire_queue_check(f, rec.r);
@@ -562,7 +609,7 @@ __device__ __forceinline__ uint32_t clip_warp(const Frame& f, const DrawDesc& d,
         store_varyings(f, recIndex, nv, v0, v1, v2);
         if (f.chunkCounts == nullptr) count_tiles(rec.r[6], f);
     }
-    return 2u + survivors;
+    return fits ? 2u + survivors : 0u;
 }
 
 __device__ __forceinline__ int find_draw(const Frame& f, uint64_t slot)
@@ -1038,6 +1085,10 @@ __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, Ti
     }
     if (vis == 1)
     {
+        if (clip_trivially_empty(clip))
+        {
+            return 0;
+        }
         /* partially visible: queued for clip_kernel */
         const uint32_t q = atomicAdd(f.clipCount, 1u);
         f.clipQueue[q] = (uint32_t)slot;
@@ -1055,22 +1106,26 @@ __global__ void __launch_bounds__(128) clip_kernel(const Frame f)
 {
     const uint32_t count = *f.clipCount;
     const int lane = threadIdx.x & 31;
-    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < count; q += warps)
+    const int sl = lane & (kClipLanes - 1);
+    const uint32_t pairs = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t q0 = 2u * (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); q0 < count; q0 += 2u * pairs)
     {
-        const uint64_t slot = f.clipQueue[q];
-        const int di = (f.numDraws > 1) ? find_draw(f, slot) : 0;
+        /* half h of the warp clips queue entry q0 + h */
+        const uint32_t q = q0 + (uint32_t)(lane >> 4);
+        const bool active = q < count;
+        const uint64_t slot = active ? f.clipQueue[q] : 0u;
+        const int di = (active && f.numDraws > 1) ? find_draw(f, slot) : 0;
         const DrawDesc& d = f.draws[di];
         const uint64_t local = slot - d.slotBase;
-        const uint64_t inst = local / d.numTris;
+        const uint64_t inst = active ? local / d.numTris : 0u;
         const uint64_t tri = local - inst * d.numTris;
         const uint64_t i = d.elementBegin + 3u * tri;
-        /* lanes 0..2: the triangle's vertices */
+        /* lanes 0..2 of the half: the triangle's vertices */
         uint64_t vid = 0;
         float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (lane < 3)
+        if (active && sl < 3)
         {
-            vid = (d.indexType >= 0) ? read_index(d, i + lane) : (i + lane);
+            vid = (d.indexType >= 0) ? read_index(d, i + sl) : (i + sl);
             if (d.cacheVerts)
             {
                 vid += d.cacheBase + inst * d.cacheVerts;
@@ -1083,8 +1138,8 @@ __global__ void __launch_bounds__(128) clip_kernel(const Frame f)
             }
         }
         const uint64_t primIndex = d.primBase + d.numElements * inst + i;
-        const uint32_t info = clip_warp<P>(f, d, (uint32_t)di, slot, primIndex, inst, vid, p);
-        if (lane == 0) f.slotInfo[slot] = info;
+        const uint32_t info = clip_pair<P>(f, active, d, (uint32_t)di, slot, primIndex, inst, vid, p);
+        if (active && sl == 0) f.slotInfo[slot] = info;
     }
 }
 
@@ -2369,7 +2424,7 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
             if (p < *reinterpret_cast<volatile unsigned long long*>(sBest + idx))
             {
                 atomicMin(sBest + idx, p);
-                if (!marked)
+                if (kGeneral && !marked)
                 {
                     marked = true;
                     atomicOr(sWon + (i >> 5), 1u << (i & 31));
@@ -2575,12 +2630,21 @@ __global__ void __launch_bounds__(kFreeThreads, kGeneral ? 4 : FreeLayout<TW, TH
         for (int w = 0; w < warp; ++w) incl += sWarp[w];
         sPre[threadIdx.x + 1] = incl;
         if (threadIdx.x == 0) sPre[0] = 0u;
-        for (int w = threadIdx.x; w < L::kWonWords; w += kFreeThreads) sWon[w] = 0u;
+        if (kGeneral)
+        {
+            for (int w = threadIdx.x; w < L::kWonWords; w += kFreeThreads) sWon[w] = 0u;
+        }
         __syncthreads();
 
         free_walk<TW, TH, false, kGeneral>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB, sWon);
-        __syncthreads();
-        free_walk<TW, TH, true, kGeneral>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB, sWon);
+        if (kGeneral)
+        {
+            /* line and wireframe fragments cannot be re-derived from the
+             * pixel alone: the winners store their interpolants */
+            __syncthreads();
+            free_walk<TW, TH, true, kGeneral>(sRec, sKey, sPre, cnt, x0, y0, xLimit, f.width, f.height, depthFunc, mask, sD0, sBest, sB,
+                                              sWon);
+        }
     }
     __syncthreads();
 
@@ -2599,11 +2663,29 @@ __global__ void __launch_bounds__(kFreeThreads, kGeneral ? 4 : FreeLayout<TW, TH
         const uint64_t rec = key_to_record(f, key);
         const float4* R = f.records + rec * kRecordVec4;
         const DrawDesc& dd = f.draws[__float_as_uint(R[7].x)];
-        const float4 b = sB[i];
+        const uint32_t kind = __float_as_uint(R[7].w);
+        float4 b;
+        if (kGeneral)
+        {
+            b = sB[i];
+        }
+        else if (kind & kRecordPoint)
+        {
+            b = make_float4(0.f, 0.f, 0.f, R[0].z);
+        }
+        else
+        {
+            /* the winner's barycentrics and depth at this pixel, re-derived
+             * by the walk's own chain: the column class of x starts at the
+             * same xs and takes the same (x - xs) / 4 additions */
+            const float yf = (float)y;
+            Chain ch;
+            (void)chain_begin_span(R, yf, scanline_span(R[0], R[1], yf), x, x + 1, ch);
+            b = make_float4(ch.b0, ch.b1, ch.b2, chain_depth(R, ch));
+        }
         if ((f.color || f.generic0) && dd.numOutputs > 0)
         {
             float4 o;
-            const uint32_t kind = __float_as_uint(R[7].w);
             bool kept;
             if (kind & kRecordPoint)
             {
@@ -2871,7 +2953,7 @@ cudaError_t launch_vertex_stage(const Frame& f, cudaStream_t s)
         if (f.hasLines || f.hasWire) vs_setup_kernel<P, true, false><<<blocks, vsBlock, 0, s>>>(f);
         else if (f.allCached) vs_setup_kernel<P, false, true><<<blocks, vsBlock, 0, s>>>(f);
         else vs_setup_kernel<P, false, false><<<blocks, vsBlock, 0, s>>>(f);
-        clip_kernel<P><<<152 * 6, 128, 0, s>>>(f);   /* 80 registers: six CTAs per SM */
+        clip_kernel<P><<<152 * 3, 128, 0, s>>>(f);   /* 128 registers: three CTAs per SM */
     }
     return cudaGetLastError();
 }
