@@ -1845,19 +1845,52 @@ __device__ __forceinline__ bool shade_line(const Frame& f, const DrawDesc& dd, u
     return kept;
 }
 
+/* Shared-memory pitch of a staged record: its 8 vectors and one unused, so
+ * that lanes reading one vector of 32 different records spread over the
+ * banks (a 128-byte pitch puts them all in the same four). */
+constexpr int kStagedVec4 = kRecordVec4 + 1;
+
 template <int TW, int TH, class Color>
 struct RasterLayout
 {
     static constexpr int kThreads = TH * 4;
     static constexpr int kStride = TW + 4;       /* row pitch of the tile buffers (bank spread) */
-    static constexpr int kBatch = 64;            /* records staged per step */
+    static constexpr int kBatch = 48;            /* records staged per step (two buffers: 7 CTAs of 64x32 RGBA8 fit an SM) */
     static constexpr int kPix = TH * kStride;
-    static constexpr size_t kRecBytes = sizeof(float4) * kBatch * kRecordVec4;
-    /* ordered path: colour + depth tile, records, record ids, then keys,
-     * then each tile row's depth range (lo, hi) at the start of a batch */
-    static constexpr size_t kRowDOff = sizeof(typename Color::stored) * kPix + sizeof(float) * kPix + kRecBytes + 2 * sizeof(uint32_t) * kBatch;
+    static constexpr size_t kRecBytes = sizeof(float4) * kBatch * kStagedVec4;
+    /* ordered path: colour + depth tile, two record buffers (one batch is
+     * walked while the next arrives), their keys, then each tile row's
+     * depth range (lo, hi) at the start of a batch */
+    static constexpr size_t kRecOff = sizeof(typename Color::stored) * kPix + sizeof(float) * kPix;
+    static constexpr size_t kKeyOff = kRecOff + 2 * kRecBytes;
+    static constexpr size_t kRowDOff = kKeyOff + 2 * sizeof(uint32_t) * kBatch;
     static constexpr size_t ordered_bytes() { return kRowDOff + 2 * sizeof(float) * TH; }
 };
+
+/* Starts copying records [b0, b0+cnt) of the tile list into shared memory
+ * (cp.async, one commit group per call); their keys are stored directly.
+ * The copies are complete for the calling thread after cp_async_wait, and
+ * for the block after a barrier that follows it. */
+__device__ __forceinline__ void stage_records_async(const Frame& f, const uint32_t* keys, int cnt, float4* sRec, uint32_t* sKey)
+{
+    for (int i = threadIdx.x; i < cnt * kRecordVec4; i += blockDim.x)
+    {
+        const int ri = i / kRecordVec4, part = i % kRecordVec4;
+        const uint32_t key = keys[ri];
+        if (part == 0) sKey[ri] = key;
+        const float4* src = f.records + key_to_record(f, key) * kRecordVec4 + part;
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sRec + ri * kStagedVec4 + part);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+/* Waits for this thread's copies of all groups but the newest `pending`. */
+template <int pending>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(pending) : "memory");
+}
 
 /* Stages records [b0, b0+cnt) of the tile list into shared memory. */
 template <int Batch>
@@ -1868,7 +1901,7 @@ __device__ __forceinline__ void stage_records(const Frame& f, const uint32_t* ke
         const int ri = i / kRecordVec4, part = i % kRecordVec4;
         const uint32_t key = keys[ri];
         if (part == 0) sKey[ri] = key;
-        sRec[i] = f.records[key_to_record(f, key) * kRecordVec4 + part];
+        sRec[ri * kStagedVec4 + part] = f.records[key_to_record(f, key) * kRecordVec4 + part];
     }
 }
 
@@ -1886,7 +1919,7 @@ __device__ __forceinline__ void for_band_records(const float4* sRec, int cnt, in
         bool hit = false;
         if (ri < cnt)
         {
-            const float4 r6 = sRec[ri * kRecordVec4 + 6];
+            const float4 r6 = sRec[ri * kStagedVec4 + 6];
             hit = __float_as_int(r6.x) < bandY0 + 8 && __float_as_int(r6.y) > bandY0 && keep(ri, r6);
         }
         unsigned mask = __ballot_sync(0xFFFFFFFFu, hit);
@@ -2024,8 +2057,8 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
     extern __shared__ __align__(16) uint8_t smem[];
     Stored*   sColor = reinterpret_cast<Stored*>(smem);
     float*    sDepth = reinterpret_cast<float*>(smem + sizeof(Stored) * L::kPix);
-    float4*   sRec   = reinterpret_cast<float4*>(smem + sizeof(Stored) * L::kPix + sizeof(float) * L::kPix);
-    uint32_t* sRecKey = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(sRec) + L::kRecBytes);
+    float4*   sRecBuf = reinterpret_cast<float4*>(smem + L::kRecOff);
+    uint32_t* sKeyBuf = reinterpret_cast<uint32_t*>(smem + L::kKeyOff);
     float*    sRowD  = reinterpret_cast<float*>(smem + L::kRowDOff);
 
     const int tile = blockIdx.x;
@@ -2063,10 +2096,24 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
     const float yf = (float)y;
     const int bandY0 = y0 + ((threadIdx.x >> 5) << 3);
 
-    for (uint32_t b0 = 0; b0 < n; b0 += L::kBatch)
+    /* batch k is walked from buffer k & 1 while batch k + 1 is copied into
+     * the other (its last readers finished at the barrier ending batch k - 1) */
+    stage_records_async(f, sKeys, (int)min((uint32_t)L::kBatch, n), sRecBuf, sKeyBuf);
+    for (uint32_t b0 = 0, k = 0; b0 < n; b0 += L::kBatch, ++k)
     {
         const int cnt = (int)min((uint32_t)L::kBatch, n - b0);
-        stage_records<L::kBatch>(f, sKeys + b0, cnt, sRec, sRecKey);
+        float4* sRec = sRecBuf + (k & 1) * (L::kBatch * kStagedVec4);
+        uint32_t* sRecKey = sKeyBuf + (k & 1) * L::kBatch;
+        if (b0 + L::kBatch < n)
+        {
+            stage_records_async(f, sKeys + b0 + L::kBatch, (int)min((uint32_t)L::kBatch, n - b0 - L::kBatch),
+                                sRecBuf + ((k + 1) & 1) * (L::kBatch * kStagedVec4), sKeyBuf + ((k + 1) & 1) * L::kBatch);
+            cp_async_wait<1>();
+        }
+        else
+        {
+            cp_async_wait<0>();
+        }
         /* the depth range of this thread's pixels at the start of the batch:
          * a bound for the whole batch, since depth only moves one way
          * (Frame::depthBound) */
@@ -2107,7 +2154,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
             {
                 return true;
             }
-            const float4* R = sRec + ri * kRecordVec4;
+            const float4* R = sRec + ri * kStagedVec4;
             const uint32_t flags = __float_as_uint(R[7].w);
             const int minX = __float_as_int(r6.z), maxX = __float_as_int(r6.w);
             if ((flags & (kRecordLine | kRecordWire | kRecordPoint)) || maxX >= kRectBoundMaxX || maxX < minX)
@@ -2132,7 +2179,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
         };
 
         for_band_records(sRec, cnt, bandY0, keep, [&](int ri) {
-            const float4* R = sRec + ri * kRecordVec4;
+            const float4* R = sRec + ri * kStagedVec4;
             const float4 r6 = R[6];
             if (!rowActive || y < __float_as_int(r6.x) || y >= __float_as_int(r6.y))
             {
@@ -2366,8 +2413,8 @@ struct FreeLayout
     static constexpr int kBatch = (TW * TH <= 64) ? 96 : kFreeBatch;
     /* resident CTAs the launch bounds ask for */
     static constexpr int kMinBlocks = (TW * TH <= 64) ? 12 : 4;
-    static constexpr size_t kRecOff = 0;                                                   /* float4 [batch][8] */
-    static constexpr size_t kBOff = kRecOff + sizeof(float4) * kBatch * kRecordVec4;        /* float4 (b0, b1, b2, z) per pixel */
+    static constexpr size_t kRecOff = 0;                                                   /* float4 [batch][kStagedVec4] */
+    static constexpr size_t kBOff = kRecOff + sizeof(float4) * kBatch * kStagedVec4;        /* float4 (b0, b1, b2, z) per pixel */
     static constexpr size_t kBestOff = kBOff + sizeof(float4) * kPix;                      /* u64 per pixel */
     static constexpr size_t kD0Off = kBestOff + sizeof(unsigned long long) * kPix;         /* pre-launch depth per pixel */
     static constexpr size_t kKeyOff = kD0Off + sizeof(float) * kPix;                       /* u32 per staged record */
@@ -2438,7 +2485,7 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
             if (sPre[mid] <= i) lo = mid;
             else hi = mid;
         }
-        const float4* R = sRec + lo * kRecordVec4;
+        const float4* R = sRec + lo * kStagedVec4;
         const int y = max(__float_as_int(R[6].x), y0) + (int)(i - sPre[lo]);
         if (kGeneral && (__float_as_uint(R[7].w) & kRecordLine))
         {
@@ -2537,18 +2584,35 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
         }
         const uint32_t key = sKey[lo];
         const int rowBase = (y - y0) * TW - x0;
+        /* the four column chains of chain_begin_span / chain_step /
+         * chain_depth, with the row terms they share computed once */
+        const float4 r2 = R[2], r3 = R[3], r4 = R[4], r5 = R[5];
+        const float bcY0 = r3.x * yf + r4.x, bcY1 = r3.y * yf + r4.y, bcY2 = r3.z * yf + r4.z;
+        const float s0 = r2.x * 4.f, s1 = r2.y * 4.f, s2 = r2.z * 4.f;
+        const float zw = 0.f * r2.w;
+        const int xEnd = min(sp.xMax, xLimit);
 #pragma unroll 1
         for (int l = 0; l < 4; ++l)
         {
-            Chain ch;
-            if (!chain_begin_span(R, yf, sp, x0 + l, xLimit, ch))
+            const int myX0 = x0 + l;
+            const int xs = sp.xMin + ((myX0 - sp.xMin) & 3);
+            const int xFirst = max(xs, myX0);
+            if (xFirst >= xEnd)
             {
                 continue;
             }
-            for (; ch.x < ch.xEnd; chain_step(ch))
+            const float xsf = (float)xs;
+            float b0 = r2.x * xsf + bcY0, b1 = r2.y * xsf + bcY1, b2 = r2.z * xsf + bcY2;
+            for (int g = (xFirst - xs) >> 2; g > 0; --g)
             {
-                const float z = chain_depth(R, ch);
-                const int idx = rowBase + ch.x;
+                b0 += s0;
+                b1 += s1;
+                b2 += s2;
+            }
+            for (int x = xFirst; x < xEnd; x += 4, b0 += s0, b1 += s1, b2 += s2)
+            {
+                const float z = __fadd_rn((r3.w * b0 + r4.w * b1) + r5.x * b2, zw);
+                const int idx = rowBase + x;
                 if (!depth_cmp(func, z, sD0[idx]))
                 {
                     continue;
@@ -2556,7 +2620,7 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
                 const unsigned long long p = free_pack(func, mask, z, key);
                 if (kStore)
                 {
-                    if (sBest[idx] == p) sB[idx] = make_float4(ch.b0, ch.b1, ch.b2, z);
+                    if (sBest[idx] == p) sB[idx] = make_float4(b0, b1, b2, z);
                 }
                 else
                 {
@@ -2613,7 +2677,7 @@ __global__ void __launch_bounds__(kFreeThreads, kGeneral ? 4 : FreeLayout<TW, TH
         uint32_t rows = 0;
         if ((int)threadIdx.x < cnt)
         {
-            const float4 r6 = sRec[threadIdx.x * kRecordVec4 + 6];
+            const float4 r6 = sRec[threadIdx.x * kStagedVec4 + 6];
             const int ry0 = max(__float_as_int(r6.x), y0);
             const int ry1 = min(__float_as_int(r6.y), yLimit);
             rows = (ry1 > ry0) ? (uint32_t)(ry1 - ry0) : 0u;
