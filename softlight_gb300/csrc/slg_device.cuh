@@ -238,7 +238,7 @@ struct Frame
     uint32_t  binChunks;
     uint32_t* itemKey;            /* per bin in push order: its tile-list key (launches without recOfRank) */
 
-    /* the ordered raster's depth bound (depth_bound_rejects): 1 when every
+    /* the ordered raster's depth bound (depth_range_rect): 1 when every
      * draw uses LESS / LESS_EQUAL, 2 when every draw uses GREATER /
      * GREATER_EQUAL, and no fragment program writes depth (the depth of a
      * pixel then only moves one way); 0 otherwise */

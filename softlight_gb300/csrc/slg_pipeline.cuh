@@ -1907,8 +1907,9 @@ __device__ __forceinline__ void stage_records(const Frame& f, const uint32_t* ke
 
 /* The warp owns rows [bandY0, bandY0 + 8): the 32 lanes test 32 staged
  * records at once against that band and the warp walks only the hits, in
- * order (ballot + find-first-set compaction). keep(ri, r6) may drop a hit
- * whose walk can change nothing. */
+ * order (ballot + find-first-set compaction). keep(ri, r6, lo, hi) may drop
+ * a hit whose walk can change nothing, and bound its depths in the band;
+ * fn(ri, lo, hi) walks it. */
 template <class Keep, class Fn>
 __device__ __forceinline__ void for_band_records(const float4* sRec, int cnt, int bandY0, Keep&& keep, Fn&& fn)
 {
@@ -1917,17 +1918,19 @@ __device__ __forceinline__ void for_band_records(const float4* sRec, int cnt, in
     {
         const int ri = base + lane;
         bool hit = false;
+        /* keep may narrow the record's depths in the band to [lo, hi] */
+        float lo = __int_as_float(0xFF800000), hi = __int_as_float(0x7F800000);
         if (ri < cnt)
         {
             const float4 r6 = sRec[ri * kStagedVec4 + 6];
-            hit = __float_as_int(r6.x) < bandY0 + 8 && __float_as_int(r6.y) > bandY0 && keep(ri, r6);
+            hit = __float_as_int(r6.x) < bandY0 + 8 && __float_as_int(r6.y) > bandY0 && keep(ri, r6, lo, hi);
         }
         unsigned mask = __ballot_sync(0xFFFFFFFFu, hit);
         while (mask)
         {
             const int j = __ffs(mask) - 1;
             mask &= mask - 1;
-            fn(base + j);
+            fn(base + j, __shfl_sync(0xFFFFFFFFu, lo, j), __shfl_sync(0xFFFFFFFFu, hi, j));
         }
     }
 }
@@ -1945,70 +1948,28 @@ __device__ __forceinline__ bool ordered_raster_runs(const Frame& f)
     return !f.orderFree || (f.aliasCount != nullptr && *f.aliasCount != 0u);
 }
 
-/* Whether no pixel of one thread's part of a scan-line can pass the depth
- * test: the pixels xFirst, xFirst + 4, .. <= xLast of row yf, whose stored
- * depth is at most dMax (dMin for the greater tests). Their depth, as the
- * walk computes it (chain_begin_span / chain_step / chain_depth), is the
- * plane z = A x + Cy of the record's barycentric gradients plus rounding;
- * the plane's extreme over the pixels is at xFirst or xLast, and the
- * rounding is bounded by the magnitudes the walk meets: the start value
- * bc0 * xs + (bc1 * y + bc2) (terms of size Binit, a few roundings), then k
- * additions of 4 * bc0 to values of size at most Bchain (one rounding each,
- * |error| <= 2^-24 * |value|), then the depth dot product (three roundings
- * on terms |z_i b_i|). The margin counts each rounding at 2^-21, eight
- * times the unit roundoff. NaNs make every comparison false: nothing is
- * rejected. */
-__device__ __forceinline__ bool depth_bound_rejects(const float4* R, float yf, int xs, int xFirst, int xLast, int func, float dMin,
-                                                    float dMax)
-{
-    const float4 r2 = R[2], r3 = R[3], r4 = R[4];
-    const float z0 = r3.w, z1 = r4.w, z2 = R[5].x;
-    const float bx[3] = {r2.x, r2.y, r2.z};
-    const float by[3] = {r3.x * yf + r4.x, r3.y * yf + r4.y, r3.z * yf + r4.z};
-    const float xsf = (float)xs, xaf = (float)xFirst, xbf = (float)xLast;
-    float binit = 0.f, bchain = 0.f;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-    {
-        const float ri = (i == 0) ? r3.x : (i == 1) ? r3.y : r3.z;
-        const float ci = (i == 0) ? r4.x : (i == 1) ? r4.y : r4.z;
-        binit = fmaxf(binit, fabsf(bx[i] * xsf) + fabsf(ri * yf) + fabsf(ci));
-        bchain = fmaxf(bchain, fmaxf(fabsf(bx[i] * xsf + by[i]), fabsf(bx[i] * xbf + by[i])));
-    }
-    const float A = (z0 * bx[0] + z1 * bx[1]) + z2 * bx[2];
-    const float C = (z0 * by[0] + z1 * by[1]) + z2 * by[2];
-    const float za = A * xaf + C, zb = A * xbf + C;
-    const float k = (float)((xLast - xs) / 4 + 1);
-    const float zs = (fabsf(z0) + fabsf(z1)) + fabsf(z2);
-    const float margin = 4.76837158203125e-07f * zs * (4.f * binit + (k + 8.f) * bchain);   /* 2^-21 */
-    const float lo = fminf(za, zb) - margin, hi = fmaxf(za, zb) + margin;
-    switch (func)
-    {
-        case SLG_DEPTH_TEST_LESS_THAN:     return lo >= dMax;
-        case SLG_DEPTH_TEST_LESS_EQUAL:    return lo > dMax;
-        case SLG_DEPTH_TEST_GREATER_THAN:  return hi <= dMin;
-        case SLG_DEPTH_TEST_GREATER_EQUAL: return hi < dMin;
-        default:                           return false;
-    }
-}
-
-/* Largest screen coordinate for which depth_bound_rect holds: below it the
+/* Largest screen coordinate for which depth_range_rect holds: below it the
  * scan-line span arithmetic errs by far less than a pixel, so every span
  * lies in the record's [minX - 1, maxX + 1] (screen vertices are whole
  * pixels: to_screen floors them), as the tile binning also relies on. */
 constexpr int kRectBoundMaxX = 1 << 20;
 
-/* depth_bound_rejects for every thread of a warp at once: whether no pixel
- * of a triangle record on rows [ya, yb] of columns [xa, xb] can pass, given
- * the range [dMin, dMax] of the stored depths there. Each walked chain
- * starts at some xs in [xsMin, xb] (xsMin <= the span's start, >= 0) and
- * ends by xb; the plane z = A x + B y + C takes its extremes over the
- * rectangle at its corners, and the rounding terms take the largest start
- * (|bc0| xb + |bc1| yb + |bc2|) and chain values (the corners of
- * [xsMin, xb] x [ya, yb], the barycentrics being affine) and the longest
- * chain, so the margin bounds the one of every thread's walk. */
-__device__ __forceinline__ bool depth_bound_rect(const float4* R, int ya, int yb, int xa, int xb, int xsMin, int func, float dMin,
-                                                 float dMax)
+/* The depths a triangle record's walk can produce on rows [ya, yb] of
+ * columns [xa, xb], as [lo, hi]. A fragment's depth, as the walk computes it
+ * (chain_begin_span / chain_step / chain_depth), is the plane z = A x + B y
+ * + C of the record's barycentric gradients plus rounding: the start value
+ * bc0 * xs + (bc1 * y + bc2) (terms of size Binit, a few roundings), then k
+ * additions of 4 * bc0 to values of size at most Bchain (one rounding each,
+ * |error| <= 2^-24 * |value|), then the depth dot product (three roundings
+ * on terms |z_i b_i|). The margin counts each rounding at 2^-21, eight
+ * times the unit roundoff. Each walked chain starts at some xs in [xsMin,
+ * xb] (xsMin <= the span's start, >= 0) and ends by xb; the plane takes its
+ * extremes over the rectangle at its corners, and the rounding terms take
+ * the largest start (|bc0| xb + |bc1| yb + |bc2|) and chain values (the
+ * corners of [xsMin, xb] x [ya, yb], the barycentrics being affine) and the
+ * longest chain, so the margin bounds the one of every walk there. NaNs
+ * make the range NaN, which rejects nothing. */
+__device__ __forceinline__ void depth_range_rect(const float4* R, int ya, int yb, int xa, int xb, int xsMin, float& lo, float& hi)
 {
     const float4 r2 = R[2], r3 = R[3], r4 = R[4];
     const float z0 = r3.w, z1 = r4.w, z2 = R[5].x;
@@ -2034,8 +1995,14 @@ __device__ __forceinline__ bool depth_bound_rect(const float4* R, int ya, int yb
     const float k = (float)((xb - xsMin) / 4 + 1);
     const float zs = (fabsf(z0) + fabsf(z1)) + fabsf(z2);
     const float margin = 4.76837158203125e-07f * zs * (4.f * binit + (k + 8.f) * bchain);   /* 2^-21 */
-    const float lo = fminf(fminf(zaa, zba), fminf(zab, zbb)) - margin;
-    const float hi = fmaxf(fmaxf(zaa, zba), fmaxf(zab, zbb)) + margin;
+    lo = fminf(fminf(zaa, zba), fminf(zab, zbb)) - margin;
+    hi = fmaxf(fmaxf(zaa, zba), fmaxf(zab, zbb)) + margin;
+}
+
+/* Whether no fragment of depth in [lo, hi] passes func against stored
+ * depths in [dMin, dMax] (NaNs reject nothing). */
+__device__ __forceinline__ bool depth_range_rejects(int func, float lo, float hi, float dMin, float dMax)
+{
     switch (func)
     {
         case SLG_DEPTH_TEST_LESS_THAN:     return lo >= dMax;
@@ -2147,9 +2114,9 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
         __syncthreads();
 
         /* a triangle record none of whose pixels in the band can pass the
-         * depth test is dropped for the whole warp (depth_bound_rect over
+         * depth test is dropped for the whole warp (depth_range_rect over
          * its rows in the band and its columns in the tile) */
-        const auto keep = [&](int ri, const float4 r6) {
+        const auto keep = [&](int ri, const float4 r6, float& zlo, float& zhi) {
             if (!f.depthBound)
             {
                 return true;
@@ -2175,10 +2142,11 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 lo = fminf(lo, sRowD[2 * (yy - y0)]);
                 hi = fmaxf(hi, sRowD[2 * (yy - y0) + 1]);
             }
-            return !depth_bound_rect(R, ya, yb, xa, xb, xsMin, flags & 0xF, lo, hi);
+            depth_range_rect(R, ya, yb, xa, xb, xsMin, zlo, zhi);
+            return !depth_range_rejects(flags & 0xF, zlo, zhi, lo, hi);
         };
 
-        for_band_records(sRec, cnt, bandY0, keep, [&](int ri) {
+        for_band_records(sRec, cnt, bandY0, keep, [&](int ri, float zlo, float zhi) {
             const float4* R = sRec + ri * kStagedVec4;
             const float4 r6 = R[6];
             if (!rowActive || y < __float_as_int(r6.x) || y >= __float_as_int(r6.y))
@@ -2315,16 +2283,10 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 return;
             }
             const int depthFunc = flags & 0xF;
-            if (f.depthBound)
+            /* the record's depths in the band against this thread's pixels */
+            if (f.depthBound && depth_range_rejects(depthFunc, zlo, zhi, dMin, dMax))
             {
-                const int xEnd = min(sp.xMax, xLimit);
-                const int xs = sp.xMin + ((myX0 - sp.xMin) & 3);
-                const int xFirst = max(xs, myX0);
-                if (xFirst >= xEnd ||
-                    depth_bound_rejects(R, yf, xs, xFirst, xFirst + ((xEnd - 1 - xFirst) & ~3), depthFunc, dMin, dMax))
-                {
-                    return;
-                }
+                return;
             }
             Chain ch;
             if (!chain_begin_span(R, yf, sp, myX0, xLimit, ch))
