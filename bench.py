@@ -15,6 +15,7 @@ the uniform block and instance matrices are uploaded, the frame is drawn and
 the colour attachment is read back to pinned host memory.
 """
 import argparse
+import atexit
 import json
 import os
 import statistics
@@ -116,7 +117,8 @@ def workload_config(name):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 20 ms; only the
+    samples taken inside the timed windows (begin() .. end()) count."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -124,35 +126,55 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.lines = []
+        self.lines = []      # (perf_counter, line)
+        self.windows = []    # (t0, t1)
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            atexit.register(self._stop)
+            # the first sample takes a moment: start timing once it arrived
+            t_end = time.perf_counter() + 3.0
+            while not self.lines and time.perf_counter() < t_end and self.proc.poll() is None:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
-    def __exit__(self, *exc):
-        if self.proc:
+    def begin(self):
+        self.windows.append([time.perf_counter(), None])
+
+    def end(self):
+        if self.windows and self.windows[-1][1] is None:
+            self.windows[-1][1] = time.perf_counter()
+
+    def _stop(self):
+        if self.proc and self.proc.poll() is None:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.05)     # the sample covering the end of the last window
+            self._stop()
+
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for t, ln in self.lines:
+            if not any(t0 <= t <= (t1 if t1 is not None else t) for t0, t1 in self.windows):
+                continue
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -166,7 +188,8 @@ class ClockSampler:
                     reasons.add(n)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm),
+                "interval_ms": 20}
 
 
 def measured_peaks():
@@ -440,12 +463,15 @@ def time_workload(name, args, sg, torch, flush, world, local, rank, clocks=None,
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    # clocks are sampled over the timed frames, the stage-timed ones and the
+    # end-to-end frames below
     if clocks is not None:
-        with clocks:
-            step_ms, _ = timed_frames(args.steps, False)
-    else:
-        step_ms, _ = timed_frames(args.steps, False)
+        clocks.__enter__()
+        clocks.begin()
+    step_ms, _ = timed_frames(args.steps, False)
     _, stage_ms = timed_frames(max(3, min(args.steps, 10)), True)
+    if clocks is not None:
+        clocks.end()
     torch.cuda.synchronize()
     total_ms = max_over_ranks(sum(step_ms), world)
     fps = replica_throughput(world, args.steps, total_ms / 1000.0)
@@ -489,6 +515,8 @@ def time_workload(name, args, sg, torch, flush, world, local, rank, clocks=None,
         read_color()
     if world > 1:
         torch.distributed.barrier()
+    if clocks is not None:
+        clocks.begin()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         ctx.ubo_assign_many(ubo_ids, ubo_host)
@@ -497,6 +525,9 @@ def time_workload(name, args, sg, torch, flush, world, local, rank, clocks=None,
         scene.render()
         read_color()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    if clocks is not None:
+        clocks.end()
+        clocks.__exit__(None, None, None)
     out["e2e"] = {"value": replica_throughput(world, args.steps, e2e_s), "unit": "frames/s", "h2d_bytes_per_step": h2d,
                   "d2h_bytes_per_step": color_bytes}
 
