@@ -44,6 +44,9 @@ def parse():
     p.add_argument("--ref-seconds", type=float, default=0.0,
                    help="reference arm: time full frames for about this long (median) instead of --steps")
     p.add_argument("--tile", default="auto", help="screen tile WxH (8x8 .. 64x64) or auto (autotuner)")
+    p.add_argument("--raster", default="auto", choices=["auto", "tiled", "untiled"],
+                   help="order-free launches: the autotuner's pick (with --tile auto; tiled with a fixed tile), on "
+                        "screen tiles, or untiled")
     return p.parse_args()
 
 
@@ -425,6 +428,8 @@ def time_workload(name, args, sg, torch, flush, world, local, rank, clocks=None,
     scene = builder(ctx, **kwargs)
     stream = torch.cuda.ExternalStream(ctx.stream_handle())
     cmds = [sg.api.DrawCmd(m, n, sh) for (m, n, sh) in scene.draws]
+    if args.raster != "auto":
+        ctx.set_raster_mode(2 if args.raster == "tiled" else 3)
     if args.tile == "auto":
         tw, th, vb = ctx.autotune(cmds, scene.fbo, scene.clear_color, scene.clear_depth)
     else:
@@ -477,6 +482,7 @@ def time_workload(name, args, sg, torch, flush, world, local, rank, clocks=None,
     fps = replica_throughput(world, args.steps, total_ms / 1000.0)
     out = {"workload": cfg["workload"], "config": cfg, "value": fps, "unit": "frames/s", "ms_per_step": total_ms / args.steps,
            "tile": f"{tw}x{th}", "vertex_block": vb, "batched_graph": bool(scene.batched),
+           "order_free_raster": "untiled" if ctx.untiled_raster() else "tiles",
            "triangles_per_frame": scene.num_triangles, "launches_per_frame": launches_per_frame(scene)}
 
     if scene.batched:
@@ -592,7 +598,7 @@ def run_gpu(args):
         cfg = dict(head["config"])
         cfg.update({"l2": "flushed between timed frames (256 MiB write)", "tile": head["tile"],
                     "vertex_block": head["vertex_block"], "tuned": args.tile == "auto", "batched_graph": head["batched_graph"],
-                    "triangles_per_frame": head["triangles_per_frame"]})
+                    "order_free_raster": head["order_free_raster"], "triangles_per_frame": head["triangles_per_frame"]})
         line = {"metric": METRIC, "value": head["value"], "unit": "frames/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",

@@ -476,9 +476,17 @@ int slg_set_scratch_caps(slg_context* ctx, size_t maxEntries, size_t maxClipReco
 
 /* Raster strategy: 0 (default) picks the order-free resolve for launches
  * without blending and with one order-independent depth rule, else the
- * ordered per-pixel replay; 1 forces the ordered replay. Both give the same
+ * ordered per-pixel replay; the order-free resolve of triangle and point
+ * launches with one colour target runs untiled (every record walked once
+ * into per-pixel best words) when slg_autotune found that faster, on screen
+ * tiles otherwise. 1 forces the ordered replay, 2 keeps order-free launches
+ * on tiles, 3 runs them untiled where they qualify. All give the same
  * image. */
 int slg_set_raster_mode(slg_context* ctx, int mode);
+
+/* Whether order-free triangle and point launches run untiled (1) or on
+ * screen tiles (0) under the current raster mode and autotuner pick. */
+int slg_untiled_raster(const slg_context* ctx);
 
 /* Threads per block of the vertex/set-up stage, i.e. triangles per CTA: 64,
  * 128 (default) or 256. */
@@ -490,8 +498,10 @@ int slg_set_vertex_block(slg_context* ctx, int threads);
 int slg_set_batch_graphs(slg_context* ctx, int enable);
 
 /* Autotuner: renders clear(rgba, depth) + slg_draw_batch(cmds) with every
- * supported tile size and vertex block size, keeps the fastest for the
- * context and returns it in out = {tileW, tileH, vertex block}. The
+ * supported tile size and vertex block size, then untiled (order-free
+ * launches of triangles and points) with every vertex block size, keeps the
+ * fastest for the context and returns it in out = {tileW, tileH, vertex
+ * block}; slg_untiled_raster tells whether the untiled raster won. The
  * framebuffer holds the last trial's frame afterwards. */
 int slg_autotune(slg_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, size_t fboId,
                  const double rgba[4], double depth, int out[3]);

@@ -161,6 +161,7 @@ _GPU_SIGNATURES = [
     ("profile_stages", C.c_int, [C.c_void_p, C.c_int]),
     ("stage_times", C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     ("set_raster_mode", C.c_int, [C.c_void_p, C.c_int]),
+    ("untiled_raster", C.c_int, [C.c_void_p]),
     ("set_vertex_block", C.c_int, [C.c_void_p, C.c_int]),
     ("set_batch_graphs", C.c_int, [C.c_void_p, C.c_int]),
     ("autotune", C.c_int, [C.c_void_p, C.POINTER(DrawCmd), C.c_size_t, C.c_size_t, C.POINTER(C.c_double),
@@ -473,6 +474,10 @@ class SLContext:
 
     def set_raster_mode(self, mode):
         self._call("set_raster_mode", mode)
+
+    def untiled_raster(self):
+        """Whether order-free triangle / point launches run untiled."""
+        return bool(self._fn("untiled_raster")(self._h))
 
     def set_vertex_block(self, threads):
         self._call("set_vertex_block", threads)

@@ -277,6 +277,10 @@ struct slg_context
     DevBuffer rankOf, recOfRank, seqRec, seqKey, binBlocks;   /* blend order of a multi-mesh draw */
     uint64_t rankCap = 0;
     DevBuffer chunkCounts, itemKey;    /* tile lists in key order (Frame::chunkCounts) */
+    DevBuffer bestWords, ovfKey;       /* untiled order-free raster (Frame::bestWords) */
+    bool forceTiled = false;           /* slg_set_raster_mode 2: order-free launches on tiles */
+    bool forceUntiled = false;         /* slg_set_raster_mode 3: untiled where eligible */
+    bool untiled = false;              /* the autotuner's pick for order-free triangle / point launches */
     bool sortKeysCapped = false;       /* slg_set_scratch_caps set a sort-key cap */
     uint64_t slotCap = 0, ovfCap = 0, tileCap = 0, entryCap = 0;
 
@@ -1200,6 +1204,19 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
         }
     }
 
+    /* order-free launches of triangles and points run untiled when the
+     * autotuner picked it (or raster mode 3): every record is walked once
+     * into per-pixel best words, no tile lists */
+    if (f.orderFree && !f.hasLines && !f.hasWire && !f.hasMrt && !f.generic0 && numSlots > 0 && !ctx->forceTiled &&
+        (ctx->untiled || ctx->forceUntiled))
+    {
+        const uint64_t pixels = (uint64_t)f.width * f.height;
+        if ((r = dev_alloc(ctx, ctx->bestWords, pixels * sizeof(unsigned long long), false))) return r;
+        if ((r = dev_alloc(ctx, ctx->ovfKey, std::max<uint64_t>(ctx->ovfCap, 1) * sizeof(uint32_t), false))) return r;
+        f.bestWords = static_cast<unsigned long long*>(ctx->bestWords.ptr);
+        f.ovfKey = static_cast<uint32_t*>(ctx->ovfKey.ptr);
+    }
+
     /* from here on the launch is queued: a launch with a device-written
      * draw list (the scene graph's) cannot be replayed */
     {
@@ -1482,7 +1499,7 @@ void slg_context_destroy(slg_context* ctx)
                             &ctx->tileCount, &ctx->tileOffset,
                             &ctx->tileCursor, &ctx->entries, &ctx->blitBuf,
                             &ctx->rankOf, &ctx->recOfRank, &ctx->seqRec, &ctx->seqKey, &ctx->binBlocks,
-                            &ctx->chunkCounts, &ctx->itemKey, &ctx->sortScratch,
+                            &ctx->chunkCounts, &ctx->itemKey, &ctx->bestWords, &ctx->ovfKey, &ctx->sortScratch,
                             &ctx->status, &ctx->devDescs, &ctx->devStarts};
     for (DevBuffer* b : scratch) dev_free(*b);
     if (ctx->graph.exec) cudaGraphExecDestroy(ctx->graph.exec);
@@ -2100,6 +2117,36 @@ int slg_autotune(slg_context* ctx, const slg_draw_cmd* cmds, size_t numCmds, siz
         }
         if (status) break;
     }
+    /* then the untiled order-free raster (the tile size does not matter to
+     * it; launches it does not apply to keep the tiles) */
+    const bool wasUntiled = ctx->untiled;
+    bool bu = wasUntiled && !status;
+    if (!status && !ctx->forceTiled && !ctx->forceOrdered)
+    {
+        bu = false;
+        ctx->tileW = bw;
+        ctx->tileH = bh;
+        ctx->untiled = true;
+        for (int b : blocks)
+        {
+            ctx->vsBlock = b;
+            int r = frame();
+            if (!r) r = frame();
+            if (!r) r = slg_finish(ctx);
+            if (r == SLG_ERR_OVERFLOW) continue;
+            if (r) { status = r; break; }
+            cudaEventRecord(t0, ctx->stream);
+            for (int k = 0; k < 3 && !r; ++k) r = frame();
+            cudaEventRecord(t1, ctx->stream);
+            if (!r) r = slg_finish(ctx);
+            if (r == SLG_ERR_OVERFLOW) continue;
+            if (r) { status = r; break; }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, t0, t1);
+            if (ms < best) { best = ms; bb = b; bu = true; }
+        }
+    }
+    ctx->untiled = status ? wasUntiled : bu;
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     ctx->tileW = bw;
@@ -2335,9 +2382,16 @@ int slg_set_tile_size(slg_context* ctx, int tileW, int tileH)
 
 int slg_set_raster_mode(slg_context* ctx, int mode)
 {
-    if (mode != 0 && mode != 1) return ctx->fail(SLG_ERR_INVALID_ARG, "raster mode must be 0 or 1");
+    if (mode < 0 || mode > 3) return ctx->fail(SLG_ERR_INVALID_ARG, "raster mode must be 0, 1, 2 or 3");
     ctx->forceOrdered = (mode == 1);
+    ctx->forceTiled = (mode == 2);
+    ctx->forceUntiled = (mode == 3);
     return SLG_OK;
+}
+
+int slg_untiled_raster(const slg_context* ctx)
+{
+    return (!ctx->forceTiled && (ctx->untiled || ctx->forceUntiled)) ? 1 : 0;
 }
 
 int slg_profile_stages(slg_context* ctx, int enable)

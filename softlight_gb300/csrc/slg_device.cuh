@@ -238,6 +238,12 @@ struct Frame
     uint32_t  binChunks;
     uint32_t* itemKey;            /* per bin in push order: its tile-list key (launches without recOfRank) */
 
+    /* untiled order-free raster (raster_global_kernel): per pixel the best
+     * word of raster_free_kernel in global memory, and per overflow record
+     * (clipped fan) its key; null: the tiled rasters run */
+    unsigned long long* bestWords;
+    uint32_t* ovfKey;
+
     /* the ordered raster's depth bound (depth_range_rect): 1 when every
      * draw uses LESS / LESS_EQUAL, 2 when every draw uses GREATER /
      * GREATER_EQUAL, and no fragment program writes depth (the depth of a

@@ -794,6 +794,12 @@ cudaError_t launch_scene_draw(const SceneDrawArgs& a, cudaStream_t s)
 /* After the last kernel that can overflow a buffer: counts the launch as
  * done when no overflow has happened yet (status[3]), which tells the host
  * the first launch to replay. */
+__global__ void reset_counts_kernel(const Frame f)
+{
+    *f.ovfCount = 0;
+    *f.clipCount = 0;
+}
+
 __global__ void launch_mark_kernel(int32_t* status)
 {
     if (!(status[0] & kStatusSticky)) status[3] += 1;
@@ -828,6 +834,8 @@ cudaError_t launch_pipeline(const Frame& f, const slg_pipeline_ops& ops, int key
         if (f.rankOf) flush_sort_kernel<<<f.rankGrid, 1024, 0, s>>>(f, numBlocks);
     }
     if (ev) cudaEventRecord(ev[1], s);
+    /* the untiled order-free raster needs no tile lists */
+    const bool untiled = f.bestWords != nullptr;
     const unsigned chunkBlocks = (f.binChunks + kOrderedWarps - 1) / kOrderedWarps;
     const size_t chunkSmem = sizeof(uint32_t) * kOrderedWarps * (size_t)numTiles;
     if (ordered)
@@ -836,19 +844,19 @@ cudaError_t launch_pipeline(const Frame& f, const slg_pipeline_ops& ops, int key
         bin_count_ordered_kernel<<<chunkBlocks, kOrderedWarps * 32, chunkSmem, s>>>(f, numBlocks);
         bin_chunk_scan_kernel<<<(numTiles + 31) / 32, 1024, 0, s>>>(f);
     }
-    tile_scan_kernel<<<1, 1024, 0, s>>>(f, numTiles);
+    if (!untiled) tile_scan_kernel<<<1, 1024, 0, s>>>(f, numTiles);
     if (ev) cudaEventRecord(ev[2], s);
     if (ordered)
     {
         bin_fill_ordered_kernel<<<chunkBlocks, kOrderedWarps * 32, chunkSmem, s>>>(f, numBlocks);
     }
-    else if (f.numSlots > 0)
+    else if (f.numSlots > 0 && !untiled)
     {
         const unsigned blocks = (unsigned)((f.numSlots + 255) / 256);
         bin_fill_kernel<<<blocks, 256, 0, s>>>(f);
     }
     if (ev) cudaEventRecord(ev[3], s);
-    if ((!f.orderFree || f.aliasCount) && !ordered)
+    if ((!f.orderFree || f.aliasCount) && !ordered && !untiled)
     {
         /* keyCap keys of 4 bytes per tile (<= 227 KB of shared memory); for an
          * order-free launch with line draws the device decides whether the
@@ -859,6 +867,12 @@ cudaError_t launch_pipeline(const Frame& f, const slg_pipeline_ops& ops, int key
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     e = (cudaError_t)ops.launch_raster(&f, s);
+    if (untiled)
+    {
+        /* the raster read the clipped-record count: reset it (and the clip
+         * queue's) for the next launch, as tile_scan_kernel does otherwise */
+        reset_counts_kernel<<<1, 1, 0, s>>>(f);
+    }
     if (ev) cudaEventRecord(ev[4], s);
     return e;
 }

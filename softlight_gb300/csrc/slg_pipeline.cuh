@@ -607,7 +607,8 @@ __device__ __forceinline__ uint32_t clip_pair(const Frame& f, bool active, const
         const uint64_t recIndex = f.numSlots + base + sub;
         store_record(f, recIndex, rec);
         store_varyings(f, recIndex, nv, v0, v1, v2);
-        if (f.chunkCounts == nullptr) count_tiles(rec.r[6], f);
+        if (f.ovfKey) f.ovfKey[base + sub] = (uint32_t)(slot << kSubShift) | (sub + 1u);
+        if (f.chunkCounts == nullptr && f.bestWords == nullptr) count_tiles(rec.r[6], f);
     }
     return fits ? 2u + survivors : 0u;
 }
@@ -1195,8 +1196,9 @@ __global__ void __launch_bounds__(256) vs_setup_kernel(const Frame f)
     }
     /* per-tile counts of the unclipped records, one atomic per group of
      * lanes touching the same tile (clipped records count themselves);
-     * launches filling their lists in key order count per chunk instead */
-    warp_tile_walk(f, tr, counted && f.chunkCounts == nullptr, f.tileCount, [](uint32_t, uint32_t) {});
+     * launches filling their lists in key order count per chunk instead,
+     * untiled launches not at all */
+    warp_tile_walk(f, tr, counted && f.chunkCounts == nullptr && f.bestWords == nullptr, f.tileCount, [](uint32_t, uint32_t) {});
 }
 
 /*-----------------------------------------------------------------------------
@@ -2593,6 +2595,83 @@ __device__ __forceinline__ void free_walk(const float4* sRec, const uint32_t* sK
     }
 }
 
+/* Shades the winning fragment p (a best word) of pixel (x, y) once and
+ * writes its colour, depth and visibility id. Triangle winners re-derive
+ * their barycentrics and depth from the record with the walk's own chain
+ * (the column class of x starts at the same xs and takes the same
+ * (x - xs) / 4 additions); kGeneral launches pass what their store pass
+ * kept (`stored`), which line winners need. */
+template <class P, class Color, bool kGeneral>
+__device__ __forceinline__ void resolve_winner(const Frame& f, unsigned long long p, bool keyMax, bool mask, int x, int y, float4 stored)
+{
+    const uint32_t key = keyMax ? ~(uint32_t)p : (uint32_t)p;
+    const size_t gi = (size_t)x + (size_t)f.width * y;
+    const uint64_t rec = key_to_record(f, key);
+    const float4* R = f.records + rec * kRecordVec4;
+    const DrawDesc& dd = f.draws[__float_as_uint(R[7].x)];
+    const uint32_t kind = __float_as_uint(R[7].w);
+    float4 b;
+    if (kGeneral)
+    {
+        b = stored;
+    }
+    else if (kind & kRecordPoint)
+    {
+        b = make_float4(0.f, 0.f, 0.f, R[0].z);
+    }
+    else
+    {
+        const float yf = (float)y;
+        Chain ch;
+        (void)chain_begin_span(R, yf, scanline_span(R[0], R[1], yf), x, x + 1, ch);
+        b = make_float4(ch.b0, ch.b1, ch.b2, chain_depth(R, ch));
+    }
+    if ((f.color || f.generic0) && dd.numOutputs > 0)
+    {
+        float4 o;
+        bool kept;
+        if (kind & kRecordPoint)
+        {
+            slg_frag_coord fc = point_coord(R);
+            kept = shade_point<P, kGeneral>(f, dd, rec, fc, o, gi);
+        }
+        else if (kGeneral && (kind & kRecordLine))
+        {
+            /* stored.y keeps the line step's 16-bit (X, Y): X = W on the row
+             * above for the step stored at column 0 */
+            const uint32_t xy = __float_as_uint(b.y);
+            slg_frag_coord fc = frag_coord(xy & 0xFFFFu, xy >> 16, b.w);
+            kept = shade_line<P, kGeneral>(f, dd, rec, b.x, fc, o, gi);
+        }
+        else
+        {
+            slg_frag_coord fc = frag_coord((uint32_t)x, (uint32_t)y, b.w);
+            kept = shade<P, kGeneral>(f, dd, rec, kind, R[2].w, R[5], b.x, b.y, b.z, fc, o, gi);
+        }
+        if (kept && f.color)
+        {
+            Color::write(f.color, gi, Color::store(o));
+        }
+        if (!kept)
+        {
+            /* the winner is the last fragment that passes, in the
+             * reference's order; when it is discarded the pixel keeps an
+             * earlier fragment's colour, which only the ordered raster
+             * knows: programs that discard are registered as such and
+             * their launches never come here */
+            atomicOr(f.status, kStatusUndeclaredDiscard);
+        }
+    }
+    if (mask)
+    {
+        depth_store(f, gi, b.w);
+    }
+    if (f.ids)
+    {
+        f.ids[gi] = (key >> kSubShift) + 1u;
+    }
+}
+
 template <class P, int TW, int TH, class Color, bool kGeneral>
 __global__ void __launch_bounds__(kFreeThreads, kGeneral ? 4 : FreeLayout<TW, TH>::kMinBlocks) raster_free_kernel(const Frame f, int depthFunc, int depthMask)
 {
@@ -2679,79 +2758,165 @@ __global__ void __launch_bounds__(kFreeThreads, kGeneral ? 4 : FreeLayout<TW, TH
     for (int i = threadIdx.x; i < L::kPix; i += kFreeThreads)
     {
         const unsigned long long p = sBest[i];
-        if (p == ~0ull)
+        if (p != ~0ull)
         {
-            continue;
+            resolve_winner<P, Color, kGeneral>(f, p, keyMax, mask, x0 + i % TW, y0 + i / TW, kGeneral ? sB[i] : make_float4(0.f, 0.f, 0.f, 0.f));
         }
-        const int x = x0 + i % TW, y = y0 + i / TW;
-        const uint32_t key = keyMax ? ~(uint32_t)p : (uint32_t)p;
-        const size_t gi = (size_t)x + (size_t)f.width * y;
-        const uint64_t rec = key_to_record(f, key);
-        const float4* R = f.records + rec * kRecordVec4;
-        const DrawDesc& dd = f.draws[__float_as_uint(R[7].x)];
-        const uint32_t kind = __float_as_uint(R[7].w);
-        float4 b;
-        if (kGeneral)
+    }
+}
+
+/*-----------------------------------------------------------------------------
+ * Untiled order-free raster, for launches of triangles and points: the
+ * fragment set and the winner rule of raster_free_kernel without tile
+ * lists. Every record is walked once, row by row (the tile version stages a
+ * record once per tile it touches), and each fragment that passes against
+ * the pre-launch depth is folded into its pixel's best word in global memory
+ * (64-bit atomicMin, skipped when a plain read already shows a better word;
+ * the words stay in L2). resolve_global_kernel then shades each pixel's
+ * winner with resolve_winner. A warp takes 32 records at a time and deals
+ * their rows to the lanes 32 per step, so triangles of any height keep the
+ * lanes busy. The walk of a row runs the reference's four column chains
+ * from the span's start: the chain of x starts at the same xs and takes the
+ * same additions as in the tiled walk, so depths are identical.
+-----------------------------------------------------------------------------*/
+constexpr int kGlobalWarps = 4;
+
+struct GroupRecs
+{
+    uint32_t start[32];   /* first task (row) of each record of the group */
+    uint32_t rec[32];
+    uint32_t key[32];
+    int32_t  y0[32];      /* first row walked */
+};
+
+/* Folds a fragment of pixel gi into its best word when it passes against
+ * the pre-launch depth: the word only decreases, so a fragment not below a
+ * plain read of it can never win and issues no atomic. */
+__device__ __forceinline__ void global_fold(const Frame& f, size_t gi, float z, uint32_t key, int func, bool mask)
+{
+    if (!depth_cmp(func, z, depth_load(f, gi)))
+    {
+        return;
+    }
+    const unsigned long long p = free_pack(func, mask, z, key);
+    unsigned long long* w = f.bestWords + gi;
+    if (p < *reinterpret_cast<volatile unsigned long long*>(w))
+    {
+        atomicMin(w, p);
+    }
+}
+
+template <class P>
+__global__ void __launch_bounds__(kGlobalWarps * 32) raster_global_kernel(const Frame f, int depthFunc, int depthMask)
+{
+    __shared__ GroupRecs sG[kGlobalWarps];
+    if (f.status[0] & kStatusSticky)
+    {
+        return;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    GroupRecs& g = sG[warp];
+    const bool mask = depthMask != 0;
+    /* records: the slots' main records, then the clipped fans' (the count
+     * can pass the capacity only in a launch that overflowed, which the
+     * sticky status already stopped) */
+    const uint64_t nItems = f.numSlots + min(*f.ovfCount, f.ovfCap);
+    const uint64_t stride = (uint64_t)gridDim.x * kGlobalWarps * 32;
+    for (uint64_t g0 = ((uint64_t)blockIdx.x * kGlobalWarps + warp) * 32; g0 < nItems; g0 += stride)
+    {
+        const uint64_t i = g0 + lane;
+        uint32_t rows = 0, key = 0;
+        int ya = 0;
+        if (i < nItems && (i >= f.numSlots || f.slotInfo[i] == 1))
         {
-            b = sB[i];
+            key = (i < f.numSlots) ? (uint32_t)(i << kSubShift) : f.ovfKey[i - f.numSlots];
+            const float4 r6 = f.records[i * kRecordVec4 + 6];
+            ya = max(__float_as_int(r6.x), 0);
+            const int yb = min(__float_as_int(r6.y), f.height);
+            if (yb > ya && __float_as_int(r6.w) >= 0 && __float_as_int(r6.z) < f.width)
+            {
+                rows = (uint32_t)(yb - ya);
+            }
         }
-        else if (kind & kRecordPoint)
+        uint32_t incl = rows;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
         {
-            b = make_float4(0.f, 0.f, 0.f, R[0].z);
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += v;
         }
-        else
+        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        __syncwarp();
+        g.start[lane] = incl - rows;
+        g.rec[lane] = (uint32_t)min(i, (uint64_t)0xFFFFFFFFu);
+        g.key[lane] = key;
+        g.y0[lane] = ya;
+        __syncwarp();
+        for (uint32_t e = lane; e < total; e += 32)
         {
-            /* the winner's barycentrics and depth at this pixel, re-derived
-             * by the walk's own chain: the column class of x starts at the
-             * same xs and takes the same (x - xs) / 4 additions */
+            /* the record holding task e: the last one starting at or before
+             * e (records without rows share their start with the next) */
+            int lo = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+            {
+                if (lo + step < 32 && g.start[lo + step] <= e) lo += step;
+            }
+            const uint32_t k = g.key[lo];
+            const int y = g.y0[lo] + (int)(e - g.start[lo]);
+            const float4* R = f.records + (uint64_t)g.rec[lo] * kRecordVec4;
+            const size_t rowBase = (size_t)f.width * y;
+            if (__float_as_uint(R[7].w) & kRecordPoint)
+            {
+                const int px = __float_as_int(R[6].z);
+                if (px >= 0 && px < f.width) global_fold(f, rowBase + px, R[0].z, k, depthFunc, mask);
+                continue;
+            }
             const float yf = (float)y;
-            Chain ch;
-            (void)chain_begin_span(R, yf, scanline_span(R[0], R[1], yf), x, x + 1, ch);
-            b = make_float4(ch.b0, ch.b1, ch.b2, chain_depth(R, ch));
-        }
-        if ((f.color || f.generic0) && dd.numOutputs > 0)
-        {
-            float4 o;
-            bool kept;
-            if (kind & kRecordPoint)
+            const Span sp = scanline_span(R[0], R[1], yf);
+            if (!((uint32_t)sp.xMin < (uint32_t)sp.xMax))
             {
-                slg_frag_coord fc = point_coord(R);
-                kept = shade_point<P, kGeneral>(f, dd, rec, fc, o, gi);
+                continue;
             }
-            else if (kGeneral && (kind & kRecordLine))
+            const float4 r2 = R[2], r3 = R[3], r4 = R[4], r5 = R[5];
+            const float bcY0 = r3.x * yf + r4.x, bcY1 = r3.y * yf + r4.y, bcY2 = r3.z * yf + r4.z;
+            const float s0 = r2.x * 4.f, s1 = r2.y * 4.f, s2 = r2.z * 4.f;
+            const float zw = 0.f * r2.w;
+            const int xEnd = min(sp.xMax, f.width);
+            /* the four column chains from the span's start (chain_begin_span
+             * with no catch-up: each starts at its first pixel) */
+#pragma unroll 1
+            for (int xs = sp.xMin; xs < min(sp.xMin + 4, xEnd); ++xs)
             {
-                /* sB.y keeps the line step's 16-bit (X, Y): X = W on the row
-                 * above for the step stored at column 0 */
-                const uint32_t xy = __float_as_uint(b.y);
-                slg_frag_coord fc = frag_coord(xy & 0xFFFFu, xy >> 16, b.w);
-                kept = shade_line<P, kGeneral>(f, dd, rec, b.x, fc, o, gi);
-            }
-            else
-            {
-                slg_frag_coord fc = frag_coord((uint32_t)x, (uint32_t)y, b.w);
-                kept = shade<P, kGeneral>(f, dd, rec, kind, R[2].w, R[5], b.x, b.y, b.z, fc, o, gi);
-            }
-            if (kept && f.color)
-            {
-                Color::write(f.color, gi, Color::store(o));
-            }
-            if (!kept)
-            {
-                /* the winner is the last fragment that passes, in the
-                 * reference's order; when it is discarded the pixel keeps an
-                 * earlier fragment's colour, which only the ordered raster
-                 * knows: programs that discard are registered as such and
-                 * their launches never come here */
-                atomicOr(f.status, kStatusUndeclaredDiscard);
+                const float xsf = (float)xs;
+                float b0 = r2.x * xsf + bcY0, b1 = r2.y * xsf + bcY1, b2 = r2.z * xsf + bcY2;
+                for (int x = xs; x < xEnd; x += 4, b0 += s0, b1 += s1, b2 += s2)
+                {
+                    global_fold(f, rowBase + x, __fadd_rn((r3.w * b0 + r4.w * b1) + r5.x * b2, zw), k, depthFunc, mask);
+                }
             }
         }
-        if (mask)
+        __syncwarp();
+    }
+}
+
+template <class P, class Color>
+__global__ void __launch_bounds__(256) resolve_global_kernel(const Frame f, int depthFunc, int depthMask)
+{
+    if (f.status[0] & kStatusSticky)
+    {
+        return;
+    }
+    const bool mask = depthMask != 0;
+    const bool keyMax = free_key_max(depthFunc, mask);
+    const size_t n = (size_t)f.width * f.height;
+    for (size_t gi = (size_t)blockIdx.x * blockDim.x + threadIdx.x; gi < n; gi += (size_t)gridDim.x * blockDim.x)
+    {
+        const unsigned long long p = f.bestWords[gi];
+        if (p != ~0ull)
         {
-            depth_store(f, gi, b.w);
-        }
-        if (f.ids)
-        {
-            f.ids[gi] = (key >> kSubShift) + 1u;
+            resolve_winner<P, Color, false>(f, p, keyMax, mask, (int)(gi % (size_t)f.width), (int)(gi / (size_t)f.width),
+                                            make_float4(0.f, 0.f, 0.f, 0.f));
         }
     }
 }
@@ -3025,6 +3190,16 @@ template <class P, class Color>
 cudaError_t launch_raster_color(const Frame& f, cudaStream_t s)
 {
     const int numTiles = f.tilesX * f.tilesY;
+    if (f.bestWords)
+    {
+        /* untiled order-free raster: best words reset, records walked, winners shaded */
+        const size_t n = (size_t)f.width * f.height;
+        cudaMemsetAsync(f.bestWords, 0xFF, n * sizeof(unsigned long long), s);
+        raster_global_kernel<P><<<152 * 16, kGlobalWarps * 32, 0, s>>>(f, f.freeDepthFunc, f.freeDepthMask);
+        resolve_global_kernel<P, Color><<<(unsigned)std::min<size_t>((n + 255) / 256, 152 * 32), 256, 0, s>>>(f, f.freeDepthFunc,
+                                                                                                              f.freeDepthMask);
+        return cudaGetLastError();
+    }
     if (f.hasLines || f.hasWire || f.hasMrt)
     {
         /* the host sets kLineTile x kLineTile tiles for these launches */

@@ -16,7 +16,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 @pytest.mark.parametrize("name", sorted(G.SCENES))
-@pytest.mark.parametrize("mode,tile", [(0, (16, 16)), (1, (32, 32)), (0, (8, 8))])
+@pytest.mark.parametrize("mode,tile", [(0, (16, 16)), (1, (32, 32)), (3, (8, 8))])
 def test_gpu_matches_reference_golden(gpu_lib, name, mode, tile):
     builder, kw = G.SCENES[name]
     ctx = gpu_lib.Context()
@@ -60,7 +60,7 @@ def test_gpu_blits_match_reference_golden(gpu_lib):
         assert same, f"blit {name} differs from the reference"
 
 
-@pytest.mark.parametrize("mode,tile", [(0, (16, 16)), (1, (32, 32)), (0, (8, 8))])
+@pytest.mark.parametrize("mode,tile", [(0, (16, 16)), (1, (32, 32)), (3, (8, 8))])
 def test_gpu_scene_graph_matches_reference_golden(gpu_lib, mode, tile):
     """SL_SceneGraph::update and the mesh-node traversal on the GPU (update
     kernel, draw-list kernel, one batched launch per frame): model matrices,

@@ -29,9 +29,11 @@ def test_c1_sphere_exact(ctxs):
     assert (sg.read_depth() < 1.0).sum() > 50000
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3])
 def test_raster_modes_agree(ctxs, mode):
-    """Order-free resolve (mode 0) and the ordered replay (mode 1) both match."""
+    """The default plan (mode 0: order-free on tiles until the autotuner
+    picks otherwise), the ordered replay (1), the order-free resolve on
+    tiles (2) and untiled (3) all match."""
     g, o = ctxs
     g.set_raster_mode(mode)
     sg, so = render_both(S.build_c2, g, o, num_instances=24, width=320, height=200, tex_size=128)
@@ -42,10 +44,13 @@ def test_raster_modes_agree(ctxs, mode):
 
 @pytest.mark.parametrize("depth_test", [1, 2, 3, 4, 5, 0])
 @pytest.mark.parametrize("depth_mask", [0, 1])
-def test_order_free_depth_rules(ctxs, depth_test, depth_mask):
-    """Opaque draws take the order-free path; every depth rule it accepts must
-    reproduce the sequential result, ties included."""
+@pytest.mark.parametrize("mode", [2, 3])
+def test_order_free_depth_rules(ctxs, depth_test, depth_mask, mode):
+    """Opaque draws take the order-free path (on tiles in mode 2, untiled in
+    mode 3); every depth rule it accepts must reproduce the sequential
+    result, ties included."""
     g, o = ctxs
+    g.set_raster_mode(mode)
     sg, so = render_both(E.random_soup, g, o, depth_test=depth_test, depth_mask=depth_mask, clear_depth=0.5,
                          frames=2, num_tris=500)
     compare_scenes(sg, so, f"free depth {depth_test}/{depth_mask}")

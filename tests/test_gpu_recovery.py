@@ -37,8 +37,12 @@ CAPS = {
 
 @pytest.mark.parametrize("caps", sorted(CAPS))
 @pytest.mark.parametrize("blend", [A.BLEND_OFF, A.BLEND_ALPHA])
-def test_overflowed_launch_is_replayed(ctxs, caps, blend):
+@pytest.mark.parametrize("mode", [2, 3])
+def test_overflowed_launch_is_replayed(ctxs, caps, blend, mode):
+    """mode 2: opaque launches on tiles (tile entries can overflow); mode 3:
+    untiled (only the clipped-record region can)."""
     g, o = ctxs
+    g.set_raster_mode(mode)
     kw = dict(num_tris=3000, width=200, height=150, seed=111, blend=blend, cull=A.CULL_OFF)
     sg, so = E.random_soup(g, **kw), E.random_soup(o, **kw)
     sg.render()
@@ -106,8 +110,10 @@ def test_scene_graph_overflow_is_reported(gpu_lib, oracle_mod):
     """The scene graph's draw list is written on the device, so its launch
     is not replayed: the overflow is reported at finish with the buffers
     grown, and the next frame renders in full (the scene animates: frame 3
-    is compared with the oracle's frame 3)."""
+    is compared with the oracle's frame 3). Its opaque launches run on
+    tiles here (raster mode 2), so a small tile-entry cap overflows."""
     g = gpu_lib.Context()
+    g.set_raster_mode(2)
     o = oracle_mod.Context()
     s = S.build_scene_graph(g, width=160, height=120, groups=3, per_group=3)
     so = S.build_scene_graph(o, width=160, height=120, groups=3, per_group=3)
