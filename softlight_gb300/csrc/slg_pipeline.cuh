@@ -613,6 +613,13 @@ __device__ __forceinline__ uint32_t clip_pair(const Frame& f, bool active, const
     return fits ? 2u + survivors : 0u;
 }
 
+/* a / b in slot arithmetic: one 32-bit division when both fit (slots stay
+ * below 2^29), the 64-bit routine otherwise; the same quotient either way */
+__device__ __forceinline__ uint64_t udiv_slot(uint64_t a, uint64_t b)
+{
+    return ((a | b) >> 32) == 0 ? (uint64_t)((uint32_t)a / (uint32_t)b) : a / b;
+}
+
 __device__ __forceinline__ int find_draw(const Frame& f, uint64_t slot)
 {
     int lo = 0, hi = f.numDraws - 1;
@@ -649,7 +656,7 @@ template <class P>
 __device__ __forceinline__ uint32_t setup_point(const Frame& f, const DrawDesc& d, int di, uint64_t slot, uint64_t local,
                                                 TileRange& tr, bool& counted)
 {
-    const uint64_t inst = local / d.numTris;
+    const uint64_t inst = udiv_slot(local, d.numTris);
     const uint64_t e = d.elementBegin + (local - inst * d.numTris);
     const uint64_t vid = (d.indexType >= 0) ? read_index(d, e) : e;
     slg_v4 vary[kMaxVaryings];
@@ -774,7 +781,7 @@ template <class P>
 __device__ __forceinline__ uint32_t setup_line(const Frame& f, const DrawDesc& d, int di, uint64_t slot, uint64_t local,
                                                TileRange& tr, bool& counted)
 {
-    const uint64_t inst = local / d.numTris;
+    const uint64_t inst = udiv_slot(local, d.numTris);
     const uint64_t i = d.elementBegin + 2u * (local - inst * d.numTris);
     slg_v4 va[kMaxVaryings], vb[kMaxVaryings];
     const uint64_t vid0 = (d.indexType >= 0) ? read_index(d, i) : i;
@@ -1000,7 +1007,7 @@ __device__ __forceinline__ uint32_t setup_slot(const Frame& f, uint64_t slot, Ti
     {
         return setup_line<P>(f, d, di, slot, local, tr, counted);
     }
-    const uint64_t inst = local / d.numTris;
+    const uint64_t inst = udiv_slot(local, d.numTris);
     const uint64_t tri = local - inst * d.numTris;
     const uint64_t i = d.elementBegin + 3u * tri;
 
@@ -1118,7 +1125,7 @@ __global__ void __launch_bounds__(128) clip_kernel(const Frame f)
         const int di = (active && f.numDraws > 1) ? find_draw(f, slot) : 0;
         const DrawDesc& d = f.draws[di];
         const uint64_t local = slot - d.slotBase;
-        const uint64_t inst = active ? local / d.numTris : 0u;
+        const uint64_t inst = active ? udiv_slot(local, d.numTris) : 0u;
         const uint64_t tri = local - inst * d.numTris;
         const uint64_t i = d.elementBegin + 3u * tri;
         /* lanes 0..2 of the half: the triangle's vertices */
@@ -1172,7 +1179,7 @@ __global__ void __launch_bounds__(256) vertex_cache_kernel(const Frame f)
         return;
     }
     const uint64_t local = e - d.cacheBase;
-    const uint64_t inst = local / d.cacheVerts;
+    const uint64_t inst = udiv_slot(local, d.cacheVerts);
     const uint64_t vid = local - inst * d.cacheVerts;
     slg_v4 vary[kMaxVaryings];
     f.cachePos[e] = to_f4(P::vertex(d, f.tables, vid, inst, vary));
@@ -2909,15 +2916,19 @@ __global__ void __launch_bounds__(256) resolve_global_kernel(const Frame f, int 
     }
     const bool mask = depthMask != 0;
     const bool keyMax = free_key_max(depthFunc, mask);
-    const size_t n = (size_t)f.width * f.height;
-    for (size_t gi = (size_t)blockIdx.x * blockDim.x + threadIdx.x; gi < n; gi += (size_t)gridDim.x * blockDim.x)
+    /* one 16x16 block of pixels per CTA, so the pixels of a small triangle
+     * share its record, cache entries and texels in L1 */
+    const int gx = (f.width + 15) >> 4;
+    const int x = (int)(blockIdx.x % (unsigned)gx) * 16 + (int)(threadIdx.x & 15);
+    const int y = (int)(blockIdx.x / (unsigned)gx) * 16 + (int)(threadIdx.x >> 4);
+    if (x >= f.width || y >= f.height)
     {
-        const unsigned long long p = f.bestWords[gi];
-        if (p != ~0ull)
-        {
-            resolve_winner<P, Color, false>(f, p, keyMax, mask, (int)(gi % (size_t)f.width), (int)(gi / (size_t)f.width),
-                                            make_float4(0.f, 0.f, 0.f, 0.f));
-        }
+        return;
+    }
+    const unsigned long long p = f.bestWords[(size_t)x + (size_t)f.width * y];
+    if (p != ~0ull)
+    {
+        resolve_winner<P, Color, false>(f, p, keyMax, mask, x, y, make_float4(0.f, 0.f, 0.f, 0.f));
     }
 }
 
@@ -3196,8 +3207,8 @@ cudaError_t launch_raster_color(const Frame& f, cudaStream_t s)
         const size_t n = (size_t)f.width * f.height;
         cudaMemsetAsync(f.bestWords, 0xFF, n * sizeof(unsigned long long), s);
         raster_global_kernel<P><<<152 * 16, kGlobalWarps * 32, 0, s>>>(f, f.freeDepthFunc, f.freeDepthMask);
-        resolve_global_kernel<P, Color><<<(unsigned)std::min<size_t>((n + 255) / 256, 152 * 32), 256, 0, s>>>(f, f.freeDepthFunc,
-                                                                                                              f.freeDepthMask);
+        const unsigned blocks = (unsigned)(((f.width + 15) >> 4) * ((f.height + 15) >> 4));
+        resolve_global_kernel<P, Color><<<blocks, 256, 0, s>>>(f, f.freeDepthFunc, f.freeDepthMask);
         return cudaGetLastError();
     }
     if (f.hasLines || f.hasWire || f.hasMrt)
