@@ -2797,17 +2797,17 @@ struct GroupRecs
 };
 
 /* Folds a fragment of pixel gi into its best word when it passes against
- * the pre-launch depth: the word only decreases, so a fragment not below a
- * plain read of it can never win and issues no atomic. */
+ * the pre-launch depth. The word only decreases, so any earlier value of it
+ * is an upper bound: a fragment not below what a plain (L1-cached, possibly
+ * older) read returns can never win and issues no atomic. */
 __device__ __forceinline__ void global_fold(const Frame& f, size_t gi, float z, uint32_t key, int func, bool mask)
 {
-    if (!depth_cmp(func, z, depth_load(f, gi)))
-    {
-        return;
-    }
-    const unsigned long long p = free_pack(func, mask, z, key);
+    /* both reads issued together, then the tests */
     unsigned long long* w = f.bestWords + gi;
-    if (p < *reinterpret_cast<volatile unsigned long long*>(w))
+    const float d0 = depth_load(f, gi);
+    const unsigned long long cur = *w;
+    const unsigned long long p = free_pack(func, mask, z, key);
+    if (depth_cmp(func, z, d0) && p < cur)
     {
         atomicMin(w, p);
     }
