@@ -1191,7 +1191,7 @@ __global__ void __launch_bounds__(256) vertex_cache_kernel(const Frame f)
 }
 
 template <class P, bool kLines, bool kCached>
-__global__ void __launch_bounds__(256) vs_setup_kernel(const Frame f)
+__global__ void __launch_bounds__(256, kCached ? 6 : 1) vs_setup_kernel(const Frame f)
 {
     const uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     TileRange tr;
