@@ -400,19 +400,32 @@ def adjoint_timing(sg, torch, flush, steps, warmup):
             "tile": f"{tw}x{th}", "vertex_block": vb, "l2": "flushed before each timed frame"}
 
 
-def launches_per_frame(scene):
-    """Kernels one frame launches: two clears, then vs_setup, clip, tile_scan,
-    bin_fill and raster per launch, plus tile_sort on the ordered path and
-    the vertex cache for launches of 64K or more indexed triangles."""
+def launches_per_frame(scene, tile):
+    """Kernels one frame launches (counted from the launch sequence, matched
+    against the ncu launch lists in profiles/): two clears, then per draw
+    launch the vertex cache (indexed draws of 64K or more triangles),
+    vs_setup, clip and the launch mark, plus the path's tile-list and raster
+    kernels: untiled order-free raster + resolve + counter reset; tiled
+    order-free tile scan + fill + raster; blended with key-order lists (grids
+    of at most 4 096 tiles) bin numbering (3) + count + chunk scan + tile
+    scan + fill + raster, else tile scan + fill + tile sort + raster."""
     from softlight_gb300 import api as A
-    per_launch = 5 + (1 if scene.blending else 0)
-    indexed = any(m.mode == A.RENDER_MODE_INDEXED_TRIANGLES for (m, _, _) in scene.draws)
+    tw, th = tile
+    tiles = -(-scene.width // tw) * -(-scene.height // th)
+    # order-free untiled: raster + resolve + counter reset; on tiles: tile
+    # scan + fill + raster (three either way)
+    path = (8 if tiles <= 4096 else 4) if scene.blending else 3
+    per_launch = 3 + path
+
+    def cache(tris, indexed):
+        return 1 if indexed and tris >= 65536 else 0
     if scene.batched:
-        return 2 + per_launch + (1 if indexed and scene.num_triangles >= 65536 else 0)
+        indexed = any(m.mode == A.RENDER_MODE_INDEXED_TRIANGLES for (m, _, _) in scene.draws)
+        return 2 + per_launch + cache(scene.num_triangles, indexed)
     total = 2
     for (m, n, _) in scene.draws:
         tris = n * (m.elementEnd - m.elementBegin) // 3
-        total += per_launch + (1 if m.mode == A.RENDER_MODE_INDEXED_TRIANGLES and tris >= 65536 else 0)
+        total += per_launch + cache(tris, m.mode == A.RENDER_MODE_INDEXED_TRIANGLES)
     return total
 
 
@@ -483,7 +496,8 @@ def time_workload(name, args, sg, torch, flush, world, local, rank, clocks=None,
     out = {"workload": cfg["workload"], "config": cfg, "value": fps, "unit": "frames/s", "ms_per_step": total_ms / args.steps,
            "tile": f"{tw}x{th}", "vertex_block": vb, "batched_graph": bool(scene.batched),
            "order_free_raster": "untiled" if ctx.untiled_raster() else "tiles",
-           "triangles_per_frame": scene.num_triangles, "launches_per_frame": launches_per_frame(scene)}
+           "triangles_per_frame": scene.num_triangles,
+           "launches_per_frame": launches_per_frame(scene, (tw, th))}
 
     if scene.batched:
         # the same frames issued as one slg_draw call per mesh
