@@ -1190,23 +1190,6 @@ __global__ void __launch_bounds__(256) vertex_cache_kernel(const Frame f)
     }
 }
 
-template <class P, bool kLines, bool kCached>
-__global__ void __launch_bounds__(256, kCached ? 6 : 1) vs_setup_kernel(const Frame f)
-{
-    const uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    TileRange tr;
-    tr.tx0 = 0; tr.tx1 = -1; tr.ty0 = 0; tr.ty1 = -1;
-    bool counted = false;
-    if (slot < f.numSlots)
-    {
-        f.slotInfo[slot] = setup_slot<P, kLines, kCached>(f, slot, tr, counted);
-    }
-    /* per-tile counts of the unclipped records, one atomic per group of
-     * lanes touching the same tile (clipped records count themselves);
-     * launches filling their lists in key order count per chunk instead,
-     * untiled launches not at all */
-    warp_tile_walk(f, tr, counted && f.chunkCounts == nullptr && f.bestWords == nullptr, f.tileCount, [](uint32_t, uint32_t) {});
-}
 
 /*-----------------------------------------------------------------------------
  * Kernel 4: tile raster + shade
@@ -2813,6 +2796,87 @@ __device__ __forceinline__ void global_fold(const Frame& f, size_t gi, float z, 
     }
 }
 
+/* Walks 32 records, one named per lane (have: the lane holds one; rec: its
+ * index; key: its ordering key), row by row into the best words: the group's
+ * rows are dealt to the lanes 32 per step. Every lane of the warp calls it. */
+__device__ __forceinline__ void walk_group(const Frame& f, bool have, uint64_t rec, uint32_t key, int depthFunc, bool mask, GroupRecs& g)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t rows = 0;
+    int ya = 0;
+    if (have)
+    {
+        const float4 r6 = f.records[rec * kRecordVec4 + 6];
+        ya = max(__float_as_int(r6.x), 0);
+        const int yb = min(__float_as_int(r6.y), f.height);
+        if (yb > ya && __float_as_int(r6.w) >= 0 && __float_as_int(r6.z) < f.width)
+        {
+            rows = (uint32_t)(yb - ya);
+        }
+    }
+    uint32_t incl = rows;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    __syncwarp();
+    g.start[lane] = incl - rows;
+    g.rec[lane] = (uint32_t)min(rec, (uint64_t)0xFFFFFFFFu);
+    g.key[lane] = key;
+    g.y0[lane] = ya;
+    __syncwarp();
+    for (uint32_t e = lane; e < total; e += 32)
+    {
+        /* the record holding task e: the last one starting at or before
+         * e (records without rows share their start with the next) */
+        int lo = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+        {
+            if (lo + step < 32 && g.start[lo + step] <= e) lo += step;
+        }
+        const uint32_t k = g.key[lo];
+        const int y = g.y0[lo] + (int)(e - g.start[lo]);
+        const float4* R = f.records + (uint64_t)g.rec[lo] * kRecordVec4;
+        const size_t rowBase = (size_t)f.width * y;
+        if (__float_as_uint(R[7].w) & kRecordPoint)
+        {
+            const int px = __float_as_int(R[6].z);
+            if (px >= 0 && px < f.width) global_fold(f, rowBase + px, R[0].z, k, depthFunc, mask);
+            continue;
+        }
+        const float yf = (float)y;
+        const Span sp = scanline_span(R[0], R[1], yf);
+        if (!((uint32_t)sp.xMin < (uint32_t)sp.xMax))
+        {
+            continue;
+        }
+        const float4 r2 = R[2], r3 = R[3], r4 = R[4], r5 = R[5];
+        const float bcY0 = r3.x * yf + r4.x, bcY1 = r3.y * yf + r4.y, bcY2 = r3.z * yf + r4.z;
+        const float s0 = r2.x * 4.f, s1 = r2.y * 4.f, s2 = r2.z * 4.f;
+        const float zw = 0.f * r2.w;
+        const int xEnd = min(sp.xMax, f.width);
+        /* the four column chains from the span's start (chain_begin_span
+         * with no catch-up: each starts at its first pixel) */
+#pragma unroll 1
+        for (int xs = sp.xMin; xs < min(sp.xMin + 4, xEnd); ++xs)
+        {
+            const float xsf = (float)xs;
+            float b0 = r2.x * xsf + bcY0, b1 = r2.y * xsf + bcY1, b2 = r2.z * xsf + bcY2;
+            for (int x = xs; x < xEnd; x += 4, b0 += s0, b1 += s1, b2 += s2)
+            {
+                global_fold(f, rowBase + x, __fadd_rn((r3.w * b0 + r4.w * b1) + r5.x * b2, zw), k, depthFunc, mask);
+            }
+        }
+    }
+    __syncwarp();
+}
+
+/* The clipped fans' records (vs_setup_kernel walks the slots' own records
+ * as it stores them): records [numSlots, numSlots + ovfCount). */
 template <class P>
 __global__ void __launch_bounds__(kGlobalWarps * 32) raster_global_kernel(const Frame f, int depthFunc, int depthMask)
 {
@@ -2822,88 +2886,41 @@ __global__ void __launch_bounds__(kGlobalWarps * 32) raster_global_kernel(const 
         return;
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    GroupRecs& g = sG[warp];
-    const bool mask = depthMask != 0;
-    /* records: the slots' main records, then the clipped fans' (the count
-     * can pass the capacity only in a launch that overflowed, which the
-     * sticky status already stopped) */
-    const uint64_t nItems = f.numSlots + min(*f.ovfCount, f.ovfCap);
+    /* the count can pass the capacity only in a launch that overflowed,
+     * which the sticky status already stopped */
+    const uint64_t nOvf = min(*f.ovfCount, f.ovfCap);
     const uint64_t stride = (uint64_t)gridDim.x * kGlobalWarps * 32;
-    for (uint64_t g0 = ((uint64_t)blockIdx.x * kGlobalWarps + warp) * 32; g0 < nItems; g0 += stride)
+    for (uint64_t g0 = ((uint64_t)blockIdx.x * kGlobalWarps + warp) * 32; g0 < nOvf; g0 += stride)
     {
-        const uint64_t i = g0 + lane;
-        uint32_t rows = 0, key = 0;
-        int ya = 0;
-        if (i < nItems && (i >= f.numSlots || f.slotInfo[i] == 1))
-        {
-            key = (i < f.numSlots) ? (uint32_t)(i << kSubShift) : f.ovfKey[i - f.numSlots];
-            const float4 r6 = f.records[i * kRecordVec4 + 6];
-            ya = max(__float_as_int(r6.x), 0);
-            const int yb = min(__float_as_int(r6.y), f.height);
-            if (yb > ya && __float_as_int(r6.w) >= 0 && __float_as_int(r6.z) < f.width)
-            {
-                rows = (uint32_t)(yb - ya);
-            }
-        }
-        uint32_t incl = rows;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        __syncwarp();
-        g.start[lane] = incl - rows;
-        g.rec[lane] = (uint32_t)min(i, (uint64_t)0xFFFFFFFFu);
-        g.key[lane] = key;
-        g.y0[lane] = ya;
-        __syncwarp();
-        for (uint32_t e = lane; e < total; e += 32)
-        {
-            /* the record holding task e: the last one starting at or before
-             * e (records without rows share their start with the next) */
-            int lo = 0;
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1)
-            {
-                if (lo + step < 32 && g.start[lo + step] <= e) lo += step;
-            }
-            const uint32_t k = g.key[lo];
-            const int y = g.y0[lo] + (int)(e - g.start[lo]);
-            const float4* R = f.records + (uint64_t)g.rec[lo] * kRecordVec4;
-            const size_t rowBase = (size_t)f.width * y;
-            if (__float_as_uint(R[7].w) & kRecordPoint)
-            {
-                const int px = __float_as_int(R[6].z);
-                if (px >= 0 && px < f.width) global_fold(f, rowBase + px, R[0].z, k, depthFunc, mask);
-                continue;
-            }
-            const float yf = (float)y;
-            const Span sp = scanline_span(R[0], R[1], yf);
-            if (!((uint32_t)sp.xMin < (uint32_t)sp.xMax))
-            {
-                continue;
-            }
-            const float4 r2 = R[2], r3 = R[3], r4 = R[4], r5 = R[5];
-            const float bcY0 = r3.x * yf + r4.x, bcY1 = r3.y * yf + r4.y, bcY2 = r3.z * yf + r4.z;
-            const float s0 = r2.x * 4.f, s1 = r2.y * 4.f, s2 = r2.z * 4.f;
-            const float zw = 0.f * r2.w;
-            const int xEnd = min(sp.xMax, f.width);
-            /* the four column chains from the span's start (chain_begin_span
-             * with no catch-up: each starts at its first pixel) */
-#pragma unroll 1
-            for (int xs = sp.xMin; xs < min(sp.xMin + 4, xEnd); ++xs)
-            {
-                const float xsf = (float)xs;
-                float b0 = r2.x * xsf + bcY0, b1 = r2.y * xsf + bcY1, b2 = r2.z * xsf + bcY2;
-                for (int x = xs; x < xEnd; x += 4, b0 += s0, b1 += s1, b2 += s2)
-                {
-                    global_fold(f, rowBase + x, __fadd_rn((r3.w * b0 + r4.w * b1) + r5.x * b2, zw), k, depthFunc, mask);
-                }
-            }
-        }
-        __syncwarp();
+        const uint64_t j = g0 + lane;
+        const bool have = j < nOvf;
+        walk_group(f, have, f.numSlots + j, have ? f.ovfKey[j] : 0u, depthFunc, depthMask != 0, sG[warp]);
+    }
+}
+
+template <class P, bool kLines, bool kCached>
+__global__ void __launch_bounds__(256, kCached ? 6 : 1) vs_setup_kernel(const Frame f)
+{
+    const uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    TileRange tr;
+    tr.tx0 = 0; tr.tx1 = -1; tr.ty0 = 0; tr.ty1 = -1;
+    bool counted = false;
+    if (slot < f.numSlots)
+    {
+        f.slotInfo[slot] = setup_slot<P, kLines, kCached>(f, slot, tr, counted);
+    }
+    /* per-tile counts of the unclipped records, one atomic per group of
+     * lanes touching the same tile (clipped records count themselves);
+     * launches filling their lists in key order count per chunk instead,
+     * untiled launches not at all */
+    warp_tile_walk(f, tr, counted && f.chunkCounts == nullptr && f.bestWords == nullptr, f.tileCount, [](uint32_t, uint32_t) {});
+    if (f.bestWords)
+    {
+        /* untiled launch: the warp walks the records its lanes just stored
+         * (raster_global_kernel walks the clipped fans later) */
+        __shared__ GroupRecs sG[8];
+        const bool have = slot < f.numSlots && f.slotInfo[slot] == 1;
+        walk_group(f, have, slot, (uint32_t)(slot << kSubShift), f.freeDepthFunc, f.freeDepthMask != 0, sG[threadIdx.x >> 5]);
     }
 }
 
@@ -3149,6 +3166,11 @@ cudaError_t launch_vertex_stage(const Frame& f, cudaStream_t s)
     {
         vertex_cache_kernel<P><<<(unsigned)((f.cacheEntries + 255) / 256), 256, 0, s>>>(f);
     }
+    if (f.bestWords)
+    {
+        /* the untiled raster's best words, reset before vs_setup_kernel walks into them */
+        cudaMemsetAsync(f.bestWords, 0xFF, (size_t)f.width * f.height * sizeof(unsigned long long), s);
+    }
     if (f.numSlots > 0)
     {
         const unsigned blocks = (unsigned)((f.numSlots + vsBlock - 1) / vsBlock);
@@ -3203,9 +3225,8 @@ cudaError_t launch_raster_color(const Frame& f, cudaStream_t s)
     const int numTiles = f.tilesX * f.tilesY;
     if (f.bestWords)
     {
-        /* untiled order-free raster: best words reset, records walked, winners shaded */
-        const size_t n = (size_t)f.width * f.height;
-        cudaMemsetAsync(f.bestWords, 0xFF, n * sizeof(unsigned long long), s);
+        /* untiled order-free raster: the clipped fans walked (vs_setup_kernel
+         * walked the rest), winners shaded */
         raster_global_kernel<P><<<152 * 16, kGlobalWarps * 32, 0, s>>>(f, f.freeDepthFunc, f.freeDepthMask);
         const unsigned blocks = (unsigned)(((f.width + 15) >> 4) * ((f.height + 15) >> 4));
         resolve_global_kernel<P, Color><<<blocks, 256, 0, s>>>(f, f.freeDepthFunc, f.freeDepthMask);
