@@ -150,14 +150,22 @@ def test_multi_draw(ctxs, batched):
     compare_scenes(sg, so, f"multi batched={batched}")
 
 
-def test_batched_equals_per_draw(gpu_lib):
+@pytest.mark.parametrize("mode", [0, 3])
+@pytest.mark.parametrize("graphs", [False, True])
+def test_batched_equals_per_draw(gpu_lib, mode, graphs):
+    """One batched launch (replayed from a CUDA graph when enabled) gives the
+    frames of one launch per draw, on tiles (mode 0) and untiled (mode 3)."""
     a, b = gpu_lib.Context(), gpu_lib.Context()
+    a.set_raster_mode(mode)
+    b.set_raster_mode(mode)
+    a.set_batch_graphs(graphs)
     sa = S.build_c4(a, num_draws=20, width=320, height=200, tex_size=32, batched=True)
     sb = S.build_c4(b, num_draws=20, width=320, height=200, tex_size=32, batched=False)
-    sa.render()
-    sb.render()
-    assert np.array_equal(sa.read_color(), sb.read_color())
-    assert np.array_equal(sa.read_depth().view(np.uint32), sb.read_depth().view(np.uint32))
+    for _ in range(2):
+        sa.render()
+        sb.render()
+        assert np.array_equal(sa.read_color(), sb.read_color())
+        assert np.array_equal(sa.read_depth().view(np.uint32), sb.read_depth().view(np.uint32))
 
 
 def test_flat_triangle_draw_test_scene(ctxs):
