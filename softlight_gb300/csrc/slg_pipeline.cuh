@@ -17,23 +17,28 @@
  * kernels for its built-in programs (slg_builtin.cuh); a caller instantiates
  * them for its own programs through include/slg_shader.cuh and registers the
  * result with slg_register_programs. The kernels that do not run programs
- * (tile scan, tile lists, tile sort, clears, blits) live in slg_kernels.cu.
+ * (tile scan, tile lists, key-order fill, tile sort, clears, blits) live in
+ * slg_kernels.cu.
  *
  * Pipeline of one launch (one draw, one instanced draw or a batch of draws):
+ *   0. vertex cache : the vertex program once per (draw, instance, vertex)
+ *                  of indexed draws that share vertices.
  *   1. vs_setup  : one thread per triangle slot (draw, instance, element
- *                  triple): three vertex-program calls, back-face cull,
- *                  clip-space classification, perspective divide, viewport
- *                  mapping, the sub-pixel reject and barycentric set-up of
- *                  SL_TriProcessor (softlight/src/SL_TriProcessor.cpp:248-640);
- *                  writes one 128-byte raster record (+ varyings) per
- *                  surviving triangle and counts, per screen tile, the
- *                  records whose bounding box touches it; partially visible
- *                  triangles are queued for clip_kernel
- *                  (Sutherland-Hodgman, SL_TriProcessor.cpp:370-519).
- *   2. tile_scan : exclusive scan of the per-tile counts (library).
- *   3. bin_fill  : writes every record's ordering key into each tile list
- *                  (library).
- *   4. raster    : one CTA per tile. The order-free raster (no blending, one
+ *                  triple): three positions (cache or vertex program),
+ *                  back-face cull, clip-space classification, perspective
+ *                  divide, viewport mapping, the sub-pixel reject and
+ *                  barycentric set-up of SL_TriProcessor
+ *                  (softlight/src/SL_TriProcessor.cpp:248-640); writes one
+ *                  128-byte raster record (+ varyings) per surviving
+ *                  triangle and counts, per screen tile, the records whose
+ *                  bounding box touches it; partially visible triangles are
+ *                  queued for clip_kernel (Sutherland-Hodgman,
+ *                  SL_TriProcessor.cpp:370-519). In an untiled launch each
+ *                  warp then walks the records it stored (step 4).
+ *   2. tile lists: scan of the per-tile counts and the fill of every
+ *                  record's key into each tile list it touches (library),
+ *                  in key order for blended launches.
+ *   3. raster    : one CTA per tile. The order-free raster (no blending, one
  *                  order-independent depth rule) folds fragments into a
  *                  per-pixel best word and shades each pixel once; the
  *                  ordered raster replays, per pixel and in submission order,
@@ -42,6 +47,9 @@
  *                  program, blend and depth write
  *                  (softlight/src/SL_TriRasterizer.cpp:807-923,
  *                  softlight/src/SL_FragmentProcessor.cpp:417-531).
+ *   4. untiled   : the order-free rule without tiles (steps 2-3 skipped):
+ *                  records walked once into per-pixel best words in global
+ *                  memory, then a pixel-parallel resolve.
  *
  * Ordering. SoftLight with one thread rasterises triangles in the order
  * push_bin emits them. Every record gets the key slot << 3 | sub, where the
