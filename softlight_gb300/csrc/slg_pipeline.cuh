@@ -1859,12 +1859,13 @@ struct RasterLayout
     static constexpr int kPix = TH * kStride;
     static constexpr size_t kRecBytes = sizeof(float4) * kBatch * kStagedVec4;
     /* ordered path: colour + depth tile, two record buffers (one batch is
-     * walked while the next arrives), their keys, then each tile row's
-     * depth range (lo, hi) at the start of a batch */
+     * walked while the next arrives), their keys, then each tile row's and
+     * each 8-row band's depth range (lo, hi) at the start of a batch */
     static constexpr size_t kRecOff = sizeof(typename Color::stored) * kPix + sizeof(float) * kPix;
     static constexpr size_t kKeyOff = kRecOff + 2 * kRecBytes;
     static constexpr size_t kRowDOff = kKeyOff + 2 * sizeof(uint32_t) * kBatch;
-    static constexpr size_t ordered_bytes() { return kRowDOff + 2 * sizeof(float) * TH; }
+    static constexpr size_t kBandDOff = kRowDOff + 2 * sizeof(float) * TH;
+    static constexpr size_t ordered_bytes() { return kBandDOff + 2 * sizeof(float) * (TH / 8); }
 };
 
 /* Starts copying records [b0, b0+cnt) of the tile list into shared memory
@@ -2013,6 +2014,39 @@ __device__ __forceinline__ bool depth_range_rejects(int func, float lo, float hi
     }
 }
 
+/* Whether no pixel of the tile (rows [y0, yEnd), columns [x0, xLimit)) can
+ * take a fragment of the staged triangle record R: depth_range_rect over the
+ * record's box in the tile against the depth range of the 8-row bands the
+ * box spans (bandD: (lo, hi) per band). A record whose box misses the tile's
+ * columns has no pixel there either. Line, wireframe and point records, and
+ * boxes reaching kRectBoundMaxX, are never rejected. */
+__device__ __forceinline__ bool tile_rejects(const float4* R, const float4 r6, int y0, int yEnd, int x0, int xLimit, const float* bandD)
+{
+    const uint32_t flags = __float_as_uint(R[7].w);
+    const int minX = __float_as_int(r6.z), maxX = __float_as_int(r6.w);
+    if ((flags & (kRecordLine | kRecordWire | kRecordPoint)) || maxX >= kRectBoundMaxX || maxX < minX)
+    {
+        return false;
+    }
+    const int ya = max(__float_as_int(r6.x), y0);
+    const int yb = min(__float_as_int(r6.y), yEnd) - 1;
+    const int xsMin = max(minX - 2, 0);
+    const int xa = max(x0, xsMin), xb = min(xLimit - 1, maxX);
+    if (yb < ya || xb < xa)
+    {
+        return true;
+    }
+    float lo = __int_as_float(0x7F800000), hi = __int_as_float(0xFF800000);
+    for (int b = (ya - y0) >> 3; b <= (yb - y0) >> 3; ++b)
+    {
+        lo = fminf(lo, bandD[2 * b]);
+        hi = fmaxf(hi, bandD[2 * b + 1]);
+    }
+    float zlo, zhi;
+    depth_range_rect(R, ya, yb, xa, xb, xsMin, zlo, zhi);
+    return depth_range_rejects(flags & 0xF, zlo, zhi, lo, hi);
+}
+
 /* kGeneral: the instantiation that carries line and wireframe records and
  * writes several render targets (such launches use kLineTile tiles); the
  * others keep the triangle loop's registers. */
@@ -2027,6 +2061,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
     float4*   sRecBuf = reinterpret_cast<float4*>(smem + L::kRecOff);
     uint32_t* sKeyBuf = reinterpret_cast<uint32_t*>(smem + L::kKeyOff);
     float*    sRowD  = reinterpret_cast<float*>(smem + L::kRowDOff);
+    float*    sBandD = reinterpret_cast<float*>(smem + L::kBandDOff);
 
     const int tile = blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
@@ -2110,8 +2145,42 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 sRowD[2 * r] = rowLo;
                 sRowD[2 * r + 1] = rowHi;
             }
+            if (!kGeneral)
+            {
+                /* and the warp's band of 8 rows */
+#pragma unroll
+                for (int o = 4; o < 32; o <<= 1)
+                {
+                    rowLo = fminf(rowLo, __shfl_xor_sync(0xFFFFFFFFu, rowLo, o));
+                    rowHi = fmaxf(rowHi, __shfl_xor_sync(0xFFFFFFFFu, rowHi, o));
+                }
+                if ((threadIdx.x & 31) == 0)
+                {
+                    sBandD[2 * (threadIdx.x >> 5)] = rowLo;
+                    sBandD[2 * (threadIdx.x >> 5) + 1] = rowHi;
+                }
+            }
         }
         __syncthreads();
+
+        if (!kGeneral && f.depthBound)
+        {
+            /* a triangle record none of whose pixels in the tile can pass is
+             * dropped for every band at once (one thread per record, the
+             * same bound over its rows and columns in the tile against the
+             * range of the bands it spans): its staged row range is emptied.
+             * Launches with line, wireframe or several-target records keep
+             * the per-band test only. */
+            for (int ri = threadIdx.x; ri < cnt; ri += blockDim.x)
+            {
+                float4* R = sRec + ri * kStagedVec4;
+                if (tile_rejects(R, R[6], y0, min(y0 + TH, f.height), x0, xLimit, sBandD))
+                {
+                    R[6].y = __uint_as_float(0x80000000u);   /* INT32_MIN: below every band */
+                }
+            }
+            __syncthreads();
+        }
 
         /* a triangle record none of whose pixels in the band can pass the
          * depth test is dropped for the whole warp (depth_range_rect over
