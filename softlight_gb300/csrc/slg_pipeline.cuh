@@ -1865,7 +1865,10 @@ struct RasterLayout
     static constexpr size_t kKeyOff = kRecOff + 2 * kRecBytes;
     static constexpr size_t kRowDOff = kKeyOff + 2 * sizeof(uint32_t) * kBatch;
     static constexpr size_t kBandDOff = kRowDOff + 2 * sizeof(float) * TH;
-    static constexpr size_t ordered_bytes() { return kBandDOff + 2 * sizeof(float) * (TH / 8); }
+    /* the survivor count of each warp while a batch is gathered, and where
+     * the next gathering resumes */
+    static constexpr size_t kScanOff = kBandDOff + 2 * sizeof(float) * (TH / 8);
+    static constexpr size_t ordered_bytes() { return kScanOff + sizeof(uint32_t) * (TH / 8 + 1); }
 };
 
 /* Starts copying records [b0, b0+cnt) of the tile list into shared memory
@@ -2051,7 +2054,7 @@ __device__ __forceinline__ bool tile_rejects(const float4* R, const float4 r6, i
  * writes several render targets (such launches use kLineTile tiles); the
  * others keep the triangle loop's registers. */
 template <class P, int TW, int TH, class Color, bool kGeneral>
-__global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
+__global__ void __launch_bounds__(TH * 4, kGeneral ? 512 / (TH * 4) : 896 / (TH * 4)) raster_ordered_kernel(const Frame f)
 {
     typedef RasterLayout<TW, TH, Color> L;
     typedef typename Color::stored Stored;
@@ -2062,6 +2065,7 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
     uint32_t* sKeyBuf = reinterpret_cast<uint32_t*>(smem + L::kKeyOff);
     float*    sRowD  = reinterpret_cast<float*>(smem + L::kRowDOff);
     float*    sBandD = reinterpret_cast<float*>(smem + L::kBandDOff);
+    uint32_t* sScan  = reinterpret_cast<uint32_t*>(smem + L::kScanOff);
 
     const int tile = blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
@@ -2098,28 +2102,12 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
     const float yf = (float)y;
     const int bandY0 = y0 + ((threadIdx.x >> 5) << 3);
 
-    /* batch k is walked from buffer k & 1 while batch k + 1 is copied into
-     * the other (its last readers finished at the barrier ending batch k - 1) */
-    stage_records_async(f, sKeys, (int)min((uint32_t)L::kBatch, n), sRecBuf, sKeyBuf);
-    for (uint32_t b0 = 0, k = 0; b0 < n; b0 += L::kBatch, ++k)
-    {
-        const int cnt = (int)min((uint32_t)L::kBatch, n - b0);
-        float4* sRec = sRecBuf + (k & 1) * (L::kBatch * kStagedVec4);
-        uint32_t* sRecKey = sKeyBuf + (k & 1) * L::kBatch;
-        if (b0 + L::kBatch < n)
-        {
-            stage_records_async(f, sKeys + b0 + L::kBatch, (int)min((uint32_t)L::kBatch, n - b0 - L::kBatch),
-                                sRecBuf + ((k + 1) & 1) * (L::kBatch * kStagedVec4), sKeyBuf + ((k + 1) & 1) * L::kBatch);
-            cp_async_wait<1>();
-        }
-        else
-        {
-            cp_async_wait<0>();
-        }
-        /* the depth range of this thread's pixels at the start of the batch:
-         * a bound for the whole batch, since depth only moves one way
-         * (Frame::depthBound) */
-        float dMin = 0.f, dMax = 0.f;
+    /* the depth range of this thread's pixels at the start of a batch: a
+     * bound for the whole batch, since depth only moves one way
+     * (Frame::depthBound); each tile row's range for the warp-wide record
+     * test and each 8-row band's for the tile-wide one */
+    float dMin = 0.f, dMax = 0.f;
+    const auto batch_ranges = [&]() {
         if (f.depthBound && rowActive)
         {
             dMin = __int_as_float(0x7F800000);
@@ -2133,7 +2121,6 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
         }
         if (f.depthBound)
         {
-            /* each tile row's range, for the warp-wide record test */
             float rowLo = rowActive ? dMin : __int_as_float(0x7F800000);
             float rowHi = rowActive ? dMax : __int_as_float(0xFF800000);
             rowLo = fminf(rowLo, __shfl_xor_sync(0xFFFFFFFFu, rowLo, 1));
@@ -2147,7 +2134,6 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
             }
             if (!kGeneral)
             {
-                /* and the warp's band of 8 rows */
 #pragma unroll
                 for (int o = 4; o < 32; o <<= 1)
                 {
@@ -2161,25 +2147,123 @@ __global__ void __launch_bounds__(TH * 4) raster_ordered_kernel(const Frame f)
                 }
             }
         }
-        __syncthreads();
+    };
 
-        if (!kGeneral && f.depthBound)
+    /* Triangle launches under a depth bound gather each batch: the threads
+     * test list entries [cursor, cursor + blockDim) straight from the
+     * records (one each, tile_rejects against the bands' ranges at the
+     * start of the batch), and only the records that can pass somewhere in
+     * the tile are copied into the staging buffers, in list order, up to
+     * kGather of them; the rest of the list is resumed at the first record
+     * that did not fit. Most records of a deep scene end there, so the
+     * batches, their barriers and their depth ranges are few. */
+    constexpr int kGather = 2 * L::kBatch;
+    const int nWarps = (int)(blockDim.x >> 5);
+    const int yEnd = min(y0 + TH, f.height);
+    const auto gather = [&](uint32_t& cursor) -> int {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        int cnt = 0;
+        while (cnt < kGather && cursor < n)
         {
-            /* a triangle record none of whose pixels in the tile can pass is
-             * dropped for every band at once (one thread per record, the
-             * same bound over its rows and columns in the tile against the
-             * range of the bands it spans): its staged row range is emptied.
-             * Launches with line, wireframe or several-target records keep
-             * the per-band test only. */
-            for (int ri = threadIdx.x; ri < cnt; ri += blockDim.x)
+            const uint32_t i = cursor + threadIdx.x;
+            bool take = false;
+            uint32_t key = 0;
+            const float4* Rg = f.records;
+            float4 Rl[8];
+            if (i < n)
             {
-                float4* R = sRec + ri * kStagedVec4;
-                if (tile_rejects(R, R[6], y0, min(y0 + TH, f.height), x0, xLimit, sBandD))
+                key = sKeys[i];
+                Rg = f.records + key_to_record(f, key) * kRecordVec4;
+#pragma unroll
+                for (int j = 2; j < 8; ++j)
                 {
-                    R[6].y = __uint_as_float(0x80000000u);   /* INT32_MIN: below every band */
+                    Rl[j] = Rg[j];
                 }
+                take = !tile_rejects(Rl, Rl[6], y0, yEnd, x0, xLimit, sBandD);
+            }
+            const unsigned m = __ballot_sync(0xFFFFFFFFu, take);
+            if (lane == 0)
+            {
+                sScan[warp] = (uint32_t)__popc(m);
             }
             __syncthreads();
+            int before = 0, total = 0;
+            for (int w = 0; w < nWarps; ++w)
+            {
+                const int cw = (int)sScan[w];
+                before += (w < warp) ? cw : 0;
+                total += cw;
+            }
+            const int slot = cnt + before + __popc(m & ((1u << lane) - 1u));
+            if (take && slot < kGather)
+            {
+                /* read again (L1) rather than held across the barrier */
+                float4* dst = sRecBuf + slot * kStagedVec4;
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                {
+                    dst[j] = Rg[j];
+                }
+                sKeyBuf[slot] = key;
+            }
+            if (take && slot == kGather)
+            {
+                sScan[nWarps] = i;
+            }
+            __syncthreads();
+            if (cnt + total > kGather)
+            {
+                cursor = sScan[nWarps];
+                cnt = kGather;
+            }
+            else
+            {
+                cursor += blockDim.x;
+                cnt += total;
+            }
+        }
+        return cnt;
+    };
+    const bool gathered = !kGeneral && f.depthBound;
+
+    /* Otherwise batch k is walked from buffer k & 1 while batch k + 1 is
+     * copied into the other (its last readers finished at the barrier
+     * ending batch k - 1). */
+    if (!gathered)
+    {
+        stage_records_async(f, sKeys, (int)min((uint32_t)L::kBatch, n), sRecBuf, sKeyBuf);
+    }
+    for (uint32_t b0 = 0, k = 0; b0 < n; ++k)
+    {
+        int cnt;
+        float4* sRec;
+        uint32_t* sRecKey;
+        if (gathered)
+        {
+            batch_ranges();
+            __syncthreads();
+            cnt = gather(b0);
+            sRec = sRecBuf;
+            sRecKey = sKeyBuf;
+        }
+        else
+        {
+            cnt = (int)min((uint32_t)L::kBatch, n - b0);
+            sRec = sRecBuf + (k & 1) * (L::kBatch * kStagedVec4);
+            sRecKey = sKeyBuf + (k & 1) * L::kBatch;
+            if (b0 + L::kBatch < n)
+            {
+                stage_records_async(f, sKeys + b0 + L::kBatch, (int)min((uint32_t)L::kBatch, n - b0 - L::kBatch),
+                                    sRecBuf + ((k + 1) & 1) * (L::kBatch * kStagedVec4), sKeyBuf + ((k + 1) & 1) * L::kBatch);
+                cp_async_wait<1>();
+            }
+            else
+            {
+                cp_async_wait<0>();
+            }
+            batch_ranges();
+            __syncthreads();
+            b0 += L::kBatch;
         }
 
         /* a triangle record none of whose pixels in the band can pass the
