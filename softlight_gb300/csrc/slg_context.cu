@@ -277,6 +277,7 @@ struct slg_context
     DevBuffer rankOf, recOfRank, seqRec, seqKey, binBlocks;   /* blend order of a multi-mesh draw */
     uint64_t rankCap = 0;
     DevBuffer chunkCounts, itemKey;    /* tile lists in key order (Frame::chunkCounts) */
+    DevBuffer tileOrder;               /* Frame::tileOrder */
     DevBuffer bestWords, ovfKey;       /* untiled order-free raster (Frame::bestWords) */
     bool forceTiled = false;           /* slg_set_raster_mode 2: order-free launches on tiles */
     bool forceUntiled = false;         /* slg_set_raster_mode 3: untiled where eligible */
@@ -1196,11 +1197,13 @@ int run_launch(slg_context* ctx, const std::vector<DrawRequest>& reqs, size_t fb
             if (!f.rankOf && (r = dev_alloc(ctx, ctx->itemKey, recs * sizeof(uint32_t), false))) return r;
             if ((r = dev_alloc(ctx, ctx->binBlocks, (blocks + 1) * sizeof(uint32_t), false))) return r;
             if ((r = dev_alloc(ctx, ctx->chunkCounts, numTiles * chunks * sizeof(uint32_t), false))) return r;
+            if ((r = dev_alloc(ctx, ctx->tileOrder, numTiles * sizeof(uint32_t), false))) return r;
             f.seqRec = static_cast<uint32_t*>(ctx->seqRec.ptr);
             f.itemKey = f.rankOf ? nullptr : static_cast<uint32_t*>(ctx->itemKey.ptr);
             f.binBlocks = static_cast<uint32_t*>(ctx->binBlocks.ptr);
             f.chunkCounts = static_cast<uint32_t*>(ctx->chunkCounts.ptr);
             f.binChunks = (uint32_t)chunks;
+            f.tileOrder = static_cast<uint32_t*>(ctx->tileOrder.ptr);
         }
     }
 
@@ -1499,7 +1502,7 @@ void slg_context_destroy(slg_context* ctx)
                             &ctx->tileCount, &ctx->tileOffset,
                             &ctx->tileCursor, &ctx->entries, &ctx->blitBuf,
                             &ctx->rankOf, &ctx->recOfRank, &ctx->seqRec, &ctx->seqKey, &ctx->binBlocks,
-                            &ctx->chunkCounts, &ctx->itemKey, &ctx->bestWords, &ctx->ovfKey, &ctx->sortScratch,
+                            &ctx->chunkCounts, &ctx->itemKey, &ctx->tileOrder, &ctx->bestWords, &ctx->ovfKey, &ctx->sortScratch,
                             &ctx->status, &ctx->devDescs, &ctx->devStarts};
     for (DevBuffer* b : scratch) dev_free(*b);
     if (ctx->graph.exec) cudaGraphExecDestroy(ctx->graph.exec);

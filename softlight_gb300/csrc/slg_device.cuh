@@ -237,6 +237,10 @@ struct Frame
     uint32_t* chunkCounts;
     uint32_t  binChunks;
     uint32_t* itemKey;            /* per bin in push order: its tile-list key (launches without recOfRank) */
+    /* the order in which the ordered raster's CTAs take the tiles (longest
+     * tile list first; written by tile_scan_kernel), for launches with
+     * lists in key order; null: CTA i takes tile i */
+    uint32_t* tileOrder;
 
     /* untiled order-free raster (raster_global_kernel): per pixel the best
      * word of raster_free_kernel in global memory, and per overflow record

@@ -28,10 +28,10 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const Frame f, int numT
      * warp sums scanned by warp 0 */
     const bool vec = ((reinterpret_cast<uintptr_t>(f.tileCount) | reinterpret_cast<uintptr_t>(f.tileOffset) |
                        reinterpret_cast<uintptr_t>(f.tileCursor)) & 15u) == 0;
+    uint32_t c[4] = {0u, 0u, 0u, 0u};
     for (int base = 0; base < numTiles; base += 4096)
     {
         const int t0 = base + 4 * tid;
-        uint32_t c[4];
         if (vec && t0 + 3 < numTiles)
         {
             const uint4 q = *reinterpret_cast<const uint4*>(f.tileCount + t0);
@@ -102,6 +102,48 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const Frame f, int numT
         }
         *f.ovfCount = 0;
         *f.clipCount = 0;
+    }
+    if (f.tileOrder != nullptr && numTiles <= 4096)
+    {
+        /* the ordered raster's tile order: longest list first, by a counting
+         * sort of the counts (c: this thread's four tiles, the loop's only
+         * step) into 256 buckets scaled to the longest list; the order
+         * within a bucket is the atomics' */
+        __shared__ uint32_t sHist[256];
+        __shared__ uint32_t sMax;
+        if (tid == 0) sMax = 0;
+        if (tid < 256) sHist[tid] = 0;
+        __syncthreads();
+        uint32_t m = max(max(c[0], c[1]), max(c[2], c[3]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+        if (lane == 0) atomicMax(&sMax, m);
+        __syncthreads();
+        const uint64_t maxN = sMax;
+        uint32_t b[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            b[k] = maxN ? (uint32_t)(((maxN - c[k]) * 255u) / maxN) : 0u;
+            if (4 * tid + k < numTiles) atomicAdd(&sHist[b[k]], 1u);
+        }
+        __syncthreads();
+        if (tid == 0)
+        {
+            uint32_t run = 0;
+            for (int i = 0; i < 256; ++i)
+            {
+                const uint32_t h = sHist[i];
+                sHist[i] = run;
+                run += h;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            if (4 * tid + k < numTiles) f.tileOrder[atomicAdd(&sHist[b[k]], 1u)] = (uint32_t)(4 * tid + k);
+        }
     }
 }
 

@@ -2067,7 +2067,9 @@ __global__ void __launch_bounds__(TH * 4, kGeneral ? 512 / (TH * 4) : 896 / (TH 
     float*    sBandD = reinterpret_cast<float*>(smem + L::kBandDOff);
     uint32_t* sScan  = reinterpret_cast<uint32_t*>(smem + L::kScanOff);
 
-    const int tile = blockIdx.x;
+    /* longest tile lists first (tile_scan_kernel), so that the short ones
+     * fill in behind them */
+    const int tile = f.tileOrder ? (int)f.tileOrder[blockIdx.x] : (int)blockIdx.x;
     const uint32_t begin = f.tileOffset[tile];
     const uint32_t n = f.tileOffset[tile + 1] - begin;
     if (n == 0 || (f.status[0] & kStatusSticky) || !ordered_raster_runs(f))
