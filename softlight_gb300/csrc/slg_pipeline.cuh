@@ -3340,7 +3340,7 @@ cudaError_t launch_vertex_stage(const Frame& f, cudaStream_t s)
         if (f.hasLines || f.hasWire) vs_setup_kernel<P, true, false><<<blocks, vsBlock, 0, s>>>(f);
         else if (f.allCached) vs_setup_kernel<P, false, true><<<blocks, vsBlock, 0, s>>>(f);
         else vs_setup_kernel<P, false, false><<<blocks, vsBlock, 0, s>>>(f);
-        clip_kernel<P><<<152 * 3, 128, 0, s>>>(f);   /* 128 registers: three CTAs per SM */
+        clip_kernel<P><<<152 * 4, 128, 0, s>>>(f);   /* 128 registers: four CTAs per SM */
     }
     return cudaGetLastError();
 }
